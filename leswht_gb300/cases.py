@@ -1,0 +1,177 @@
+"""Synthetic LES cases with the shapes of the benchmark configurations.
+
+A case = settings (settings.input + boundary.input + periodicity flags, as a
+dict matching lesgpu_config), a grid (gridgen.GridMetrics) and an initial
+field in the state prefld (misc_init.f90:610-786) leaves after reading a
+field file with IREAD = 1.  No dataset is involved: grids come from the
+gridline recipes below and the initial fields from a seeded PCG64 stream.
+
+Presets
+  channel(...)  : turbulent channel, periodic x/z, walls at y = +-1, tanh
+                  wall-normal stretching, constant flow rate (ICH = 1),
+                  passive temperature with the decomposition source
+                  (IDECOMP = 1), dynamic SGS.  64^3 is the Re_tau = 180
+                  configuration; 384x256x384 the Re_tau = 590 one.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Any, Dict, Optional
+
+import numpy as np
+
+from . import abi
+from .gridgen import GridMetrics, Segment, make_grid
+
+
+def base_settings() -> Dict[str, Any]:
+    """Defaults of 02_solver/settings.input and boundary.input."""
+    return dict(
+        re=180.0, pr=0.71, gr=0.0, grdir=2, tflu_i=0.0, tsol_i=0.0,
+        ireset=0, iread=1, iavg=0, ipzero=0, eps_ptr=0.0, udrv_i=1.0,
+        nend=999999, nprint=10000, npriavg=50000, npin=1,
+        tend=1.0e9, ptb_tst=-1.0, avg_tst=1.0e9,
+        idtopt=1, dt_size=0.005, cflfac=0.5,
+        resid1=1.0e-6, nlev=5, nbli=3, ioldv=0, mgitr=500, imgsor=170, wwsor=1.8,
+        iles=1, insmdl=1, itemdl=0, idvmon=1, csgsts=0.025, csgshf=0.003, filter=3,
+        ibmon=0, masson=0, imovingon=0, ihtrans=1, idecomp=0,
+        bc_ybtm=0, bc_ytop=0, bc_zbtm=0, bc_ztop=0,
+        bc_t_ybtm=0, bc_t_ytop=0, val_t_ybtm=0.0, val_t_ytop=0.0,
+        bc_t_zbtm=1, bc_t_ztop=1, val_t_zbtm=0.0, val_t_ztop=0.0,
+        ich=0, iconjg=0,
+        xprdic=0, yprdic=0, zprdic=0, iintp=0,
+        poisson=abi.POISSON_FTFT, precision=abi.PREC_FP64,
+        body=dict(kind=abi.BODY_NONE, cx=0.0, cy=0.0, cz=0.0, r=0.5, p0=0.0),
+    )
+
+
+@dataclass
+class Case:
+    name: str
+    settings: Dict[str, Any]
+    grid: GridMetrics
+    grid_dat: str
+    grid_bin: str
+    fields: Dict[str, np.ndarray]          # u, v, w, p, t in (n3+1, n2+1, n1+1) C order
+    time: float = 0.0
+    dt: float = 0.0
+    ihist: int = 0
+    m: int = 0
+    ibm: Optional[Dict[str, Any]] = None   # pack_ibm tables, or None
+
+    @property
+    def cells(self) -> int:
+        g = self.grid
+        return g.n1m * g.n2m * g.n3m
+
+
+def prefld_apply(s: Dict[str, Any], g: GridMetrics, u, v, w, p, t):
+    """Leave the arrays the way prefld (misc_init.f90:610-786) does after an
+    IREAD = 1 read: only the record ranges are kept, T's unread cells are
+    TSOL_I, then the periodic ghost copies."""
+    n1, n2, n3, n1m, n2m, n3m = g.n1, g.n2, g.n3, g.n1m, g.n2m, g.n3m
+    U = np.zeros(g.shape); U[0:n3 + 1, 0:n2 + 1, 1:n1 + 1] = u[0:n3 + 1, 0:n2 + 1, 1:n1 + 1]
+    V = np.zeros(g.shape); V[0:n3 + 1, 1:n2 + 1, 0:n1 + 1] = v[0:n3 + 1, 1:n2 + 1, 0:n1 + 1]
+    W = np.zeros(g.shape); W[1:n3 + 1, 0:n2 + 1, 0:n1 + 1] = w[1:n3 + 1, 0:n2 + 1, 0:n1 + 1]
+    P = np.zeros(g.shape); P[1:n3m + 1, 1:n2m + 1, 1:n1m + 1] = p[1:n3m + 1, 1:n2m + 1, 1:n1m + 1]
+    T = np.full(g.shape, float(s["tsol_i"]))
+    T[1:n3m + 1, 1:n2m + 1, 1:n1m + 1] = t[1:n3m + 1, 1:n2m + 1, 1:n1m + 1]
+    if s.get("ipzero", 0) == 1:
+        P[:] = 0.0
+    if s["xprdic"] == 1:
+        U[:, :, 0] = U[:, :, n1m]; U[:, :, n1] = U[:, :, 1]
+        V[:, 1:, 0] = V[:, 1:, n1m]; V[:, 1:, n1] = V[:, 1:, 1]
+        W[1:, :, 0] = W[1:, :, n1m]; W[1:, :, n1] = W[1:, :, 1]
+        T[:, :, 0] = T[:, :, n1m]; T[:, :, n1] = T[:, :, 1]
+    if s["yprdic"] == 1:
+        U[:, 0, 1:] = U[:, n2m, 1:]; U[:, n2, 1:] = U[:, 1, 1:]
+        V[:, 0, :] = V[:, n2m, :]; V[:, n2, :] = V[:, 1, :]
+        W[1:, 0, :] = W[1:, n2m, :]; W[1:, n2, :] = W[1:, 1, :]
+        T[:, 0, :] = T[:, n2m, :]; T[:, n2, :] = T[:, 1, :]
+    if s["zprdic"] == 1:
+        U[0, :, 1:] = U[n3m, :, 1:]; U[n3, :, 1:] = U[1, :, 1:]
+        V[0, 1:, :] = V[n3m, 1:, :]; V[n3, 1:, :] = V[1, 1:, :]
+        W[0, :, :] = W[n3m, :, :]; W[n3, :, :] = W[1, :, :]
+        T[0, :, :] = T[n3m, :, :]; T[n3, :, :] = T[1, :, :]
+    return U, V, W, P, T
+
+
+def _plane_mean_correct(f, mask, weight, axis):
+    """Subtract the weighted mean of the perturbation over each plane normal
+    to `axis` (the correction of addperturb_isotropic, misc_init.f90:900-926)."""
+    num = (f * mask * weight).sum(axis=tuple(a for a in range(3) if a != axis), keepdims=True)
+    den = (mask * weight).sum(axis=tuple(a for a in range(3) if a != axis), keepdims=True)
+    adj = np.where(den > 0, num / np.where(den > 0, den, 1.0), 0.0)
+    return f - adj * mask
+
+
+def channel(n1m: int = 64, n2m: int = 64, n3m: int = 64,
+            lx: float = 4.0 * math.pi, ly: float = 2.0, lz: float = 4.0 * math.pi / 3.0,
+            gamma: float = 2.75, re: float = 2800.0, pr: float = 0.71,
+            amp: float = 0.1, seed: int = 20261203, precision: int = abi.PREC_FP64,
+            name: Optional[str] = None) -> Case:
+    """Channel with passive heat transfer (temperature decomposition source).
+
+    Re is the bulk Reynolds number on the half height (Re_b = 2800 gives
+    Re_tau ~ 180 for the 4pi x 2 x 4pi/3 box); the initial field is the
+    laminar profile 1.5(1 - y^2) plus a seeded uniform perturbation of
+    relative amplitude `amp`, mean-corrected plane by plane."""
+    s = base_settings()
+    s.update(re=re, pr=pr, ich=1, iconjg=1, idecomp=1, ihtrans=1, iles=1, idvmon=1,
+             xprdic=1, zprdic=1, yprdic=0, udrv_i=1.0, cflfac=0.5, idtopt=1, dt_size=0.002,
+             bc_ybtm=0, bc_ytop=0, bc_t_ybtm=0, bc_t_ytop=0, poisson=abi.POISSON_FTFT,
+             precision=precision,
+             body=dict(kind=abi.BODY_CHANNEL, cx=0.0, cy=0.0, cz=0.0, r=0.0, p0=1.0e-6))
+    n1, n2, n3 = n1m + 1, n2m + 1, n3m + 1
+    g, gdat, gbin = make_grid(
+        n1, n2, n3, lx, ly, lz,
+        [Segment("X", 0.0, lx, 1, n1, "U")],
+        [Segment("Y", -1.0, 1.0, 1, n2, "H", 0.5, gamma)],
+        [Segment("Z", 0.0, lz, 1, n3, "U")],
+        xprdic=True, zprdic=True)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sh = g.shape
+    u = np.zeros(sh); v = np.zeros(sh); w = np.zeros(sh); p = np.zeros(sh); t = np.zeros(sh)
+    ymp = g.ymp[None, :, None]
+    u[:] = 1.5 * s["udrv_i"] * (1.0 - ymp ** 2)
+    # walls: no-slip ghosts (the ghost centre ymp(0), ymp(n2) lies on the wall)
+    u[:, 0, :] = 0.0; u[:, n2, :] = 0.0
+    # perturbations on the interior unknowns
+    def pert():
+        return (rng.random(sh) - 0.5) * 2.0 * amp * s["udrv_i"]
+    fl = np.zeros(sh); fl[1:n3m + 1, 1:n2m + 1, 1:n1m + 1] = 1.0
+    dy = g.f2fy[None, :, None]; dz = g.f2fz[:, None, None]; dx = g.f2fx[None, None, :]
+    fv = np.zeros(sh); fv[1:n3m + 1, 2:n2m + 1, 1:n1m + 1] = 1.0   # v unknowns: j = 2..n2m
+    u += _plane_mean_correct(pert(), fl, dy * dz, axis=2)
+    v += _plane_mean_correct(pert(), fv, dz * dx, axis=1)
+    w += _plane_mean_correct(pert(), fl, dx * dy, axis=0)
+    u *= fl; v *= fv; w *= fl
+    u[:, 0, :] = 0.0; u[:, n2, :] = 0.0
+    # temperature of the decomposition form: t = u / Pr in the fluid (makefld :529-541)
+    t[:] = 0.0
+    t[1:n3m + 1, 1:n2m + 1, 1:n1m + 1] = (0.5 * (u[1:n3m + 1, 1:n2m + 1, 1:n1m + 1]
+                                              + u[1:n3m + 1, 1:n2m + 1, 2:n1m + 2])) / pr
+    U, V, W, P, T = prefld_apply(s, g, u, v, w, p, t)
+    nm = name or f"channel_{n1m}x{n2m}x{n3m}"
+    return Case(nm, s, g, gdat, gbin, dict(u=U, v=V, w=W, p=P, t=T), time=0.0, dt=s["dt_size"],
+                ihist=0, m=0, ibm=channel_ibm_tables(g))
+
+
+def channel_ibm_tables(g: GridMetrics) -> Dict[str, Any]:
+    """The placeholder pre-processing outputs of write_ibmpre_placeholders
+    (lib_preprocessing.py:172-221): no forcing points, no zero-viscosity
+    points, nwall = 1, c* = k* = 1."""
+    z3 = np.zeros((0, 3), np.int64)
+    return dict(nintp=[0, 0, 0, 0], nbody=[0, 0, 0, 0], fc=[z3] * 4, intpindx=[z3] * 4,
+                geomfac=[np.zeros((0, 27))] * 4, nzero=0,
+                inz=np.zeros(0, np.int64), jnz=np.zeros(0, np.int64), knz=np.zeros(0, np.int64),
+                nwall_dvm=np.ones(g.n1m * g.n2m * g.n3m, np.int64),
+                cstar=np.ones(g.n1m * g.n2m * g.n3m), kstar=np.ones(6 * g.n1m * g.n2m * g.n3m),
+                omega=np.ones(g.n1m * g.n2m * g.n3m, np.int64))
+
+
+PRESETS = {
+    "channel64": lambda **kw: channel(64, 64, 64, **kw),
+    "channel590": lambda **kw: channel(384, 256, 384, lx=2 * math.pi, lz=math.pi, re=10950.0, **kw),
+}

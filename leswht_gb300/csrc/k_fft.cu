@@ -1,0 +1,351 @@
+// Pressure Poisson solve of poiss_ftft.f90 (FFT in x and z, Thomas in y)
+// with this library's own batched FFT.
+//
+// FFT: a Stockham auto-sort transform (Govindaraju et al., "High
+// performance discrete Fourier transforms on graphics processors", SC'08)
+// with radix-4/2/3/5 stages, executed by one thread block on a batch of L
+// lines held in shared memory.  Lines are interleaved (element e of line l at
+// e*L + l) so consecutive threads touch consecutive words.  Conventions are
+// those of FFTE's ZFFT1D (zfft1d.f:18-84): forward = sum a_n exp(-2 pi i nk/N)
+// unnormalised; inverse = exp(+...) scaled by 1/N.  Twiddles come from a
+// table computed once on the host in long double.
+//
+// Data flow of one solve (spectrum ccap laid out i fastest, then k, then j):
+//   k_fft_z_fwd : divgsum(i,j,:) real -> z-spectrum, keep modes 1..n3mh
+//   k_fft_x     : complex x transform of every (k,j) line, in place
+//   k_ytri      : complex Thomas along y for every (k,i) wavenumber pair,
+//                 with the (1,1) mode pinned as poiss_ftft.f90:93-112
+//   k_fft_x     : inverse x transform
+//   k_fft_z_inv : conjugate-symmetric completion, inverse z, real part -> phi
+#include "lesgpu_internal.cuh"
+#include <math.h>
+#include <stdlib.h>
+
+namespace lg {
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+
+struct DevPlan {
+    int n, nst;
+    int rad[24];
+    const double2 *tw;
+};
+
+// Run all stages on L interleaved lines; returns the buffer holding the result.
+__device__ double2 *block_fft(double2 *b0, double2 *b1, int L, const DevPlan &P, int inv) {
+    const int N = P.n;
+    int Ns = 1;
+    double2 *in = b0, *out = b1;
+    for (int st = 0; st < P.nst; st++) {
+        const int R = P.rad[st];
+        const int NR = N / R;
+        const int twstep = N / (Ns * R);
+        const int work = NR * L;
+        for (int w = threadIdx.x; w < work; w += blockDim.x) {
+            const int l = w % L, jb = w / L;
+            double2 v[8];
+            const int jm = jb % Ns;
+#pragma unroll 4
+            for (int r = 0; r < R; r++) {
+                double2 x = in[(jb + r * NR) * L + l];
+                if (r > 0 && jm > 0) {
+                    double2 t = P.tw[(jm * r * twstep) % N];
+                    if (inv) t.y = -t.y;
+                    x = cmul(x, t);
+                }
+                v[r] = x;
+            }
+            double2 y[8];
+            if (R == 2) {
+                y[0] = cadd(v[0], v[1]);
+                y[1] = csub(v[0], v[1]);
+            } else if (R == 4) {
+                double2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+                double2 s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
+                // forward: W4 = -i; inverse: +i
+                double2 jd13 = inv ? make_double2(-d13.y, d13.x) : make_double2(d13.y, -d13.x);
+                y[0] = cadd(s02, s13);
+                y[2] = csub(s02, s13);
+                y[1] = cadd(d02, jd13);
+                y[3] = csub(d02, jd13);
+            } else {
+                for (int m = 0; m < R; m++) {
+                    double2 acc = v[0];
+                    for (int r = 1; r < R; r++) {
+                        double2 t = P.tw[((m * r) % R) * NR];
+                        if (inv) t.y = -t.y;
+                        acc = cadd(acc, cmul(v[r], t));
+                    }
+                    y[m] = acc;
+                }
+            }
+            const int idxD = (jb / Ns) * Ns * R + jm;
+            for (int r = 0; r < R; r++) out[(idxD + r * Ns) * L + l] = y[r];
+        }
+        __syncthreads();
+        double2 *tmp = in; in = out; out = tmp;
+        Ns *= R;
+    }
+    return in;
+}
+
+static DevPlan devplan(const FftPlan &p) {
+    DevPlan d;
+    d.n = p.n;
+    d.nst = p.nst;
+    for (int s = 0; s < 24; s++) d.rad[s] = p.rad[s];
+    d.tw = p.tw;
+    return d;
+}
+
+// ---- z transforms: block = (i-tile of L lines) x j ----------------------
+__global__ void k_fft_z_fwd(KP p, double2 *ccap, DevPlan P, int L) {
+    extern __shared__ double2 sm[];
+    const DGrid &g = p.g;
+    const int N = P.n;
+    double2 *b0 = sm, *b1 = sm + (size_t)N * L;
+    int i0 = 1 + blockIdx.x * L, j = 1 + blockIdx.y;
+    for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
+        int l = w % L, e = w / L;
+        int i = i0 + l;
+        double val = (i <= g.n1m) ? p.f.divgsum[g.ix(i, j, e + 1)] : 0.0;
+        b0[e * L + l] = make_double2(val, 0.0);
+    }
+    __syncthreads();
+    double2 *res = block_fft(b0, b1, L, P, 0);
+    const int n3mh = g.n3mh;
+    for (int w = threadIdx.x; w < n3mh * L; w += blockDim.x) {
+        int l = w % L, kk = w / L;
+        int i = i0 + l;
+        if (i <= g.n1m) ccap[(i - 1) + (size_t)g.n1m * (kk + (size_t)n3mh * (j - 1))] = res[kk * L + l];
+    }
+}
+
+__global__ void k_fft_z_inv(KP p, const double2 *ccap, DevPlan P, int L) {
+    extern __shared__ double2 sm[];
+    const DGrid &g = p.g;
+    const int N = P.n;
+    double2 *b0 = sm, *b1 = sm + (size_t)N * L;
+    int i0 = 1 + blockIdx.x * L, j = 1 + blockIdx.y;
+    const int n3mh = g.n3mh;
+    for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
+        int l = w % L, e = w / L;
+        int i = i0 + l;
+        double2 val = make_double2(0.0, 0.0);
+        if (i <= g.n1m) {
+            if (e < n3mh) {
+                val = ccap[(i - 1) + (size_t)g.n1m * (e + (size_t)n3mh * (j - 1))];
+            } else {
+                // zzz(k) = conjg(zzz(n3m+2-k)), poiss_ftft.f90:143-147
+                int src = N - e;
+                double2 s = ccap[(i - 1) + (size_t)g.n1m * (src + (size_t)n3mh * (j - 1))];
+                val = make_double2(s.x, -s.y);
+            }
+        }
+        b0[e * L + l] = val;
+    }
+    __syncthreads();
+    double2 *res = block_fft(b0, b1, L, P, 1);
+    const double dn = 1.0 / (double)N;
+    for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
+        int l = w % L, e = w / L;
+        int i = i0 + l;
+        if (i <= g.n1m) p.f.phi[g.ix(i, j, e + 1)] = res[e * L + l].x * dn;
+    }
+}
+
+// ---- x transforms of the (k,j) lines of ccap, in place -------------------
+__global__ void k_fft_x(double2 *ccap, int nlines, DevPlan P, int L, int inv) {
+    extern __shared__ double2 sm[];
+    const int N = P.n;
+    double2 *b0 = sm, *b1 = sm + (size_t)N * L;
+    int line0 = blockIdx.x * L;
+    for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
+        int e = w % N, l = w / N;           // coalesced global read along the line
+        int line = line0 + l;
+        b0[e * L + l] = (line < nlines) ? ccap[(size_t)line * N + e] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    double2 *res = block_fft(b0, b1, L, P, inv);
+    const double dn = 1.0 / (double)N;
+    for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
+        int e = w % N, l = w / N;
+        int line = line0 + l;
+        if (line < nlines) {
+            double2 v = res[e * L + l];
+            if (inv) { v.x *= dn; v.y *= dn; }
+            ccap[(size_t)line * N + e] = v;
+        }
+    }
+}
+
+// ---- complex Thomas along y, ctrdiag (poiss_ftft.f90:207-244) ------------
+__device__ __forceinline__ void ycoef(const DGrid &g, const double *ak1, const double *ak3, int i, int k, int j,
+                                      double &am, double &ac, double &ap) {
+    double fl = fixd(g.fixjl[j]), fu = fixd(g.fixju[j]);
+    am = g.f2fyi[j] * g.c2cyi[j] * (1.0 - fl);
+    ap = g.f2fyi[j] * g.c2cyi[g.jpv[j]] * (1.0 - fu);
+    double akk = ak1[i] + ak3[k];
+    ac = -((am + ap + akk) * (1.0 - fl) * (1.0 - fu) + (g.f2fyi[1] * g.c2cyi[2] + akk) * fl
+           + (g.f2fyi[g.n2m] * g.c2cyi[g.n2m] + akk) * fu);
+}
+
+__global__ void k_ytri(KP p, double2 *ccap, const double *ak1, const double *ak3, double *gam) {
+    const DGrid &g = p.g;
+    const int n1m = g.n1m, n2m = g.n2m, n3mh = g.n3mh;
+    long long nl = (long long)n1m * n3mh;
+    const long long sj = (long long)n1m * n3mh;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nl; t += (long long)gridDim.x * blockDim.x) {
+        int i = 1 + (int)(t % n1m), k = 1 + (int)(t / n1m);
+        double2 *r = ccap + (i - 1) + (size_t)n1m * (k - 1);
+        double *gm = gam + (i - 1) + (size_t)n1m * (k - 1);
+        bool pin = (i == 1 && k == 1);
+        double am, ac, ap;
+        double ajcref = 0.0, ajmref = 0.0;
+        double2 crhsref = make_double2(0.0, 0.0);
+        if (pin) crhsref = r[(n2m - 1) * sj];
+        // forward
+        ycoef(g, ak1, ak3, i, k, 1, am, ac, ap);
+        if (pin && n2m == 1) { ajcref = ac; ajmref = am; ac = 1.0; am = 0.0; ap = 0.0; }
+        double bet = 1.0 / ac;
+        double2 x = r[0];
+        if (pin && n2m == 1) x = make_double2(0.0, 0.0);
+        x.x *= bet; x.y *= bet;
+        r[0] = x;
+        double cprev = ap;
+        for (int j = 2; j <= n2m; j++) {
+            ycoef(g, ak1, ak3, i, k, j, am, ac, ap);
+            double2 rj = r[(j - 1) * sj];
+            if (pin && j == n2m) {
+                ajcref = ac; ajmref = am;
+                ac = 1.0; am = 0.0; ap = 0.0;
+                rj = make_double2(0.0, 0.0);
+            }
+            double gj = cprev * bet;
+            bet = 1.0 / (ac - am * gj);
+            x = make_double2((rj.x - am * x.x) * bet, (rj.y - am * x.y) * bet);
+            gm[(j - 1) * sj] = gj;
+            r[(j - 1) * sj] = x;
+            cprev = ap;
+        }
+        // backward
+        double2 xn = x;
+        for (int j = n2m - 1; j >= 1; j--) {
+            double2 xj = r[(j - 1) * sj];
+            double gn = gm[j * sj];
+            xj = make_double2(xj.x - gn * xn.x, xj.y - gn * xn.y);
+            r[(j - 1) * sj] = xj;
+            xn = xj;
+        }
+        if (pin) {
+            // phref = (-ajmref*crhs(n2m-1,1) + crhsref)/ajcref; shift; crhs(n2m,1) = 0
+            double2 cm = n2m >= 2 ? r[(n2m - 2) * sj] : make_double2(0.0, 0.0);
+            double2 ph = make_double2((-ajmref * cm.x + crhsref.x) / ajcref, (-ajmref * cm.y + crhsref.y) / ajcref);
+            for (int j = 1; j <= n2m; j++) {
+                double2 v = r[(j - 1) * sj];
+                r[(j - 1) * sj] = make_double2(v.x - ph.x, v.y - ph.y);
+            }
+            r[(n2m - 1) * sj] = make_double2(0.0, 0.0);
+        }
+    }
+}
+
+// ------------------------------------------------------------ host side
+static int make_plan(FftPlan &p, int n) {
+    p.n = n;
+    p.nst = 0;
+    int m = n;
+    while (m > 1) {
+        int r;
+        if (m % 4 == 0) r = 4;
+        else if (m % 2 == 0) r = 2;
+        else if (m % 3 == 0) r = 3;
+        else if (m % 5 == 0) r = 5;
+        else return LESGPU_ERR_UNSUPPORTED;      // FFTE supports 2^p 3^q 5^r only
+        if (p.nst >= 24) return LESGPU_ERR_UNSUPPORTED;
+        p.rad[p.nst++] = r;
+        m /= r;
+    }
+    double2 *h = (double2 *)malloc(sizeof(double2) * (size_t)n);
+    for (int e = 0; e < n; e++) {
+        long double ang = -2.0L * 3.14159265358979323846264338327950288L * (long double)e / (long double)n;
+        h[e] = make_double2((double)cosl(ang), (double)sinl(ang));
+    }
+    if (cudaMalloc(&p.tw, sizeof(double2) * (size_t)n) != cudaSuccess) { free(h); return LESGPU_ERR_OOM; }
+    cudaMemcpy(p.tw, h, sizeof(double2) * (size_t)n, cudaMemcpyHostToDevice);
+    free(h);
+    return 0;
+}
+
+static int lines_per_block(int n) {
+    int L = 32;
+    while (L > 1 && (size_t)2 * n * L * sizeof(double2) > 200 * 1024) L >>= 1;
+    return L;
+}
+
+// poisinit, poiss_ftft.f90:164-204
+int poisson_init(lesgpu_case *c) {
+    const DGrid &g = c->kp.g;
+    DPois &P = c->pois;
+    if (c->cfg.poisson != LESGPU_POISSON_FTFT) return LESGPU_ERR_UNSUPPORTED;
+    if (c->cfg.xprdic != 1 || c->cfg.zprdic != 1) return LESGPU_ERR_CONFIG;
+    int rc = make_plan(P.fx, g.n1m);
+    if (rc) return rc;
+    rc = make_plan(P.fz, g.n3m);
+    if (rc) return rc;
+    double pi = 2.0 * asin(1.0);
+    double *ak1 = (double *)calloc(g.n1 + 2, sizeof(double));
+    double *ak3 = (double *)calloc(g.n3mh + 2, sizeof(double));
+    double sdzis = c->h_f2fz[1], sdxis = c->h_f2fx[1];
+    for (int k = 1; k <= g.n3mh; k++) {
+        double ai = (k == 1) ? 0.0 : (double)(k - 1) * 2.0 * pi;
+        ak3[k] = 2.0 * (1.0 - cos(ai / (double)g.n3m)) * sdzis * sdzis;
+    }
+    for (int i = 1; i <= g.n1mh; i++) {
+        double ai = (i == 1) ? 0.0 : (double)(i - 1) * 2.0 * pi;
+        ak1[i] = 2.0 * (1.0 - cos(ai / (double)g.n1m)) * sdxis * sdxis;
+    }
+    for (int i = g.n1m; i >= g.n1mh + 1; i--) ak1[i] = ak1[g.n1m + 2 - i];
+    if (cudaMalloc(&P.ak1, sizeof(double) * (g.n1 + 2)) != cudaSuccess) return LESGPU_ERR_OOM;
+    if (cudaMalloc(&P.ak3, sizeof(double) * (g.n3mh + 2)) != cudaSuccess) return LESGPU_ERR_OOM;
+    cudaMemcpy(P.ak1, ak1, sizeof(double) * (g.n1 + 2), cudaMemcpyHostToDevice);
+    cudaMemcpy(P.ak3, ak3, sizeof(double) * (g.n3mh + 2), cudaMemcpyHostToDevice);
+    free(ak1); free(ak3);
+    size_t nspec = (size_t)g.n1m * g.n3mh * g.n2m;
+    if (cudaMalloc(&P.ccap, sizeof(double2) * nspec) != cudaSuccess) return LESGPU_ERR_OOM;
+    int Lz = lines_per_block(g.n3m), Lx = lines_per_block(g.n1m);
+    size_t smz = (size_t)2 * g.n3m * Lz * sizeof(double2), smx = (size_t)2 * g.n1m * Lx * sizeof(double2);
+    cudaFuncSetAttribute(k_fft_z_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
+    cudaFuncSetAttribute(k_fft_z_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
+    cudaFuncSetAttribute(k_fft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+    return 0;
+}
+
+void poisson_free(lesgpu_case *c) {
+    DPois &P = c->pois;
+    cudaFree(P.ak1); cudaFree(P.ak3); cudaFree(P.ccap);
+    cudaFree(P.fx.tw); cudaFree(P.fz.tw);
+    P.ak1 = P.ak3 = nullptr; P.ccap = nullptr; P.fx.tw = P.fz.tw = nullptr;
+}
+
+void launch_poisson(lesgpu_case *c) {
+    const DGrid &g = c->kp.g;
+    DPois &P = c->pois;
+    DevPlan px = devplan(P.fx), pz = devplan(P.fz);
+    int Lz = lines_per_block(g.n3m), Lx = lines_per_block(g.n1m);
+    size_t smz = (size_t)2 * g.n3m * Lz * sizeof(double2), smx = (size_t)2 * g.n1m * Lx * sizeof(double2);
+    dim3 gz((g.n1m + Lz - 1) / Lz, g.n2m);
+    int nxl = g.n3mh * g.n2m;
+    k_fft_z_fwd<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz);
+    k_fft_x<<<(nxl + Lx - 1) / Lx, kThreads, smx, c->stream>>>(P.ccap, nxl, px, Lx, 0);
+    long long nl = (long long)g.n1m * g.n3mh;
+    k_ytri<<<blocks_for(nl, 128), 128, 0, c->stream>>>(c->kp, P.ccap, P.ak1, P.ak3, c->kp.f.scr[0]);
+    k_fft_x<<<(nxl + Lx - 1) / Lx, kThreads, smx, c->stream>>>(P.ccap, nxl, px, Lx, 1);
+    k_fft_z_inv<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz);
+}
+
+}  // namespace lg

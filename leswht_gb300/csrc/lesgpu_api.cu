@@ -1,0 +1,630 @@
+// C ABI of the GB300 LES time-step library (include/lesgpu.h).
+//
+// lesgpu_create allocates the whole solver state in device memory and builds
+// the init-time tables of the reference (lhsinit slv_mmtm.f90:180,
+// sgsfilterinit sgs.f90:2, poisinit of the Poisson solver, and the body
+// function values that the reference re-evaluates inside its reductions).
+// lesgpu_step enqueues one time step (solver.f90:85-151 plus the per-step
+// checks) on the case's stream; from the second eligible step on, the step
+// is replayed from a captured CUDA graph, so one step costs one graph launch
+// and one 400-byte read-back of the step scalars.
+#include "lesgpu_internal.cuh"
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#include <vector>
+
+using namespace lg;
+
+namespace lg {
+void launch_sgs_post(lesgpu_case *c);
+void launch_sgs_t_post(lesgpu_case *c);
+}
+
+// ------------------------------------------------------------------ helpers
+namespace {
+
+struct Alloc {
+    std::vector<void *> ptrs;
+    bool ok = true;
+    template <class T> T *get(size_t n) {
+        void *p = nullptr;
+        if (n == 0) n = 1;
+        if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) { ok = false; return nullptr; }
+        cudaMemset(p, 0, n * sizeof(T));
+        ptrs.push_back(p);
+        return (T *)p;
+    }
+};
+
+struct CaseExtra {
+    Alloc alloc;
+};
+
+double funcbody(const lesgpu_body &b, double x, double y, double z) {
+    switch (b.kind) {
+    case LESGPU_BODY_CHANNEL: return (1.0 + b.p0) - fabs(y);
+    case LESGPU_BODY_CYLINDER: { double dx = x - b.cx, dy = y - b.cy; return sqrt(dx * dx + dy * dy) - b.r; }
+    case LESGPU_BODY_SPHERE: { double dx = x - b.cx, dy = y - b.cy, dz = z - b.cz; return sqrt(dx * dx + dy * dy + dz * dz) - b.r; }
+    case LESGPU_BODY_SQUARE: { double ax = fabs(x - b.cx), ay = fabs(y - b.cy); return (ax > ay ? ax : ay) - b.r; }
+    default: return 1.0;
+    }
+}
+
+template <class T> T *upload(Alloc &A, const T *h, size_t n) {
+    T *d = A.get<T>(n);
+    if (d && h) cudaMemcpy(d, h, n * sizeof(T), cudaMemcpyHostToDevice);
+    return d;
+}
+
+// (0:n) vector -> device array of n+2
+double *vec0(Alloc &A, const double *src, long long n) {
+    std::vector<double> h(n + 2, 0.0);
+    for (long long i = 0; i <= n; i++) h[i] = src[i];
+    return upload(A, h.data(), h.size());
+}
+// (1:n) vector -> device array of n+2 with Fortran index
+double *vec1(Alloc &A, const double *src, long long n) {
+    std::vector<double> h(n + 2, 0.0);
+    for (long long i = 1; i <= n; i++) h[i] = src[i - 1];
+    return upload(A, h.data(), h.size());
+}
+int *ivec1(Alloc &A, const int64_t *src, long long n) {
+    std::vector<int> h(n + 2, 0);
+    for (long long i = 1; i <= n; i++) h[i] = (int)src[i - 1];
+    return upload(A, h.data(), h.size());
+}
+
+int check_config(const lesgpu_config *c, const lesgpu_grid *g) {
+    if (g->n1 != g->n1m + 1 || g->n2 != g->n2m + 1 || g->n3 != g->n3m + 1) return LESGPU_ERR_ARG;
+    if (g->n1m < 2 || g->n2m < 2 || g->n3m < 1) return LESGPU_ERR_ARG;
+    if ((long long)(g->n1 + 1) * (g->n2 + 1) * (g->n3 + 1) > (1LL << 40)) return LESGPU_ERR_ARG;
+    if (c->precision != LESGPU_PREC_FP64) return LESGPU_ERR_UNSUPPORTED;
+    if (c->poisson != LESGPU_POISSON_FTFT) return LESGPU_ERR_UNSUPPORTED;
+    if (c->ibmon != 0 || c->imovingon != 0) return LESGPU_ERR_UNSUPPORTED;
+    if (c->xprdic != 1) return LESGPU_ERR_UNSUPPORTED;        // convective outlet: not built yet
+    if (c->iles == 1 && c->insmdl != 1) return LESGPU_ERR_CONFIG;   // sgs.f90:314 stops
+    if (c->ihtrans == 1 && c->iles == 1 && c->itemdl != 0) return LESGPU_ERR_CONFIG;
+    if (c->filter < 1 || c->filter > 3) return LESGPU_ERR_CONFIG;
+    if (c->ich != 0 && c->bc_ybtm != 0 && c->bc_ytop != 0 && c->bc_zbtm != 0 && c->bc_ztop != 0)
+        return LESGPU_ERR_CONFIG;                                    // meanpg stops
+    if (c->idecomp == 1) {                                            // check_idecomp_input
+        if (c->xprdic != 1 || c->bc_ybtm != 0 || c->bc_ytop != 0 || c->bc_t_ybtm != 0 || c->bc_t_ytop != 0)
+            return LESGPU_ERR_CONFIG;
+        if (fabs(c->val_t_ybtm) > 1e-12 || fabs(c->val_t_ytop) > 1e-12) return LESGPU_ERR_CONFIG;
+    }
+    return 0;
+}
+
+int cuda_rc(cudaError_t e) { return e == cudaSuccess ? 0 : LESGPU_ERR_CUDA; }
+
+}  // namespace
+
+// ------------------------------------------------------------------ create
+extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, lesgpu_case **out) {
+    if (!cfg || !g || !out) return LESGPU_ERR_ARG;
+    *out = nullptr;
+    int rc = check_config(cfg, g);
+    if (rc) return rc;
+    lesgpu_case *c = (lesgpu_case *)calloc(1, sizeof(lesgpu_case));
+    if (!c) return LESGPU_ERR_OOM;
+    CaseExtra *X = new CaseExtra();
+    c->dmem_pool = X;
+    c->cfg = *cfg;
+    c->use_graph = 1;
+    Alloc &A = X->alloc;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { lesgpu_destroy(c); return LESGPU_ERR_CUDA; }
+
+    DGrid &d = c->kp.g;
+    d.n1 = (int)g->n1; d.n2 = (int)g->n2; d.n3 = (int)g->n3;
+    d.n1m = (int)g->n1m; d.n2m = (int)g->n2m; d.n3m = (int)g->n3m;
+    d.n1mh = d.n1m / 2 + 1; d.n3mh = d.n3m / 2 + 1;
+    d.sx = d.n1 + 1; d.sxy = d.sx * (d.n2 + 1); d.nt = d.sxy * (d.n3 + 1);
+    d.xl = g->xl; d.yl = g->yl; d.zl = g->zl;
+    d.x = vec1(A, g->x, d.n1); d.y = vec1(A, g->y, d.n2); d.z = vec1(A, g->z, d.n3);
+    d.xmp = vec0(A, g->xmp, d.n1); d.ymp = vec0(A, g->ymp, d.n2); d.zmp = vec0(A, g->zmp, d.n3);
+    d.f2fx = vec0(A, g->f2fx, d.n1); d.f2fy = vec0(A, g->f2fy, d.n2); d.f2fz = vec0(A, g->f2fz, d.n3);
+    d.f2fxi = vec0(A, g->f2fxi, d.n1); d.f2fyi = vec0(A, g->f2fyi, d.n2); d.f2fzi = vec0(A, g->f2fzi, d.n3);
+    d.c2cx = vec0(A, g->c2cx, d.n1); d.c2cy = vec0(A, g->c2cy, d.n2); d.c2cz = vec0(A, g->c2cz, d.n3);
+    d.c2cxi = vec0(A, g->c2cxi, d.n1); d.c2cyi = vec0(A, g->c2cyi, d.n2); d.c2czi = vec0(A, g->c2czi, d.n3);
+    d.ipv = ivec1(A, g->ipv, d.n1m); d.jpv = ivec1(A, g->jpv, d.n2m); d.kpv = ivec1(A, g->kpv, d.n3m);
+    d.imv = ivec1(A, g->imv, d.n1m); d.jmv = ivec1(A, g->jmv, d.n2m); d.kmv = ivec1(A, g->kmv, d.n3m);
+    d.fixil = ivec1(A, g->fixil, d.n1m); d.fixjl = ivec1(A, g->fixjl, d.n2m); d.fixkl = ivec1(A, g->fixkl, d.n3m);
+    d.fixiu = ivec1(A, g->fixiu, d.n1m); d.fixju = ivec1(A, g->fixju, d.n2m); d.fixku = ivec1(A, g->fixku, d.n3m);
+    d.i_bgpx = cfg->xprdic == 1 ? 1 : 2;
+    d.j_bgpy = cfg->yprdic == 1 ? 1 : 2;
+    d.k_bgpz = cfg->zprdic == 1 ? 1 : 2;
+
+    DCfg &k = c->kp.c;
+    k.re = cfg->re; k.pr = cfg->pr; k.gr = cfg->gr; k.udrv_i = cfg->udrv_i; k.tflu_i = cfg->tflu_i; k.tsol_i = cfg->tsol_i;
+    k.val_t_ybtm = cfg->val_t_ybtm; k.val_t_ytop = cfg->val_t_ytop; k.val_t_zbtm = cfg->val_t_zbtm; k.val_t_ztop = cfg->val_t_ztop;
+    k.resid1 = cfg->resid1; k.csgsts = cfg->csgsts; k.csgshf = cfg->csgshf; k.cflfac = cfg->cflfac; k.dt_size = cfg->dt_size;
+    k.ptb_tst = cfg->ptb_tst; k.avg_tst = cfg->avg_tst; k.tend = cfg->tend;
+    k.grdir = (int)cfg->grdir; k.iles = (int)cfg->iles; k.ihtrans = (int)cfg->ihtrans; k.ich = (int)cfg->ich;
+    k.iconjg = (int)cfg->iconjg; k.idecomp = (int)cfg->idecomp; k.idvmon = (int)cfg->idvmon; k.filter = (int)cfg->filter;
+    k.ibmon = (int)cfg->ibmon; k.masson = (int)cfg->masson; k.imovingon = (int)cfg->imovingon; k.iread = (int)cfg->iread;
+    k.xprdic = (int)cfg->xprdic; k.yprdic = (int)cfg->yprdic; k.zprdic = (int)cfg->zprdic;
+    k.bc_ybtm = (int)cfg->bc_ybtm; k.bc_ytop = (int)cfg->bc_ytop; k.bc_zbtm = (int)cfg->bc_zbtm; k.bc_ztop = (int)cfg->bc_ztop;
+    k.bc_t_ybtm = (int)cfg->bc_t_ybtm; k.bc_t_ytop = (int)cfg->bc_t_ytop; k.bc_t_zbtm = (int)cfg->bc_t_zbtm; k.bc_t_ztop = (int)cfg->bc_t_ztop;
+    k.idtopt = (int)cfg->idtopt;
+
+    size_t nt = (size_t)d.nt;
+    DFields &f = c->kp.f;
+    f.u = A.get<double>(nt); f.v = A.get<double>(nt); f.w = A.get<double>(nt);
+    f.p = A.get<double>(nt); f.t = A.get<double>(nt);
+    for (int l = 0; l < 4; l++) { f.rhs1[l] = A.get<double>(nt); f.rk3o[l] = A.get<double>(nt); f.rk3oo[l] = A.get<double>(nt); }
+    f.nusgs = A.get<double>(nt); f.alsgs = A.get<double>(nt);
+    for (int l = 0; l < 3; l++) { f.nusgs1[l] = A.get<double>(nt); f.alsgs1[l] = A.get<double>(nt); }
+    f.qmass = A.get<double>(nt); f.divgsum = A.get<double>(nt); f.phi = A.get<double>(nt);
+    int nscr = (cfg->iles == 1) ? 33 : 3;
+    for (int s = 0; s < nscr; s++) f.scr[s] = A.get<double>(nt);
+    f.part = A.get<double>((size_t)(kRedBlocks + 1) * kMaxRed);
+    size_t np = (size_t)(d.n2 + 1) * (d.n3 + 1);
+    f.uout = A.get<double>(np); f.vout = A.get<double>(np); f.wout = A.get<double>(np); f.tout = A.get<double>(np);
+    f.duout = A.get<double>(np); f.dvout = A.get<double>(np); f.dwout = A.get<double>(np); f.dtout = A.get<double>(np);
+
+    // conjugate / LES defaults (conjg_allo, les_allo): c* = k* = 1, omega = nwall = 1
+    {
+        std::vector<double> one(nt, 1.0);
+        std::vector<int> ione(nt, 1);
+        f.cstar = upload(A, one.data(), nt);
+        for (int l = 0; l < 6; l++) f.kstar[l] = upload(A, one.data(), nt);
+        f.omega = upload(A, ione.data(), nt);
+        f.nwall = upload(A, ione.data(), nt);
+    }
+    // body function at the u points and at the cell centres
+    {
+        std::vector<double> fbu(nt), fbc(nt);
+        for (long long kk = 0; kk <= d.n3; kk++)
+            for (long long jj = 0; jj <= d.n2; jj++)
+                for (long long ii = 0; ii <= d.n1; ii++) {
+                    double xi = ii >= 1 ? g->x[ii - 1] : 0.0;
+                    size_t q = (size_t)(ii + d.sx * jj + d.sxy * kk);
+                    fbu[q] = funcbody(cfg->body, xi, g->ymp[jj], g->zmp[kk]);
+                    fbc[q] = funcbody(cfg->body, g->xmp[ii], g->ymp[jj], g->zmp[kk]);
+                }
+        f.fb_u = upload(A, fbu.data(), nt);
+        f.fb_c = upload(A, fbc.data(), nt);
+    }
+    // lhsinit (slv_mmtm.f90:180-249)
+    {
+        long long n1 = d.n1, n2 = d.n2, n3 = d.n3;
+        std::vector<double> aiu(n1 + 2, 0), ciu(n1 + 2, 0), aivw(n1 + 2, 0), civw(n1 + 2, 0);
+        std::vector<double> ajv(n2 + 2, 0), cjv(n2 + 2, 0), ajuw(n2 + 2, 0), cjuw(n2 + 2, 0);
+        std::vector<double> akw(n3 + 2, 0), ckw(n3 + 2, 0), akuv(n3 + 2, 0), ckuv(n3 + 2, 0);
+        auto C2CXI = [&](long long i) { return g->c2cxi[i]; };
+        auto C2CYI = [&](long long j) { return g->c2cyi[j]; };
+        auto C2CZI = [&](long long kk) { return g->c2czi[kk]; };
+        for (long long i = d.i_bgpx; i <= d.n1m; i++) {
+            long long im = g->imv[i - 1];
+            aiu[i] = -C2CXI(i) * g->f2fxi[im];
+            ciu[i] = -C2CXI(i) * g->f2fxi[i];
+        }
+        for (long long i = 1; i <= d.n1m; i++) {
+            long long ip = g->ipv[i - 1];
+            aivw[i] = -C2CXI(i) * g->f2fxi[i];
+            civw[i] = -C2CXI(ip) * g->f2fxi[i];
+        }
+        for (long long j = d.j_bgpy; j <= d.n2m; j++) {
+            long long jm = g->jmv[j - 1];
+            ajv[j] = -C2CYI(j) * g->f2fyi[jm];
+            cjv[j] = -C2CYI(j) * g->f2fyi[j];
+        }
+        for (long long j = 1; j <= d.n2m; j++) {
+            long long jp = g->jpv[j - 1];
+            ajuw[j] = -C2CYI(j) * g->f2fyi[j];
+            cjuw[j] = -C2CYI(jp) * g->f2fyi[j];
+        }
+        for (long long kk = d.k_bgpz; kk <= d.n3m; kk++) {
+            long long km = g->kmv[kk - 1];
+            akw[kk] = -C2CZI(kk) * g->f2fzi[km];
+            ckw[kk] = -C2CZI(kk) * g->f2fzi[kk];
+        }
+        for (long long kk = 1; kk <= d.n3m; kk++) {
+            long long kp = g->kpv[kk - 1];
+            akuv[kk] = -C2CZI(kk) * g->f2fzi[kk];
+            ckuv[kk] = -C2CZI(kp) * g->f2fzi[kk];
+        }
+        f.aiu = upload(A, aiu.data(), aiu.size()); f.ciu = upload(A, ciu.data(), ciu.size());
+        f.aivw = upload(A, aivw.data(), aivw.size()); f.civw = upload(A, civw.data(), civw.size());
+        f.ajv = upload(A, ajv.data(), ajv.size()); f.cjv = upload(A, cjv.data(), cjv.size());
+        f.ajuw = upload(A, ajuw.data(), ajuw.size()); f.cjuw = upload(A, cjuw.data(), cjuw.size());
+        f.akw = upload(A, akw.data(), akw.size()); f.ckw = upload(A, ckw.data(), ckw.size());
+        f.akuv = upload(A, akuv.data(), akuv.size()); f.ckuv = upload(A, ckuv.data(), ckuv.size());
+    }
+    // sgsfilterinit (sgs.f90:2-285): the 3-point weights cf?1
+    {
+        auto coefs = [&](const double *c2c, long long nm) {
+            std::vector<double> cf(3 * (nm + 2), 0.0);
+            if (nm != 1)
+                for (long long i = 1; i <= nm; i++) {
+                    double h1 = c2c[i], h2 = c2c[i + 1];
+                    cf[3 * i + 0] = (2.0 * h1 - h2) / 6.0 / h1;
+                    cf[3 * i + 1] = ((h1 + h2) * (h1 + h2)) / 6.0 / h1 / h2;
+                    cf[3 * i + 2] = (2.0 * h2 - h1) / 6.0 / h2;
+                }
+            return cf;
+        };
+        auto cx = coefs(g->c2cx, d.n1m), cy = coefs(g->c2cy, d.n2m), cz = coefs(g->c2cz, d.n3m);
+        f.cfx1 = upload(A, cx.data(), cx.size());
+        f.cfy1 = upload(A, cy.data(), cy.size());
+        f.cfz1 = upload(A, cz.data(), cz.size());
+    }
+    // IB placeholders (no forcing points until lesgpu_load_ibm)
+    for (int l = 0; l < 4; l++) {
+        f.ifc[l] = A.get<int>(1); f.jfc[l] = A.get<int>(1); f.kfc[l] = A.get<int>(1); f.intpindx[l] = A.get<int>(3);
+        f.geomfac[l] = A.get<double>(27); f.fcv[l] = A.get<double>(1); f.fcvavg[l] = A.get<double>(1);
+    }
+    for (int l = 0; l < 3; l++) f.dudtr[l] = A.get<double>(1);
+    f.inz = A.get<int>(1); f.jnz = A.get<int>(1); f.knz = A.get<int>(1);
+
+    c->S = A.get<DScal>(1);
+    c->kp.S = c->S;
+    c->h_f2fx = (double *)calloc(d.n1 + 2, sizeof(double));
+    c->h_f2fz = (double *)calloc(d.n3 + 2, sizeof(double));
+    for (long long i = 0; i <= d.n1; i++) c->h_f2fx[i] = g->f2fxi[i];
+    for (long long kk = 0; kk <= d.n3; kk++) c->h_f2fz[kk] = g->f2fzi[kk];
+    if (!A.ok) { lesgpu_destroy(c); return LESGPU_ERR_OOM; }
+    rc = poisson_init(c);
+    if (rc) { lesgpu_destroy(c); return rc; }
+    if (cudaDeviceSynchronize() != cudaSuccess) { lesgpu_destroy(c); return LESGPU_ERR_CUDA; }
+    *out = c;
+    return 0;
+}
+
+// --------------------------------------------------------------- load_ibm
+extern "C" int lesgpu_load_ibm(lesgpu_case *c, const lesgpu_ibm *b) {
+    if (!c || !b) return LESGPU_ERR_ARG;
+    const DGrid &d = c->kp.g;
+    DFields &f = c->kp.f;
+    Alloc &A = ((CaseExtra *)c->dmem_pool)->alloc;
+    int nl = c->cfg.ihtrans == 1 ? 4 : 3;
+    for (int l = 0; l < nl; l++)
+        if (b->nbody[l] != 0 || b->nintp[l] != 0) return LESGPU_ERR_UNSUPPORTED;   // IB forcing: not built yet
+    c->kp.c.nzero = (int)b->nzero;
+    if (b->nzero > 0) {
+        std::vector<int> a(b->nzero + 2), bb(b->nzero + 2), cc(b->nzero + 2);
+        for (long long n = 0; n < b->nzero; n++) { a[n + 1] = (int)b->inz[n]; bb[n + 1] = (int)b->jnz[n]; cc[n + 1] = (int)b->knz[n]; }
+        f.inz = upload(A, a.data(), a.size()); f.jnz = upload(A, bb.data(), bb.size()); f.knz = upload(A, cc.data(), cc.size());
+    }
+    size_t nt = (size_t)d.nt;
+    long long n1m = d.n1m, n2m = d.n2m, n3m = d.n3m, ncell = n1m * n2m * n3m;
+    auto scatter_d = [&](const double *src, double *dst) {
+        std::vector<double> h(nt, 1.0);
+        for (long long kk = 1; kk <= n3m; kk++)
+            for (long long j = 1; j <= n2m; j++)
+                for (long long i = 1; i <= n1m; i++)
+                    h[i + d.sx * j + d.sxy * kk] = src[(i - 1) + n1m * ((j - 1) + n2m * (kk - 1))];
+        cudaMemcpy(dst, h.data(), nt * sizeof(double), cudaMemcpyHostToDevice);
+    };
+    auto scatter_i = [&](const int64_t *src, int *dst) {
+        std::vector<int> h(nt, 1);
+        for (long long kk = 1; kk <= n3m; kk++)
+            for (long long j = 1; j <= n2m; j++)
+                for (long long i = 1; i <= n1m; i++)
+                    h[i + d.sx * j + d.sxy * kk] = (int)src[(i - 1) + n1m * ((j - 1) + n2m * (kk - 1))];
+        cudaMemcpy(dst, h.data(), nt * sizeof(int), cudaMemcpyHostToDevice);
+    };
+    if (b->nwall_dvm) scatter_i(b->nwall_dvm, f.nwall);
+    if (b->omega) scatter_i(b->omega, f.omega);
+    if (b->cstar) scatter_d(b->cstar, f.cstar);
+    if (b->kstar)
+        for (int l = 0; l < 6; l++) scatter_d(b->kstar + (size_t)l * ncell, f.kstar[l]);
+    if (!A.ok) return LESGPU_ERR_OOM;
+    return cuda_rc(cudaDeviceSynchronize());
+}
+
+// ------------------------------------------------------------- set_fields
+extern "C" int lesgpu_set_fields(lesgpu_case *c, const double *u, const double *v, const double *w,
+                                 const double *p, const double *t, double time, double dt, int64_t ihist, int64_t m) {
+    if (!c || !u || !v || !w || !p) return LESGPU_ERR_ARG;
+    size_t bytes = sizeof(double) * (size_t)c->kp.g.nt;
+    DFields &f = c->kp.f;
+    cudaMemcpyAsync(f.u, u, bytes, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(f.v, v, bytes, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(f.w, w, bytes, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(f.p, p, bytes, cudaMemcpyHostToDevice, c->stream);
+    if (t) cudaMemcpyAsync(f.t, t, bytes, cudaMemcpyHostToDevice, c->stream);
+    DScal s;
+    cudaMemcpy(&s, c->S, sizeof(DScal), cudaMemcpyDeviceToHost);
+    s.time = time; s.dt = dt; s.ihist = ihist; s.m = m;
+    cudaMemcpyAsync(c->S, &s, sizeof(DScal), cudaMemcpyHostToDevice, c->stream);
+    return cuda_rc(cudaStreamSynchronize(c->stream));
+}
+
+// ------------------------------------------------------------------ start
+__global__ void k_start(KP p) {
+    DScal *S = p.S;
+    S->ntime = 0;
+    S->cflmax = p.c.cflfac;
+    S->err_integral = 0.0;
+    S->err = 0;
+}
+
+extern "C" int lesgpu_start(lesgpu_case *c) {
+    if (!c) return LESGPU_ERR_ARG;
+    const lesgpu_config &g = c->cfg;
+    DScal s;
+    cudaMemcpy(&s, c->S, sizeof(DScal), cudaMemcpyDeviceToHost);
+    // dttimeinit, misc_init.f90:1001-1028
+    if (g.idtopt == 0) s.dt = g.dt_size;
+    if (g.idtopt != 0 && g.iread == 0) s.dt = g.dt_size;
+    if (g.ireset == 1) { s.ihist = 0; s.time = 0.0; }
+    cudaMemcpy(c->S, &s, sizeof(DScal), cudaMemcpyHostToDevice);
+    k_start<<<1, 1, 0, c->stream>>>(c->kp);
+    if (g.ich != 0) launch_meanpg(c);
+    if (g.ihtrans == 1 && g.ich == 1) launch_cvol(c);
+    c->ntime_host = 0;
+    c->started = 1;
+    if (c->graph_ok) { cudaGraphExecDestroy(c->graph); c->graph_ok = 0; }
+    return cuda_rc(cudaStreamSynchronize(c->stream));
+}
+
+// ------------------------------------------------------------------- step
+__global__ void k_retrv_uvw(KP p) {   // retrv_uvw, slv_mmtm.f90:1710-1743
+    const DGrid &g = p.g;
+    long long n = (long long)g.n2m * g.n3m;
+    for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (long long)gridDim.x * blockDim.x) {
+        int j = 1 + (int)(s % g.n2m), k = 1 + (int)(s / g.n2m);
+        long long pq = j + (long long)(g.n2 + 1) * k;
+        p.f.u[g.ix(g.n1, j, k)] = p.f.uout[pq];
+        if (j >= 2) p.f.v[g.ix(g.n1, j, k)] = p.f.vout[pq];
+        if (k >= g.k_bgpz) p.f.w[g.ix(g.n1, j, k)] = p.f.wout[pq];
+    }
+}
+
+static void enqueue_sgs(lesgpu_case *c, bool first) {
+    const lesgpu_config &g = c->cfg;
+    if (first) launch_sgs_zero_first(c, 0);
+    else launch_sgs(c);
+    launch_sgs_post(c);
+    if (g.ihtrans == 1) {
+        if (first) launch_sgs_zero_first(c, 1);
+        else launch_sgs_t(c);
+        launch_sgs_t_post(c);
+    }
+}
+
+static void enqueue_rhsnlhs(lesgpu_case *c, int msub) {
+    launch_rhs(c, msub);
+    launch_adi_uvw(c);
+    k_retrv_uvw<<<blocks_for((long long)c->kp.g.n2m * c->kp.g.n3m), kThreads, 0, c->stream>>>(c->kp);
+    launch_ghost_uvw(c);
+}
+
+static void enqueue_energy(lesgpu_case *c, int msub) {
+    const lesgpu_config &g = c->cfg;
+    if (g.ich == 1) launch_tvolcalc(c, 1);
+    launch_rhs_t(c, msub);
+    launch_adi_t(c);
+    launch_energy_bc(c);
+    if (g.ich == 1) { launch_tvolcalc(c, 2); launch_tvolcorr(c); }
+    launch_tcalc(c);
+    if (g.ich == 1) launch_tvolcalc(c, 0);
+}
+
+static void enqueue_step(lesgpu_case *c, bool first) {
+    const lesgpu_config &g = c->cfg;
+    launch_stepinit(c);
+    for (int msub = 1; msub <= 3; msub++) {
+        launch_substepinit(c, msub);
+        if (g.ich == 1) launch_qvolcalc(c, 1);
+        if (g.iles == 1 && msub == 1) enqueue_sgs(c, first);
+        enqueue_rhsnlhs(c, msub);
+        launch_divgs(c);
+        launch_poisson(c);
+        if (g.ich == 1) launch_qvolcalc(c, 2);
+        launch_ucalc(c);
+        if (g.ich == 1) launch_qvolcalc(c, 0);
+        launch_pcalc(c);
+        if (g.ich != 0) launch_meanpg(c);
+        if (g.ihtrans == 1) enqueue_energy(c, msub);
+    }
+    launch_time_advance(c);
+    launch_convergence(c);
+    launch_bulk_diag(c);
+}
+
+static void fill_report(const lesgpu_case *c, const DScal &s, lesgpu_step_report *r) {
+    memset(r, 0, sizeof(*r));
+    r->ntime = s.ntime; r->ihist = s.ihist; r->m = s.m;
+    r->time = s.time; r->dt = s.dt;
+    r->cflmax = s.cflmax; r->dvmax = s.dvmax; r->qmmax = s.qmmax;
+    for (int q = 0; q < 5; q++) r->pmi[q] = s.pmi[q];
+    r->pmiavg = s.pmiavg;
+    for (int q = 0; q < 3; q++) { r->qvol[q] = s.qvol[q]; r->tvol[q] = s.tvol[q]; r->cd[q] = s.cd[q]; r->heat_flux[q] = s.heat_flux[q]; }
+    r->csgsts = s.csgsts; r->csgshf = s.csgshf;
+    r->nutavg = s.nutavg; r->nutmax = s.nutmax; r->alpavg = s.alpavg; r->alpmax = s.alpmax;
+    r->ubulk = s.ubulk; r->tbulk_fluid = s.tbulk_fluid; r->tbulk_solid = s.tbulk_solid;
+    for (int q = 0; q < 3; q++) r->poisson_iters[q] = s.poisson_iters[q];
+}
+
+extern "C" int lesgpu_step(lesgpu_case *c, lesgpu_step_report *rep) {
+    if (!c) return LESGPU_ERR_ARG;
+    if (!c->started) return LESGPU_ERR_STATE;
+    c->ntime_host += 1;
+    bool first = (c->cfg.iread == 0 && c->ntime_host == 1);
+    if (c->use_graph && !first) {
+        if (!c->graph_ok) {
+            cudaGraph_t gr;
+            if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return LESGPU_ERR_CUDA;
+            enqueue_step(c, false);
+            if (cudaStreamEndCapture(c->stream, &gr) != cudaSuccess) return LESGPU_ERR_CUDA;
+            if (cudaGraphInstantiate(&c->graph, gr, 0) != cudaSuccess) { cudaGraphDestroy(gr); return LESGPU_ERR_CUDA; }
+            cudaGraphDestroy(gr);
+            c->graph_ok = 1;
+        }
+        if (cudaGraphLaunch(c->graph, c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
+    } else {
+        enqueue_step(c, first);
+    }
+    if (cudaMemcpyAsync(&c->hS, c->S, sizeof(DScal), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
+    if (rep) fill_report(c, c->hS, rep);
+    if (c->hS.err) return LESGPU_ERR_NAN;
+    return 0;
+}
+
+// Enqueue n steps without reading anything back (benchmark path; the
+// caller synchronises the stream).  n must be >= 1; steps follow the same
+// graph path as lesgpu_step.
+extern "C" int lesgpu_step_async(lesgpu_case *c, int64_t n) {
+    if (!c || n < 1) return LESGPU_ERR_ARG;
+    if (!c->started) return LESGPU_ERR_STATE;
+    for (int64_t s = 0; s < n; s++) {
+        c->ntime_host += 1;
+        bool first = (c->cfg.iread == 0 && c->ntime_host == 1);
+        if (c->use_graph && !first) {
+            if (!c->graph_ok) {
+                cudaGraph_t gr;
+                if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return LESGPU_ERR_CUDA;
+                enqueue_step(c, false);
+                if (cudaStreamEndCapture(c->stream, &gr) != cudaSuccess) return LESGPU_ERR_CUDA;
+                if (cudaGraphInstantiate(&c->graph, gr, 0) != cudaSuccess) { cudaGraphDestroy(gr); return LESGPU_ERR_CUDA; }
+                cudaGraphDestroy(gr);
+                c->graph_ok = 1;
+            }
+            if (cudaGraphLaunch(c->graph, c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
+        } else {
+            enqueue_step(c, first);
+        }
+    }
+    return 0;
+}
+
+extern "C" int lesgpu_stream(lesgpu_case *c, void **stream) {
+    if (!c || !stream) return LESGPU_ERR_ARG;
+    *stream = (void *)c->stream;
+    return 0;
+}
+
+extern "C" int lesgpu_use_graph(lesgpu_case *c, int on) {
+    if (!c) return LESGPU_ERR_ARG;
+    c->use_graph = on ? 1 : 0;
+    return 0;
+}
+
+extern "C" int lesgpu_get_report(lesgpu_case *c, lesgpu_step_report *rep) {
+    if (!c || !rep) return LESGPU_ERR_ARG;
+    if (cudaMemcpy(&c->hS, c->S, sizeof(DScal), cudaMemcpyDeviceToHost) != cudaSuccess) return LESGPU_ERR_CUDA;
+    fill_report(c, c->hS, rep);
+    return 0;
+}
+
+extern "C" int lesgpu_get_fields(lesgpu_case *c, double *u, double *v, double *w, double *p, double *t) {
+    if (!c) return LESGPU_ERR_ARG;
+    size_t bytes = sizeof(double) * (size_t)c->kp.g.nt;
+    DFields &f = c->kp.f;
+    if (u) cudaMemcpyAsync(u, f.u, bytes, cudaMemcpyDeviceToHost, c->stream);
+    if (v) cudaMemcpyAsync(v, f.v, bytes, cudaMemcpyDeviceToHost, c->stream);
+    if (w) cudaMemcpyAsync(w, f.w, bytes, cudaMemcpyDeviceToHost, c->stream);
+    if (p) cudaMemcpyAsync(p, f.p, bytes, cudaMemcpyDeviceToHost, c->stream);
+    if (t) cudaMemcpyAsync(t, f.t, bytes, cudaMemcpyDeviceToHost, c->stream);
+    return cuda_rc(cudaStreamSynchronize(c->stream));
+}
+
+static int field_ptrs(lesgpu_case *c, int64_t fld, double **ptr, int *nc) {
+    DFields &f = c->kp.f;
+    *nc = 1;
+    switch (fld) {
+    case LESGPU_F_U: ptr[0] = f.u; return 0;
+    case LESGPU_F_V: ptr[0] = f.v; return 0;
+    case LESGPU_F_W: ptr[0] = f.w; return 0;
+    case LESGPU_F_P: ptr[0] = f.p; return 0;
+    case LESGPU_F_T: ptr[0] = f.t; return 0;
+    case LESGPU_F_NUSGS: ptr[0] = f.nusgs; return 0;
+    case LESGPU_F_ALSGS: ptr[0] = f.alsgs; return 0;
+    case LESGPU_F_NUSGS1: *nc = 3; for (int l = 0; l < 3; l++) ptr[l] = f.nusgs1[l]; return 0;
+    case LESGPU_F_ALSGS1: *nc = 3; for (int l = 0; l < 3; l++) ptr[l] = f.alsgs1[l]; return 0;
+    case LESGPU_F_RHS1: *nc = 4; for (int l = 0; l < 4; l++) ptr[l] = f.rhs1[l]; return 0;
+    case LESGPU_F_RK3O: *nc = 4; for (int l = 0; l < 4; l++) ptr[l] = f.rk3o[l]; return 0;
+    case LESGPU_F_RK3OO: *nc = 4; for (int l = 0; l < 4; l++) ptr[l] = f.rk3oo[l]; return 0;
+    case LESGPU_F_DIVGSUM: ptr[0] = f.divgsum; return 0;
+    case LESGPU_F_PHI: ptr[0] = f.phi; return 0;
+    case LESGPU_F_QMASS: ptr[0] = f.qmass; return 0;
+    default: return LESGPU_ERR_ARG;
+    }
+}
+
+extern "C" int lesgpu_get_array(lesgpu_case *c, int64_t fld, double *out) {
+    double *ptr[4];
+    int nc;
+    if (!c || !out || field_ptrs(c, fld, ptr, &nc)) return LESGPU_ERR_ARG;
+    size_t nt = (size_t)c->kp.g.nt;
+    for (int l = 0; l < nc; l++) cudaMemcpyAsync(out + l * nt, ptr[l], nt * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    return cuda_rc(cudaStreamSynchronize(c->stream));
+}
+
+extern "C" int lesgpu_set_array(lesgpu_case *c, int64_t fld, const double *in) {
+    double *ptr[4];
+    int nc;
+    if (!c || !in || field_ptrs(c, fld, ptr, &nc)) return LESGPU_ERR_ARG;
+    size_t nt = (size_t)c->kp.g.nt;
+    for (int l = 0; l < nc; l++) cudaMemcpyAsync(ptr[l], in + l * nt, nt * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    return cuda_rc(cudaStreamSynchronize(c->stream));
+}
+
+extern "C" int lesgpu_run_phase(lesgpu_case *c, int64_t phase, int64_t msub) {
+    if (!c || msub < 1 || msub > 3) return LESGPU_ERR_ARG;
+    const lesgpu_config &g = c->cfg;
+    switch (phase) {
+    case LESGPU_PH_STEPINIT: launch_stepinit(c); c->ntime_host += 1; break;
+    case LESGPU_PH_SUBSTEPINIT: launch_substepinit(c, (int)msub); break;
+    case LESGPU_PH_SGS:
+        if (g.iles == 1 && msub == 1) enqueue_sgs(c, g.iread == 0 && c->ntime_host == 1);
+        break;
+    case LESGPU_PH_RHSNLHS: enqueue_rhsnlhs(c, (int)msub); break;
+    case LESGPU_PH_DIVGS:
+        cudaMemsetAsync(c->kp.f.divgsum, 0, sizeof(double) * c->kp.g.nt, c->stream);
+        launch_divgs(c);
+        break;
+    case LESGPU_PH_POISSON:
+        cudaMemsetAsync(c->kp.f.phi, 0, sizeof(double) * c->kp.g.nt, c->stream);
+        launch_poisson(c);
+        break;
+    case LESGPU_PH_UCALC:
+        if (g.ich == 1) launch_qvolcalc(c, 2);
+        launch_ucalc(c);
+        if (g.ich == 1) launch_qvolcalc(c, 0);
+        launch_pcalc(c);
+        break;
+    case LESGPU_PH_MEANPG: if (g.ich != 0) launch_meanpg(c); break;
+    case LESGPU_PH_ENERGY: if (g.ihtrans == 1) enqueue_energy(c, (int)msub); break;
+    default: return LESGPU_ERR_ARG;
+    }
+    return cuda_rc(cudaStreamSynchronize(c->stream));
+}
+
+extern "C" int lesgpu_destroy(lesgpu_case *c) {
+    if (!c) return 0;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->graph_ok) cudaGraphExecDestroy(c->graph);
+    poisson_free(c);
+    CaseExtra *X = (CaseExtra *)c->dmem_pool;
+    if (X) {
+        for (void *p : X->alloc.ptrs) cudaFree(p);
+        delete X;
+    }
+    if (c->stream) cudaStreamDestroy(c->stream);
+    free(c->h_f2fx);
+    free(c->h_f2fz);
+    free(c);
+    return 0;
+}
+
+extern "C" const char *lesgpu_strerror(int code) {
+    switch (code) {
+    case LESGPU_OK: return "ok";
+    case LESGPU_ERR_ARG: return "invalid argument";
+    case LESGPU_ERR_CONFIG: return "option combination rejected by the reference solver";
+    case LESGPU_ERR_CUDA: return "CUDA runtime error";
+    case LESGPU_ERR_OOM: return "device memory exhausted";
+    case LESGPU_ERR_NOT_CONVERGED: return "Poisson iteration limit exceeded";
+    case LESGPU_ERR_NAN: return "non-finite value in the solver state";
+    case LESGPU_ERR_STATE: return "call out of order";
+    case LESGPU_ERR_UNSUPPORTED: return "option not built in this library";
+    default: return "unknown error";
+    }
+}
+
+extern "C" int lesgpu_abi_version(void) { return LESGPU_ABI_VERSION; }

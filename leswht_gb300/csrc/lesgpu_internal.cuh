@@ -1,0 +1,282 @@
+// Internal declarations of the GB300 LES time-step library.
+//
+// Data layout in HBM: every 3-D array (fields, right-hand sides, RK3
+// histories, eddy viscosities, Poisson source and solution) is a dense FP64
+// array in the reference's Fortran (0:n1,0:n2,0:n3) layout, i fastest:
+// element (i,j,k) at i + sx*j + sxy*k with sx = n1+1, sxy = (n1+1)(n2+1).
+// Keeping the reference layout makes lesgpu_set_fields / get_fields a single
+// contiguous copy and lets a warp read 32 consecutive i with one 256-byte
+// transaction.  1-D metric vectors keep their Fortran index (x[1..n1],
+// c2cx[0..n1]); index vectors are int32 on the device.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+#include "../../include/lesgpu.h"
+
+#define LG_HD __host__ __device__ __forceinline__
+
+namespace lg {
+
+constexpr int kThreads = 256;
+constexpr int kRedBlocks = 608;        // 4 x 152 SMs: reduction grid, fixed for determinism
+constexpr int kMaxRed = 8;             // values reduced together in one pass
+
+struct DGrid {
+    int n1, n2, n3, n1m, n2m, n3m, n1mh, n3mh;
+    long long sx, sxy, nt;
+    double xl, yl, zl;
+    const double *x, *y, *z, *xmp, *ymp, *zmp;
+    const double *f2fx, *f2fy, *f2fz, *f2fxi, *f2fyi, *f2fzi;
+    const double *c2cx, *c2cy, *c2cz, *c2cxi, *c2cyi, *c2czi;
+    const int *ipv, *jpv, *kpv, *imv, *jmv, *kmv;
+    const int *fixil, *fixiu, *fixjl, *fixju, *fixkl, *fixku;
+    int i_bgpx, j_bgpy, k_bgpz;
+    LG_HD long long ix(long long i, long long j, long long k) const { return i + sx * j + sxy * k; }
+};
+
+struct DCfg {
+    double re, pr, gr, udrv_i, tflu_i, tsol_i;
+    double val_t_ybtm, val_t_ytop, val_t_zbtm, val_t_ztop;
+    double resid1, csgsts, csgshf, cflfac, dt_size, ptb_tst, avg_tst, tend;
+    int grdir, iles, ihtrans, ich, iconjg, idecomp, idvmon, filter, ibmon, masson, imovingon, iread;
+    int xprdic, yprdic, zprdic;
+    int bc_ybtm, bc_ytop, bc_zbtm, bc_ztop, bc_t_ybtm, bc_t_ytop, bc_t_zbtm, bc_t_ztop;
+    int idtopt;
+    int nintp[4], nbody[4];
+    int nzero;
+};
+
+// Scalars of mod_common that change during a step.  They live in device
+// memory so a whole step can run (and be captured in a CUDA graph) without
+// a host round trip; the host reads them once at the end of the step.
+struct DScal {
+    double dt, time, subdt;
+    double cflmax, dvmax, qmmax;
+    double alpha, dtconst, dtconsti, test1, acoef, acoefi;
+    double pmi[5], pmiavg, qvol[3], tvol[3], thcap;
+    double csgsts, csgshf, nutavg, nutmax, alpavg, alpmax;
+    double err_integral;
+    double dudta, dvdta, dwdta;
+    double cd[3], heat_flux[3];
+    double ubulk, tbulk_fluid, tbulk_solid;
+    double u_bulk_t;          // rhs_t's bulk velocity of the current substep
+    double phiref;            // pcalc's outlet-plane mean of phi
+    double cvol;              // tvolcorr's volume integral of 1/c*
+    long long ntime, m, ihist;
+    long long poisson_iters[3];
+    int err;                  // device-side error flag (non-finite values etc.)
+};
+
+struct DFields {
+    double *u, *v, *w, *p, *t;
+    double *rhs1[4], *rk3o[4], *rk3oo[4];
+    double *nusgs, *nusgs1[3], *alsgs, *alsgs1[3];
+    double *qmass, *divgsum, *phi;
+    double *cstar, *kstar[6];
+    int *omega, *nwall;
+    double *fb_u, *fb_c;
+    // convective outlet planes (0:n2,0:n3)
+    double *uout, *vout, *wout, *tout, *duout, *dvout, *dwout, *dtout;
+    // ADI coefficient vectors (lhsinit)
+    double *aiu, *ciu, *aivw, *civw, *ajv, *cjv, *ajuw, *cjuw, *akw, *ckw, *akuv, *ckuv;
+    // Simpson test-filter weights cf?1(n?m,-1:1)
+    double *cfx1, *cfy1, *cfz1;
+    // IB tables (component l = 0..3); 1-based rows
+    int *ifc[4], *jfc[4], *kfc[4], *intpindx[4];
+    double *geomfac[4], *fcv[4], *fcvavg[4], *dudtr[3];
+    int *inz, *jnz, *knz;
+    // scratch
+    double *scr[34];          // SGS temporaries / tridiagonal work, nt each
+    double *part;             // reduction partials kRedBlocks * kMaxRed
+};
+
+// Poisson FFT plan of one line length.
+struct FftPlan {
+    int n;
+    int nst;
+    int rad[24];
+    double2 *tw;              // exp(-2 pi i e / n), e = 0..n-1 (device)
+};
+
+struct DPois {
+    double *ak1, *ak3;
+    double2 *ccap;            // spectrum (n1m, n3mh, n2m): i fastest, then k, then j
+    FftPlan fx, fz;
+};
+
+struct KP {                   // everything a kernel may read, passed by value
+    DGrid g;
+    DCfg c;
+    DFields f;
+    DScal *S;
+};
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ double fixd(int v) { return (double)v; }
+
+// Decode a linear thread index over the interior box [i0..i1]x[j0..j1]x[k0..k1].
+struct Box {
+    int i0, j0, k0, ni, nj, nk;
+    LG_HD long long count() const { return (long long)ni * nj * nk; }
+    LG_HD void at(long long t, int &i, int &j, int &k) const {
+        i = i0 + (int)(t % ni);
+        long long r = t / ni;
+        j = j0 + (int)(r % nj);
+        k = k0 + (int)(r / nj);
+    }
+};
+
+inline int blocks_for(long long n, int threads = kThreads) {
+    long long b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > 0x7fffffffLL) b = 0x7fffffffLL;
+    return (int)b;
+}
+
+// Deterministic block reduction of NV doubles (sum or max); result valid in thread 0.
+template <int NV, bool MAX>
+__device__ __forceinline__ void block_reduce(double (&v)[NV]) {
+    __shared__ double sh[NV][kThreads / 32];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+        double x = v[q];
+        for (int o = 16; o > 0; o >>= 1) {
+            double y = __shfl_down_sync(0xffffffffu, x, o);
+            x = MAX ? fmax(x, y) : x + y;
+        }
+        if (lane == 0) sh[q][wid] = x;
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            double x = (lane < (int)(blockDim.x >> 5)) ? sh[q][lane] : (MAX ? -1.0e308 : 0.0);
+            for (int o = 16; o > 0; o >>= 1) {
+                double y = __shfl_down_sync(0xffffffffu, x, o);
+                x = MAX ? fmax(x, y) : x + y;
+            }
+            v[q] = x;
+        }
+    }
+    __syncthreads();
+}
+
+// Sum (or max) the kRedBlocks partials of NV values in a fixed order.
+template <int NV, bool MAX>
+__device__ __forceinline__ void finalize_partials(const double *part, int nblk, double (&out)[NV]) {
+    double v[NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++) v[q] = MAX ? -1.0e308 : 0.0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x)
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            double x = part[(size_t)b * kMaxRed + q];
+            v[q] = MAX ? fmax(v[q], x) : v[q] + x;
+        }
+    block_reduce<NV, MAX>(v);
+#pragma unroll
+    for (int q = 0; q < NV; q++) out[q] = v[q];
+}
+
+}  // namespace lg
+
+// --------------------------------------------------------------- the case
+struct lesgpu_case {
+    lesgpu_config cfg;
+    lg::KP kp;
+    lg::DPois pois;
+    cudaStream_t stream;
+    cudaEvent_t ev[8];
+    void *dmem_pool;           // single device allocation backing every array
+    size_t dmem_bytes;
+    lg::DScal *S;              // == kp.S
+    lg::DScal hS;              // host copy after the last step
+    int started;
+    int ntime_host;
+    cudaGraphExec_t graph;     // captured steady-state step
+    int graph_ok;
+    int use_graph;
+    // host mirrors of metrics used for init-time tables
+    double *h_f2fx, *h_f2fy, *h_f2fz;
+};
+
+namespace lg {
+// launch wrappers implemented in the k_*.cu files
+void launch_stepinit(lesgpu_case *c);
+void launch_substepinit(lesgpu_case *c, int msub);
+void launch_qvolcalc(lesgpu_case *c, int slot);
+void launch_tvolcalc(lesgpu_case *c, int slot);
+void launch_tvolcorr(lesgpu_case *c);
+void launch_meanpg(lesgpu_case *c);
+void launch_ucalc(lesgpu_case *c);
+void launch_pcalc(lesgpu_case *c);
+void launch_tcalc(lesgpu_case *c);
+void launch_convergence(lesgpu_case *c);
+void launch_bulk_diag(lesgpu_case *c);
+void launch_time_advance(lesgpu_case *c);
+void launch_rhs(lesgpu_case *c, int msub);
+void launch_divgs(lesgpu_case *c);
+void launch_ghost_uvw(lesgpu_case *c);
+void launch_rhs_t(lesgpu_case *c, int msub);
+void launch_energy_bc(lesgpu_case *c);
+void launch_adi_uvw(lesgpu_case *c);
+void launch_adi_t(lesgpu_case *c);
+void launch_sgs(lesgpu_case *c);
+void launch_sgs_t(lesgpu_case *c);
+void launch_poisson(lesgpu_case *c);
+int poisson_init(lesgpu_case *c);
+void poisson_free(lesgpu_case *c);
+void launch_sgs_zero_first(lesgpu_case *c, int thermal);
+}  // namespace lg
+
+namespace lg {
+// ----------------------------------------------------------- generic sums
+template <int NV, bool MAX, class F>
+__global__ void __launch_bounds__(kThreads) k_reduce(KP p, Box b, F f) {
+    double v[NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++) v[q] = MAX ? -1.0e308 : 0.0;
+    long long n = b.count();
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        b.at(t, i, j, k);
+        double w[NV];
+        f(p, i, j, k, w);
+#pragma unroll
+        for (int q = 0; q < NV; q++) v[q] = MAX ? fmax(v[q], w[q]) : v[q] + w[q];
+    }
+    block_reduce<NV, MAX>(v);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int q = 0; q < NV; q++) p.f.part[(size_t)blockIdx.x * kMaxRed + q] = v[q];
+}
+
+template <int NV, bool MAX, class G>
+__global__ void __launch_bounds__(kThreads) k_final(KP p, int nblk, G g) {
+    double out[NV];
+    finalize_partials<NV, MAX>(p.f.part, nblk, out);
+    if (threadIdx.x == 0) g(p, out);
+}
+
+template <int NV, bool MAX, class F, class G>
+inline void reduce(lesgpu_case *c, Box b, F f, G g) {
+    int nb = blocks_for(b.count());
+    if (nb > kRedBlocks) nb = kRedBlocks;
+    k_reduce<NV, MAX><<<nb, kThreads, 0, c->stream>>>(c->kp, b, f);
+    k_final<NV, MAX><<<1, kThreads, 0, c->stream>>>(c->kp, nb, g);
+}
+
+
+// Periodic ghost copy of one plane pair (see k_ghost in k_aux.cu).
+struct GhostSpec {
+    double *a;
+    int lo0, hi0, lo1, hi1;   // ranges of the two in-plane indices (in index order)
+};
+void ghost(lesgpu_case *c, int dir, GhostSpec *s, int na);
+void launch_cvol(lesgpu_case *c);
+void launch_rhs_t_kernel(lesgpu_case *c, int msub);
+}  // namespace lg

@@ -1,0 +1,120 @@
+"""GPU parity: the CUDA library against the CPU oracle on identical inputs,
+phase by phase and over whole steps, through the C ABI.
+
+Tolerance: relative L2 <= 1e-10 per field after one step (FP64 path; the
+two implementations differ only in summation order and FMA contraction,
+~1e-15 per operation).  Multi-step runs are held to 1e-9.
+"""
+import numpy as np
+import pytest
+
+import leswht_gb300
+from leswht_gb300 import abi, cases, solver
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def rel(a, b):
+    den = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (den if den > 0 else 1.0)
+
+
+def make_pair(oracle_lib, case):
+    return leswht_gb300.gpu_solver(case), solver.Solver(oracle_lib, "ref_", case)
+
+
+@pytest.fixture(scope="module")
+def small_case():
+    return cases.channel(32, 32, 16)
+
+
+def test_one_step_fields(oracle_lib, small_case):
+    g, r = make_pair(oracle_lib, small_case)
+    rg, rr = g.step(), r.step()
+    fg, fr = g.fields(), r.fields()
+    for k in ("u", "v", "w", "p", "t"):
+        assert rel(fg[k], fr[k]) <= TOL, (k, rel(fg[k], fr[k]))
+    assert rg["dt"] == pytest.approx(rr["dt"], rel=1e-14)
+    assert rg["cflmax"] == pytest.approx(rr["cflmax"], rel=1e-13)
+    assert rg["csgsts"] == pytest.approx(rr["csgsts"], rel=1e-9)
+    assert rg["csgshf"] == pytest.approx(rr["csgshf"], rel=1e-9)
+    assert rg["pmi"][0] == pytest.approx(rr["pmi"][0], rel=1e-9)
+    assert rg["ubulk"] == pytest.approx(rr["ubulk"], rel=1e-12)
+    assert rg["dvmax"] < 1e-11 and rr["dvmax"] < 1e-11
+
+
+def test_phases(oracle_lib, small_case):
+    """stepinit -> substepinit -> SGS -> RHS+ADI -> divgs -> Poisson -> projection -> meanpg -> energy."""
+    g, r = make_pair(oracle_lib, small_case)
+    for s in (g, r):
+        s.phase(abi.PH_STEPINIT)
+        s.phase(abi.PH_SUBSTEPINIT, 1)
+    assert g.report()["dt"] == pytest.approx(r.report()["dt"], rel=1e-14)
+    for s in (g, r):
+        s.phase(abi.PH_SGS, 1)
+    for f in (abi.F_NUSGS, abi.F_NUSGS1, abi.F_ALSGS, abi.F_ALSGS1):
+        assert rel(g.get(f), r.get(f)) <= TOL, f
+    for s in (g, r):
+        s.phase(abi.PH_RHSNLHS, 1)
+    for f in (abi.F_U, abi.F_V, abi.F_W, abi.F_RK3O):
+        assert rel(g.get(f), r.get(f)) <= TOL, f
+    for s in (g, r):
+        s.phase(abi.PH_DIVGS, 1)
+    assert rel(g.get(abi.F_DIVGSUM), r.get(abi.F_DIVGSUM)) <= TOL
+    for s in (g, r):
+        s.phase(abi.PH_POISSON, 1)
+    assert rel(g.get(abi.F_PHI), r.get(abi.F_PHI)) <= TOL
+    for s in (g, r):
+        s.phase(abi.PH_UCALC, 1)
+        s.phase(abi.PH_MEANPG, 1)
+        s.phase(abi.PH_ENERGY, 1)
+    for f in (abi.F_U, abi.F_V, abi.F_W, abi.F_P, abi.F_T):
+        assert rel(g.get(f), r.get(f)) <= TOL, f
+
+
+def test_poisson_same_input(oracle_lib, small_case):
+    g, r = make_pair(oracle_lib, small_case)
+    gm = small_case.grid
+    rng = np.random.default_rng(11)
+    d = np.zeros(gm.shape)
+    d[1:gm.n3m + 1, 1:gm.n2m + 1, 1:gm.n1m + 1] = rng.standard_normal((gm.n3m, gm.n2m, gm.n1m))
+    for s in (g, r):
+        s.set(abi.F_DIVGSUM, d)
+        s.phase(abi.PH_POISSON)
+    assert rel(g.get(abi.F_PHI), r.get(abi.F_PHI)) <= 1e-12
+
+
+def test_five_steps(oracle_lib, small_case):
+    g, r = make_pair(oracle_lib, small_case)
+    for n in range(5):
+        rg, rr = g.step(), r.step()
+    fg, fr = g.fields(), r.fields()
+    for k in ("u", "v", "w", "p", "t"):
+        assert rel(fg[k], fr[k]) <= 1e-9, (k, rel(fg[k], fr[k]))
+    assert rg["time"] == pytest.approx(rr["time"], rel=1e-13)
+
+
+def test_channel64_one_step(oracle_lib):
+    c = cases.channel(64, 64, 64)
+    g, r = make_pair(oracle_lib, c)
+    g.step()
+    r.step()
+    fg, fr = g.fields(), r.fields()
+    for k in ("u", "v", "w", "p", "t"):
+        assert rel(fg[k], fr[k]) <= TOL, (k, rel(fg[k], fr[k]))
+
+
+def test_gpu_deterministic_and_graph_equals_eager(small_case):
+    lib = leswht_gb300.load_library()
+    outs = []
+    for use_graph in (1, 1, 0):
+        s = leswht_gb300.gpu_solver(small_case)
+        lib.lesgpu_use_graph(s.h, use_graph)
+        for _ in range(3):
+            s.step()
+        outs.append(s.fields())
+    for k in outs[0]:
+        np.testing.assert_array_equal(outs[0][k], outs[1][k])
+        np.testing.assert_array_equal(outs[0][k], outs[2][k])
