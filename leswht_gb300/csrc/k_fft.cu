@@ -317,11 +317,13 @@ int poisson_init(lesgpu_case *c) {
     free(ak1); free(ak3);
     size_t nspec = (size_t)g.n1m * g.n3mh * g.n2m;
     if (cudaMalloc(&P.ccap, sizeof(double2) * nspec) != cudaSuccess) return LESGPU_ERR_OOM;
-    int Lz = lines_per_block(g.n3m), Lx = lines_per_block(g.n1m);
-    size_t smz = (size_t)2 * g.n3m * Lz * sizeof(double2), smx = (size_t)2 * g.n1m * Lx * sizeof(double2);
-    cudaFuncSetAttribute(k_fft_z_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
-    cudaFuncSetAttribute(k_fft_z_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
-    cudaFuncSetAttribute(k_fft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+    // the attribute is per function and shared by every case: set it to the
+    // largest size lines_per_block() can ask for
+    const int kMaxSmem = 200 * 1024;
+    if (cudaFuncSetAttribute(k_fft_z_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_fft_z_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_fft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem) != cudaSuccess)
+        return LESGPU_ERR_CUDA;
     return 0;
 }
 

@@ -326,7 +326,8 @@ extern "C" int lesgpu_set_fields(lesgpu_case *c, const double *u, const double *
     cudaMemcpyAsync(f.p, p, bytes, cudaMemcpyHostToDevice, c->stream);
     if (t) cudaMemcpyAsync(f.t, t, bytes, cudaMemcpyHostToDevice, c->stream);
     DScal s;
-    cudaMemcpy(&s, c->S, sizeof(DScal), cudaMemcpyDeviceToHost);
+    cudaMemcpyAsync(&s, c->S, sizeof(DScal), cudaMemcpyDeviceToHost, c->stream);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
     s.time = time; s.dt = dt; s.ihist = ihist; s.m = m;
     cudaMemcpyAsync(c->S, &s, sizeof(DScal), cudaMemcpyHostToDevice, c->stream);
     return cuda_rc(cudaStreamSynchronize(c->stream));
@@ -345,12 +346,13 @@ extern "C" int lesgpu_start(lesgpu_case *c) {
     if (!c) return LESGPU_ERR_ARG;
     const lesgpu_config &g = c->cfg;
     DScal s;
-    cudaMemcpy(&s, c->S, sizeof(DScal), cudaMemcpyDeviceToHost);
+    cudaMemcpyAsync(&s, c->S, sizeof(DScal), cudaMemcpyDeviceToHost, c->stream);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
     // dttimeinit, misc_init.f90:1001-1028
     if (g.idtopt == 0) s.dt = g.dt_size;
     if (g.idtopt != 0 && g.iread == 0) s.dt = g.dt_size;
     if (g.ireset == 1) { s.ihist = 0; s.time = 0.0; }
-    cudaMemcpy(c->S, &s, sizeof(DScal), cudaMemcpyHostToDevice);
+    cudaMemcpyAsync(c->S, &s, sizeof(DScal), cudaMemcpyHostToDevice, c->stream);
     k_start<<<1, 1, 0, c->stream>>>(c->kp);
     if (g.ich != 0) launch_meanpg(c);
     if (g.ihtrans == 1 && g.ich == 1) launch_cvol(c);
@@ -506,7 +508,8 @@ extern "C" int lesgpu_use_graph(lesgpu_case *c, int on) {
 
 extern "C" int lesgpu_get_report(lesgpu_case *c, lesgpu_step_report *rep) {
     if (!c || !rep) return LESGPU_ERR_ARG;
-    if (cudaMemcpy(&c->hS, c->S, sizeof(DScal), cudaMemcpyDeviceToHost) != cudaSuccess) return LESGPU_ERR_CUDA;
+    if (cudaMemcpyAsync(&c->hS, c->S, sizeof(DScal), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
     fill_report(c, c->hS, rep);
     return 0;
 }
