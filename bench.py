@@ -1,0 +1,368 @@
+#!/usr/bin/env python
+"""Benchmark of the LES time step on GB300.
+
+Metric: Mcell-steps/s = n1m*n2m*n3m*steps / seconds / 1e6, one step being the
+three RK3 substeps with SGS, momentum RHS + ADI, Poisson, projection,
+temperature and the per-step checks.  Workload (default): the turbulent
+channel at Re_tau ~ 180 with passive heat transfer, 64x64x64 cells, seeded
+synthetic initial field (laminar profile + 10% uniform perturbation).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Our arm (one JSON line on rank 0):
+  value    : device-resident throughput; every step is bracketed by CUDA
+             events on the case's own stream and L2 is flushed (256 MiB
+             write) between timed steps, outside the timed region.
+  e2e      : the same metric through the C ABI with host buffers: each step
+             uploads u,v,w,p,t from pinned host memory (lesgpu_set_fields),
+             steps (lesgpu_step, which reads the step report back) and
+             downloads u,v,w,p,t (lesgpu_get_fields); host wall clock.
+  roofline : the dominant kernel class (largest device time in the
+             instrumented steps), its algorithmic bytes per launch divided by
+             its average launch time (events on the launching stream), against
+             the measured HBM copy bandwidth.
+  cpu_baseline : the CPU oracle (C/OpenMP restatement of the solver, the
+             reference's Fortran cannot be built on this host) on a bounded
+             sample of the same workload, all host threads.
+Reference arm (--impl reference): the same CPU restatement timed on the same
+config with all host threads; rank 0 alone runs under torchrun.
+
+Multi-GPU: replicas only (one independent case per GPU, no collective on the
+data path); value = all ranks' cell-steps / max over ranks of the time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mcell-steps/s (mixed vs FP64 GPU) at stated error; p50/p99 served-case latency"
+UNIT = "Mcell-steps/s"
+
+# Algorithmic FP64 words per cell of one launch of each kernel class
+# (each distinct input read once, each output written once).
+#   RHS   : read u,v,w,p,nu,nu1(3),rk3o(3); write rhs1(3),rk3o(3),rk3oo(3)   -> 20 w
+#   ADI   : one sweep of one component: z and y read rhs + a coefficient
+#           field and write the result (3 w); x also reads and writes the
+#           field (4 w); mean over the three directions                     -> 10/3 w
+#   POISSON : whole FFT/Thomas solve (div in, phi out, spectrum round trips) -> 6 w
+#   SGS   : one batched test-filter launch of m arrays: read m, write m      -> 2m w
+#   RHS_T : read t,u,v,w,al1(3),rk3to,c*,k*(6),omega; write rhs,rk3to,rk3too -> 19 w
+KCLASS = {1: "rhs", 2: "adi", 3: "sgs_filter", 4: "poisson", 5: "rhs_t"}
+KWORDS = {1: 20.0, 2: 10.0 / 3.0, 4: 6.0, 5: 19.0}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def make_case(name, form):
+    from leswht_gb300 import abi, cases
+    prec = abi.PREC_FP64 if form == "fp64" else abi.PREC_MIXED
+    if name == "channel64":
+        return cases.channel(64, 64, 64, precision=prec)
+    if name == "channel590":
+        return cases.PRESETS["channel590"](precision=prec)
+    if name == "channel_small":
+        return cases.channel(32, 32, 16, precision=prec)
+    raise SystemExit(f"unknown config {name}")
+
+
+WORKLOAD = {
+    "channel64": "turbulent channel Re_tau~180 with passive heat transfer, 4pi x 2 x 4pi/3, 64x64x64 cells, "
+                 "tanh wall-normal stretching (gamma 2.75), CFR forcing, dynamic Vreman + dynamic EDM, poiss_ftft",
+    "channel590": "turbulent channel Re_tau~590 with passive heat transfer, 2pi x 2 x pi, 384x256x384 cells, poiss_ftft",
+    "channel_small": "turbulent channel 32x32x16 (test size)",
+}
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    parts = [x.strip() for x in line.split(",")]
+                    if len(parts) >= 9:
+                        rows.append(parts)
+            os.unlink(self.path)
+        except Exception:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def cpu_baseline(name, form, seconds=12.0):
+    """The oracle on the host cores: a bounded sample of the same workload."""
+    import oracle
+    from leswht_gb300 import solver
+    case = make_case(name, form)
+    lib = oracle.load()
+    s = solver.Solver(lib, "ref_", case)
+    s.step()                                   # warm-up (page-in, first touch)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        s.step()
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or n >= 200:
+            break
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": case.cells * n / el / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n} steps of {case.name} after 1 warm-up step ({el:.1f} s), C/OpenMP oracle",
+            "steps": n, "seconds": el}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import oracle
+    from leswht_gb300 import solver
+    case = make_case(args.config, args.form)
+    lib = oracle.load()
+    s = solver.Solver(lib, "ref_", case)
+    for _ in range(args.warmup):
+        s.step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.step()
+    el = time.perf_counter() - t0
+    v = case.cells * args.steps / el / 1e6
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded PCG64 perturbation of the laminar profile)",
+            "config": {"workload": WORKLOAD[args.config], "cells": case.cells, "form": "fp64 CPU"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} timed steps of {case.name} after {args.warmup} warm-up, "
+                                       "C/OpenMP restatement of the reference solver (the Fortran reference "
+                                       "cannot be compiled: no Fortran compiler on the host)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import leswht_gb300
+    from leswht_gb300 import abi
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world != args.gpus and world > 1:
+        print(f"warning: WORLD_SIZE={world} but --gpus {args.gpus}", file=sys.stderr)
+    dev = local if torch.cuda.device_count() > local else 0
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+    lib = leswht_gb300.load_library()
+    if lib.lesgpu_set_device(dev) != 0:
+        raise RuntimeError("lesgpu_set_device failed")
+    case = make_case(args.config, args.form)
+    s = leswht_gb300.gpu_solver(case)
+    h = s.h
+    stream_ptr = C.c_void_p()
+    lib.lesgpu_stream(h, C.byref(stream_ptr))
+    stream = torch.cuda.ExternalStream(stream_ptr.value, device=torch.device("cuda", dev))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+
+    def check(rc, what):
+        if rc != 0:
+            raise RuntimeError(f"{what}: {lib.lesgpu_strerror(rc).decode()}")
+
+    # warm-up (captures the step graph)
+    for _ in range(args.warmup):
+        check(lib.lesgpu_step_async(h, 1), "step")
+    torch.cuda.synchronize()
+    kps = C.c_int64()
+    check(lib.lesgpu_launch_count(h, C.byref(kps)), "launch_count")
+
+    # ---- device-resident timed region
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    with Clocks(dev) as clk:
+        with torch.cuda.stream(stream):
+            for q in range(args.steps):
+                flush.zero_()
+                ev[q][0].record(stream)
+                check(lib.lesgpu_step_async(h, 1), "step")
+                ev[q][1].record(stream)
+        torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    tot_s = sum(step_ms) / 1e3
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([tot_s], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_s = float(t.item())
+    rep = s.report()
+    value = world * case.cells * args.steps / tot_s / 1e6
+
+    # ---- live per-kernel-class timing (instrumented eager steps)
+    kstats = {}
+    if rank == 0:
+        for cls in (1, 2, 4, 5):
+            check(lib.lesgpu_instrument(h, cls), "instrument")
+            with torch.cuda.stream(stream):
+                for q in range(max(2, min(args.steps, 5))):
+                    flush.zero_()
+                    check(lib.lesgpu_step_async(h, 1), "step")
+            ms, n = C.c_double(), C.c_int64()
+            check(lib.lesgpu_instrument_read(h, C.byref(ms), C.byref(n)), "instrument_read")
+            kstats[KCLASS[cls]] = {"ms_total": ms.value, "launches": n.value,
+                                   "avg_us": ms.value / max(n.value, 1) * 1e3, "cls": cls}
+        check(lib.lesgpu_instrument(h, 0), "instrument")
+    roofline = None
+    if kstats:
+        peak, src = peaks()
+        dom = max(kstats.values(), key=lambda d: d["ms_total"])
+        words = KWORDS[dom["cls"]]
+        bytes_per_launch = words * 8.0 * case.cells
+        achieved = bytes_per_launch / (dom["avg_us"] * 1e-6) / 1e9
+        for k, d in kstats.items():
+            w = KWORDS.get(d["cls"])
+            if w:
+                d["achieved_gbs"] = w * 8.0 * case.cells / (d["avg_us"] * 1e-6) / 1e9
+        name = [k for k, d in kstats.items() if d is dom][0]
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "traffic": None, "kernel": name, "peak_source": src,
+                    "algorithmic_bytes_per_launch": bytes_per_launch,
+                    "avg_launch_us": dom["avg_us"], "kernels": kstats}
+
+    # ---- end to end through the C ABI with host buffers
+    e2e = None
+    if rank == 0:
+        shape = case.grid.shape
+        host = {k: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy() for k in ("u", "v", "w", "p", "t")}
+        f0 = s.fields()
+        for k in host:
+            host[k][...] = f0[k]
+        r0 = s.report()
+        tm, dt, ih, m = r0["time"], r0["dt"], r0["ihist"], r0["m"]
+        ptr = lambda a: a.ctypes.data_as(abi.PD)
+        rep_s = abi.StepReport()
+        n_e2e = max(3, min(args.steps, 20))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            check(lib.lesgpu_set_fields(h, *(ptr(host[k]) for k in ("u", "v", "w", "p", "t")), tm, dt, ih, m), "set_fields")
+            check(lib.lesgpu_step(h, C.byref(rep_s)), "step")
+            check(lib.lesgpu_get_fields(h, *(ptr(host[k]) for k in ("u", "v", "w", "p", "t"))), "get_fields")
+            tm, dt, ih, m = rep_s.time, rep_s.dt, rep_s.ihist, rep_s.m
+        el = time.perf_counter() - t0
+        nbytes = 5 * int(np.prod(shape)) * 8
+        e2e = {"value": case.cells * n_e2e / el / 1e6, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes + C.sizeof(abi.StepReport), "steps": n_e2e,
+               "path": "lesgpu_set_fields + lesgpu_step + lesgpu_get_fields, pinned host buffers"}
+
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu:
+            cpu = cpu_baseline(args.config, args.form, seconds=args.cpu_seconds)
+        clocks = clk.summary()
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": tot_s / args.steps * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.form == "fp64" else "f32/f64",
+                "data": "synthetic (seeded PCG64 perturbation of the laminar profile)",
+                "config": {"workload": WORKLOAD[args.config], "cells": case.cells, "form": args.form,
+                           "l2": "flushed between timed steps (256 MiB write, outside the timed region)",
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": int(kps.value) * args.steps, "kernels_per_step": int(kps.value),
+                "clocks": clocks,
+                "check": {"dvmax": rep["dvmax"], "ubulk": rep["ubulk"], "csgsts": rep["csgsts"],
+                          "time": rep["time"], "dt": rep["dt"]},
+                "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)}}
+        print(json.dumps(line))
+    s.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", default="channel64", choices=sorted(WORKLOAD))
+    ap.add_argument("--form", default="fp64", choices=["fp64"])
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -241,6 +241,26 @@ int lesgpu_step_async(lesgpu_case *c, int64_t n);
 int lesgpu_stream(lesgpu_case *c, void **stream);
 int lesgpu_use_graph(lesgpu_case *c, int on);
 
+/* Kernel launches one step makes (counted from the captured step graph). */
+int lesgpu_launch_count(lesgpu_case *c, int64_t *kernels_per_step);
+
+/* Event instrumentation of one kernel class for roofline measurements:
+ * lesgpu_instrument(c, cls) makes the following steps run without the graph
+ * and brackets every launch of class `cls` (LESGPU_K_*) with CUDA events on
+ * the case's stream; lesgpu_instrument_read returns the summed device time
+ * (ms) and the number of launches since the call, and cls = 0 switches the
+ * instrumentation off. */
+#define LESGPU_K_RHS      1   /* fused rhs + rhssgs (momentum)          */
+#define LESGPU_K_ADI      2   /* tridiagonal sweeps, momentum and T     */
+#define LESGPU_K_SGS      3   /* SGS passes and test filters            */
+#define LESGPU_K_POISSON  4   /* FFT + y-Thomas Poisson solve           */
+#define LESGPU_K_RHS_T    5   /* rhs_t                                  */
+int lesgpu_instrument(lesgpu_case *c, int64_t cls);
+/* Select the CUDA device used by the cases this thread creates next
+ * (one process per GPU when several GPUs run replicas). */
+int lesgpu_set_device(int64_t device);
+int lesgpu_instrument_read(lesgpu_case *c, double *ms, int64_t *launches);
+
 int lesgpu_destroy(lesgpu_case *c);
 const char *lesgpu_strerror(int code);
 int lesgpu_abi_version(void);

@@ -37,6 +37,14 @@ def load_library(rebuild: bool = False) -> C.CDLL:
     lib.lesgpu_strerror.argtypes = [C.c_int]
     lib.lesgpu_strerror.restype = C.c_char_p
     lib.lesgpu_abi_version.restype = C.c_int
+    lib.lesgpu_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+    lib.lesgpu_launch_count.restype = C.c_int
+    lib.lesgpu_instrument.argtypes = [C.c_void_p, C.c_int64]
+    lib.lesgpu_instrument.restype = C.c_int
+    lib.lesgpu_instrument_read.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    lib.lesgpu_instrument_read.restype = C.c_int
+    lib.lesgpu_set_device.argtypes = [C.c_int64]
+    lib.lesgpu_set_device.restype = C.c_int
     _LIB = lib
     return lib
 

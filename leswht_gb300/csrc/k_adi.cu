@@ -195,7 +195,9 @@ static void adi_launch(lesgpu_case *c, const AdiArgs &A) {
     long long nl = (long long)(A.a1 - A.a0 + 1) * (A.b1 - A.b0 + 1);
     if (nl <= 0 || A.l2 < A.l1) return;
     int nb = (int)((nl + 127) / 128);
+    inst_begin(c, LESGPU_K_ADI);
     k_adi<<<nb, 128, 0, c->stream>>>(c->kp, A);
+    inst_end(c, LESGPU_K_ADI);
 }
 
 // One component: z sweep in place on rhs1, y sweep into scratch G, x sweep

@@ -342,12 +342,14 @@ void launch_poisson(lesgpu_case *c) {
     size_t smz = (size_t)2 * g.n3m * Lz * sizeof(double2), smx = (size_t)2 * g.n1m * Lx * sizeof(double2);
     dim3 gz((g.n1m + Lz - 1) / Lz, g.n2m);
     int nxl = g.n3mh * g.n2m;
+    inst_begin(c, LESGPU_K_POISSON);
     k_fft_z_fwd<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz);
     k_fft_x<<<(nxl + Lx - 1) / Lx, kThreads, smx, c->stream>>>(P.ccap, nxl, px, Lx, 0);
     long long nl = (long long)g.n1m * g.n3mh;
     k_ytri<<<blocks_for(nl, 128), 128, 0, c->stream>>>(c->kp, P.ccap, P.ak1, P.ak3, c->kp.f.scr[0]);
     k_fft_x<<<(nxl + Lx - 1) / Lx, kThreads, smx, c->stream>>>(P.ccap, nxl, px, Lx, 1);
     k_fft_z_inv<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz);
+    inst_end(c, LESGPU_K_POISSON);
 }
 
 }  // namespace lg

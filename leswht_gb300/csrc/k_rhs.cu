@@ -157,7 +157,9 @@ void launch_rhs(lesgpu_case *c, int msub) {
     const double ro[4] = {0.0, 0.0, -17.0 / 60.0, -5.0 / 12.0};
     const DGrid &g = c->kp.g;
     Box b{1, 1, 1, g.n1m, g.n2m, g.n3m};
+    inst_begin(c, LESGPU_K_RHS);
     k_rhs<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, gam[msub], ro[msub]);
+    inst_end(c, LESGPU_K_RHS);
 }
 
 // ------------------------------------------------------------------- divgs
@@ -306,7 +308,9 @@ void launch_rhs_t_kernel(lesgpu_case *c, int msub) {
     const double ro[4] = {0.0, 0.0, -17.0 / 60.0, -5.0 / 12.0};
     const DGrid &g = c->kp.g;
     Box b{1, 1, 1, g.n1m, g.n2m, g.n3m};
+    inst_begin(c, LESGPU_K_RHS_T);
     k_rhs_t<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, gam[msub], ro[msub]);
+    inst_end(c, LESGPU_K_RHS_T);
 }
 
 }  // namespace lg

@@ -195,7 +195,9 @@ __global__ void __launch_bounds__(kThreads) k_filter(KP p, Box b, FiltBatch F) {
 static void filter_batch(lesgpu_case *c, FiltBatch &F) {
     const DGrid &g = c->kp.g;
     Box b{1, 1, 1, g.n1m, g.n2m, g.n3m};
+    inst_begin(c, LESGPU_K_SGS);
     k_filter<<<blocks_for(b.count() * F.na), kThreads, 0, c->stream>>>(c->kp, b, F);
+    inst_end(c, LESGPU_K_SGS);
 }
 
 // pass 2 of sgs_dvmg (:504-580): filtered gradients -> test-level Vreman

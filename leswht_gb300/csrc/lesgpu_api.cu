@@ -427,6 +427,29 @@ static void enqueue_step(lesgpu_case *c, bool first) {
     launch_bulk_diag(c);
 }
 
+// Capture one steady-state step into a CUDA graph and count its kernels.
+static int capture_step(lesgpu_case *c) {
+    cudaGraph_t gr;
+    if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return LESGPU_ERR_CUDA;
+    enqueue_step(c, false);
+    if (cudaStreamEndCapture(c->stream, &gr) != cudaSuccess) return LESGPU_ERR_CUDA;
+    size_t nn = 0;
+    cudaGraphGetNodes(gr, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (nn) cudaGraphGetNodes(gr, nodes.data(), &nn);
+    long long nk = 0;
+    for (size_t q = 0; q < nn; q++) {
+        cudaGraphNodeType t;
+        cudaGraphNodeGetType(nodes[q], &t);
+        if (t == cudaGraphNodeTypeKernel) nk++;
+    }
+    c->kernels_per_step = nk;
+    if (cudaGraphInstantiate(&c->graph, gr, 0) != cudaSuccess) { cudaGraphDestroy(gr); return LESGPU_ERR_CUDA; }
+    cudaGraphDestroy(gr);
+    c->graph_ok = 1;
+    return 0;
+}
+
 static void fill_report(const lesgpu_case *c, const DScal &s, lesgpu_step_report *r) {
     memset(r, 0, sizeof(*r));
     r->ntime = s.ntime; r->ihist = s.ihist; r->m = s.m;
@@ -446,15 +469,10 @@ extern "C" int lesgpu_step(lesgpu_case *c, lesgpu_step_report *rep) {
     if (!c->started) return LESGPU_ERR_STATE;
     c->ntime_host += 1;
     bool first = (c->cfg.iread == 0 && c->ntime_host == 1);
-    if (c->use_graph && !first) {
+    if (c->use_graph && !first && c->inst_cls == 0) {
         if (!c->graph_ok) {
-            cudaGraph_t gr;
-            if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return LESGPU_ERR_CUDA;
-            enqueue_step(c, false);
-            if (cudaStreamEndCapture(c->stream, &gr) != cudaSuccess) return LESGPU_ERR_CUDA;
-            if (cudaGraphInstantiate(&c->graph, gr, 0) != cudaSuccess) { cudaGraphDestroy(gr); return LESGPU_ERR_CUDA; }
-            cudaGraphDestroy(gr);
-            c->graph_ok = 1;
+            int rc = capture_step(c);
+            if (rc) return rc;
         }
         if (cudaGraphLaunch(c->graph, c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
     } else {
@@ -476,15 +494,10 @@ extern "C" int lesgpu_step_async(lesgpu_case *c, int64_t n) {
     for (int64_t s = 0; s < n; s++) {
         c->ntime_host += 1;
         bool first = (c->cfg.iread == 0 && c->ntime_host == 1);
-        if (c->use_graph && !first) {
+        if (c->use_graph && !first && c->inst_cls == 0) {
             if (!c->graph_ok) {
-                cudaGraph_t gr;
-                if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return LESGPU_ERR_CUDA;
-                enqueue_step(c, false);
-                if (cudaStreamEndCapture(c->stream, &gr) != cudaSuccess) return LESGPU_ERR_CUDA;
-                if (cudaGraphInstantiate(&c->graph, gr, 0) != cudaSuccess) { cudaGraphDestroy(gr); return LESGPU_ERR_CUDA; }
-                cudaGraphDestroy(gr);
-                c->graph_ok = 1;
+                int rc = capture_step(c);
+                if (rc) return rc;
             }
             if (cudaGraphLaunch(c->graph, c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
         } else {
@@ -503,6 +516,43 @@ extern "C" int lesgpu_stream(lesgpu_case *c, void **stream) {
 extern "C" int lesgpu_use_graph(lesgpu_case *c, int on) {
     if (!c) return LESGPU_ERR_ARG;
     c->use_graph = on ? 1 : 0;
+    return 0;
+}
+
+extern "C" int lesgpu_launch_count(lesgpu_case *c, int64_t *kernels_per_step) {
+    if (!c || !kernels_per_step) return LESGPU_ERR_ARG;
+    if (!c->graph_ok) {
+        if (!c->started) return LESGPU_ERR_STATE;
+        int rc = capture_step(c);
+        if (rc) return rc;
+    }
+    *kernels_per_step = c->kernels_per_step;
+    return 0;
+}
+
+extern "C" int lesgpu_instrument(lesgpu_case *c, int64_t cls) {
+    if (!c || cls < 0 || cls > 5) return LESGPU_ERR_ARG;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
+    if (cls != 0 && c->inst_ev[0] == nullptr)
+        for (int q = 0; q < 2 * 4096; q++)
+            if (cudaEventCreate(&c->inst_ev[q]) != cudaSuccess) return LESGPU_ERR_CUDA;
+    c->inst_cls = (int)cls;
+    c->inst_n = 0;
+    return 0;
+}
+
+extern "C" int lesgpu_instrument_read(lesgpu_case *c, double *ms, int64_t *launches) {
+    if (!c || !ms || !launches) return LESGPU_ERR_ARG;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
+    double tot = 0.0;
+    for (int q = 0; q < c->inst_n; q++) {
+        float m = 0.f;
+        if (cudaEventElapsedTime(&m, c->inst_ev[2 * q], c->inst_ev[2 * q + 1]) != cudaSuccess) return LESGPU_ERR_CUDA;
+        tot += m;
+    }
+    *ms = tot;
+    *launches = c->inst_n;
+    c->inst_n = 0;
     return 0;
 }
 
@@ -602,6 +652,8 @@ extern "C" int lesgpu_destroy(lesgpu_case *c) {
     if (!c) return 0;
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->graph_ok) cudaGraphExecDestroy(c->graph);
+    if (c->inst_ev[0])
+        for (int q = 0; q < 2 * 4096; q++) cudaEventDestroy(c->inst_ev[q]);
     poisson_free(c);
     CaseExtra *X = (CaseExtra *)c->dmem_pool;
     if (X) {
@@ -631,3 +683,8 @@ extern "C" const char *lesgpu_strerror(int code) {
 }
 
 extern "C" int lesgpu_abi_version(void) { return LESGPU_ABI_VERSION; }
+
+extern "C" int lesgpu_set_device(int64_t device) {
+    if (device < 0) return LESGPU_ERR_ARG;
+    return cuda_rc(cudaSetDevice((int)device));
+}

@@ -201,7 +201,25 @@ struct lesgpu_case {
     int use_graph;
     // host mirrors of metrics used for init-time tables
     double *h_f2fx, *h_f2fy, *h_f2fz;
+    // kernel launches per step (from the captured graph)
+    long long kernels_per_step;
+    // event instrumentation of one kernel class (lesgpu_instrument)
+    int inst_cls;
+    int inst_n;
+    cudaEvent_t inst_ev[2 * 4096];
+    double inst_ms;
+    long long inst_launches;
 };
+
+namespace lg {
+// bracket a launch of class `cls` with events when that class is instrumented
+inline void inst_begin(lesgpu_case *c, int cls) {
+    if (c->inst_cls == cls && c->inst_n < 4096) cudaEventRecord(c->inst_ev[2 * c->inst_n], c->stream);
+}
+inline void inst_end(lesgpu_case *c, int cls) {
+    if (c->inst_cls == cls && c->inst_n < 4096) { cudaEventRecord(c->inst_ev[2 * c->inst_n + 1], c->stream); c->inst_n++; }
+}
+}  // namespace lg
 
 namespace lg {
 // launch wrappers implemented in the k_*.cu files
