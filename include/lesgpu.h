@@ -43,6 +43,8 @@ extern "C" {
 #define LESGPU_ERR_NAN          (-6)  /* non-finite value detected in the state     */
 #define LESGPU_ERR_STATE        (-7)  /* call out of order (e.g. step before start) */
 #define LESGPU_ERR_UNSUPPORTED  (-8)  /* option valid in the reference, not built    */
+#define LESGPU_ERR_TOO_LARGE    (-9)  /* grid exceeds the fixed scratch of the
+                                         allocation-free entry point              */
 
 /* ---- option values ---------------------------------------------------- */
 /* Poisson solver: chosen at link time in the reference (02_solver/Makefile:23-34). */
@@ -260,6 +262,27 @@ int lesgpu_instrument(lesgpu_case *c, int64_t cls);
  * (one process per GPU when several GPUs run replicas). */
 int lesgpu_set_device(int64_t device);
 int lesgpu_instrument_read(lesgpu_case *c, double *ms, int64_t *launches);
+
+/* Allocation-free pressure Poisson solve.  No counterpart in the reference:
+ * it serves callers that cannot call cudaMalloc (a runtime that hands out
+ * device memory only from its own pool, a real-time loop that must not enter
+ * the driver's allocator, a plugin that must not bypass its host's
+ * allocator).  It runs the poiss_ftft solve of a case -- FFT in x and z,
+ * Thomas in y, the (1,1) mode pinned -- on caller-owned DEVICE buffers
+ * divgsum (input) and phi (output, interior written), both in the
+ * (0:n1,0:n2,0:n3) layout, on `stream` (a cudaStream_t, or NULL), and keeps
+ * all its temporaries in one fixed 32 MiB device array per GPU.  The grid
+ * (x and z periodic, uniform) is read from host memory.
+ *   - It calls no cudaMalloc/cudaFree; grids needing more than the fixed
+ *     array (24*n1m*(n3m/2+1)*n2m bytes plus tables, about 128^3 at most,
+ *     and at most 1024 cells per direction) return LESGPU_ERR_TOO_LARGE.
+ *   - The first call on a device sets it up (resolves the array's device
+ *     address); make that first call before any stream capture.
+ *   - All calls on a device share the array and leave their contents in it;
+ *     calls that overlap on the GPU race with each other -- serialise them.
+ *   - Returns after enqueueing; synchronise `stream` before reading phi. */
+int lesgpu_poisson_ftft_noalloc(const lesgpu_grid *grid, const double *d_divgsum,
+                                double *d_phi, void *stream);
 
 int lesgpu_destroy(lesgpu_case *c);
 const char *lesgpu_strerror(int code);

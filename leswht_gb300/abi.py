@@ -22,8 +22,10 @@ PI = C.POINTER(C.c_int64)
 OK = 0
 ERR_ARG, ERR_CONFIG, ERR_CUDA, ERR_OOM, ERR_NOT_CONVERGED, ERR_NAN, ERR_STATE, ERR_UNSUPPORTED = (
     -1, -2, -3, -4, -5, -6, -7, -8)
+ERR_TOO_LARGE = -9
 ERR_NAMES = {0: "OK", -1: "ERR_ARG", -2: "ERR_CONFIG", -3: "ERR_CUDA", -4: "ERR_OOM",
-             -5: "ERR_NOT_CONVERGED", -6: "ERR_NAN", -7: "ERR_STATE", -8: "ERR_UNSUPPORTED"}
+             -5: "ERR_NOT_CONVERGED", -6: "ERR_NAN", -7: "ERR_STATE", -8: "ERR_UNSUPPORTED",
+             -9: "ERR_TOO_LARGE"}
 
 POISSON_FTFT, POISSON_Z_FT, POISSON_MGRD = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1

@@ -17,7 +17,7 @@
 //                 with the (1,1) mode pinned as poiss_ftft.f90:93-112
 //   k_fft_x     : inverse x transform
 //   k_fft_z_inv : conjugate-symmetric completion, inverse z, real part -> phi
-#include "lesgpu_internal.cuh"
+#include "k_fft.cuh"
 #include <math.h>
 #include <stdlib.h>
 
@@ -28,12 +28,6 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 }
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
-
-struct DevPlan {
-    int n, nst;
-    int rad[24];
-    const double2 *tw;
-};
 
 // Run all stages on L interleaved lines; returns the buffer holding the result.
 __device__ double2 *block_fft(double2 *b0, double2 *b1, int L, const DevPlan &P, int inv) {
@@ -286,6 +280,8 @@ static int lines_per_block(int n) {
     while (L > 1 && (size_t)2 * n * L * sizeof(double2) > 200 * 1024) L >>= 1;
     return L;
 }
+
+int fft_lines_per_block(int n) { return lines_per_block(n); }
 
 // poisinit, poiss_ftft.f90:164-204
 int poisson_init(lesgpu_case *c) {

@@ -1,0 +1,20 @@
+// Declarations of the FFT / poiss_ftft kernels of k_fft.cu, shared with the
+// allocation-free entry point of noalloc.cu.
+#pragma once
+#include "lesgpu_internal.cuh"
+
+namespace lg {
+
+struct DevPlan {
+    int n, nst;
+    int rad[24];
+    const double2 *tw;
+};
+
+__global__ void k_fft_z_fwd(KP p, double2 *ccap, DevPlan P, int L);
+__global__ void k_fft_z_inv(KP p, const double2 *ccap, DevPlan P, int L);
+__global__ void k_fft_x(double2 *ccap, int nlines, DevPlan P, int L, int inv);
+__global__ void k_ytri(KP p, double2 *ccap, const double *ak1, const double *ak3, double *gam);
+int fft_lines_per_block(int n);
+
+}  // namespace lg

@@ -678,6 +678,7 @@ extern "C" const char *lesgpu_strerror(int code) {
     case LESGPU_ERR_NAN: return "non-finite value in the solver state";
     case LESGPU_ERR_STATE: return "call out of order";
     case LESGPU_ERR_UNSUPPORTED: return "option not built in this library";
+    case LESGPU_ERR_TOO_LARGE: return "grid exceeds the fixed scratch of the allocation-free entry point";
     default: return "unknown error";
     }
 }
