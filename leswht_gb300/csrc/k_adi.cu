@@ -78,131 +78,217 @@ __device__ __forceinline__ void adi_coef(const KP &p, int comp, int dir, int i, 
     }
 }
 
-__global__ void __launch_bounds__(128) k_adi(KP p, AdiArgs A) {
+// Elements per chunk: a thread issues the loads of CH consecutive line
+// elements before it runs the (serial) recurrence over them, so CH loads are
+// in flight instead of one.  Stores of a chunk follow all its loads, which
+// keeps in-place sweeps (src == dst) correct.
+constexpr int CH = 8;
+
+struct AdiBatch {
+    AdiArgs a[3];
+};
+
+__global__ void __launch_bounds__(64) k_adi(KP p, AdiBatch B) {
+    const AdiArgs &A = B.a[blockIdx.y];
     const DGrid &g = p.g;
     const double diag = (A.comp == CT) ? p.S->acoefi * p.c.pr : p.S->acoefi;
     int na = A.a1 - A.a0 + 1, nb = A.b1 - A.b0 + 1;
     long long nl = (long long)na * nb;
-    long long stride = A.dir == 2 ? g.sxy : A.dir == 1 ? g.sx : 1;
+    const long long stride = A.dir == 2 ? g.sxy : A.dir == 1 ? g.sx : 1;
+    const int nline = A.l2 - A.l1 + 1;
+    if (nl <= 0 || A.l2 < A.l1) return;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nl; t += (long long)gridDim.x * blockDim.x) {
-        int x0 = A.a0 + (int)(t % na), x1 = A.b0 + (int)(t / na);
-        int i, j, k;
-        line_coords(A.dir, A.l1, x0, x1, i, j, k);
-        long long q0 = g.ix(i, j, k);
+        const int x0 = A.a0 + (int)(t % na), x1 = A.b0 + (int)(t / na);
+        int i0, j0, k0;
+        line_coords(A.dir, A.l1, x0, x1, i0, j0, k0);
+        const long long q0 = g.ix(i0, j0, k0);
         if (!A.periodic) {
-            // ---- trdiag: forward elimination
-            double a, c;
-            adi_coef(p, A.comp, A.dir, i, j, k, a, c);
-            double b = diag - a - c;
-            double bet = 1.0 / b;
-            double x = diag * A.src[q0] * bet;
-            double cprev = c;
-            double *out = A.add ? A.gam + 0 : A.dst;   // solution holder during the sweep
-            // when adding to the field the provisional solution lives in sarr
-            if (A.add) out = A.sarr;
-            out[q0] = x;
-            long long q = q0;
-            for (int l = A.l1 + 1; l <= A.l2; l++) {
-                q += stride;
-                line_coords(A.dir, l, x0, x1, i, j, k);
-                adi_coef(p, A.comp, A.dir, i, j, k, a, c);
-                b = diag - a - c;
-                double gm = cprev * bet;
-                bet = 1.0 / (b - a * gm);
-                x = (diag * A.src[q] - a * x) * bet;
-                A.gam[q] = gm;
-                out[q] = x;
-                cprev = c;
+            // ---- trdiag: forward elimination, chunk by chunk
+            double *out = A.add ? A.sarr : A.dst;    // provisional solution
+            double bet = 0.0, x = 0.0, cprev = 0.0;
+            for (int c0 = 0; c0 < nline; c0 += CH) {
+                double av[CH], cv[CH], rv[CH];
+#pragma unroll
+                for (int u = 0; u < CH; u++) {
+                    if (c0 + u < nline) {
+                        int i, j, k;
+                        line_coords(A.dir, A.l1 + c0 + u, x0, x1, i, j, k);
+                        adi_coef(p, A.comp, A.dir, i, j, k, av[u], cv[u]);
+                        rv[u] = A.src[q0 + (long long)(c0 + u) * stride];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < CH; u++) {
+                    if (c0 + u < nline) {
+                        const long long q = q0 + (long long)(c0 + u) * stride;
+                        const double a = av[u], c = cv[u];
+                        const double b = diag - a - c;
+                        if (c0 + u == 0) {
+                            bet = 1.0 / b;
+                            x = diag * rv[u] * bet;
+                        } else {
+                            const double gm = cprev * bet;
+                            bet = 1.0 / (b - a * gm);
+                            x = (diag * rv[u] - a * x) * bet;
+                            A.gam[q] = gm;
+                        }
+                        out[q] = x;
+                        cprev = c;
+                    }
+                }
             }
-            // ---- back substitution
+            // ---- back substitution, chunk by chunk from the end
             double xn = x;
-            if (A.add) A.dst[q] += xn;
-            for (int l = A.l2 - 1; l >= A.l1; l--) {
-                long long qn = q;
-                q -= stride;
-                double xl = out[q] - A.gam[qn] * xn;
-                if (A.add) A.dst[q] += xl;
-                else out[q] = xl;
-                xn = xl;
+            const long long qlast = q0 + (long long)(nline - 1) * stride;
+            if (A.add) A.dst[qlast] += xn;
+            for (int c1 = nline - 2; c1 >= 0; c1 -= CH) {
+                double ov[CH], gv[CH], fv[CH];
+#pragma unroll
+                for (int u = 0; u < CH; u++) {
+                    const int l = c1 - u;
+                    if (l >= 0) {
+                        const long long q = q0 + (long long)l * stride;
+                        ov[u] = out[q];
+                        gv[u] = A.gam[q + stride];
+                        if (A.add) fv[u] = A.dst[q];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < CH; u++) {
+                    const int l = c1 - u;
+                    if (l >= 0) {
+                        const long long q = q0 + (long long)l * stride;
+                        const double xl = ov[u] - gv[u] * xn;
+                        if (A.add) A.dst[q] = fv[u] + xl;
+                        else out[q] = xl;
+                        xn = xl;
+                    }
+                }
             }
         } else {
-            // ---- trdiagp: forward sweep (q in gam, s in sarr, f in dst/work)
-            double *f = A.add ? nullptr : A.dst;
-            double a, c;
-            adi_coef(p, A.comp, A.dir, i, j, k, a, c);
-            double b = diag - a - c;
-            long long q = q0;
-            long long qn_last = q0 + (long long)(A.l2 - A.l1) * stride;
-            double fn;
-            {
-                // original right-hand side at the last element
-                fn = diag * A.src[qn_last];
-            }
-            double binv = 1.0 / b;
-            double qq = -c * binv, ss = -a * binv;
-            double ff = diag * A.src[q0] * binv;
-            // when adding to the field, the f/qe vector lives in a private
-            // region of dst's companion: reuse the src array only if it is a
-            // scratch (x sweeps read the y-sweep result G, which is private)
-            double *fw = A.add ? (double *)A.src : f;
-            A.gam[q] = qq;
-            A.sarr[q] = ss;
-            fw[q] = ff;
+            // ---- trdiagp: forward sweep; q factors in gam, s in sarr, f in fw
+            double *fw = A.add ? (double *)A.src : A.dst;
+            const long long qn_last = q0 + (long long)(nline - 1) * stride;
+            const double fn = diag * A.src[qn_last];   // original right-hand side at the last element
+            double qq = 0.0, ss = 0.0, ff = 0.0;
             double a_last = 0.0, b_last = 0.0, c_last = 0.0;
-            for (int l = A.l1 + 1; l <= A.l2; l++) {
-                q += stride;
-                line_coords(A.dir, l, x0, x1, i, j, k);
-                adi_coef(p, A.comp, A.dir, i, j, k, a, c);
-                b = diag - a - c;
-                double pn = 1.0 / (b + a * qq);
-                double qn = -c * pn;
-                double sn = -a * ss * pn;
-                double fnw = (diag * A.src[q] - a * ff) * pn;
-                qq = qn; ss = sn; ff = fnw;
-                A.gam[q] = qq;
-                A.sarr[q] = ss;
-                fw[q] = ff;
-                a_last = a; b_last = b; c_last = c;
+            for (int c0 = 0; c0 < nline; c0 += CH) {
+                double av[CH], cv[CH], rv[CH];
+#pragma unroll
+                for (int u = 0; u < CH; u++) {
+                    if (c0 + u < nline) {
+                        int i, j, k;
+                        line_coords(A.dir, A.l1 + c0 + u, x0, x1, i, j, k);
+                        adi_coef(p, A.comp, A.dir, i, j, k, av[u], cv[u]);
+                        rv[u] = A.src[q0 + (long long)(c0 + u) * stride];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < CH; u++) {
+                    if (c0 + u < nline) {
+                        const long long q = q0 + (long long)(c0 + u) * stride;
+                        const double a = av[u], c = cv[u];
+                        const double b = diag - a - c;
+                        if (c0 + u == 0) {
+                            const double binv = 1.0 / b;
+                            qq = -c * binv;
+                            ss = -a * binv;
+                            ff = diag * rv[u] * binv;
+                        } else {
+                            const double pn = 1.0 / (b + a * qq);
+                            const double qn = -c * pn;
+                            const double sn = -a * ss * pn;
+                            ff = (diag * rv[u] - a * ff) * pn;
+                            qq = qn;
+                            ss = sn;
+                        }
+                        A.gam[q] = qq;
+                        A.sarr[q] = ss;
+                        fw[q] = ff;
+                        a_last = a; b_last = b; c_last = c;
+                    }
+                }
             }
             // backward pass: s(j) += q(j) s(j+1); qe(j) = f(j) + q(j) qe(j+1)
-            double s_next = 1.0, qe_next = 0.0;
-            double s_j2m1 = 0.0, qe_j2m1 = 0.0;
-            long long qe_pos = qn_last;
-            for (int l = A.l2 - 1; l >= A.l1; l--) {
-                qe_pos -= stride;
-                double qj = A.gam[qe_pos];
-                double sj = A.sarr[qe_pos] + qj * s_next;
-                double qej = fw[qe_pos] + qj * qe_next;
-                A.sarr[qe_pos] = sj;
-                fw[qe_pos] = qej;
-                if (l == A.l2 - 1) { s_j2m1 = sj; qe_j2m1 = qej; }
-                s_next = sj; qe_next = qej;
+            double s_next = 1.0, qe_next = 0.0, s_j2m1 = 0.0, qe_j2m1 = 0.0;
+            for (int c1 = nline - 2; c1 >= 0; c1 -= CH) {
+                double qv[CH], sv[CH], fv[CH];
+#pragma unroll
+                for (int u = 0; u < CH; u++) {
+                    const int l = c1 - u;
+                    if (l >= 0) {
+                        const long long q = q0 + (long long)l * stride;
+                        qv[u] = A.gam[q];
+                        sv[u] = A.sarr[q];
+                        fv[u] = fw[q];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < CH; u++) {
+                    const int l = c1 - u;
+                    if (l >= 0) {
+                        const long long q = q0 + (long long)l * stride;
+                        const double sj = sv[u] + qv[u] * s_next;
+                        const double qej = fv[u] + qv[u] * qe_next;
+                        A.sarr[q] = sj;
+                        fw[q] = qej;
+                        if (l == nline - 2) { s_j2m1 = sj; qe_j2m1 = qej; }
+                        s_next = sj;
+                        qe_next = qej;
+                    }
+                }
             }
-            double s_j1 = s_next, qe_j1 = qe_next;
-            double fj2 = (fn - c_last * qe_j1 - a_last * qe_j2m1) / (c_last * s_j1 + a_last * s_j2m1 + b_last);
+            const double s_j1 = s_next, qe_j1 = qe_next;
+            const double fj2 = (fn - c_last * qe_j1 - a_last * qe_j2m1) / (c_last * s_j1 + a_last * s_j2m1 + b_last);
             if (A.add) A.dst[qn_last] += fj2; else fw[qn_last] = fj2;
-            long long qp = qn_last;
-            for (int l = A.l2 - 1; l >= A.l1; l--) {
-                qp -= stride;
-                double val = fj2 * A.sarr[qp] + fw[qp];
-                if (A.add) A.dst[qp] += val; else fw[qp] = val;
+            for (int c1 = nline - 2; c1 >= 0; c1 -= CH) {
+                double sv[CH], ev[CH], dv[CH];
+#pragma unroll
+                for (int u = 0; u < CH; u++) {
+                    const int l = c1 - u;
+                    if (l >= 0) {
+                        const long long q = q0 + (long long)l * stride;
+                        sv[u] = A.sarr[q];
+                        ev[u] = fw[q];
+                        if (A.add) dv[u] = A.dst[q];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < CH; u++) {
+                    const int l = c1 - u;
+                    if (l >= 0) {
+                        const long long q = q0 + (long long)l * stride;
+                        const double val = fj2 * sv[u] + ev[u];
+                        if (A.add) A.dst[q] = dv[u] + val; else fw[q] = val;
+                    }
+                }
             }
         }
     }
 }
 
-static void adi_launch(lesgpu_case *c, const AdiArgs &A) {
-    long long nl = (long long)(A.a1 - A.a0 + 1) * (A.b1 - A.b0 + 1);
-    if (nl <= 0 || A.l2 < A.l1) return;
-    int nb = (int)((nl + 127) / 128);
+// One launch sweeps the same direction for up to three components at once
+// (blockIdx.y = component): the u, v and w solves of lhsu/lhsv/lhsw are
+// independent of each other, and three times the lines keep three times as
+// many FP64 pipes busy on small grids.
+static void adi_launch(lesgpu_case *c, const AdiBatch &B, int ncomp) {
+    long long mx = 0;
+    for (int q = 0; q < ncomp; q++) {
+        const AdiArgs &A = B.a[q];
+        long long nl = (long long)(A.a1 - A.a0 + 1) * (A.b1 - A.b0 + 1);
+        if (nl > mx) mx = nl;
+    }
+    if (mx <= 0) return;
+    dim3 grid((unsigned)((mx + 31) / 32), (unsigned)ncomp);
     inst_begin(c, LESGPU_K_ADI);
-    k_adi<<<nb, 128, 0, c->stream>>>(c->kp, A);
+    k_adi<<<grid, 32, 0, c->stream>>>(c->kp, B);
     inst_end(c, LESGPU_K_ADI);
 }
 
-// One component: z sweep in place on rhs1, y sweep into scratch G, x sweep
-// added to the field (the structure of lhsu :1044-1148).
-static void adi_component(lesgpu_case *c, int comp) {
+// The three sweeps of one component (the structure of lhsu :1044-1148):
+// z in place on rhs1, y into the scratch G, x added to the field.  Scratch
+// arrays per component slot: G, factor, second vector.
+static void adi_args(lesgpu_case *c, int comp, int slot, int dir, AdiArgs &A) {
     const DGrid &g = c->kp.g;
     const DCfg &cf = c->kp.c;
     DFields &f = c->kp.f;
@@ -211,43 +297,53 @@ static void adi_component(lesgpu_case *c, int comp) {
     int ib = comp == CU ? g.i_bgpx : 1;
     int jb = comp == CV ? 2 : 1;
     int kb = comp == CW ? g.k_bgpz : 1;
-    double *G = f.scr[0], *GAM = f.scr[1], *SA = f.scr[2];
-    bool zsweep = (comp == CW) || g.n3m != 1;
-    if (zsweep) {
-        AdiArgs A{};
-        A.comp = comp; A.dir = 2;
+    double *G = f.scr[3 * slot], *GAM = f.scr[3 * slot + 1], *SA = f.scr[3 * slot + 2];
+    A = AdiArgs{};
+    A.comp = comp;
+    A.dir = dir;
+    A.gam = GAM;
+    A.sarr = SA;
+    if (dir == 2) {
         A.periodic = cf.zprdic == 1;
-        A.l1 = (comp == CW && !A.periodic) ? 2 : 1;
-        if (comp == CW && !A.periodic) A.l1 = kb;
+        A.l1 = (comp == CW && !A.periodic) ? kb : 1;
         A.l2 = g.n3m;
         A.a0 = ib; A.a1 = g.n1m; A.b0 = jb; A.b1 = g.n2m;
-        A.src = rhs; A.dst = rhs; A.add = 0; A.gam = GAM; A.sarr = SA;
-        adi_launch(c, A);
-    }
-    {
-        AdiArgs A{};
-        A.comp = comp; A.dir = 1; A.periodic = 0;
+        A.src = rhs; A.dst = rhs; A.add = 0;
+    } else if (dir == 1) {
+        A.periodic = 0;
         A.l1 = jb; A.l2 = g.n2m;
         A.a0 = ib; A.a1 = g.n1m; A.b0 = kb; A.b1 = g.n3m;
-        A.src = rhs; A.dst = G; A.add = 0; A.gam = GAM; A.sarr = SA;
-        adi_launch(c, A);
-    }
-    {
-        AdiArgs A{};
-        A.comp = comp; A.dir = 0; A.periodic = cf.xprdic == 1;
+        A.src = rhs; A.dst = G; A.add = 0;
+    } else {
+        A.periodic = cf.xprdic == 1;
         A.l1 = ib; A.l2 = g.n1m;
         A.a0 = jb; A.a1 = g.n2m; A.b0 = kb; A.b1 = g.n3m;
-        A.src = G; A.dst = fld; A.add = 1; A.gam = GAM; A.sarr = SA;
-        adi_launch(c, A);
+        A.src = G; A.dst = fld; A.add = 1;
+    }
+}
+
+static void adi_components(lesgpu_case *c, const int *comps, int n) {
+    const DGrid &g = c->kp.g;
+    for (int dir = 2; dir >= 0; dir--) {
+        AdiBatch B{};
+        int m = 0;
+        for (int q = 0; q < n; q++) {
+            // lhsu/lhsv skip their z sweep when n3m = 1 (lhsw is not called then)
+            if (dir == 2 && comps[q] != CW && g.n3m == 1) continue;
+            adi_args(c, comps[q], q, dir, B.a[m++]);
+        }
+        if (m) adi_launch(c, B, m);
     }
 }
 
 void launch_adi_uvw(lesgpu_case *c) {
-    adi_component(c, CU);
-    adi_component(c, CV);
-    if (c->kp.g.n3m != 1) adi_component(c, CW);
+    const int comps3[3] = {CU, CV, CW};
+    adi_components(c, comps3, c->kp.g.n3m != 1 ? 3 : 2);
 }
 
-void launch_adi_t(lesgpu_case *c) { adi_component(c, CT); }
+void launch_adi_t(lesgpu_case *c) {
+    const int comps[1] = {CT};
+    adi_components(c, comps, 1);
+}
 
 }  // namespace lg

@@ -156,7 +156,7 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
     f.nusgs = A.get<double>(nt); f.alsgs = A.get<double>(nt);
     for (int l = 0; l < 3; l++) { f.nusgs1[l] = A.get<double>(nt); f.alsgs1[l] = A.get<double>(nt); }
     f.qmass = A.get<double>(nt); f.divgsum = A.get<double>(nt); f.phi = A.get<double>(nt);
-    int nscr = (cfg->iles == 1) ? 33 : 3;
+    int nscr = (cfg->iles == 1) ? 33 : 9;   // ADI uses scr[0..8] (three components), SGS scr[3..32]
     for (int s = 0; s < nscr; s++) f.scr[s] = A.get<double>(nt);
     f.part = A.get<double>((size_t)(kRedBlocks + 1) * kMaxRed);
     size_t np = (size_t)(d.n2 + 1) * (d.n3 + 1);
