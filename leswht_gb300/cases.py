@@ -12,6 +12,10 @@ Presets
                   passive temperature with the decomposition source
                   (IDECOMP = 1), dynamic SGS.  64^3 is the Re_tau = 180
                   configuration; 384x256x384 the Re_tau = 590 one.
+  cylinder_array(...)  : a row of heated circular cylinders, periodic in x
+                  and z, between no-slip isothermal walls, constant flow
+                  rate, direct-forcing IB with interpolation (the IB path
+                  with the FFT Poisson solver).
 """
 from __future__ import annotations
 
@@ -22,7 +26,8 @@ from typing import Any, Dict, Optional
 import numpy as np
 
 from . import abi
-from .gridgen import GridMetrics, Segment, make_grid
+from .gridgen import GridMetrics, Segment, axis_vectors, make_grid
+from . import ibmpre
 
 
 def base_settings() -> Dict[str, Any]:
@@ -169,6 +174,55 @@ def channel_ibm_tables(g: GridMetrics) -> Dict[str, Any]:
                 nwall_dvm=np.ones(g.n1m * g.n2m * g.n3m, np.int64),
                 cstar=np.ones(g.n1m * g.n2m * g.n3m), kstar=np.ones(6 * g.n1m * g.n2m * g.n3m),
                 omega=np.ones(g.n1m * g.n2m * g.n3m, np.int64))
+
+
+def cylinder_array(n1m: int = 48, n2m: int = 40, n3m: int = 8,
+                   lx: float = 6.0, ly: float = 4.0, lz: float = math.pi,
+                   re: float = 200.0, pr: float = 0.71, amp: float = 0.05,
+                   seed: int = 20261203, precision: int = abi.PREC_FP64,
+                   name: Optional[str] = None) -> Case:
+    """Cylinders of diameter 1 on a pitch lx, centred between no-slip walls
+    at y = -ly/2 and +ly/2, periodic in x and z, constant flow rate.  The
+    temperature uses the decomposition source (IDECOMP = 1) with T = 0 on the
+    walls and, through thermal IB forcing (ICONJG = 0), on the cylinder.
+    IB tables come from ibmpre (forcing points with interpolation, zero-eddy-
+    viscosity list, wall-function mask).  Initial field: plane Poiseuille
+    profile outside the body plus a seeded uniform perturbation."""
+    s = base_settings()
+    s.update(re=re, pr=pr, ich=1, iconjg=0, idecomp=1, ihtrans=1, iles=1, idvmon=1,
+             ibmon=1, masson=1, iintp=1,
+             xprdic=1, zprdic=1, yprdic=0, udrv_i=1.0, cflfac=0.5, idtopt=1, dt_size=0.002,
+             bc_ybtm=0, bc_ytop=0, bc_t_ybtm=0, bc_t_ytop=0, poisson=abi.POISSON_FTFT,
+             precision=precision,
+             body=dict(kind=abi.BODY_CYLINDER, cx=0.5 * lx, cy=0.0, cz=0.0, r=0.5, p0=0.0))
+    n1, n2, n3 = n1m + 1, n2m + 1, n3m + 1
+    h = 0.5 * ly
+    g, gdat, gbin = make_grid(
+        n1, n2, n3, lx, ly, lz,
+        [Segment("X", 0.0, lx, 1, n1, "U")],
+        [Segment("Y", -h, h, 1, n2, "U")],
+        [Segment("Z", 0.0, lz, 1, n3, "U")],
+        xprdic=True, zprdic=True)
+    tables = ibmpre.build_tables(g, s, axis_vectors(gdat, True, False, True))
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sh = g.shape
+    body = s["body"]
+    X = np.concatenate([[0.0], g.x])[None, None, :]
+    fl_u = ibmpre.funcbody(body, X, g.ymp[None, :, None], g.zmp[:, None, None]) > 1.0e-10
+    u = np.where(fl_u, 1.5 * (1.0 - (g.ymp[None, :, None] / h) ** 2), 0.0) * np.ones(sh)
+    v = np.zeros(sh); w = np.zeros(sh); p = np.zeros(sh); t = np.zeros(sh)
+    inner = np.zeros(sh); inner[1:n3m + 1, 1:n2m + 1, 1:n1m + 1] = 1.0
+    fv = np.zeros(sh); fv[1:n3m + 1, 2:n2m + 1, 1:n1m + 1] = 1.0
+    u += (rng.random(sh) - 0.5) * 2.0 * amp * inner * fl_u
+    v += (rng.random(sh) - 0.5) * 2.0 * amp * fv
+    w += (rng.random(sh) - 0.5) * 2.0 * amp * inner
+    u *= inner; v *= fv; w *= inner
+    t[1:n3m + 1, 1:n2m + 1, 1:n1m + 1] = (0.5 * (u[1:n3m + 1, 1:n2m + 1, 1:n1m + 1]
+                                              + u[1:n3m + 1, 1:n2m + 1, 2:n1m + 2])) / pr
+    U, V, W, P, T = prefld_apply(s, g, u, v, w, p, t)
+    nm = name or f"cylinder_array_{n1m}x{n2m}x{n3m}"
+    return Case(nm, s, g, gdat, gbin, dict(u=U, v=V, w=W, p=P, t=T), time=0.0, dt=s["dt_size"],
+                ihist=0, m=0, ibm=tables)
 
 
 PRESETS = {

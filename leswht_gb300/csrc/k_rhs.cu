@@ -179,35 +179,6 @@ __global__ void __launch_bounds__(kThreads) k_divgs(KP p, Box b, int scale) {
     }
 }
 
-// IB mass source/sink (slv_cont.f90:48-113): one serial pass per list so the
-// accumulation order into shared cells is the reference's.
-__global__ void k_divgs_ibm(KP p) {
-    const DGrid &g = p.g;
-    double *qm = p.f.qmass, *dv = p.f.divgsum;
-    const double *vel[3] = {p.f.u, p.f.v, p.f.w};
-    for (int l = 0; l < 3; l++) {
-        int nb = p.c.nbody[l];
-        for (int pass = 0; pass < 2; pass++) {
-            for (int n = 1; n <= nb; n++) {
-                int ii = p.f.ifc[l][n], jj = p.f.jfc[l][n], kk = p.f.kfc[l][n];
-                double val = vel[l][g.ix(ii, jj, kk)];
-                if (pass == 0) {
-                    long long q = g.ix(ii, jj, kk);
-                    double ds = l == 0 ? g.f2fxi[ii] : l == 1 ? g.f2fyi[jj] : g.f2fzi[kk];
-                    qm[q] = qm[q] - val * ds;
-                    dv[q] = dv[q] + val * ds;
-                } else {
-                    int im = l == 0 ? g.imv[ii] : ii, jm = l == 1 ? g.jmv[jj] : jj, km = l == 2 ? g.kmv[kk] : kk;
-                    long long q = g.ix(im, jm, km);
-                    double ds = l == 0 ? g.f2fxi[im] : l == 1 ? g.f2fyi[jm] : g.f2fzi[km];
-                    qm[q] = qm[q] + val * ds;
-                    dv[q] = dv[q] - val * ds;
-                }
-            }
-        }
-    }
-}
-
 __global__ void k_scale_div(KP p, Box b) {
     double dti = p.S->dtconsti;
     long long n = b.count();
@@ -226,7 +197,7 @@ void launch_divgs(lesgpu_case *c) {
     k_divgs<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, ibm ? 0 : 1);
     if (ibm) {
         cudaMemsetAsync(c->kp.f.qmass, 0, sizeof(double) * g.nt, c->stream);
-        k_divgs_ibm<<<1, 1, 0, c->stream>>>(c->kp);
+        launch_divgs_ibm(c);       // slv_cont.f90:48-113
         k_scale_div<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b);
     }
 }

@@ -81,8 +81,9 @@ int check_config(const lesgpu_config *c, const lesgpu_grid *g) {
     if ((long long)(g->n1 + 1) * (g->n2 + 1) * (g->n3 + 1) > (1LL << 40)) return LESGPU_ERR_ARG;
     if (c->precision != LESGPU_PREC_FP64) return LESGPU_ERR_UNSUPPORTED;
     if (c->poisson != LESGPU_POISSON_FTFT) return LESGPU_ERR_UNSUPPORTED;
-    if (c->ibmon != 0 || c->imovingon != 0) return LESGPU_ERR_UNSUPPORTED;
-    if (c->xprdic != 1) return LESGPU_ERR_UNSUPPORTED;        // convective outlet: not built yet
+    if (c->imovingon != 0) return LESGPU_ERR_UNSUPPORTED;     // moving bodies: not built
+    // poiss_ftft transforms x and z: both must be periodic
+    if (c->poisson == LESGPU_POISSON_FTFT && (c->xprdic != 1 || c->zprdic != 1)) return LESGPU_ERR_CONFIG;
     if (c->iles == 1 && c->insmdl != 1) return LESGPU_ERR_CONFIG;   // sgs.f90:314 stops
     if (c->ihtrans == 1 && c->iles == 1 && c->itemdl != 0) return LESGPU_ERR_CONFIG;
     if (c->filter < 1 || c->filter > 3) return LESGPU_ERR_CONFIG;
@@ -185,6 +186,21 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
                 }
         f.fb_u = upload(A, fbu.data(), nt);
         f.fb_c = upload(A, fbc.data(), nt);
+        // face points of heatflux (slv_auxi.f90:573-663)
+        size_t nxz = (size_t)(d.n1 + 1) * (d.n3 + 1), nxy = (size_t)(d.n1 + 1) * (d.n2 + 1);
+        std::vector<double> vb(nxz, 0.0), vt(nxz, 0.0), wb(nxy, 0.0), wt(nxy, 0.0);
+        for (long long kk = 0; kk <= d.n3; kk++)
+            for (long long ii = 0; ii <= d.n1; ii++) {
+                vb[ii + (d.n1 + 1) * kk] = funcbody(cfg->body, g->xmp[ii], g->y[0], g->zmp[kk]);
+                vt[ii + (d.n1 + 1) * kk] = funcbody(cfg->body, g->xmp[ii], g->y[d.n2 - 1], g->zmp[kk]);
+            }
+        for (long long jj = 0; jj <= d.n2; jj++)
+            for (long long ii = 0; ii <= d.n1; ii++) {
+                wb[ii + (d.n1 + 1) * jj] = funcbody(cfg->body, g->xmp[ii], g->ymp[jj], g->z[0]);
+                wt[ii + (d.n1 + 1) * jj] = funcbody(cfg->body, g->xmp[ii], g->ymp[jj], g->z[d.n3 - 1]);
+            }
+        f.fb_vb = upload(A, vb.data(), nxz); f.fb_vt = upload(A, vt.data(), nxz);
+        f.fb_wb = upload(A, wb.data(), nxy); f.fb_wt = upload(A, wt.data(), nxy);
     }
     // lhsinit (slv_mmtm.f90:180-249)
     {
@@ -256,6 +272,7 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
         f.geomfac[l] = A.get<double>(27); f.fcv[l] = A.get<double>(1); f.fcvavg[l] = A.get<double>(1);
     }
     for (int l = 0; l < 3; l++) f.dudtr[l] = A.get<double>(1);
+    for (int l = 0; l < 4; l++) f.ibtarg[l] = A.get<double>(1);
     f.inz = A.get<int>(1); f.jnz = A.get<int>(1); f.knz = A.get<int>(1);
 
     c->S = A.get<DScal>(1);
@@ -279,8 +296,59 @@ extern "C" int lesgpu_load_ibm(lesgpu_case *c, const lesgpu_ibm *b) {
     DFields &f = c->kp.f;
     Alloc &A = ((CaseExtra *)c->dmem_pool)->alloc;
     int nl = c->cfg.ihtrans == 1 ? 4 : 3;
-    for (int l = 0; l < nl; l++)
-        if (b->nbody[l] != 0 || b->nintp[l] != 0) return LESGPU_ERR_UNSUPPORTED;   // IB forcing: not built yet
+    for (int l = 0; l < nl; l++) {
+        if (b->nbody[l] < b->nintp[l] || b->nintp[l] < 0 || b->nbody[l] > 0x7ffffff0LL) return LESGPU_ERR_ARG;
+        if (b->nbody[l] > 0 && c->cfg.ibmon == 0) return LESGPU_ERR_CONFIG;
+        if (b->nbody[l] > 0 && (!b->fc[l] || (b->nintp[l] > 0 && (!b->intpindx[l] || !b->geomfac[l]))))
+            return LESGPU_ERR_ARG;
+    }
+    // forcing lists (ibmpreread, misc_init.f90:312-378): 1-based rows on the
+    // device.  Every index is checked against the grid before anything is
+    // uploaded, so a rejected table leaves the case as it was and no gather
+    // can leave the arrays.
+    struct HostList { std::vector<int> fi, fj, fk, ix; std::vector<double> gf; };
+    HostList H[4];
+    for (int l = 0; l < nl; l++) {
+        long long nb = b->nbody[l], ni = b->nintp[l];
+        HostList &h = H[l];
+        h.fi.assign(nb + 1, 0); h.fj.assign(nb + 1, 0); h.fk.assign(nb + 1, 0);
+        h.ix.assign(3 * (ni + 1), 0); h.gf.assign(27 * (ni + 1), 0.0);
+        for (long long n = 0; n < nb; n++) {
+            long long i = b->fc[l][3 * n], j = b->fc[l][3 * n + 1], k = b->fc[l][3 * n + 2];
+            if (i < 1 || i > d.n1m || j < 1 || j > d.n2m || k < 1 || k > d.n3m) return LESGPU_ERR_ARG;
+            h.fi[n + 1] = (int)i; h.fj[n + 1] = (int)j; h.fk[n + 1] = (int)k;
+        }
+        for (long long n = 0; n < ni; n++) {
+            for (int q = 0; q < 3; q++) {
+                long long dq = b->intpindx[l][3 * n + q];
+                if (dq < -1 || dq > 1) return LESGPU_ERR_ARG;
+                h.ix[3 * (n + 1) + q] = (int)dq;
+            }
+            // x and z wrap through reindex_i / reindex_k; y must stay in 0..n2
+            long long jpp = h.fj[n + 1] + 2 * h.ix[3 * (n + 1) + 1];
+            if (jpp < 0 || jpp > d.n2) return LESGPU_ERR_ARG;
+            for (int q = 0; q < 27; q++) h.gf[27 * (n + 1) + q] = b->geomfac[l][27 * n + q];
+        }
+    }
+    // zero-eddy-viscosity list: the file's 0-based numbers are used as
+    // indices as they are (sgs.f90:893-895), so 0..n?m-1 are valid
+    if (b->nzero < 0 || b->nzero > 0x7ffffff0LL || (b->nzero > 0 && (!b->inz || !b->jnz || !b->knz)))
+        return LESGPU_ERR_ARG;
+    for (long long n = 0; n < b->nzero; n++)
+        if (b->inz[n] < 0 || b->inz[n] > d.n1 || b->jnz[n] < 0 || b->jnz[n] > d.n2 || b->knz[n] < 0 || b->knz[n] > d.n3)
+            return LESGPU_ERR_ARG;
+    for (int l = 0; l < nl; l++) {
+        long long nb = b->nbody[l];
+        HostList &h = H[l];
+        f.ifc[l] = upload(A, h.fi.data(), h.fi.size()); f.jfc[l] = upload(A, h.fj.data(), h.fj.size());
+        f.kfc[l] = upload(A, h.fk.data(), h.fk.size());
+        f.intpindx[l] = upload(A, h.ix.data(), h.ix.size()); f.geomfac[l] = upload(A, h.gf.data(), h.gf.size());
+        f.fcv[l] = A.get<double>(nb + 1); f.fcvavg[l] = A.get<double>(nb + 1);
+        f.ibtarg[l] = A.get<double>(nb + 1);
+        if (l < 3) f.dudtr[l] = A.get<double>(nb + 1);
+        c->kp.c.nbody[l] = (int)nb; c->kp.c.nintp[l] = b->nintp[l] > 0 ? (int)b->nintp[l] : 0;
+    }
+    if (c->graph_ok) { cudaGraphExecDestroy(c->graph); c->graph_ok = 0; }
     c->kp.c.nzero = (int)b->nzero;
     if (b->nzero > 0) {
         std::vector<int> a(b->nzero + 2), bb(b->nzero + 2), cc(b->nzero + 2);
@@ -389,6 +457,8 @@ static void enqueue_sgs(lesgpu_case *c, bool first) {
 
 static void enqueue_rhsnlhs(lesgpu_case *c, int msub) {
     launch_rhs(c, msub);
+    if (c->cfg.ibmon != 0) launch_rhs_ibm(c);
+    launch_convbc(c);
     launch_adi_uvw(c);
     k_retrv_uvw<<<blocks_for((long long)c->kp.g.n2m * c->kp.g.n3m), kThreads, 0, c->stream>>>(c->kp);
     launch_ghost_uvw(c);
@@ -398,6 +468,8 @@ static void enqueue_energy(lesgpu_case *c, int msub) {
     const lesgpu_config &g = c->cfg;
     if (g.ich == 1) launch_tvolcalc(c, 1);
     launch_rhs_t(c, msub);
+    if (g.ibmon != 0 && g.iconjg == 0) launch_rhs_ibm_t(c);
+    launch_convbc_t(c);
     launch_adi_t(c);
     launch_energy_bc(c);
     if (g.ich == 1) { launch_tvolcalc(c, 2); launch_tvolcorr(c); }
@@ -420,11 +492,14 @@ static void enqueue_step(lesgpu_case *c, bool first) {
         if (g.ich == 1) launch_qvolcalc(c, 0);
         launch_pcalc(c);
         if (g.ich != 0) launch_meanpg(c);
+        if (g.ibmon == 1) launch_lagforce(c, msub);
         if (g.ihtrans == 1) enqueue_energy(c, msub);
     }
     launch_time_advance(c);
     launch_convergence(c);
     launch_bulk_diag(c);
+    if (g.ibmon == 1) launch_draglift(c);
+    if (g.ihtrans == 1) launch_heatflux(c);
 }
 
 // Capture one steady-state step into a CUDA graph and count its kernels.

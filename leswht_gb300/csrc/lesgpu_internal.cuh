@@ -64,6 +64,7 @@ struct DScal {
     double u_bulk_t;          // rhs_t's bulk velocity of the current substep
     double phiref;            // pcalc's outlet-plane mean of phi
     double cvol;              // tvolcorr's volume integral of 1/c*
+    double cb[4];             // convective outlet: qin, ucoef, vwcoef, qratio
     long long ntime, m, ihist;
     long long poisson_iters[3];
     int err;                  // device-side error flag (non-finite values etc.)
@@ -77,6 +78,9 @@ struct DFields {
     double *cstar, *kstar[6];
     int *omega, *nwall;
     double *fb_u, *fb_c;
+    // body function on the y faces (xmp_i, y_1 | y_n2, zmp_k) and the z faces
+    // (xmp_i, ymp_j, z_1 | z_n3), planes indexed i + (n1+1) * (k | j)
+    double *fb_vb, *fb_vt, *fb_wb, *fb_wt;
     // convective outlet planes (0:n2,0:n3)
     double *uout, *vout, *wout, *tout, *duout, *dvout, *dwout, *dtout;
     // ADI coefficient vectors (lhsinit)
@@ -86,6 +90,7 @@ struct DFields {
     // IB tables (component l = 0..3); 1-based rows
     int *ifc[4], *jfc[4], *kfc[4], *intpindx[4];
     double *geomfac[4], *fcv[4], *fcvavg[4], *dudtr[3];
+    double *ibtarg[4];        // forcing targets of the current substep (two-phase forcing)
     int *inz, *jnz, *knz;
     // scratch
     double *scr[34];          // SGS temporaries / tridiagonal work, nt each
@@ -248,6 +253,14 @@ void launch_poisson(lesgpu_case *c);
 int poisson_init(lesgpu_case *c);
 void poisson_free(lesgpu_case *c);
 void launch_sgs_zero_first(lesgpu_case *c, int thermal);
+void launch_rhs_ibm(lesgpu_case *c);
+void launch_rhs_ibm_t(lesgpu_case *c);
+void launch_divgs_ibm(lesgpu_case *c);
+void launch_lagforce(lesgpu_case *c, int msub);
+void launch_draglift(lesgpu_case *c);
+void launch_heatflux(lesgpu_case *c);
+void launch_convbc(lesgpu_case *c);
+void launch_convbc_t(lesgpu_case *c);
 }  // namespace lg
 
 namespace lg {

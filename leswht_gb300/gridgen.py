@@ -257,6 +257,20 @@ def read_grid_bin(text: str) -> GridMetrics:
     return GridMetrics(n1=n1, n2=n2, n3=n3, n1m=n1m, n2m=n2m, n3m=n3m, xl=xl, yl=yl, zl=zl, **d)
 
 
+def axis_vectors(grid_dat: str, xprdic: bool, yprdic: bool, zprdic: bool) -> Dict[str, Tuple[np.ndarray, np.ndarray]]:
+    """Per-axis (coord, center) vectors, indices 0..N, as lib_setgrid holds
+    them in full precision before grid.bin is written (the pre-processor's
+    X/XM, Y/YM, Z/ZM of preprocessing.py:102-113)."""
+    lines = grid_dat.split("\n")
+    out = {}
+    for name, line, prd in (("x", lines[2], xprdic), ("y", lines[3], yprdic), ("z", lines[4], zprdic)):
+        info = _axis_info(line.split(), prd)
+        n = len(info) - 1
+        out[name] = (np.array([info[i]["coord"] for i in range(n + 1)]),
+                     np.array([info[i]["center"] for i in range(n + 1)]))
+    return out
+
+
 def make_grid(nx: int, ny: int, nz: int, lx: float, ly: float, lz: float,
               xseg: Sequence[Segment], yseg: Sequence[Segment], zseg: Sequence[Segment],
               xprdic: bool, zprdic: bool, yprdic: bool = False) -> Tuple[GridMetrics, str, str]:
