@@ -16,6 +16,12 @@ Presets
                   and z, between no-slip isothermal walls, constant flow
                   rate, direct-forcing IB with interpolation (the IB path
                   with the FFT Poisson solver).
+  cylinder(...) : flow past a heated circular cylinder (D = 1) in a
+                  30D x 20D x pi D box: uniform inflow, convective outlet,
+                  far-field (slip) lateral boundaries, periodic z, grid
+                  clustered at the body, direct-forcing IB, FFT-z +
+                  multigrid-xy Poisson solver.  128x96x16 at Re = 100 and
+                  256x192x64 at Re = 3900 are the benchmark sizes.
 """
 from __future__ import annotations
 
@@ -26,7 +32,7 @@ from typing import Any, Dict, Optional
 import numpy as np
 
 from . import abi
-from .gridgen import GridMetrics, Segment, axis_vectors, make_grid
+from .gridgen import GridMetrics, Segment, axis_vectors, clustered_lines, make_grid, make_grid_lines
 from . import ibmpre
 
 
@@ -49,6 +55,17 @@ def base_settings() -> Dict[str, Any]:
         poisson=abi.POISSON_FTFT, precision=abi.PREC_FP64,
         body=dict(kind=abi.BODY_NONE, cx=0.0, cy=0.0, cz=0.0, r=0.5, p0=0.0),
     )
+
+
+def readbcs_overrides(s: Dict[str, Any]) -> Dict[str, Any]:
+    """What readbcs (misc_init.f90:95-160) does to the boundary.input flags
+    once the periodicity flags are known: a periodic direction's momentum
+    flags become 4 (periodic), so no wall term is evaluated there."""
+    if s.get("yprdic", 0) == 1:
+        s["bc_ybtm"] = s["bc_ytop"] = 4
+    if s.get("zprdic", 0) == 1:
+        s["bc_zbtm"] = s["bc_ztop"] = 4
+    return s
 
 
 @dataclass
@@ -128,6 +145,7 @@ def channel(n1m: int = 64, n2m: int = 64, n3m: int = 64,
              bc_ybtm=0, bc_ytop=0, bc_t_ybtm=0, bc_t_ytop=0, poisson=abi.POISSON_FTFT,
              precision=precision,
              body=dict(kind=abi.BODY_CHANNEL, cx=0.0, cy=0.0, cz=0.0, r=0.0, p0=1.0e-6))
+    readbcs_overrides(s)
     n1, n2, n3 = n1m + 1, n2m + 1, n3m + 1
     g, gdat, gbin = make_grid(
         n1, n2, n3, lx, ly, lz,
@@ -195,6 +213,7 @@ def cylinder_array(n1m: int = 48, n2m: int = 40, n3m: int = 8,
              bc_ybtm=0, bc_ytop=0, bc_t_ybtm=0, bc_t_ytop=0, poisson=abi.POISSON_FTFT,
              precision=precision,
              body=dict(kind=abi.BODY_CYLINDER, cx=0.5 * lx, cy=0.0, cz=0.0, r=0.5, p0=0.0))
+    readbcs_overrides(s)
     n1, n2, n3 = n1m + 1, n2m + 1, n3m + 1
     h = 0.5 * ly
     g, gdat, gbin = make_grid(
@@ -225,7 +244,60 @@ def cylinder_array(n1m: int = 48, n2m: int = 40, n3m: int = 8,
                 ihist=0, m=0, ibm=tables)
 
 
+def cylinder(n1m: int = 128, n2m: int = 96, n3m: int = 16, re: float = 100.0, pr: float = 0.71,
+             dmin: float = 0.02, amp: float = 1.0e-3, body_kind: int = abi.BODY_CYLINDER,
+             center=(0.0, 0.0, 0.5 * math.pi), seed: int = 20261203, nlev: Optional[int] = None,
+             precision: int = abi.PREC_FP64, name: Optional[str] = None) -> Case:
+    """Heated body (wall T = 0 through the thermal forcing) in a free stream
+    (U = 1, T = TFLU_I = -1) on x in [-10, 20], y in [-10, 10], z in [0, pi],
+    gridlines clustered at the body with a first spacing of `dmin`.  The
+    initial field is the one makefld (misc_init.f90:442-560) builds for
+    ICH = 0 -- U = 1 in the fluid, 0 in the body -- plus a seeded uniform
+    perturbation of amplitude `amp` on the interior unknowns, in the state
+    prefld leaves after reading it back."""
+    s = base_settings()
+    s.update(re=re, pr=pr, ich=0, iconjg=0, idecomp=0, ihtrans=1, iles=1, idvmon=1,
+             ibmon=1, masson=1, iintp=1, tflu_i=-1.0, tsol_i=0.0,
+             xprdic=0, yprdic=0, zprdic=1, udrv_i=1.0, cflfac=0.5, idtopt=1, dt_size=0.005,
+             bc_ybtm=1, bc_ytop=1, bc_t_ybtm=1, bc_t_ytop=1, val_t_ybtm=0.0, val_t_ytop=0.0,
+             poisson=abi.POISSON_Z_FT, precision=precision,
+             body=dict(kind=body_kind, cx=float(center[0]), cy=float(center[1]), cz=float(center[2]),
+                       r=0.5, p0=0.0))
+    if nlev is None:
+        nlev = 1
+        while nlev < 5 and n1m % (2 ** (nlev + 1)) == 0 and n1m // (2 ** (nlev + 1)) >= 2:
+            nlev += 1
+    s["nlev"] = nlev
+    readbcs_overrides(s)
+    xs = clustered_lines(-10.0, 20.0, float(center[0]), n1m, dmin)
+    ys = clustered_lines(-10.0, 10.0, float(center[1]), n2m, dmin)
+    zs = [math.pi * k / n3m for k in range(n3m + 1)]
+    g, gdat, gbin = make_grid_lines(xs, ys, zs, xprdic=False, zprdic=True)
+    tables = ibmpre.build_tables(g, s, axis_vectors(gdat, False, False, True))
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sh = g.shape
+    body = s["body"]
+    X = np.concatenate([[g.x[0]], g.x])[None, None, :]
+    fl_u = ibmpre.funcbody(body, X, g.ymp[None, :, None], g.zmp[:, None, None]) >= 1.0e-10
+    fl_c = ibmpre.funcbody(body, g.xmp[None, None, :], g.ymp[None, :, None], g.zmp[:, None, None]) >= 1.0e-10
+    u = np.where(fl_u, s["udrv_i"], 0.0) * np.ones(sh)
+    v = np.zeros(sh); w = np.zeros(sh); p = np.zeros(sh)
+    t = np.where(fl_c, s["tflu_i"], s["tsol_i"]) * np.ones(sh)
+    inner = np.zeros(sh); inner[1:n3m + 1, 1:n2m + 1, 2:n1m + 1] = 1.0     # u unknowns i = 2..n1m
+    fv = np.zeros(sh); fv[1:n3m + 1, 2:n2m + 1, 1:n1m + 1] = 1.0
+    fw = np.zeros(sh); fw[1:n3m + 1, 1:n2m + 1, 1:n1m + 1] = 1.0
+    u += (rng.random(sh) - 0.5) * 2.0 * amp * inner * fl_u
+    v += (rng.random(sh) - 0.5) * 2.0 * amp * fv
+    w += (rng.random(sh) - 0.5) * 2.0 * amp * fw
+    U, V, W, P, T = prefld_apply(s, g, u, v, w, p, t)
+    nm = name or f"cylinder_{n1m}x{n2m}x{n3m}"
+    return Case(nm, s, g, gdat, gbin, dict(u=U, v=V, w=W, p=P, t=T), time=0.0, dt=s["dt_size"],
+                ihist=0, m=0, ibm=tables)
+
+
 PRESETS = {
     "channel64": lambda **kw: channel(64, 64, 64, **kw),
     "channel590": lambda **kw: channel(384, 256, 384, lx=2 * math.pi, lz=math.pi, re=10950.0, **kw),
+    "cylinder100": lambda **kw: cylinder(128, 96, 16, re=100.0, **kw),
+    "cylinder3900": lambda **kw: cylinder(256, 192, 64, re=3900.0, **kw),
 }

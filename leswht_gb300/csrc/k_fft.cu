@@ -87,7 +87,7 @@ __device__ double2 *block_fft(double2 *b0, double2 *b1, int L, const DevPlan &P,
     return in;
 }
 
-static DevPlan devplan(const FftPlan &p) {
+DevPlan devplan(const FftPlan &p) {
     DevPlan d;
     d.n = p.n;
     d.nst = p.nst;
@@ -97,7 +97,7 @@ static DevPlan devplan(const FftPlan &p) {
 }
 
 // ---- z transforms: block = (i-tile of L lines) x j ----------------------
-__global__ void k_fft_z_fwd(KP p, double2 *ccap, DevPlan P, int L) {
+__global__ void k_fft_z_fwd(KP p, double2 *ccap, DevPlan P, int L, long long sk, long long sj) {
     extern __shared__ double2 sm[];
     const DGrid &g = p.g;
     const int N = P.n;
@@ -115,11 +115,11 @@ __global__ void k_fft_z_fwd(KP p, double2 *ccap, DevPlan P, int L) {
     for (int w = threadIdx.x; w < n3mh * L; w += blockDim.x) {
         int l = w % L, kk = w / L;
         int i = i0 + l;
-        if (i <= g.n1m) ccap[(i - 1) + (size_t)g.n1m * (kk + (size_t)n3mh * (j - 1))] = res[kk * L + l];
+        if (i <= g.n1m) ccap[(i - 1) + sk * kk + sj * (j - 1)] = res[kk * L + l];
     }
 }
 
-__global__ void k_fft_z_inv(KP p, const double2 *ccap, DevPlan P, int L) {
+__global__ void k_fft_z_inv(KP p, const double2 *ccap, DevPlan P, int L, long long sk, long long sj) {
     extern __shared__ double2 sm[];
     const DGrid &g = p.g;
     const int N = P.n;
@@ -132,11 +132,11 @@ __global__ void k_fft_z_inv(KP p, const double2 *ccap, DevPlan P, int L) {
         double2 val = make_double2(0.0, 0.0);
         if (i <= g.n1m) {
             if (e < n3mh) {
-                val = ccap[(i - 1) + (size_t)g.n1m * (e + (size_t)n3mh * (j - 1))];
+                val = ccap[(i - 1) + sk * e + sj * (j - 1)];
             } else {
                 // zzz(k) = conjg(zzz(n3m+2-k)), poiss_ftft.f90:143-147
                 int src = N - e;
-                double2 s = ccap[(i - 1) + (size_t)g.n1m * (src + (size_t)n3mh * (j - 1))];
+                double2 s = ccap[(i - 1) + sk * src + sj * (j - 1)];
                 val = make_double2(s.x, -s.y);
             }
         }
@@ -249,7 +249,7 @@ __global__ void k_ytri(KP p, double2 *ccap, const double *ak1, const double *ak3
 }
 
 // ------------------------------------------------------------ host side
-static int make_plan(FftPlan &p, int n) {
+int make_plan(FftPlan &p, int n) {
     p.n = n;
     p.nst = 0;
     int m = n;
@@ -264,7 +264,7 @@ static int make_plan(FftPlan &p, int n) {
         p.rad[p.nst++] = r;
         m /= r;
     }
-    double2 *h = (double2 *)malloc(sizeof(double2) * (size_t)n);
+    double2 *h = (double2 *)malloc(sizeof(double2) * (size_t)(n > 0 ? n : 1));
     for (int e = 0; e < n; e++) {
         long double ang = -2.0L * 3.14159265358979323846264338327950288L * (long double)e / (long double)n;
         h[e] = make_double2((double)cosl(ang), (double)sinl(ang));
@@ -287,6 +287,7 @@ int fft_lines_per_block(int n) { return lines_per_block(n); }
 int poisson_init(lesgpu_case *c) {
     const DGrid &g = c->kp.g;
     DPois &P = c->pois;
+    if (c->cfg.poisson == LESGPU_POISSON_Z_FT) return zft_init(c);
     if (c->cfg.poisson != LESGPU_POISSON_FTFT) return LESGPU_ERR_UNSUPPORTED;
     if (c->cfg.xprdic != 1 || c->cfg.zprdic != 1) return LESGPU_ERR_CONFIG;
     int rc = make_plan(P.fx, g.n1m);
@@ -325,26 +326,29 @@ int poisson_init(lesgpu_case *c) {
 
 void poisson_free(lesgpu_case *c) {
     DPois &P = c->pois;
+    zft_free(c);
     cudaFree(P.ak1); cudaFree(P.ak3); cudaFree(P.ccap);
     cudaFree(P.fx.tw); cudaFree(P.fz.tw);
     P.ak1 = P.ak3 = nullptr; P.ccap = nullptr; P.fx.tw = P.fz.tw = nullptr;
 }
 
-void launch_poisson(lesgpu_case *c) {
+void launch_poisson(lesgpu_case *c, int msub) {
     const DGrid &g = c->kp.g;
     DPois &P = c->pois;
+    if (c->cfg.poisson == LESGPU_POISSON_Z_FT) { launch_zft(c, msub); return; }
     DevPlan px = devplan(P.fx), pz = devplan(P.fz);
     int Lz = lines_per_block(g.n3m), Lx = lines_per_block(g.n1m);
     size_t smz = (size_t)2 * g.n3m * Lz * sizeof(double2), smx = (size_t)2 * g.n1m * Lx * sizeof(double2);
     dim3 gz((g.n1m + Lz - 1) / Lz, g.n2m);
     int nxl = g.n3mh * g.n2m;
     inst_begin(c, LESGPU_K_POISSON);
-    k_fft_z_fwd<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz);
+    const long long sk = g.n1m, sj = (long long)g.n1m * g.n3mh;
+    k_fft_z_fwd<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
     k_fft_x<<<(nxl + Lx - 1) / Lx, kThreads, smx, c->stream>>>(P.ccap, nxl, px, Lx, 0);
     long long nl = (long long)g.n1m * g.n3mh;
     k_ytri<<<blocks_for(nl, 128), 128, 0, c->stream>>>(c->kp, P.ccap, P.ak1, P.ak3, c->kp.f.scr[0]);
     k_fft_x<<<(nxl + Lx - 1) / Lx, kThreads, smx, c->stream>>>(P.ccap, nxl, px, Lx, 1);
-    k_fft_z_inv<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz);
+    k_fft_z_inv<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
     inst_end(c, LESGPU_K_POISSON);
 }
 

@@ -11,10 +11,17 @@ struct DevPlan {
     const double2 *tw;
 };
 
-__global__ void k_fft_z_fwd(KP p, double2 *ccap, DevPlan P, int L);
-__global__ void k_fft_z_inv(KP p, const double2 *ccap, DevPlan P, int L);
+// z transforms; the spectrum element (i, k, j) sits at (i-1) + sk*(k-1) + sj*(j-1)
+__global__ void k_fft_z_fwd(KP p, double2 *ccap, DevPlan P, int L, long long sk, long long sj);
+__global__ void k_fft_z_inv(KP p, const double2 *ccap, DevPlan P, int L, long long sk, long long sj);
 __global__ void k_fft_x(double2 *ccap, int nlines, DevPlan P, int L, int inv);
 __global__ void k_ytri(KP p, double2 *ccap, const double *ak1, const double *ak3, double *gam);
 int fft_lines_per_block(int n);
+int make_plan(FftPlan &p, int n);
+DevPlan devplan(const FftPlan &p);
+// poiss_z_ft (k_mg.cu)
+int zft_init(lesgpu_case *c);
+void zft_free(lesgpu_case *c);
+void launch_zft(lesgpu_case *c, int msub);
 
 }  // namespace lg

@@ -1,0 +1,621 @@
+// Pressure Poisson solve of poiss_z_ft.f90: FFT in z, then for each of the
+// n3mh z modes a complex 2-D problem in x-y solved by the reference's
+// multigrid -- semi-coarsened in x (levels of n1m, n1m/2, ... x-lines),
+// zebra x-line relaxation with y-Thomas solves, linear restriction and the
+// prolongation onto the even lines only -- or, for modes above IMGSOR, by
+// zebra line SOR.
+//
+// GPU design: one thread block per z mode runs that mode's whole solve
+// (every V-cycle and its convergence test) as one launch; the phases of a
+// cycle are separated by block barriers, so the iteration count needs no
+// host round trip and the solve can sit inside the step's CUDA graph.
+// Within a phase, the y-Thomas solve of an x-line is done by one warp: each
+// lane composes the affine maps of its chunk of rows, a 5-step shuffle scan
+// joins the chunks, and each lane re-runs its chunk with the reference's
+// recurrence from the scanned incoming value (forward elimination with the
+// precomputed LU factors, then back substitution the same way).  That cuts
+// the dependent chain of a 192-row line from 384 steps to about 30.
+//
+// Tables (pmat :55-94, mwavenumber :97-113, coefmg :643-798, the LU factors
+// of poisinit :18-52) are built on the host in the reference's arithmetic
+// order and uploaded once.
+#include "k_fft.cuh"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <vector>
+
+namespace lg {
+
+constexpr int kMgThreads = 1024;
+constexpr int kMaxLev = 20;
+
+struct MgTables {
+    int n1md, nlev;
+    int iimg[kMaxLev + 1][3];
+    double *aw, *ae, *as, *an, *coi1, *coi2, *cor1, *cor2;   // 1-based
+    int *ipm, *imm;
+    double *ac, *bet, *gam;     // (i-1) + n1md*((j-1) + n2m*(kv-1))
+    double2 *pc, *gg, *rs;      // per-mode work arrays
+    long long *iters;           // per mode, last solve
+    long long pc_plane, gg_plane;
+};
+
+struct MgArgs {
+    int n1m, n2m, n1md, nlev, nbli, mgitr, imgsor;
+    double wwsor;
+    int ldp, ldg;
+    int iimg[kMaxLev + 1][3];
+    const double *aw, *ae, *as, *an, *coi1, *coi2, *cor1, *cor2;
+    const int *ipm, *imm;
+    const double *ac, *bet, *gam;
+    double2 *ccap, *pc, *gg, *rs;
+    long long pc_plane, gg_plane;
+    long long *iters;
+    DScal *S;
+    int slot;
+};
+
+// ------------------------------------------------------------- device side
+struct Mode {
+    const MgArgs &a;
+    int kv;
+    double2 *pc, *gg, *rs;
+    const double2 *rhs;                 // ccap plane of the mode, (i-1) + n1m*(j-1)
+    size_t cb;                          // coefficient base of the mode
+    __device__ Mode(const MgArgs &a_, int kv_) : a(a_), kv(kv_) {
+        pc = a.pc + a.pc_plane * (kv - 1);
+        gg = a.gg + a.gg_plane * (kv - 1);
+        rs = a.rs + a.gg_plane * (kv - 1);
+        rhs = a.ccap + (size_t)a.n1m * a.n2m * (kv - 1);
+        cb = (size_t)a.n1md * a.n2m * (kv - 1);
+    }
+    __device__ double2 &P(int i, int j) const { return pc[i + (size_t)a.ldp * j]; }
+    __device__ double2 &G(int i, int j) const { return gg[i + (size_t)a.ldg * j]; }
+    __device__ double2 &R(int i, int j) const { return rs[i + (size_t)a.ldg * j]; }
+    __device__ double2 B(int i, int j) const { return rhs[(i - 1) + (size_t)a.n1m * (j - 1)]; }
+    __device__ double AC(int i, int j) const { return a.ac[cb + (i - 1) + (size_t)a.n1md * (j - 1)]; }
+};
+
+__device__ __forceinline__ double2 axmy(double2 y, double s, double2 x) {   // y - s*x
+    return make_double2(y.x - s * x.x, y.y - s * x.y);
+}
+
+// trdiag1m (poiss_z_ft.f90:383-408) on the x-lines l1, l1+2, ..., l2 of gg,
+// in place, one warp per line (see the file comment).
+__device__ void mg_trdiag(const Mode &m, int l1, int l2) {
+    const MgArgs &a = m.a;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (l2 < l1) return;
+    const int n2m = a.n2m, nl = (l2 - l1) / 2 + 1;
+    const int ch = (n2m + 31) / 32;
+    const int j0 = 1 + lane * ch, j1 = min(n2m, j0 + ch - 1);
+    const size_t sj = (size_t)a.n1md;
+    for (int li = warp; li < nl; li += nw) {
+        const int i = l1 + 2 * li;
+        const double *bet = a.bet + m.cb + (i - 1) - sj;     // bet(i, j) = bet[sj * j]
+        const double *gam = a.gam + m.cb + (i - 1) - sj;
+        // forward: y_j = (r_j - as_j y_{j-1}) bet_j  =  A_j y_{j-1} + B_j
+        double A = 1.0;
+        double2 Bv = make_double2(0.0, 0.0);
+        for (int j = j0; j <= j1; j++) {
+            const double bj = bet[sj * j], aj = -a.as[j] * bj;
+            const double2 r = m.G(i, j);
+            Bv = make_double2(aj * Bv.x + r.x * bj, aj * Bv.y + r.y * bj);
+            A = aj * A;
+        }
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const double Ap = __shfl_up_sync(0xffffffffu, A, d);
+            const double bx = __shfl_up_sync(0xffffffffu, Bv.x, d), by = __shfl_up_sync(0xffffffffu, Bv.y, d);
+            if (lane >= d) { Bv = make_double2(A * bx + Bv.x, A * by + Bv.y); A = A * Ap; }
+        }
+        double yx = __shfl_up_sync(0xffffffffu, Bv.x, 1), yy = __shfl_up_sync(0xffffffffu, Bv.y, 1);
+        if (lane == 0) { yx = 0.0; yy = 0.0; }
+        for (int j = j0; j <= j1; j++) {
+            const double bj = bet[sj * j];
+            const double2 r = m.G(i, j);
+            yx = (r.x - a.as[j] * yx) * bj;
+            yy = (r.y - a.as[j] * yy) * bj;
+            m.G(i, j) = make_double2(yx, yy);
+        }
+        __syncwarp();
+        // backward: x_j = y_j - gam_{j+1} x_{j+1}  =  C_j x_{j+1} + D_j
+        double C = 1.0;
+        double2 D = make_double2(0.0, 0.0);
+        for (int j = j1; j >= j0; j--) {
+            const double cj = j < n2m ? -gam[sj * (j + 1)] : 0.0;
+            const double2 y = m.G(i, j);
+            D = make_double2(cj * D.x + y.x, cj * D.y + y.y);
+            C = cj * C;
+        }
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const double Cn = __shfl_down_sync(0xffffffffu, C, d);
+            const double dx = __shfl_down_sync(0xffffffffu, D.x, d), dy = __shfl_down_sync(0xffffffffu, D.y, d);
+            if (lane + d < 32) { D = make_double2(C * dx + D.x, C * dy + D.y); C = C * Cn; }
+        }
+        double xx = __shfl_down_sync(0xffffffffu, D.x, 1), xy = __shfl_down_sync(0xffffffffu, D.y, 1);
+        if (lane == 31) { xx = 0.0; xy = 0.0; }
+        for (int j = j1; j >= j0; j--) {
+            const double2 y = m.G(i, j);
+            if (j < n2m) {
+                const double gj = gam[sj * (j + 1)];
+                xx = y.x - gj * xx;
+                xy = y.y - gj * xy;
+            } else {
+                xx = y.x;
+                xy = y.y;
+            }
+            m.G(i, j) = make_double2(xx, xy);
+        }
+        __syncwarp();
+    }
+}
+
+// src - aw*g(imm) - ae*g(ipm) - as*g(j-1) - an*g(j+1) - ac*g  on the gg array
+__device__ __forceinline__ double2 mg_defect(const Mode &m, double2 src, const double2 *g, int ld, int i, int j) {
+    const MgArgs &a = m.a;
+    src = axmy(src, a.aw[i], g[a.imm[i] + (size_t)ld * j]);
+    src = axmy(src, a.ae[i], g[a.ipm[i] + (size_t)ld * j]);
+    src = axmy(src, a.as[j], g[i + (size_t)ld * (j - 1)]);
+    src = axmy(src, a.an[j], g[i + (size_t)ld * (j + 1)]);
+    src = axmy(src, m.AC(i, j), g[i + (size_t)ld * j]);
+    return src;
+}
+
+__device__ double block_max(double v) {
+    __shared__ double sh[kMgThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) r = fmax(r, sh[q]);
+    return r;
+}
+
+// toplevel, poiss_z_ft.f90:302-380; returns the max-norm residual
+__device__ double mg_toplevel(const Mode &m, int id, double oldv, double test) {
+    const MgArgs &a = m.a;
+    const int n1m = a.n1m, n2m = a.n2m, nt = blockDim.x;
+    const int cl = a.iimg[a.nlev - 1][0], ce = a.iimg[a.nlev - 1][1];
+    if (id == 1) {   // prolong the coarse correction onto the even lines
+        const int nc = ce - cl + 1;
+        for (int t = threadIdx.x; t < nc * n2m; t += nt) {
+            const int i = cl + t % nc, j = 1 + t / nc, ic = 2 * (i - cl + 1);
+            double2 p = m.P(ic, j);
+            const double2 g1 = m.G(i, j);
+            if (i < ce) {
+                const double2 g2 = m.G(a.ipm[i], j);
+                p = make_double2(p.x + a.coi1[i] * g1.x + a.coi2[i] * g2.x, p.y + a.coi1[i] * g1.y + a.coi2[i] * g2.y);
+            } else {
+                p = make_double2(p.x + a.coi1[i] * g1.x, p.y + a.coi1[i] * g1.y);
+            }
+            m.P(ic, j) = p;
+        }
+        __syncthreads();
+    }
+    const int nh = n1m / 2;
+    for (int t = threadIdx.x; t < nh * n2m; t += nt) {          // odd lines
+        const int i = 1 + 2 * (t % nh), j = 1 + t / nh;
+        const double2 pm = m.P(a.imm[i], j), pp = m.P(a.ipm[i], j), r = m.B(i, j);
+        const double sx = a.aw[i] * pm.x + a.ae[i] * pp.x, sy = a.aw[i] * pm.y + a.ae[i] * pp.y;
+        m.G(i, j) = make_double2(r.x - oldv * sx, r.y - oldv * sy);
+    }
+    __syncthreads();
+    mg_trdiag(m, 1, n1m);
+    __syncthreads();
+    const double2 tt = m.kv == 1 ? m.G(1, n2m - 1) : make_double2(0.0, 0.0);
+    for (int t = threadIdx.x; t < nh * n2m; t += nt) {          // even lines, with the pin shift
+        const int i = 2 + 2 * (t % nh), j = 1 + t / nh;
+        const int ip = a.ipm[i];
+        double2 gm = m.G(a.imm[i], j), gp = m.G(ip, j);
+        gm = make_double2(gm.x - tt.x, gm.y - tt.y);            // shifted before use
+        if (ip < i) gp = make_double2(gp.x - tt.x, gp.y - tt.y);   // x-periodic wrap: shifted already
+        const double2 r = m.B(i, j);
+        m.G(i, j) = make_double2(r.x - a.aw[i] * gm.x - a.ae[i] * (gp.x - tt.x),
+                                 r.y - a.aw[i] * gm.y - a.ae[i] * (gp.y - tt.y));
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nh * n2m; t += nt) {          // then shift the odd lines
+        const int i = 1 + 2 * (t % nh), j = 1 + t / nh;
+        const double2 g = m.G(i, j);
+        m.G(i, j) = make_double2(g.x - tt.x, g.y - tt.y);
+    }
+    __syncthreads();
+    mg_trdiag(m, 2, n1m);
+    __syncthreads();
+    double mx = 0.0;
+    for (int t = threadIdx.x; t < n1m * n2m; t += nt) {
+        const int i = 1 + t % n1m, j = 1 + t / n1m;
+        const double2 d = mg_defect(m, m.B(i, j), m.gg, a.ldg, i, j);
+        m.R(i, j) = d;
+        mx = fmax(mx, hypot(d.x, d.y));
+        m.P(i, j) = m.G(i, j);
+    }
+    const double sumres = block_max(mx);
+    __syncthreads();
+    if (sumres < test) return sumres;
+    const int nc = ce - cl + 1;                                  // restrict
+    for (int t = threadIdx.x; t < nc * n2m; t += nt) {
+        const int i = cl + t % nc, j = 1 + t / nc, ic = 2 * (i - cl) + 1;
+        const double2 r1 = m.R(ic, j), r2 = m.R(ic + 1, j);
+        m.R(i, j) = make_double2(r1.x * a.cor1[i] + r2.x * a.cor2[i], r1.y * a.cor1[i] + r2.y * a.cor2[i]);
+    }
+    __syncthreads();
+    return sumres;
+}
+
+// relax, poiss_z_ft.f90:466-511 (zebra version)
+__device__ void mg_relax(const Mode &m, int ilev, double oldv, int iiter) {
+    const MgArgs &a = m.a;
+    const int ibg = a.iimg[ilev][0], iend = a.iimg[ilev][1], n2m = a.n2m, nt = blockDim.x;
+    const int nodd = (iend - ibg) / 2 + 1, nev = iend > ibg ? (iend - ibg - 1) / 2 + 1 : 0;
+    for (int it = 0; it < iiter; it++) {
+        const double ov = it == 0 ? oldv : 1.0;
+        for (int t = threadIdx.x; t < nodd * n2m; t += nt) {
+            const int i = ibg + 2 * (t % nodd), j = 1 + t / nodd;
+            const double2 gm = m.G(a.imm[i], j), gp = m.G(a.ipm[i], j), r = m.R(i, j);
+            const double sx = a.aw[i] * gm.x + a.ae[i] * gp.x, sy = a.aw[i] * gm.y + a.ae[i] * gp.y;
+            m.G(i, j) = make_double2(r.x - ov * sx, r.y - ov * sy);
+        }
+        __syncthreads();
+        mg_trdiag(m, ibg, iend);
+        __syncthreads();
+        for (int t = threadIdx.x; t < nev * n2m; t += nt) {
+            const int i = ibg + 1 + 2 * (t % nev), j = 1 + t / nev;
+            const double2 gm = m.G(a.imm[i], j), gp = m.G(a.ipm[i], j), r = m.R(i, j);
+            m.G(i, j) = make_double2(r.x - a.aw[i] * gm.x - a.ae[i] * gp.x, r.y - a.aw[i] * gm.y - a.ae[i] * gp.y);
+        }
+        __syncthreads();
+        mg_trdiag(m, ibg + 1, iend);
+        __syncthreads();
+    }
+}
+
+// godown, poiss_z_ft.f90:438-463
+__device__ void mg_godown(const Mode &m, int ilev) {
+    const MgArgs &a = m.a;
+    const int ibg = a.iimg[ilev][0], iend = a.iimg[ilev][1], n2m = a.n2m, nt = blockDim.x;
+    const int nf = iend - ibg + 1;
+    for (int t = threadIdx.x; t < nf * n2m; t += nt) {
+        const int i = ibg + t % nf, j = 1 + t / nf;
+        m.R(i, j) = mg_defect(m, m.R(i, j), m.gg, a.ldg, i, j);
+    }
+    __syncthreads();
+    const int cl = a.iimg[ilev - 1][0], nc = a.iimg[ilev - 1][1] - cl + 1;
+    for (int t = threadIdx.x; t < nc * n2m; t += nt) {
+        const int i = cl + t % nc, j = 1 + t / nc, f = ibg + 2 * (i - cl);
+        const double2 r1 = m.R(f, j), r2 = m.R(f + 1, j);
+        m.R(i, j) = make_double2(r1.x * a.cor1[i] + r2.x * a.cor2[i], r1.y * a.cor1[i] + r2.y * a.cor2[i]);
+    }
+    __syncthreads();
+}
+
+// goup, poiss_z_ft.f90:411-435
+__device__ void mg_goup(const Mode &m, int ilev) {
+    const MgArgs &a = m.a;
+    const int cl = a.iimg[ilev][0], ce = a.iimg[ilev][1], n2m = a.n2m, nt = blockDim.x;
+    const int fb = a.iimg[ilev + 1][0], nc = ce - cl + 1;
+    for (int t = threadIdx.x; t < nc * n2m; t += nt) {
+        const int i = cl + t % nc, j = 1 + t / nc, f = fb + 1 + 2 * (i - cl);
+        double2 g = m.G(f, j);
+        const double2 g1 = m.G(i, j);
+        if (i < ce) {
+            const double2 g2 = m.G(a.ipm[i], j);
+            g = make_double2(g.x + a.coi1[i] * g1.x + a.coi2[i] * g2.x, g.y + a.coi1[i] * g1.y + a.coi2[i] * g2.y);
+        } else {
+            g = make_double2(g.x + a.coi1[i] * g1.x, g.y + a.coi1[i] * g1.y);
+        }
+        m.G(f, j) = g;
+    }
+    __syncthreads();
+}
+
+// mg2d, poiss_z_ft.f90:239-299
+__device__ int mg_mg2d(const Mode &m, double test) {
+    const MgArgs &a = m.a;
+    double sumres = mg_toplevel(m, 0, 0.0, test);
+    if (sumres < test) return 0;
+    for (int kk = 1; kk <= a.mgitr; kk++) {
+        for (int ilev = a.nlev - 1; ilev >= 1; ilev--) {
+            mg_relax(m, ilev, 0.0, 1);
+            mg_godown(m, ilev);
+        }
+        mg_relax(m, 0, 0.0, a.nbli);
+        for (int ilev = 0; ilev <= a.nlev - 2; ilev++) {
+            mg_goup(m, ilev);
+            mg_relax(m, ilev + 1, 1.0, 1);
+        }
+        sumres = mg_toplevel(m, 1, 1.0, test);
+        if (sumres < test) return kk;
+    }
+    return a.mgitr;       // iteration limit: the reference warns and goes on
+}
+
+// gsor2d + resid3, poiss_z_ft.f90:513-641 (pc is the iterate u)
+__device__ int mg_gsor2d(const Mode &m, double test) {
+    const MgArgs &a = m.a;
+    const int n1m = a.n1m, n2m = a.n2m, nt = blockDim.x, nh = n1m / 2;
+    const double ww = a.wwsor, ww2 = 1.0 - ww;
+    for (int kk = 0; kk <= a.mgitr; kk++) {
+        const double ov = kk == 0 ? 0.0 : 1.0, o2 = ov * ww2;
+        for (int half = 0; half < 2; half++) {
+            const double f = half == 0 ? ov : 1.0;
+            for (int t = threadIdx.x; t < nh * n2m; t += nt) {
+                const int i = 1 + half + 2 * (t % nh), j = 1 + t / nh;
+                const double2 um = m.P(a.imm[i], j), up = m.P(a.ipm[i], j), r = m.B(i, j);
+                const double sx = a.aw[i] * um.x + a.ae[i] * up.x, sy = a.aw[i] * um.y + a.ae[i] * up.y;
+                m.G(i, j) = make_double2(r.x - f * sx, r.y - f * sy);
+            }
+            __syncthreads();
+            mg_trdiag(m, 1 + half, n1m);
+            __syncthreads();
+            for (int t = threadIdx.x; t < nh * n2m; t += nt) {
+                const int i = 1 + half + 2 * (t % nh), j = 1 + t / nh;
+                const double2 g = m.G(i, j), u = m.P(i, j);
+                m.P(i, j) = make_double2(ww * g.x + o2 * u.x, ww * g.y + o2 * u.y);
+            }
+            __syncthreads();
+        }
+        double mx = 0.0;
+        for (int t = threadIdx.x; t < n1m * n2m; t += nt) {
+            const int i = 1 + t % n1m, j = 1 + t / n1m;
+            const double2 d = mg_defect(m, m.B(i, j), m.pc, a.ldp, i, j);
+            mx = fmax(mx, hypot(d.x, d.y));
+        }
+        const double e = block_max(mx);
+        __syncthreads();
+        if (e < test) return kk;
+    }
+    return a.mgitr;
+}
+
+__global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes(MgArgs a) {
+    const int kv = blockIdx.x + 1;
+    Mode m(a, kv);
+    const double test = a.S->mg_test;
+    const int it = kv <= a.imgsor ? mg_mg2d(m, test) : mg_gsor2d(m, test);
+    // the mode's solution replaces its right-hand side (ccap(i,j,kkk) = cp(i,j))
+    double2 *out = a.ccap + (size_t)a.n1m * a.n2m * (kv - 1);
+    for (int t = threadIdx.x; t < a.n1m * a.n2m; t += blockDim.x) {
+        const int i = 1 + t % a.n1m, j = 1 + t / a.n1m;
+        out[t] = m.P(i, j);
+    }
+    if (threadIdx.x == 0) {
+        a.iters[kv - 1] = it;
+        atomicMax((unsigned long long *)&a.S->poisson_iters[a.slot], (unsigned long long)it);
+    }
+}
+
+// convergence criterion of the substep: test1 / n3mh * n3m * 0.8 (poiss_z_ft.f90:166), test1 in 2-D
+__global__ void k_zft_begin(DScal *S, int slot, int n3m, int n3mh) {
+    S->poisson_iters[slot] = 0;
+    S->mg_test = n3m == 1 ? S->test1 : S->test1 / (double)n3mh * (double)n3m * 0.8;
+}
+
+// ---------------------------------------------------------------- host side
+static int set_up_tables(lesgpu_case *c, MgTables &T, std::vector<double> &h_ak3) {
+    const DGrid &g = c->kp.g;
+    const lesgpu_config &cf = c->cfg;
+    const int n1m = g.n1m, n2m = g.n2m, n3m = g.n3m, n3mh = g.n3mh, n1md = 2 * n1m, nlev = (int)cf.nlev;
+    const int n1 = g.n1;
+    const lesgpu_grid *hg = c->h_grid;
+    // host copies in Fortran index
+    auto v0 = [&](const double *p, int n) { std::vector<double> v(n + 2, 0.0); for (int q = 0; q <= n; q++) v[q] = p[q]; return v; };
+    auto v1 = [&](const double *p, int n) { std::vector<double> v(n + 2, 0.0); for (int q = 1; q <= n; q++) v[q] = p[q - 1]; return v; };
+    auto i1 = [&](const int64_t *p, int n) { std::vector<long long> v(n + 2, 0); for (int q = 1; q <= n; q++) v[q] = p[q - 1]; return v; };
+    std::vector<double> x = v1(hg->x, n1), xmp = v0(hg->xmp, n1);
+    std::vector<double> c2cxi = v0(hg->c2cxi, n1), f2fxi = v0(hg->f2fxi, n1), c2cyi = v0(hg->c2cyi, g.n2), f2fyi = v0(hg->f2fyi, g.n2);
+    std::vector<double> f2fzi = v0(hg->f2fzi, g.n3);
+    std::vector<long long> ipv = i1(hg->ipv, n1m), jpv = i1(hg->jpv, n2m);
+    std::vector<long long> fixil = i1(hg->fixil, n1m), fixiu = i1(hg->fixiu, n1m), fixjl = i1(hg->fixjl, n2m), fixju = i1(hg->fixju, n2m);
+
+    const size_t nv = (size_t)n1md + 2, na = (size_t)n1md * n2m * n3mh;
+    std::vector<double> aw(nv, 0.0), ae(nv, 0.0), as(n2m + 2, 0.0), an(n2m + 2, 0.0);
+    std::vector<double> coi1(nv, 0.0), coi2(nv, 0.0), cor1(nv, 0.0), cor2(nv, 0.0);
+    std::vector<int> ipm(nv, 0), imm(nv, 0);
+    std::vector<double> ac(na, 0.0), bet(na, 0.0), gam(na, 0.0);
+    h_ak3.assign(n3mh + 2, 0.0);
+    auto AC = [&](int i, int j, int k) -> double & { return ac[(size_t)(i - 1) + (size_t)n1md * ((size_t)(j - 1) + (size_t)n2m * (size_t)(k - 1))]; };
+    // pmat
+    for (int i = 1; i <= n1m; i++) {
+        long long ip = ipv[i];
+        aw[i] = (1.0 - (double)fixil[i]) * c2cxi[i] * f2fxi[i];
+        ae[i] = (1.0 - (double)fixiu[i]) * c2cxi[ip] * f2fxi[i];
+    }
+    for (int j = 1; j <= n2m; j++) {
+        long long jp = jpv[j];
+        as[j] = (1.0 - (double)fixjl[j]) * c2cyi[j] * f2fyi[j];
+        an[j] = (1.0 - (double)fixju[j]) * c2cyi[jp] * f2fyi[j];
+    }
+    for (int j = 1; j <= n2m; j++)
+        for (int i = 1; i <= n1m; i++) AC(i, j, 1) = -1.0 * (aw[i] + ae[i] + as[j] + an[j]);
+    if (n3m > 1) {
+        const double pi = acos(-1.0);
+        for (int k = 1; k <= n3mh; k++)
+            h_ak3[k] = 2.0 * (1.0 - cos(2.0 * (double)(k - 1) * pi / (double)n3m)) * f2fzi[1] * f2fzi[1];
+    }
+    for (int k = 2; k <= n3mh; k++)
+        for (int j = 1; j <= n2m; j++)
+            for (int i = 1; i <= n1m; i++) AC(i, j, k) = AC(i, j, 1) - h_ak3[k];
+    // coefmg
+    const int minrow = n1m / (1 << nlev);
+    std::vector<double> xmpm(nv, 0.0), iwz(nv, 0.0), iez(nv, 0.0);
+    int (&iimg)[kMaxLev + 1][3] = T.iimg;
+    iimg[nlev][0] = 1; iimg[nlev][1] = n1m; iimg[nlev][2] = n1m;
+    for (int i = 1; i <= n1m; i++) xmpm[i] = xmp[i];
+    for (int ilev = nlev - 1; ilev >= 0; ilev--) {
+        iimg[ilev][0] = iimg[ilev + 1][0] + iimg[ilev + 1][2];
+        iimg[ilev][2] = minrow * (1 << ilev);
+        iimg[ilev][1] = iimg[ilev][0] + iimg[ilev][2] - 1;
+        const int ibg = iimg[ilev][0], iend = iimg[ilev][1], isp = 1 << (nlev - ilev);
+        int ic = 0;
+        for (int i = ibg; i <= iend; i++) {
+            ic++;
+            xmpm[i] = 0.5 * (x[ic * isp + 1] + x[(ic - 1) * isp + 1]);
+            iwz[i] = (double)(1 - ibg / i);
+            iez[i] = (double)(1 - i / iend);
+        }
+        ic = 0;
+        for (int i = ibg; i <= iend; i++) {
+            ic++;
+            const double w = x[ic * isp + 1] - x[(ic - 1) * isp + 1];
+            aw[i] = iwz[i] / ((xmpm[i] - xmpm[i - 1]) * w);
+            ae[i] = iez[i] / ((xmpm[i + 1] - xmpm[i]) * w);
+        }
+        for (int j = 1; j <= n2m; j++)
+            for (int i = ibg; i <= iend; i++) AC(i, j, 1) = -1.0 * (aw[i] + ae[i] + as[j] + an[j]);
+        for (int k = 2; k <= n3mh; k++)
+            for (int j = 1; j <= n2m; j++)
+                for (int i = ibg; i <= iend; i++) AC(i, j, k) = AC(i, j, 1) - h_ak3[k];
+    }
+    for (int ilev = nlev; ilev >= 1; ilev--) {
+        int ibgh = iimg[ilev][0];
+        for (int i = iimg[ilev - 1][0]; i <= iimg[ilev - 1][1]; i++) {
+            cor1[i] = (xmpm[ibgh + 1] - xmpm[i]) / (xmpm[ibgh + 1] - xmpm[ibgh]);
+            cor2[i] = 1.0 - cor1[i];
+            ibgh += 2;
+        }
+    }
+    for (int ilev = 0; ilev <= nlev - 1; ilev++) {
+        int ibgh = iimg[ilev + 1][0] + 1;
+        for (int i = iimg[ilev][0]; i <= iimg[ilev][1] - 1; i++) {
+            coi1[i] = (xmpm[i + 1] - xmpm[ibgh]) / (xmpm[i + 1] - xmpm[i]);
+            coi2[i] = 1.0 - coi1[i];
+            ibgh += 2;
+        }
+        coi1[iimg[ilev][1]] = 1.0;
+    }
+    for (int ilev = nlev; ilev >= 0; ilev--)
+        for (int i = iimg[ilev][0]; i <= iimg[ilev][1]; i++) { ipm[i] = i + 1; imm[i] = i - 1; }
+    if (cf.xprdic == 1) {
+        for (int ilev = nlev; ilev >= 0; ilev--) { ipm[iimg[ilev][1]] = iimg[ilev][0]; imm[iimg[ilev][0]] = iimg[ilev][1]; }
+        for (int ilev = nlev - 1; ilev >= 0; ilev--) {
+            const int ibg = iimg[ilev][0], iend = iimg[ilev][1], isp = 1 << (nlev - ilev);
+            const double vdx = xmpm[ibg] - x[1] + x[n1] - xmpm[iend];
+            aw[ibg] = 1.0 / (vdx * (x[1 + isp] - x[1]));
+            ae[iend] = 1.0 / (vdx * (x[n1] - x[n1 - isp]));
+        }
+        for (int ilev = nlev - 1; ilev >= 0; ilev--) {
+            for (int j = 1; j <= n2m; j++)
+                for (int i = iimg[ilev][0]; i <= iimg[ilev][1]; i++) AC(i, j, 1) = -1.0 * (aw[i] + ae[i] + as[j] + an[j]);
+            for (int k = 2; k <= n3mh; k++)
+                for (int j = 1; j <= n2m; j++)
+                    for (int i = iimg[ilev][0]; i <= iimg[ilev][1]; i++) AC(i, j, k) = AC(i, j, 1) - h_ak3[k];
+        }
+        for (int ilev = 0; ilev <= nlev - 1; ilev++) {
+            const int ibg = iimg[ilev][0], iend = iimg[ilev][1];
+            const double vdx = xmpm[ibg] - x[1] + x[n1] - xmpm[iend];
+            coi2[iend] = (xmpm[iimg[ilev + 1][1]] - xmpm[iend]) / vdx;
+            coi1[iend] = 1.0 - coi2[iend];
+        }
+    }
+    // poisinit: LU factors of every level's y-operator
+    auto IX3 = [&](int i, int j, int k) { return (size_t)(i - 1) + (size_t)n1md * ((size_t)(j - 1) + (size_t)n2m * (size_t)(k - 1)); };
+    for (int ilev = 0; ilev <= nlev; ilev++)
+        for (int k = 1; k <= n3mh; k++) {
+            for (int i = iimg[ilev][0]; i <= iimg[ilev][1]; i++) bet[IX3(i, 1, k)] = 1.0 / ac[IX3(i, 1, k)];
+            for (int j = 2; j <= n2m; j++)
+                for (int i = iimg[ilev][0]; i <= iimg[ilev][1]; i++) {
+                    gam[IX3(i, j, k)] = an[j - 1] * bet[IX3(i, j - 1, k)];
+                    bet[IX3(i, j, k)] = 1.0 / (ac[IX3(i, j, k)] - as[j] * gam[IX3(i, j, k)]);
+                }
+        }
+    // upload
+    bool ok = true;
+    auto up = [&](auto *&dst, const auto &v) {
+        using T0 = typename std::remove_reference<decltype(v[0])>::type;
+        if (cudaMalloc((void **)&dst, sizeof(T0) * v.size()) != cudaSuccess) { ok = false; return; }
+        cudaMemcpy(dst, v.data(), sizeof(T0) * v.size(), cudaMemcpyHostToDevice);
+    };
+    up(T.aw, aw); up(T.ae, ae); up(T.as, as); up(T.an, an);
+    up(T.coi1, coi1); up(T.coi2, coi2); up(T.cor1, cor1); up(T.cor2, cor2);
+    up(T.ipm, ipm); up(T.imm, imm); up(T.ac, ac); up(T.bet, bet); up(T.gam, gam);
+    return ok ? 0 : LESGPU_ERR_OOM;
+}
+
+int zft_init(lesgpu_case *c) {
+    const DGrid &g = c->kp.g;
+    const lesgpu_config &cf = c->cfg;
+    DPois &P = c->pois;
+    const int nlev = (int)cf.nlev;
+    if (nlev < 1 || nlev > kMaxLev || g.n1m % (1 << nlev) != 0) return LESGPU_ERR_CONFIG;
+    if (g.n3m > 1 && cf.zprdic != 1) return LESGPU_ERR_CONFIG;
+    if (cf.mgitr < 0 || cf.nbli < 1) return LESGPU_ERR_CONFIG;
+    int rc = make_plan(P.fz, g.n3m);
+    if (rc) return rc;
+    MgTables *T = new MgTables();
+    memset(T, 0, sizeof(*T));
+    P.mg = T;
+    T->n1md = 2 * g.n1m;
+    T->nlev = nlev;
+    std::vector<double> ak3;
+    rc = set_up_tables(c, *T, ak3);
+    if (rc) return rc;
+    const int ldp = g.n1m + 2, ldg = T->n1md + 1;
+    T->pc_plane = (long long)ldp * (g.n2m + 2);
+    T->gg_plane = (long long)ldg * (g.n2m + 2);
+    const size_t nm = (size_t)g.n3mh;
+    if (cudaMalloc(&T->pc, sizeof(double2) * T->pc_plane * nm) != cudaSuccess ||
+        cudaMalloc(&T->gg, sizeof(double2) * T->gg_plane * nm) != cudaSuccess ||
+        cudaMalloc(&T->rs, sizeof(double2) * T->gg_plane * nm) != cudaSuccess ||
+        cudaMalloc(&T->iters, sizeof(long long) * nm) != cudaSuccess ||
+        cudaMalloc(&P.ccap, sizeof(double2) * (size_t)g.n1m * g.n2m * nm) != cudaSuccess)
+        return LESGPU_ERR_OOM;
+    // the boundary rows and columns of pc / gg are read as zeros and never written
+    cudaMemset(T->pc, 0, sizeof(double2) * T->pc_plane * nm);
+    cudaMemset(T->gg, 0, sizeof(double2) * T->gg_plane * nm);
+    cudaMemset(T->rs, 0, sizeof(double2) * T->gg_plane * nm);
+    cudaMemset(T->iters, 0, sizeof(long long) * nm);
+    const int kMaxSmem = 200 * 1024;
+    if (cudaFuncSetAttribute(k_fft_z_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_fft_z_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem) != cudaSuccess)
+        return LESGPU_ERR_CUDA;
+    return 0;
+}
+
+void zft_free(lesgpu_case *c) {
+    MgTables *T = c->pois.mg;
+    if (!T) return;
+    void *ptrs[] = {T->aw, T->ae, T->as, T->an, T->coi1, T->coi2, T->cor1, T->cor2, T->ipm, T->imm,
+                    T->ac, T->bet, T->gam, T->pc, T->gg, T->rs, T->iters};
+    for (void *q : ptrs) cudaFree(q);
+    delete T;
+    c->pois.mg = nullptr;
+}
+
+void launch_zft(lesgpu_case *c, int msub) {
+    const DGrid &g = c->kp.g;
+    const lesgpu_config &cf = c->cfg;
+    DPois &P = c->pois;
+    MgTables *T = P.mg;
+    DevPlan pz = devplan(P.fz);
+    const int slot = (msub >= 1 && msub <= 3) ? msub - 1 : 0;
+    inst_begin(c, LESGPU_K_POISSON);
+    k_zft_begin<<<1, 1, 0, c->stream>>>(c->S, slot, g.n3m, g.n3mh);
+    const int Lz = fft_lines_per_block(g.n3m);
+    const size_t smz = (size_t)2 * (g.n3m > 1 ? g.n3m : 1) * Lz * sizeof(double2);
+    const dim3 gz((g.n1m + Lz - 1) / Lz, g.n2m);
+    const long long sk = (long long)g.n1m * g.n2m, sj = g.n1m;
+    k_fft_z_fwd<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
+    MgArgs a;
+    memset(&a, 0, sizeof(a));
+    a.n1m = g.n1m; a.n2m = g.n2m; a.n1md = T->n1md; a.nlev = T->nlev;
+    a.nbli = (int)cf.nbli; a.mgitr = (int)cf.mgitr; a.imgsor = (int)cf.imgsor; a.wwsor = cf.wwsor;
+    a.ldp = g.n1m + 2; a.ldg = T->n1md + 1;
+    memcpy(a.iimg, T->iimg, sizeof(a.iimg));
+    a.aw = T->aw; a.ae = T->ae; a.as = T->as; a.an = T->an;
+    a.coi1 = T->coi1; a.coi2 = T->coi2; a.cor1 = T->cor1; a.cor2 = T->cor2;
+    a.ipm = T->ipm; a.imm = T->imm; a.ac = T->ac; a.bet = T->bet; a.gam = T->gam;
+    a.ccap = P.ccap; a.pc = T->pc; a.gg = T->gg; a.rs = T->rs;
+    a.pc_plane = T->pc_plane; a.gg_plane = T->gg_plane;
+    a.iters = T->iters; a.S = c->S; a.slot = slot;
+    k_zft_modes<<<g.n3mh, kMgThreads, 0, c->stream>>>(a);
+    k_fft_z_inv<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
+    inst_end(c, LESGPU_K_POISSON);
+}
+
+}  // namespace lg

@@ -80,7 +80,7 @@ int check_config(const lesgpu_config *c, const lesgpu_grid *g) {
     if (g->n1m < 2 || g->n2m < 2 || g->n3m < 1) return LESGPU_ERR_ARG;
     if ((long long)(g->n1 + 1) * (g->n2 + 1) * (g->n3 + 1) > (1LL << 40)) return LESGPU_ERR_ARG;
     if (c->precision != LESGPU_PREC_FP64) return LESGPU_ERR_UNSUPPORTED;
-    if (c->poisson != LESGPU_POISSON_FTFT) return LESGPU_ERR_UNSUPPORTED;
+    if (c->poisson != LESGPU_POISSON_FTFT && c->poisson != LESGPU_POISSON_Z_FT) return LESGPU_ERR_UNSUPPORTED;
     if (c->imovingon != 0) return LESGPU_ERR_UNSUPPORTED;     // moving bodies: not built
     // poiss_ftft transforms x and z: both must be periodic
     if (c->poisson == LESGPU_POISSON_FTFT && (c->xprdic != 1 || c->zprdic != 1)) return LESGPU_ERR_CONFIG;
@@ -282,7 +282,9 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
     for (long long i = 0; i <= d.n1; i++) c->h_f2fx[i] = g->f2fxi[i];
     for (long long kk = 0; kk <= d.n3; kk++) c->h_f2fz[kk] = g->f2fzi[kk];
     if (!A.ok) { lesgpu_destroy(c); return LESGPU_ERR_OOM; }
+    c->h_grid = g;
     rc = poisson_init(c);
+    c->h_grid = nullptr;
     if (rc) { lesgpu_destroy(c); return rc; }
     if (cudaDeviceSynchronize() != cudaSuccess) { lesgpu_destroy(c); return LESGPU_ERR_CUDA; }
     *out = c;
@@ -486,7 +488,7 @@ static void enqueue_step(lesgpu_case *c, bool first) {
         if (g.iles == 1 && msub == 1) enqueue_sgs(c, first);
         enqueue_rhsnlhs(c, msub);
         launch_divgs(c);
-        launch_poisson(c);
+        launch_poisson(c, msub);
         if (g.ich == 1) launch_qvolcalc(c, 2);
         launch_ucalc(c);
         if (g.ich == 1) launch_qvolcalc(c, 0);
@@ -708,7 +710,7 @@ extern "C" int lesgpu_run_phase(lesgpu_case *c, int64_t phase, int64_t msub) {
         break;
     case LESGPU_PH_POISSON:
         cudaMemsetAsync(c->kp.f.phi, 0, sizeof(double) * c->kp.g.nt, c->stream);
-        launch_poisson(c);
+        launch_poisson(c, (int)msub);
         break;
     case LESGPU_PH_UCALC:
         if (g.ich == 1) launch_qvolcalc(c, 2);

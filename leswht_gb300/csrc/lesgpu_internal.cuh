@@ -65,6 +65,7 @@ struct DScal {
     double phiref;            // pcalc's outlet-plane mean of phi
     double cvol;              // tvolcorr's volume integral of 1/c*
     double cb[4];             // convective outlet: qin, ucoef, vwcoef, qratio
+    double mg_test;           // z_ft multigrid convergence criterion of the substep
     long long ntime, m, ihist;
     long long poisson_iters[3];
     int err;                  // device-side error flag (non-finite values etc.)
@@ -105,10 +106,14 @@ struct FftPlan {
     double2 *tw;              // exp(-2 pi i e / n), e = 0..n-1 (device)
 };
 
+struct MgTables;              // poiss_z_ft multigrid tables (k_mg.cu)
+
 struct DPois {
     double *ak1, *ak3;
-    double2 *ccap;            // spectrum (n1m, n3mh, n2m): i fastest, then k, then j
+    double2 *ccap;            // spectrum; ftft: (n1m, n3mh, n2m) i fastest, then k, then j;
+                              // z_ft: (n1m, n2m, n3mh), one x-y plane per z mode
     FftPlan fx, fz;
+    MgTables *mg;
 };
 
 struct KP {                   // everything a kernel may read, passed by value
@@ -206,6 +211,7 @@ struct lesgpu_case {
     int use_graph;
     // host mirrors of metrics used for init-time tables
     double *h_f2fx, *h_f2fy, *h_f2fz;
+    const lesgpu_grid *h_grid;  // the caller's grid, valid only inside lesgpu_create
     // kernel launches per step (from the captured graph)
     long long kernels_per_step;
     // event instrumentation of one kernel class (lesgpu_instrument)
@@ -249,7 +255,7 @@ void launch_adi_uvw(lesgpu_case *c);
 void launch_adi_t(lesgpu_case *c);
 void launch_sgs(lesgpu_case *c);
 void launch_sgs_t(lesgpu_case *c);
-void launch_poisson(lesgpu_case *c);
+void launch_poisson(lesgpu_case *c, int msub);
 int poisson_init(lesgpu_case *c);
 void poisson_free(lesgpu_case *c);
 void launch_sgs_zero_first(lesgpu_case *c, int thermal);

@@ -15,6 +15,7 @@ after readgeom, i.e. after the 15- and 6-decimal text round trips.
 """
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass
 from typing import Dict, List, Sequence, Tuple
 
@@ -269,6 +270,50 @@ def axis_vectors(grid_dat: str, xprdic: bool, yprdic: bool, zprdic: bool) -> Dic
         out[name] = (np.array([info[i]["coord"] for i in range(n + 1)]),
                      np.array([info[i]["center"] for i in range(n + 1)]))
     return out
+
+
+def clustered_lines(x0: float, x1: float, xc: float, n_cells: int, dmin: float) -> List[float]:
+    """n_cells + 1 gridlines on [x0, x1] clustered at xc (x0 <= xc <= x1):
+    on each side a sinh distribution x = xc +- L sinh(b s) / sinh(b), s in
+    [0, 1], whose first spacing at xc is dmin (uniform where the side's
+    plain spacing is already finer).  The cells are split between the sides
+    in proportion to their lengths."""
+    la, lb = xc - x0, x1 - xc
+    na = int(round(n_cells * la / (la + lb))) if la > 0 else 0
+    nb = n_cells - na
+
+    def side(length, n):
+        if n == 0:
+            return np.zeros(1)
+        s = np.arange(n + 1) / n
+        target = dmin * n / length          # b / sinh(b) for a first spacing of dmin
+        if target >= 1.0:
+            return length * s
+        lo, hi = 1.0e-6, 60.0
+        for _ in range(200):
+            mid = 0.5 * (lo + hi)
+            if mid / math.sinh(mid) > target:
+                lo = mid
+            else:
+                hi = mid
+        b = 0.5 * (lo + hi)
+        return length * np.sinh(b * s) / math.sinh(b)
+
+    left = xc - side(la, na)[::-1]
+    right = xc + side(lb, nb)
+    xs = np.concatenate([left, right[1:]])
+    xs[0], xs[-1] = x0, x1
+    return [float(v) for v in xs]
+
+
+def make_grid_lines(xs: Sequence[float], ys: Sequence[float], zs: Sequence[float],
+                    xprdic: bool, zprdic: bool, yprdic: bool = False) -> Tuple[GridMetrics, str, str]:
+    """Explicit gridlines -> grid.dat -> grid.bin -> metrics."""
+    nx, ny, nz = len(xs), len(ys), len(zs)
+    lx, ly, lz = xs[-1] - xs[0], ys[-1] - ys[0], zs[-1] - zs[0]
+    gdat = grid_dat_text(nx, ny, nz, lx, ly, lz, xs, ys, zs)
+    gbin = grid_bin_text(gdat, xprdic, yprdic, zprdic)
+    return read_grid_bin(gbin), gdat, gbin
 
 
 def make_grid(nx: int, ny: int, nz: int, lx: float, ly: float, lz: float,

@@ -252,7 +252,7 @@ int ref_get_report(ref_case *c, lesgpu_step_report *r)
     r->csgsts = c->csgsts; r->csgshf = c->csgshf;
     r->nutavg = c->nutavg; r->nutmax = c->nutmax; r->alpavg = c->alpavg; r->alpmax = c->alpmax;
     r->ubulk = c->ubulk; r->tbulk_fluid = c->tbulk_fluid; r->tbulk_solid = c->tbulk_solid;
-    r->poisson_iters[0] = c->poisson_iters;
+    for (int i = 0; i < 3; i++) r->poisson_iters[i] = c->poisson_iters[i];
     return 0;
 }
 
@@ -357,6 +357,8 @@ int ref_destroy(ref_case *c)
     for (int l = 0; l < 6; l++) free(c->kstar[l]);
     free(c->omega); free(c->nwall);
     free(c->ac); free(c->gam); free(c->bet);
+    free(c->aw); free(c->ae); free(c->as); free(c->an); free(c->coi1); free(c->coi2); free(c->cor1); free(c->cor2);
+    free(c->ipm); free(c->imm); free(c->ak1); free(c->ak3);
     ref_fft_plan_free(&c->fftx); ref_fft_plan_free(&c->fftz);
     free(c);
     return 0;

@@ -93,7 +93,7 @@ typedef struct ref_case {
     ll *ih1, *ih2, *kh1, *kh2, *il1, *il2, *kl1, *kl2;
     ll *ipm, *imm, *kpm, *kmm;
     double *ac, *gam, *bet;            /* z_ft: (n1md,n2m,n3mh); mgrd: (n1md,n2m,n3md) */
-    ll poisson_iters;
+    ll poisson_iters[3];               /* per substep: most cycles any mode took */
 
     /* scalars (mod_common) */
     ll ntime, ihist, m, msub;

@@ -243,6 +243,467 @@ static void ftft_poisson(ref_case *c)
     free(ccap);
 }
 
+/* -------------------------------------------------------- poiss_z_ft -- */
+/* FFT in z, then for every z-mode a 2-D problem in x-y solved by multigrid
+   semi-coarsened in x with zebra x-line relaxation (y-Thomas per line).
+   Level ilev occupies x slots iimg[ilev][0]..iimg[ilev][1] of the 1-D
+   coefficient vectors; the finest level nlev is 1..n1m. */
+
+#define ZAC(c, i, j, k) ((size_t)((i) - 1) + (size_t)(c)->n1md * ((size_t)((j) - 1) + (size_t)(c)->n2m * (size_t)((k) - 1)))
+
+/* pmat + mwavenumber, poiss_z_ft.f90:55-113 */
+static void zft_pmat(ref_case *c)
+{
+    ll n1m = c->n1m, n2m = c->n2m, n3m = c->n3m;
+    for (ll i = 1; i <= n1m; i++) {
+        ll ip = c->ipv[i];
+        c->aw[i] = (1.0 - (double)c->fixil[i]) * c->c2cxi[i] * c->f2fxi[i];
+        c->ae[i] = (1.0 - (double)c->fixiu[i]) * c->c2cxi[ip] * c->f2fxi[i];
+    }
+    for (ll j = 1; j <= n2m; j++) {
+        ll jp = c->jpv[j];
+        c->as[j] = (1.0 - (double)c->fixjl[j]) * c->c2cyi[j] * c->f2fyi[j];
+        c->an[j] = (1.0 - (double)c->fixju[j]) * c->c2cyi[jp] * c->f2fyi[j];
+    }
+    for (ll j = 1; j <= n2m; j++)
+        for (ll i = 1; i <= n1m; i++)
+            c->ac[ZAC(c, i, j, 1)] = -1.0 * (c->aw[i] + c->ae[i] + c->as[j] + c->an[j]);
+    if (n3m > 1) {
+        double pi = acos(-1.0);
+        for (ll k = 1; k <= c->n3mh; k++)
+            c->ak3[k] = 2.0 * (1.0 - cos(2.0 * (double)(k - 1) * pi / (double)n3m)) * c->f2fzi[1] * c->f2fzi[1];
+    }
+    for (ll k = 2; k <= c->n3mh; k++)
+        for (ll j = 1; j <= n2m; j++)
+            for (ll i = 1; i <= n1m; i++) c->ac[ZAC(c, i, j, k)] = c->ac[ZAC(c, i, j, 1)] - c->ak3[k];
+}
+
+/* coefmg, poiss_z_ft.f90:643-798 */
+static void zft_coefmg(ref_case *c)
+{
+    ll n1m = c->n1m, n2m = c->n2m, n1md = c->n1md, nlev = c->c.nlev, n1 = c->n1;
+    ll minrow = n1m / (1LL << nlev);
+    double *xmpm = ref_zalloc((size_t)n1md + 2), *iwz = ref_zalloc((size_t)n1md + 2), *iez = ref_zalloc((size_t)n1md + 2);
+    const double *x = c->x;
+    c->iimg[nlev][0] = 1; c->iimg[nlev][1] = n1m; c->iimg[nlev][2] = n1m;
+    for (ll i = 1; i <= n1m; i++) {
+        xmpm[i] = c->xmp[i];
+        iwz[i] = (double)(1 - 1 / i);
+        iez[i] = (double)(1 - i / n1m);
+    }
+    for (ll ilev = nlev - 1; ilev >= 0; ilev--) {
+        c->iimg[ilev][0] = c->iimg[ilev + 1][0] + c->iimg[ilev + 1][2];
+        c->iimg[ilev][2] = minrow * (1LL << ilev);
+        c->iimg[ilev][1] = c->iimg[ilev][0] + c->iimg[ilev][2] - 1;
+        ll ibg = c->iimg[ilev][0], iend = c->iimg[ilev][1], isp = 1LL << (nlev - ilev);
+        ll ic = 0;
+        for (ll i = ibg; i <= iend; i++) {
+            ic++;
+            xmpm[i] = 0.5 * (x[ic * isp + 1] + x[(ic - 1) * isp + 1]);
+            iwz[i] = (double)(1 - ibg / i);
+            iez[i] = (double)(1 - i / iend);
+        }
+        ic = 0;
+        for (ll i = ibg; i <= iend; i++) {
+            ic++;
+            double w = x[ic * isp + 1] - x[(ic - 1) * isp + 1];
+            c->aw[i] = iwz[i] / ((xmpm[i] - xmpm[i - 1]) * w);
+            c->ae[i] = iez[i] / ((xmpm[i + 1] - xmpm[i]) * w);
+        }
+        for (ll j = 1; j <= n2m; j++)
+            for (ll i = ibg; i <= iend; i++)
+                c->ac[ZAC(c, i, j, 1)] = -1.0 * (c->aw[i] + c->ae[i] + c->as[j] + c->an[j]);
+        for (ll k = 2; k <= c->n3mh; k++)
+            for (ll j = 1; j <= n2m; j++)
+                for (ll i = ibg; i <= iend; i++) c->ac[ZAC(c, i, j, k)] = c->ac[ZAC(c, i, j, 1)] - c->ak3[k];
+    }
+    for (ll ilev = nlev; ilev >= 1; ilev--) {
+        ll ibgh = c->iimg[ilev][0];
+        for (ll i = c->iimg[ilev - 1][0]; i <= c->iimg[ilev - 1][1]; i++) {
+            c->cor1[i] = (xmpm[ibgh + 1] - xmpm[i]) / (xmpm[ibgh + 1] - xmpm[ibgh]);
+            c->cor2[i] = 1.0 - c->cor1[i];
+            ibgh += 2;
+        }
+    }
+    for (ll ilev = 0; ilev <= nlev - 1; ilev++) {
+        ll ibgh = c->iimg[ilev + 1][0] + 1;
+        for (ll i = c->iimg[ilev][0]; i <= c->iimg[ilev][1] - 1; i++) {
+            c->coi1[i] = (xmpm[i + 1] - xmpm[ibgh]) / (xmpm[i + 1] - xmpm[i]);
+            c->coi2[i] = 1.0 - c->coi1[i];
+            ibgh += 2;
+        }
+        c->coi1[c->iimg[ilev][1]] = 1.0;
+    }
+    for (ll ilev = nlev; ilev >= 0; ilev--)
+        for (ll i = c->iimg[ilev][0]; i <= c->iimg[ilev][1]; i++) { c->ipm[i] = i + 1; c->imm[i] = i - 1; }
+    if (c->c.xprdic == 1) {
+        for (ll ilev = nlev; ilev >= 0; ilev--) {
+            ll ibg = c->iimg[ilev][0], iend = c->iimg[ilev][1];
+            c->ipm[iend] = ibg;
+            c->imm[ibg] = iend;
+        }
+        for (ll ilev = nlev - 1; ilev >= 0; ilev--) {
+            ll ibg = c->iimg[ilev][0], iend = c->iimg[ilev][1], isp = 1LL << (nlev - ilev);
+            double vdx = xmpm[ibg] - x[1] + x[n1] - xmpm[iend];
+            double sdx_b = x[1 + isp] - x[1], sdx_e = x[n1] - x[n1 - isp];
+            c->aw[ibg] = 1.0 / (vdx * sdx_b);
+            c->ae[iend] = 1.0 / (vdx * sdx_e);
+        }
+        for (ll ilev = nlev - 1; ilev >= 0; ilev--) {
+            for (ll j = 1; j <= n2m; j++)
+                for (ll i = c->iimg[ilev][0]; i <= c->iimg[ilev][1]; i++)
+                    c->ac[ZAC(c, i, j, 1)] = -1.0 * (c->aw[i] + c->ae[i] + c->as[j] + c->an[j]);
+            for (ll k = 2; k <= c->n3mh; k++)
+                for (ll j = 1; j <= n2m; j++)
+                    for (ll i = c->iimg[ilev][0]; i <= c->iimg[ilev][1]; i++)
+                        c->ac[ZAC(c, i, j, k)] = c->ac[ZAC(c, i, j, 1)] - c->ak3[k];
+        }
+        for (ll ilev = 0; ilev <= nlev - 1; ilev++) {
+            ll ibg = c->iimg[ilev][0], iend = c->iimg[ilev][1];
+            double vdx = xmpm[ibg] - x[1] + x[n1] - xmpm[iend];
+            c->coi2[iend] = (xmpm[c->iimg[ilev + 1][1]] - xmpm[iend]) / vdx;
+            c->coi1[iend] = 1.0 - c->coi2[iend];
+        }
+    }
+    free(xmpm); free(iwz); free(iez);
+}
+
+/* poisinit, poiss_z_ft.f90:18-52 */
+static int zft_init(ref_case *c)
+{
+    ll n1md = c->n1md, n2m = c->n2m, n3mh = c->n3mh, nlev = c->c.nlev;
+    if (nlev < 1 || nlev > 20 || c->n1m % (1LL << nlev) != 0) return LESGPU_ERR_CONFIG;
+    if (c->n3m > 1 && ref_fft_plan_init(&c->fftz, (int)c->n3m)) return LESGPU_ERR_ARG;
+    size_t nv = (size_t)n1md + 2, na = (size_t)n1md * (size_t)n2m * (size_t)n3mh;
+    c->aw = ref_zalloc(nv); c->ae = ref_zalloc(nv);
+    c->as = ref_zalloc((size_t)n2m + 2); c->an = ref_zalloc((size_t)n2m + 2);
+    c->coi1 = ref_zalloc(nv); c->coi2 = ref_zalloc(nv); c->cor1 = ref_zalloc(nv); c->cor2 = ref_zalloc(nv);
+    c->ipm = ref_izalloc(nv); c->imm = ref_izalloc(nv);
+    c->ak3 = ref_zalloc((size_t)n3mh + 2);
+    c->ac = ref_zalloc(na); c->gam = ref_zalloc(na); c->bet = ref_zalloc(na);
+    zft_pmat(c);
+    zft_coefmg(c);
+    for (ll ilev = 0; ilev <= nlev; ilev++)
+        for (ll k = 1; k <= n3mh; k++) {
+            for (ll i = c->iimg[ilev][0]; i <= c->iimg[ilev][1]; i++) c->bet[ZAC(c, i, 1, k)] = 1.0 / c->ac[ZAC(c, i, 1, k)];
+            for (ll j = 2; j <= n2m; j++)
+                for (ll i = c->iimg[ilev][0]; i <= c->iimg[ilev][1]; i++) {
+                    c->gam[ZAC(c, i, j, k)] = c->an[j - 1] * c->bet[ZAC(c, i, j - 1, k)];
+                    c->bet[ZAC(c, i, j, k)] = 1.0 / (c->ac[ZAC(c, i, j, k)] - c->as[j] * c->gam[ZAC(c, i, j, k)]);
+                }
+        }
+    return 0;
+}
+
+/* Work arrays of one mode: pc(0:n1,0:n2), rhs(n1,n2), resd(n1md,n2m), ggii(0:n1md,0:n2). */
+typedef struct {
+    ll ld_p, ld_g;            /* leading dimensions: n1+1 and n1md+1 */
+    cplx *pc, *rhs, *resd, *gg;
+} zmode;
+
+#define PC(z, i, j) (z)->pc[(size_t)(i) + (size_t)(z)->ld_p * (size_t)(j)]
+#define RH(z, i, j) (z)->rhs[(size_t)(i) + (size_t)(z)->ld_p * (size_t)(j)]
+#define RS(z, i, j) (z)->resd[(size_t)(i) + (size_t)(z)->ld_g * (size_t)(j)]
+#define GG(z, i, j) (z)->gg[(size_t)(i) + (size_t)(z)->ld_g * (size_t)(j)]
+
+static inline cplx cx_axpy(cplx y, double a, cplx x) { cplx r = { y.re - a * x.re, y.im - a * x.im }; return r; }
+
+/* trdiag1m, poiss_z_ft.f90:383-408: y-Thomas on x-lines l1, l1+2, ..., l2 (in place) */
+static void zft_trdiag(const ref_case *c, zmode *z, ll l1, ll l2, ll kv)
+{
+    ll n2m = c->n2m;
+    for (ll i = l1; i <= l2; i += 2) {
+        double b = c->bet[ZAC(c, i, 1, kv)];
+        GG(z, i, 1).re *= b; GG(z, i, 1).im *= b;
+    }
+    for (ll j = 2; j <= n2m; j++)
+        for (ll i = l1; i <= l2; i += 2) {
+            double b = c->bet[ZAC(c, i, j, kv)];
+            cplx t = cx_axpy(GG(z, i, j), c->as[j], GG(z, i, j - 1));
+            GG(z, i, j).re = t.re * b; GG(z, i, j).im = t.im * b;
+        }
+    for (ll j = n2m - 1; j >= 1; j--)
+        for (ll i = l1; i <= l2; i += 2)
+            GG(z, i, j) = cx_axpy(GG(z, i, j), c->gam[ZAC(c, i, j + 1, kv)], GG(z, i, j + 1));
+}
+
+/* rhs - aw*g(imm) - ae*g(ipm) - as*g(j-1) - an*g(j+1) - ac*g */
+static inline cplx zft_defect(const ref_case *c, cplx r, const cplx *g, ll ld, ll i, ll j, ll kv)
+{
+    const cplx *gm = &g[(size_t)c->imm[i] + (size_t)ld * (size_t)j], *gp = &g[(size_t)c->ipm[i] + (size_t)ld * (size_t)j];
+    const cplx *gs = &g[(size_t)i + (size_t)ld * (size_t)(j - 1)], *gn = &g[(size_t)i + (size_t)ld * (size_t)(j + 1)];
+    const cplx *gc = &g[(size_t)i + (size_t)ld * (size_t)j];
+    double ac = c->ac[ZAC(c, i, j, kv)];
+    r = cx_axpy(r, c->aw[i], *gm);
+    r = cx_axpy(r, c->ae[i], *gp);
+    r = cx_axpy(r, c->as[j], *gs);
+    r = cx_axpy(r, c->an[j], *gn);
+    r = cx_axpy(r, ac, *gc);
+    return r;
+}
+
+/* toplevel, poiss_z_ft.f90:302-380 (zebra version) */
+static void zft_toplevel(const ref_case *c, zmode *z, int id, double *sumres, double oldv, double test, ll kv)
+{
+    ll n1m = c->n1m, n2m = c->n2m, nlev = c->c.nlev;
+    if (id == 1) {
+        ll ic = 0;
+        for (ll i = c->iimg[nlev - 1][0]; i <= c->iimg[nlev - 1][1] - 1; i++) {
+            ic += 2;
+            for (ll j = 1; j <= n2m; j++) {
+                cplx p = PC(z, ic, j), a = GG(z, i, j), b = GG(z, c->ipm[i], j);
+                p.re = p.re + c->coi1[i] * a.re + c->coi2[i] * b.re;
+                p.im = p.im + c->coi1[i] * a.im + c->coi2[i] * b.im;
+                PC(z, ic, j) = p;
+            }
+        }
+        ll i = c->iimg[nlev - 1][1];
+        ic += 2;
+        for (ll j = 1; j <= n2m; j++) {
+            PC(z, ic, j).re = PC(z, ic, j).re + c->coi1[i] * GG(z, i, j).re;
+            PC(z, ic, j).im = PC(z, ic, j).im + c->coi1[i] * GG(z, i, j).im;
+        }
+    }
+    for (ll j = 1; j <= n2m; j++)
+        for (ll i = 1; i <= n1m; i += 2) {
+            cplx pm = PC(z, c->imm[i], j), pp = PC(z, c->ipm[i], j), r = RH(z, i, j);
+            double sre = c->aw[i] * pm.re + c->ae[i] * pp.re, sim = c->aw[i] * pm.im + c->ae[i] * pp.im;
+            GG(z, i, j).re = r.re - oldv * sre;
+            GG(z, i, j).im = r.im - oldv * sim;
+        }
+    zft_trdiag(c, z, 1, n1m, kv);
+    cplx tt = { 0.0, 0.0 };
+    if (kv == 1) tt = GG(z, 1, n2m - 1);
+    for (ll j = 1; j <= n2m; j++)
+        for (ll i = 2; i <= n1m; i += 2) {
+            GG(z, i - 1, j).re -= tt.re; GG(z, i - 1, j).im -= tt.im;
+            cplx gm = GG(z, c->imm[i], j), gp = GG(z, c->ipm[i], j), r = RH(z, i, j);
+            GG(z, i, j).re = r.re - c->aw[i] * gm.re - c->ae[i] * (gp.re - tt.re);
+            GG(z, i, j).im = r.im - c->aw[i] * gm.im - c->ae[i] * (gp.im - tt.im);
+        }
+    zft_trdiag(c, z, 2, n1m, kv);
+    double sr = 0.0;
+    for (ll j = 1; j <= n2m; j++)
+        for (ll i = 1; i <= n1m; i++) {
+            cplx d = zft_defect(c, RH(z, i, j), z->gg, z->ld_g, i, j, kv);
+            RS(z, i, j) = d;
+            double a = hypot(d.re, d.im);
+            if (a > sr) sr = a;
+            PC(z, i, j) = GG(z, i, j);
+        }
+    *sumres = sr;
+    if (sr < test || id == 2) return;
+    ll ic = -1;
+    for (ll i = c->iimg[nlev - 1][0]; i <= c->iimg[nlev - 1][1]; i++) {
+        ic += 2;
+        for (ll j = 1; j <= n2m; j++) {
+            cplx a = RS(z, ic, j), b = RS(z, ic + 1, j);
+            RS(z, i, j).re = a.re * c->cor1[i] + b.re * c->cor2[i];
+            RS(z, i, j).im = a.im * c->cor1[i] + b.im * c->cor2[i];
+        }
+    }
+}
+
+/* relax, poiss_z_ft.f90:466-511 (zebra version) */
+static void zft_relax(const ref_case *c, zmode *z, ll ilev, double oldv, ll iiter, ll kv)
+{
+    ll n2m = c->n2m, ibg = c->iimg[ilev][0], iend = c->iimg[ilev][1];
+    for (ll it = 0; it < iiter; it++) {
+        double ov = it == 0 ? oldv : 1.0;
+        for (ll j = 1; j <= n2m; j++)
+            for (ll i = ibg; i <= iend; i += 2) {
+                cplx gm = GG(z, c->imm[i], j), gp = GG(z, c->ipm[i], j), r = RS(z, i, j);
+                double sre = c->aw[i] * gm.re + c->ae[i] * gp.re, sim = c->aw[i] * gm.im + c->ae[i] * gp.im;
+                GG(z, i, j).re = r.re - ov * sre;
+                GG(z, i, j).im = r.im - ov * sim;
+            }
+        zft_trdiag(c, z, ibg, iend, kv);
+        for (ll j = 1; j <= n2m; j++)
+            for (ll i = ibg + 1; i <= iend; i += 2) {
+                cplx gm = GG(z, c->imm[i], j), gp = GG(z, c->ipm[i], j), r = RS(z, i, j);
+                GG(z, i, j).re = r.re - c->aw[i] * gm.re - c->ae[i] * gp.re;
+                GG(z, i, j).im = r.im - c->aw[i] * gm.im - c->ae[i] * gp.im;
+            }
+        zft_trdiag(c, z, ibg + 1, iend, kv);
+    }
+}
+
+/* godown, poiss_z_ft.f90:438-463: residual of level ilev, restricted to ilev-1 */
+static void zft_godown(const ref_case *c, zmode *z, ll ilev, ll kv)
+{
+    ll n2m = c->n2m;
+    for (ll j = 1; j <= n2m; j++)
+        for (ll i = c->iimg[ilev][0]; i <= c->iimg[ilev][1]; i++)
+            RS(z, i, j) = zft_defect(c, RS(z, i, j), z->gg, z->ld_g, i, j, kv);
+    ll ibg = c->iimg[ilev][0] - 2;
+    for (ll i = c->iimg[ilev - 1][0]; i <= c->iimg[ilev - 1][1]; i++) {
+        ibg += 2;
+        for (ll j = 1; j <= n2m; j++) {
+            cplx a = RS(z, ibg, j), b = RS(z, ibg + 1, j);
+            RS(z, i, j).re = a.re * c->cor1[i] + b.re * c->cor2[i];
+            RS(z, i, j).im = a.im * c->cor1[i] + b.im * c->cor2[i];
+        }
+    }
+}
+
+/* goup, poiss_z_ft.f90:411-435: coarse correction onto the even lines of ilev+1 */
+static void zft_goup(const ref_case *c, zmode *z, ll ilev)
+{
+    ll n2m = c->n2m, ibgh = c->iimg[ilev + 1][0] - 1;
+    for (ll i = c->iimg[ilev][0]; i <= c->iimg[ilev][1] - 1; i++) {
+        ibgh += 2;
+        for (ll j = 1; j <= n2m; j++) {
+            cplx g = GG(z, ibgh, j), a = GG(z, i, j), b = GG(z, c->ipm[i], j);
+            GG(z, ibgh, j).re = g.re + c->coi1[i] * a.re + c->coi2[i] * b.re;
+            GG(z, ibgh, j).im = g.im + c->coi1[i] * a.im + c->coi2[i] * b.im;
+        }
+    }
+    ll i = c->iimg[ilev][1];
+    ibgh += 2;
+    for (ll j = 1; j <= n2m; j++) {
+        GG(z, ibgh, j).re = GG(z, ibgh, j).re + c->coi1[i] * GG(z, i, j).re;
+        GG(z, ibgh, j).im = GG(z, ibgh, j).im + c->coi1[i] * GG(z, i, j).im;
+    }
+}
+
+/* mg2d, poiss_z_ft.f90:239-299; returns the number of V-cycles */
+static ll zft_mg2d(const ref_case *c, zmode *z, ll kv, double test, double oldv)
+{
+    ll nlev = c->c.nlev, kk = 0;
+    double sumres;
+    zft_toplevel(c, z, 0, &sumres, oldv, test, kv);
+    if (sumres < test) return 0;
+    for (kk = 1; kk <= c->c.mgitr; kk++) {
+        for (ll ilev = nlev - 1; ilev >= 1; ilev--) {
+            zft_relax(c, z, ilev, 0.0, 1, kv);
+            zft_godown(c, z, ilev, kv);
+        }
+        zft_relax(c, z, 0, 0.0, c->c.nbli, kv);
+        for (ll ilev = 0; ilev <= nlev - 2; ilev++) {
+            zft_goup(c, z, ilev);
+            zft_relax(c, z, ilev + 1, 1.0, 1, kv);
+        }
+        zft_toplevel(c, z, 1, &sumres, 1.0, test, kv);
+        if (sumres < test) return kk;
+    }
+    return kk;   /* iteration limit (the reference prints a warning and goes on) */
+}
+
+/* resid3, poiss_z_ft.f90:619-641 */
+static double zft_resid3(const ref_case *c, zmode *z, ll kv)
+{
+    double e = 0.0;
+    for (ll j = 1; j <= c->n2m; j++)
+        for (ll i = 1; i <= c->n1m; i++) {
+            cplx d = zft_defect(c, RH(z, i, j), z->pc, z->ld_p, i, j, kv);
+            double a = hypot(d.re, d.im);
+            if (a > e) e = a;
+        }
+    return e;
+}
+
+/* gsor2d, poiss_z_ft.f90:513-616: zebra line SOR on pc (= u) */
+static ll zft_gsor2d(const ref_case *c, zmode *z, ll kv, double test, double oldv)
+{
+    ll n1m = c->n1m, n2m = c->n2m;
+    double ww = c->c.wwsor, ww2 = 1.0 - ww;
+    for (ll kk = 0; kk <= c->c.mgitr; kk++) {
+        double ov = kk == 0 ? oldv : 1.0;
+        for (int half = 0; half < 2; half++) {
+            ll i0 = half == 0 ? 1 : 2;
+            for (ll j = 1; j <= n2m; j++)
+                for (ll i = i0; i <= n1m; i += 2) {
+                    cplx um = PC(z, c->imm[i], j), up = PC(z, c->ipm[i], j), r = RH(z, i, j);
+                    double sre = c->aw[i] * um.re + c->ae[i] * up.re, sim = c->aw[i] * um.im + c->ae[i] * up.im;
+                    double f = half == 0 ? ov : 1.0;
+                    GG(z, i, j).re = r.re - f * sre;
+                    GG(z, i, j).im = r.im - f * sim;
+                }
+            zft_trdiag(c, z, i0, n1m, kv);
+            double o2 = ov * ww2;
+            for (ll j = 1; j <= n2m; j++)
+                for (ll i = i0; i <= n1m; i += 2) {
+                    PC(z, i, j).re = ww * GG(z, i, j).re + o2 * PC(z, i, j).re;
+                    PC(z, i, j).im = ww * GG(z, i, j).im + o2 * PC(z, i, j).im;
+                }
+        }
+        if (zft_resid3(c, z, kv) < test) return kk;
+    }
+    return c->c.mgitr;
+}
+
+/* poisson, poiss_z_ft.f90:116-236 */
+static void zft_poisson(ref_case *c)
+{
+    ll n1 = c->n1, n2 = c->n2, n1m = c->n1m, n2m = c->n2m, n3m = c->n3m, n3mh = c->n3mh, n1md = c->n1md;
+    ll ld_p = n1 + 1, ld_g = n1md + 1;
+    size_t np = (size_t)ld_p * (size_t)(n2 + 1), ng = (size_t)ld_g * (size_t)(n2 + 1);
+    cplx *ccap = (cplx *)calloc(np * (size_t)n3mh, sizeof(cplx));
+    ll itmax = 0;
+    if (n3m == 1) {
+        for (ll j = 1; j <= n2m; j++)
+            for (ll i = 1; i <= n1m; i++) { ccap[(size_t)i + (size_t)ld_p * (size_t)j].re = c->divgsum[IX(c, i, j, 1)]; }
+    } else {
+        #pragma omp parallel
+        {
+            cplx *line = (cplx *)malloc(sizeof(cplx) * (size_t)n3m), *wk = (cplx *)malloc(sizeof(cplx) * 2 * (size_t)n3m);
+            #pragma omp for
+            for (ll j = 1; j <= n2m; j++)
+                for (ll i = 1; i <= n1m; i++) {
+                    for (ll k = 1; k <= n3m; k++) { line[k - 1].re = c->divgsum[IX(c, i, j, k)]; line[k - 1].im = 0.0; }
+                    ref_fft(&c->fftz, line, wk, -1);
+                    for (ll k = 1; k <= n3mh; k++) ccap[(size_t)i + (size_t)ld_p * (size_t)j + np * (size_t)(k - 1)] = line[k - 1];
+                }
+            free(line); free(wk);
+        }
+    }
+    double test = n3m == 1 ? c->test1 : c->test1 / (double)n3mh * (double)n3m * 0.8;
+    #pragma omp parallel reduction(max:itmax)
+    {
+        zmode z;
+        z.ld_p = ld_p; z.ld_g = ld_g;
+        z.pc = (cplx *)malloc(sizeof(cplx) * np);
+        z.resd = (cplx *)malloc(sizeof(cplx) * ng);
+        z.gg = (cplx *)malloc(sizeof(cplx) * ng);
+        #pragma omp for schedule(dynamic, 1)
+        for (ll kkk = 1; kkk <= n3mh; kkk++) {
+            z.rhs = ccap + np * (size_t)(kkk - 1);
+            memset(z.pc, 0, sizeof(cplx) * np);
+            memset(z.resd, 0, sizeof(cplx) * ng);
+            memset(z.gg, 0, sizeof(cplx) * ng);
+            ll it = kkk <= c->c.imgsor ? zft_mg2d(c, &z, kkk, test, 0.0) : zft_gsor2d(c, &z, kkk, test, 0.0);
+            if (it > itmax) itmax = it;
+            for (ll j = 1; j <= n2m; j++)
+                for (ll i = 1; i <= n1m; i++) z.rhs[(size_t)i + (size_t)ld_p * (size_t)j] = PC(&z, i, j);
+        }
+        free(z.pc); free(z.resd); free(z.gg);
+    }
+    if (n3m == 1) {
+        for (ll j = 1; j <= n2m; j++)
+            for (ll i = 1; i <= n1m; i++) c->phi[IX(c, i, j, 1)] = ccap[(size_t)i + (size_t)ld_p * (size_t)j].re;
+    } else {
+        #pragma omp parallel
+        {
+            cplx *line = (cplx *)malloc(sizeof(cplx) * (size_t)n3m), *wk = (cplx *)malloc(sizeof(cplx) * 2 * (size_t)n3m);
+            #pragma omp for
+            for (ll j = 1; j <= n2m; j++)
+                for (ll i = 1; i <= n1m; i++) {
+                    for (ll k = 1; k <= n3mh; k++) line[k - 1] = ccap[(size_t)i + (size_t)ld_p * (size_t)j + np * (size_t)(k - 1)];
+                    for (ll k = n3mh + 1; k <= n3m; k++) {
+                        cplx s = line[n3m + 2 - k - 1];
+                        s.im = -s.im;
+                        line[k - 1] = s;
+                    }
+                    ref_fft(&c->fftz, line, wk, 1);
+                    for (ll k = 1; k <= n3m; k++) c->phi[IX(c, i, j, k)] = line[k - 1].re;
+                }
+            free(line); free(wk);
+        }
+    }
+    free(ccap);
+    c->poisson_iters[c->msub >= 1 && c->msub <= 3 ? c->msub - 1 : 0] = itmax;
+}
+
 /* ------------------------------------------------------------ dispatch -- */
 int ref_poisinit(ref_case *c)
 {
@@ -252,6 +713,9 @@ int ref_poisinit(ref_case *c)
         if (ref_fft_plan_init(&c->fftx, (int)c->n1m) || ref_fft_plan_init(&c->fftz, (int)c->n3m)) return LESGPU_ERR_ARG;
         ftft_init(c);
         return 0;
+    case LESGPU_POISSON_Z_FT:
+        if (c->c.zprdic != 1 && c->n3m > 1) return LESGPU_ERR_CONFIG;
+        return zft_init(c);
     default:
         return LESGPU_ERR_UNSUPPORTED;
     }
@@ -259,9 +723,9 @@ int ref_poisinit(ref_case *c)
 
 void ref_poisson(ref_case *c)
 {
-    c->poisson_iters = 0;
     switch (c->c.poisson) {
     case LESGPU_POISSON_FTFT: ftft_poisson(c); break;
+    case LESGPU_POISSON_Z_FT: zft_poisson(c); break;
     default: break;
     }
 }
