@@ -20,6 +20,7 @@
 // of poisinit :18-52) are built on the host in the reference's arithmetic
 // order and uploaded once.
 #include "k_fft.cuh"
+#include <cooperative_groups.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -27,11 +28,13 @@
 
 namespace lg {
 
-constexpr int kMgThreads = 1024;
+constexpr int kMgThreads = 512;
+constexpr int kMC = 8;            // rows per lane: y lines of up to 32 * kMC = 256 cells
 constexpr int kMaxLev = 20;
 
 struct MgTables {
     int n1md, nlev;
+    int cs;                     // blocks per cluster (one cluster per z mode)
     int iimg[kMaxLev + 1][3];
     double *aw, *ae, *as, *an, *coi1, *coi2, *cor1, *cor2;   // 1-based
     int *ipm, *imm;
@@ -57,13 +60,19 @@ struct MgArgs {
 };
 
 // ------------------------------------------------------------- device side
+// One z mode is solved by one thread-block cluster; `tid`/`nt` number the
+// threads of the whole cluster and sync() is the cluster barrier (release /
+// acquire at cluster scope, so global writes of a phase are visible to every
+// block of the cluster in the next phase).
 struct Mode {
     const MgArgs &a;
     int kv;
+    int tid, nt;                        // thread index / count over the cluster
     double2 *pc, *gg, *rs;
     const double2 *rhs;                 // ccap plane of the mode, (i-1) + n1m*(j-1)
     size_t cb;                          // coefficient base of the mode
-    __device__ Mode(const MgArgs &a_, int kv_) : a(a_), kv(kv_) {
+    __device__ void sync() const { cooperative_groups::this_cluster().sync(); }
+    __device__ Mode(const MgArgs &a_, int kv_, int tid_, int nt_) : a(a_), kv(kv_), tid(tid_), nt(nt_) {
         pc = a.pc + a.pc_plane * (kv - 1);
         gg = a.gg + a.gg_plane * (kv - 1);
         rs = a.rs + a.gg_plane * (kv - 1);
@@ -81,75 +90,125 @@ __device__ __forceinline__ double2 axmy(double2 y, double s, double2 x) {   // y
     return make_double2(y.x - s * x.x, y.y - s * x.y);
 }
 
-// trdiag1m (poiss_z_ft.f90:383-408) on the x-lines l1, l1+2, ..., l2 of gg,
-// in place, one warp per line (see the file comment).
-__device__ void mg_trdiag(const Mode &m, int l1, int l2) {
-    const MgArgs &a = m.a;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (l2 < l1) return;
-    const int n2m = a.n2m, nl = (l2 - l1) / 2 + 1;
-    const int ch = (n2m + 31) / 32;
-    const int j0 = 1 + lane * ch, j1 = min(n2m, j0 + ch - 1);
-    const size_t sj = (size_t)a.n1md;
-    for (int li = warp; li < nl; li += nw) {
-        const int i = l1 + 2 * li;
-        const double *bet = a.bet + m.cb + (i - 1) - sj;     // bet(i, j) = bet[sj * j]
-        const double *gam = a.gam + m.cb + (i - 1) - sj;
-        // forward: y_j = (r_j - as_j y_{j-1}) bet_j  =  A_j y_{j-1} + B_j
-        double A = 1.0;
-        double2 Bv = make_double2(0.0, 0.0);
-        for (int j = j0; j <= j1; j++) {
-            const double bj = bet[sj * j], aj = -a.as[j] * bj;
-            const double2 r = m.G(i, j);
-            Bv = make_double2(aj * Bv.x + r.x * bj, aj * Bv.y + r.y * bj);
+// trdiag1m (poiss_z_ft.f90:383-408) of one x-line held in registers: lane
+// `lane` owns rows j0..j0+cnt-1 (v, with as_j, bet_j and gam_{j+1} beside
+// them; gam_{n2m+1} = 0).  Affine maps of the chunks are composed, joined by
+// a shuffle scan, then each chunk is re-run with the reference recurrence
+// from its scanned incoming value (see the file comment).
+template <int MC>
+__device__ __forceinline__ void line_solve(double2 (&v)[MC], const double (&as_)[MC], const double (&bt)[MC],
+                                           const double (&gm)[MC], int cnt, int lane) {
+    double A = 1.0;
+    double2 Bv = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int q = 0; q < MC; q++)
+        if (q < cnt) {
+            const double aj = -as_[q] * bt[q];
+            Bv = make_double2(aj * Bv.x + v[q].x * bt[q], aj * Bv.y + v[q].y * bt[q]);
             A = aj * A;
         }
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const double Ap = __shfl_up_sync(0xffffffffu, A, d);
-            const double bx = __shfl_up_sync(0xffffffffu, Bv.x, d), by = __shfl_up_sync(0xffffffffu, Bv.y, d);
-            if (lane >= d) { Bv = make_double2(A * bx + Bv.x, A * by + Bv.y); A = A * Ap; }
+    for (int d = 1; d < 32; d <<= 1) {
+        const double Ap = __shfl_up_sync(0xffffffffu, A, d);
+        const double bx = __shfl_up_sync(0xffffffffu, Bv.x, d), by = __shfl_up_sync(0xffffffffu, Bv.y, d);
+        if (lane >= d) { Bv = make_double2(A * bx + Bv.x, A * by + Bv.y); A = A * Ap; }
+    }
+    double yx = __shfl_up_sync(0xffffffffu, Bv.x, 1), yy = __shfl_up_sync(0xffffffffu, Bv.y, 1);
+    if (lane == 0) { yx = 0.0; yy = 0.0; }
+#pragma unroll
+    for (int q = 0; q < MC; q++)
+        if (q < cnt) {
+            yx = (v[q].x - as_[q] * yx) * bt[q];
+            yy = (v[q].y - as_[q] * yy) * bt[q];
+            v[q] = make_double2(yx, yy);
         }
-        double yx = __shfl_up_sync(0xffffffffu, Bv.x, 1), yy = __shfl_up_sync(0xffffffffu, Bv.y, 1);
-        if (lane == 0) { yx = 0.0; yy = 0.0; }
-        for (int j = j0; j <= j1; j++) {
-            const double bj = bet[sj * j];
-            const double2 r = m.G(i, j);
-            yx = (r.x - a.as[j] * yx) * bj;
-            yy = (r.y - a.as[j] * yy) * bj;
-            m.G(i, j) = make_double2(yx, yy);
-        }
-        __syncwarp();
-        // backward: x_j = y_j - gam_{j+1} x_{j+1}  =  C_j x_{j+1} + D_j
-        double C = 1.0;
-        double2 D = make_double2(0.0, 0.0);
-        for (int j = j1; j >= j0; j--) {
-            const double cj = j < n2m ? -gam[sj * (j + 1)] : 0.0;
-            const double2 y = m.G(i, j);
-            D = make_double2(cj * D.x + y.x, cj * D.y + y.y);
+    double C = 1.0;
+    double2 D = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int q = MC - 1; q >= 0; q--)
+        if (q < cnt) {
+            const double cj = -gm[q];
+            D = make_double2(cj * D.x + v[q].x, cj * D.y + v[q].y);
             C = cj * C;
         }
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const double Cn = __shfl_down_sync(0xffffffffu, C, d);
-            const double dx = __shfl_down_sync(0xffffffffu, D.x, d), dy = __shfl_down_sync(0xffffffffu, D.y, d);
-            if (lane + d < 32) { D = make_double2(C * dx + D.x, C * dy + D.y); C = C * Cn; }
+    for (int d = 1; d < 32; d <<= 1) {
+        const double Cn = __shfl_down_sync(0xffffffffu, C, d);
+        const double dx = __shfl_down_sync(0xffffffffu, D.x, d), dy = __shfl_down_sync(0xffffffffu, D.y, d);
+        if (lane + d < 32) { D = make_double2(C * dx + D.x, C * dy + D.y); C = C * Cn; }
+    }
+    double xx = __shfl_down_sync(0xffffffffu, D.x, 1), xy = __shfl_down_sync(0xffffffffu, D.y, 1);
+    if (lane == 31) { xx = 0.0; xy = 0.0; }
+#pragma unroll
+    for (int q = MC - 1; q >= 0; q--)
+        if (q < cnt) {
+            xx = v[q].x - gm[q] * xx;
+            xy = v[q].y - gm[q] * xy;
+            v[q] = make_double2(xx, xy);
         }
-        double xx = __shfl_down_sync(0xffffffffu, D.x, 1), xy = __shfl_down_sync(0xffffffffu, D.y, 1);
-        if (lane == 31) { xx = 0.0; xy = 0.0; }
-        for (int j = j1; j >= j0; j--) {
-            const double2 y = m.G(i, j);
-            if (j < n2m) {
-                const double gj = gam[sj * (j + 1)];
-                xx = y.x - gj * xx;
-                xy = y.y - gj * xy;
-            } else {
-                xx = y.x;
-                xy = y.y;
+}
+
+// How the right-hand side of a line is formed before its y solve.
+enum HalfKind {
+    H_ODD = 0,      // src - ov*(aw*nb(imm) + ae*nb(ipm))      toplevel/relax odd lines, gsor
+    H_EVEN = 1,     // src - aw*nb(imm) - ae*nb(ipm)            relax even lines
+    H_EVEN_TT = 2,  // src - aw*(nb(imm)-tt) - ae*(nb(ipm)-tt)   toplevel even lines (pinned mode)
+};
+
+// One zebra half sweep: lines l1, l1+2, ..., l2; one warp per line.
+//   src: the rhs plane (top level) or resd; nb: the array the neighbours come from
+//   out: G(i,j) = solution, or for gsor P(i,j) = ww*solution + o2*P(i,j)
+template <int MC>
+__device__ __noinline__ void mg_half(const Mode &m, int l1, int l2, int kind, bool src_rhs, const double2 *nb, int ldn,
+                        double ov, double2 tt, bool gsor, double ww, double o2) {
+    const MgArgs &a = m.a;
+    if (l2 < l1) return;
+    const int lane = m.tid & 31, warp = m.tid >> 5, nw = m.nt >> 5;
+    const int n2m = a.n2m, nl = (l2 - l1) / 2 + 1;
+    const int ch = (n2m + 31) / 32;
+    const int j0 = 1 + lane * ch;
+    const int cnt = max(0, min(ch, n2m - j0 + 1));
+    const size_t sj = (size_t)a.n1md;
+    for (int li = warp; li < nl; li += nw) {
+        const int i = l1 + 2 * li;
+        const int im = a.imm[i], ip = a.ipm[i];
+        const double aw = a.aw[i], ae = a.ae[i];
+        const double *bet = a.bet + m.cb + (i - 1);
+        const double *gam = a.gam + m.cb + (i - 1);
+        double2 v[MC];
+        double as_[MC], bt[MC], gm[MC];
+#pragma unroll
+        for (int q = 0; q < MC; q++)
+            if (q < cnt) {
+                const int j = j0 + q;
+                const double2 sr = src_rhs ? m.B(i, j) : m.R(i, j);
+                double2 nm = nb[im + (size_t)ldn * j], np = nb[ip + (size_t)ldn * j];
+                if (kind == H_ODD) {
+                    const double sx = aw * nm.x + ae * np.x, sy = aw * nm.y + ae * np.y;
+                    v[q] = make_double2(sr.x - ov * sx, sr.y - ov * sy);
+                } else if (kind == H_EVEN) {
+                    v[q] = make_double2(sr.x - aw * nm.x - ae * np.x, sr.y - aw * nm.y - ae * np.y);
+                } else {
+                    nm = make_double2(nm.x - tt.x, nm.y - tt.y);
+                    if (ip < i) np = make_double2(np.x - tt.x, np.y - tt.y);   // x-periodic wrap: shifted already
+                    v[q] = make_double2(sr.x - aw * nm.x - ae * (np.x - tt.x), sr.y - aw * nm.y - ae * (np.y - tt.y));
+                }
+                as_[q] = a.as[j];
+                bt[q] = bet[sj * (j - 1)];
+                gm[q] = j < n2m ? gam[sj * j] : 0.0;
             }
-            m.G(i, j) = make_double2(xx, xy);
-        }
-        __syncwarp();
+        line_solve<MC>(v, as_, bt, gm, cnt, lane);
+#pragma unroll
+        for (int q = 0; q < MC; q++)
+            if (q < cnt) {
+                const int j = j0 + q;
+                if (gsor) {
+                    const double2 u = m.P(i, j);
+                    m.P(i, j) = make_double2(ww * v[q].x + o2 * u.x, ww * v[q].y + o2 * u.y);
+                } else {
+                    m.G(i, j) = v[q];
+                }
+            }
     }
 }
 
@@ -164,26 +223,38 @@ __device__ __forceinline__ double2 mg_defect(const Mode &m, double2 src, const d
     return src;
 }
 
-__device__ double block_max(double v) {
+// Max over the cluster: warp shuffles, one value per block in shared memory,
+// then every thread reads every block's value through distributed shared
+// memory, in the same order, so all threads get the same result.
+__device__ double cluster_max(const Mode &m, double v) {
     __shared__ double sh[kMgThreads / 32];
+    __shared__ double blk;
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
-    __syncthreads();
     if (lane == 0) sh[w] = v;
-    __syncthreads();
+    m.sync();
+    if (threadIdx.x == 0) {
+        double r = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) r = fmax(r, sh[q]);
+        blk = r;
+    }
+    cl.sync();
     double r = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); q++) r = fmax(r, sh[q]);
+    for (int q = 0; q < (int)cl.num_blocks(); q++) r = fmax(r, *cl.map_shared_rank(&blk, q));
+    cl.sync();          // nobody overwrites blk before every block has read it
     return r;
 }
 
 // toplevel, poiss_z_ft.f90:302-380; returns the max-norm residual
 __device__ double mg_toplevel(const Mode &m, int id, double oldv, double test) {
     const MgArgs &a = m.a;
-    const int n1m = a.n1m, n2m = a.n2m, nt = blockDim.x;
+    const int n1m = a.n1m, n2m = a.n2m, nt = m.nt;
     const int cl = a.iimg[a.nlev - 1][0], ce = a.iimg[a.nlev - 1][1];
     if (id == 1) {   // prolong the coarse correction onto the even lines
         const int nc = ce - cl + 1;
-        for (int t = threadIdx.x; t < nc * n2m; t += nt) {
+        for (int t = m.tid; t < nc * n2m; t += nt) {
             const int i = cl + t % nc, j = 1 + t / nc, ic = 2 * (i - cl + 1);
             double2 p = m.P(ic, j);
             const double2 g1 = m.G(i, j);
@@ -195,111 +266,79 @@ __device__ double mg_toplevel(const Mode &m, int id, double oldv, double test) {
             }
             m.P(ic, j) = p;
         }
-        __syncthreads();
+        m.sync();
     }
     const int nh = n1m / 2;
-    for (int t = threadIdx.x; t < nh * n2m; t += nt) {          // odd lines
-        const int i = 1 + 2 * (t % nh), j = 1 + t / nh;
-        const double2 pm = m.P(a.imm[i], j), pp = m.P(a.ipm[i], j), r = m.B(i, j);
-        const double sx = a.aw[i] * pm.x + a.ae[i] * pp.x, sy = a.aw[i] * pm.y + a.ae[i] * pp.y;
-        m.G(i, j) = make_double2(r.x - oldv * sx, r.y - oldv * sy);
-    }
-    __syncthreads();
-    mg_trdiag(m, 1, n1m);
-    __syncthreads();
+    mg_half<kMC>(m, 1, n1m, H_ODD, true, m.pc, a.ldp, oldv, make_double2(0.0, 0.0), false, 0.0, 0.0);
+    m.sync();
     const double2 tt = m.kv == 1 ? m.G(1, n2m - 1) : make_double2(0.0, 0.0);
-    for (int t = threadIdx.x; t < nh * n2m; t += nt) {          // even lines, with the pin shift
-        const int i = 2 + 2 * (t % nh), j = 1 + t / nh;
-        const int ip = a.ipm[i];
-        double2 gm = m.G(a.imm[i], j), gp = m.G(ip, j);
-        gm = make_double2(gm.x - tt.x, gm.y - tt.y);            // shifted before use
-        if (ip < i) gp = make_double2(gp.x - tt.x, gp.y - tt.y);   // x-periodic wrap: shifted already
-        const double2 r = m.B(i, j);
-        m.G(i, j) = make_double2(r.x - a.aw[i] * gm.x - a.ae[i] * (gp.x - tt.x),
-                                 r.y - a.aw[i] * gm.y - a.ae[i] * (gp.y - tt.y));
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < nh * n2m; t += nt) {          // then shift the odd lines
-        const int i = 1 + 2 * (t % nh), j = 1 + t / nh;
-        const double2 g = m.G(i, j);
-        m.G(i, j) = make_double2(g.x - tt.x, g.y - tt.y);
-    }
-    __syncthreads();
-    mg_trdiag(m, 2, n1m);
-    __syncthreads();
+    mg_half<kMC>(m, 2, n1m, H_EVEN_TT, true, m.gg, a.ldg, 1.0, tt, false, 0.0, 0.0);
+    m.sync();
+    if (m.kv == 1)
+        for (int t = m.tid; t < nh * n2m; t += nt) {      // then shift the odd lines
+            const int i = 1 + 2 * (t % nh), j = 1 + t / nh;
+            const double2 g = m.G(i, j);
+            m.G(i, j) = make_double2(g.x - tt.x, g.y - tt.y);
+        }
+    m.sync();
     double mx = 0.0;
-    for (int t = threadIdx.x; t < n1m * n2m; t += nt) {
+    for (int t = m.tid; t < n1m * n2m; t += nt) {
         const int i = 1 + t % n1m, j = 1 + t / n1m;
         const double2 d = mg_defect(m, m.B(i, j), m.gg, a.ldg, i, j);
         m.R(i, j) = d;
-        mx = fmax(mx, hypot(d.x, d.y));
+        mx = fmax(mx, d.x * d.x + d.y * d.y);
         m.P(i, j) = m.G(i, j);
     }
-    const double sumres = block_max(mx);
-    __syncthreads();
+    const double sumres = sqrt(cluster_max(m, mx));
     if (sumres < test) return sumres;
     const int nc = ce - cl + 1;                                  // restrict
-    for (int t = threadIdx.x; t < nc * n2m; t += nt) {
+    for (int t = m.tid; t < nc * n2m; t += nt) {
         const int i = cl + t % nc, j = 1 + t / nc, ic = 2 * (i - cl) + 1;
         const double2 r1 = m.R(ic, j), r2 = m.R(ic + 1, j);
         m.R(i, j) = make_double2(r1.x * a.cor1[i] + r2.x * a.cor2[i], r1.y * a.cor1[i] + r2.y * a.cor2[i]);
     }
-    __syncthreads();
+    m.sync();
     return sumres;
 }
 
 // relax, poiss_z_ft.f90:466-511 (zebra version)
 __device__ void mg_relax(const Mode &m, int ilev, double oldv, int iiter) {
     const MgArgs &a = m.a;
-    const int ibg = a.iimg[ilev][0], iend = a.iimg[ilev][1], n2m = a.n2m, nt = blockDim.x;
-    const int nodd = (iend - ibg) / 2 + 1, nev = iend > ibg ? (iend - ibg - 1) / 2 + 1 : 0;
+    const int ibg = a.iimg[ilev][0], iend = a.iimg[ilev][1];
     for (int it = 0; it < iiter; it++) {
         const double ov = it == 0 ? oldv : 1.0;
-        for (int t = threadIdx.x; t < nodd * n2m; t += nt) {
-            const int i = ibg + 2 * (t % nodd), j = 1 + t / nodd;
-            const double2 gm = m.G(a.imm[i], j), gp = m.G(a.ipm[i], j), r = m.R(i, j);
-            const double sx = a.aw[i] * gm.x + a.ae[i] * gp.x, sy = a.aw[i] * gm.y + a.ae[i] * gp.y;
-            m.G(i, j) = make_double2(r.x - ov * sx, r.y - ov * sy);
-        }
-        __syncthreads();
-        mg_trdiag(m, ibg, iend);
-        __syncthreads();
-        for (int t = threadIdx.x; t < nev * n2m; t += nt) {
-            const int i = ibg + 1 + 2 * (t % nev), j = 1 + t / nev;
-            const double2 gm = m.G(a.imm[i], j), gp = m.G(a.ipm[i], j), r = m.R(i, j);
-            m.G(i, j) = make_double2(r.x - a.aw[i] * gm.x - a.ae[i] * gp.x, r.y - a.aw[i] * gm.y - a.ae[i] * gp.y);
-        }
-        __syncthreads();
-        mg_trdiag(m, ibg + 1, iend);
-        __syncthreads();
+        mg_half<kMC>(m, ibg, iend, H_ODD, false, m.gg, a.ldg, ov, make_double2(0.0, 0.0), false, 0.0, 0.0);
+        m.sync();
+        mg_half<kMC>(m, ibg + 1, iend, H_EVEN, false, m.gg, a.ldg, 1.0, make_double2(0.0, 0.0), false, 0.0, 0.0);
+        m.sync();
     }
 }
 
 // godown, poiss_z_ft.f90:438-463
 __device__ void mg_godown(const Mode &m, int ilev) {
     const MgArgs &a = m.a;
-    const int ibg = a.iimg[ilev][0], iend = a.iimg[ilev][1], n2m = a.n2m, nt = blockDim.x;
+    const int ibg = a.iimg[ilev][0], iend = a.iimg[ilev][1], n2m = a.n2m, nt = m.nt;
     const int nf = iend - ibg + 1;
-    for (int t = threadIdx.x; t < nf * n2m; t += nt) {
+    for (int t = m.tid; t < nf * n2m; t += nt) {
         const int i = ibg + t % nf, j = 1 + t / nf;
         m.R(i, j) = mg_defect(m, m.R(i, j), m.gg, a.ldg, i, j);
     }
-    __syncthreads();
+    m.sync();
     const int cl = a.iimg[ilev - 1][0], nc = a.iimg[ilev - 1][1] - cl + 1;
-    for (int t = threadIdx.x; t < nc * n2m; t += nt) {
+    for (int t = m.tid; t < nc * n2m; t += nt) {
         const int i = cl + t % nc, j = 1 + t / nc, f = ibg + 2 * (i - cl);
         const double2 r1 = m.R(f, j), r2 = m.R(f + 1, j);
         m.R(i, j) = make_double2(r1.x * a.cor1[i] + r2.x * a.cor2[i], r1.y * a.cor1[i] + r2.y * a.cor2[i]);
     }
-    __syncthreads();
+    m.sync();
 }
 
 // goup, poiss_z_ft.f90:411-435
 __device__ void mg_goup(const Mode &m, int ilev) {
     const MgArgs &a = m.a;
-    const int cl = a.iimg[ilev][0], ce = a.iimg[ilev][1], n2m = a.n2m, nt = blockDim.x;
+    const int cl = a.iimg[ilev][0], ce = a.iimg[ilev][1], n2m = a.n2m, nt = m.nt;
     const int fb = a.iimg[ilev + 1][0], nc = ce - cl + 1;
-    for (int t = threadIdx.x; t < nc * n2m; t += nt) {
+    for (int t = m.tid; t < nc * n2m; t += nt) {
         const int i = cl + t % nc, j = 1 + t / nc, f = fb + 1 + 2 * (i - cl);
         double2 g = m.G(f, j);
         const double2 g1 = m.G(i, j);
@@ -311,7 +350,7 @@ __device__ void mg_goup(const Mode &m, int ilev) {
         }
         m.G(f, j) = g;
     }
-    __syncthreads();
+    m.sync();
 }
 
 // mg2d, poiss_z_ft.f90:239-299
@@ -338,53 +377,46 @@ __device__ int mg_mg2d(const Mode &m, double test) {
 // gsor2d + resid3, poiss_z_ft.f90:513-641 (pc is the iterate u)
 __device__ int mg_gsor2d(const Mode &m, double test) {
     const MgArgs &a = m.a;
-    const int n1m = a.n1m, n2m = a.n2m, nt = blockDim.x, nh = n1m / 2;
+    const int n1m = a.n1m, n2m = a.n2m, nt = m.nt;
     const double ww = a.wwsor, ww2 = 1.0 - ww;
     for (int kk = 0; kk <= a.mgitr; kk++) {
         const double ov = kk == 0 ? 0.0 : 1.0, o2 = ov * ww2;
         for (int half = 0; half < 2; half++) {
             const double f = half == 0 ? ov : 1.0;
-            for (int t = threadIdx.x; t < nh * n2m; t += nt) {
-                const int i = 1 + half + 2 * (t % nh), j = 1 + t / nh;
-                const double2 um = m.P(a.imm[i], j), up = m.P(a.ipm[i], j), r = m.B(i, j);
-                const double sx = a.aw[i] * um.x + a.ae[i] * up.x, sy = a.aw[i] * um.y + a.ae[i] * up.y;
-                m.G(i, j) = make_double2(r.x - f * sx, r.y - f * sy);
-            }
-            __syncthreads();
-            mg_trdiag(m, 1 + half, n1m);
-            __syncthreads();
-            for (int t = threadIdx.x; t < nh * n2m; t += nt) {
-                const int i = 1 + half + 2 * (t % nh), j = 1 + t / nh;
-                const double2 g = m.G(i, j), u = m.P(i, j);
-                m.P(i, j) = make_double2(ww * g.x + o2 * u.x, ww * g.y + o2 * u.y);
-            }
-            __syncthreads();
+            mg_half<kMC>(m, 1 + half, n1m, H_ODD, true, m.pc, a.ldp, f, make_double2(0.0, 0.0), true, ww, o2);
+            m.sync();
         }
         double mx = 0.0;
-        for (int t = threadIdx.x; t < n1m * n2m; t += nt) {
+        for (int t = m.tid; t < n1m * n2m; t += nt) {
             const int i = 1 + t % n1m, j = 1 + t / n1m;
             const double2 d = mg_defect(m, m.B(i, j), m.pc, a.ldp, i, j);
-            mx = fmax(mx, hypot(d.x, d.y));
+            mx = fmax(mx, d.x * d.x + d.y * d.y);
         }
-        const double e = block_max(mx);
-        __syncthreads();
+        const double e = sqrt(cluster_max(m, mx));
         if (e < test) return kk;
     }
     return a.mgitr;
 }
 
 __global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes(MgArgs a) {
-    const int kv = blockIdx.x + 1;
-    Mode m(a, kv);
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const int cs = (int)cl.num_blocks();
+    const int kv = blockIdx.x / cs + 1;
+    // warp w of block r is the cluster's warp w*cs + r: consecutive lines and
+    // 32-point chunks go to different SMs (the work of a phase is spread over
+    // every block, each warp still touches 32 consecutive points)
+    const int gw = (int)(threadIdx.x >> 5) * cs + (int)cl.block_rank();
+    Mode m(a, kv, gw * 32 + (int)(threadIdx.x & 31), cs * blockDim.x);
     const double test = a.S->mg_test;
     const int it = kv <= a.imgsor ? mg_mg2d(m, test) : mg_gsor2d(m, test);
     // the mode's solution replaces its right-hand side (ccap(i,j,kkk) = cp(i,j))
     double2 *out = a.ccap + (size_t)a.n1m * a.n2m * (kv - 1);
-    for (int t = threadIdx.x; t < a.n1m * a.n2m; t += blockDim.x) {
+    for (int t = m.tid; t < a.n1m * a.n2m; t += m.nt) {
         const int i = 1 + t % a.n1m, j = 1 + t / a.n1m;
         out[t] = m.P(i, j);
     }
-    if (threadIdx.x == 0) {
+    if (m.tid == 0) {
         a.iters[kv - 1] = it;
         atomicMax((unsigned long long *)&a.S->poisson_iters[a.slot], (unsigned long long)it);
     }
@@ -545,6 +577,7 @@ int zft_init(lesgpu_case *c) {
     if (nlev < 1 || nlev > kMaxLev || g.n1m % (1 << nlev) != 0) return LESGPU_ERR_CONFIG;
     if (g.n3m > 1 && cf.zprdic != 1) return LESGPU_ERR_CONFIG;
     if (cf.mgitr < 0 || cf.nbli < 1) return LESGPU_ERR_CONFIG;
+    if (g.n2m > 32 * kMC) return LESGPU_ERR_UNSUPPORTED;    // one warp per y line, kMC rows per lane
     int rc = make_plan(P.fz, g.n3m);
     if (rc) return rc;
     MgTables *T = new MgTables();
@@ -574,6 +607,32 @@ int zft_init(lesgpu_case *c) {
     if (cudaFuncSetAttribute(k_fft_z_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem) != cudaSuccess ||
         cudaFuncSetAttribute(k_fft_z_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem) != cudaSuccess)
         return LESGPU_ERR_CUDA;
+    // Cluster size: the mode solves are FP64-throughput bound (a GB300 SM
+    // retires few FP64 FMAs per clock), so each mode gets as many SMs as the
+    // GPU can co-schedule for all modes: minimise waves / blocks-per-mode.
+    cudaFuncSetAttribute(k_zft_modes, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    T->cs = 1;
+    double best = 1e300;
+    const int cands[5] = {16, 8, 4, 2, 1};
+    for (int q = 0; q < 5; q++) {
+        const int cs = cands[q];
+        cudaLaunchConfig_t lc = {};
+        lc.gridDim = dim3(g.n3mh * cs);
+        lc.blockDim = dim3(kMgThreads);
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cs; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+        lc.attrs = at;
+        lc.numAttrs = 1;
+        int nact = 0;
+        if (cudaOccupancyMaxActiveClusters(&nact, k_zft_modes, &lc) != cudaSuccess || nact < 1) {
+            cudaGetLastError();
+            continue;
+        }
+        const double waves = (double)((g.n3mh + nact - 1) / nact);
+        const double cost = waves / cs;
+        if (cost < best - 1e-12) { best = cost; T->cs = cs; }
+    }
     return 0;
 }
 
@@ -613,7 +672,17 @@ void launch_zft(lesgpu_case *c, int msub) {
     a.ccap = P.ccap; a.pc = T->pc; a.gg = T->gg; a.rs = T->rs;
     a.pc_plane = T->pc_plane; a.gg_plane = T->gg_plane;
     a.iters = T->iters; a.S = c->S; a.slot = slot;
-    k_zft_modes<<<g.n3mh, kMgThreads, 0, c->stream>>>(a);
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(g.n3mh * T->cs);
+    lc.blockDim = dim3(kMgThreads);
+    lc.dynamicSmemBytes = 0;
+    lc.stream = c->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = T->cs; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    cudaLaunchKernelEx(&lc, k_zft_modes, a);
     k_fft_z_inv<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
     inst_end(c, LESGPU_K_POISSON);
 }

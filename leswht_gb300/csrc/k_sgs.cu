@@ -175,7 +175,10 @@ __global__ void __launch_bounds__(kThreads) k_filter(KP p, Box b, FiltBatch F) {
         b.at(tt - (long long)a * n, i, j, k);
         const double *s = F.src[a];
         double out;
-        bool zin = zf && ((k >= 2 && k <= g.n3m - 1) || (p.c.zprdic == 1 && g.n3m > 1));
+        // z-periodic ends use the wrapped neighbours; with n3m = 1 the weights
+        // are zero (sgsfilterinit skips them), so the filtered value is 0 as
+        // in test_filter (sgs.f90:735-764)
+        bool zin = zf && ((k >= 2 && k <= g.n3m - 1) || p.c.zprdic == 1);
         if (!zin) {
             out = filt_x(p, s, i, g.ix(0, j, k), xf);
         } else {
