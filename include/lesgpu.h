@@ -228,6 +228,18 @@ int lesgpu_step(lesgpu_case *c, lesgpu_step_report *rep);
 int lesgpu_get_fields(lesgpu_case *c, double *u, double *v, double *w,
                       double *p, double *t);
 
+/* Running time averages of field_avg (misc_hist.f90:287-527).  With IAVG = 1
+ * every lesgpu_step after time > AVG_TST adds dt-weighted cell-centre
+ * statistics on the device.  lesgpu_get_averages copies them out in the
+ * record order of the reference's fav file -- uavg, vavg, wavg, uiujavg(1..6),
+ * pavg, p2avg, voravg(1..3), vor2avg(1..6), ssavg, then tavg, t2avg when
+ * IHTRANS = 1 -- each an (n1m, n2m, n3m) array in Fortran order, so `out`
+ * holds LESGPU_NAVG (or LESGPU_NAVG - 2) * n1m*n2m*n3m doubles; *nsamples
+ * is the number of steps summed; reset != 0 zeroes the sums (the reference
+ * does so after writing each fav file, every NPRIAVG samples). */
+#define LESGPU_NAVG 23
+int lesgpu_get_averages(lesgpu_case *c, double *out, int64_t *nsamples, int reset);
+
 /* Phase-level access for parity tests (not needed by a driver). */
 int lesgpu_get_array(lesgpu_case *c, int64_t field, double *out);
 int lesgpu_set_array(lesgpu_case *c, int64_t field, const double *in);

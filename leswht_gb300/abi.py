@@ -36,6 +36,11 @@ F_NUSGS, F_NUSGS1, F_ALSGS, F_ALSGS1 = 5, 6, 7, 8
 F_RHS1, F_RK3O, F_RK3OO, F_DIVGSUM, F_PHI, F_QMASS = 9, 10, 11, 12, 13, 14
 FIELD_NCOMP = {F_NUSGS1: 3, F_ALSGS1: 3, F_RHS1: 4, F_RK3O: 4, F_RK3OO: 4}
 
+NAVG = 23          # field_avg arrays (21 without temperature)
+AVG_NAMES = ["uavg", "vavg", "wavg", "uu", "uv", "uw", "vv", "vw", "ww", "pavg", "p2avg",
+             "wxavg", "wyavg", "wzavg", "wxwx", "wxwy", "wxwz", "wywy", "wywz", "wzwz", "ssavg",
+             "tavg", "t2avg"]
+
 PH_SUBSTEPINIT, PH_SGS, PH_RHSNLHS, PH_DIVGS, PH_POISSON, PH_UCALC, PH_MEANPG, PH_ENERGY, PH_STEPINIT = range(9)
 
 
@@ -216,6 +221,7 @@ def declare_api(lib, prefix: str, case_type=C.c_void_p) -> None:
         "set_array": ([case_type, i64, PD], C.c_int),
         "run_phase": ([case_type, i64, i64], C.c_int),
         "get_report": ([case_type, C.POINTER(StepReport)], C.c_int),
+        "get_averages": ([case_type, PD, PI, C.c_int], C.c_int),
         "destroy": ([case_type], C.c_int),
     }
     for name, (args, res) in sig.items():

@@ -157,6 +157,7 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
     f.nusgs = A.get<double>(nt); f.alsgs = A.get<double>(nt);
     for (int l = 0; l < 3; l++) { f.nusgs1[l] = A.get<double>(nt); f.alsgs1[l] = A.get<double>(nt); }
     f.qmass = A.get<double>(nt); f.divgsum = A.get<double>(nt); f.phi = A.get<double>(nt);
+    if (cfg->iavg == 1) f.avg = A.get<double>(nt * LESGPU_NAVG);
     int nscr = (cfg->iles == 1) ? 33 : 9;   // ADI uses scr[0..8] (three components), SGS scr[3..32]
     for (int s = 0; s < nscr; s++) f.scr[s] = A.get<double>(nt);
     f.part = A.get<double>((size_t)(kRedBlocks + 1) * kMaxRed);
@@ -502,6 +503,7 @@ static void enqueue_step(lesgpu_case *c, bool first) {
     launch_bulk_diag(c);
     if (g.ibmon == 1) launch_draglift(c);
     if (g.ihtrans == 1) launch_heatflux(c);
+    if (g.iavg == 1) launch_field_avg(c);
 }
 
 // Capture one steady-state step into a CUDA graph and count its kernels.
@@ -723,6 +725,43 @@ extern "C" int lesgpu_run_phase(lesgpu_case *c, int64_t phase, int64_t msub) {
     default: return LESGPU_ERR_ARG;
     }
     return cuda_rc(cudaStreamSynchronize(c->stream));
+}
+
+// ----------------------------------------------------------- field_avg
+__global__ void k_avg_reset_count(KP p) { p.S->avg_count = 0; }
+
+extern "C" int lesgpu_get_averages(lesgpu_case *c, double *out, int64_t *nsamples, int reset) {
+    if (!c) return LESGPU_ERR_ARG;
+    const DGrid &g = c->kp.g;
+    const int na = c->cfg.ihtrans == 1 ? LESGPU_NAVG : LESGPU_NAVG - 2;
+    double *avg = c->kp.f.avg;
+    const size_t nt = (size_t)g.nt, nc = (size_t)g.n1m * g.n2m * g.n3m;
+    if (out) {
+        if (!avg) {
+            memset(out, 0, sizeof(double) * nc * na);
+        } else {
+            for (int a = 0; a < na; a++) {
+                cudaMemcpy3DParms m = {};
+                m.srcPtr = make_cudaPitchedPtr(avg + nt * a, sizeof(double) * g.sx, g.sx, g.n2 + 1);
+                m.srcPos = make_cudaPos(sizeof(double) * 1, 1, 1);
+                m.dstPtr = make_cudaPitchedPtr(out + nc * a, sizeof(double) * g.n1m, g.n1m, g.n2m);
+                m.dstPos = make_cudaPos(0, 0, 0);
+                m.extent = make_cudaExtent(sizeof(double) * g.n1m, g.n2m, g.n3m);
+                m.kind = cudaMemcpyDeviceToHost;
+                if (cudaMemcpy3DAsync(&m, c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
+            }
+        }
+    }
+    DScal s;
+    cudaMemcpyAsync(&s, c->S, sizeof(DScal), cudaMemcpyDeviceToHost, c->stream);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
+    if (nsamples) *nsamples = s.avg_count;
+    if (reset) {
+        if (avg) cudaMemsetAsync(avg, 0, sizeof(double) * nt * LESGPU_NAVG, c->stream);
+        k_avg_reset_count<<<1, 1, 0, c->stream>>>(c->kp);
+        if (cudaStreamSynchronize(c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
+    }
+    return 0;
 }
 
 extern "C" int lesgpu_destroy(lesgpu_case *c) {

@@ -66,6 +66,7 @@ struct DScal {
     double cvol;              // tvolcorr's volume integral of 1/c*
     double cb[4];             // convective outlet: qin, ucoef, vwcoef, qratio
     double mg_test;           // z_ft multigrid convergence criterion of the substep
+    long long avg_count;      // field_avg samples since the last reset
     long long ntime, m, ihist;
     long long poisson_iters[3];
     int err;                  // device-side error flag (non-finite values etc.)
@@ -96,6 +97,7 @@ struct DFields {
     // scratch
     double *scr[34];          // SGS temporaries / tridiagonal work, nt each
     double *part;             // reduction partials kRedBlocks * kMaxRed
+    double *avg;              // field_avg sums: LESGPU_NAVG arrays of nt (IAVG = 1 only)
 };
 
 // Poisson FFT plan of one line length.
@@ -267,6 +269,7 @@ void launch_draglift(lesgpu_case *c);
 void launch_heatflux(lesgpu_case *c);
 void launch_convbc(lesgpu_case *c);
 void launch_convbc_t(lesgpu_case *c);
+void launch_field_avg(lesgpu_case *c);
 }  // namespace lg
 
 namespace lg {

@@ -95,6 +95,15 @@ class Solver:
         a = np.ascontiguousarray(arr, dtype=np.float64)
         self._call("set_array", self.h, int(field), a.ctypes.data_as(abi.PD))
 
+    def averages(self, reset: bool = False):
+        """field_avg sums as {name: (n3m, n2m, n1m) array} and the sample count."""
+        g = self.case.grid
+        na = abi.NAVG if self.case.settings.get("ihtrans", 0) == 1 else abi.NAVG - 2
+        out = np.empty((na, g.n3m, g.n2m, g.n1m))
+        n = C.c_int64()
+        self._call("get_averages", self.h, out.ctypes.data_as(abi.PD), C.byref(n), int(reset))
+        return {abi.AVG_NAMES[a]: out[a] for a in range(na)}, n.value
+
     def phase(self, ph: int, msub: int = 1):
         self._call("run_phase", self.h, int(ph), int(msub))
 

@@ -28,6 +28,7 @@ int ref_get_array(ref_case *c, int64_t field, double *out);
 int ref_set_array(ref_case *c, int64_t field, const double *in);
 int ref_run_phase(ref_case *c, int64_t phase, int64_t msub);
 int ref_get_report(ref_case *c, lesgpu_step_report *rep);
+int ref_get_averages(ref_case *c, double *out, int64_t *nsamples, int reset);
 int ref_destroy(ref_case *c);
 
 /* building blocks exposed for invariant tests */

@@ -235,6 +235,7 @@ int ref_step(ref_case *c, lesgpu_step_report *rep)
     ref_bulk_diag(c);
     if (g->ibmon == 1) ref_draglift(c);
     if (g->ihtrans == 1) ref_heatflux(c);
+    if (g->iavg == 1) ref_field_avg(c);
     if (rep) ref_get_report(c, rep);
     return 0;
 }
@@ -358,7 +359,7 @@ int ref_destroy(ref_case *c)
     free(c->omega); free(c->nwall);
     free(c->ac); free(c->gam); free(c->bet);
     free(c->aw); free(c->ae); free(c->as); free(c->an); free(c->coi1); free(c->coi2); free(c->cor1); free(c->cor2);
-    free(c->ipm); free(c->imm); free(c->ak1); free(c->ak3);
+    free(c->ipm); free(c->imm); free(c->ak1); free(c->ak3); free(c->avg);
     ref_fft_plan_free(&c->fftx); ref_fft_plan_free(&c->fftz);
     free(c);
     return 0;
@@ -707,4 +708,131 @@ void ref_bulk_diag(ref_case *c)
     c->ubulk = fv > 0 ? qv / fv : 0.0;
     c->tbulk_fluid = tfv > 0 ? tfi / tfv : 0.0;
     c->tbulk_solid = tsv > 0 ? tsi / tsv : 0.0;
+}
+
+/* ===================== misc_hist.f90 ==================================== */
+
+/* field_avg, misc_hist.f90:287-527: running sums of dt-weighted cell-centre
+   statistics once time > AVG_TST.  The fav file write and the reset every
+   NPRIAVG samples are host work (ref_get_averages). */
+void ref_field_avg(ref_case *c)
+{
+    const lesgpu_config *g = &c->c;
+    if (c->time <= g->avg_tst) return;
+    size_t nt = c->nt;
+    if (!c->avg) c->avg = ref_zalloc(nt * LESGPU_NAVG);
+    double *A[LESGPU_NAVG];
+    for (int q = 0; q < LESGPU_NAVG; q++) A[q] = c->avg + nt * (size_t)q;
+    double dt = c->dt;
+    const double *u = c->u, *v = c->v, *w = c->w, *p = c->p, *t = c->t;
+    ll n1 = c->n1, n2 = c->n2, n3 = c->n3;
+    #pragma omp parallel for
+    for (ll k = 1; k <= c->n3m; k++)
+        for (ll j = 1; j <= c->n2m; j++)
+            for (ll i = 1; i <= c->n1m; i++) {
+                size_t q = IX(c, i, j, k);
+                double ucc = 0.5 * (u[q] + u[IX(c, i + 1, j, k)]);
+                double vcc = 0.5 * (v[q] + v[IX(c, i, j + 1, k)]);
+                double wcc = 0.5 * (w[q] + w[IX(c, i, j, k + 1)]);
+                A[0][q] = A[0][q] + ucc * dt;
+                A[1][q] = A[1][q] + vcc * dt;
+                A[2][q] = A[2][q] + wcc * dt;
+                A[3][q] = A[3][q] + ucc * ucc * dt;
+                A[4][q] = A[4][q] + ucc * vcc * dt;
+                A[5][q] = A[5][q] + ucc * wcc * dt;
+                A[6][q] = A[6][q] + vcc * vcc * dt;
+                A[7][q] = A[7][q] + vcc * wcc * dt;
+                A[8][q] = A[8][q] + wcc * wcc * dt;
+                A[9][q] = A[9][q] + p[q] * dt;
+                A[10][q] = A[10][q] + p[q] * p[q] * dt;
+                if (g->ihtrans == 1) {
+                    A[21][q] = A[21][q] + t[q] * dt;
+                    A[22][q] = A[22][q] + t[q] * t[q] * dt;
+                }
+                /* velocity gradients at the cell centre (misc_hist.f90:379-455) */
+                double fju = (double)c->fixju[j], fjl = (double)c->fixjl[j];
+                double fku = (double)c->fixku[k], fkl = (double)c->fixkl[k];
+                double fiu = (double)c->fixiu[i], fil = (double)c->fixil[i];
+                double vg11 = c->f2fxi[i] * (u[IX(c, i + 1, j, k)] - u[q]);
+                double up = c->c2cyi[j + 1] * 0.25 * (c->f2fy[j + 1] * (u[q] + u[IX(c, i + 1, j, k)])
+                            + c->f2fy[j] * (u[IX(c, i, j + 1, k)] + u[IX(c, i + 1, j + 1, k)])) * (1. - fju)
+                            + 0.5 * (u[IX(c, i, n2, k)] + u[IX(c, i + 1, n2, k)]) * fju;
+                double um = c->c2cyi[j] * 0.25 * (c->f2fy[j] * (u[IX(c, i, j - 1, k)] + u[IX(c, i + 1, j - 1, k)])
+                            + c->f2fy[j - 1] * (u[q] + u[IX(c, i + 1, j, k)])) * (1. - fjl)
+                            + 0.5 * (u[IX(c, i, 0, k)] + u[IX(c, i + 1, 0, k)]) * fjl;
+                double vg12 = c->f2fyi[j] * (up - um);
+                up = c->c2czi[k + 1] * 0.25 * (c->f2fz[k + 1] * (u[q] + u[IX(c, i + 1, j, k)])
+                     + c->f2fz[k] * (u[IX(c, i, j, k + 1)] + u[IX(c, i + 1, j, k + 1)])) * (1. - fku)
+                     + 0.5 * (u[IX(c, i, j, n3)] + u[IX(c, i + 1, j, n3)]) * fku;
+                um = c->c2czi[k] * 0.25 * (c->f2fz[k] * (u[IX(c, i, j, k - 1)] + u[IX(c, i + 1, j, k - 1)])
+                     + c->f2fz[k - 1] * (u[q] + u[IX(c, i + 1, j, k)])) * (1. - fkl)
+                     + 0.5 * (u[IX(c, i, j, 0)] + u[IX(c, i + 1, j, 0)]) * fkl;
+                double vg13 = c->f2fzi[k] * (up - um);
+                double vp = c->c2cxi[i + 1] * 0.25 * (c->f2fx[i + 1] * (v[q] + v[IX(c, i, j + 1, k)])
+                            + c->f2fx[i] * (v[IX(c, i + 1, j, k)] + v[IX(c, i + 1, j + 1, k)])) * (1. - fiu)
+                            + 0.5 * (v[IX(c, n1, j, k)] + v[IX(c, n1, j + 1, k)]) * fiu;
+                double vm = c->c2cxi[i] * 0.25 * (c->f2fx[i] * (v[IX(c, i - 1, j, k)] + v[IX(c, i - 1, j + 1, k)])
+                            + c->f2fx[i - 1] * (v[q] + v[IX(c, i, j + 1, k)])) * (1. - fil)
+                            + 0.5 * (v[IX(c, 0, j, k)] + v[IX(c, 0, j + 1, k)]) * fil;
+                double vg21 = c->f2fxi[i] * (vp - vm);
+                double vg22 = c->f2fyi[j] * (v[IX(c, i, j + 1, k)] - v[q]);
+                vp = c->c2czi[k + 1] * 0.25 * (c->f2fz[k + 1] * (v[q] + v[IX(c, i, j + 1, k)])
+                     + c->f2fz[k] * (v[IX(c, i, j, k + 1)] + v[IX(c, i, j + 1, k + 1)])) * (1. - fku)
+                     + 0.5 * (v[IX(c, i, j, n3)] + v[IX(c, i, j + 1, n3)]) * fku;
+                vm = c->c2czi[k] * 0.25 * (c->f2fz[k] * (v[IX(c, i, j, k - 1)] + v[IX(c, i, j + 1, k - 1)])
+                     + c->f2fz[k - 1] * (v[q] + v[IX(c, i, j + 1, k)])) * (1. - fkl)
+                     + 0.5 * (v[IX(c, i, j, 0)] + v[IX(c, i, j + 1, 0)]) * fkl;
+                double vg23 = c->f2fzi[k] * (vp - vm);
+                double wp = c->c2cxi[i + 1] * 0.25 * (c->f2fx[i + 1] * (w[q] + w[IX(c, i, j, k + 1)])
+                            + c->f2fx[i] * (w[IX(c, i + 1, j, k)] + w[IX(c, i + 1, j, k + 1)])) * (1. - fiu)
+                            + 0.5 * (w[IX(c, n1, j, k)] + w[IX(c, n1, j, k + 1)]) * fiu;
+                double wm = c->c2cxi[i] * 0.25 * (c->f2fx[i] * (w[IX(c, i - 1, j, k)] + w[IX(c, i - 1, j, k + 1)])
+                            + c->f2fx[i - 1] * (w[q] + w[IX(c, i, j, k + 1)])) * (1. - fil)
+                            + 0.5 * (w[IX(c, 0, j, k)] + w[IX(c, 0, j, k + 1)]) * fil;
+                double vg31 = c->f2fxi[i] * (wp - wm);
+                wp = c->c2cyi[j + 1] * 0.25 * (c->f2fy[j + 1] * (w[q] + w[IX(c, i, j, k + 1)])
+                     + c->f2fy[j] * (w[IX(c, i, j + 1, k)] + w[IX(c, i, j + 1, k + 1)])) * (1. - fju)
+                     + 0.5 * (w[IX(c, i, n2, k)] + w[IX(c, i, n2, k + 1)]) * fju;
+                wm = c->c2cyi[j] * 0.25 * (c->f2fy[j] * (w[IX(c, i, j - 1, k)] + w[IX(c, i, j - 1, k + 1)])
+                     + c->f2fy[j - 1] * (w[q] + w[IX(c, i, j, k + 1)])) * (1. - fjl)
+                     + 0.5 * (w[IX(c, i, 0, k)] + w[IX(c, i, 0, k + 1)]) * fjl;
+                double vg32 = c->f2fyi[j] * (wp - wm);
+                double vg33 = c->f2fzi[k] * (w[IX(c, i, j, k + 1)] - w[q]);
+                double s1 = vg11, s2 = 0.5 * (vg12 + vg21), s3 = 0.5 * (vg13 + vg31);
+                double s4 = vg22, s5 = 0.5 * (vg23 + vg32), s6 = vg33;
+                double wx = vg32 - vg23, wy = vg13 - vg31, wz = vg21 - vg12;
+                A[11][q] = A[11][q] + wx * dt;
+                A[12][q] = A[12][q] + wy * dt;
+                A[13][q] = A[13][q] + wz * dt;
+                A[14][q] = A[14][q] + wx * wx * dt;
+                A[15][q] = A[15][q] + wx * wy * dt;
+                A[16][q] = A[16][q] + wx * wz * dt;
+                A[17][q] = A[17][q] + wy * wy * dt;
+                A[18][q] = A[18][q] + wy * wz * dt;
+                A[19][q] = A[19][q] + wz * wz * dt;
+                double srsr = 2. * (s2 * s2) + s1 * s1 + 2. * (s3 * s3) + s4 * s4 + 2. * (s5 * s5) + s6 * s6;
+                A[20][q] = A[20][q] + srsr * dt;
+            }
+    c->avg_count += 1;
+}
+
+int ref_get_averages(ref_case *c, double *out, int64_t *nsamples, int reset)
+{
+    if (!c) return LESGPU_ERR_ARG;
+    int na = c->c.ihtrans == 1 ? LESGPU_NAVG : LESGPU_NAVG - 2;
+    ll n1m = c->n1m, n2m = c->n2m, n3m = c->n3m;
+    size_t nc = (size_t)n1m * n2m * n3m;
+    if (out)
+        for (int a = 0; a < na; a++)
+            for (ll k = 1; k <= n3m; k++)
+                for (ll j = 1; j <= n2m; j++)
+                    for (ll i = 1; i <= n1m; i++)
+                        out[nc * a + (size_t)(i - 1) + (size_t)n1m * ((size_t)(j - 1) + (size_t)n2m * (size_t)(k - 1))] =
+                            c->avg ? c->avg[c->nt * (size_t)a + IX(c, i, j, k)] : 0.0;
+    if (nsamples) *nsamples = c->avg_count;
+    if (reset) {
+        if (c->avg) memset(c->avg, 0, sizeof(double) * c->nt * LESGPU_NAVG);
+        c->avg_count = 0;
+    }
+    return 0;
 }

@@ -108,6 +108,9 @@ typedef struct ref_case {
     double dudta, dvdta, dwdta;
     double cd[3], heat_flux[3];
     double ubulk, tbulk_fluid, tbulk_solid;
+    /* field_avg accumulators: LESGPU_NAVG arrays in the full layout, record order of the fav file */
+    double *avg;
+    ll avg_count;
     int started;
 } ref_case;
 
@@ -173,6 +176,8 @@ int ref_poisinit(ref_case *c);
 void ref_poisson(ref_case *c);
 /* misc_init.f90 */
 void ref_convergence_check(ref_case *c);
+/* misc_hist.f90 */
+void ref_field_avg(ref_case *c);
 void ref_masscheck(ref_case *c);
 void ref_bulk_diag(ref_case *c);
 

@@ -118,3 +118,23 @@ def test_gpu_deterministic_and_graph_equals_eager(small_case):
     for k in outs[0]:
         np.testing.assert_array_equal(outs[0][k], outs[1][k])
         np.testing.assert_array_equal(outs[0][k], outs[2][k])
+
+
+def test_field_averages(oracle_lib):
+    """field_avg (misc_hist.f90:287-527) sums after three steps, and the reset."""
+    case = cases.channel(32, 32, 16)
+    case.settings.update(iavg=1, avg_tst=0.0)
+    g, r = make_pair(oracle_lib, case)
+    for _ in range(3):
+        g.step(), r.step()
+    ag, ng = g.averages()
+    ar, nr = r.averages()
+    assert ng == nr == 3
+    for k in ar:
+        assert rel(ag[k], ar[k]) <= TOL, (k, rel(ag[k], ar[k]))
+    g.averages(reset=True)
+    a0, n0 = g.averages()
+    assert n0 == 0 and all(float(abs(v).max()) == 0.0 for v in a0.values())
+    g.step()
+    a1, n1 = g.averages()
+    assert n1 == 1 and float(abs(a1["uavg"]).max()) > 0.0
