@@ -35,46 +35,48 @@ __device__ __forceinline__ void line_coords(int dir, int l, int x0, int x1, int 
     else { j = x0; k = x1; i = l; }                 // x-lines: batch (j, k)
 }
 
-// a and c of the element (i,j,k); b = diag - a - c.
-__device__ __forceinline__ void adi_coef(const KP &p, int comp, int dir, int i, int j, int k, double &a, double &c) {
+// a and c of the element (i,j,k); b = diag - a - c.  R is the arithmetic
+// type (double; float for the x and z sweeps of the mixed-precision form).
+template <class R>
+__device__ __forceinline__ void adi_coef(const KP &p, int comp, int dir, int i, int j, int k, R &a, R &c) {
     const DGrid &g = p.g;
     const DFields &f = p.f;
-    const double re = p.c.re;
+    const R re = p.c.re;
     long long q = g.ix(i, j, k);
     if (comp == CT) {
-        const double cre = (double)p.c.iles * re * p.c.pr;
-        double cs = 1.0, ks1 = 1.0, ks2 = 1.0, omc = 1.0;
+        const R cre = (double)p.c.iles * re * p.c.pr;
+        R cs = R(1.0), ks1 = R(1.0), ks2 = R(1.0), omc = R(1.0);
         int ka = dir == 2 ? 5 : dir == 1 ? 3 : 1;
         if (p.c.iconjg == 1) {
-            cs = f.cstar[q];
-            ks1 = f.kstar[ka][q];
-            ks2 = f.kstar[ka - 1][q];
-            omc = p.c.imovingon == 0 ? (double)f.omega[q] : 1.0;
+            cs = R(f.cstar[q]);
+            ks1 = R(f.kstar[ka][q]);
+            ks2 = R(f.kstar[ka - 1][q]);
+            omc = p.c.imovingon == 0 ? R(f.omega[q]) : R(1.0);
         }
         if (dir == 2) {
-            a = f.akuv[k] * (cs * ks1 + cre * omc * f.alsgs1[1][q]);
-            c = f.ckuv[k] * (cs * ks2 + cre * omc * f.alsgs1[1][q + g.sxy]);
+            a = R(f.akuv[k]) * (cs * ks1 + cre * omc * R(f.alsgs1[1][q]));
+            c = R(f.ckuv[k]) * (cs * ks2 + cre * omc * R(f.alsgs1[1][q + g.sxy]));
         } else if (dir == 1) {
-            a = f.ajuw[j] * (cs * ks1 + cre * omc * f.alsgs1[2][q]);
-            c = f.cjuw[j] * (cs * ks2 + cre * omc * f.alsgs1[2][q + g.sx]);
+            a = R(f.ajuw[j]) * (cs * ks1 + cre * omc * R(f.alsgs1[2][q]));
+            c = R(f.cjuw[j]) * (cs * ks2 + cre * omc * R(f.alsgs1[2][q + g.sx]));
         } else {
-            a = f.aivw[i] * (cs * ks1 + cre * omc * f.alsgs1[0][q]);
-            c = f.civw[i] * (cs * ks2 + cre * omc * f.alsgs1[0][q + 1]);
+            a = R(f.aivw[i]) * (cs * ks1 + cre * omc * R(f.alsgs1[0][q]));
+            c = R(f.civw[i]) * (cs * ks2 + cre * omc * R(f.alsgs1[0][q + 1]));
         }
         return;
     }
-    const double cre = (double)p.c.iles * re, cre2 = 2.0 * (double)p.c.iles * re;
+    const R cre = (double)p.c.iles * re, cre2 = R(2.0) * (double)p.c.iles * re;
     const double *nu = f.nusgs, *nu1 = f.nusgs1[0], *nu2 = f.nusgs1[1], *nu3 = f.nusgs1[2];
     switch (comp * 3 + dir) {
-    case CU * 3 + 2: a = f.akuv[k] * (1.0 + cre * nu2[q]); c = f.ckuv[k] * (1.0 + cre * nu2[q + g.sxy]); break;
-    case CU * 3 + 1: a = f.ajuw[j] * (1.0 + cre * nu3[q]); c = f.cjuw[j] * (1.0 + cre * nu3[q + g.sx]); break;
-    case CU * 3 + 0: a = f.aiu[i] * (1.0 + cre2 * nu[q - 1]); c = f.ciu[i] * (1.0 + cre2 * nu[q]); break;
-    case CV * 3 + 2: a = f.akuv[k] * (1.0 + cre * nu1[q]); c = f.ckuv[k] * (1.0 + cre * nu1[q + g.sxy]); break;
-    case CV * 3 + 1: a = f.ajv[j] * (1.0 + cre2 * nu[q - g.sx]); c = f.cjv[j] * (1.0 + cre2 * nu[q]); break;
-    case CV * 3 + 0: a = f.aivw[i] * (1.0 + cre * nu3[q]); c = f.civw[i] * (1.0 + cre * nu3[q + 1]); break;
-    case CW * 3 + 2: a = f.akw[k] * (1.0 + cre2 * nu[q - g.sxy]); c = f.ckw[k] * (1.0 + cre2 * nu[q]); break;
-    case CW * 3 + 1: a = f.ajuw[j] * (1.0 + cre * nu1[q]); c = f.cjuw[j] * (1.0 + cre * nu1[q + g.sx]); break;
-    default:         a = f.aivw[i] * (1.0 + cre * nu2[q]); c = f.civw[i] * (1.0 + cre * nu2[q + 1]); break;
+    case CU * 3 + 2: a = R(f.akuv[k]) * (R(1.0) + cre * R(nu2[q])); c = R(f.ckuv[k]) * (R(1.0) + cre * R(nu2[q + g.sxy])); break;
+    case CU * 3 + 1: a = R(f.ajuw[j]) * (R(1.0) + cre * R(nu3[q])); c = R(f.cjuw[j]) * (R(1.0) + cre * R(nu3[q + g.sx])); break;
+    case CU * 3 + 0: a = R(f.aiu[i]) * (R(1.0) + cre2 * R(nu[q - 1])); c = R(f.ciu[i]) * (R(1.0) + cre2 * R(nu[q])); break;
+    case CV * 3 + 2: a = R(f.akuv[k]) * (R(1.0) + cre * R(nu1[q])); c = R(f.ckuv[k]) * (R(1.0) + cre * R(nu1[q + g.sxy])); break;
+    case CV * 3 + 1: a = R(f.ajv[j]) * (R(1.0) + cre2 * R(nu[q - g.sx])); c = R(f.cjv[j]) * (R(1.0) + cre2 * R(nu[q])); break;
+    case CV * 3 + 0: a = R(f.aivw[i]) * (R(1.0) + cre * R(nu3[q])); c = R(f.civw[i]) * (R(1.0) + cre * R(nu3[q + 1])); break;
+    case CW * 3 + 2: a = R(f.akw[k]) * (R(1.0) + cre2 * R(nu[q - g.sxy])); c = R(f.ckw[k]) * (R(1.0) + cre2 * R(nu[q])); break;
+    case CW * 3 + 1: a = R(f.ajuw[j]) * (R(1.0) + cre * R(nu1[q])); c = R(f.cjuw[j]) * (R(1.0) + cre * R(nu1[q + g.sx])); break;
+    default:         a = R(f.aivw[i]) * (R(1.0) + cre * R(nu2[q])); c = R(f.civw[i]) * (R(1.0) + cre * R(nu2[q + 1])); break;
     }
 }
 
@@ -88,10 +90,11 @@ struct AdiBatch {
     AdiArgs a[3];
 };
 
+template <class R>
 __global__ void __launch_bounds__(64) k_adi(KP p, AdiBatch B) {
     const AdiArgs &A = B.a[blockIdx.y];
     const DGrid &g = p.g;
-    const double diag = (A.comp == CT) ? p.S->acoefi * p.c.pr : p.S->acoefi;
+    const R diag = (A.comp == CT) ? p.S->acoefi * p.c.pr : p.S->acoefi;
     int na = A.a1 - A.a0 + 1, nb = A.b1 - A.b0 + 1;
     long long nl = (long long)na * nb;
     const long long stride = A.dir == 2 ? g.sxy : A.dir == 1 ? g.sx : 1;
@@ -105,30 +108,30 @@ __global__ void __launch_bounds__(64) k_adi(KP p, AdiBatch B) {
         if (!A.periodic) {
             // ---- trdiag: forward elimination, chunk by chunk
             double *out = A.add ? A.sarr : A.dst;    // provisional solution
-            double bet = 0.0, x = 0.0, cprev = 0.0;
+            R bet = R(0.0), x = R(0.0), cprev = R(0.0);
             for (int c0 = 0; c0 < nline; c0 += CH) {
-                double av[CH], cv[CH], rv[CH];
+                R av[CH], cv[CH], rv[CH];
 #pragma unroll
                 for (int u = 0; u < CH; u++) {
                     if (c0 + u < nline) {
                         int i, j, k;
                         line_coords(A.dir, A.l1 + c0 + u, x0, x1, i, j, k);
                         adi_coef(p, A.comp, A.dir, i, j, k, av[u], cv[u]);
-                        rv[u] = A.src[q0 + (long long)(c0 + u) * stride];
+                        rv[u] = R(A.src[q0 + (long long)(c0 + u) * stride]);
                     }
                 }
 #pragma unroll
                 for (int u = 0; u < CH; u++) {
                     if (c0 + u < nline) {
                         const long long q = q0 + (long long)(c0 + u) * stride;
-                        const double a = av[u], c = cv[u];
-                        const double b = diag - a - c;
+                        const R a = av[u], c = cv[u];
+                        const R b = diag - a - c;
                         if (c0 + u == 0) {
-                            bet = 1.0 / b;
+                            bet = R(1.0) / b;
                             x = diag * rv[u] * bet;
                         } else {
-                            const double gm = cprev * bet;
-                            bet = 1.0 / (b - a * gm);
+                            const R gm = cprev * bet;
+                            bet = R(1.0) / (b - a * gm);
                             x = (diag * rv[u] - a * x) * bet;
                             A.gam[q] = gm;
                         }
@@ -138,19 +141,19 @@ __global__ void __launch_bounds__(64) k_adi(KP p, AdiBatch B) {
                 }
             }
             // ---- back substitution, chunk by chunk from the end
-            double xn = x;
+            R xn = x;
             const long long qlast = q0 + (long long)(nline - 1) * stride;
             if (A.add) A.dst[qlast] += xn;
             for (int c1 = nline - 2; c1 >= 0; c1 -= CH) {
-                double ov[CH], gv[CH], fv[CH];
+                R ov[CH], gv[CH], fv[CH];
 #pragma unroll
                 for (int u = 0; u < CH; u++) {
                     const int l = c1 - u;
                     if (l >= 0) {
                         const long long q = q0 + (long long)l * stride;
-                        ov[u] = out[q];
-                        gv[u] = A.gam[q + stride];
-                        if (A.add) fv[u] = A.dst[q];
+                        ov[u] = R(out[q]);
+                        gv[u] = R(A.gam[q + stride]);
+                        if (A.add) fv[u] = R(A.dst[q]);
                     }
                 }
 #pragma unroll
@@ -158,7 +161,7 @@ __global__ void __launch_bounds__(64) k_adi(KP p, AdiBatch B) {
                     const int l = c1 - u;
                     if (l >= 0) {
                         const long long q = q0 + (long long)l * stride;
-                        const double xl = ov[u] - gv[u] * xn;
+                        const R xl = ov[u] - gv[u] * xn;
                         if (A.add) A.dst[q] = fv[u] + xl;
                         else out[q] = xl;
                         xn = xl;
@@ -169,35 +172,35 @@ __global__ void __launch_bounds__(64) k_adi(KP p, AdiBatch B) {
             // ---- trdiagp: forward sweep; q factors in gam, s in sarr, f in fw
             double *fw = A.add ? (double *)A.src : A.dst;
             const long long qn_last = q0 + (long long)(nline - 1) * stride;
-            const double fn = diag * A.src[qn_last];   // original right-hand side at the last element
-            double qq = 0.0, ss = 0.0, ff = 0.0;
-            double a_last = 0.0, b_last = 0.0, c_last = 0.0;
+            const R fn = diag * R(A.src[qn_last]);   // original right-hand side at the last element
+            R qq = R(0.0), ss = R(0.0), ff = R(0.0);
+            R a_last = R(0.0), b_last = R(0.0), c_last = R(0.0);
             for (int c0 = 0; c0 < nline; c0 += CH) {
-                double av[CH], cv[CH], rv[CH];
+                R av[CH], cv[CH], rv[CH];
 #pragma unroll
                 for (int u = 0; u < CH; u++) {
                     if (c0 + u < nline) {
                         int i, j, k;
                         line_coords(A.dir, A.l1 + c0 + u, x0, x1, i, j, k);
                         adi_coef(p, A.comp, A.dir, i, j, k, av[u], cv[u]);
-                        rv[u] = A.src[q0 + (long long)(c0 + u) * stride];
+                        rv[u] = R(A.src[q0 + (long long)(c0 + u) * stride]);
                     }
                 }
 #pragma unroll
                 for (int u = 0; u < CH; u++) {
                     if (c0 + u < nline) {
                         const long long q = q0 + (long long)(c0 + u) * stride;
-                        const double a = av[u], c = cv[u];
-                        const double b = diag - a - c;
+                        const R a = av[u], c = cv[u];
+                        const R b = diag - a - c;
                         if (c0 + u == 0) {
-                            const double binv = 1.0 / b;
+                            const R binv = R(1.0) / b;
                             qq = -c * binv;
                             ss = -a * binv;
                             ff = diag * rv[u] * binv;
                         } else {
-                            const double pn = 1.0 / (b + a * qq);
-                            const double qn = -c * pn;
-                            const double sn = -a * ss * pn;
+                            const R pn = R(1.0) / (b + a * qq);
+                            const R qn = -c * pn;
+                            const R sn = -a * ss * pn;
                             ff = (diag * rv[u] - a * ff) * pn;
                             qq = qn;
                             ss = sn;
@@ -210,17 +213,17 @@ __global__ void __launch_bounds__(64) k_adi(KP p, AdiBatch B) {
                 }
             }
             // backward pass: s(j) += q(j) s(j+1); qe(j) = f(j) + q(j) qe(j+1)
-            double s_next = 1.0, qe_next = 0.0, s_j2m1 = 0.0, qe_j2m1 = 0.0;
+            R s_next = R(1.0), qe_next = R(0.0), s_j2m1 = R(0.0), qe_j2m1 = R(0.0);
             for (int c1 = nline - 2; c1 >= 0; c1 -= CH) {
-                double qv[CH], sv[CH], fv[CH];
+                R qv[CH], sv[CH], fv[CH];
 #pragma unroll
                 for (int u = 0; u < CH; u++) {
                     const int l = c1 - u;
                     if (l >= 0) {
                         const long long q = q0 + (long long)l * stride;
-                        qv[u] = A.gam[q];
-                        sv[u] = A.sarr[q];
-                        fv[u] = fw[q];
+                        qv[u] = R(A.gam[q]);
+                        sv[u] = R(A.sarr[q]);
+                        fv[u] = R(fw[q]);
                     }
                 }
 #pragma unroll
@@ -228,8 +231,8 @@ __global__ void __launch_bounds__(64) k_adi(KP p, AdiBatch B) {
                     const int l = c1 - u;
                     if (l >= 0) {
                         const long long q = q0 + (long long)l * stride;
-                        const double sj = sv[u] + qv[u] * s_next;
-                        const double qej = fv[u] + qv[u] * qe_next;
+                        const R sj = sv[u] + qv[u] * s_next;
+                        const R qej = fv[u] + qv[u] * qe_next;
                         A.sarr[q] = sj;
                         fw[q] = qej;
                         if (l == nline - 2) { s_j2m1 = sj; qe_j2m1 = qej; }
@@ -238,19 +241,19 @@ __global__ void __launch_bounds__(64) k_adi(KP p, AdiBatch B) {
                     }
                 }
             }
-            const double s_j1 = s_next, qe_j1 = qe_next;
-            const double fj2 = (fn - c_last * qe_j1 - a_last * qe_j2m1) / (c_last * s_j1 + a_last * s_j2m1 + b_last);
+            const R s_j1 = s_next, qe_j1 = qe_next;
+            const R fj2 = (fn - c_last * qe_j1 - a_last * qe_j2m1) / (c_last * s_j1 + a_last * s_j2m1 + b_last);
             if (A.add) A.dst[qn_last] += fj2; else fw[qn_last] = fj2;
             for (int c1 = nline - 2; c1 >= 0; c1 -= CH) {
-                double sv[CH], ev[CH], dv[CH];
+                R sv[CH], ev[CH], dv[CH];
 #pragma unroll
                 for (int u = 0; u < CH; u++) {
                     const int l = c1 - u;
                     if (l >= 0) {
                         const long long q = q0 + (long long)l * stride;
-                        sv[u] = A.sarr[q];
-                        ev[u] = fw[q];
-                        if (A.add) dv[u] = A.dst[q];
+                        sv[u] = R(A.sarr[q]);
+                        ev[u] = R(fw[q]);
+                        if (A.add) dv[u] = R(A.dst[q]);
                     }
                 }
 #pragma unroll
@@ -258,13 +261,348 @@ __global__ void __launch_bounds__(64) k_adi(KP p, AdiBatch B) {
                     const int l = c1 - u;
                     if (l >= 0) {
                         const long long q = q0 + (long long)l * stride;
-                        const double val = fj2 * sv[u] + ev[u];
+                        const R val = fj2 * sv[u] + ev[u];
                         if (A.add) A.dst[q] = dv[u] + val; else fw[q] = val;
                     }
                 }
             }
         }
     }
+}
+
+// ------------------------------------------------------------------------
+// Warp-per-line sweeps.  One thread per line leaves a 64^3 grid with ~2.5
+// warps per SM and a 2n-step dependent chain per line, so the sweep is
+// latency bound in FP64 and FP32 alike.  Here a warp solves a line: lane l
+// owns rows [l*m, l*m+m) (m = ceil(n/32) <= MC, held in registers), and each
+// recurrence of the reference's algorithm is split into
+//   1. the chunk's composed map (a 2x2 matrix for the pivots, whose
+//      recurrence bet_j = 1/(b_j - a_j c_{j-1} bet_{j-1}) is a Moebius map;
+//      an affine map for the substitutions),
+//   2. a 5-step shuffle scan over the lanes,
+//   3. the chunk re-run with the reference's recurrence from the scanned
+//      incoming value.
+// The dependent chain of a 64-row line drops from 128 steps to ~30 and the
+// GPU holds 32 times as many threads.  Matrix products are rescaled by their
+// largest entry (the pivot is a ratio), so nothing overflows in FP32.
+template <class R>
+struct M22 { R a, b, c, d; };     // [[a, b], [c, d]]
+
+template <class R>
+__device__ __forceinline__ M22<R> mmul_raw(const M22<R> &x, const M22<R> &y) {   // x * y
+    return M22<R>{x.a * y.a + x.b * y.c, x.a * y.b + x.b * y.d, x.c * y.a + x.d * y.c, x.c * y.b + x.d * y.d};
+}
+template <class R>
+__device__ __forceinline__ M22<R> mmul(const M22<R> &x, const M22<R> &y) {   // x * y, rescaled
+    M22<R> r = mmul_raw(x, y);
+    R m = fmax(fmax(fabs(r.a), fabs(r.b)), fmax(fabs(r.c), fabs(r.d)));
+    if (m > R(0.0)) {
+        const R s = R(1.0) / m;
+        r.a *= s; r.b *= s; r.c *= s; r.d *= s;
+    }
+    return r;
+}
+// Inside a chunk FP64 needs no rescaling (at most 12 rows of ~1e8 entries);
+// FP32 rescales every row.
+template <class R>
+__device__ __forceinline__ M22<R> mmul_chunk(const M22<R> &x, const M22<R> &y) {
+    if (sizeof(R) == 8) return mmul_raw(x, y);
+    return mmul(x, y);
+}
+
+template <class R, int W>
+__device__ __forceinline__ M22<R> shfl_up_m(const M22<R> &x, int d) {
+    return M22<R>{__shfl_up_sync(0xffffffffu, x.a, d, W), __shfl_up_sync(0xffffffffu, x.b, d, W),
+                  __shfl_up_sync(0xffffffffu, x.c, d, W), __shfl_up_sync(0xffffffffu, x.d, d, W)};
+}
+
+// exclusive prefix over lanes of a matrix product applied to (0, 1):
+// returns the column vector (P, Q) entering this lane's chunk
+template <class R, int W>
+__device__ __forceinline__ void scan_moebius(M22<R> T, int lane, R &P, R &Q) {
+#pragma unroll
+    for (int d = 1; d < W; d <<= 1) {
+        M22<R> o = shfl_up_m<R, W>(T, d);
+        if (lane >= d) T = mmul(T, o);
+    }
+    // inclusive product S_l = T_l ... T_0; the incoming vector is S_{l-1} (0, 1)^T
+    R pb = __shfl_up_sync(0xffffffffu, T.b, 1, W), qd = __shfl_up_sync(0xffffffffu, T.d, 1, W);
+    if (lane == 0) { pb = R(0.0); qd = R(1.0); }
+    P = pb;
+    Q = qd;
+}
+
+// exclusive forward scan of affine maps y = A y_prev + B; y_(-1) = y0
+template <class R, int W>
+__device__ __forceinline__ R scan_affine_up(R A, R B, int lane, R y0) {
+#pragma unroll
+    for (int d = 1; d < W; d <<= 1) {
+        const R Ap = __shfl_up_sync(0xffffffffu, A, d, W), Bp = __shfl_up_sync(0xffffffffu, B, d, W);
+        if (lane >= d) { B = A * Bp + B; A = A * Ap; }
+    }
+    R Ai = __shfl_up_sync(0xffffffffu, A, 1, W), Bi = __shfl_up_sync(0xffffffffu, B, 1, W);
+    if (lane == 0) return y0;
+    return Ai * y0 + Bi;
+}
+
+// exclusive backward scan of x = C x_next + D; x past the end = 0
+template <class R, int W>
+__device__ __forceinline__ R scan_affine_down(R C, R D, int lane) {
+#pragma unroll
+    for (int d = 1; d < W; d <<= 1) {
+        const R Cn = __shfl_down_sync(0xffffffffu, C, d, W), Dn = __shfl_down_sync(0xffffffffu, D, d, W);
+        if (lane + d < W) { D = C * Dn + D; C = C * Cn; }
+    }
+    R Di = __shfl_down_sync(0xffffffffu, D, 1, W);
+    return lane == W - 1 ? R(0.0) : Di;
+}
+
+template <class R, int MC, int W>
+__global__ void __launch_bounds__(128) k_adis(KP p, AdiBatch B) {
+    const AdiArgs &A = B.a[blockIdx.y];
+    const DGrid &g = p.g;
+    const R diag = (A.comp == CT) ? p.S->acoefi * p.c.pr : p.S->acoefi;
+    const int na = A.a1 - A.a0 + 1, nb = A.b1 - A.b0 + 1;
+    const long long nl = (long long)na * nb;
+    const long long stride = A.dir == 2 ? g.sxy : A.dir == 1 ? g.sx : 1;
+    const int n = A.l2 - A.l1 + 1;
+    if (nl <= 0 || n <= 0) return;
+    const int lane = threadIdx.x & (W - 1);       // W lanes per line, 32/W lines per warp
+    const int m = (n + W - 1) / W;
+    const int r0 = lane * m;
+    const int cnt = max(0, min(m, n - r0));
+    const long long lpb = blockDim.x / W;
+    // every lane of a warp runs the same number of iterations (shuffles need the full warp)
+    const long long nl_pad = (nl + (32 / W) - 1) / (32 / W) * (32 / W);
+    for (long long t = blockIdx.x * lpb + threadIdx.x / W; t < nl_pad; t += (long long)gridDim.x * lpb) {
+        const bool live = t < nl;
+        const long long tl = live ? t : nl - 1;     // a dead lane repeats the last line, stores nothing
+        const int x0 = A.a0 + (int)(tl % na), x1 = A.b0 + (int)(tl / na);
+        int i0, j0, k0;
+        line_coords(A.dir, A.l1, x0, x1, i0, j0, k0);
+        const long long q0 = g.ix(i0, j0, k0);
+        R av[MC], bv[MC], cv[MC], rv[MC];
+#pragma unroll
+        for (int u = 0; u < MC; u++)
+            if (u < cnt) {
+                int i, j, k;
+                line_coords(A.dir, A.l1 + r0 + u, x0, x1, i, j, k);
+                adi_coef<R>(p, A.comp, A.dir, i, j, k, av[u], cv[u]);
+                bv[u] = diag - av[u] - cv[u];
+                rv[u] = diag * R(A.src[q0 + (long long)(r0 + u) * stride]);
+            }
+        // c of the row before this chunk
+        R clast = R(0.0);
+#pragma unroll
+        for (int u = 0; u < MC; u++)
+            if (u == cnt - 1) clast = cv[u];
+        R cprev0 = __shfl_up_sync(0xffffffffu, clast, 1, W);
+        if (lane == 0) cprev0 = R(0.0);
+        R xv[MC];
+        if (!A.periodic) {
+            // 1. pivots bet_j (Moebius in bet_{j-1})
+            M22<R> T{R(1.0), R(0.0), R(0.0), R(1.0)};
+            {
+                R cp = cprev0;
+#pragma unroll
+                for (int u = 0; u < MC; u++)
+                    if (u < cnt) {
+                        M22<R> Tj{R(0.0), R(1.0), -av[u] * cp, bv[u]};
+                        T = mmul_chunk(Tj, T);
+                        cp = cv[u];
+                    }
+            }
+            R P, Q;
+            scan_moebius<R, W>(T, lane, P, Q);
+            R bet = (lane == 0) ? R(0.0) : P / Q;     // bet of the row before the chunk
+            R gmv[MC];
+            {
+                R cp = cprev0;
+#pragma unroll
+                for (int u = 0; u < MC; u++)
+                    if (u < cnt) {
+                        if (lane == 0 && u == 0) {
+                            bet = R(1.0) / bv[u];
+                            gmv[u] = R(0.0);
+                        } else {
+                            const R gm = cp * bet;
+                            bet = R(1.0) / (bv[u] - av[u] * gm);
+                            gmv[u] = gm;
+                        }
+                        bv[u] = bet;          // bv now holds bet_j
+                        cp = cv[u];
+                    }
+            }
+            // 2. forward substitution y_j = (r_j - a_j y_{j-1}) bet_j
+            R Aa = R(1.0), Bb = R(0.0);
+#pragma unroll
+            for (int u = 0; u < MC; u++)
+                if (u < cnt) {
+                    const R mj = (lane == 0 && u == 0) ? R(0.0) : -av[u] * bv[u];
+                    Bb = mj * Bb + rv[u] * bv[u];
+                    Aa = mj * Aa;
+                }
+            R y = scan_affine_up<R, W>(Aa, Bb, lane, R(0.0));
+#pragma unroll
+            for (int u = 0; u < MC; u++)
+                if (u < cnt) {
+                    y = (lane == 0 && u == 0) ? rv[u] * bv[u] : (rv[u] - av[u] * y) * bv[u];
+                    rv[u] = y;            // rv now holds y_j
+                }
+            // 3. back substitution x_j = y_j - gm_{j+1} x_{j+1}
+            R gnext0 = __shfl_down_sync(0xffffffffu, gmv[0], 1, W);   // gm of the row after the chunk
+            R Cc = R(1.0), Dd = R(0.0);
+#pragma unroll
+            for (int u = MC - 1; u >= 0; u--)
+                if (u < cnt) {
+                    const bool last = (r0 + u == n - 1);
+                    const R gn = last ? R(0.0) : (u + 1 < cnt ? gmv[u + 1] : gnext0);
+                    Dd = -gn * Dd + rv[u];
+                    Cc = -gn * Cc;
+                }
+            R x = scan_affine_down<R, W>(Cc, Dd, lane);
+#pragma unroll
+            for (int u = MC - 1; u >= 0; u--)
+                if (u < cnt) {
+                    const bool last = (r0 + u == n - 1);
+                    const R gn = last ? R(0.0) : (u + 1 < cnt ? gmv[u + 1] : gnext0);
+                    x = rv[u] - gn * x;
+                    xv[u] = x;
+                }
+        } else {
+            // trdiagp: q_j = -c_j / (b_j + a_j q_{j-1}) (Moebius), pn_j the pivots
+            M22<R> T{R(1.0), R(0.0), R(0.0), R(1.0)};
+#pragma unroll
+            for (int u = 0; u < MC; u++)
+                if (u < cnt) {
+                    M22<R> Tj{R(0.0), -cv[u], av[u], bv[u]};
+                    T = mmul_chunk(Tj, T);
+                }
+            R P, Q;
+            scan_moebius<R, W>(T, lane, P, Q);
+            R qq = (lane == 0) ? R(0.0) : P / Q;
+            R qv[MC], pv[MC];
+#pragma unroll
+            for (int u = 0; u < MC; u++)
+                if (u < cnt) {
+                    const R pn = (lane == 0 && u == 0) ? R(1.0) / bv[u] : R(1.0) / (bv[u] + av[u] * qq);
+                    qq = -cv[u] * pn;
+                    qv[u] = qq;
+                    pv[u] = pn;
+                }
+            // s_j = (-a_j pn_j) s_{j-1}, s_{-1} = 1;  f_j = (-a_j pn_j) f_{j-1} + r_j pn_j, f_{-1} = 0
+            R Aa = R(1.0), Bb = R(0.0);
+#pragma unroll
+            for (int u = 0; u < MC; u++)
+                if (u < cnt) {
+                    const R mj = -av[u] * pv[u];
+                    Bb = mj * Bb + rv[u] * pv[u];
+                    Aa = mj * Aa;
+                }
+            // incoming s and f: run the same scan for the pair
+            R sA = Aa, fA = Aa, fB = Bb;
+#pragma unroll
+            for (int d = 1; d < W; d <<= 1) {
+                const R sp = __shfl_up_sync(0xffffffffu, sA, d, W);
+                const R Ap = __shfl_up_sync(0xffffffffu, fA, d, W), Bp = __shfl_up_sync(0xffffffffu, fB, d, W);
+                if (lane >= d) { sA = sA * sp; fB = fA * Bp + fB; fA = fA * Ap; }
+            }
+            R s_in = __shfl_up_sync(0xffffffffu, sA, 1, W), f_in = __shfl_up_sync(0xffffffffu, fB, 1, W);
+            if (lane == 0) { s_in = R(1.0); f_in = R(0.0); }
+            R sv[MC], fv[MC];
+            {
+                R sc = s_in, fc = f_in;
+#pragma unroll
+                for (int u = 0; u < MC; u++)
+                    if (u < cnt) {
+                        if (lane == 0 && u == 0) {
+                            sc = -av[u] * pv[u];
+                            fc = rv[u] * pv[u];
+                        } else {
+                            sc = -av[u] * sc * pv[u];
+                            fc = (rv[u] - av[u] * fc) * pv[u];
+                        }
+                        sv[u] = sc;
+                        fv[u] = fc;
+                    }
+            }
+            // backward: S_j = s_j + q_j S_{j+1}, QE_j = f_j + q_j QE_{j+1}; S_{n-1} = 1, QE_{n-1} = 0
+            R Cs = R(1.0), Ds = R(0.0), De = R(0.0);
+#pragma unroll
+            for (int u = MC - 1; u >= 0; u--)
+                if (u < cnt) {
+                    const bool last = (r0 + u == n - 1);
+                    const R mq = last ? R(0.0) : qv[u];
+                    const R os = last ? R(1.0) : sv[u], oe = last ? R(0.0) : fv[u];
+                    Ds = mq * Ds + os;
+                    De = mq * De + oe;
+                    Cs = mq * Cs;
+                }
+#pragma unroll
+            for (int d = 1; d < W; d <<= 1) {
+                const R Cn = __shfl_down_sync(0xffffffffu, Cs, d, W);
+                const R Dsn = __shfl_down_sync(0xffffffffu, Ds, d, W), Den = __shfl_down_sync(0xffffffffu, De, d, W);
+                if (lane + d < W) { Ds = Cs * Dsn + Ds; De = Cs * Den + De; Cs = Cs * Cn; }
+            }
+            R S_in = __shfl_down_sync(0xffffffffu, Ds, 1, W), E_in = __shfl_down_sync(0xffffffffu, De, 1, W);
+            if (lane == W - 1) { S_in = R(0.0); E_in = R(0.0); }
+            {
+                R Sc = S_in, Ec = E_in;
+#pragma unroll
+                for (int u = MC - 1; u >= 0; u--)
+                    if (u < cnt) {
+                        if (r0 + u == n - 1) { Sc = R(1.0); Ec = R(0.0); }
+                        else {
+                            Sc = sv[u] + qv[u] * Sc;
+                            Ec = fv[u] + qv[u] * Ec;
+                        }
+                        sv[u] = Sc;          // S_j
+                        fv[u] = Ec;          // QE_j
+                    }
+            }
+            // fj2 from S_0, QE_0, S_{n-2}, QE_{n-2} and the last row
+            const int own_last = (n - 1) / m, u_last = (n - 1) - own_last * m;
+            const int own_pen = (n - 2) / m, u_pen = (n - 2) - own_pen * m;
+            R al = R(0.0), bl = R(0.0), cl = R(0.0), fnl = R(0.0), Sp = R(0.0), Ep = R(0.0);
+#pragma unroll
+            for (int u = 0; u < MC; u++) {
+                if (u == u_last) { al = av[u]; bl = bv[u]; cl = cv[u]; fnl = rv[u]; }
+                if (u == u_pen) { Sp = sv[u]; Ep = fv[u]; }
+            }
+            al = __shfl_sync(0xffffffffu, al, own_last, W);
+            bl = __shfl_sync(0xffffffffu, bl, own_last, W);
+            cl = __shfl_sync(0xffffffffu, cl, own_last, W);
+            fnl = __shfl_sync(0xffffffffu, fnl, own_last, W);
+            Sp = __shfl_sync(0xffffffffu, Sp, own_pen, W);
+            Ep = __shfl_sync(0xffffffffu, Ep, own_pen, W);
+            const R S0 = __shfl_sync(0xffffffffu, sv[0], 0, W), E0 = __shfl_sync(0xffffffffu, fv[0], 0, W);
+            const R fj2 = (fnl - cl * E0 - al * Ep) / (cl * S0 + al * Sp + bl);
+#pragma unroll
+            for (int u = 0; u < MC; u++)
+                if (u < cnt) xv[u] = (r0 + u == n - 1) ? fj2 : fj2 * sv[u] + fv[u];
+        }
+        // store: the solution, or added to the field
+#pragma unroll
+        for (int u = 0; u < MC; u++)
+            if (live && u < cnt) {
+                const long long q = q0 + (long long)(r0 + u) * stride;
+                if (A.add) A.dst[q] = A.dst[q] + xv[u];
+                else A.dst[q] = xv[u];
+            }
+    }
+}
+
+template <class R, int W>
+static bool adis_launch(lesgpu_case *c, const AdiBatch &B, int ncomp, long long mx, int nmax) {
+    const int m = (nmax + W - 1) / W;
+    const long long lpb = 128 / W;
+    dim3 grid((unsigned)((mx + lpb - 1) / lpb), (unsigned)ncomp);
+    if (m <= 2) k_adis<R, 2, W><<<grid, 128, 0, c->stream>>>(c->kp, B);
+    else if (m <= 4) k_adis<R, 4, W><<<grid, 128, 0, c->stream>>>(c->kp, B);
+    else if (m <= 8) k_adis<R, 8, W><<<grid, 128, 0, c->stream>>>(c->kp, B);
+    else if (m <= 12) k_adis<R, 12, W><<<grid, 128, 0, c->stream>>>(c->kp, B);
+    else return false;
+    return true;
 }
 
 // One launch sweeps the same direction for up to three components at once
@@ -280,8 +618,30 @@ static void adi_launch(lesgpu_case *c, const AdiBatch &B, int ncomp) {
     }
     if (mx <= 0) return;
     dim3 grid((unsigned)((mx + 31) / 32), (unsigned)ncomp);
+    // mixed-precision form: FP32 arithmetic for the x and z sweeps, the
+    // wall-normal (stretched) y sweep stays FP64
+    const bool f32 = c->cfg.precision == LESGPU_PREC_MIXED && B.a[0].dir != 1;
+    int nmax = 0;
+    for (int q = 0; q < ncomp; q++) nmax = max(nmax, B.a[q].l2 - B.a[q].l1 + 1);
     inst_begin(c, LESGPU_K_ADI);
-    k_adi<<<grid, 32, 0, c->stream>>>(c->kp, B);
+    // FP32 sweeps: 32 lanes per line; FP64 sweeps: about 8 rows per lane, since
+    // the scan form costs ~2.5x the FP64 operations of the serial recurrence and
+    // a GB300 SM retires few FP64 FMAs per clock.  Longer lines (more than 12
+    // rows per lane) keep one thread per line.
+    bool done;
+    if (f32) {
+        done = adis_launch<float, 32>(c, B, ncomp, mx, nmax);
+    } else {
+        // about 8 rows per lane: 8 lanes for 64-row lines, 16 up to 128, 32 above
+        const int w = nmax <= 64 ? 8 : nmax <= 128 ? 16 : 32;
+        done = w == 8 ? adis_launch<double, 8>(c, B, ncomp, mx, nmax)
+             : w == 16 ? adis_launch<double, 16>(c, B, ncomp, mx, nmax)
+                       : adis_launch<double, 32>(c, B, ncomp, mx, nmax);
+    }
+    if (!done) {
+        if (f32) k_adi<float><<<grid, 32, 0, c->stream>>>(c->kp, B);
+        else k_adi<double><<<grid, 32, 0, c->stream>>>(c->kp, B);
+    }
     inst_end(c, LESGPU_K_ADI);
 }
 

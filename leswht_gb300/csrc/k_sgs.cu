@@ -14,155 +14,169 @@
 
 namespace lg {
 
-// velgrad, sgs.f90:772-875
-__device__ void velgrad(const KP &p, int i, int j, int k, double a[9], double sr[6]) {
+// velgrad, sgs.f90:772-875.  R: arithmetic type (float in the mixed form).
+template <class R>
+__device__ void velgrad(const KP &p, int i, int j, int k, R a[9], R sr[6]) {
     const DGrid &g = p.g;
     const double *u = p.f.u, *v = p.f.v, *w = p.f.w;
     int kp = g.kpv[k], km = g.kmv[k], jp = g.jpv[j], jm = g.jmv[j], ip = g.ipv[i], im = g.imv[i];
     int n1 = g.n1, n2 = g.n2, n3 = g.n3;
-    double fju = fixd(g.fixju[j]), fjl = fixd(g.fixjl[j]), fku = fixd(g.fixku[k]), fkl = fixd(g.fixkl[k]);
-    double fiu = fixd(g.fixiu[i]), fil = fixd(g.fixil[i]);
+    R fju = fixd(g.fixju[j]), fjl = fixd(g.fixjl[j]), fku = fixd(g.fixku[k]), fkl = fixd(g.fixkl[k]);
+    R fiu = fixd(g.fixiu[i]), fil = fixd(g.fixil[i]);
     const double *f2fx = g.f2fx, *f2fy = g.f2fy, *f2fz = g.f2fz;
-#define U(a_, b_, c_) u[g.ix(a_, b_, c_)]
-#define V(a_, b_, c_) v[g.ix(a_, b_, c_)]
-#define W(a_, b_, c_) w[g.ix(a_, b_, c_)]
-    double vg11 = g.f2fxi[i] * (U(ip, j, k) - U(i, j, k));
-    double up = g.c2cyi[jp] * 0.25 * (f2fy[jp] * (U(i, j, k) + U(ip, j, k)) + f2fy[j] * (U(i, jp, k) + U(ip, jp, k))) * (1.0 - fju)
-              + 0.5 * (U(i, n2, k) + U(ip, n2, k)) * fju;
-    double um = g.c2cyi[j] * 0.25 * (f2fy[j] * (U(i, jm, k) + U(ip, jm, k)) + f2fy[jm] * (U(i, j, k) + U(ip, j, k))) * (1.0 - fjl)
-              + 0.5 * (U(i, 0, k) + U(ip, 0, k)) * fjl;
-    double vg12 = g.f2fyi[j] * (up - um);
-    up = g.c2czi[kp] * 0.25 * (f2fz[kp] * (U(i, j, k) + U(ip, j, k)) + f2fz[k] * (U(i, j, kp) + U(ip, j, kp))) * (1.0 - fku)
-       + 0.5 * (U(i, j, n3) + U(ip, j, n3)) * fku;
-    um = g.c2czi[k] * 0.25 * (f2fz[k] * (U(i, j, km) + U(ip, j, km)) + f2fz[km] * (U(i, j, k) + U(ip, j, k))) * (1.0 - fkl)
-       + 0.5 * (U(i, j, 0) + U(ip, j, 0)) * fkl;
-    double vg13 = g.f2fzi[k] * (up - um);
-    double vp = g.c2cxi[ip] * 0.25 * (f2fx[ip] * (V(i, j, k) + V(i, jp, k)) + f2fx[i] * (V(ip, j, k) + V(ip, jp, k))) * (1.0 - fiu)
-              + 0.5 * (V(n1, j, k) + V(n1, jp, k)) * fiu;
-    double vm = g.c2cxi[i] * 0.25 * (f2fx[i] * (V(im, j, k) + V(im, jp, k)) + f2fx[im] * (V(i, j, k) + V(i, jp, k))) * (1.0 - fil)
-              + 0.5 * (V(0, j, k) + V(0, jp, k)) * fil;
-    double vg21 = g.f2fxi[i] * (vp - vm);
-    double vg22 = g.f2fyi[j] * (V(i, jp, k) - V(i, j, k));
-    vp = g.c2czi[kp] * 0.25 * (f2fz[kp] * (V(i, j, k) + V(i, jp, k)) + f2fz[k] * (V(i, j, kp) + V(i, jp, kp))) * (1.0 - fku)
-       + 0.5 * (V(i, j, n3) + V(i, jp, n3)) * fku;
-    vm = g.c2czi[k] * 0.25 * (f2fz[k] * (V(i, j, km) + V(i, jp, km)) + f2fz[km] * (V(i, j, k) + V(i, jp, k))) * (1.0 - fkl)
-       + 0.5 * (V(i, j, 0) + V(i, jp, 0)) * fkl;
-    double vg23 = g.f2fzi[k] * (vp - vm);
-    double wp = g.c2cxi[ip] * 0.25 * (f2fx[ip] * (W(i, j, k) + W(i, j, kp)) + f2fx[i] * (W(ip, j, k) + W(ip, j, kp))) * (1.0 - fiu)
-              + 0.5 * (W(n1, j, k) + W(n1, j, kp)) * fiu;
-    double wm = g.c2cxi[i] * 0.25 * (f2fx[i] * (W(im, j, k) + W(im, j, kp)) + f2fx[im] * (W(i, j, k) + W(i, j, kp))) * (1.0 - fil)
-              + 0.5 * (W(0, j, k) + W(0, j, kp)) * fil;
-    double vg31 = g.f2fxi[i] * (wp - wm);
-    wp = g.c2cyi[jp] * 0.25 * (f2fy[jp] * (W(i, j, k) + W(i, j, kp)) + f2fy[j] * (W(i, jp, k) + W(i, jp, kp))) * (1.0 - fju)
-       + 0.5 * (W(i, n2, k) + W(i, n2, kp)) * fju;
-    wm = g.c2cyi[j] * 0.25 * (f2fy[j] * (W(i, jm, k) + W(i, jm, kp)) + f2fy[jm] * (W(i, j, k) + W(i, j, kp))) * (1.0 - fjl)
-       + 0.5 * (W(i, 0, k) + W(i, 0, kp)) * fjl;
-    double vg32 = g.f2fyi[j] * (wp - wm);
-    double vg33 = g.f2fzi[k] * (W(i, j, kp) - W(i, j, k));
+#define U(a_, b_, c_) R(u[g.ix(a_, b_, c_)])
+#define V(a_, b_, c_) R(v[g.ix(a_, b_, c_)])
+#define W(a_, b_, c_) R(w[g.ix(a_, b_, c_)])
+    R vg11 = R(g.f2fxi[i]) * (U(ip, j, k) - U(i, j, k));
+    R up = R(g.c2cyi[jp]) * R(0.25) * (R(f2fy[jp]) * (U(i, j, k) + U(ip, j, k)) + R(f2fy[j]) * (U(i, jp, k) + U(ip, jp, k))) * (R(1.0) - fju)
+              + R(0.5) * (U(i, n2, k) + U(ip, n2, k)) * fju;
+    R um = R(g.c2cyi[j]) * R(0.25) * (R(f2fy[j]) * (U(i, jm, k) + U(ip, jm, k)) + R(f2fy[jm]) * (U(i, j, k) + U(ip, j, k))) * (R(1.0) - fjl)
+              + R(0.5) * (U(i, 0, k) + U(ip, 0, k)) * fjl;
+    R vg12 = R(g.f2fyi[j]) * (up - um);
+    up = R(g.c2czi[kp]) * R(0.25) * (R(f2fz[kp]) * (U(i, j, k) + U(ip, j, k)) + R(f2fz[k]) * (U(i, j, kp) + U(ip, j, kp))) * (R(1.0) - fku)
+       + R(0.5) * (U(i, j, n3) + U(ip, j, n3)) * fku;
+    um = R(g.c2czi[k]) * R(0.25) * (R(f2fz[k]) * (U(i, j, km) + U(ip, j, km)) + R(f2fz[km]) * (U(i, j, k) + U(ip, j, k))) * (R(1.0) - fkl)
+       + R(0.5) * (U(i, j, 0) + U(ip, j, 0)) * fkl;
+    R vg13 = R(g.f2fzi[k]) * (up - um);
+    R vp = R(g.c2cxi[ip]) * R(0.25) * (R(f2fx[ip]) * (V(i, j, k) + V(i, jp, k)) + R(f2fx[i]) * (V(ip, j, k) + V(ip, jp, k))) * (R(1.0) - fiu)
+              + R(0.5) * (V(n1, j, k) + V(n1, jp, k)) * fiu;
+    R vm = R(g.c2cxi[i]) * R(0.25) * (R(f2fx[i]) * (V(im, j, k) + V(im, jp, k)) + R(f2fx[im]) * (V(i, j, k) + V(i, jp, k))) * (R(1.0) - fil)
+              + R(0.5) * (V(0, j, k) + V(0, jp, k)) * fil;
+    R vg21 = R(g.f2fxi[i]) * (vp - vm);
+    R vg22 = R(g.f2fyi[j]) * (V(i, jp, k) - V(i, j, k));
+    vp = R(g.c2czi[kp]) * R(0.25) * (R(f2fz[kp]) * (V(i, j, k) + V(i, jp, k)) + R(f2fz[k]) * (V(i, j, kp) + V(i, jp, kp))) * (R(1.0) - fku)
+       + R(0.5) * (V(i, j, n3) + V(i, jp, n3)) * fku;
+    vm = R(g.c2czi[k]) * R(0.25) * (R(f2fz[k]) * (V(i, j, km) + V(i, jp, km)) + R(f2fz[km]) * (V(i, j, k) + V(i, jp, k))) * (R(1.0) - fkl)
+       + R(0.5) * (V(i, j, 0) + V(i, jp, 0)) * fkl;
+    R vg23 = R(g.f2fzi[k]) * (vp - vm);
+    R wp = R(g.c2cxi[ip]) * R(0.25) * (R(f2fx[ip]) * (W(i, j, k) + W(i, j, kp)) + R(f2fx[i]) * (W(ip, j, k) + W(ip, j, kp))) * (R(1.0) - fiu)
+              + R(0.5) * (W(n1, j, k) + W(n1, j, kp)) * fiu;
+    R wm = R(g.c2cxi[i]) * R(0.25) * (R(f2fx[i]) * (W(im, j, k) + W(im, j, kp)) + R(f2fx[im]) * (W(i, j, k) + W(i, j, kp))) * (R(1.0) - fil)
+              + R(0.5) * (W(0, j, k) + W(0, j, kp)) * fil;
+    R vg31 = R(g.f2fxi[i]) * (wp - wm);
+    wp = R(g.c2cyi[jp]) * R(0.25) * (R(f2fy[jp]) * (W(i, j, k) + W(i, j, kp)) + R(f2fy[j]) * (W(i, jp, k) + W(i, jp, kp))) * (R(1.0) - fju)
+       + R(0.5) * (W(i, n2, k) + W(i, n2, kp)) * fju;
+    wm = R(g.c2cyi[j]) * R(0.25) * (R(f2fy[j]) * (W(i, jm, k) + W(i, jm, kp)) + R(f2fy[jm]) * (W(i, j, k) + W(i, j, kp))) * (R(1.0) - fjl)
+       + R(0.5) * (W(i, 0, k) + W(i, 0, kp)) * fjl;
+    R vg32 = R(g.f2fyi[j]) * (wp - wm);
+    R vg33 = R(g.f2fzi[k]) * (W(i, j, kp) - W(i, j, k));
 #undef U
 #undef V
 #undef W
     a[0] = vg11; a[1] = vg21; a[2] = vg31;
     a[3] = vg12; a[4] = vg22; a[5] = vg32;
     a[6] = vg13; a[7] = vg23; a[8] = vg33;
-    sr[0] = vg11; sr[1] = 0.5 * (vg12 + vg21); sr[2] = 0.5 * (vg13 + vg31);
-    sr[3] = vg22; sr[4] = 0.5 * (vg23 + vg32); sr[5] = vg33;
+    sr[0] = vg11; sr[1] = R(0.5) * (vg12 + vg21); sr[2] = R(0.5) * (vg13 + vg31);
+    sr[3] = vg22; sr[4] = R(0.5) * (vg23 + vg32); sr[5] = vg33;
 }
 
 // temgrad, sgs.f90:1480-1525
-__device__ void temgrad(const KP &p, int i, int j, int k, double a[3]) {
+template <class R>
+__device__ void temgrad(const KP &p, int i, int j, int k, R a[3]) {
     const DGrid &g = p.g;
     const double *t = p.f.t;
     int kp = g.kpv[k], km = g.kmv[k], jp = g.jpv[j], jm = g.jmv[j], ip = g.ipv[i], im = g.imv[i];
-    double fiu = fixd(g.fixiu[i]), fil = fixd(g.fixil[i]), fju = fixd(g.fixju[j]), fjl = fixd(g.fixjl[j]);
-    double fku = fixd(g.fixku[k]), fkl = fixd(g.fixkl[k]);
-    double tc = t[g.ix(i, j, k)];
-    double tip = t[g.ix(ip, j, k)], tim = t[g.ix(im, j, k)];
-    double tp = 0.5 * (g.f2fx[i] * tip + g.f2fx[ip] * tc) * g.c2cxi[ip] * (1.0 - fiu) + tip * fiu;
-    double tm = 0.5 * (g.f2fx[im] * tc + g.f2fx[i] * tim) * g.c2cxi[i] * (1.0 - fil) + tim * fil;
-    a[0] = g.f2fxi[i] * (tp - tm);
-    double tjp = t[g.ix(i, jp, k)], tjm = t[g.ix(i, jm, k)];
-    tp = 0.5 * (g.f2fy[j] * tjp + g.f2fy[jp] * tc) * g.c2cyi[jp] * (1.0 - fju) + tjp * fju;
-    tm = 0.5 * (g.f2fy[jm] * tc + g.f2fy[j] * tjm) * g.c2cyi[j] * (1.0 - fjl) + tjm * fjl;
-    a[1] = g.f2fyi[j] * (tp - tm);
-    double tkp = t[g.ix(i, j, kp)], tkm = t[g.ix(i, j, km)];
-    tp = 0.5 * (g.f2fz[k] * tkp + g.f2fz[kp] * tc) * g.c2czi[kp] * (1.0 - fku) + tkp * fku;
-    tm = 0.5 * (g.f2fz[km] * tc + g.f2fz[k] * tkm) * g.c2czi[k] * (1.0 - fkl) + tkm * fkl;
-    a[2] = g.f2fzi[k] * (tp - tm);
+    R fiu = fixd(g.fixiu[i]), fil = fixd(g.fixil[i]), fju = fixd(g.fixju[j]), fjl = fixd(g.fixjl[j]);
+    R fku = fixd(g.fixku[k]), fkl = fixd(g.fixkl[k]);
+    R tc = R(t[g.ix(i, j, k)]);
+    R tip = R(t[g.ix(ip, j, k)]), tim = R(t[g.ix(im, j, k)]);
+    R tp = R(0.5) * (R(g.f2fx[i]) * tip + R(g.f2fx[ip]) * tc) * R(g.c2cxi[ip]) * (R(1.0) - fiu) + tip * fiu;
+    R tm = R(0.5) * (R(g.f2fx[im]) * tc + R(g.f2fx[i]) * tim) * R(g.c2cxi[i]) * (R(1.0) - fil) + tim * fil;
+    a[0] = R(g.f2fxi[i]) * (tp - tm);
+    R tjp = R(t[g.ix(i, jp, k)]), tjm = R(t[g.ix(i, jm, k)]);
+    tp = R(0.5) * (R(g.f2fy[j]) * tjp + R(g.f2fy[jp]) * tc) * R(g.c2cyi[jp]) * (R(1.0) - fju) + tjp * fju;
+    tm = R(0.5) * (R(g.f2fy[jm]) * tc + R(g.f2fy[j]) * tjm) * R(g.c2cyi[j]) * (R(1.0) - fjl) + tjm * fjl;
+    a[1] = R(g.f2fyi[j]) * (tp - tm);
+    R tkp = R(t[g.ix(i, j, kp)]), tkm = R(t[g.ix(i, j, km)]);
+    tp = R(0.5) * (R(g.f2fz[k]) * tkp + R(g.f2fz[kp]) * tc) * R(g.c2czi[kp]) * (R(1.0) - fku) + tkp * fku;
+    tm = R(0.5) * (R(g.f2fz[km]) * tc + R(g.f2fz[k]) * tkm) * R(g.c2czi[k]) * (R(1.0) - fkl) + tkm * fkl;
+    a[2] = R(g.f2fzi[k]) * (tp - tm);
 }
 
-__device__ __forceinline__ void vreman(const double alp[9], double sdx2, double sdy2, double sdz2, double &aaa, double &bbb) {
-    double b1 = sdx2 * alp[0] * alp[0] + sdy2 * alp[3] * alp[3] + sdz2 * alp[6] * alp[6];
-    double b2 = sdx2 * alp[0] * alp[1] + sdy2 * alp[3] * alp[4] + sdz2 * alp[6] * alp[7];
-    double b3 = sdx2 * alp[0] * alp[2] + sdy2 * alp[3] * alp[5] + sdz2 * alp[6] * alp[8];
-    double b4 = sdx2 * alp[1] * alp[1] + sdy2 * alp[4] * alp[4] + sdz2 * alp[7] * alp[7];
-    double b5 = sdx2 * alp[1] * alp[2] + sdy2 * alp[4] * alp[5] + sdz2 * alp[7] * alp[8];
-    double b6 = sdx2 * alp[2] * alp[2] + sdy2 * alp[5] * alp[5] + sdz2 * alp[8] * alp[8];
-    double a = 0.0;
+template <class R>
+__device__ __forceinline__ void vreman(const R alp[9], R sdx2, R sdy2, R sdz2, R &aaa, R &bbb) {
+    R b1 = sdx2 * R(alp[0]) * R(alp[0]) + sdy2 * R(alp[3]) * R(alp[3]) + sdz2 * R(alp[6]) * R(alp[6]);
+    R b2 = sdx2 * R(alp[0]) * R(alp[1]) + sdy2 * R(alp[3]) * R(alp[4]) + sdz2 * R(alp[6]) * R(alp[7]);
+    R b3 = sdx2 * R(alp[0]) * R(alp[2]) + sdy2 * R(alp[3]) * R(alp[5]) + sdz2 * R(alp[6]) * R(alp[8]);
+    R b4 = sdx2 * R(alp[1]) * R(alp[1]) + sdy2 * R(alp[4]) * R(alp[4]) + sdz2 * R(alp[7]) * R(alp[7]);
+    R b5 = sdx2 * R(alp[1]) * R(alp[2]) + sdy2 * R(alp[4]) * R(alp[5]) + sdz2 * R(alp[7]) * R(alp[8]);
+    R b6 = sdx2 * R(alp[2]) * R(alp[2]) + sdy2 * R(alp[5]) * R(alp[5]) + sdz2 * R(alp[8]) * R(alp[8]);
+    R a = R(0.0);
 #pragma unroll
-    for (int q = 0; q < 9; q++) a += alp[q] * alp[q];
-    double b = b1 * b4 + b4 * b6 + b6 * b1 - b2 * b2 - b3 * b3 - b5 * b5;
-    if (b < 1.0e-16) b = 1.0e-16;
+    for (int q = 0; q < 9; q++) a += R(alp[q]) * R(alp[q]);
+    R b = b1 * b4 + b4 * b6 + b6 * b1 - b2 * b2 - b3 * b3 - b5 * b5;
+    if (b < R(1.0e-16)) b = R(1.0e-16);
     aaa = a;
     bbb = b;
 }
 
 // Test-filter width at a cell: the sum of the three test-filter cell widths
 // used in the second Vreman / eddy-diffusivity evaluation (sgs.f90:528-533).
-__device__ __forceinline__ double tf_width(const double *f2f, const int *fl, const int *fu, int i) {
-    return 0.5 * f2f[i - 1] * (1.0 - fixd(fu[i])) + f2f[i] + 0.5 * f2f[i + 1] * (1.0 - fixd(fl[i]));
+template <class R>
+__device__ __forceinline__ R tf_width(const double *f2f, const int *fl, const int *fu, int i) {
+    return R(0.5) * R(f2f[i - 1]) * (R(1.0) - fixd(fu[i])) + R(f2f[i]) + R(0.5) * R(f2f[i + 1]) * (R(1.0) - fixd(fl[i]));
 }
 
 #define GRID_LOOP(b)                                                                                   \
     for (long long tt = (long long)blockIdx.x * blockDim.x + threadIdx.x, nn_ = (b).count(); tt < nn_; \
          tt += (long long)gridDim.x * blockDim.x)
 
+// SGS scratch arrays (scr[3..32]) hold R values: float in the mixed form,
+// where they take half of each nt-double buffer.
+template <class R>
+__device__ __forceinline__ R *scr(const KP &p, int s) { return reinterpret_cast<R *>(p.f.scr[s]); }
+
 // pass 1 of sgs_dvmg (:434-491) and the constant model sgs_cvm
+template <class R>
 __global__ void __launch_bounds__(kThreads) k_vreman1(KP p, Box b, int dynamic) {
     const DGrid &g = p.g;
-    double **A = p.f.scr + 3;       // mm[0..5] in scr[3..8], alp[0..8] in scr[9..17]
-    GRID_LOOP(b) {
+    GRID_LOOP(b) {      // mm[0..5] in scr[3..8], alp[0..8] in scr[9..17]
         int i, j, k;
         b.at(tt, i, j, k);
-        double alp[9], str[6], aaa, bbb;
-        velgrad(p, i, j, k, alp, str);
-        vreman(alp, g.f2fx[i] * g.f2fx[i], g.f2fy[j] * g.f2fy[j], g.f2fz[k] * g.f2fz[k], aaa, bbb);
+        R alp[9], str[6], aaa, bbb;
+        velgrad<R>(p, i, j, k, alp, str);
+        const R fx = R(g.f2fx[i]), fy = R(g.f2fy[j]), fz = R(g.f2fz[k]);
+        vreman<R>(alp, fx * fx, fy * fy, fz * fz, aaa, bbb);
         long long q = g.ix(i, j, k);
         if (!dynamic) {
-            p.f.nusgs[q] = (aaa == 0.0) ? 0.0 : p.c.csgsts * sqrt(bbb / aaa);
+            p.f.nusgs[q] = (aaa == R(0.0)) ? R(0.0) : R(p.c.csgsts) * sqrt(bbb / aaa);
             continue;
         }
-        double nu = (aaa == 0.0) ? 0.0 : sqrt(bbb / aaa);
+        R nu = (aaa == R(0.0)) ? R(0.0) : sqrt(bbb / aaa);
         p.f.nusgs[q] = nu;
 #pragma unroll
-        for (int m = 0; m < 6; m++) A[m][q] = nu * str[m];
+        for (int m = 0; m < 6; m++) scr<R>(p, 3 + m)[q] = nu * str[m];
 #pragma unroll
-        for (int m = 0; m < 9; m++) A[6 + m][q] = alp[m];
+        for (int m = 0; m < 9; m++) scr<R>(p, 9 + m)[q] = alp[m];
     }
 }
 
-// Batched test filter: dst[a] = filter(src[a]) on the interior, a < na.
+// Batched test filter: dst[a] = filter(src[a]) on the interior, a < na
+// (arrays of R).
 struct FiltBatch {
-    const double *src[16];
-    double *dst[16];
+    const void *src[16];
+    void *dst[16];
     int na;
 };
 
-__device__ __forceinline__ double filt_x(const KP &p, const double *s, int i, long long qrow, int xf) {
+template <class R>
+__device__ __forceinline__ R filt_x(const KP &p, const R *s, int i, long long qrow, int xf) {
     const DGrid &g = p.g;
     // qrow = index of (0, j, k)
     if (!xf) return s[qrow + i];
     const double *cf = p.f.cfx1 + 3 * i;
+    const R c0 = R(cf[0]), c1 = R(cf[1]), c2 = R(cf[2]);
     if (i >= 2 && i <= g.n1m - 1)
-        return cf[0] * s[qrow + i - 1] + cf[1] * s[qrow + i] + cf[2] * s[qrow + i + 1];
+        return c0 * s[qrow + i - 1] + c1 * s[qrow + i] + c2 * s[qrow + i + 1];
     if (p.c.xprdic == 1) {
         if (g.n1m == 1) return s[qrow + i];
-        if (i == 1) return cf[0] * s[qrow + g.n1m] + cf[1] * s[qrow + 1] + cf[2] * s[qrow + 2];
-        return cf[0] * s[qrow + g.n1m - 1] + cf[1] * s[qrow + g.n1m] + cf[2] * s[qrow + 1];
+        if (i == 1) return c0 * s[qrow + g.n1m] + c1 * s[qrow + 1] + c2 * s[qrow + 2];
+        return c0 * s[qrow + g.n1m - 1] + c1 * s[qrow + g.n1m] + c2 * s[qrow + 1];
     }
     return s[qrow + i];
 }
 
+template <class R>
 __global__ void __launch_bounds__(kThreads) k_filter(KP p, Box b, FiltBatch F) {
     const DGrid &g = p.g;
     int xf = (p.c.filter == 1 || p.c.filter == 3) ? 1 : 0;
@@ -173,83 +187,87 @@ __global__ void __launch_bounds__(kThreads) k_filter(KP p, Box b, FiltBatch F) {
         int a = (int)(tt / n);
         int i, j, k;
         b.at(tt - (long long)a * n, i, j, k);
-        const double *s = F.src[a];
-        double out;
+        const R *s = static_cast<const R *>(F.src[a]);
+        R out;
         // z-periodic ends use the wrapped neighbours; with n3m = 1 the weights
         // are zero (sgsfilterinit skips them), so the filtered value is 0 as
         // in test_filter (sgs.f90:735-764)
         bool zin = zf && ((k >= 2 && k <= g.n3m - 1) || p.c.zprdic == 1);
         if (!zin) {
-            out = filt_x(p, s, i, g.ix(0, j, k), xf);
+            out = filt_x<R>(p, s, i, g.ix(0, j, k), xf);
         } else {
             int km = k - 1, kp = k + 1;
             if (k == 1) km = g.n3m;
             if (k == g.n3m) kp = 1;
             const double *cf = p.f.cfz1 + 3 * k;
-            double xm = filt_x(p, s, i, g.ix(0, j, km), xf);
-            double x0 = filt_x(p, s, i, g.ix(0, j, k), xf);
-            double xp = filt_x(p, s, i, g.ix(0, j, kp), xf);
-            out = cf[0] * xm + cf[1] * x0 + cf[2] * xp;
+            R xm = filt_x<R>(p, s, i, g.ix(0, j, km), xf);
+            R x0 = filt_x<R>(p, s, i, g.ix(0, j, k), xf);
+            R xp = filt_x<R>(p, s, i, g.ix(0, j, kp), xf);
+            out = R(cf[0]) * xm + R(cf[1]) * x0 + R(cf[2]) * xp;
         }
-        F.dst[a][g.ix(i, j, k)] = out;
+        static_cast<R *>(F.dst[a])[g.ix(i, j, k)] = out;
     }
 }
+
+static bool mixed(const lesgpu_case *c) { return c->cfg.precision == LESGPU_PREC_MIXED; }
 
 static void filter_batch(lesgpu_case *c, FiltBatch &F) {
     const DGrid &g = c->kp.g;
     Box b{1, 1, 1, g.n1m, g.n2m, g.n3m};
     inst_begin(c, LESGPU_K_SGS);
-    k_filter<<<blocks_for(b.count() * F.na), kThreads, 0, c->stream>>>(c->kp, b, F);
+    if (mixed(c)) k_filter<float><<<blocks_for(b.count() * F.na), kThreads, 0, c->stream>>>(c->kp, b, F);
+    else k_filter<double><<<blocks_for(b.count() * F.na), kThreads, 0, c->stream>>>(c->kp, b, F);
     inst_end(c, LESGPU_K_SGS);
 }
 
 // pass 2 of sgs_dvmg (:504-580): filtered gradients -> test-level Vreman
 // viscosity, M_ij update, resolved velocities and their products.
+// filtered mm[0..5] in scr[18..23] (updated in place), filtered alp[0..8] in
+// scr[24..32]; out: uui[0..2], llij[0..5] in scr[3..11]
+template <class R>
 __global__ void __launch_bounds__(kThreads) k_vreman2(KP p, Box b) {
     const DGrid &g = p.g;
-    double **FM = p.f.scr + 18;     // filtered mm[0..5]  (updated in place)
-    double **FA = p.f.scr + 24;     // filtered alp[0..8] (scr[24..32])
-    double **OUT = p.f.scr + 3;     // uui[0..2], llij[0..5] -> scr[3..11]
     GRID_LOOP(b) {
         int i, j, k;
         b.at(tt, i, j, k);
         long long q = g.ix(i, j, k);
-        double alp[9], str[6], aaa, bbb;
+        R alp[9], str[6], aaa, bbb;
 #pragma unroll
-        for (int m = 0; m < 9; m++) alp[m] = FA[m][q];
-        str[0] = alp[0]; str[1] = 0.5 * (alp[3] + alp[1]); str[2] = 0.5 * (alp[6] + alp[2]);
-        str[3] = alp[4]; str[4] = 0.5 * (alp[7] + alp[5]); str[5] = alp[8];
-        double sx = tf_width(g.f2fx, g.fixil, g.fixiu, i);
-        double sy = tf_width(g.f2fy, g.fixjl, g.fixju, j);
-        double sz = tf_width(g.f2fz, g.fixkl, g.fixku, k);
-        vreman(alp, sx * sx, sy * sy, sz * sz, aaa, bbb);
-        double ami = (aaa == 0.0) ? 0.0 : sqrt(bbb / aaa);
+        for (int m = 0; m < 9; m++) alp[m] = scr<R>(p, 24 + m)[q];
+        str[0] = alp[0]; str[1] = R(0.5) * (alp[3] + alp[1]); str[2] = R(0.5) * (alp[6] + alp[2]);
+        str[3] = alp[4]; str[4] = R(0.5) * (alp[7] + alp[5]); str[5] = alp[8];
+        R sx = tf_width<R>(g.f2fx, g.fixil, g.fixiu, i);
+        R sy = tf_width<R>(g.f2fy, g.fixjl, g.fixju, j);
+        R sz = tf_width<R>(g.f2fz, g.fixkl, g.fixku, k);
+        vreman<R>(alp, sx * sx, sy * sy, sz * sz, aaa, bbb);
+        R ami = (aaa == R(0.0)) ? R(0.0) : sqrt(bbb / aaa);
 #pragma unroll
-        for (int m = 0; m < 6; m++) FM[m][q] = ami * str[m] - FM[m][q];
-        double u1 = 0.5 * (p.f.u[q] + p.f.u[q + 1]);
-        double u2 = 0.5 * (p.f.v[q] + p.f.v[q + g.sx]);
-        double u3 = 0.5 * (p.f.w[q] + p.f.w[q + g.sxy]);
-        OUT[0][q] = u1; OUT[1][q] = u2; OUT[2][q] = u3;
-        OUT[3][q] = u1 * u1; OUT[4][q] = u1 * u2; OUT[5][q] = u1 * u3;
-        OUT[6][q] = u2 * u2; OUT[7][q] = u2 * u3; OUT[8][q] = u3 * u3;
+        for (int m = 0; m < 6; m++) scr<R>(p, 18 + m)[q] = ami * str[m] - scr<R>(p, 18 + m)[q];
+        R u1 = R(0.5) * (R(p.f.u[q]) + R(p.f.u[q + 1]));
+        R u2 = R(0.5) * (R(p.f.v[q]) + R(p.f.v[q + g.sx]));
+        R u3 = R(0.5) * (R(p.f.w[q]) + R(p.f.w[q + g.sxy]));
+        scr<R>(p, 3)[q] = u1; scr<R>(p, 4)[q] = u2; scr<R>(p, 5)[q] = u3;
+        scr<R>(p, 6)[q] = u1 * u1; scr<R>(p, 7)[q] = u1 * u2; scr<R>(p, 8)[q] = u1 * u3;
+        scr<R>(p, 9)[q] = u2 * u2; scr<R>(p, 10)[q] = u2 * u3; scr<R>(p, 11)[q] = u3 * u3;
     }
 }
 
-// global least-squares sums (:593-618)
+// global least-squares sums (:593-618): M_ij in scr[18..23], filtered uui in
+// scr[24..26], filtered llij in scr[27..32]
+template <class R>
 struct LmMmTerm {
     __device__ void operator()(const KP &p, int i, int j, int k, double *w) const {
         const DGrid &g = p.g;
         long long q = g.ix(i, j, k);
-        double *const *FM = p.f.scr + 18;   // M_ij
-        double *const *FU = p.f.scr + 24;   // filtered uui (scr[24..26]) and llij (scr[27..32])
-        double vol = g.f2fx[i] * g.f2fy[j] * g.f2fz[k];
-        double u1 = FU[0][q], u2 = FU[1][q], u3 = FU[2][q];
-        double L0 = FU[3][q] - u1 * u1, L1 = FU[4][q] - u1 * u2, L2 = FU[5][q] - u1 * u3;
-        double L3 = FU[6][q] - u2 * u2, L4 = FU[7][q] - u2 * u3, L5 = FU[8][q] - u3 * u3;
-        double M0 = FM[0][q], M1 = FM[1][q], M2 = FM[2][q], M3 = FM[3][q], M4 = FM[4][q], M5 = FM[5][q];
-        double nw = (double)p.f.nwall[q];
-        w[0] = (2.0 * L1 * M1 + L0 * M0 + 2.0 * L2 * M2 + L3 * M3 + 2.0 * L4 * M4 + L5 * M5) * nw * vol;
-        w[1] = (2.0 * M1 * M1 + M0 * M0 + 2.0 * M2 * M2 + M3 * M3 + 2.0 * M4 * M4 + M5 * M5) * nw * vol;
+        R vol = R(g.f2fx[i]) * R(g.f2fy[j]) * R(g.f2fz[k]);
+        R u1 = scr<R>(p, 24)[q], u2 = scr<R>(p, 25)[q], u3 = scr<R>(p, 26)[q];
+        R L0 = scr<R>(p, 27)[q] - u1 * u1, L1 = scr<R>(p, 28)[q] - u1 * u2, L2 = scr<R>(p, 29)[q] - u1 * u3;
+        R L3 = scr<R>(p, 30)[q] - u2 * u2, L4 = scr<R>(p, 31)[q] - u2 * u3, L5 = scr<R>(p, 32)[q] - u3 * u3;
+        R M0 = scr<R>(p, 18)[q], M1 = scr<R>(p, 19)[q], M2 = scr<R>(p, 20)[q];
+        R M3 = scr<R>(p, 21)[q], M4 = scr<R>(p, 22)[q], M5 = scr<R>(p, 23)[q];
+        R nw = R(p.f.nwall[q]);
+        w[0] = (R(2.0) * L1 * M1 + L0 * M0 + R(2.0) * L2 * M2 + L3 * M3 + R(2.0) * L4 * M4 + L5 * M5) * nw * vol;
+        w[1] = (R(2.0) * M1 * M1 + M0 * M0 + R(2.0) * M2 * M2 + M3 * M3 + R(2.0) * M4 * M4 + M5 * M5) * nw * vol;
     }
 };
 struct CsgstsFinal {
@@ -438,21 +456,25 @@ void launch_sgs(lesgpu_case *c) {
     DFields &f = c->kp.f;
     Box b{1, 1, 1, g.n1m, g.n2m, g.n3m};
     if (c->kp.c.idvmon == 1) {
-        k_vreman1<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, 1);
+        if (mixed(c)) k_vreman1<float><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, 1);
+        else k_vreman1<double><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, 1);
         FiltBatch F{};
         F.na = 15;
         for (int m = 0; m < 6; m++) { F.src[m] = f.scr[3 + m]; F.dst[m] = f.scr[18 + m]; }
         for (int m = 0; m < 9; m++) { F.src[6 + m] = f.scr[9 + m]; F.dst[6 + m] = f.scr[24 + m]; }
         filter_batch(c, F);
-        k_vreman2<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b);
+        if (mixed(c)) k_vreman2<float><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b);
+        else k_vreman2<double><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b);
         FiltBatch G{};
         G.na = 9;
         for (int m = 0; m < 9; m++) { G.src[m] = f.scr[3 + m]; G.dst[m] = f.scr[24 + m]; }
         filter_batch(c, G);
-        reduce<2, false>(c, b, LmMmTerm{}, CsgstsFinal{});
+        if (mixed(c)) reduce<2, false>(c, b, LmMmTerm<float>{}, CsgstsFinal{});
+        else reduce<2, false>(c, b, LmMmTerm<double>{}, CsgstsFinal{});
         k_scale<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, f.nusgs, 0);
     } else {
-        k_vreman1<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, 0);
+        if (mixed(c)) k_vreman1<float><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, 0);
+        else k_vreman1<double><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, 0);
     }
 }
 
@@ -462,75 +484,81 @@ void launch_sgs_post(lesgpu_case *c) {
 }
 
 // ------------------------------------------------------------ thermal EDM
+// pass 1 of sgs_edm: mm[0..2] scr[3..5]; s[0..5] scr[6..11]; tgrad[0..2] scr[12..14]
+template <class R>
 __global__ void __launch_bounds__(kThreads) k_edm1(KP p, Box b, int dynamic) {
     const DGrid &g = p.g;
-    double **A = p.f.scr + 3;   // mm[0..2] scr[3..5]; s[0..5] scr[6..11]; tgrad[0..2] scr[12..14]
     GRID_LOOP(b) {
         int i, j, k;
         b.at(tt, i, j, k);
-        double d[9], s[6], alp[3];
-        velgrad(p, i, j, k, d, s);
-        double del = pow(g.f2fx[i] * g.f2fy[j] * g.f2fz[k], 1.0 / 3.0);
-        double sss = s[0] * s[0] + 2.0 * s[1] * s[1] + 2.0 * s[2] * s[2] + s[3] * s[3] + 2.0 * s[4] * s[4] + s[5] * s[5];
-        if (sss < 1.0e-16) sss = 1.0e-16;
+        R d[9], s[6], alp[3];
+        velgrad<R>(p, i, j, k, d, s);
+        R del = pow(R(g.f2fx[i]) * R(g.f2fy[j]) * R(g.f2fz[k]), R(1.0) / R(3.0));
+        R sss = s[0] * s[0] + R(2.0) * s[1] * s[1] + R(2.0) * s[2] * s[2] + s[3] * s[3] + R(2.0) * s[4] * s[4] + s[5] * s[5];
+        if (sss < R(1.0e-16)) sss = R(1.0e-16);
         long long q = g.ix(i, j, k);
         if (!dynamic) {
-            p.f.alsgs[q] = p.c.csgshf * (del * del) * sqrt(2.0 * sss);
+            p.f.alsgs[q] = R(p.c.csgshf) * (del * del) * sqrt(R(2.0) * sss);
             continue;
         }
-        temgrad(p, i, j, k, alp);
-        double al = (del * del) * sqrt(2.0 * sss);
+        temgrad<R>(p, i, j, k, alp);
+        R al = (del * del) * sqrt(R(2.0) * sss);
         p.f.alsgs[q] = al;
 #pragma unroll
-        for (int m = 0; m < 3; m++) A[m][q] = al * alp[m];
+        for (int m = 0; m < 3; m++) scr<R>(p, 3 + m)[q] = al * alp[m];
 #pragma unroll
-        for (int m = 0; m < 6; m++) A[3 + m][q] = s[m];
+        for (int m = 0; m < 6; m++) scr<R>(p, 6 + m)[q] = s[m];
 #pragma unroll
-        for (int m = 0; m < 3; m++) A[9 + m][q] = alp[m];
+        for (int m = 0; m < 3; m++) scr<R>(p, 12 + m)[q] = alp[m];
     }
 }
 
+// pass 2: filtered mm[0..2] scr[18..20] (updated in place), filtered s[0..5]
+// scr[21..26] and tgrad[0..2] scr[27..29]; out uui[0..2] scr[3..5], t scr[6],
+// llij[0..2] scr[7..9]
+template <class R>
 __global__ void __launch_bounds__(kThreads) k_edm2(KP p, Box b) {
     const DGrid &g = p.g;
-    double **FM = p.f.scr + 18;   // filtered mm[0..2] (updated in place)
-    double **FS = p.f.scr + 21;   // filtered s[0..5] scr[21..26], tgrad[0..2] scr[27..29]
-    double **OUT = p.f.scr + 3;   // uui[0..2] scr[3..5], t scr[6], llij[0..2] scr[7..9]
     GRID_LOOP(b) {
         int i, j, k;
         b.at(tt, i, j, k);
         long long q = g.ix(i, j, k);
-        double d1 = tf_width(g.f2fx, g.fixil, g.fixiu, i);
-        double d2 = tf_width(g.f2fy, g.fixjl, g.fixju, j);
-        double d3 = tf_width(g.f2fz, g.fixkl, g.fixku, k);
-        double del = pow(d1 * d2 * d3, 1.0 / 3.0);
-        double s0 = FS[0][q], s1 = FS[1][q], s2 = FS[2][q], s3 = FS[3][q], s4 = FS[4][q], s5 = FS[5][q];
-        double sss = s0 * s0 + 2.0 * s1 * s1 + 2.0 * s2 * s2 + s3 * s3 + 2.0 * s4 * s4 + s5 * s5;
-        if (sss < 1.0e-16) sss = 1.0e-16;
-        double ami = (del * del) * sqrt(2.0 * sss);
+        R d1 = tf_width<R>(g.f2fx, g.fixil, g.fixiu, i);
+        R d2 = tf_width<R>(g.f2fy, g.fixjl, g.fixju, j);
+        R d3 = tf_width<R>(g.f2fz, g.fixkl, g.fixku, k);
+        R del = pow(d1 * d2 * d3, R(1.0) / R(3.0));
+        R s0 = scr<R>(p, 21)[q], s1 = scr<R>(p, 22)[q], s2 = scr<R>(p, 23)[q];
+        R s3 = scr<R>(p, 24)[q], s4 = scr<R>(p, 25)[q], s5 = scr<R>(p, 26)[q];
+        R sss = s0 * s0 + R(2.0) * s1 * s1 + R(2.0) * s2 * s2 + s3 * s3 + R(2.0) * s4 * s4 + s5 * s5;
+        if (sss < R(1.0e-16)) sss = R(1.0e-16);
+        R ami = (del * del) * sqrt(R(2.0) * sss);
 #pragma unroll
-        for (int m = 0; m < 3; m++) FM[m][q] = ami * FS[6 + m][q] - FM[m][q];
-        double u1 = 0.5 * (p.f.u[q] + p.f.u[q + 1]);
-        double u2 = 0.5 * (p.f.v[q] + p.f.v[q + g.sx]);
-        double u3 = 0.5 * (p.f.w[q] + p.f.w[q + g.sxy]);
-        double tq = p.f.t[q];
-        OUT[0][q] = u1; OUT[1][q] = u2; OUT[2][q] = u3;
-        OUT[3][q] = tq;
-        OUT[4][q] = u1 * tq; OUT[5][q] = u2 * tq; OUT[6][q] = u3 * tq;
+        for (int m = 0; m < 3; m++) scr<R>(p, 18 + m)[q] = ami * scr<R>(p, 27 + m)[q] - scr<R>(p, 18 + m)[q];
+        R u1 = R(0.5) * (R(p.f.u[q]) + R(p.f.u[q + 1]));
+        R u2 = R(0.5) * (R(p.f.v[q]) + R(p.f.v[q + g.sx]));
+        R u3 = R(0.5) * (R(p.f.w[q]) + R(p.f.w[q + g.sxy]));
+        R tq = R(p.f.t[q]);
+        scr<R>(p, 3)[q] = u1; scr<R>(p, 4)[q] = u2; scr<R>(p, 5)[q] = u3;
+        scr<R>(p, 6)[q] = tq;
+        scr<R>(p, 7)[q] = u1 * tq; scr<R>(p, 8)[q] = u2 * tq; scr<R>(p, 9)[q] = u3 * tq;
     }
 }
 
+// M_j in scr[18..20]; filtered uui [24..26], t [27], llij [28..30]
+template <class R>
 struct LmMmTTerm {
     __device__ void operator()(const KP &p, int i, int j, int k, double *w) const {
         const DGrid &g = p.g;
         long long q = g.ix(i, j, k);
-        double *const *FM = p.f.scr + 18;   // M_j
-        double *const *FU = p.f.scr + 24;   // filtered uui [24..26], t [27], llij [28..30]
-        double vol = g.f2fx[i] * g.f2fy[j] * g.f2fz[k];
-        double tf = FU[3][q];
-        double L0 = FU[4][q] - FU[0][q] * tf, L1 = FU[5][q] - FU[1][q] * tf, L2 = FU[6][q] - FU[2][q] * tf;
-        double nw = (double)p.f.nwall[q];
-        w[0] = (L0 * FM[0][q] + L1 * FM[1][q] + L2 * FM[2][q]) * nw * vol;
-        w[1] = (FM[0][q] * FM[0][q] + FM[1][q] * FM[1][q] + FM[2][q] * FM[2][q]) * nw * vol;
+        R vol = R(g.f2fx[i]) * R(g.f2fy[j]) * R(g.f2fz[k]);
+        R tf = scr<R>(p, 27)[q];
+        R L0 = scr<R>(p, 28)[q] - scr<R>(p, 24)[q] * tf;
+        R L1 = scr<R>(p, 29)[q] - scr<R>(p, 25)[q] * tf;
+        R L2 = scr<R>(p, 30)[q] - scr<R>(p, 26)[q] * tf;
+        R M0 = scr<R>(p, 18)[q], M1 = scr<R>(p, 19)[q], M2 = scr<R>(p, 20)[q];
+        R nw = R(p.f.nwall[q]);
+        w[0] = (L0 * M0 + L1 * M1 + L2 * M2) * nw * vol;
+        w[1] = (M0 * M0 + M1 * M1 + M2 * M2) * nw * vol;
     }
 };
 struct CsgshfFinal {
@@ -545,21 +573,25 @@ void launch_sgs_t(lesgpu_case *c) {
     DFields &f = c->kp.f;
     Box b{1, 1, 1, g.n1m, g.n2m, g.n3m};
     if (c->kp.c.idvmon == 1) {
-        k_edm1<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, 1);
+        if (mixed(c)) k_edm1<float><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, 1);
+        else k_edm1<double><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, 1);
         FiltBatch F{};
         F.na = 12;
         for (int m = 0; m < 3; m++) { F.src[m] = f.scr[3 + m]; F.dst[m] = f.scr[18 + m]; }
         for (int m = 0; m < 9; m++) { F.src[3 + m] = f.scr[6 + m]; F.dst[3 + m] = f.scr[21 + m]; }
         filter_batch(c, F);
-        k_edm2<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b);
+        if (mixed(c)) k_edm2<float><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b);
+        else k_edm2<double><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b);
         FiltBatch G{};
         G.na = 7;
         for (int m = 0; m < 7; m++) { G.src[m] = f.scr[3 + m]; G.dst[m] = f.scr[24 + m]; }
         filter_batch(c, G);
-        reduce<2, false>(c, b, LmMmTTerm{}, CsgshfFinal{});
+        if (mixed(c)) reduce<2, false>(c, b, LmMmTTerm<float>{}, CsgshfFinal{});
+        else reduce<2, false>(c, b, LmMmTTerm<double>{}, CsgshfFinal{});
         k_scale<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, f.alsgs, 1);
     } else {
-        k_edm1<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, 0);
+        if (mixed(c)) k_edm1<float><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, 0);
+        else k_edm1<double><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, 0);
     }
 }
 

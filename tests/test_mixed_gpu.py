@@ -1,0 +1,63 @@
+"""The mixed-precision form (FP32 stencils, SGS and x/z ADI sweeps; FP64 y
+sweeps, Poisson, projection, flow-rate and divergence) against the FP64 form
+on the same case.
+
+Stated error bounds (relative L2 of each field against the FP64 form): u, v,
+w, t within 1e-5 after one step and 1e-4 after ten on the channel; the
+pressure, which the projection builds from small differences of the FP32
+right-hand sides, within 1e-3; divergence after projection below 1e-6 (the
+Poisson solve and projection stay FP64).
+"""
+import numpy as np
+import pytest
+
+import leswht_gb300
+from leswht_gb300 import abi, cases
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    den = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (den if den > 0 else 1.0)
+
+
+def pair(builder):
+    f64 = builder(abi.PREC_FP64)
+    mix = builder(abi.PREC_MIXED)
+    return leswht_gb300.gpu_solver(f64), leswht_gb300.gpu_solver(mix)
+
+
+@pytest.mark.parametrize("nsteps,tol", [(1, 1e-5), (10, 1e-4)])
+def test_channel_mixed_close_to_fp64(nsteps, tol):
+    a, b = pair(lambda prec: cases.channel(32, 32, 16, precision=prec))
+    for _ in range(nsteps):
+        ra, rb = a.step(), b.step()
+    fa, fb = a.fields(), b.fields()
+    for k in ("u", "v", "w", "p", "t"):
+        e = rel(fb[k], fa[k])
+        assert e <= (1e-3 if k == "p" else tol), (k, e)
+        assert e > 0.0 or k == "p", k            # the mixed path really differs
+    assert rb["dvmax"] < 1e-6
+    assert rb["csgsts"] == pytest.approx(ra["csgsts"], rel=1e-3)
+
+
+def test_cylinder_mixed_close_to_fp64():
+    a, b = pair(lambda prec: cases.cylinder(64, 48, 8, precision=prec))
+    for _ in range(3):
+        ra, rb = a.step(), b.step()
+    fa, fb = a.fields(), b.fields()
+    for k in ("u", "v", "w", "t"):
+        assert rel(fb[k], fa[k]) <= 1e-4, k
+    assert rb["dvmax"] < 1e-5
+    assert rb["cd"][0] == pytest.approx(ra["cd"][0], rel=1e-3, abs=1e-6)
+
+
+def test_mixed_is_deterministic():
+    x = leswht_gb300.gpu_solver(cases.channel(32, 32, 16, precision=abi.PREC_MIXED))
+    y = leswht_gb300.gpu_solver(cases.channel(32, 32, 16, precision=abi.PREC_MIXED))
+    for _ in range(3):
+        x.step(); y.step()
+    fx, fy = x.fields(), y.fields()
+    for k in ("u", "v", "w", "p", "t"):
+        assert np.array_equal(fx[k], fy[k]), k
