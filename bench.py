@@ -10,9 +10,17 @@ synthetic initial field (laminar profile + 10% uniform perturbation).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Our arm (one JSON line on rank 0):
-  value    : device-resident throughput; every step is bracketed by CUDA
-             events on the case's own stream and L2 is flushed (256 MiB
-             write) between timed steps, outside the timed region.
+  value    : device-resident throughput of the mixed-precision form (FP32
+             stencils, SGS and x/z ADI sweeps; FP64 wall-normal sweeps,
+             Poisson, projection, flow-rate and divergence); every step is
+             bracketed by CUDA events on the case's own stream and L2 is
+             flushed (256 MiB write) between timed steps, outside the timed
+             region.  `--form fp64` times the plain FP64 form instead.
+  fp64, mixed_vs_fp64, error : with the default form, the FP64 form is timed
+             the same way on the same config, and `error` states the mixed
+             form's deviation from it after `steps` steps from the same
+             initial field (relative L2 of u, v, w, p, t; divergence; bulk
+             velocity; drag and heat flux).
   e2e      : the same metric through the C ABI with host buffers: each step
              uploads u,v,w,p,t from pinned host memory (lesgpu_set_fields),
              steps (lesgpu_step, which reads the step report back) and
@@ -184,7 +192,7 @@ def run_reference(args):
         return 0
     import oracle
     from leswht_gb300 import solver
-    case = make_case(args.config, args.form)
+    case = make_case(args.config, "fp64")
     lib = oracle.load()
     s = solver.Solver(lib, "ref_", case)
     for _ in range(args.warmup):
@@ -209,39 +217,27 @@ def run_reference(args):
     return 0
 
 
-def run_ours(args):
+def time_form(args, form, lib, dev, world, rank, flush, full):
+    """Time one arithmetic form of the step on this GPU.  Returns the
+    device-resident figures and, when `full`, the live per-kernel-class
+    timings, the roofline of the dominant class and the end-to-end figure."""
     import numpy as np
     import torch
     import leswht_gb300
     from leswht_gb300 import abi
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world != args.gpus and world > 1:
-        print(f"warning: WORLD_SIZE={world} but --gpus {args.gpus}", file=sys.stderr)
-    dev = local if torch.cuda.device_count() > local else 0
-    torch.cuda.set_device(dev)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
-    lib = leswht_gb300.load_library()
-    if lib.lesgpu_set_device(dev) != 0:
-        raise RuntimeError("lesgpu_set_device failed")
-    case = make_case(args.config, args.form)
+    case = make_case(args.config, form)
     s = leswht_gb300.gpu_solver(case)
     h = s.h
     stream_ptr = C.c_void_p()
     lib.lesgpu_stream(h, C.byref(stream_ptr))
     stream = torch.cuda.ExternalStream(stream_ptr.value, device=torch.device("cuda", dev))
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
 
     def check(rc, what):
         if rc != 0:
             raise RuntimeError(f"{what}: {lib.lesgpu_strerror(rc).decode()}")
 
-    # warm-up (captures the step graph)
-    for _ in range(args.warmup):
+    for _ in range(args.warmup):                     # warm-up (captures the step graph)
         check(lib.lesgpu_step_async(h, 1), "step")
     torch.cuda.synchronize()
     kps = C.c_int64()
@@ -261,7 +257,7 @@ def run_ours(args):
                 check(lib.lesgpu_step_async(h, 1), "step")
                 ev[q][1].record(stream)
         torch.cuda.synchronize()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
+    step_ms = [x.elapsed_time(y) for x, y in ev]
     tot_s = sum(step_ms) / 1e3
     if world > 1:
         import torch.distributed as dist
@@ -269,90 +265,150 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         tot_s = float(t.item())
     rep = s.report()
-    value = world * case.cells * args.steps / tot_s / 1e6
+    out = {"case": case, "value": world * case.cells * args.steps / tot_s / 1e6,
+           "ms_per_step": tot_s / args.steps * 1e3, "kernels_per_step": int(kps.value),
+           "clocks": clk.summary(), "report": rep,
+           "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)}}
+    if not full or rank != 0:
+        s.close()
+        return out
 
     # ---- live per-kernel-class timing (instrumented eager steps)
     kstats = {}
-    if rank == 0:
-        for cls in (1, 2, 4, 5):
-            check(lib.lesgpu_instrument(h, cls), "instrument")
-            with torch.cuda.stream(stream):
-                for q in range(max(2, min(args.steps, 5))):
-                    flush.zero_()
-                    check(lib.lesgpu_step_async(h, 1), "step")
-            ms, n = C.c_double(), C.c_int64()
-            check(lib.lesgpu_instrument_read(h, C.byref(ms), C.byref(n)), "instrument_read")
-            kstats[KCLASS[cls]] = {"ms_total": ms.value, "launches": n.value,
-                                   "avg_us": ms.value / max(n.value, 1) * 1e3, "cls": cls}
-        check(lib.lesgpu_instrument(h, 0), "instrument")
-    roofline = None
+    for cls in (1, 2, 4, 5):
+        check(lib.lesgpu_instrument(h, cls), "instrument")
+        with torch.cuda.stream(stream):
+            for q in range(max(2, min(args.steps, 5))):
+                flush.zero_()
+                check(lib.lesgpu_step_async(h, 1), "step")
+        ms, n = C.c_double(), C.c_int64()
+        check(lib.lesgpu_instrument_read(h, C.byref(ms), C.byref(n)), "instrument_read")
+        kstats[KCLASS[cls]] = {"ms_total": ms.value, "launches": n.value,
+                               "avg_us": ms.value / max(n.value, 1) * 1e3, "cls": cls}
+    check(lib.lesgpu_instrument(h, 0), "instrument")
     kwords = dict(KWORDS)
     if case.settings.get("poisson") == abi.POISSON_Z_FT:
         # z FFT in/out 4 w + 14 w per multigrid V-cycle (mean over the substeps)
         its = [x for x in rep["poisson_iters"] if x > 0] or [0]
         kwords[4] = 4.0 + 14.0 * sum(its) / len(its)
-    if kstats:
-        peak, src = peaks()
-        dom = max(kstats.values(), key=lambda d: d["ms_total"])
-        words = kwords[dom["cls"]]
-        bytes_per_launch = words * 8.0 * case.cells
-        achieved = bytes_per_launch / (dom["avg_us"] * 1e-6) / 1e9
-        for k, d in kstats.items():
-            w = kwords.get(d["cls"])
-            if w:
-                d["achieved_gbs"] = w * 8.0 * case.cells / (d["avg_us"] * 1e-6) / 1e9
-        name = [k for k, d in kstats.items() if d is dom][0]
-        roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                    "frac": achieved / peak, "traffic": None, "kernel": name, "peak_source": src,
-                    "algorithmic_bytes_per_launch": bytes_per_launch,
-                    "avg_launch_us": dom["avg_us"], "kernels": kstats}
+    peak, src = peaks()
+    dom = max(kstats.values(), key=lambda d: d["ms_total"])
+    bytes_per_launch = kwords[dom["cls"]] * 8.0 * case.cells
+    achieved = bytes_per_launch / (dom["avg_us"] * 1e-6) / 1e9
+    for k, d in kstats.items():
+        w = kwords.get(d["cls"])
+        if w:
+            d["achieved_gbs"] = w * 8.0 * case.cells / (d["avg_us"] * 1e-6) / 1e9
+    name = [k for k, d in kstats.items() if d is dom][0]
+    out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                       "frac": achieved / peak, "traffic": None, "kernel": name, "peak_source": src,
+                       "algorithmic_bytes_per_launch": bytes_per_launch,
+                       "avg_launch_us": dom["avg_us"], "kernels": kstats}
 
     # ---- end to end through the C ABI with host buffers
-    e2e = None
-    if rank == 0:
-        shape = case.grid.shape
-        host = {k: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy() for k in ("u", "v", "w", "p", "t")}
-        f0 = s.fields()
-        for k in host:
-            host[k][...] = f0[k]
-        r0 = s.report()
-        tm, dt, ih, m = r0["time"], r0["dt"], r0["ihist"], r0["m"]
-        ptr = lambda a: a.ctypes.data_as(abi.PD)
-        rep_s = abi.StepReport()
-        n_e2e = max(3, min(args.steps, 20))
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(n_e2e):
-            check(lib.lesgpu_set_fields(h, *(ptr(host[k]) for k in ("u", "v", "w", "p", "t")), tm, dt, ih, m), "set_fields")
-            check(lib.lesgpu_step(h, C.byref(rep_s)), "step")
-            check(lib.lesgpu_get_fields(h, *(ptr(host[k]) for k in ("u", "v", "w", "p", "t"))), "get_fields")
-            tm, dt, ih, m = rep_s.time, rep_s.dt, rep_s.ihist, rep_s.m
-        el = time.perf_counter() - t0
-        nbytes = 5 * int(np.prod(shape)) * 8
-        e2e = {"value": case.cells * n_e2e / el / 1e6, "unit": UNIT, "h2d_bytes_per_step": nbytes,
-               "d2h_bytes_per_step": nbytes + C.sizeof(abi.StepReport), "steps": n_e2e,
-               "path": "lesgpu_set_fields + lesgpu_step + lesgpu_get_fields, pinned host buffers"}
+    shape = case.grid.shape
+    host = {k: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy() for k in ("u", "v", "w", "p", "t")}
+    f0 = s.fields()
+    for k in host:
+        host[k][...] = f0[k]
+    r0 = s.report()
+    tm, dt, ih, m = r0["time"], r0["dt"], r0["ihist"], r0["m"]
+    ptr = lambda a: a.ctypes.data_as(abi.PD)
+    rep_s = abi.StepReport()
+    n_e2e = max(3, min(args.steps, 20))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        check(lib.lesgpu_set_fields(h, *(ptr(host[k]) for k in ("u", "v", "w", "p", "t")), tm, dt, ih, m), "set_fields")
+        check(lib.lesgpu_step(h, C.byref(rep_s)), "step")
+        check(lib.lesgpu_get_fields(h, *(ptr(host[k]) for k in ("u", "v", "w", "p", "t"))), "get_fields")
+        tm, dt, ih, m = rep_s.time, rep_s.dt, rep_s.ihist, rep_s.m
+    el = time.perf_counter() - t0
+    nbytes = 5 * int(np.prod(shape)) * 8
+    out["e2e"] = {"value": case.cells * n_e2e / el / 1e6, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+                  "d2h_bytes_per_step": nbytes + C.sizeof(abi.StepReport), "steps": n_e2e,
+                  "path": "lesgpu_set_fields + lesgpu_step + lesgpu_get_fields, pinned host buffers"}
+    s.close()
+    return out
+
+
+def form_error(args, nsteps):
+    """The mixed form's error against the FP64 form: both run `nsteps` steps
+    from the same initial field; relative L2 of each field, the divergence
+    after the last projection, and the drag / heat-flux / bulk diagnostics."""
+    import numpy as np
+    import leswht_gb300
+    a = leswht_gb300.gpu_solver(make_case(args.config, "fp64"))
+    b = leswht_gb300.gpu_solver(make_case(args.config, "mixed"))
+    for _ in range(nsteps):
+        ra, rb = a.step(), b.step()
+    fa, fb = a.fields(), b.fields()
+
+    def rel(x, y):
+        d = float(np.linalg.norm(y))
+        return float(np.linalg.norm(x - y)) / (d if d > 0 else 1.0)
+
+    def reldiff(x, y):
+        return abs(x - y) / max(abs(y), 1e-300)
+
+    err = {"steps": nsteps, "rel_l2": {k: rel(fb[k], fa[k]) for k in ("u", "v", "w", "p", "t")},
+           "max_div_mixed": rb["dvmax"], "max_div_fp64": ra["dvmax"],
+           "ubulk_rel": reldiff(rb["ubulk"], ra["ubulk"])}
+    if make_case(args.config, "fp64").settings.get("ibmon", 0) == 1:
+        err["drag_rel"] = reldiff(rb["cd"][0], ra["cd"][0])
+    err["heat_flux_x_abs"] = abs(rb["heat_flux"][0] - ra["heat_flux"][0])
+    a.close(); b.close()
+    return err
+
+
+def run_ours(args):
+    import torch
+    import leswht_gb300
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world != args.gpus and world > 1:
+        print(f"warning: WORLD_SIZE={world} but --gpus {args.gpus}", file=sys.stderr)
+    dev = local if torch.cuda.device_count() > local else 0
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+    lib = leswht_gb300.load_library()
+    if lib.lesgpu_set_device(dev) != 0:
+        raise RuntimeError("lesgpu_set_device failed")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+
+    main = time_form(args, args.form, lib, dev, world, rank, flush, full=True)
+    other_form = "fp64" if args.form == "mixed" else None
+    other = time_form(args, other_form, lib, dev, world, rank, flush, full=False) if other_form else None
 
     if rank == 0:
+        case, rep = main["case"], main["report"]
         cpu = None
         if world == 1 and not args.no_cpu:
-            cpu = cpu_baseline(args.config, args.form, seconds=args.cpu_seconds)
-        clocks = clk.summary()
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": tot_s / args.steps * 1e3, "higher_is_better": True,
+            cpu = cpu_baseline(args.config, "fp64", seconds=args.cpu_seconds)
+        line = {"metric": METRIC, "value": main["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": main["ms_per_step"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.form == "fp64" else "f32/f64",
                 "data": "synthetic (seeded PCG64 perturbation of the laminar profile)",
                 "config": {"workload": WORKLOAD[args.config], "cells": case.cells, "form": args.form,
                            "l2": "flushed between timed steps (256 MiB write, outside the timed region)",
                            "parallelism": "replicas" if world > 1 else "single GPU"},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "gpu_launches": int(kps.value) * args.steps, "kernels_per_step": int(kps.value),
-                "clocks": clocks,
+                "roofline": main.get("roofline"), "cpu_baseline": cpu, "e2e": main.get("e2e"),
+                "gpu_launches": main["kernels_per_step"] * args.steps, "kernels_per_step": main["kernels_per_step"],
+                "clocks": main["clocks"],
                 "check": {"dvmax": rep["dvmax"], "ubulk": rep["ubulk"], "csgsts": rep["csgsts"],
                           "time": rep["time"], "dt": rep["dt"]},
-                "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)}}
+                "step_ms": main["step_ms"]}
+        if other is not None:
+            line["fp64"] = {"value": other["value"], "ms_per_step": other["ms_per_step"],
+                            "kernels_per_step": other["kernels_per_step"], "clocks": other["clocks"]}
+            line["mixed_vs_fp64"] = main["value"] / other["value"]
+            line["gpu_launches"] += other["kernels_per_step"] * args.steps
+            line["error"] = form_error(args, args.steps)
         print(json.dumps(line))
-    s.close()
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
@@ -367,7 +423,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="channel64", choices=sorted(WORKLOAD))
-    ap.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--form", default="mixed", choices=["fp64", "mixed"],
+                    help="mixed (default): the mixed form is timed, then the FP64 form on the same "
+                         "config, and the mixed form's error against FP64 is stated")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     args = ap.parse_args()
