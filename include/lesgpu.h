@@ -240,6 +240,32 @@ int lesgpu_get_fields(lesgpu_case *c, double *u, double *v, double *w,
 #define LESGPU_NAVG 23
 int lesgpu_get_averages(lesgpu_case *c, double *out, int64_t *nsamples, int reset);
 
+/* Serving loop (no reference counterpart; the reference runs one case per
+ * process).  A server owns one worker thread on `device`.  Cases submitted at
+ * any time wait until their device footprint fits `hbm_budget_bytes` and fewer
+ * than `max_active` cases are resident; an admitted case keeps its fields on
+ * the device for its whole run and advances `steps_in_flight` steps at a time
+ * on its own stream and captured step graph, so the work of all resident
+ * cases overlaps on the GPU.  A finished case is copied back and freed at
+ * once, which admits the next waiting case.  Submission copies every input;
+ * results (the five fields, the last step report and the seconds from
+ * submission to completion) are copied out by lesgpu_server_result.
+ * Request states: 0 waiting, 1 running, 2 done, 3 failed, 4 cancelled. */
+typedef struct lesgpu_server lesgpu_server;
+int lesgpu_server_create(int64_t device, int64_t hbm_budget_bytes, int64_t max_active,
+                         int64_t steps_in_flight, lesgpu_server **out);
+int lesgpu_server_submit(lesgpu_server *s, const lesgpu_config *cfg, const lesgpu_grid *grid,
+                         const lesgpu_ibm *ibm, const double *u, const double *v, const double *w,
+                         const double *p, const double *t, double time, double dt, int64_t ihist,
+                         int64_t m, int64_t nsteps, int64_t *ticket);
+int lesgpu_server_poll(lesgpu_server *s, int64_t ticket, int64_t *state, int64_t *steps_done);
+int lesgpu_server_result(lesgpu_server *s, int64_t ticket, double *u, double *v, double *w,
+                         double *p, double *t, lesgpu_step_report *rep, double *seconds_to_solution);
+int lesgpu_server_release(lesgpu_server *s, int64_t ticket);
+int lesgpu_server_stats(lesgpu_server *s, int64_t *pending, int64_t *active, int64_t *bytes_used,
+                        double *cell_steps);
+int lesgpu_server_destroy(lesgpu_server *s);
+
 /* Phase-level access for parity tests (not needed by a driver). */
 int lesgpu_get_array(lesgpu_case *c, int64_t field, double *out);
 int lesgpu_set_array(lesgpu_case *c, int64_t field, const double *in);
