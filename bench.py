@@ -29,6 +29,10 @@ Our arm (one JSON line on rank 0):
              instrumented steps), its algorithmic bytes per launch divided by
              its average launch time (events on the launching stream), against
              the measured HBM copy bandwidth.
+  serving  : a bounded sample of the serving stream through lesgpu_server
+             (mixed form, cases admitted and advanced concurrently): p50/p99
+             time-to-solution and aggregate Mcell-steps/s, beside the same
+             cases run one at a time in the FP64 form.
   cpu_baseline : the CPU oracle (C/OpenMP restatement of the solver, the
              reference's Fortran cannot be built on this host) on a bounded
              sample of the same workload, all host threads.
@@ -361,6 +365,25 @@ def form_error(args, nsteps):
     return err
 
 
+def serving_sample(args, lib):
+    """A bounded sample of the serving stream (seeded Poisson arrivals at
+    2 cases/s; grid, body, Re and Pr drawn as in the benchmark stream), run
+    through the server in the mixed form, then the same cases one at a time
+    in the FP64 form.  p50/p99 are times from arrival to completion."""
+    from leswht_gb300 import abi, serving
+    stream = serving.c4_stream(n_cases=args.serving_cases, rate=2.0, nsteps=args.serving_steps)
+    srv = serving.Server(lib, hbm_budget_bytes=64 << 30, max_active=32, steps_in_flight=4)
+    mixed = serving.serve(srv, stream, precision=abi.PREC_MIXED)
+    srv.close()
+    seq = serving.one_at_a_time(lib, stream, precision=abi.PREC_FP64)
+    return {"sample": f"{args.serving_cases} cases x {args.serving_steps} steps of the seeded serving stream "
+                      "(Poisson arrivals 2/s; grids 64x48x8 .. 256x192x32; circle/square/sphere; Re 40-1000; "
+                      "Pr 0.71/7); the benchmark stream has 256 cases x 500 steps",
+            "served_mixed": {k: mixed[k] for k in ("p50_s", "p99_s", "mcell_steps_per_s", "elapsed_s", "completed")},
+            "one_at_a_time_fp64": {k: seq[k] for k in ("p50_s", "p99_s", "mcell_steps_per_s", "elapsed_s")},
+            "throughput_ratio": mixed["mcell_steps_per_s"] / seq["mcell_steps_per_s"]}
+
+
 def run_ours(args):
     import torch
     import leswht_gb300
@@ -402,6 +425,8 @@ def run_ours(args):
                 "check": {"dvmax": rep["dvmax"], "ubulk": rep["ubulk"], "csgsts": rep["csgsts"],
                           "time": rep["time"], "dt": rep["dt"]},
                 "step_ms": main["step_ms"]}
+        if args.serving_cases > 0 and world == 1:
+            line["serving"] = serving_sample(args, lib)
         if other is not None:
             line["fp64"] = {"value": other["value"], "ms_per_step": other["ms_per_step"],
                             "kernels_per_step": other["kernels_per_step"], "clocks": other["clocks"]}
@@ -427,6 +452,9 @@ def main():
                     help="mixed (default): the mixed form is timed, then the FP64 form on the same "
                          "config, and the mixed form's error against FP64 is stated")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serving-cases", type=int, default=16,
+                    help="cases in the serving sample (0: skip it)")
+    ap.add_argument("--serving-steps", type=int, default=40)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -131,8 +131,10 @@ typedef struct lesgpu_grid {
  * intpindx[l] : nintp[l]*3 int64, row n = direction offsets (-1/0/+1)
  * geomfac[l]  : nintp[l]*27 double, row n = geomfac(n,l,i,j,k) at
  *               i*9 + j*3 + k for i,j,k in 0..2 (the file's record order)
- * nzero, inz/jnz/knz : zero-eddy-viscosity list, indices as the solver uses
- *               them (1-based after reading the 0-based file, sgs.f90:893)
+ * nzero, inz/jnz/knz : zero-eddy-viscosity list exactly as ibmpre_nutzero.bin
+ *               holds it; the solver uses the values as Fortran (1-based)
+ *               indices (sgs.f90:893) although the pre-processor writes
+ *               0-based ones, and so does this library
  * nwall_dvm   : (1:n1m,1:n2m,1:n3m) int64 mask, i fastest, or NULL (= 1)
  * cstar       : (1:n1m,1:n2m,1:n3m) double or NULL (= 1)
  * kstar       : (1:n1m,1:n2m,1:n3m,6) double or NULL (= 1)
@@ -169,6 +171,7 @@ typedef struct lesgpu_step_report {
     double tbulk_fluid, tbulk_solid;
     int64_t poisson_iters[3];   /* iterations of each substep's Poisson solve */
     double phase_ms[4];     /* SGS, RHS+LHS, Poisson, whole step (device ms)  */
+    double qflux;           /* flow rate qvol_u / xl (writehistory)           */
 } lesgpu_step_report;
 
 /* Fields of lesgpu_get_array / lesgpu_set_array (phase-level parity tests). */

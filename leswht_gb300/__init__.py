@@ -13,7 +13,7 @@ import ctypes as C
 from pathlib import Path
 
 from . import abi
-from .build import SO, build
+from .build import EXEC, SO, build
 
 _LIB = None
 
@@ -47,6 +47,14 @@ def load_library(rebuild: bool = False) -> C.CDLL:
     lib.lesgpu_set_device.restype = C.c_int
     _LIB = lib
     return lib
+
+
+def exec_path(rebuild: bool = False) -> Path:
+    """The compiled case driver (lesgpu_exec), built with the library."""
+    build(force=rebuild)
+    if not EXEC.exists():
+        raise RuntimeError(f"lesgpu_exec missing at {EXEC}")
+    return EXEC
 
 
 def gpu_solver(case, **kw):

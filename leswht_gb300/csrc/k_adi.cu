@@ -628,15 +628,23 @@ static void adi_launch(lesgpu_case *c, const AdiBatch &B, int ncomp) {
     // the scan form costs ~2.5x the FP64 operations of the serial recurrence and
     // a GB300 SM retires few FP64 FMAs per clock.  Longer lines (more than 12
     // rows per lane) keep one thread per line.
-    bool done;
+    bool done = false;
     if (f32) {
         done = adis_launch<float, 32>(c, B, ncomp, mx, nmax);
     } else {
-        // about 8 rows per lane: 8 lanes for 64-row lines, 16 up to 128, 32 above
-        const int w = nmax <= 64 ? 8 : nmax <= 128 ? 16 : 32;
-        done = w == 8 ? adis_launch<double, 8>(c, B, ncomp, mx, nmax)
-             : w == 16 ? adis_launch<double, 16>(c, B, ncomp, mx, nmax)
-                       : adis_launch<double, 32>(c, B, ncomp, mx, nmax);
+        // lanes per line so that the launch holds ~64k threads: the scan form
+        // pays only while one thread per line leaves the GPU latency bound
+        long long lines = 0;
+        for (int q = 0; q < ncomp; q++)
+            lines += (long long)(B.a[q].a1 - B.a[q].a0 + 1) * (B.a[q].b1 - B.a[q].b0 + 1);
+        int w = 1;
+        while (w < 32 && lines * w < 65536) w <<= 1;
+        if (w == 4) w = 8;
+        if (w >= 8) {
+            done = w == 8 ? adis_launch<double, 8>(c, B, ncomp, mx, nmax)
+                 : w == 16 ? adis_launch<double, 16>(c, B, ncomp, mx, nmax)
+                           : adis_launch<double, 32>(c, B, ncomp, mx, nmax);
+        }
     }
     if (!done) {
         if (f32) k_adi<float><<<grid, 32, 0, c->stream>>>(c->kp, B);

@@ -408,6 +408,7 @@ struct BulkFinal {
     __device__ void operator()(const KP &p, const double *o) const {
         DScal *S = p.S;
         S->ubulk = o[1] > 0.0 ? o[0] / o[1] : 0.0;
+        S->qflux = o[0] / p.g.xl;
         S->tbulk_fluid = o[2] > 0.0 ? o[3] / o[2] : 0.0;
         S->tbulk_solid = o[4] > 0.0 ? o[5] / o[4] : 0.0;
     }

@@ -539,7 +539,7 @@ static void fill_report(const lesgpu_case *c, const DScal &s, lesgpu_step_report
     for (int q = 0; q < 3; q++) { r->qvol[q] = s.qvol[q]; r->tvol[q] = s.tvol[q]; r->cd[q] = s.cd[q]; r->heat_flux[q] = s.heat_flux[q]; }
     r->csgsts = s.csgsts; r->csgshf = s.csgshf;
     r->nutavg = s.nutavg; r->nutmax = s.nutmax; r->alpavg = s.alpavg; r->alpmax = s.alpmax;
-    r->ubulk = s.ubulk; r->tbulk_fluid = s.tbulk_fluid; r->tbulk_solid = s.tbulk_solid;
+    r->ubulk = s.ubulk; r->qflux = s.qflux; r->tbulk_fluid = s.tbulk_fluid; r->tbulk_solid = s.tbulk_solid;
     for (int q = 0; q < 3; q++) r->poisson_iters[q] = s.poisson_iters[q];
 }
 

@@ -60,7 +60,7 @@ struct DScal {
     double err_integral;
     double dudta, dvdta, dwdta;
     double cd[3], heat_flux[3];
-    double ubulk, tbulk_fluid, tbulk_solid;
+    double ubulk, qflux, tbulk_fluid, tbulk_solid;
     double u_bulk_t;          // rhs_t's bulk velocity of the current substep
     double phiref;            // pcalc's outlet-plane mean of phi
     double cvol;              // tvolcorr's volume integral of 1/c*

@@ -252,7 +252,7 @@ int ref_get_report(ref_case *c, lesgpu_step_report *r)
     for (int i = 0; i < 3; i++) { r->qvol[i] = c->qvol[i]; r->tvol[i] = c->tvol[i]; r->cd[i] = c->cd[i]; r->heat_flux[i] = c->heat_flux[i]; }
     r->csgsts = c->csgsts; r->csgshf = c->csgshf;
     r->nutavg = c->nutavg; r->nutmax = c->nutmax; r->alpavg = c->alpavg; r->alpmax = c->alpmax;
-    r->ubulk = c->ubulk; r->tbulk_fluid = c->tbulk_fluid; r->tbulk_solid = c->tbulk_solid;
+    r->ubulk = c->ubulk; r->qflux = c->qflux; r->tbulk_fluid = c->tbulk_fluid; r->tbulk_solid = c->tbulk_solid;
     for (int i = 0; i < 3; i++) r->poisson_iters[i] = c->poisson_iters[i];
     return 0;
 }
@@ -360,6 +360,9 @@ int ref_destroy(ref_case *c)
     free(c->ac); free(c->gam); free(c->bet);
     free(c->aw); free(c->ae); free(c->as); free(c->an); free(c->coi1); free(c->coi2); free(c->cor1); free(c->cor2);
     free(c->ipm); free(c->imm); free(c->ak1); free(c->ak3); free(c->avg);
+    free(c->ab); free(c->af); free(c->fidw); free(c->fkdw); free(c->fiup); free(c->fkup);
+    free(c->ih1); free(c->ih2); free(c->kh1); free(c->kh2); free(c->il1); free(c->il2); free(c->kl1); free(c->kl2);
+    free(c->kpm); free(c->kmm);
     ref_fft_plan_free(&c->fftx); ref_fft_plan_free(&c->fftz);
     free(c);
     return 0;
@@ -706,6 +709,7 @@ void ref_bulk_diag(ref_case *c)
                 }
             }
     c->ubulk = fv > 0 ? qv / fv : 0.0;
+    c->qflux = qv / c->xl;
     c->tbulk_fluid = tfv > 0 ? tfi / tfv : 0.0;
     c->tbulk_solid = tsv > 0 ? tsi / tsv : 0.0;
 }

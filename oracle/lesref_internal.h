@@ -107,7 +107,7 @@ typedef struct ref_case {
     double err_integral;          /* meanpg's SAVEd controller state */
     double dudta, dvdta, dwdta;
     double cd[3], heat_flux[3];
-    double ubulk, tbulk_fluid, tbulk_solid;
+    double ubulk, qflux, tbulk_fluid, tbulk_solid;
     /* field_avg accumulators: LESGPU_NAVG arrays in the full layout, record order of the fav file */
     double *avg;
     ll avg_count;
