@@ -295,6 +295,24 @@ def cylinder(n1m: int = 128, n2m: int = 96, n3m: int = 16, re: float = 100.0, pr
                 ihist=0, m=0, ibm=tables)
 
 
+def with_poisson(case: Case, poisson: int, nlev: Optional[int] = None) -> Case:
+    """The same case solved with another of the reference's Poisson solvers.
+    For poiss_mgrd (x and z coarsened together) the default NLEV is the
+    deepest with n1m and n3m divisible by 2^NLEV and at least two cells per
+    direction on the coarsest level."""
+    s = dict(case.settings)
+    s["poisson"] = int(poisson)
+    if nlev is None and poisson == abi.POISSON_MGRD:
+        g = case.grid
+        nlev = 0
+        while nlev < 5 and all(n % (2 ** (nlev + 1)) == 0 and n // (2 ** (nlev + 1)) >= 2 for n in (g.n1m, g.n3m)):
+            nlev += 1
+    if nlev is not None:
+        s["nlev"] = int(nlev)
+    return Case(case.name + f"_p{poisson}", s, case.grid, case.grid_dat, case.grid_bin, case.fields, time=case.time,
+                dt=case.dt, ihist=case.ihist, m=case.m, ibm=case.ibm)
+
+
 PRESETS = {
     "channel64": lambda **kw: channel(64, 64, 64, **kw),
     "channel590": lambda **kw: channel(384, 256, 384, lx=2 * math.pi, lz=math.pi, re=10950.0, **kw),

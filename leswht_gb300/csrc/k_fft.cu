@@ -288,6 +288,7 @@ int poisson_init(lesgpu_case *c) {
     const DGrid &g = c->kp.g;
     DPois &P = c->pois;
     if (c->cfg.poisson == LESGPU_POISSON_Z_FT) return zft_init(c);
+    if (c->cfg.poisson == LESGPU_POISSON_MGRD) return mgrd_init(c);
     if (c->cfg.poisson != LESGPU_POISSON_FTFT) return LESGPU_ERR_UNSUPPORTED;
     if (c->cfg.xprdic != 1 || c->cfg.zprdic != 1) return LESGPU_ERR_CONFIG;
     int rc = make_plan(P.fx, g.n1m);
@@ -327,6 +328,7 @@ int poisson_init(lesgpu_case *c) {
 void poisson_free(lesgpu_case *c) {
     DPois &P = c->pois;
     zft_free(c);
+    mgrd_free(c);
     cudaFree(P.ak1); cudaFree(P.ak3); cudaFree(P.ccap);
     cudaFree(P.fx.tw); cudaFree(P.fz.tw);
     P.ak1 = P.ak3 = nullptr; P.ccap = nullptr; P.fx.tw = P.fz.tw = nullptr;
@@ -336,6 +338,7 @@ void launch_poisson(lesgpu_case *c, int msub) {
     const DGrid &g = c->kp.g;
     DPois &P = c->pois;
     if (c->cfg.poisson == LESGPU_POISSON_Z_FT) { launch_zft(c, msub); return; }
+    if (c->cfg.poisson == LESGPU_POISSON_MGRD) { launch_mgrd(c, msub); return; }
     DevPlan px = devplan(P.fx), pz = devplan(P.fz);
     int Lz = lines_per_block(g.n3m), Lx = lines_per_block(g.n1m);
     size_t smz = (size_t)2 * g.n3m * Lz * sizeof(double2), smx = (size_t)2 * g.n1m * Lx * sizeof(double2);

@@ -23,5 +23,9 @@ DevPlan devplan(const FftPlan &p);
 int zft_init(lesgpu_case *c);
 void zft_free(lesgpu_case *c);
 void launch_zft(lesgpu_case *c, int msub);
+// poiss_mgrd (k_mgrd.cu)
+int mgrd_init(lesgpu_case *c);
+void mgrd_free(lesgpu_case *c);
+void launch_mgrd(lesgpu_case *c, int msub);
 
 }  // namespace lg

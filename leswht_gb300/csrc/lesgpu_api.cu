@@ -80,7 +80,8 @@ int check_config(const lesgpu_config *c, const lesgpu_grid *g) {
     if (g->n1m < 2 || g->n2m < 2 || g->n3m < 1) return LESGPU_ERR_ARG;
     if ((long long)(g->n1 + 1) * (g->n2 + 1) * (g->n3 + 1) > (1LL << 40)) return LESGPU_ERR_ARG;
     if (c->precision != LESGPU_PREC_FP64 && c->precision != LESGPU_PREC_MIXED) return LESGPU_ERR_ARG;
-    if (c->poisson != LESGPU_POISSON_FTFT && c->poisson != LESGPU_POISSON_Z_FT) return LESGPU_ERR_UNSUPPORTED;
+    if (c->poisson != LESGPU_POISSON_FTFT && c->poisson != LESGPU_POISSON_Z_FT && c->poisson != LESGPU_POISSON_MGRD)
+        return LESGPU_ERR_UNSUPPORTED;
     if (c->imovingon != 0) return LESGPU_ERR_UNSUPPORTED;     // moving bodies: not built
     // poiss_ftft transforms x and z: both must be periodic
     if (c->poisson == LESGPU_POISSON_FTFT && (c->xprdic != 1 || c->zprdic != 1)) return LESGPU_ERR_CONFIG;

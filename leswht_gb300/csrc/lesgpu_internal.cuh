@@ -110,12 +110,14 @@ struct FftPlan {
 
 struct MgTables;              // poiss_z_ft multigrid tables (k_mg.cu)
 
+struct MgrdTables;
 struct DPois {
     double *ak1, *ak3;
     double2 *ccap;            // spectrum; ftft: (n1m, n3mh, n2m) i fastest, then k, then j;
                               // z_ft: (n1m, n2m, n3mh), one x-y plane per z mode
     FftPlan fx, fz;
     MgTables *mg;
+    MgrdTables *mgrd;         // poiss_mgrd (BiCGSTAB + MG3D)
 };
 
 struct KP {                   // everything a kernel may read, passed by value

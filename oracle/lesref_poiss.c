@@ -704,6 +704,394 @@ static void zft_poisson(ref_case *c)
     c->poisson_iters[c->msub >= 1 && c->msub <= 3 ? c->msub - 1 : 0] = itmax;
 }
 
+/* ------------------------------------------------------------ mgrd ---- */
+/* BiCGSTAB with a one-V-cycle MG3D preconditioner (poiss_mgrd.f90).  The
+   levels are laid side by side along x and along z as in the reference
+   (level ilev occupies i = iimg[ilev][0..1], k = kkmg[ilev][0..1]); y is never
+   coarsened.  gi is (0:n1md, 0:n2, 0:n3md), resid and bet/gam are
+   (n1md, n2m, n3md).  gi starts at zero in every mg3d call (the reference's
+   automatic array is uninitialised; every read of a never-written element is
+   multiplied by a zero coefficient). */
+#define MG_G(c, i, j, k) ((size_t)(i) + (size_t)((c)->n1md + 1) * ((size_t)(j) + (size_t)((c)->n2 + 1) * (size_t)(k)))
+#define MG_R(c, i, j, k) ((size_t)((i) - 1) + (size_t)(c)->n1md * ((size_t)((j) - 1) + (size_t)(c)->n2m * (size_t)((k) - 1)))
+
+/* mgcoef + tridcoef, poiss_mgrd.f90:717-993 (poisinit :678-715 gives the
+   finest-level coefficients) */
+static int mgrd_init(ref_case *c)
+{
+    ll n1 = c->n1, n3 = c->n3, n1m = c->n1m, n2m = c->n2m, n3m = c->n3m, n1md = c->n1md, n3md = c->n3md;
+    ll nlev = c->c.nlev;
+    if (nlev < 0 || nlev > 20 || n1m % (1LL << nlev) != 0 || n3m % (1LL << nlev) != 0) return LESGPU_ERR_CONFIG;
+    if (c->c.yprdic == 1) return LESGPU_ERR_UNSUPPORTED;
+    for (ll l = 0; l <= nlev; l++) {      /* periodic directions need even level sizes (a proper zebra) */
+        if (c->c.xprdic == 1 && ((n1m >> (nlev - l)) % 2) != 0 && (n1m >> (nlev - l)) > 1) return LESGPU_ERR_CONFIG;
+        if (c->c.zprdic == 1 && ((n3m >> (nlev - l)) % 2) != 0 && (n3m >> (nlev - l)) > 1) return LESGPU_ERR_CONFIG;
+    }
+    size_t nvx = (size_t)n1md + 2, nvz = (size_t)n3md + 2;
+    c->aw = ref_zalloc(nvx); c->ae = ref_zalloc(nvx); c->as = ref_zalloc((size_t)n2m + 2); c->an = ref_zalloc((size_t)n2m + 2);
+    c->ab = ref_zalloc(nvz); c->af = ref_zalloc(nvz);
+    c->fidw = ref_zalloc(nvx); c->fiup = ref_zalloc(nvx); c->fkdw = ref_zalloc(nvz); c->fkup = ref_zalloc(nvz);
+    c->ih1 = ref_izalloc(nvx); c->ih2 = ref_izalloc(nvx); c->il1 = ref_izalloc(nvx); c->il2 = ref_izalloc(nvx);
+    c->kh1 = ref_izalloc(nvz); c->kh2 = ref_izalloc(nvz); c->kl1 = ref_izalloc(nvz); c->kl2 = ref_izalloc(nvz);
+    c->ipm = ref_izalloc(nvx); c->imm = ref_izalloc(nvx); c->kpm = ref_izalloc(nvz); c->kmm = ref_izalloc(nvz);
+    size_t na = (size_t)n1md * (size_t)n2m * (size_t)n3md;
+    c->gam = ref_zalloc(na); c->bet = ref_zalloc(na);
+    /* poisinit */
+    for (ll i = 1; i <= n1m; i++) {
+        ll ip = c->ipv[i];
+        c->aw[i] = (1.0 - (double)c->fixil[i]) * c->c2cxi[i] * c->f2fxi[i];
+        c->ae[i] = (1.0 - (double)c->fixiu[i]) * c->c2cxi[ip] * c->f2fxi[i];
+    }
+    for (ll j = 1; j <= n2m; j++) {
+        ll jp = c->jpv[j];
+        c->as[j] = (1.0 - (double)c->fixjl[j]) * c->c2cyi[j] * c->f2fyi[j];
+        c->an[j] = (1.0 - (double)c->fixju[j]) * c->c2cyi[jp] * c->f2fyi[j];
+    }
+    for (ll k = 1; k <= n3m; k++) {
+        ll kp = c->kpv[k];
+        c->ab[k] = (1.0 - (double)c->fixkl[k]) * c->c2czi[k] * c->f2fzi[k];
+        c->af[k] = (1.0 - (double)c->fixku[k]) * c->c2czi[kp] * c->f2fzi[k];
+    }
+    /* mgcoef: level index ranges */
+    c->iimg[nlev][0] = 1; c->iimg[nlev][1] = n1m; c->iimg[nlev][2] = n1m;
+    c->kkmg[nlev][0] = 1; c->kkmg[nlev][1] = n3m; c->kkmg[nlev][2] = n3m;
+    for (ll l = nlev - 1; l >= 0; l--) {
+        c->iimg[l][0] = c->iimg[l + 1][0] + c->iimg[l + 1][2];
+        c->iimg[l][2] = (n1m / (1LL << nlev)) * (1LL << l);
+        c->iimg[l][1] = c->iimg[l][0] + c->iimg[l][2] - 1;
+        c->kkmg[l][0] = c->kkmg[l + 1][0] + c->kkmg[l + 1][2];
+        c->kkmg[l][2] = (n3m / (1LL << nlev)) * (1LL << l);
+        c->kkmg[l][1] = c->kkmg[l][0] + c->kkmg[l][2] - 1;
+    }
+    double *xmpm = ref_zalloc(nvx), *zmpm = ref_zalloc(nvz);
+    ll *iwest = ref_izalloc(nvx), *ieast = ref_izalloc(nvx), *kback = ref_izalloc(nvz), *kforw = ref_izalloc(nvz);
+    const double *x = c->x, *z = c->z;
+    for (ll i = 1; i <= n1m; i++) { xmpm[i] = c->xmp[i]; iwest[i] = 1 - 1 / i; ieast[i] = 1 - i / n1m; }
+    for (ll k = 1; k <= n3m; k++) { zmpm[k] = c->zmp[k]; kback[k] = 1 - 1 / k; kforw[k] = 1 - k / n3m; }
+    for (ll l = nlev - 1; l >= 0; l--) {
+        ll ibg = c->iimg[l][0], iend = c->iimg[l][1], kbg = c->kkmg[l][0], kend = c->kkmg[l][1];
+        ll sp = 1LL << (nlev - l), ic = 0;
+        for (ll i = ibg; i <= iend; i++) {
+            ic++;
+            xmpm[i] = 0.5 * (x[(ic - 1) * sp + 1] + x[ic * sp + 1]);
+            iwest[i] = 1 - ibg / i; ieast[i] = 1 - i / iend;
+        }
+        ic = 0;
+        for (ll k = kbg; k <= kend; k++) {
+            ic++;
+            zmpm[k] = 0.5 * (z[(ic - 1) * sp + 1] + z[ic * sp + 1]);
+            kback[k] = 1 - kbg / k; kforw[k] = 1 - k / kend;
+        }
+        /* a factor that is zero (the non-periodic edges) multiplies a
+           difference with a point outside the level: left at zero here */
+        ic = 0;
+        for (ll i = ibg; i <= iend; i++) {
+            ic++;
+            double w = x[ic * sp + 1] - x[(ic - 1) * sp + 1];
+            c->aw[i] = iwest[i] ? 1.0 / ((xmpm[i] - xmpm[i - 1]) * w) : 0.0;
+            c->ae[i] = ieast[i] ? 1.0 / ((xmpm[i + 1] - xmpm[i]) * w) : 0.0;
+        }
+        ic = 0;
+        for (ll k = kbg; k <= kend; k++) {
+            ic++;
+            double w = z[ic * sp + 1] - z[(ic - 1) * sp + 1];
+            c->ab[k] = kback[k] ? 1.0 / ((zmpm[k] - zmpm[k - 1]) * w) : 0.0;
+            c->af[k] = kforw[k] ? 1.0 / ((zmpm[k + 1] - zmpm[k]) * w) : 0.0;
+        }
+    }
+    /* restriction */
+    for (ll l = 0; l <= nlev - 1; l++) {
+        ll h = c->iimg[l + 1][0];
+        for (ll i = c->iimg[l][0]; i <= c->iimg[l][1]; i++, h += 2) {
+            c->fidw[i] = (xmpm[i] - xmpm[h]) / (xmpm[h + 1] - xmpm[h]);
+            c->ih1[i] = h; c->ih2[i] = h + 1;
+        }
+        h = c->kkmg[l + 1][0];
+        for (ll k = c->kkmg[l][0]; k <= c->kkmg[l][1]; k++, h += 2) {
+            c->fkdw[k] = (zmpm[k] - zmpm[h]) / (zmpm[h + 1] - zmpm[h]);
+            c->kh1[k] = h; c->kh2[k] = h + 1;
+        }
+    }
+    /* prolongation (the first and last points get the Neumann weights 1 and
+       0; their other index points outside the coarser level) */
+    for (ll l = 1; l <= nlev; l++) {
+        ll lo = c->iimg[l - 1][0];
+        for (ll i = c->iimg[l][0]; i <= c->iimg[l][1]; i += 2, lo++) {
+            if (i > c->iimg[l][0]) c->fiup[i] = (xmpm[i] - xmpm[lo - 1]) / (xmpm[lo] - xmpm[lo - 1]);
+            if (i + 1 < c->iimg[l][1]) c->fiup[i + 1] = (xmpm[i + 1] - xmpm[lo]) / (xmpm[lo + 1] - xmpm[lo]);
+            c->il1[i] = lo - 1; c->il2[i] = lo; c->il1[i + 1] = lo; c->il2[i + 1] = lo + 1;
+        }
+        c->fiup[c->iimg[l][0]] = 1.0;
+        c->fiup[c->iimg[l][1]] = 0.0;
+        lo = c->kkmg[l - 1][0];
+        for (ll k = c->kkmg[l][0]; k <= c->kkmg[l][1]; k += 2, lo++) {
+            if (k > c->kkmg[l][0]) c->fkup[k] = (zmpm[k] - zmpm[lo - 1]) / (zmpm[lo] - zmpm[lo - 1]);
+            if (k + 1 < c->kkmg[l][1]) c->fkup[k + 1] = (zmpm[k + 1] - zmpm[lo]) / (zmpm[lo + 1] - zmpm[lo]);
+            c->kl1[k] = lo - 1; c->kl2[k] = lo; c->kl1[k + 1] = lo; c->kl2[k + 1] = lo + 1;
+        }
+        c->fkup[c->kkmg[l][0]] = 1.0;
+        c->fkup[c->kkmg[l][1]] = 0.0;
+    }
+    for (ll l = nlev; l >= 0; l--) {
+        for (ll k = c->kkmg[l][0]; k <= c->kkmg[l][1]; k++) { c->kpm[k] = k + 1; c->kmm[k] = k - 1; }
+        for (ll i = c->iimg[l][0]; i <= c->iimg[l][1]; i++) { c->ipm[i] = i + 1; c->imm[i] = i - 1; }
+    }
+    if (c->c.xprdic == 1) {
+        for (ll l = nlev; l >= 0; l--) { c->ipm[c->iimg[l][1]] = c->iimg[l][0]; c->imm[c->iimg[l][0]] = c->iimg[l][1]; }
+        for (ll l = nlev - 1; l >= 0; l--) {
+            ll ibg = c->iimg[l][0], iend = c->iimg[l][1], sp = 1LL << (nlev - l);
+            double vdx = xmpm[ibg] - x[1] + x[n1] - xmpm[iend];
+            c->aw[ibg] = 1.0 / (vdx * (x[1 + sp] - x[1]));
+            c->ae[iend] = 1.0 / (vdx * (x[n1] - x[n1 - sp]));
+        }
+        for (ll l = 1; l <= nlev; l++) {
+            ll ibg = c->iimg[l][0], iend = c->iimg[l][1], ibgl = c->iimg[l - 1][0], iendl = c->iimg[l - 1][1];
+            double dx = xmpm[ibgl] - x[1] + x[n1] - xmpm[iendl];
+            c->fiup[ibg] = (x[n1] - xmpm[iendl] + xmpm[ibg] - x[1]) / dx;
+            c->fiup[iend] = (xmpm[iend] - xmpm[iendl]) / dx;
+            c->il1[ibg] = iendl; c->il2[ibg] = ibgl; c->il1[iend] = iendl; c->il2[iend] = ibgl;
+        }
+    }
+    if (c->c.zprdic == 1) {
+        for (ll l = nlev; l >= 0; l--) { c->kpm[c->kkmg[l][1]] = c->kkmg[l][0]; c->kmm[c->kkmg[l][0]] = c->kkmg[l][1]; }
+        for (ll l = nlev - 1; l >= 0; l--) {
+            ll kbg = c->kkmg[l][0], kend = c->kkmg[l][1], sp = 1LL << (nlev - l);
+            double vdz = zmpm[kbg] - z[1] + z[n3] - zmpm[kend];
+            c->ab[kbg] = 1.0 / (vdz * (z[1 + sp] - z[1]));
+            c->af[kend] = 1.0 / (vdz * (z[n3] - z[n3 - sp]));
+        }
+        for (ll l = 1; l <= nlev; l++) {
+            ll kbg = c->kkmg[l][0], kend = c->kkmg[l][1], kbgl = c->kkmg[l - 1][0], kendl = c->kkmg[l - 1][1];
+            double dz = zmpm[kbgl] - z[1] + z[n3] - zmpm[kendl];
+            c->fkup[kbg] = (z[n3] - zmpm[kendl] + zmpm[kbg] - z[1]) / dz;
+            c->fkup[kend] = (zmpm[kend] - zmpm[kendl]) / dz;
+            c->kl1[kbg] = kendl; c->kl2[kbg] = kbgl; c->kl1[kend] = kendl; c->kl2[kend] = kbgl;
+        }
+    }
+    /* tridcoef */
+    for (ll l = 0; l <= nlev; l++)
+        for (ll k = c->kkmg[l][0]; k <= c->kkmg[l][1]; k++)
+            for (ll i = c->iimg[l][0]; i <= c->iimg[l][1]; i++) {
+                double acc = -1.0 * (c->aw[i] + c->ae[i] + c->as[1] + c->an[1] + c->ab[k] + c->af[k]);
+                c->bet[MG_R(c, i, 1, k)] = 1.0 / acc;
+                for (ll j = 2; j <= n2m; j++) {
+                    acc = -1.0 * (c->aw[i] + c->ae[i] + c->as[j] + c->an[j] + c->ab[k] + c->af[k]);
+                    double g = c->an[j - 1] * c->bet[MG_R(c, i, j - 1, k)];
+                    c->gam[MG_R(c, i, j, k)] = g;
+                    c->bet[MG_R(c, i, j, k)] = 1.0 / (acc - c->as[j] * g);
+                }
+            }
+    free(xmpm); free(zmpm); free(iwest); free(ieast); free(kback); free(kforw);
+    return 0;
+}
+
+/* One zebra half-sweep at level l: the y lines (i, k) with
+   i = i0(k), i0(k)+2, ... take rhs - iold * (x and z neighbours) and are
+   solved with the stored LU (relax / toplevel, poiss_mgrd.f90:271-330,
+   502-568).  color 0 starts at iimg + mod(kpm(k), 2), color 1 at
+   iimg + mod(k, 2).  src(i, j, k) gives the right-hand side. */
+typedef double (*mg_src_fn)(const ref_case *c, const double *src, ll i, ll j, ll k);
+static double mg_src_resid(const ref_case *c, const double *src, ll i, ll j, ll k) { return src[MG_R(c, i, j, k)]; }
+static double mg_src_full(const ref_case *c, const double *src, ll i, ll j, ll k) { return src[IX(c, i, j, k)]; }
+
+static void mg_half(const ref_case *c, double *gi, const double *src, mg_src_fn fs, ll l, int color, double iold)
+{
+    ll n2m = c->n2m;
+    for (ll k = c->kkmg[l][0]; k <= c->kkmg[l][1]; k++) {
+        ll i0 = c->iimg[l][0] + (color == 0 ? c->kpm[k] % 2 : k % 2);
+        for (ll i = i0; i <= c->iimg[l][1]; i += 2) {
+            for (ll j = 1; j <= n2m; j++)
+                gi[MG_G(c, i, j, k)] = fs(c, src, i, j, k) - iold * (c->aw[i] * gi[MG_G(c, c->imm[i], j, k)] + c->ae[i] * gi[MG_G(c, c->ipm[i], j, k)]
+                                                                     + c->ab[k] * gi[MG_G(c, i, j, c->kmm[k])] + c->af[k] * gi[MG_G(c, i, j, c->kpm[k])]);
+        }
+    }
+    for (ll k = c->kkmg[l][0]; k <= c->kkmg[l][1]; k++) {
+        ll i0 = c->iimg[l][0] + (color == 0 ? c->kpm[k] % 2 : k % 2);
+        for (ll i = i0; i <= c->iimg[l][1]; i += 2) {
+            gi[MG_G(c, i, 1, k)] = gi[MG_G(c, i, 1, k)] * c->bet[MG_R(c, i, 1, k)];
+            for (ll j = 2; j <= n2m; j++)
+                gi[MG_G(c, i, j, k)] = (gi[MG_G(c, i, j, k)] - c->as[j] * gi[MG_G(c, i, j - 1, k)]) * c->bet[MG_R(c, i, j, k)];
+            for (ll j = n2m - 1; j >= 1; j--)
+                gi[MG_G(c, i, j, k)] = gi[MG_G(c, i, j, k)] - c->gam[MG_R(c, i, j + 1, k)] * gi[MG_G(c, i, j + 1, k)];
+        }
+    }
+}
+
+/* rhs - A gi at (i, j, k) of any level (rescal / toplevel's residual) */
+static inline double mg_defect(const ref_case *c, const double *gi, double rhs, ll i, ll j, ll k)
+{
+    double acc = -1.0 * (c->aw[i] + c->ae[i] + c->as[j] + c->an[j] + c->ab[k] + c->af[k]);
+    return rhs - acc * gi[MG_G(c, i, j, k)] - c->aw[i] * gi[MG_G(c, c->imm[i], j, k)] - c->ae[i] * gi[MG_G(c, c->ipm[i], j, k)]
+           - c->as[j] * gi[MG_G(c, i, j - 1, k)] - c->an[j] * gi[MG_G(c, i, j + 1, k)]
+           - c->ab[k] * gi[MG_G(c, i, j, c->kmm[k])] - c->af[k] * gi[MG_G(c, i, j, c->kpm[k])];
+}
+
+/* godown, poiss_mgrd.f90:455-476: restrict resid from level l+1 to l */
+static void mg_godown(const ref_case *c, double *resid, ll l)
+{
+    for (ll k = c->kkmg[l][0]; k <= c->kkmg[l][1]; k++)
+        for (ll j = 1; j <= c->n2m; j++)
+            for (ll i = c->iimg[l][0]; i <= c->iimg[l][1]; i++) {
+                double fi = c->fidw[i], fk = c->fkdw[k];
+                resid[MG_R(c, i, j, k)] = (1.0 - fi) * (1.0 - fk) * resid[MG_R(c, c->ih1[i], j, c->kh1[k])]
+                                          + fi * (1.0 - fk) * resid[MG_R(c, c->ih2[i], j, c->kh1[k])]
+                                          + (1.0 - fi) * fk * resid[MG_R(c, c->ih1[i], j, c->kh2[k])]
+                                          + fi * fk * resid[MG_R(c, c->ih2[i], j, c->kh2[k])];
+            }
+}
+
+/* goup, poiss_mgrd.f90:479-500: add the interpolated correction of level
+   l-1 to the points i = iimg + mod(k, 2), +2, ... of level l.  An index
+   outside the coarser level carries a zero weight and reads zero. */
+static void mg_goup(const ref_case *c, double *gi, ll l)
+{
+    ll lo_i = c->iimg[l - 1][0], hi_i = c->iimg[l - 1][1], lo_k = c->kkmg[l - 1][0], hi_k = c->kkmg[l - 1][1];
+    for (ll k = c->kkmg[l][0]; k <= c->kkmg[l][1]; k++) {
+        ll i0 = c->iimg[l][0] + k % 2;
+        for (ll j = 1; j <= c->n2m; j++)
+            for (ll i = i0; i <= c->iimg[l][1]; i += 2) {
+                double fi = c->fiup[i], fk = c->fkup[k];
+                ll a1 = c->il1[i], a2 = c->il2[i], b1 = c->kl1[k], b2 = c->kl2[k];
+#define MG_C(ii, kk) (((ii) >= lo_i && (ii) <= hi_i && (kk) >= lo_k && (kk) <= hi_k) ? gi[MG_G(c, ii, j, kk)] : 0.0)
+                gi[MG_G(c, i, j, k)] = gi[MG_G(c, i, j, k)] + (1.0 - fi) * (1.0 - fk) * MG_C(a1, b1) + fi * (1.0 - fk) * MG_C(a2, b1)
+                                       + (1.0 - fi) * fk * MG_C(a1, b2) + fi * fk * MG_C(a2, b2);
+#undef MG_C
+            }
+    }
+}
+
+/* mg3d, poiss_mgrd.f90:227-268 (+ toplevel :271-400, rescal :403-425,
+   relax :502-675); sol and rhs are full arrays, only their interior is used */
+static void mg3d(const ref_case *c, double *sol, const double *rhs, double *gi, double *resid, double iold)
+{
+    ll nlev = c->c.nlev, n2m = c->n2m, nbli = c->c.nbli;
+    memset(gi, 0, sizeof(double) * (size_t)(c->n1md + 1) * (size_t)(c->n2 + 1) * (size_t)(c->n3md + 1));
+    for (int pass = 0; pass < 2; pass++) {
+        double io = pass == 0 ? iold : 1.0;
+        /* toplevel */
+        mg_half(c, gi, rhs, mg_src_full, nlev, 0, io);
+        mg_half(c, gi, rhs, mg_src_full, nlev, 1, 1.0);
+        if (pass == 1) break;              /* the closing toplevel's residual is discarded */
+        for (ll k = 1; k <= c->n3m; k++)
+            for (ll j = 1; j <= n2m; j++)
+                for (ll i = 1; i <= c->n1m; i++)
+                    resid[MG_R(c, i, j, k)] = mg_defect(c, gi, rhs[IX(c, i, j, k)], i, j, k);
+        if (nlev > 0) {
+            mg_godown(c, resid, nlev - 1);
+            for (ll l = nlev - 1; l >= 1; l--) {
+                mg_half(c, gi, resid, mg_src_resid, l, 0, 0.0);
+                mg_half(c, gi, resid, mg_src_resid, l, 1, 1.0);
+                for (ll k = c->kkmg[l][0]; k <= c->kkmg[l][1]; k++)
+                    for (ll j = 1; j <= n2m; j++)
+                        for (ll i = c->iimg[l][0]; i <= c->iimg[l][1]; i++)
+                            resid[MG_R(c, i, j, k)] = mg_defect(c, gi, resid[MG_R(c, i, j, k)], i, j, k);
+                mg_godown(c, resid, l - 1);
+            }
+            mg_half(c, gi, resid, mg_src_resid, 0, 0, 0.0);
+            mg_half(c, gi, resid, mg_src_resid, 0, 1, 1.0);
+            for (ll it = 1; it < nbli; it++) {
+                mg_half(c, gi, resid, mg_src_resid, 0, 0, 1.0);
+                mg_half(c, gi, resid, mg_src_resid, 0, 1, 1.0);
+            }
+            for (ll l = 1; l <= nlev - 1; l++) {
+                mg_goup(c, gi, l);
+                mg_half(c, gi, resid, mg_src_resid, l, 0, 1.0);
+                mg_half(c, gi, resid, mg_src_resid, l, 1, 1.0);
+            }
+            mg_goup(c, gi, nlev);
+        }
+    }
+    for (ll k = 1; k <= c->n3m; k++)
+        for (ll j = 1; j <= n2m; j++)
+            for (ll i = 1; i <= c->n1m; i++) sol[IX(c, i, j, k)] = gi[MG_G(c, i, j, k)];
+}
+
+/* A q at an interior point (the 7-point operator of poisson :113-122) */
+static inline double mg_apply(const ref_case *c, const double *q, ll i, ll j, ll k)
+{
+    double acc = -1.0 * (c->aw[i] + c->ae[i] + c->as[j] + c->an[j] + c->ab[k] + c->af[k]);
+    return c->aw[i] * q[IX(c, c->imm[i], j, k)] + c->ae[i] * q[IX(c, c->ipm[i], j, k)] + c->as[j] * q[IX(c, i, j - 1, k)]
+           + c->an[j] * q[IX(c, i, j + 1, k)] + c->ab[k] * q[IX(c, i, j, c->kmm[k])] + c->af[k] * q[IX(c, i, j, c->kpm[k])]
+           + acc * q[IX(c, i, j, k)];
+}
+
+/* poisson, poiss_mgrd.f90:25-224 (IOLDV = 1 starts from phi = 0 as well:
+   solver.f90 zeroes phi before every call) */
+static void mgrd_poisson(ref_case *c)
+{
+    ll n1m = c->n1m, n2m = c->n2m, n3m = c->n3m;
+    size_t nt = (size_t)(c->n1 + 1) * (size_t)(c->n2 + 1) * (size_t)(c->n3 + 1);
+    double *p = ref_zalloc(nt), *s = ref_zalloc(nt), *y = ref_zalloc(nt), *zz = ref_zalloc(nt), *v = ref_zalloc(nt);
+    double *t = ref_zalloc(nt), *res = ref_zalloc(nt);
+    double *gi = ref_zalloc((size_t)(c->n1md + 1) * (size_t)(c->n2 + 1) * (size_t)(c->n3md + 1));
+    double *resid = ref_zalloc((size_t)c->n1md * (size_t)n2m * (size_t)c->n3md);
+    const double *b = c->divgsum;
+    double *phi = c->phi;
+    for (size_t q = 0; q < nt; q++) phi[q] = 0.0;
+    for (ll k = 1; k <= n3m; k++)
+        for (ll j = 1; j <= n2m; j++)
+            for (ll i = 1; i <= n1m; i++) res[IX(c, i, j, k)] = b[IX(c, i, j, k)];
+    double rho_ol = 1.0, alp = 1.0, w = 1.0;
+    ll it, done = c->c.mgitr;
+    for (it = 1; it <= c->c.mgitr; it++) {
+        double rho = 0.0;
+        for (ll k = 1; k <= n3m; k++)
+            for (ll j = 1; j <= n2m; j++)
+                for (ll i = 1; i <= n1m; i++) rho += b[IX(c, i, j, k)] * res[IX(c, i, j, k)];
+        double bet = rho / rho_ol * alp / w;
+        for (ll k = 1; k <= n3m; k++)
+            for (ll j = 1; j <= n2m; j++)
+                for (ll i = 1; i <= n1m; i++) {
+                    size_t q = IX(c, i, j, k);
+                    p[q] = res[q] + bet * (p[q] - w * v[q]);
+                }
+        mg3d(c, y, p, gi, resid, (double)c->c.ioldv);
+        double rv = 0.0;
+        for (ll k = 1; k <= n3m; k++)
+            for (ll j = 1; j <= n2m; j++)
+                for (ll i = 1; i <= n1m; i++) {
+                    size_t q = IX(c, i, j, k);
+                    v[q] = mg_apply(c, y, i, j, k);
+                    rv += b[q] * v[q];
+                }
+        alp = rho / rv;
+        for (ll k = 1; k <= n3m; k++)
+            for (ll j = 1; j <= n2m; j++)
+                for (ll i = 1; i <= n1m; i++) {
+                    size_t q = IX(c, i, j, k);
+                    s[q] = res[q] - alp * v[q];
+                }
+        mg3d(c, zz, s, gi, resid, (double)c->c.ioldv);
+        double up = 0.0, bt = 0.0;
+        for (ll k = 1; k <= n3m; k++)
+            for (ll j = 1; j <= n2m; j++)
+                for (ll i = 1; i <= n1m; i++) {
+                    size_t q = IX(c, i, j, k);
+                    t[q] = mg_apply(c, zz, i, j, k);
+                    up += t[q] * s[q];
+                    bt += t[q] * t[q];
+                }
+        w = up / bt;
+        double resm = 0.0;
+        for (ll k = 1; k <= n3m; k++)
+            for (ll j = 1; j <= n2m; j++)
+                for (ll i = 1; i <= n1m; i++) {
+                    size_t q = IX(c, i, j, k);
+                    phi[q] = phi[q] + alp * y[q] + w * zz[q];
+                    res[q] = s[q] - w * t[q];
+                    if (fabs(res[q]) > resm) resm = fabs(res[q]);
+                }
+        rho_ol = rho;
+        if (resm < c->test1) { done = it; break; }
+    }
+    double phiref = phi[IX(c, 1, n2m, 1)];
+    for (ll k = 1; k <= n3m; k++)
+        for (ll j = 1; j <= n2m; j++)
+            for (ll i = 1; i <= n1m; i++) phi[IX(c, i, j, k)] = phi[IX(c, i, j, k)] - phiref;
+    free(p); free(s); free(y); free(zz); free(v); free(t); free(res); free(gi); free(resid);
+    c->poisson_iters[c->msub >= 1 && c->msub <= 3 ? c->msub - 1 : 0] = done;
+}
+
 /* ------------------------------------------------------------ dispatch -- */
 int ref_poisinit(ref_case *c)
 {
@@ -716,6 +1104,8 @@ int ref_poisinit(ref_case *c)
     case LESGPU_POISSON_Z_FT:
         if (c->c.zprdic != 1 && c->n3m > 1) return LESGPU_ERR_CONFIG;
         return zft_init(c);
+    case LESGPU_POISSON_MGRD:
+        return mgrd_init(c);
     default:
         return LESGPU_ERR_UNSUPPORTED;
     }
@@ -726,6 +1116,7 @@ void ref_poisson(ref_case *c)
     switch (c->c.poisson) {
     case LESGPU_POISSON_FTFT: ftft_poisson(c); break;
     case LESGPU_POISSON_Z_FT: zft_poisson(c); break;
+    case LESGPU_POISSON_MGRD: mgrd_poisson(c); break;
     default: break;
     }
 }
