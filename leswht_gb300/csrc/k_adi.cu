@@ -39,6 +39,7 @@ __device__ __forceinline__ void line_coords(int dir, int l, int x0, int x1, int 
 // type (double; float for the x and z sweeps of the mixed-precision form).
 template <class R>
 __device__ __forceinline__ void adi_coef(const KP &p, int comp, int dir, int i, int j, int k, R &a, R &c) {
+    const Mir<R> &M = mir<R>(p);
     const DGrid &g = p.g;
     const DFields &f = p.f;
     const R re = p.c.re;
@@ -48,35 +49,35 @@ __device__ __forceinline__ void adi_coef(const KP &p, int comp, int dir, int i, 
         R cs = R(1.0), ks1 = R(1.0), ks2 = R(1.0), omc = R(1.0);
         int ka = dir == 2 ? 5 : dir == 1 ? 3 : 1;
         if (p.c.iconjg == 1) {
-            cs = R(f.cstar[q]);
-            ks1 = R(f.kstar[ka][q]);
-            ks2 = R(f.kstar[ka - 1][q]);
+            cs = R(M.cstar[q]);
+            ks1 = R(M.kstar[ka][q]);
+            ks2 = R(M.kstar[ka - 1][q]);
             omc = p.c.imovingon == 0 ? R(f.omega[q]) : R(1.0);
         }
         if (dir == 2) {
-            a = R(f.akuv[k]) * (cs * ks1 + cre * omc * R(f.alsgs1[1][q]));
-            c = R(f.ckuv[k]) * (cs * ks2 + cre * omc * R(f.alsgs1[1][q + g.sxy]));
+            a = R(M.akuv[k]) * (cs * ks1 + cre * omc * R(M.alsgs1[1][q]));
+            c = R(M.ckuv[k]) * (cs * ks2 + cre * omc * R(M.alsgs1[1][q + g.sxy]));
         } else if (dir == 1) {
-            a = R(f.ajuw[j]) * (cs * ks1 + cre * omc * R(f.alsgs1[2][q]));
-            c = R(f.cjuw[j]) * (cs * ks2 + cre * omc * R(f.alsgs1[2][q + g.sx]));
+            a = R(M.ajuw[j]) * (cs * ks1 + cre * omc * R(M.alsgs1[2][q]));
+            c = R(M.cjuw[j]) * (cs * ks2 + cre * omc * R(M.alsgs1[2][q + g.sx]));
         } else {
-            a = R(f.aivw[i]) * (cs * ks1 + cre * omc * R(f.alsgs1[0][q]));
-            c = R(f.civw[i]) * (cs * ks2 + cre * omc * R(f.alsgs1[0][q + 1]));
+            a = R(M.aivw[i]) * (cs * ks1 + cre * omc * R(M.alsgs1[0][q]));
+            c = R(M.civw[i]) * (cs * ks2 + cre * omc * R(M.alsgs1[0][q + 1]));
         }
         return;
     }
     const R cre = (double)p.c.iles * re, cre2 = R(2.0) * (double)p.c.iles * re;
-    const double *nu = f.nusgs, *nu1 = f.nusgs1[0], *nu2 = f.nusgs1[1], *nu3 = f.nusgs1[2];
+    const R *nu = M.nusgs, *nu1 = M.nusgs1[0], *nu2 = M.nusgs1[1], *nu3 = M.nusgs1[2];
     switch (comp * 3 + dir) {
-    case CU * 3 + 2: a = R(f.akuv[k]) * (R(1.0) + cre * R(nu2[q])); c = R(f.ckuv[k]) * (R(1.0) + cre * R(nu2[q + g.sxy])); break;
-    case CU * 3 + 1: a = R(f.ajuw[j]) * (R(1.0) + cre * R(nu3[q])); c = R(f.cjuw[j]) * (R(1.0) + cre * R(nu3[q + g.sx])); break;
-    case CU * 3 + 0: a = R(f.aiu[i]) * (R(1.0) + cre2 * R(nu[q - 1])); c = R(f.ciu[i]) * (R(1.0) + cre2 * R(nu[q])); break;
-    case CV * 3 + 2: a = R(f.akuv[k]) * (R(1.0) + cre * R(nu1[q])); c = R(f.ckuv[k]) * (R(1.0) + cre * R(nu1[q + g.sxy])); break;
-    case CV * 3 + 1: a = R(f.ajv[j]) * (R(1.0) + cre2 * R(nu[q - g.sx])); c = R(f.cjv[j]) * (R(1.0) + cre2 * R(nu[q])); break;
-    case CV * 3 + 0: a = R(f.aivw[i]) * (R(1.0) + cre * R(nu3[q])); c = R(f.civw[i]) * (R(1.0) + cre * R(nu3[q + 1])); break;
-    case CW * 3 + 2: a = R(f.akw[k]) * (R(1.0) + cre2 * R(nu[q - g.sxy])); c = R(f.ckw[k]) * (R(1.0) + cre2 * R(nu[q])); break;
-    case CW * 3 + 1: a = R(f.ajuw[j]) * (R(1.0) + cre * R(nu1[q])); c = R(f.cjuw[j]) * (R(1.0) + cre * R(nu1[q + g.sx])); break;
-    default:         a = R(f.aivw[i]) * (R(1.0) + cre * R(nu2[q])); c = R(f.civw[i]) * (R(1.0) + cre * R(nu2[q + 1])); break;
+    case CU * 3 + 2: a = R(M.akuv[k]) * (R(1.0) + cre * R(nu2[q])); c = R(M.ckuv[k]) * (R(1.0) + cre * R(nu2[q + g.sxy])); break;
+    case CU * 3 + 1: a = R(M.ajuw[j]) * (R(1.0) + cre * R(nu3[q])); c = R(M.cjuw[j]) * (R(1.0) + cre * R(nu3[q + g.sx])); break;
+    case CU * 3 + 0: a = R(M.aiu[i]) * (R(1.0) + cre2 * R(nu[q - 1])); c = R(M.ciu[i]) * (R(1.0) + cre2 * R(nu[q])); break;
+    case CV * 3 + 2: a = R(M.akuv[k]) * (R(1.0) + cre * R(nu1[q])); c = R(M.ckuv[k]) * (R(1.0) + cre * R(nu1[q + g.sxy])); break;
+    case CV * 3 + 1: a = R(M.ajv[j]) * (R(1.0) + cre2 * R(nu[q - g.sx])); c = R(M.cjv[j]) * (R(1.0) + cre2 * R(nu[q])); break;
+    case CV * 3 + 0: a = R(M.aivw[i]) * (R(1.0) + cre * R(nu3[q])); c = R(M.civw[i]) * (R(1.0) + cre * R(nu3[q + 1])); break;
+    case CW * 3 + 2: a = R(M.akw[k]) * (R(1.0) + cre2 * R(nu[q - g.sxy])); c = R(M.ckw[k]) * (R(1.0) + cre2 * R(nu[q])); break;
+    case CW * 3 + 1: a = R(M.ajuw[j]) * (R(1.0) + cre * R(nu1[q])); c = R(M.cjuw[j]) * (R(1.0) + cre * R(nu1[q + g.sx])); break;
+    default:         a = R(M.aivw[i]) * (R(1.0) + cre * R(nu2[q])); c = R(M.civw[i]) * (R(1.0) + cre * R(nu2[q + 1])); break;
     }
 }
 

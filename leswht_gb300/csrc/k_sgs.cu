@@ -17,49 +17,50 @@ namespace lg {
 // velgrad, sgs.f90:772-875.  R: arithmetic type (float in the mixed form).
 template <class R>
 __device__ void velgrad(const KP &p, int i, int j, int k, R a[9], R sr[6]) {
+    const Mir<R> &M = mir<R>(p);
     const DGrid &g = p.g;
-    const double *u = p.f.u, *v = p.f.v, *w = p.f.w;
+    const R *u = M.u, *v = M.v, *w = M.w;
     int kp = g.kpv[k], km = g.kmv[k], jp = g.jpv[j], jm = g.jmv[j], ip = g.ipv[i], im = g.imv[i];
     int n1 = g.n1, n2 = g.n2, n3 = g.n3;
     R fju = fixd(g.fixju[j]), fjl = fixd(g.fixjl[j]), fku = fixd(g.fixku[k]), fkl = fixd(g.fixkl[k]);
     R fiu = fixd(g.fixiu[i]), fil = fixd(g.fixil[i]);
-    const double *f2fx = g.f2fx, *f2fy = g.f2fy, *f2fz = g.f2fz;
+    const R *f2fx = M.f2fx, *f2fy = M.f2fy, *f2fz = M.f2fz;
 #define U(a_, b_, c_) R(u[g.ix(a_, b_, c_)])
 #define V(a_, b_, c_) R(v[g.ix(a_, b_, c_)])
 #define W(a_, b_, c_) R(w[g.ix(a_, b_, c_)])
-    R vg11 = R(g.f2fxi[i]) * (U(ip, j, k) - U(i, j, k));
-    R up = R(g.c2cyi[jp]) * R(0.25) * (R(f2fy[jp]) * (U(i, j, k) + U(ip, j, k)) + R(f2fy[j]) * (U(i, jp, k) + U(ip, jp, k))) * (R(1.0) - fju)
+    R vg11 = R(M.f2fxi[i]) * (U(ip, j, k) - U(i, j, k));
+    R up = R(M.c2cyi[jp]) * R(0.25) * (R(f2fy[jp]) * (U(i, j, k) + U(ip, j, k)) + R(f2fy[j]) * (U(i, jp, k) + U(ip, jp, k))) * (R(1.0) - fju)
               + R(0.5) * (U(i, n2, k) + U(ip, n2, k)) * fju;
-    R um = R(g.c2cyi[j]) * R(0.25) * (R(f2fy[j]) * (U(i, jm, k) + U(ip, jm, k)) + R(f2fy[jm]) * (U(i, j, k) + U(ip, j, k))) * (R(1.0) - fjl)
+    R um = R(M.c2cyi[j]) * R(0.25) * (R(f2fy[j]) * (U(i, jm, k) + U(ip, jm, k)) + R(f2fy[jm]) * (U(i, j, k) + U(ip, j, k))) * (R(1.0) - fjl)
               + R(0.5) * (U(i, 0, k) + U(ip, 0, k)) * fjl;
-    R vg12 = R(g.f2fyi[j]) * (up - um);
-    up = R(g.c2czi[kp]) * R(0.25) * (R(f2fz[kp]) * (U(i, j, k) + U(ip, j, k)) + R(f2fz[k]) * (U(i, j, kp) + U(ip, j, kp))) * (R(1.0) - fku)
+    R vg12 = R(M.f2fyi[j]) * (up - um);
+    up = R(M.c2czi[kp]) * R(0.25) * (R(f2fz[kp]) * (U(i, j, k) + U(ip, j, k)) + R(f2fz[k]) * (U(i, j, kp) + U(ip, j, kp))) * (R(1.0) - fku)
        + R(0.5) * (U(i, j, n3) + U(ip, j, n3)) * fku;
-    um = R(g.c2czi[k]) * R(0.25) * (R(f2fz[k]) * (U(i, j, km) + U(ip, j, km)) + R(f2fz[km]) * (U(i, j, k) + U(ip, j, k))) * (R(1.0) - fkl)
+    um = R(M.c2czi[k]) * R(0.25) * (R(f2fz[k]) * (U(i, j, km) + U(ip, j, km)) + R(f2fz[km]) * (U(i, j, k) + U(ip, j, k))) * (R(1.0) - fkl)
        + R(0.5) * (U(i, j, 0) + U(ip, j, 0)) * fkl;
-    R vg13 = R(g.f2fzi[k]) * (up - um);
-    R vp = R(g.c2cxi[ip]) * R(0.25) * (R(f2fx[ip]) * (V(i, j, k) + V(i, jp, k)) + R(f2fx[i]) * (V(ip, j, k) + V(ip, jp, k))) * (R(1.0) - fiu)
+    R vg13 = R(M.f2fzi[k]) * (up - um);
+    R vp = R(M.c2cxi[ip]) * R(0.25) * (R(f2fx[ip]) * (V(i, j, k) + V(i, jp, k)) + R(f2fx[i]) * (V(ip, j, k) + V(ip, jp, k))) * (R(1.0) - fiu)
               + R(0.5) * (V(n1, j, k) + V(n1, jp, k)) * fiu;
-    R vm = R(g.c2cxi[i]) * R(0.25) * (R(f2fx[i]) * (V(im, j, k) + V(im, jp, k)) + R(f2fx[im]) * (V(i, j, k) + V(i, jp, k))) * (R(1.0) - fil)
+    R vm = R(M.c2cxi[i]) * R(0.25) * (R(f2fx[i]) * (V(im, j, k) + V(im, jp, k)) + R(f2fx[im]) * (V(i, j, k) + V(i, jp, k))) * (R(1.0) - fil)
               + R(0.5) * (V(0, j, k) + V(0, jp, k)) * fil;
-    R vg21 = R(g.f2fxi[i]) * (vp - vm);
-    R vg22 = R(g.f2fyi[j]) * (V(i, jp, k) - V(i, j, k));
-    vp = R(g.c2czi[kp]) * R(0.25) * (R(f2fz[kp]) * (V(i, j, k) + V(i, jp, k)) + R(f2fz[k]) * (V(i, j, kp) + V(i, jp, kp))) * (R(1.0) - fku)
+    R vg21 = R(M.f2fxi[i]) * (vp - vm);
+    R vg22 = R(M.f2fyi[j]) * (V(i, jp, k) - V(i, j, k));
+    vp = R(M.c2czi[kp]) * R(0.25) * (R(f2fz[kp]) * (V(i, j, k) + V(i, jp, k)) + R(f2fz[k]) * (V(i, j, kp) + V(i, jp, kp))) * (R(1.0) - fku)
        + R(0.5) * (V(i, j, n3) + V(i, jp, n3)) * fku;
-    vm = R(g.c2czi[k]) * R(0.25) * (R(f2fz[k]) * (V(i, j, km) + V(i, jp, km)) + R(f2fz[km]) * (V(i, j, k) + V(i, jp, k))) * (R(1.0) - fkl)
+    vm = R(M.c2czi[k]) * R(0.25) * (R(f2fz[k]) * (V(i, j, km) + V(i, jp, km)) + R(f2fz[km]) * (V(i, j, k) + V(i, jp, k))) * (R(1.0) - fkl)
        + R(0.5) * (V(i, j, 0) + V(i, jp, 0)) * fkl;
-    R vg23 = R(g.f2fzi[k]) * (vp - vm);
-    R wp = R(g.c2cxi[ip]) * R(0.25) * (R(f2fx[ip]) * (W(i, j, k) + W(i, j, kp)) + R(f2fx[i]) * (W(ip, j, k) + W(ip, j, kp))) * (R(1.0) - fiu)
+    R vg23 = R(M.f2fzi[k]) * (vp - vm);
+    R wp = R(M.c2cxi[ip]) * R(0.25) * (R(f2fx[ip]) * (W(i, j, k) + W(i, j, kp)) + R(f2fx[i]) * (W(ip, j, k) + W(ip, j, kp))) * (R(1.0) - fiu)
               + R(0.5) * (W(n1, j, k) + W(n1, j, kp)) * fiu;
-    R wm = R(g.c2cxi[i]) * R(0.25) * (R(f2fx[i]) * (W(im, j, k) + W(im, j, kp)) + R(f2fx[im]) * (W(i, j, k) + W(i, j, kp))) * (R(1.0) - fil)
+    R wm = R(M.c2cxi[i]) * R(0.25) * (R(f2fx[i]) * (W(im, j, k) + W(im, j, kp)) + R(f2fx[im]) * (W(i, j, k) + W(i, j, kp))) * (R(1.0) - fil)
               + R(0.5) * (W(0, j, k) + W(0, j, kp)) * fil;
-    R vg31 = R(g.f2fxi[i]) * (wp - wm);
-    wp = R(g.c2cyi[jp]) * R(0.25) * (R(f2fy[jp]) * (W(i, j, k) + W(i, j, kp)) + R(f2fy[j]) * (W(i, jp, k) + W(i, jp, kp))) * (R(1.0) - fju)
+    R vg31 = R(M.f2fxi[i]) * (wp - wm);
+    wp = R(M.c2cyi[jp]) * R(0.25) * (R(f2fy[jp]) * (W(i, j, k) + W(i, j, kp)) + R(f2fy[j]) * (W(i, jp, k) + W(i, jp, kp))) * (R(1.0) - fju)
        + R(0.5) * (W(i, n2, k) + W(i, n2, kp)) * fju;
-    wm = R(g.c2cyi[j]) * R(0.25) * (R(f2fy[j]) * (W(i, jm, k) + W(i, jm, kp)) + R(f2fy[jm]) * (W(i, j, k) + W(i, j, kp))) * (R(1.0) - fjl)
+    wm = R(M.c2cyi[j]) * R(0.25) * (R(f2fy[j]) * (W(i, jm, k) + W(i, jm, kp)) + R(f2fy[jm]) * (W(i, j, k) + W(i, j, kp))) * (R(1.0) - fjl)
        + R(0.5) * (W(i, 0, k) + W(i, 0, kp)) * fjl;
-    R vg32 = R(g.f2fyi[j]) * (wp - wm);
-    R vg33 = R(g.f2fzi[k]) * (W(i, j, kp) - W(i, j, k));
+    R vg32 = R(M.f2fyi[j]) * (wp - wm);
+    R vg33 = R(M.f2fzi[k]) * (W(i, j, kp) - W(i, j, k));
 #undef U
 #undef V
 #undef W
@@ -73,24 +74,25 @@ __device__ void velgrad(const KP &p, int i, int j, int k, R a[9], R sr[6]) {
 // temgrad, sgs.f90:1480-1525
 template <class R>
 __device__ void temgrad(const KP &p, int i, int j, int k, R a[3]) {
+    const Mir<R> &M = mir<R>(p);
     const DGrid &g = p.g;
-    const double *t = p.f.t;
+    const R *t = M.t;
     int kp = g.kpv[k], km = g.kmv[k], jp = g.jpv[j], jm = g.jmv[j], ip = g.ipv[i], im = g.imv[i];
     R fiu = fixd(g.fixiu[i]), fil = fixd(g.fixil[i]), fju = fixd(g.fixju[j]), fjl = fixd(g.fixjl[j]);
     R fku = fixd(g.fixku[k]), fkl = fixd(g.fixkl[k]);
     R tc = R(t[g.ix(i, j, k)]);
     R tip = R(t[g.ix(ip, j, k)]), tim = R(t[g.ix(im, j, k)]);
-    R tp = R(0.5) * (R(g.f2fx[i]) * tip + R(g.f2fx[ip]) * tc) * R(g.c2cxi[ip]) * (R(1.0) - fiu) + tip * fiu;
-    R tm = R(0.5) * (R(g.f2fx[im]) * tc + R(g.f2fx[i]) * tim) * R(g.c2cxi[i]) * (R(1.0) - fil) + tim * fil;
-    a[0] = R(g.f2fxi[i]) * (tp - tm);
+    R tp = R(0.5) * (R(M.f2fx[i]) * tip + R(M.f2fx[ip]) * tc) * R(M.c2cxi[ip]) * (R(1.0) - fiu) + tip * fiu;
+    R tm = R(0.5) * (R(M.f2fx[im]) * tc + R(M.f2fx[i]) * tim) * R(M.c2cxi[i]) * (R(1.0) - fil) + tim * fil;
+    a[0] = R(M.f2fxi[i]) * (tp - tm);
     R tjp = R(t[g.ix(i, jp, k)]), tjm = R(t[g.ix(i, jm, k)]);
-    tp = R(0.5) * (R(g.f2fy[j]) * tjp + R(g.f2fy[jp]) * tc) * R(g.c2cyi[jp]) * (R(1.0) - fju) + tjp * fju;
-    tm = R(0.5) * (R(g.f2fy[jm]) * tc + R(g.f2fy[j]) * tjm) * R(g.c2cyi[j]) * (R(1.0) - fjl) + tjm * fjl;
-    a[1] = R(g.f2fyi[j]) * (tp - tm);
+    tp = R(0.5) * (R(M.f2fy[j]) * tjp + R(M.f2fy[jp]) * tc) * R(M.c2cyi[jp]) * (R(1.0) - fju) + tjp * fju;
+    tm = R(0.5) * (R(M.f2fy[jm]) * tc + R(M.f2fy[j]) * tjm) * R(M.c2cyi[j]) * (R(1.0) - fjl) + tjm * fjl;
+    a[1] = R(M.f2fyi[j]) * (tp - tm);
     R tkp = R(t[g.ix(i, j, kp)]), tkm = R(t[g.ix(i, j, km)]);
-    tp = R(0.5) * (R(g.f2fz[k]) * tkp + R(g.f2fz[kp]) * tc) * R(g.c2czi[kp]) * (R(1.0) - fku) + tkp * fku;
-    tm = R(0.5) * (R(g.f2fz[km]) * tc + R(g.f2fz[k]) * tkm) * R(g.c2czi[k]) * (R(1.0) - fkl) + tkm * fkl;
-    a[2] = R(g.f2fzi[k]) * (tp - tm);
+    tp = R(0.5) * (R(M.f2fz[k]) * tkp + R(M.f2fz[kp]) * tc) * R(M.c2czi[kp]) * (R(1.0) - fku) + tkp * fku;
+    tm = R(0.5) * (R(M.f2fz[km]) * tc + R(M.f2fz[k]) * tkm) * R(M.c2czi[k]) * (R(1.0) - fkl) + tkm * fkl;
+    a[2] = R(M.f2fzi[k]) * (tp - tm);
 }
 
 template <class R>
@@ -112,8 +114,8 @@ __device__ __forceinline__ void vreman(const R alp[9], R sdx2, R sdy2, R sdz2, R
 
 // Test-filter width at a cell: the sum of the three test-filter cell widths
 // used in the second Vreman / eddy-diffusivity evaluation (sgs.f90:528-533).
-template <class R>
-__device__ __forceinline__ R tf_width(const double *f2f, const int *fl, const int *fu, int i) {
+template <class R, class T>
+__device__ __forceinline__ R tf_width(const T *f2f, const int *fl, const int *fu, int i) {
     return R(0.5) * R(f2f[i - 1]) * (R(1.0) - fixd(fu[i])) + R(f2f[i]) + R(0.5) * R(f2f[i + 1]) * (R(1.0) - fixd(fl[i]));
 }
 
@@ -129,13 +131,14 @@ __device__ __forceinline__ R *scr(const KP &p, int s) { return reinterpret_cast<
 // pass 1 of sgs_dvmg (:434-491) and the constant model sgs_cvm
 template <class R>
 __global__ void __launch_bounds__(kThreads) k_vreman1(KP p, Box b, int dynamic) {
+    const Mir<R> &M = mir<R>(p);
     const DGrid &g = p.g;
     GRID_LOOP(b) {      // mm[0..5] in scr[3..8], alp[0..8] in scr[9..17]
         int i, j, k;
         b.at(tt, i, j, k);
         R alp[9], str[6], aaa, bbb;
         velgrad<R>(p, i, j, k, alp, str);
-        const R fx = R(g.f2fx[i]), fy = R(g.f2fy[j]), fz = R(g.f2fz[k]);
+        const R fx = R(M.f2fx[i]), fy = R(M.f2fy[j]), fz = R(M.f2fz[k]);
         vreman<R>(alp, fx * fx, fy * fy, fz * fz, aaa, bbb);
         long long q = g.ix(i, j, k);
         if (!dynamic) {
@@ -226,6 +229,7 @@ static void filter_batch(lesgpu_case *c, FiltBatch &F) {
 // scr[24..32]; out: uui[0..2], llij[0..5] in scr[3..11]
 template <class R>
 __global__ void __launch_bounds__(kThreads) k_vreman2(KP p, Box b) {
+    const Mir<R> &M = mir<R>(p);
     const DGrid &g = p.g;
     GRID_LOOP(b) {
         int i, j, k;
@@ -236,16 +240,16 @@ __global__ void __launch_bounds__(kThreads) k_vreman2(KP p, Box b) {
         for (int m = 0; m < 9; m++) alp[m] = scr<R>(p, 24 + m)[q];
         str[0] = alp[0]; str[1] = R(0.5) * (alp[3] + alp[1]); str[2] = R(0.5) * (alp[6] + alp[2]);
         str[3] = alp[4]; str[4] = R(0.5) * (alp[7] + alp[5]); str[5] = alp[8];
-        R sx = tf_width<R>(g.f2fx, g.fixil, g.fixiu, i);
-        R sy = tf_width<R>(g.f2fy, g.fixjl, g.fixju, j);
-        R sz = tf_width<R>(g.f2fz, g.fixkl, g.fixku, k);
+        R sx = tf_width<R>(M.f2fx, g.fixil, g.fixiu, i);
+        R sy = tf_width<R>(M.f2fy, g.fixjl, g.fixju, j);
+        R sz = tf_width<R>(M.f2fz, g.fixkl, g.fixku, k);
         vreman<R>(alp, sx * sx, sy * sy, sz * sz, aaa, bbb);
         R ami = (aaa == R(0.0)) ? R(0.0) : sqrt(bbb / aaa);
 #pragma unroll
         for (int m = 0; m < 6; m++) scr<R>(p, 18 + m)[q] = ami * str[m] - scr<R>(p, 18 + m)[q];
-        R u1 = R(0.5) * (R(p.f.u[q]) + R(p.f.u[q + 1]));
-        R u2 = R(0.5) * (R(p.f.v[q]) + R(p.f.v[q + g.sx]));
-        R u3 = R(0.5) * (R(p.f.w[q]) + R(p.f.w[q + g.sxy]));
+        R u1 = R(0.5) * (R(M.u[q]) + R(M.u[q + 1]));
+        R u2 = R(0.5) * (R(M.v[q]) + R(M.v[q + g.sx]));
+        R u3 = R(0.5) * (R(M.w[q]) + R(M.w[q + g.sxy]));
         scr<R>(p, 3)[q] = u1; scr<R>(p, 4)[q] = u2; scr<R>(p, 5)[q] = u3;
         scr<R>(p, 6)[q] = u1 * u1; scr<R>(p, 7)[q] = u1 * u2; scr<R>(p, 8)[q] = u1 * u3;
         scr<R>(p, 9)[q] = u2 * u2; scr<R>(p, 10)[q] = u2 * u3; scr<R>(p, 11)[q] = u3 * u3;
@@ -257,9 +261,10 @@ __global__ void __launch_bounds__(kThreads) k_vreman2(KP p, Box b) {
 template <class R>
 struct LmMmTerm {
     __device__ void operator()(const KP &p, int i, int j, int k, double *w) const {
+        const Mir<R> &M = mir<R>(p);
         const DGrid &g = p.g;
         long long q = g.ix(i, j, k);
-        R vol = R(g.f2fx[i]) * R(g.f2fy[j]) * R(g.f2fz[k]);
+        R vol = R(M.f2fx[i]) * R(M.f2fy[j]) * R(M.f2fz[k]);
         R u1 = scr<R>(p, 24)[q], u2 = scr<R>(p, 25)[q], u3 = scr<R>(p, 26)[q];
         R L0 = scr<R>(p, 27)[q] - u1 * u1, L1 = scr<R>(p, 28)[q] - u1 * u2, L2 = scr<R>(p, 29)[q] - u1 * u3;
         R L3 = scr<R>(p, 30)[q] - u2 * u2, L4 = scr<R>(p, 31)[q] - u2 * u3, L5 = scr<R>(p, 32)[q] - u3 * u3;
@@ -487,13 +492,14 @@ void launch_sgs_post(lesgpu_case *c) {
 // pass 1 of sgs_edm: mm[0..2] scr[3..5]; s[0..5] scr[6..11]; tgrad[0..2] scr[12..14]
 template <class R>
 __global__ void __launch_bounds__(kThreads) k_edm1(KP p, Box b, int dynamic) {
+    const Mir<R> &M = mir<R>(p);
     const DGrid &g = p.g;
     GRID_LOOP(b) {
         int i, j, k;
         b.at(tt, i, j, k);
         R d[9], s[6], alp[3];
         velgrad<R>(p, i, j, k, d, s);
-        R del = pow(R(g.f2fx[i]) * R(g.f2fy[j]) * R(g.f2fz[k]), R(1.0) / R(3.0));
+        R del = pow(R(M.f2fx[i]) * R(M.f2fy[j]) * R(M.f2fz[k]), R(1.0) / R(3.0));
         R sss = s[0] * s[0] + R(2.0) * s[1] * s[1] + R(2.0) * s[2] * s[2] + s[3] * s[3] + R(2.0) * s[4] * s[4] + s[5] * s[5];
         if (sss < R(1.0e-16)) sss = R(1.0e-16);
         long long q = g.ix(i, j, k);
@@ -518,14 +524,15 @@ __global__ void __launch_bounds__(kThreads) k_edm1(KP p, Box b, int dynamic) {
 // llij[0..2] scr[7..9]
 template <class R>
 __global__ void __launch_bounds__(kThreads) k_edm2(KP p, Box b) {
+    const Mir<R> &M = mir<R>(p);
     const DGrid &g = p.g;
     GRID_LOOP(b) {
         int i, j, k;
         b.at(tt, i, j, k);
         long long q = g.ix(i, j, k);
-        R d1 = tf_width<R>(g.f2fx, g.fixil, g.fixiu, i);
-        R d2 = tf_width<R>(g.f2fy, g.fixjl, g.fixju, j);
-        R d3 = tf_width<R>(g.f2fz, g.fixkl, g.fixku, k);
+        R d1 = tf_width<R>(M.f2fx, g.fixil, g.fixiu, i);
+        R d2 = tf_width<R>(M.f2fy, g.fixjl, g.fixju, j);
+        R d3 = tf_width<R>(M.f2fz, g.fixkl, g.fixku, k);
         R del = pow(d1 * d2 * d3, R(1.0) / R(3.0));
         R s0 = scr<R>(p, 21)[q], s1 = scr<R>(p, 22)[q], s2 = scr<R>(p, 23)[q];
         R s3 = scr<R>(p, 24)[q], s4 = scr<R>(p, 25)[q], s5 = scr<R>(p, 26)[q];
@@ -534,10 +541,10 @@ __global__ void __launch_bounds__(kThreads) k_edm2(KP p, Box b) {
         R ami = (del * del) * sqrt(R(2.0) * sss);
 #pragma unroll
         for (int m = 0; m < 3; m++) scr<R>(p, 18 + m)[q] = ami * scr<R>(p, 27 + m)[q] - scr<R>(p, 18 + m)[q];
-        R u1 = R(0.5) * (R(p.f.u[q]) + R(p.f.u[q + 1]));
-        R u2 = R(0.5) * (R(p.f.v[q]) + R(p.f.v[q + g.sx]));
-        R u3 = R(0.5) * (R(p.f.w[q]) + R(p.f.w[q + g.sxy]));
-        R tq = R(p.f.t[q]);
+        R u1 = R(0.5) * (R(M.u[q]) + R(M.u[q + 1]));
+        R u2 = R(0.5) * (R(M.v[q]) + R(M.v[q + g.sx]));
+        R u3 = R(0.5) * (R(M.w[q]) + R(M.w[q + g.sxy]));
+        R tq = R(M.t[q]);
         scr<R>(p, 3)[q] = u1; scr<R>(p, 4)[q] = u2; scr<R>(p, 5)[q] = u3;
         scr<R>(p, 6)[q] = tq;
         scr<R>(p, 7)[q] = u1 * tq; scr<R>(p, 8)[q] = u2 * tq; scr<R>(p, 9)[q] = u3 * tq;
@@ -548,9 +555,10 @@ __global__ void __launch_bounds__(kThreads) k_edm2(KP p, Box b) {
 template <class R>
 struct LmMmTTerm {
     __device__ void operator()(const KP &p, int i, int j, int k, double *w) const {
+        const Mir<R> &M = mir<R>(p);
         const DGrid &g = p.g;
         long long q = g.ix(i, j, k);
-        R vol = R(g.f2fx[i]) * R(g.f2fy[j]) * R(g.f2fz[k]);
+        R vol = R(M.f2fx[i]) * R(M.f2fy[j]) * R(M.f2fz[k]);
         R tf = scr<R>(p, 27)[q];
         R L0 = scr<R>(p, 28)[q] - scr<R>(p, 24)[q] * tf;
         R L1 = scr<R>(p, 29)[q] - scr<R>(p, 25)[q] * tf;

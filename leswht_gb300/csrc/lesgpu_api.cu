@@ -37,8 +37,17 @@ struct Alloc {
     }
 };
 
+// FP32 mirrors of the mixed form: source and destination of every 3-D
+// mirror, in the order of the kMir* bits
+struct MirState {
+    const double *src[20];
+    float *dst[20];
+    int n = 0;
+};
+
 struct CaseExtra {
     Alloc alloc;
+    MirState mir;
 };
 
 double funcbody(const lesgpu_body &b, double x, double y, double z) {
@@ -101,6 +110,53 @@ int check_config(const lesgpu_config *c, const lesgpu_grid *g) {
 int cuda_rc(cudaError_t e) { return e == cudaSuccess ? 0 : LESGPU_ERR_CUDA; }
 
 }  // namespace
+
+// ------------------------------------------------------------- FP32 mirrors
+namespace lg {
+struct MirBatch {
+    const double *src[20];
+    float *dst[20];
+    int n;
+};
+
+// FP64 -> FP32 (round to nearest, as the per-load conversions it replaces)
+__global__ void __launch_bounds__(kThreads) k_mirror(MirBatch b, long long nt) {
+    const long long npair = nt >> 1;
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
+    for (int a = 0; a < b.n; a++) {
+        const double2 *s = reinterpret_cast<const double2 *>(b.src[a]);
+        float2 *d = reinterpret_cast<float2 *>(b.dst[a]);
+        for (long long q = t0; q < npair; q += st) {
+            const double2 x = s[q];
+            d[q] = make_float2((float)x.x, (float)x.y);
+        }
+        if ((nt & 1) && t0 == 0) b.dst[a][nt - 1] = (float)b.src[a][nt - 1];
+    }
+}
+
+void launch_mirror(lesgpu_case *c, unsigned sets) {
+    const MirState &ms = ((CaseExtra *)c->dmem_pool)->mir;
+    if (ms.n == 0) return;                       // FP64 form
+    MirBatch b;
+    b.n = 0;
+    auto take = [&](int first, int count) {
+        for (int q = first; q < first + count; q++) { b.src[b.n] = ms.src[q]; b.dst[b.n] = ms.dst[q]; b.n++; }
+    };
+    if (sets & kMirU) take(0, 1);
+    if (sets & kMirV) take(1, 1);
+    if (sets & kMirW) take(2, 1);
+    if (sets & kMirP) take(3, 1);
+    if (sets & kMirT) take(4, 1);
+    if (sets & kMirNu) take(5, 4);
+    if (sets & kMirAl) take(9, 4);
+    if (sets & kMirConj) take(13, 7);
+    if (b.n == 0) return;
+    const long long nt = c->kp.g.nt;
+    int nb = blocks_for(nt / 2 + 1);
+    if (nb > 4 * 152) nb = 4 * 152;
+    k_mirror<<<nb, kThreads, 0, c->stream>>>(b, nt);
+}
+}  // namespace lg
 
 // ------------------------------------------------------------------ create
 extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, lesgpu_case **out) {
@@ -277,6 +333,51 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
     for (int l = 0; l < 4; l++) f.ibtarg[l] = A.get<double>(1);
     f.inz = A.get<int>(1); f.jnz = A.get<int>(1); f.knz = A.get<int>(1);
 
+    // stencil operand views (Mir<double> aliases the state) and, in the mixed
+    // form, their FP32 mirrors: 1-D tables converted here, 3-D arrays
+    // allocated here and filled by launch_mirror
+    {
+        Mir<double> &m = c->kp.md;
+        m.u = f.u; m.v = f.v; m.w = f.w; m.p = f.p; m.t = f.t;
+        m.nusgs = f.nusgs; m.alsgs = f.alsgs;
+        for (int l = 0; l < 3; l++) { m.nusgs1[l] = f.nusgs1[l]; m.alsgs1[l] = f.alsgs1[l]; }
+        m.cstar = f.cstar;
+        for (int l = 0; l < 6; l++) m.kstar[l] = f.kstar[l];
+        m.f2fx = d.f2fx; m.f2fy = d.f2fy; m.f2fz = d.f2fz; m.f2fxi = d.f2fxi; m.f2fyi = d.f2fyi; m.f2fzi = d.f2fzi;
+        m.c2cxi = d.c2cxi; m.c2cyi = d.c2cyi; m.c2czi = d.c2czi;
+        m.aiu = f.aiu; m.ciu = f.ciu; m.aivw = f.aivw; m.civw = f.civw; m.ajv = f.ajv; m.cjv = f.cjv;
+        m.ajuw = f.ajuw; m.cjuw = f.cjuw; m.akw = f.akw; m.ckw = f.ckw; m.akuv = f.akuv; m.ckuv = f.ckuv;
+        if (cfg->precision == LESGPU_PREC_MIXED) {
+            Mir<float> &r = c->kp.mf;
+            MirState &ms = X->mir;
+            auto add = [&](const double *src, const float *&dst) {
+                float *q = A.get<float>(nt);
+                dst = q;
+                ms.src[ms.n] = src; ms.dst[ms.n] = q; ms.n++;
+            };
+            // order = the kMir* bits: u v w p t | nusgs nusgs1(3) | alsgs alsgs1(3) | cstar kstar(6)
+            add(f.u, r.u); add(f.v, r.v); add(f.w, r.w); add(f.p, r.p); add(f.t, r.t);
+            add(f.nusgs, r.nusgs);
+            for (int l = 0; l < 3; l++) add(f.nusgs1[l], r.nusgs1[l]);
+            add(f.alsgs, r.alsgs);
+            for (int l = 0; l < 3; l++) add(f.alsgs1[l], r.alsgs1[l]);
+            add(f.cstar, r.cstar);
+            for (int l = 0; l < 6; l++) add(f.kstar[l], r.kstar[l]);
+            auto v32 = [&](const double *dev, long long n) -> const float * {
+                std::vector<double> h((size_t)n);
+                cudaMemcpy(h.data(), dev, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost);
+                std::vector<float> hf(h.begin(), h.end());
+                return upload(A, hf.data(), hf.size());
+            };
+            const long long nx = d.n1 + 2, ny = d.n2 + 2, nz = d.n3 + 2;
+            r.f2fx = v32(d.f2fx, nx); r.f2fy = v32(d.f2fy, ny); r.f2fz = v32(d.f2fz, nz);
+            r.f2fxi = v32(d.f2fxi, nx); r.f2fyi = v32(d.f2fyi, ny); r.f2fzi = v32(d.f2fzi, nz);
+            r.c2cxi = v32(d.c2cxi, nx); r.c2cyi = v32(d.c2cyi, ny); r.c2czi = v32(d.c2czi, nz);
+            r.aiu = v32(f.aiu, nx); r.ciu = v32(f.ciu, nx); r.aivw = v32(f.aivw, nx); r.civw = v32(f.civw, nx);
+            r.ajv = v32(f.ajv, ny); r.cjv = v32(f.cjv, ny); r.ajuw = v32(f.ajuw, ny); r.cjuw = v32(f.cjuw, ny);
+            r.akw = v32(f.akw, nz); r.ckw = v32(f.ckw, nz); r.akuv = v32(f.akuv, nz); r.ckuv = v32(f.ckuv, nz);
+        }
+    }
     c->S = A.get<DScal>(1);
     c->kp.S = c->S;
     c->h_f2fx = (double *)calloc(d.n1 + 2, sizeof(double));
@@ -383,6 +484,7 @@ extern "C" int lesgpu_load_ibm(lesgpu_case *c, const lesgpu_ibm *b) {
     if (b->kstar)
         for (int l = 0; l < 6; l++) scatter_d(b->kstar + (size_t)l * ncell, f.kstar[l]);
     if (!A.ok) return LESGPU_ERR_OOM;
+    launch_mirror(c, kMirConj);
     return cuda_rc(cudaDeviceSynchronize());
 }
 
@@ -426,6 +528,7 @@ extern "C" int lesgpu_start(lesgpu_case *c) {
     if (g.ireset == 1) { s.ihist = 0; s.time = 0.0; }
     cudaMemcpyAsync(c->S, &s, sizeof(DScal), cudaMemcpyHostToDevice, c->stream);
     k_start<<<1, 1, 0, c->stream>>>(c->kp);
+    launch_mirror(c, kMirConj | kMirNu | kMirAl);
     if (g.ich != 0) launch_meanpg(c);
     if (g.ihtrans == 1 && g.ich == 1) launch_cvol(c);
     c->ntime_host = 0;
@@ -449,17 +552,21 @@ __global__ void k_retrv_uvw(KP p) {   // retrv_uvw, slv_mmtm.f90:1710-1743
 
 static void enqueue_sgs(lesgpu_case *c, bool first) {
     const lesgpu_config &g = c->cfg;
+    launch_mirror(c, kMirVel | kMirT);
     if (first) launch_sgs_zero_first(c, 0);
     else launch_sgs(c);
     launch_sgs_post(c);
+    launch_mirror(c, kMirNu);
     if (g.ihtrans == 1) {
         if (first) launch_sgs_zero_first(c, 1);
         else launch_sgs_t(c);
         launch_sgs_t_post(c);
+        launch_mirror(c, kMirAl);
     }
 }
 
 static void enqueue_rhsnlhs(lesgpu_case *c, int msub) {
+    launch_mirror(c, kMirVel | kMirP | kMirT);
     launch_rhs(c, msub);
     if (c->cfg.ibmon != 0) launch_rhs_ibm(c);
     launch_convbc(c);
@@ -470,6 +577,7 @@ static void enqueue_rhsnlhs(lesgpu_case *c, int msub) {
 
 static void enqueue_energy(lesgpu_case *c, int msub) {
     const lesgpu_config &g = c->cfg;
+    launch_mirror(c, kMirVel | kMirT);     // the projected velocity
     if (g.ich == 1) launch_tvolcalc(c, 1);
     launch_rhs_t(c, msub);
     if (g.ibmon != 0 && g.iconjg == 0) launch_rhs_ibm_t(c);
@@ -694,6 +802,7 @@ extern "C" int lesgpu_set_array(lesgpu_case *c, int64_t fld, const double *in) {
     if (!c || !in || field_ptrs(c, fld, ptr, &nc)) return LESGPU_ERR_ARG;
     size_t nt = (size_t)c->kp.g.nt;
     for (int l = 0; l < nc; l++) cudaMemcpyAsync(ptr[l], in + l * nt, nt * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    launch_mirror(c, ~0u);
     return cuda_rc(cudaStreamSynchronize(c->stream));
 }
 

@@ -120,12 +120,37 @@ struct DPois {
     MgrdTables *mgrd;         // poiss_mgrd (BiCGSTAB + MG3D)
 };
 
+// The arrays a kernel of arithmetic type T reads in its stencils.  Mir<double>
+// aliases the FP64 state; in the mixed form Mir<float> holds FP32 mirrors
+// (1-D metrics and ADI tables converted once; fields, eddy viscosities and
+// c*/k* refreshed by k_mirror where they change), so an FP32 kernel loads
+// FP32 and converts nothing -- on GB300 an FP64->FP32 conversion issues on the
+// narrow FP64 pipe, and a stencil converting every operand is bound by it.
+template <class T>
+struct Mir {
+    const T *u, *v, *w, *p, *t;
+    const T *nusgs, *nusgs1[3], *alsgs, *alsgs1[3];
+    const T *cstar, *kstar[6];
+    const T *f2fx, *f2fy, *f2fz, *f2fxi, *f2fyi, *f2fzi, *c2cxi, *c2cyi, *c2czi;
+    const T *aiu, *ciu, *aivw, *civw, *ajv, *cjv, *ajuw, *cjuw, *akw, *ckw, *akuv, *ckuv;
+};
+
 struct KP {                   // everything a kernel may read, passed by value
     DGrid g;
     DCfg c;
     DFields f;
     DScal *S;
+    Mir<double> md;
+    Mir<float> mf;            // mixed form only (null otherwise)
 };
+
+template <class R> __device__ __forceinline__ const Mir<R> &mir(const KP &p);
+template <> __device__ __forceinline__ const Mir<double> &mir<double>(const KP &p) { return p.md; }
+template <> __device__ __forceinline__ const Mir<float> &mir<float>(const KP &p) { return p.mf; }
+
+// FP32 mirror refresh sets (k_mirror)
+constexpr unsigned kMirU = 1, kMirV = 2, kMirW = 4, kMirP = 8, kMirT = 16, kMirNu = 32, kMirAl = 64, kMirConj = 128;
+constexpr unsigned kMirVel = kMirU | kMirV | kMirW;
 
 // ------------------------------------------------------------------ helpers
 __device__ __forceinline__ double fixd(int v) { return (double)v; }
@@ -319,6 +344,8 @@ struct GhostSpec {
     int lo0, hi0, lo1, hi1;   // ranges of the two in-plane indices (in index order)
 };
 void ghost(lesgpu_case *c, int dir, GhostSpec *s, int na);
+// refresh FP32 mirrors (mixed form; no-op in the FP64 form)
+void launch_mirror(lesgpu_case *c, unsigned sets);
 void launch_cvol(lesgpu_case *c);
 void launch_rhs_t_kernel(lesgpu_case *c, int msub);
 }  // namespace lg

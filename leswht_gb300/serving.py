@@ -186,26 +186,25 @@ def serve(server: Server, stream: List[Arrival], precision: int = abi.PREC_MIXED
             "mcell_steps_per_s": work / el / 1e6, "records": recs}
 
 
-def one_at_a_time(lib, stream: List[Arrival], precision: int = abi.PREC_FP64) -> dict:
+def one_at_a_time(lib, stream: List[Arrival], precision: int = abi.PREC_FP64, time_scale: float = 1.0) -> dict:
     """The same cases run one after another, each alone on the GPU, with the
-    arrival times honoured (a case waits for its arrival and for the case
-    before it); time-to-solution counts from arrival."""
+    arrival times (divided by `time_scale`) honoured: a case waits for its
+    arrival and for the case before it; time-to-solution counts from arrival."""
     from .solver import Solver
+    built = [(a.t / time_scale, build_case(a.spec, precision), a.spec["nsteps"]) for a in stream]
     t0 = time.perf_counter()
     recs = []
-    clock = 0.0
-    for a in stream:
-        case = build_case(a.spec, precision)
+    for at, case, nsteps in built:
         now = time.perf_counter() - t0
-        start = max(now, a.t)
+        start = max(now, at)
         if start > now:
             time.sleep(start - now)
         s = Solver(lib, "lesgpu_", case)
-        lib.lesgpu_step_async(s.h, a.spec["nsteps"])
+        lib.lesgpu_step_async(s.h, nsteps)
         rep = s.report()          # synchronises
         s.close()
         fin = time.perf_counter() - t0
-        recs.append({"tts_s": fin - a.t, "cells": case.cells, "nsteps": a.spec["nsteps"], "dvmax": rep["dvmax"]})
+        recs.append({"tts_s": fin - at, "cells": case.cells, "nsteps": nsteps, "dvmax": rep["dvmax"]})
     el = time.perf_counter() - t0
     tts = np.array([r["tts_s"] for r in recs])
     work = sum(r["cells"] * r["nsteps"] for r in recs)
