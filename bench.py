@@ -278,7 +278,10 @@ def time_form(args, form, lib, dev, world, rank, flush, full):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         tot_s = float(t.item())
     rep = s.report()
-    out = {"case": case, "value": world * case.cells * args.steps / tot_s / 1e6,
+    import leswht_gb300
+    tuned = [{"dir": "xyz"[d], "components": nc, "fp32": bool(f32), "lanes_per_line": w}
+             for d, nc, f32, w in leswht_gb300.tuning(lib, h)]
+    out = {"case": case, "value": world * case.cells * args.steps / tot_s / 1e6, "autotune": tuned,
            "ms_per_step": tot_s / args.steps * 1e3, "kernels_per_step": int(kps.value),
            "clocks": clk.summary(), "report": rep,
            "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)}}
@@ -448,12 +451,13 @@ def run_ours(args):
                 "clocks": main["clocks"],
                 "check": {"dvmax": rep["dvmax"], "ubulk": rep["ubulk"], "csgsts": rep["csgsts"],
                           "time": rep["time"], "dt": rep["dt"]},
-                "step_ms": main["step_ms"]}
+                "step_ms": main["step_ms"], "autotune": main["autotune"]}
         if args.serving_cases > 0 and world == 1:
             line["serving"] = serving_sample(args, lib)
         if other is not None:
             line["fp64"] = {"value": other["value"], "ms_per_step": other["ms_per_step"],
-                            "kernels_per_step": other["kernels_per_step"], "clocks": other["clocks"]}
+                            "kernels_per_step": other["kernels_per_step"], "clocks": other["clocks"],
+                            "autotune": other["autotune"]}
             line["mixed_vs_fp64"] = main["value"] / other["value"]
             line["gpu_launches"] += other["kernels_per_step"] * args.steps
             line["error"] = form_error(args, args.steps)

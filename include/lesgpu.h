@@ -287,6 +287,16 @@ int lesgpu_use_graph(lesgpu_case *c, int on);
 /* Kernel launches one step makes (counted from the captured step graph). */
 int lesgpu_launch_count(lesgpu_case *c, int64_t *kernels_per_step);
 
+/* The autotuner's choices for this case's shape (no reference counterpart).
+ * At lesgpu_start every feasible lanes-per-line count of each ADI sweep class
+ * (direction, components batched, FP32 or FP64) is timed on the case's own
+ * sweeps and the fastest kept for the process; LESGPU_AUTOTUNE=0 in the
+ * environment turns it off for cases started afterwards (defaults are then
+ * used, and results are reproducible across processes).  Writes up to maxn
+ * tuples (dir 0..2 = x,y,z; components; fp32 0/1; lanes, 1 = one thread per
+ * line) to out as 4 int64 each and their number to *nclasses. */
+int lesgpu_tuning(lesgpu_case *c, int64_t *out, int64_t maxn, int64_t *nclasses);
+
 /* Event instrumentation of one kernel class for roofline measurements:
  * lesgpu_instrument(c, cls) makes the following steps run without the graph
  * and brackets every launch of class `cls` (LESGPU_K_*) with CUDA events on

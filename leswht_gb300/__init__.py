@@ -39,6 +39,8 @@ def load_library(rebuild: bool = False) -> C.CDLL:
     lib.lesgpu_abi_version.restype = C.c_int
     lib.lesgpu_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
     lib.lesgpu_launch_count.restype = C.c_int
+    lib.lesgpu_tuning.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.c_int64, C.POINTER(C.c_int64)]
+    lib.lesgpu_tuning.restype = C.c_int
     lib.lesgpu_instrument.argtypes = [C.c_void_p, C.c_int64]
     lib.lesgpu_instrument.restype = C.c_int
     lib.lesgpu_instrument_read.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
@@ -47,6 +49,15 @@ def load_library(rebuild: bool = False) -> C.CDLL:
     lib.lesgpu_set_device.restype = C.c_int
     _LIB = lib
     return lib
+
+
+def tuning(lib, handle) -> list:
+    """The autotuner's choices for a started case: [(dir, ncomp, fp32, lanes)]."""
+    buf = (C.c_int64 * 256)()
+    n = C.c_int64()
+    if lib.lesgpu_tuning(handle, buf, 64, C.byref(n)) != 0:
+        raise RuntimeError("lesgpu_tuning failed")
+    return [tuple(buf[4 * q:4 * q + 4]) for q in range(min(n.value, 64))]
 
 
 def exec_path(rebuild: bool = False) -> Path:

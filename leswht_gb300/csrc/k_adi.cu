@@ -10,6 +10,10 @@
 // sweep reads once.  z- and y-lines are laid out so that the 32 threads of a
 // warp hold 32 consecutive i: every load and store of a step is one
 // coalesced 256-byte row.
+#include <algorithm>
+#include <map>
+#include <mutex>
+
 #include "lesgpu_internal.cuh"
 
 namespace lg {
@@ -610,48 +614,130 @@ static bool adis_launch(lesgpu_case *c, const AdiBatch &B, int ncomp, long long 
 // (blockIdx.y = component): the u, v and w solves of lhsu/lhsv/lhsw are
 // independent of each other, and three times the lines keep three times as
 // many FP64 pipes busy on small grids.
-static void adi_launch(lesgpu_case *c, const AdiBatch &B, int ncomp) {
-    long long mx = 0;
+//
+// Lanes per line (W) of each sweep class -- 1 = one thread per line
+// (k_adi), else the warp-scan form k_adis -- are picked by an autotuner: at
+// the first start of a case of a given shape every feasible W is timed on the
+// case's own sweeps (results redirected to scratch) and the fastest kept in a
+// process-wide table, so later cases of the shape (the serving loop) reuse it.
+// Mixed form: FP32 arithmetic for the x and z sweeps, the wall-normal
+// (stretched) y sweep stays FP64.
+struct AdiShape {
+    long long mx;
+    int nmax, ncomp;
+    bool f32;
+};
+
+static AdiShape adi_shape(const lesgpu_case *c, const AdiBatch &B, int ncomp) {
+    AdiShape h{0, 0, ncomp, c->cfg.precision == LESGPU_PREC_MIXED && B.a[0].dir != 1};
     for (int q = 0; q < ncomp; q++) {
         const AdiArgs &A = B.a[q];
-        long long nl = (long long)(A.a1 - A.a0 + 1) * (A.b1 - A.b0 + 1);
-        if (nl > mx) mx = nl;
+        h.mx = std::max(h.mx, (long long)(A.a1 - A.a0 + 1) * (A.b1 - A.b0 + 1));
+        h.nmax = std::max(h.nmax, A.l2 - A.l1 + 1);
     }
-    if (mx <= 0) return;
-    dim3 grid((unsigned)((mx + 31) / 32), (unsigned)ncomp);
-    // mixed-precision form: FP32 arithmetic for the x and z sweeps, the
-    // wall-normal (stretched) y sweep stays FP64
-    const bool f32 = c->cfg.precision == LESGPU_PREC_MIXED && B.a[0].dir != 1;
-    int nmax = 0;
-    for (int q = 0; q < ncomp; q++) nmax = max(nmax, B.a[q].l2 - B.a[q].l1 + 1);
-    inst_begin(c, LESGPU_K_ADI);
-    // FP32 sweeps: 32 lanes per line; FP64 sweeps: about 8 rows per lane, since
-    // the scan form costs ~2.5x the FP64 operations of the serial recurrence and
-    // a GB300 SM retires few FP64 FMAs per clock.  Longer lines (more than 12
-    // rows per lane) keep one thread per line.
-    bool done = false;
-    if (f32) {
-        done = adis_launch<float, 32>(c, B, ncomp, mx, nmax);
+    return h;
+}
+
+// launch with W lanes per line; false if W cannot hold the line (MC <= 12)
+static bool adi_run(lesgpu_case *c, const AdiBatch &B, const AdiShape &h, int w) {
+    if (h.mx <= 0) return true;
+    if (w <= 1) {
+        dim3 grid((unsigned)((h.mx + 31) / 32), (unsigned)h.ncomp);
+        if (h.f32) k_adi<float><<<grid, 32, 0, c->stream>>>(c->kp, B);
+        else k_adi<double><<<grid, 32, 0, c->stream>>>(c->kp, B);
+        return true;
+    }
+    if (h.f32) {
+        switch (w) {
+        case 8: return adis_launch<float, 8>(c, B, h.ncomp, h.mx, h.nmax);
+        case 16: return adis_launch<float, 16>(c, B, h.ncomp, h.mx, h.nmax);
+        case 32: return adis_launch<float, 32>(c, B, h.ncomp, h.mx, h.nmax);
+        }
     } else {
-        // lanes per line so that the launch holds ~64k threads: the scan form
-        // pays only while one thread per line leaves the GPU latency bound
-        long long lines = 0;
-        for (int q = 0; q < ncomp; q++)
-            lines += (long long)(B.a[q].a1 - B.a[q].a0 + 1) * (B.a[q].b1 - B.a[q].b0 + 1);
-        int w = 1;
-        while (w < 32 && lines * w < 65536) w <<= 1;
-        if (w == 4) w = 8;
-        if (w >= 8) {
-            done = w == 8 ? adis_launch<double, 8>(c, B, ncomp, mx, nmax)
-                 : w == 16 ? adis_launch<double, 16>(c, B, ncomp, mx, nmax)
-                           : adis_launch<double, 32>(c, B, ncomp, mx, nmax);
+        switch (w) {
+        case 8: return adis_launch<double, 8>(c, B, h.ncomp, h.mx, h.nmax);
+        case 16: return adis_launch<double, 16>(c, B, h.ncomp, h.mx, h.nmax);
+        case 32: return adis_launch<double, 32>(c, B, h.ncomp, h.mx, h.nmax);
         }
     }
-    if (!done) {
-        if (f32) k_adi<float><<<grid, 32, 0, c->stream>>>(c->kp, B);
-        else k_adi<double><<<grid, 32, 0, c->stream>>>(c->kp, B);
+    return false;
+}
+
+struct AdiTuneKey {
+    int n1m, n2m, n3m, dir, ncomp, f32, periodic, nmax;
+    bool operator<(const AdiTuneKey &o) const {
+        const int a[8] = {n1m, n2m, n3m, dir, ncomp, f32, periodic, nmax};
+        const int b[8] = {o.n1m, o.n2m, o.n3m, o.dir, o.ncomp, o.f32, o.periodic, o.nmax};
+        return std::lexicographical_compare(a, a + 8, b, b + 8);
     }
+};
+static std::map<AdiTuneKey, int> g_adi_w;
+static std::mutex g_adi_mu;
+
+static AdiTuneKey adi_key(const lesgpu_case *c, const AdiBatch &B, const AdiShape &h) {
+    const DGrid &g = c->kp.g;
+    return AdiTuneKey{g.n1m, g.n2m, g.n3m, B.a[0].dir, h.ncomp, h.f32 ? 1 : 0, B.a[0].periodic, h.nmax};
+}
+
+// W used until a shape is tuned: the FP32 form 32 lanes; FP64 about 64k threads
+static int adi_default_w(const AdiShape &h) {
+    if (h.f32) return 32;
+    const long long lines = h.mx * h.ncomp;
+    int w = 1;
+    while (w < 32 && lines * w < 65536) w <<= 1;
+    return w < 8 ? 1 : w;
+}
+
+static void adi_launch(lesgpu_case *c, const AdiBatch &B, int ncomp) {
+    const AdiShape h = adi_shape(c, B, ncomp);
+    if (h.mx <= 0) return;
+    int w = adi_default_w(h);
+    if (c->autotune) {
+        std::lock_guard<std::mutex> lk(g_adi_mu);
+        auto it = g_adi_w.find(adi_key(c, B, h));
+        if (it != g_adi_w.end()) w = it->second;
+    }
+    inst_begin(c, LESGPU_K_ADI);
+    if (!adi_run(c, B, h, w)) adi_run(c, B, h, 1);
     inst_end(c, LESGPU_K_ADI);
+}
+
+// Time every feasible W of one sweep class with its results sent to scratch
+// (z: in place on rhs -> the component's scratch G; x: adds into rhs, whose
+// contents are dead between steps; y already writes G).
+static void adi_tune_batch(lesgpu_case *c, AdiBatch B, int ncomp) {
+    const AdiShape h = adi_shape(c, B, ncomp);
+    if (h.mx <= 0) return;
+    const AdiTuneKey key = adi_key(c, B, h);
+    {
+        std::lock_guard<std::mutex> lk(g_adi_mu);
+        if (g_adi_w.count(key)) return;
+    }
+    DFields &f = c->kp.f;
+    for (int q = 0; q < ncomp; q++) {
+        AdiArgs &A = B.a[q];
+        if (A.dir == 2) A.dst = f.scr[3 * q];
+        else if (A.dir == 0) A.dst = f.rhs1[A.comp];
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int cand[4] = {1, 8, 16, 32};
+    int best = adi_default_w(h);
+    float best_ms = 3.0e38f;
+    for (int q = 0; q < 4; q++) {
+        if (!adi_run(c, B, h, cand[q])) continue;          // warm-up launch (also the feasibility check)
+        cudaEventRecord(e0, c->stream);
+        for (int r = 0; r < 3; r++) adi_run(c, B, h, cand[q]);
+        cudaEventRecord(e1, c->stream);
+        float ms = 0.0f;
+        if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) break;
+        if (ms < best_ms) { best_ms = ms; best = cand[q]; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::lock_guard<std::mutex> lk(g_adi_mu);
+    g_adi_w[key] = best;
 }
 
 // The three sweeps of one component (the structure of lhsu :1044-1148):
@@ -713,6 +799,42 @@ void launch_adi_uvw(lesgpu_case *c) {
 void launch_adi_t(lesgpu_case *c) {
     const int comps[1] = {CT};
     adi_components(c, comps, 1);
+}
+
+// Autotune the sweep classes of this case's shape (momentum and, with heat
+// transfer, temperature); a no-op for shapes already tuned in this process.
+int adi_autotune(lesgpu_case *c) {
+    const DGrid &g = c->kp.g;
+    const int comps3[3] = {CU, CV, CW};
+    const int ct[1] = {CT};
+    const int nm = g.n3m != 1 ? 3 : 2;
+    for (int pass = 0; pass < (c->cfg.ihtrans == 1 ? 2 : 1); pass++) {
+        const int *comps = pass == 0 ? comps3 : ct;
+        const int n = pass == 0 ? nm : 1;
+        for (int dir = 2; dir >= 0; dir--) {
+            AdiBatch B{};
+            int m = 0;
+            for (int q = 0; q < n; q++) {
+                if (dir == 2 && comps[q] != CW && g.n3m == 1) continue;
+                adi_args(c, comps[q], q, dir, B.a[m++]);
+            }
+            if (m) adi_tune_batch(c, B, m);
+        }
+    }
+    return cudaStreamSynchronize(c->stream) == cudaSuccess ? 0 : LESGPU_ERR_CUDA;
+}
+
+// the autotuner's choices, for reports: "dir:ncomp:f32:W" per tuned class of this shape
+int adi_tuned(const lesgpu_case *c, int *out, int maxn) {
+    const DGrid &g = c->kp.g;
+    std::lock_guard<std::mutex> lk(g_adi_mu);
+    int n = 0;
+    for (const auto &kv : g_adi_w) {
+        const AdiTuneKey &k = kv.first;
+        if (k.n1m != g.n1m || k.n2m != g.n2m || k.n3m != g.n3m || n + 4 > maxn) continue;
+        out[n++] = k.dir; out[n++] = k.ncomp; out[n++] = k.f32; out[n++] = kv.second;
+    }
+    return n / 4;
 }
 
 }  // namespace lg

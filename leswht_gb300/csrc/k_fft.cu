@@ -188,7 +188,9 @@ __device__ __forceinline__ void ycoef(const DGrid &g, const double *ak1, const d
            + (g.f2fyi[g.n2m] * g.c2cyi[g.n2m] + akk) * fu);
 }
 
-__global__ void k_ytri(KP p, double2 *ccap, const double *ak1, const double *ak3, double *gam) {
+// Elimination and substitution in one pass (the allocation-free entry point,
+// which keeps no per-case tables).
+__global__ void k_ytri_elim(KP p, double2 *ccap, const double *ak1, const double *ak3, double *gam) {
     const DGrid &g = p.g;
     const int n1m = g.n1m, n2m = g.n2m, n3mh = g.n3mh;
     long long nl = (long long)n1m * n3mh;
@@ -241,6 +243,107 @@ __global__ void k_ytri(KP p, double2 *ccap, const double *ak1, const double *ak3
             double2 ph = make_double2((-ajmref * cm.x + crhsref.x) / ajcref, (-ajmref * cm.y + crhsref.y) / ajcref);
             for (int j = 1; j <= n2m; j++) {
                 double2 v = r[(j - 1) * sj];
+                r[(j - 1) * sj] = make_double2(v.x - ph.x, v.y - ph.y);
+            }
+            r[(n2m - 1) * sj] = make_double2(0.0, 0.0);
+        }
+    }
+}
+
+// The y systems' LU (ctrdiag's forward pivots bet_j and multipliers gam_j)
+// depends only on the grid and the wavenumber pair, so it is computed once per
+// case by k_ytri_lu -- with the same device arithmetic as the reference's
+// per-call elimination -- and every solve only substitutes.  Pivot tables are
+// (i, k, j) with i fastest; yam holds am_j; pinref the (1,1) mode's
+// (ajcref, ajmref) of poiss_ftft.f90:93-112.
+__global__ void k_ytri_lu(KP p, const double *ak1, const double *ak3, double *ybet, double *ygam, double *yam,
+                          double *pinref) {
+    const DGrid &g = p.g;
+    const int n1m = g.n1m, n2m = g.n2m, n3mh = g.n3mh;
+    const long long nl = (long long)n1m * n3mh;
+    const long long sj = nl;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nl; t += (long long)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(t % n1m), k = 1 + (int)(t / n1m);
+        const bool pin = (i == 1 && k == 1);
+        double am, ac, ap;
+        ycoef(g, ak1, ak3, i, k, 1, am, ac, ap);
+        if (t == 0) yam[1] = am;
+        if (pin && n2m == 1) { pinref[0] = ac; pinref[1] = am; ac = 1.0; am = 0.0; ap = 0.0; }
+        double bet = 1.0 / ac;
+        ybet[t] = bet;
+        double cprev = ap;
+        for (int j = 2; j <= n2m; j++) {
+            ycoef(g, ak1, ak3, i, k, j, am, ac, ap);
+            if (t == 0) yam[j] = am;
+            if (pin && j == n2m) { pinref[0] = ac; pinref[1] = am; ac = 1.0; am = 0.0; ap = 0.0; }
+            const double gj = cprev * bet;
+            bet = 1.0 / (ac - am * gj);
+            ybet[t + (j - 1) * sj] = bet;
+            ygam[t + (j - 1) * sj] = gj;
+            cprev = ap;
+        }
+    }
+}
+
+// complex Thomas substitutions along y for every (k, i) pair, the (1,1) mode
+// pinned as poiss_ftft.f90:93-112; operands loaded 8 rows ahead
+__global__ void __launch_bounds__(128) k_ytri(KP p, double2 *ccap, const double *ybet, const double *ygam,
+                                              const double *yam, const double *pinref) {
+    const DGrid &g = p.g;
+    const int n1m = g.n1m, n2m = g.n2m, n3mh = g.n3mh;
+    const long long nl = (long long)n1m * n3mh;
+    const long long sj = nl;
+    constexpr int U = 8;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nl; t += (long long)gridDim.x * blockDim.x) {
+        double2 *r = ccap + t;
+        const bool pin = (t == 0);
+        const double2 crhsref = pin ? r[(n2m - 1) * sj] : make_double2(0.0, 0.0);
+        double2 x = make_double2(0.0, 0.0);
+        for (int j0 = 1; j0 <= n2m; j0 += U) {
+            double2 rv[U];
+            double bv[U], av[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int j = j0 + u;
+                if (j <= n2m) { rv[u] = r[(j - 1) * sj]; bv[u] = ybet[t + (j - 1) * sj]; av[u] = yam[j]; }
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int j = j0 + u;
+                if (j > n2m) break;
+                double2 rj = rv[u];
+                double am = av[u];
+                if (pin && j == n2m) { am = 0.0; rj = make_double2(0.0, 0.0); }
+                if (j == 1) x = make_double2(rj.x * bv[u], rj.y * bv[u]);
+                else x = make_double2((rj.x - am * x.x) * bv[u], (rj.y - am * x.y) * bv[u]);
+                r[(j - 1) * sj] = x;
+            }
+        }
+        double2 xn = x;
+        for (int j0 = n2m - 1; j0 >= 1; j0 -= U) {
+            double2 xv[U];
+            double gv[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int j = j0 - u;
+                if (j >= 1) { xv[u] = r[(j - 1) * sj]; gv[u] = ygam[t + j * sj]; }
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int j = j0 - u;
+                if (j < 1) break;
+                const double2 xj = make_double2(xv[u].x - gv[u] * xn.x, xv[u].y - gv[u] * xn.y);
+                r[(j - 1) * sj] = xj;
+                xn = xj;
+            }
+        }
+        if (pin) {
+            // phref = (-ajmref*crhs(n2m-1,1) + crhsref)/ajcref; shift; crhs(n2m,1) = 0
+            const double ajcref = pinref[0], ajmref = pinref[1];
+            const double2 cm = n2m >= 2 ? r[(n2m - 2) * sj] : make_double2(0.0, 0.0);
+            const double2 ph = make_double2((-ajmref * cm.x + crhsref.x) / ajcref, (-ajmref * cm.y + crhsref.y) / ajcref);
+            for (int j = 1; j <= n2m; j++) {
+                const double2 v = r[(j - 1) * sj];
                 r[(j - 1) * sj] = make_double2(v.x - ph.x, v.y - ph.y);
             }
             r[(n2m - 1) * sj] = make_double2(0.0, 0.0);
@@ -315,6 +418,19 @@ int poisson_init(lesgpu_case *c) {
     free(ak1); free(ak3);
     size_t nspec = (size_t)g.n1m * g.n3mh * g.n2m;
     if (cudaMalloc(&P.ccap, sizeof(double2) * nspec) != cudaSuccess) return LESGPU_ERR_OOM;
+    // LU of the y systems, fixed for the case
+    if (cudaMalloc(&P.ybet, sizeof(double) * nspec) != cudaSuccess ||
+        cudaMalloc(&P.ygam, sizeof(double) * nspec) != cudaSuccess ||
+        cudaMalloc(&P.yam, sizeof(double) * (g.n2m + 2)) != cudaSuccess ||
+        cudaMalloc(&P.pinref, sizeof(double) * 2) != cudaSuccess)
+        return LESGPU_ERR_OOM;
+    cudaMemset(P.ygam, 0, sizeof(double) * nspec);
+    cudaMemset(P.pinref, 0, sizeof(double) * 2);
+    {
+        const long long nl = (long long)g.n1m * g.n3mh;
+        k_ytri_lu<<<blocks_for(nl, 128), 128>>>(c->kp, P.ak1, P.ak3, P.ybet, P.ygam, P.yam, P.pinref);
+        if (cudaDeviceSynchronize() != cudaSuccess) return LESGPU_ERR_CUDA;
+    }
     // the attribute is per function and shared by every case: set it to the
     // largest size lines_per_block() can ask for
     const int kMaxSmem = 200 * 1024;
@@ -330,6 +446,8 @@ void poisson_free(lesgpu_case *c) {
     zft_free(c);
     mgrd_free(c);
     cudaFree(P.ak1); cudaFree(P.ak3); cudaFree(P.ccap);
+    cudaFree(P.ybet); cudaFree(P.ygam); cudaFree(P.yam); cudaFree(P.pinref);
+    P.ybet = P.ygam = P.yam = P.pinref = nullptr;
     cudaFree(P.fx.tw); cudaFree(P.fz.tw);
     P.ak1 = P.ak3 = nullptr; P.ccap = nullptr; P.fx.tw = P.fz.tw = nullptr;
 }
@@ -349,7 +467,7 @@ void launch_poisson(lesgpu_case *c, int msub) {
     k_fft_z_fwd<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
     k_fft_x<<<(nxl + Lx - 1) / Lx, kThreads, smx, c->stream>>>(P.ccap, nxl, px, Lx, 0);
     long long nl = (long long)g.n1m * g.n3mh;
-    k_ytri<<<blocks_for(nl, 128), 128, 0, c->stream>>>(c->kp, P.ccap, P.ak1, P.ak3, c->kp.f.scr[0]);
+    k_ytri<<<blocks_for(nl, 128), 128, 0, c->stream>>>(c->kp, P.ccap, P.ybet, P.ygam, P.yam, P.pinref);
     k_fft_x<<<(nxl + Lx - 1) / Lx, kThreads, smx, c->stream>>>(P.ccap, nxl, px, Lx, 1);
     k_fft_z_inv<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
     inst_end(c, LESGPU_K_POISSON);

@@ -15,7 +15,11 @@ struct DevPlan {
 __global__ void k_fft_z_fwd(KP p, double2 *ccap, DevPlan P, int L, long long sk, long long sj);
 __global__ void k_fft_z_inv(KP p, const double2 *ccap, DevPlan P, int L, long long sk, long long sj);
 __global__ void k_fft_x(double2 *ccap, int nlines, DevPlan P, int L, int inv);
-__global__ void k_ytri(KP p, double2 *ccap, const double *ak1, const double *ak3, double *gam);
+__global__ void k_ytri_elim(KP p, double2 *ccap, const double *ak1, const double *ak3, double *gam);
+__global__ void k_ytri_lu(KP p, const double *ak1, const double *ak3, double *ybet, double *ygam, double *yam,
+                          double *pinref);
+__global__ void k_ytri(KP p, double2 *ccap, const double *ybet, const double *ygam, const double *yam,
+                       const double *pinref);
 int fft_lines_per_block(int n);
 int make_plan(FftPlan &p, int n);
 DevPlan devplan(const FftPlan &p);

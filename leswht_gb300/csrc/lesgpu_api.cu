@@ -534,6 +534,15 @@ extern "C" int lesgpu_start(lesgpu_case *c) {
     c->ntime_host = 0;
     c->started = 1;
     if (c->graph_ok) { cudaGraphExecDestroy(c->graph); c->graph_ok = 0; }
+    // autotuner: on unless LESGPU_AUTOTUNE=0 (a tuned choice changes the
+    // rounding of the scan-form sweeps, so runs that must agree bitwise across
+    // processes turn it off)
+    const char *at = getenv("LESGPU_AUTOTUNE");
+    c->autotune = !(at && at[0] == '0');
+    if (c->autotune) {
+        int rc = adi_autotune(c);
+        if (rc) return rc;
+    }
     return cuda_rc(cudaStreamSynchronize(c->stream));
 }
 
@@ -704,6 +713,16 @@ extern "C" int lesgpu_stream(lesgpu_case *c, void **stream) {
 extern "C" int lesgpu_use_graph(lesgpu_case *c, int on) {
     if (!c) return LESGPU_ERR_ARG;
     c->use_graph = on ? 1 : 0;
+    return 0;
+}
+
+extern "C" int lesgpu_tuning(lesgpu_case *c, int64_t *out, int64_t maxn, int64_t *nclasses) {
+    if (!c || !nclasses || maxn < 0 || (maxn > 0 && !out)) return LESGPU_ERR_ARG;
+    int buf[4 * 64];
+    const int n = c->autotune ? adi_tuned(c, buf, 4 * 64) : 0;
+    *nclasses = n;
+    for (int q = 0; q < n && q < maxn; q++)
+        for (int e = 0; e < 4; e++) out[4 * q + e] = buf[4 * q + e];
     return 0;
 }
 

@@ -118,6 +118,7 @@ struct DPois {
     FftPlan fx, fz;
     MgTables *mg;
     MgrdTables *mgrd;         // poiss_mgrd (BiCGSTAB + MG3D)
+    double *ybet, *ygam, *yam, *pinref;   // poiss_ftft: LU of the y systems (k_ytri_lu)
 };
 
 // The arrays a kernel of arithmetic type T reads in its stencils.  Mir<double>
@@ -238,6 +239,7 @@ struct lesgpu_case {
     cudaGraphExec_t graph;     // captured steady-state step
     int graph_ok;
     int use_graph;
+    int autotune;              // use the autotuner's choices (LESGPU_AUTOTUNE != 0 at start)
     // host mirrors of metrics used for init-time tables
     double *h_f2fx, *h_f2fy, *h_f2fz;
     const lesgpu_grid *h_grid;  // the caller's grid, valid only inside lesgpu_create
@@ -346,6 +348,9 @@ struct GhostSpec {
 void ghost(lesgpu_case *c, int dir, GhostSpec *s, int na);
 // refresh FP32 mirrors (mixed form; no-op in the FP64 form)
 void launch_mirror(lesgpu_case *c, unsigned sets);
+// autotuner (k_adi.cu): time the sweep classes of this shape once per process
+int adi_autotune(lesgpu_case *c);
+int adi_tuned(const lesgpu_case *c, int *out, int maxn);
 void launch_cvol(lesgpu_case *c);
 void launch_rhs_t_kernel(lesgpu_case *c, int msub);
 }  // namespace lg

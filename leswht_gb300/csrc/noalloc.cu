@@ -188,7 +188,7 @@ extern "C" int lesgpu_poisson_ftft_noalloc(const lesgpu_grid *g, const double *d
     lg::k_fft_z_fwd<<<gz, lg::kThreads, smz, st>>>(p, ccap, pz, Lz, sk, sj);
     lg::k_fft_x<<<(nxl + Lx - 1) / Lx, lg::kThreads, smx, st>>>(ccap, nxl, px, Lx, 0);
     long long nl = (long long)n1m * n3mh;
-    lg::k_ytri<<<lg::blocks_for(nl, 128), 128, 0, st>>>(p, ccap, dak1, dak3, gam);
+    lg::k_ytri_elim<<<lg::blocks_for(nl, 128), 128, 0, st>>>(p, ccap, dak1, dak3, gam);
     lg::k_fft_x<<<(nxl + Lx - 1) / Lx, lg::kThreads, smx, st>>>(ccap, nxl, px, Lx, 1);
     lg::k_fft_z_inv<<<gz, lg::kThreads, smz, st>>>(p, ccap, pz, Lz, sk, sj);
     return cudaGetLastError() == cudaSuccess ? 0 : LESGPU_ERR_CUDA;

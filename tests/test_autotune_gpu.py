@@ -1,0 +1,49 @@
+"""The autotuner: at lesgpu_start each ADI sweep class of a case's shape is
+timed with every feasible lanes-per-line count and the fastest kept for the
+process; LESGPU_AUTOTUNE=0 turns it off.  Any choice gives the same solution
+to rounding, so tuned runs keep the parity tolerance."""
+import numpy as np
+import pytest
+
+import leswht_gb300
+from leswht_gb300 import abi, cases, solver
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def test_tuned_classes_reported_and_reused(monkeypatch):
+    monkeypatch.setenv("LESGPU_AUTOTUNE", "1")
+    case = cases.channel(32, 32, 16, precision=abi.PREC_MIXED)
+    a = leswht_gb300.gpu_solver(case)
+    ta = leswht_gb300.tuning(a.lib, a.h)
+    dirs = {(d, nc, f32) for d, nc, f32, w in ta}
+    # momentum (3 components) and temperature (1) in x, y, z; x/z in FP32, y in FP64
+    assert {(0, 3, 1), (1, 3, 0), (2, 3, 1), (0, 1, 1), (1, 1, 0), (2, 1, 1)} <= dirs
+    assert all(w in (1, 8, 16, 32) for *_, w in ta)
+    b = leswht_gb300.gpu_solver(case)
+    assert sorted(leswht_gb300.tuning(b.lib, b.h)) == sorted(ta)      # the process-wide table
+    for _ in range(2):
+        a.step(); b.step()
+    fa, fb = a.fields(), b.fields()
+    for k in ("u", "v", "w", "p", "t"):
+        assert np.array_equal(fa[k], fb[k]), k
+
+
+def test_off_reports_nothing(monkeypatch):
+    monkeypatch.setenv("LESGPU_AUTOTUNE", "0")
+    s = leswht_gb300.gpu_solver(cases.channel(16, 16, 8))
+    assert leswht_gb300.tuning(s.lib, s.h) == []
+
+
+def test_tuned_step_matches_oracle(oracle_lib, monkeypatch):
+    monkeypatch.setenv("LESGPU_AUTOTUNE", "1")
+    case = cases.cylinder(64, 48, 8)
+    g, r = leswht_gb300.gpu_solver(case), solver.Solver(oracle_lib, "ref_", case)
+    g.step(); r.step()
+    fg, fr = g.fields(), r.fields()
+    for k in ("u", "v", "w", "p", "t"):
+        assert rel(fg[k], fr[k]) <= 1e-10, k

@@ -52,6 +52,12 @@ def lines(path):
         return f.read().splitlines()
 
 
+@pytest.fixture(autouse=True)
+def _reproducible_across_processes(monkeypatch):
+    # the driver and this process must pick the same ADI lane counts
+    monkeypatch.setenv("LESGPU_AUTOTUNE", "0")
+
+
 def test_exec_channel_fields_history_and_averages(tmp_path):
     c = cases.channel(32, 32, 16)
     c.settings.update(iavg=1, avg_tst=0.0, npriavg=4)
