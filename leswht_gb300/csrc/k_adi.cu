@@ -46,10 +46,9 @@ __device__ __forceinline__ void adi_coef(const KP &p, int comp, int dir, int i, 
     const Mir<R> &M = mir<R>(p);
     const DGrid &g = p.g;
     const DFields &f = p.f;
-    const R re = p.c.re;
     long long q = g.ix(i, j, k);
     if (comp == CT) {
-        const R cre = (double)p.c.iles * re * p.c.pr;
+        const R cre = pickr<R>(p.c.adi_cd[2], p.c.adi_cf[2]);   // iles re pr
         R cs = R(1.0), ks1 = R(1.0), ks2 = R(1.0), omc = R(1.0);
         int ka = dir == 2 ? 5 : dir == 1 ? 3 : 1;
         if (p.c.iconjg == 1) {
@@ -70,7 +69,7 @@ __device__ __forceinline__ void adi_coef(const KP &p, int comp, int dir, int i, 
         }
         return;
     }
-    const R cre = (double)p.c.iles * re, cre2 = R(2.0) * (double)p.c.iles * re;
+    const R cre = pickr<R>(p.c.adi_cd[0], p.c.adi_cf[0]), cre2 = pickr<R>(p.c.adi_cd[1], p.c.adi_cf[1]);
     const R *nu = M.nusgs, *nu1 = M.nusgs1[0], *nu2 = M.nusgs1[1], *nu3 = M.nusgs1[2];
     switch (comp * 3 + dir) {
     case CU * 3 + 2: a = R(M.akuv[k]) * (R(1.0) + cre * R(nu2[q])); c = R(M.ckuv[k]) * (R(1.0) + cre * R(nu2[q + g.sxy])); break;

@@ -286,67 +286,65 @@ __global__ void k_ytri_lu(KP p, const double *ak1, const double *ak3, double *yb
 }
 
 // complex Thomas substitutions along y for every (k, i) pair, the (1,1) mode
-// pinned as poiss_ftft.f90:93-112; operands loaded 8 rows ahead
-__global__ void __launch_bounds__(128) k_ytri(KP p, double2 *ccap, const double *ybet, const double *ygam,
-                                              const double *yam, const double *pinref) {
+// pinned as poiss_ftft.f90:93-112.  The coefficients are real, so the real
+// and imaginary parts are independent recurrences: one thread each (twice
+// the lines in flight); operands are loaded 8 rows ahead.
+__global__ void __launch_bounds__(64) k_ytri(KP p, double2 *ccap, const double *ybet, const double *ygam,
+                                             const double *yam, const double *pinref) {
     const DGrid &g = p.g;
     const int n1m = g.n1m, n2m = g.n2m, n3mh = g.n3mh;
     const long long nl = (long long)n1m * n3mh;
     const long long sj = nl;
     constexpr int U = 8;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nl; t += (long long)gridDim.x * blockDim.x) {
-        double2 *r = ccap + t;
+    for (long long tt = (long long)blockIdx.x * blockDim.x + threadIdx.x; tt < 2 * nl; tt += (long long)gridDim.x * blockDim.x) {
+        const long long t = tt >> 1;
+        const int part = (int)(tt & 1);
+        double *r = reinterpret_cast<double *>(ccap + t) + part;     // element j at r[2 * (j-1) * sj]
+        const long long s2 = 2 * sj;
         const bool pin = (t == 0);
-        const double2 crhsref = pin ? r[(n2m - 1) * sj] : make_double2(0.0, 0.0);
-        double2 x = make_double2(0.0, 0.0);
+        const double crhsref = pin ? r[(n2m - 1) * s2] : 0.0;
+        double x = 0.0;
         for (int j0 = 1; j0 <= n2m; j0 += U) {
-            double2 rv[U];
-            double bv[U], av[U];
+            double rv[U], bv[U], av[U];
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int j = j0 + u;
-                if (j <= n2m) { rv[u] = r[(j - 1) * sj]; bv[u] = ybet[t + (j - 1) * sj]; av[u] = yam[j]; }
+                if (j <= n2m) { rv[u] = r[(j - 1) * s2]; bv[u] = ybet[t + (j - 1) * sj]; av[u] = yam[j]; }
             }
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int j = j0 + u;
                 if (j > n2m) break;
-                double2 rj = rv[u];
-                double am = av[u];
-                if (pin && j == n2m) { am = 0.0; rj = make_double2(0.0, 0.0); }
-                if (j == 1) x = make_double2(rj.x * bv[u], rj.y * bv[u]);
-                else x = make_double2((rj.x - am * x.x) * bv[u], (rj.y - am * x.y) * bv[u]);
-                r[(j - 1) * sj] = x;
+                double rj = rv[u], am = av[u];
+                if (pin && j == n2m) { am = 0.0; rj = 0.0; }
+                x = (j == 1) ? rj * bv[u] : (rj - am * x) * bv[u];
+                r[(j - 1) * s2] = x;
             }
         }
-        double2 xn = x;
+        double xn = x;
         for (int j0 = n2m - 1; j0 >= 1; j0 -= U) {
-            double2 xv[U];
-            double gv[U];
+            double xv[U], gv[U];
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int j = j0 - u;
-                if (j >= 1) { xv[u] = r[(j - 1) * sj]; gv[u] = ygam[t + j * sj]; }
+                if (j >= 1) { xv[u] = r[(j - 1) * s2]; gv[u] = ygam[t + j * sj]; }
             }
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int j = j0 - u;
                 if (j < 1) break;
-                const double2 xj = make_double2(xv[u].x - gv[u] * xn.x, xv[u].y - gv[u] * xn.y);
-                r[(j - 1) * sj] = xj;
+                const double xj = xv[u] - gv[u] * xn;
+                r[(j - 1) * s2] = xj;
                 xn = xj;
             }
         }
         if (pin) {
             // phref = (-ajmref*crhs(n2m-1,1) + crhsref)/ajcref; shift; crhs(n2m,1) = 0
             const double ajcref = pinref[0], ajmref = pinref[1];
-            const double2 cm = n2m >= 2 ? r[(n2m - 2) * sj] : make_double2(0.0, 0.0);
-            const double2 ph = make_double2((-ajmref * cm.x + crhsref.x) / ajcref, (-ajmref * cm.y + crhsref.y) / ajcref);
-            for (int j = 1; j <= n2m; j++) {
-                const double2 v = r[(j - 1) * sj];
-                r[(j - 1) * sj] = make_double2(v.x - ph.x, v.y - ph.y);
-            }
-            r[(n2m - 1) * sj] = make_double2(0.0, 0.0);
+            const double cm = n2m >= 2 ? r[(n2m - 2) * s2] : 0.0;
+            const double ph = (-ajmref * cm + crhsref) / ajcref;
+            for (int j = 1; j <= n2m; j++) r[(j - 1) * s2] = r[(j - 1) * s2] - ph;
+            r[(n2m - 1) * s2] = 0.0;
         }
     }
 }
@@ -467,7 +465,7 @@ void launch_poisson(lesgpu_case *c, int msub) {
     k_fft_z_fwd<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
     k_fft_x<<<(nxl + Lx - 1) / Lx, kThreads, smx, c->stream>>>(P.ccap, nxl, px, Lx, 0);
     long long nl = (long long)g.n1m * g.n3mh;
-    k_ytri<<<blocks_for(nl, 128), 128, 0, c->stream>>>(c->kp, P.ccap, P.ybet, P.ygam, P.yam, P.pinref);
+    k_ytri<<<blocks_for(2 * nl, 64), 64, 0, c->stream>>>(c->kp, P.ccap, P.ybet, P.ygam, P.yam, P.pinref);
     k_fft_x<<<(nxl + Lx - 1) / Lx, kThreads, smx, c->stream>>>(P.ccap, nxl, px, Lx, 1);
     k_fft_z_inv<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
     inst_end(c, LESGPU_K_POISSON);

@@ -22,15 +22,15 @@ __global__ void __launch_bounds__(kThreads) k_rhs(KP p, Box b, R gam, R ro) {
     const R *nu = M.nusgs, *nu1 = M.nusgs1[0], *nu2 = M.nusgs1[1], *nu3 = M.nusgs1[2];
     const R dt = p.S->dt, alpha = p.S->alpha, pmi0 = p.S->pmi[0];
     const R ichfac = c.ich != 0 ? R(1.0) : R(0.0);
-    const R rei = R(1.0) / c.re;
+    const R rei = pickr<R>(c.rei_d, c.rei_f);
     const long long sx = g.sx, sxy = g.sxy;
     long long n = b.count();
     for (long long tt = (long long)blockIdx.x * blockDim.x + threadIdx.x; tt < n; tt += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         b.at(tt, i, j, k);
         long long q = g.ix(i, j, k);
-        const R fju = fixd(g.fixju[j]), fjl = fixd(g.fixjl[j]), fku = fixd(g.fixku[k]), fkl = fixd(g.fixkl[k]);
-        const R fiu = fixd(g.fixiu[i]), fil = fixd(g.fixil[i]);
+        const R fju = R(g.fixju[j]), fjl = R(g.fixjl[j]), fku = R(g.fixku[k]), fkl = R(g.fixkl[k]);
+        const R fiu = R(g.fixiu[i]), fil = R(g.fixil[i]);
         const R f2fxm = R(M.f2fx[i - 1]), f2fx0 = R(M.f2fx[i]), f2fxp = R(M.f2fx[i + 1]);
         const R f2fym = R(M.f2fy[j - 1]), f2fy0 = R(M.f2fy[j]), f2fyp = R(M.f2fy[j + 1]);
         const R f2fzm = R(M.f2fz[k - 1]), f2fz0 = R(M.f2fz[k]), f2fzp = R(M.f2fz[k + 1]);
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(kThreads) k_rhs(KP p, Box b, R gam, R ro) {
                 alx = alx + (R(2.0) * tx + ty + tz);
                 rk3x = rk3x + (a + bb);
             }
-            if (c.ihtrans == 1 && c.grdir == 1) rk3x = rk3x + c.gr / (c.re * c.re) * R(t[q]);
+            if (c.ihtrans == 1 && c.grdir == 1 && c.gterm != 0.0) rk3x = rk3x + c.gterm * R(t[q]);
             p.f.rhs1[0][q] = dt * (gam * rk3x + ro * R(p.f.rk3o[0][q]) + R(2.0) * alpha * alx
                                    - R(2.0) * alpha * (R(pp[q]) - R(pp[q - 1])) * R(M.c2cxi[i])
                                    - R(2.0) * alpha * pmi0 * ichfac);
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(kThreads) k_rhs(KP p, Box b, R gam, R ro) {
                 aly = aly + (tx + R(2.0) * ty + tz);
                 rk3y = rk3y + (a + bb);
             }
-            if (c.ihtrans == 1 && c.grdir == 2) rk3y = rk3y + c.gr / (c.re * c.re) * R(t[q]);
+            if (c.ihtrans == 1 && c.grdir == 2 && c.gterm != 0.0) rk3y = rk3y + c.gterm * R(t[q]);
             p.f.rhs1[1][q] = dt * (gam * rk3y + ro * R(p.f.rk3o[1][q]) + R(2.0) * alpha * aly
                                    - R(2.0) * alpha * (R(pp[q]) - R(pp[q - sx])) * R(M.c2cyi[j]));
             p.f.rk3oo[1][q] = p.f.rk3o[1][q];
@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(kThreads) k_rhs(KP p, Box b, R gam, R ro) {
                 alz = alz + (tx + ty + R(2.0) * tz);
                 rk3z = rk3z + (a + bb);
             }
-            if (c.ihtrans == 1 && c.grdir == 3) rk3z = rk3z + c.gr / (c.re * c.re) * R(t[q]);
+            if (c.ihtrans == 1 && c.grdir == 3 && c.gterm != 0.0) rk3z = rk3z + c.gterm * R(t[q]);
             p.f.rhs1[2][q] = dt * (gam * rk3z + ro * R(p.f.rk3o[2][q]) + R(2.0) * alpha * alz
                                    - R(2.0) * alpha * (R(pp[q]) - R(pp[q - sxy])) * R(M.c2czi[k]));
             p.f.rk3oo[2][q] = p.f.rk3o[2][q];
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(kThreads) k_rhs_t(KP p, Box b, R gam, R ro) {
     const DCfg &c = p.c;
     const R *t = M.t, *u = M.u, *v = M.v, *w = M.w;
     const R dt = p.S->dt, alpha = p.S->alpha, u_bulk = p.S->u_bulk_t;
-    const R inv_repr = R(1.0) / (c.re * c.pr);
+    const R inv_repr = pickr<R>(c.inv_repr_d, c.inv_repr_f);
     long long n = b.count();
     for (long long tt = (long long)blockIdx.x * blockDim.x + threadIdx.x; tt < n; tt += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
@@ -231,8 +231,8 @@ __global__ void __launch_bounds__(kThreads) k_rhs_t(KP p, Box b, R gam, R ro) {
             if (i == g.n1m) ip = g.n1;
             if (i == 1) im = 0;
         }
-        const R fiu = fixd(g.fixiu[i]), fil = fixd(g.fixil[i]), fju = fixd(g.fixju[j]), fjl = fixd(g.fixjl[j]);
-        const R fku = fixd(g.fixku[k]), fkl = fixd(g.fixkl[k]);
+        const R fiu = R(g.fixiu[i]), fil = R(g.fixil[i]), fju = R(g.fixju[j]), fjl = R(g.fixjl[j]);
+        const R fku = R(g.fixku[k]), fkl = R(g.fixkl[k]);
         R tq = R(t[q]);
         long long qip = g.ix(ip, j, k), qim = g.ix(im, j, k), qjp = g.ix(i, jp, k), qjm = g.ix(i, jm, k);
         long long qkp = g.ix(i, j, kp), qkm = g.ix(i, j, km);

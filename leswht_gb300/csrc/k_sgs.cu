@@ -22,8 +22,8 @@ __device__ void velgrad(const KP &p, int i, int j, int k, R a[9], R sr[6]) {
     const R *u = M.u, *v = M.v, *w = M.w;
     int kp = g.kpv[k], km = g.kmv[k], jp = g.jpv[j], jm = g.jmv[j], ip = g.ipv[i], im = g.imv[i];
     int n1 = g.n1, n2 = g.n2, n3 = g.n3;
-    R fju = fixd(g.fixju[j]), fjl = fixd(g.fixjl[j]), fku = fixd(g.fixku[k]), fkl = fixd(g.fixkl[k]);
-    R fiu = fixd(g.fixiu[i]), fil = fixd(g.fixil[i]);
+    R fju = R(g.fixju[j]), fjl = R(g.fixjl[j]), fku = R(g.fixku[k]), fkl = R(g.fixkl[k]);
+    R fiu = R(g.fixiu[i]), fil = R(g.fixil[i]);
     const R *f2fx = M.f2fx, *f2fy = M.f2fy, *f2fz = M.f2fz;
 #define U(a_, b_, c_) R(u[g.ix(a_, b_, c_)])
 #define V(a_, b_, c_) R(v[g.ix(a_, b_, c_)])
@@ -78,8 +78,8 @@ __device__ void temgrad(const KP &p, int i, int j, int k, R a[3]) {
     const DGrid &g = p.g;
     const R *t = M.t;
     int kp = g.kpv[k], km = g.kmv[k], jp = g.jpv[j], jm = g.jmv[j], ip = g.ipv[i], im = g.imv[i];
-    R fiu = fixd(g.fixiu[i]), fil = fixd(g.fixil[i]), fju = fixd(g.fixju[j]), fjl = fixd(g.fixjl[j]);
-    R fku = fixd(g.fixku[k]), fkl = fixd(g.fixkl[k]);
+    R fiu = R(g.fixiu[i]), fil = R(g.fixil[i]), fju = R(g.fixju[j]), fjl = R(g.fixjl[j]);
+    R fku = R(g.fixku[k]), fkl = R(g.fixkl[k]);
     R tc = R(t[g.ix(i, j, k)]);
     R tip = R(t[g.ix(ip, j, k)]), tim = R(t[g.ix(im, j, k)]);
     R tp = R(0.5) * (R(M.f2fx[i]) * tip + R(M.f2fx[ip]) * tc) * R(M.c2cxi[ip]) * (R(1.0) - fiu) + tip * fiu;
@@ -116,7 +116,7 @@ __device__ __forceinline__ void vreman(const R alp[9], R sdx2, R sdy2, R sdz2, R
 // used in the second Vreman / eddy-diffusivity evaluation (sgs.f90:528-533).
 template <class R, class T>
 __device__ __forceinline__ R tf_width(const T *f2f, const int *fl, const int *fu, int i) {
-    return R(0.5) * R(f2f[i - 1]) * (R(1.0) - fixd(fu[i])) + R(f2f[i]) + R(0.5) * R(f2f[i + 1]) * (R(1.0) - fixd(fl[i]));
+    return R(0.5) * R(f2f[i - 1]) * (R(1.0) - R(fu[i])) + R(f2f[i]) + R(0.5) * R(f2f[i + 1]) * (R(1.0) - R(fl[i]));
 }
 
 #define GRID_LOOP(b)                                                                                   \

@@ -205,6 +205,15 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
     k.bc_ybtm = (int)cfg->bc_ybtm; k.bc_ytop = (int)cfg->bc_ytop; k.bc_zbtm = (int)cfg->bc_zbtm; k.bc_ztop = (int)cfg->bc_ztop;
     k.bc_t_ybtm = (int)cfg->bc_t_ybtm; k.bc_t_ytop = (int)cfg->bc_t_ytop; k.bc_t_zbtm = (int)cfg->bc_t_zbtm; k.bc_t_ztop = (int)cfg->bc_t_ztop;
     k.idtopt = (int)cfg->idtopt;
+    {
+        const double re = cfg->re, pr = cfg->pr, iles = (double)cfg->iles;
+        const double re_f = (double)(float)re;
+        k.rei_d = 1.0 / re; k.rei_f = (float)(1.0 / re);
+        k.inv_repr_d = 1.0 / (re * pr); k.inv_repr_f = (float)(1.0 / (re * pr));
+        k.gterm = cfg->gr / (re * re);
+        k.adi_cd[0] = iles * re; k.adi_cd[1] = 2.0 * iles * re; k.adi_cd[2] = iles * re * pr;
+        k.adi_cf[0] = (float)(iles * re_f); k.adi_cf[1] = (float)(2.0 * iles * re_f); k.adi_cf[2] = (float)(iles * re_f * pr);
+    }
 
     size_t nt = (size_t)d.nt;
     DFields &f = c->kp.f;

@@ -46,6 +46,13 @@ struct DCfg {
     int idtopt;
     int nintp[4], nbody[4];
     int nzero;
+    // constants of the R-templated stencils, formed once on the host exactly
+    // as the kernels formed them per cell: [0] in FP64, [1] the FP32 form's
+    // value (FP64 arithmetic on the FP32-rounded re, then rounded)
+    double rei_d, inv_repr_d, gterm;   // 1/re, 1/(re pr), gr/re^2
+    float rei_f, inv_repr_f;
+    double adi_cd[3];                   // ADI: iles re, 2 iles re, iles re pr
+    float adi_cf[3];
 };
 
 // Scalars of mod_common that change during a step.  They live in device
@@ -144,6 +151,10 @@ struct KP {                   // everything a kernel may read, passed by value
     Mir<double> md;
     Mir<float> mf;            // mixed form only (null otherwise)
 };
+
+template <class R> __device__ __forceinline__ R pickr(double d, float f);
+template <> __device__ __forceinline__ double pickr<double>(double d, float) { return d; }
+template <> __device__ __forceinline__ float pickr<float>(double, float f) { return f; }
 
 template <class R> __device__ __forceinline__ const Mir<R> &mir(const KP &p);
 template <> __device__ __forceinline__ const Mir<double> &mir<double>(const KP &p) { return p.md; }
