@@ -292,7 +292,9 @@ int lesgpu_launch_count(lesgpu_case *c, int64_t *kernels_per_step);
  * (direction, components batched, FP32 or FP64) is timed on the case's own
  * sweeps and the fastest kept for the process; LESGPU_AUTOTUNE=0 in the
  * environment turns it off for cases started afterwards (defaults are then
- * used, and results are reproducible across processes).  Writes up to maxn
+ * used, and results are reproducible across processes); LESGPU_TUNE_FILE
+ * names a text file the table is read from before tuning and written back to
+ * after, so several processes share one set of choices.  Writes up to maxn
  * tuples (dir 0..2 = x,y,z; components; fp32 0/1; lanes, 1 = one thread per
  * line) to out as 4 int64 each and their number to *nclasses. */
 int lesgpu_tuning(lesgpu_case *c, int64_t *out, int64_t maxn, int64_t *nclasses);

@@ -11,6 +11,9 @@
 // warp hold 32 consecutive i: every load and store of a step is one
 // coalesced 256-byte row.
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
 #include <map>
 #include <mutex>
 
@@ -800,9 +803,40 @@ void launch_adi_t(lesgpu_case *c) {
     adi_components(c, comps, 1);
 }
 
+// The table can persist in a text file named by LESGPU_TUNE_FILE (one
+// "adi n1m n2m n3m dir ncomp f32 periodic nmax lanes" line per class): read
+// before tuning, rewritten after, so another process -- a profiler run of the
+// same command, the compiled driver -- uses the same choices.
+static void adi_table_load(const char *path) {
+    FILE *f = fopen(path, "r");
+    if (!f) return;
+    char tag[16];
+    AdiTuneKey k;
+    int w;
+    std::lock_guard<std::mutex> lk(g_adi_mu);
+    while (fscanf(f, "%15s %d %d %d %d %d %d %d %d %d", tag, &k.n1m, &k.n2m, &k.n3m, &k.dir, &k.ncomp, &k.f32,
+                  &k.periodic, &k.nmax, &w) == 10)
+        if (!strcmp(tag, "adi") && (w == 1 || w == 8 || w == 16 || w == 32) && !g_adi_w.count(k)) g_adi_w[k] = w;
+    fclose(f);
+}
+
+static void adi_table_save(const char *path) {
+    std::lock_guard<std::mutex> lk(g_adi_mu);
+    FILE *f = fopen(path, "w");
+    if (!f) return;
+    for (const auto &kv : g_adi_w) {
+        const AdiTuneKey &k = kv.first;
+        fprintf(f, "adi %d %d %d %d %d %d %d %d %d\n", k.n1m, k.n2m, k.n3m, k.dir, k.ncomp, k.f32, k.periodic, k.nmax,
+                kv.second);
+    }
+    fclose(f);
+}
+
 // Autotune the sweep classes of this case's shape (momentum and, with heat
 // transfer, temperature); a no-op for shapes already tuned in this process.
 int adi_autotune(lesgpu_case *c) {
+    const char *tf = getenv("LESGPU_TUNE_FILE");
+    if (tf && tf[0]) adi_table_load(tf);
     const DGrid &g = c->kp.g;
     const int comps3[3] = {CU, CV, CW};
     const int ct[1] = {CT};
@@ -820,6 +854,7 @@ int adi_autotune(lesgpu_case *c) {
             if (m) adi_tune_batch(c, B, m);
         }
     }
+    if (tf && tf[0]) adi_table_save(tf);
     return cudaStreamSynchronize(c->stream) == cudaSuccess ? 0 : LESGPU_ERR_CUDA;
 }
 

@@ -303,14 +303,18 @@ __global__ void __launch_bounds__(64) k_ytri(KP p, double2 *ccap, const double *
         const long long s2 = 2 * sj;
         const bool pin = (t == 0);
         const double crhsref = pin ? r[(n2m - 1) * s2] : 0.0;
+        // forward: the next chunk's operands are loaded while one is computed
+        // (two register buffers, alternated by unrolling the chunk loop by two)
         double x = 0.0;
-        for (int j0 = 1; j0 <= n2m; j0 += U) {
-            double rv[U], bv[U], av[U];
+        double rA[U], bA[U], aA[U], rB[U], bB[U], aB[U];
+        auto load_f = [&](double (&rv)[U], double (&bv)[U], double (&av)[U], int j0) {
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int j = j0 + u;
                 if (j <= n2m) { rv[u] = r[(j - 1) * s2]; bv[u] = ybet[t + (j - 1) * sj]; av[u] = yam[j]; }
             }
+        };
+        auto solve_f = [&](const double (&rv)[U], const double (&bv)[U], const double (&av)[U], int j0) {
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int j = j0 + u;
@@ -320,15 +324,27 @@ __global__ void __launch_bounds__(64) k_ytri(KP p, double2 *ccap, const double *
                 x = (j == 1) ? rj * bv[u] : (rj - am * x) * bv[u];
                 r[(j - 1) * s2] = x;
             }
+        };
+        load_f(rA, bA, aA, 1);
+        for (int j0 = 1; j0 <= n2m; j0 += 2 * U) {
+            if (j0 + U <= n2m) load_f(rB, bB, aB, j0 + U);
+            solve_f(rA, bA, aA, j0);
+            if (j0 + U > n2m) break;
+            if (j0 + 2 * U <= n2m) load_f(rA, bA, aA, j0 + 2 * U);
+            solve_f(rB, bB, aB, j0 + U);
         }
+        // backward, pipelined the same way (the rows re-read here were written
+        // above by this thread, so program order makes them visible)
         double xn = x;
-        for (int j0 = n2m - 1; j0 >= 1; j0 -= U) {
-            double xv[U], gv[U];
+        double xA[U], gA[U], xB[U], gB[U];
+        auto load_b = [&](double (&xv)[U], double (&gv)[U], int j0) {
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int j = j0 - u;
                 if (j >= 1) { xv[u] = r[(j - 1) * s2]; gv[u] = ygam[t + j * sj]; }
             }
+        };
+        auto solve_b = [&](const double (&xv)[U], const double (&gv)[U], int j0) {
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int j = j0 - u;
@@ -337,6 +353,14 @@ __global__ void __launch_bounds__(64) k_ytri(KP p, double2 *ccap, const double *
                 r[(j - 1) * s2] = xj;
                 xn = xj;
             }
+        };
+        if (n2m >= 2) load_b(xA, gA, n2m - 1);
+        for (int j0 = n2m - 1; j0 >= 1; j0 -= 2 * U) {
+            if (j0 - U >= 1) load_b(xB, gB, j0 - U);
+            solve_b(xA, gA, j0);
+            if (j0 - U < 1) break;
+            if (j0 - 2 * U >= 1) load_b(xA, gA, j0 - 2 * U);
+            solve_b(xB, gB, j0 - U);
         }
         if (pin) {
             // phref = (-ajmref*crhs(n2m-1,1) + crhsref)/ajcref; shift; crhs(n2m,1) = 0

@@ -167,7 +167,7 @@ __device__ __forceinline__ R filt_x(const KP &p, const R *s, int i, long long qr
     const DGrid &g = p.g;
     // qrow = index of (0, j, k)
     if (!xf) return s[qrow + i];
-    const double *cf = p.f.cfx1 + 3 * i;
+    const R *cf = mir<R>(p).cfx1 + 3 * i;
     const R c0 = R(cf[0]), c1 = R(cf[1]), c2 = R(cf[2]);
     if (i >= 2 && i <= g.n1m - 1)
         return c0 * s[qrow + i - 1] + c1 * s[qrow + i] + c2 * s[qrow + i + 1];
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(kThreads) k_filter(KP p, Box b, FiltBatch F) {
             int km = k - 1, kp = k + 1;
             if (k == 1) km = g.n3m;
             if (k == g.n3m) kp = 1;
-            const double *cf = p.f.cfz1 + 3 * k;
+            const R *cf = mir<R>(p).cfz1 + 3 * k;
             R xm = filt_x<R>(p, s, i, g.ix(0, j, km), xf);
             R x0 = filt_x<R>(p, s, i, g.ix(0, j, k), xf);
             R xp = filt_x<R>(p, s, i, g.ix(0, j, kp), xf);

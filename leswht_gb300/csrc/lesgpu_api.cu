@@ -356,6 +356,7 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
         m.c2cxi = d.c2cxi; m.c2cyi = d.c2cyi; m.c2czi = d.c2czi;
         m.aiu = f.aiu; m.ciu = f.ciu; m.aivw = f.aivw; m.civw = f.civw; m.ajv = f.ajv; m.cjv = f.cjv;
         m.ajuw = f.ajuw; m.cjuw = f.cjuw; m.akw = f.akw; m.ckw = f.ckw; m.akuv = f.akuv; m.ckuv = f.ckuv;
+        m.cfx1 = f.cfx1; m.cfy1 = f.cfy1; m.cfz1 = f.cfz1;
         if (cfg->precision == LESGPU_PREC_MIXED) {
             Mir<float> &r = c->kp.mf;
             MirState &ms = X->mir;
@@ -385,6 +386,7 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
             r.aiu = v32(f.aiu, nx); r.ciu = v32(f.ciu, nx); r.aivw = v32(f.aivw, nx); r.civw = v32(f.civw, nx);
             r.ajv = v32(f.ajv, ny); r.cjv = v32(f.cjv, ny); r.ajuw = v32(f.ajuw, ny); r.cjuw = v32(f.cjuw, ny);
             r.akw = v32(f.akw, nz); r.ckw = v32(f.ckw, nz); r.akuv = v32(f.akuv, nz); r.ckuv = v32(f.ckuv, nz);
+            r.cfx1 = v32(f.cfx1, 3 * (d.n1m + 2)); r.cfy1 = v32(f.cfy1, 3 * (d.n2m + 2)); r.cfz1 = v32(f.cfz1, 3 * (d.n3m + 2));
         }
     }
     c->S = A.get<DScal>(1);

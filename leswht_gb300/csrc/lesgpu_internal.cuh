@@ -141,6 +141,7 @@ struct Mir {
     const T *cstar, *kstar[6];
     const T *f2fx, *f2fy, *f2fz, *f2fxi, *f2fyi, *f2fzi, *c2cxi, *c2cyi, *c2czi;
     const T *aiu, *ciu, *aivw, *civw, *ajv, *cjv, *ajuw, *cjuw, *akw, *ckw, *akuv, *ckuv;
+    const T *cfx1, *cfy1, *cfz1;     // test-filter weights
 };
 
 struct KP {                   // everything a kernel may read, passed by value

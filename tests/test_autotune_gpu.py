@@ -47,3 +47,15 @@ def test_tuned_step_matches_oracle(oracle_lib, monkeypatch):
     fg, fr = g.fields(), r.fields()
     for k in ("u", "v", "w", "p", "t"):
         assert rel(fg[k], fr[k]) <= 1e-10, k
+
+
+def test_table_persists_in_a_file(tmp_path, monkeypatch):
+    path = tmp_path / "tune.txt"
+    monkeypatch.setenv("LESGPU_AUTOTUNE", "1")
+    monkeypatch.setenv("LESGPU_TUNE_FILE", str(path))
+    s = leswht_gb300.gpu_solver(cases.channel(16, 16, 8))
+    lines = [ln.split() for ln in path.read_text().splitlines()]
+    mine = [ln for ln in lines if ln[0] == "adi" and ln[1:4] == ["16", "16", "8"]]
+    assert mine and all(ln[-1] in ("1", "8", "16", "32") for ln in mine)
+    tuned = {(int(ln[4]), int(ln[5]), int(ln[6]), int(ln[-1])) for ln in mine}
+    assert set(leswht_gb300.tuning(s.lib, s.h)) <= tuned
