@@ -392,7 +392,7 @@ def serving_sample(args, lib):
                      "(Poisson arrivals 2/s; grids 64x48x8 .. 256x192x32; circle/square/sphere; Re 40-1000; "
                      "Pr 0.71/7); the benchmark stream has 256 cases x 500 steps"}
     # real-time replay: latency (p50/p99 from arrival) at the stream's rate
-    srv = serving.Server(lib, hbm_budget_bytes=64 << 30, max_active=32, steps_in_flight=4)
+    srv = serving.Server(lib, hbm_budget_bytes=64 << 30, max_active=16, steps_in_flight=4)
     mixed = serving.serve(srv, stream, precision=abi.PREC_MIXED)
     srv.close()
     seq = serving.one_at_a_time(lib, stream, precision=abi.PREC_FP64)
@@ -401,7 +401,7 @@ def serving_sample(args, lib):
                        "throughput_ratio": mixed["mcell_steps_per_s"] / seq["mcell_steps_per_s"]}
     # saturated: every case arrives at once, so aggregate throughput is the
     # GPU's, not the arrival rate's
-    srv = serving.Server(lib, hbm_budget_bytes=64 << 30, max_active=32, steps_in_flight=4)
+    srv = serving.Server(lib, hbm_budget_bytes=64 << 30, max_active=16, steps_in_flight=4)
     mixed = serving.serve(srv, stream, precision=abi.PREC_MIXED, time_scale=1e9)
     srv.close()
     seq = serving.one_at_a_time(lib, stream, precision=abi.PREC_FP64, time_scale=1e9)

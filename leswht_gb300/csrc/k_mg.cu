@@ -32,6 +32,8 @@ constexpr int kMgThreads = 512;
 constexpr int kMC = 8;            // rows per lane: y lines of up to 32 * kMC = 256 cells
 constexpr int kMaxLev = 20;
 
+int mg_cluster_cap();
+
 struct MgTables {
     int n1md, nlev;
     int cs;                     // blocks per cluster (one cluster per z mode)
@@ -633,8 +635,21 @@ int zft_init(lesgpu_case *c) {
         const double cost = waves / cs;
         if (cost < best - 1e-12) { best = cost; T->cs = cs; }
     }
+    // A caller sharing the GPU among many cases caps the cluster size: the
+    // solve is latency-bound, so smaller clusters leave SMs to the other cases'
+    // solves (the serving loop sets a cap on its worker thread; the
+    // LESGPU_MG_CLUSTER_MAX environment variable sets one for every case).
+    int cap = mg_cluster_cap();
+    const char *env = getenv("LESGPU_MG_CLUSTER_MAX");
+    if (env && atoi(env) >= 1) cap = atoi(env);
+    if (cap >= 1)
+        while (T->cs > cap) T->cs >>= 1;
     return 0;
 }
+
+static thread_local int t_mg_cluster_cap = 0;
+int mg_cluster_cap() { return t_mg_cluster_cap; }
+void set_mg_cluster_cap(int cap) { t_mg_cluster_cap = cap; }
 
 void zft_free(lesgpu_case *c) {
     MgTables *T = c->pois.mg;

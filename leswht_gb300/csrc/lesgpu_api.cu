@@ -227,6 +227,7 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
     int nscr = (cfg->iles == 1) ? 33 : 9;   // ADI uses scr[0..8] (three components), SGS scr[3..32]
     for (int s = 0; s < nscr; s++) f.scr[s] = A.get<double>(nt);
     f.part = A.get<double>((size_t)(kRedBlocks + 1) * kMaxRed);
+    f.red_count = A.get<unsigned>(1);
     size_t np = (size_t)(d.n2 + 1) * (d.n3 + 1);
     f.uout = A.get<double>(np); f.vout = A.get<double>(np); f.wout = A.get<double>(np); f.tout = A.get<double>(np);
     f.duout = A.get<double>(np); f.dvout = A.get<double>(np); f.dwout = A.get<double>(np); f.dtout = A.get<double>(np);

@@ -104,6 +104,7 @@ struct DFields {
     // scratch
     double *scr[34];          // SGS temporaries / tridiagonal work, nt each
     double *part;             // reduction partials kRedBlocks * kMaxRed
+    unsigned *red_count;      // blocks of the running reduction that have written their partials
     double *avg;              // field_avg sums: LESGPU_NAVG arrays of nt (IAVG = 1 only)
 };
 
@@ -315,6 +316,52 @@ void launch_field_avg(lesgpu_case *c);
 
 namespace lg {
 // ----------------------------------------------------------- generic sums
+// One-launch reduction: every block writes its partials; the last block to
+// finish (counted with an atomic ticket after a release fence) sums all the
+// partials in block order -- the same fixed order as a separate finalize
+// kernel, so results are deterministic -- applies g and resets the ticket.
+template <int NV, bool MAX, class F, class G>
+__global__ void __launch_bounds__(kThreads) k_reduce_fin(KP p, Box b, F f, G g) {
+    __shared__ int last;
+    double v[NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++) v[q] = MAX ? -1.0e308 : 0.0;
+    const long long n = b.count();
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        b.at(t, i, j, k);
+        double w[NV];
+        f(p, i, j, k, w);
+#pragma unroll
+        for (int q = 0; q < NV; q++) v[q] = MAX ? fmax(v[q], w[q]) : v[q] + w[q];
+    }
+    block_reduce<NV, MAX>(v);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; q++) p.f.part[(size_t)blockIdx.x * kMaxRed + q] = v[q];
+        __threadfence();
+        last = atomicAdd(p.f.red_count, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double acc[NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++) acc[q] = MAX ? -1.0e308 : 0.0;
+    for (int bk = threadIdx.x; bk < (int)gridDim.x; bk += blockDim.x)
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            const double x = __ldcg(p.f.part + (size_t)bk * kMaxRed + q);
+            acc[q] = MAX ? fmax(acc[q], x) : acc[q] + x;
+        }
+    block_reduce<NV, MAX>(acc);
+    if (threadIdx.x == 0) {
+        g(p, acc);
+        *p.f.red_count = 0u;
+    }
+}
+
 template <int NV, bool MAX, class F>
 __global__ void __launch_bounds__(kThreads) k_reduce(KP p, Box b, F f) {
     double v[NV];
@@ -347,8 +394,7 @@ template <int NV, bool MAX, class F, class G>
 inline void reduce(lesgpu_case *c, Box b, F f, G g) {
     int nb = blocks_for(b.count());
     if (nb > kRedBlocks) nb = kRedBlocks;
-    k_reduce<NV, MAX><<<nb, kThreads, 0, c->stream>>>(c->kp, b, f);
-    k_final<NV, MAX><<<1, kThreads, 0, c->stream>>>(c->kp, nb, g);
+    k_reduce_fin<NV, MAX><<<nb, kThreads, 0, c->stream>>>(c->kp, b, f, g);
 }
 
 
@@ -363,6 +409,8 @@ void launch_mirror(lesgpu_case *c, unsigned sets);
 // autotuner (k_adi.cu): time the sweep classes of this shape once per process
 int adi_autotune(lesgpu_case *c);
 int adi_tuned(const lesgpu_case *c, int *out, int maxn);
+// cap on the z_ft multigrid's cluster size for cases created by this thread (0 = none)
+void set_mg_cluster_cap(int cap);
 void launch_cvol(lesgpu_case *c);
 void launch_rhs_t_kernel(lesgpu_case *c, int msub);
 }  // namespace lg
