@@ -20,6 +20,10 @@
 #include "k_fft.cuh"
 #include <math.h>
 #include <stdlib.h>
+#include <array>
+#include <functional>
+#include <map>
+#include <mutex>
 
 namespace lg {
 
@@ -407,6 +411,68 @@ static int lines_per_block(int n) {
 }
 
 int fft_lines_per_block(int n) { return lines_per_block(n); }
+int fft_lz(const lesgpu_case *c) { return c->pois.Lz > 0 ? c->pois.Lz : lines_per_block(c->kp.g.n3m); }
+int fft_lx(const lesgpu_case *c) { return c->pois.Lx > 0 ? c->pois.Lx : lines_per_block(c->kp.g.n1m); }
+
+// ---- autotuner: lines per block of the z (and, for poiss_ftft, x) transforms.
+// More lines per block make longer coalesced rows but take more shared memory
+// (2 n L complex), hence fewer resident blocks; the best L depends on n and
+// on the number of lines, so it is timed per shape (forward transforms on the
+// case's own arrays, whose contents are scratch outside a solve) and cached.
+static std::map<std::array<int, 4>, int> g_fft_l;
+static std::mutex g_fft_mu;
+
+static int fft_time_pick(lesgpu_case *c, std::array<int, 4> key, int n, int dflt,
+                         const std::function<void(int)> &run) {
+    {
+        std::lock_guard<std::mutex> lk(g_fft_mu);
+        auto it = g_fft_l.find(key);
+        if (it != g_fft_l.end()) return it->second;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int best = dflt;
+    float best_ms = 3.0e38f;
+    for (int L = 1; L <= 32; L <<= 1) {
+        if ((size_t)2 * n * L * sizeof(double2) > 200 * 1024) break;
+        run(L);                                  // warm-up
+        cudaEventRecord(e0, c->stream);
+        for (int r = 0; r < 3; r++) run(L);
+        cudaEventRecord(e1, c->stream);
+        float ms = 0.0f;
+        if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) break;
+        if (ms < best_ms) { best_ms = ms; best = L; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::lock_guard<std::mutex> lk(g_fft_mu);
+    g_fft_l[key] = best;
+    return best;
+}
+
+int fft_autotune(lesgpu_case *c) {
+    const DGrid &g = c->kp.g;
+    DPois &P = c->pois;
+    const int pois = (int)c->cfg.poisson;
+    if (pois == LESGPU_POISSON_MGRD || g.n3m <= 1) return 0;
+    const DevPlan pz = devplan(P.fz);
+    const bool ftft = pois == LESGPU_POISSON_FTFT;
+    const long long sk = ftft ? g.n1m : (long long)g.n1m * g.n2m;
+    const long long sj = ftft ? (long long)g.n1m * g.n3mh : g.n1m;
+    P.Lz = fft_time_pick(c, {0, g.n1m, g.n2m, g.n3m}, g.n3m, lines_per_block(g.n3m), [&](int L) {
+        const dim3 gz((g.n1m + L - 1) / L, g.n2m);
+        k_fft_z_fwd<<<gz, kThreads, (size_t)2 * g.n3m * L * sizeof(double2), c->stream>>>(c->kp, P.ccap, pz, L, sk, sj);
+    });
+    if (ftft) {
+        const DevPlan px = devplan(P.fx);
+        const int nxl = g.n3mh * g.n2m;
+        P.Lx = fft_time_pick(c, {1, g.n1m, g.n2m, g.n3m}, g.n1m, lines_per_block(g.n1m), [&](int L) {
+            k_fft_x<<<(nxl + L - 1) / L, kThreads, (size_t)2 * g.n1m * L * sizeof(double2), c->stream>>>(P.ccap, nxl, px, L, 0);
+        });
+    }
+    return cudaStreamSynchronize(c->stream) == cudaSuccess ? 0 : LESGPU_ERR_CUDA;
+}
 
 // poisinit, poiss_ftft.f90:164-204
 int poisson_init(lesgpu_case *c) {
@@ -480,7 +546,7 @@ void launch_poisson(lesgpu_case *c, int msub) {
     if (c->cfg.poisson == LESGPU_POISSON_Z_FT) { launch_zft(c, msub); return; }
     if (c->cfg.poisson == LESGPU_POISSON_MGRD) { launch_mgrd(c, msub); return; }
     DevPlan px = devplan(P.fx), pz = devplan(P.fz);
-    int Lz = lines_per_block(g.n3m), Lx = lines_per_block(g.n1m);
+    const int Lz = fft_lz(c), Lx = fft_lx(c);
     size_t smz = (size_t)2 * g.n3m * Lz * sizeof(double2), smx = (size_t)2 * g.n1m * Lx * sizeof(double2);
     dim3 gz((g.n1m + Lz - 1) / Lz, g.n2m);
     int nxl = g.n3mh * g.n2m;

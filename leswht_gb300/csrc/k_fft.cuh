@@ -21,6 +21,8 @@ __global__ void k_ytri_lu(KP p, const double *ak1, const double *ak3, double *yb
 __global__ void k_ytri(KP p, double2 *ccap, const double *ybet, const double *ygam, const double *yam,
                        const double *pinref);
 int fft_lines_per_block(int n);
+int fft_lz(const lesgpu_case *c);
+int fft_lx(const lesgpu_case *c);
 int make_plan(FftPlan &p, int n);
 DevPlan devplan(const FftPlan &p);
 // poiss_z_ft (k_mg.cu)

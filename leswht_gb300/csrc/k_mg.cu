@@ -670,7 +670,7 @@ void launch_zft(lesgpu_case *c, int msub) {
     const int slot = (msub >= 1 && msub <= 3) ? msub - 1 : 0;
     inst_begin(c, LESGPU_K_POISSON);
     k_zft_begin<<<1, 1, 0, c->stream>>>(c->S, slot, g.n3m, g.n3mh);
-    const int Lz = fft_lines_per_block(g.n3m);
+    const int Lz = fft_lz(c);
     const size_t smz = (size_t)2 * (g.n3m > 1 ? g.n3m : 1) * Lz * sizeof(double2);
     const dim3 gz((g.n1m + Lz - 1) / Lz, g.n2m);
     const long long sk = (long long)g.n1m * g.n2m, sj = g.n1m;

@@ -127,6 +127,7 @@ struct DPois {
     MgTables *mg;
     MgrdTables *mgrd;         // poiss_mgrd (BiCGSTAB + MG3D)
     double *ybet, *ygam, *yam, *pinref;   // poiss_ftft: LU of the y systems (k_ytri_lu)
+    int Lz, Lx;               // FFT lines per block (0 = the shared-memory rule; set by the autotuner)
 };
 
 // The arrays a kernel of arithmetic type T reads in its stencils.  Mir<double>
@@ -408,6 +409,8 @@ void ghost(lesgpu_case *c, int dir, GhostSpec *s, int na);
 void launch_mirror(lesgpu_case *c, unsigned sets);
 // autotuner (k_adi.cu): time the sweep classes of this shape once per process
 int adi_autotune(lesgpu_case *c);
+// autotuner (k_fft.cu): FFT lines per block of the case's Poisson transforms
+int fft_autotune(lesgpu_case *c);
 int adi_tuned(const lesgpu_case *c, int *out, int maxn);
 // cap on the z_ft multigrid's cluster size for cases created by this thread (0 = none)
 void set_mg_cluster_cap(int cap);

@@ -20,12 +20,14 @@ def test_tuned_classes_reported_and_reused(monkeypatch):
     case = cases.channel(32, 32, 16, precision=abi.PREC_MIXED)
     a = leswht_gb300.gpu_solver(case)
     ta = leswht_gb300.tuning(a.lib, a.h)
+    assert any(d == 3 and nc == 2 and w in (1, 2, 4, 8, 16, 32) for d, nc, f32, w in ta)   # z FFT lines per block
+    ta = [t for t in ta if t[0] < 3]
     dirs = {(d, nc, f32) for d, nc, f32, w in ta}
     # momentum (3 components) and temperature (1) in x, y, z; x/z in FP32, y in FP64
     assert {(0, 3, 1), (1, 3, 0), (2, 3, 1), (0, 1, 1), (1, 1, 0), (2, 1, 1)} <= dirs
     assert all(w in (1, 8, 16, 32) for *_, w in ta)
     b = leswht_gb300.gpu_solver(case)
-    assert sorted(leswht_gb300.tuning(b.lib, b.h)) == sorted(ta)      # the process-wide table
+    assert sorted(t for t in leswht_gb300.tuning(b.lib, b.h) if t[0] < 3) == sorted(ta)   # the process-wide table
     for _ in range(2):
         a.step(); b.step()
     fa, fb = a.fields(), b.fields()
@@ -58,4 +60,4 @@ def test_table_persists_in_a_file(tmp_path, monkeypatch):
     mine = [ln for ln in lines if ln[0] == "adi" and ln[1:4] == ["16", "16", "8"]]
     assert mine and all(ln[-1] in ("1", "8", "16", "32") for ln in mine)
     tuned = {(int(ln[4]), int(ln[5]), int(ln[6]), int(ln[-1])) for ln in mine}
-    assert set(leswht_gb300.tuning(s.lib, s.h)) <= tuned
+    assert {t for t in leswht_gb300.tuning(s.lib, s.h) if t[0] < 3} <= tuned
