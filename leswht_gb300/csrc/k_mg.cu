@@ -25,6 +25,9 @@
 #include <stdlib.h>
 #include <string.h>
 #include <vector>
+#include <array>
+#include <map>
+#include <mutex>
 
 namespace lg {
 
@@ -37,6 +40,7 @@ int mg_cluster_cap();
 struct MgTables {
     int n1md, nlev;
     int cs;                     // blocks per cluster (one cluster per z mode)
+    int cap;                    // cap on cs set by the creator (0 = none)
     int iimg[kMaxLev + 1][3];
     double *aw, *ae, *as, *an, *coi1, *coi2, *cor1, *cor2;   // 1-based
     int *ipm, *imm;
@@ -59,6 +63,7 @@ struct MgArgs {
     long long *iters;
     DScal *S;
     int slot;
+    int fixed_cycles;           // > 0: run exactly this many cycles (autotuner timing), no test
 };
 
 // ------------------------------------------------------------- device side
@@ -410,7 +415,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes(MgArgs a) {
     // every block, each warp still touches 32 consecutive points)
     const int gw = (int)(threadIdx.x >> 5) * cs + (int)cl.block_rank();
     Mode m(a, kv, gw * 32 + (int)(threadIdx.x & 31), cs * blockDim.x);
-    const double test = a.S->mg_test;
+    const double test = a.fixed_cycles > 0 ? -1.0 : a.S->mg_test;
     const int it = kv <= a.imgsor ? mg_mg2d(m, test) : mg_gsor2d(m, test);
     // the mode's solution replaces its right-hand side (ccap(i,j,kkk) = cp(i,j))
     double2 *out = a.ccap + (size_t)a.n1m * a.n2m * (kv - 1);
@@ -642,6 +647,7 @@ int zft_init(lesgpu_case *c) {
     int cap = mg_cluster_cap();
     const char *env = getenv("LESGPU_MG_CLUSTER_MAX");
     if (env && atoi(env) >= 1) cap = atoi(env);
+    T->cap = cap;
     if (cap >= 1)
         while (T->cs > cap) T->cs >>= 1;
     return 0;
@@ -661,6 +667,57 @@ void zft_free(lesgpu_case *c) {
     c->pois.mg = nullptr;
 }
 
+static MgArgs zft_args(lesgpu_case *c, int slot, int fixed_cycles) {
+    const DGrid &g = c->kp.g;
+    const lesgpu_config &cf = c->cfg;
+    DPois &P = c->pois;
+    MgTables *T = P.mg;
+    MgArgs a;
+    memset(&a, 0, sizeof(a));
+    a.n1m = g.n1m; a.n2m = g.n2m; a.n1md = T->n1md; a.nlev = T->nlev;
+    a.nbli = (int)cf.nbli; a.mgitr = fixed_cycles > 0 ? fixed_cycles : (int)cf.mgitr;
+    a.imgsor = (int)cf.imgsor; a.wwsor = cf.wwsor;
+    a.ldp = g.n1m + 2; a.ldg = T->n1md + 1;
+    memcpy(a.iimg, T->iimg, sizeof(a.iimg));
+    a.aw = T->aw; a.ae = T->ae; a.as = T->as; a.an = T->an;
+    a.coi1 = T->coi1; a.coi2 = T->coi2; a.cor1 = T->cor1; a.cor2 = T->cor2;
+    a.ipm = T->ipm; a.imm = T->imm; a.ac = T->ac; a.bet = T->bet; a.gam = T->gam;
+    a.ccap = P.ccap; a.pc = T->pc; a.gg = T->gg; a.rs = T->rs;
+    a.pc_plane = T->pc_plane; a.gg_plane = T->gg_plane;
+    a.iters = T->iters; a.S = c->S; a.slot = slot;
+    a.fixed_cycles = fixed_cycles;
+    return a;
+}
+
+static void launch_modes(lesgpu_case *c, const MgArgs &a, int cs, int nmodes = 0) {
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((nmodes > 0 ? nmodes : c->kp.g.n3mh) * cs);
+    lc.blockDim = dim3(kMgThreads);
+    lc.dynamicSmemBytes = 0;
+    lc.stream = c->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    cudaLaunchKernelEx(&lc, k_zft_modes, a);
+}
+
+// can a cluster of cs blocks be scheduled at all
+static bool cluster_fits(lesgpu_case *c, int cs) {
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(c->kp.g.n3mh * cs);
+    lc.blockDim = dim3(kMgThreads);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    int nact = 0;
+    if (cudaOccupancyMaxActiveClusters(&nact, k_zft_modes, &lc) != cudaSuccess) { cudaGetLastError(); return false; }
+    return nact >= 1;
+}
+
 void launch_zft(lesgpu_case *c, int msub) {
     const DGrid &g = c->kp.g;
     const lesgpu_config &cf = c->cfg;
@@ -675,31 +732,53 @@ void launch_zft(lesgpu_case *c, int msub) {
     const dim3 gz((g.n1m + Lz - 1) / Lz, g.n2m);
     const long long sk = (long long)g.n1m * g.n2m, sj = g.n1m;
     k_fft_z_fwd<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
-    MgArgs a;
-    memset(&a, 0, sizeof(a));
-    a.n1m = g.n1m; a.n2m = g.n2m; a.n1md = T->n1md; a.nlev = T->nlev;
-    a.nbli = (int)cf.nbli; a.mgitr = (int)cf.mgitr; a.imgsor = (int)cf.imgsor; a.wwsor = cf.wwsor;
-    a.ldp = g.n1m + 2; a.ldg = T->n1md + 1;
-    memcpy(a.iimg, T->iimg, sizeof(a.iimg));
-    a.aw = T->aw; a.ae = T->ae; a.as = T->as; a.an = T->an;
-    a.coi1 = T->coi1; a.coi2 = T->coi2; a.cor1 = T->cor1; a.cor2 = T->cor2;
-    a.ipm = T->ipm; a.imm = T->imm; a.ac = T->ac; a.bet = T->bet; a.gam = T->gam;
-    a.ccap = P.ccap; a.pc = T->pc; a.gg = T->gg; a.rs = T->rs;
-    a.pc_plane = T->pc_plane; a.gg_plane = T->gg_plane;
-    a.iters = T->iters; a.S = c->S; a.slot = slot;
-    cudaLaunchConfig_t lc = {};
-    lc.gridDim = dim3(g.n3mh * T->cs);
-    lc.blockDim = dim3(kMgThreads);
-    lc.dynamicSmemBytes = 0;
-    lc.stream = c->stream;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = T->cs; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
-    lc.attrs = at;
-    lc.numAttrs = 1;
-    cudaLaunchKernelEx(&lc, k_zft_modes, a);
+    launch_modes(c, zft_args(c, slot, 0), T->cs);
     k_fft_z_inv<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
     inst_end(c, LESGPU_K_POISSON);
 }
+
+// ---- autotuner: cluster size per mode.  A solve lasts as long as its
+// slowest mode -- the zero wavenumber, which needs the most V-cycles while
+// the others finish early -- and its cycle count depends on the data, so the
+// candidates are timed on that mode alone, three V-cycles with the
+// convergence test off (results go to scratch).
+static std::map<std::array<int, 6>, int> g_zft_cs;
+static std::mutex g_zft_mu;
+
+int zft_autotune(lesgpu_case *c) {
+    const DGrid &g = c->kp.g;
+    MgTables *T = c->pois.mg;
+    if (!T || c->cfg.poisson != LESGPU_POISSON_Z_FT) return 0;
+    const std::array<int, 6> key{g.n1m, g.n2m, g.n3m, T->nlev, (int)c->cfg.imgsor, T->cap};
+    {
+        std::lock_guard<std::mutex> lk(g_zft_mu);
+        auto it = g_zft_cs.find(key);
+        if (it != g_zft_cs.end()) { T->cs = it->second; return 0; }
+    }
+    const MgArgs a = zft_args(c, 0, 3);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int best = T->cs;
+    float best_ms = 3.0e38f;
+    for (int cs = 16; cs >= 1; cs >>= 1) {
+        if (T->cap >= 1 && cs > T->cap) continue;
+        if (!cluster_fits(c, cs)) continue;
+        launch_modes(c, a, cs, 1);              // warm-up
+        cudaEventRecord(e0, c->stream);
+        for (int r = 0; r < 2; r++) launch_modes(c, a, cs, 1);
+        cudaEventRecord(e1, c->stream);
+        float ms = 0.0f;
+        if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) break;
+        if (ms < best_ms) { best_ms = ms; best = cs; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    T->cs = best;
+    std::lock_guard<std::mutex> lk(g_zft_mu);
+    g_zft_cs[key] = best;
+    return cudaStreamSynchronize(c->stream) == cudaSuccess ? 0 : LESGPU_ERR_CUDA;
+}
+int zft_cluster(const lesgpu_case *c) { return c->pois.mg ? c->pois.mg->cs : 0; }
 
 }  // namespace lg

@@ -218,23 +218,6 @@ __device__ __forceinline__ void block_reduce(double (&v)[NV]) {
     __syncthreads();
 }
 
-// Sum (or max) the kRedBlocks partials of NV values in a fixed order.
-template <int NV, bool MAX>
-__device__ __forceinline__ void finalize_partials(const double *part, int nblk, double (&out)[NV]) {
-    double v[NV];
-#pragma unroll
-    for (int q = 0; q < NV; q++) v[q] = MAX ? -1.0e308 : 0.0;
-    for (int b = threadIdx.x; b < nblk; b += blockDim.x)
-#pragma unroll
-        for (int q = 0; q < NV; q++) {
-            double x = part[(size_t)b * kMaxRed + q];
-            v[q] = MAX ? fmax(v[q], x) : v[q] + x;
-        }
-    block_reduce<NV, MAX>(v);
-#pragma unroll
-    for (int q = 0; q < NV; q++) out[q] = v[q];
-}
-
 }  // namespace lg
 
 // --------------------------------------------------------------- the case
@@ -363,34 +346,6 @@ __global__ void __launch_bounds__(kThreads) k_reduce_fin(KP p, Box b, F f, G g) 
     }
 }
 
-template <int NV, bool MAX, class F>
-__global__ void __launch_bounds__(kThreads) k_reduce(KP p, Box b, F f) {
-    double v[NV];
-#pragma unroll
-    for (int q = 0; q < NV; q++) v[q] = MAX ? -1.0e308 : 0.0;
-    long long n = b.count();
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
-         t += (long long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        b.at(t, i, j, k);
-        double w[NV];
-        f(p, i, j, k, w);
-#pragma unroll
-        for (int q = 0; q < NV; q++) v[q] = MAX ? fmax(v[q], w[q]) : v[q] + w[q];
-    }
-    block_reduce<NV, MAX>(v);
-    if (threadIdx.x == 0)
-#pragma unroll
-        for (int q = 0; q < NV; q++) p.f.part[(size_t)blockIdx.x * kMaxRed + q] = v[q];
-}
-
-template <int NV, bool MAX, class G>
-__global__ void __launch_bounds__(kThreads) k_final(KP p, int nblk, G g) {
-    double out[NV];
-    finalize_partials<NV, MAX>(p.f.part, nblk, out);
-    if (threadIdx.x == 0) g(p, out);
-}
-
 template <int NV, bool MAX, class F, class G>
 inline void reduce(lesgpu_case *c, Box b, F f, G g) {
     int nb = blocks_for(b.count());
@@ -411,6 +366,9 @@ void launch_mirror(lesgpu_case *c, unsigned sets);
 int adi_autotune(lesgpu_case *c);
 // autotuner (k_fft.cu): FFT lines per block of the case's Poisson transforms
 int fft_autotune(lesgpu_case *c);
+// autotuner (k_mg.cu): cluster size of the z_ft multigrid; the chosen size
+int zft_autotune(lesgpu_case *c);
+int zft_cluster(const lesgpu_case *c);
 int adi_tuned(const lesgpu_case *c, int *out, int maxn);
 // cap on the z_ft multigrid's cluster size for cases created by this thread (0 = none)
 void set_mg_cluster_cap(int cap);

@@ -45,6 +45,8 @@ def test_tuned_step_matches_oracle(oracle_lib, monkeypatch):
     monkeypatch.setenv("LESGPU_AUTOTUNE", "1")
     case = cases.cylinder(64, 48, 8)
     g, r = leswht_gb300.gpu_solver(case), solver.Solver(oracle_lib, "ref_", case)
+    mg = [w for d, nc, f32, w in leswht_gb300.tuning(g.lib, g.h) if d == 4]
+    assert len(mg) == 1 and mg[0] in (1, 2, 4, 8, 16)                   # z_ft multigrid blocks per cluster
     g.step(); r.step()
     fg, fr = g.fields(), r.fields()
     for k in ("u", "v", "w", "p", "t"):
