@@ -269,6 +269,23 @@ int lesgpu_server_stats(lesgpu_server *s, int64_t *pending, int64_t *active, int
                         double *cell_steps);
 int lesgpu_server_destroy(lesgpu_server *s);
 
+/* Immersed-boundary pre-processing on the GPU (the pre-processor's
+ * ibm_body.f90 find_inout :14, findbdy_intp :49, geomfac_preset :126,
+ * geomfac_intp :160, find_zero_nu_sgs :357 as preprocessing.py drives them
+ * and lib_preprocessing.py writes them).  The tables are exactly what the
+ * solver reads back from output/ibmpre: forcing points in the reference's
+ * k, j, i order (interpolated first), geomfac rounded to its '%15.8f' text,
+ * the zero-viscosity list 0-based, the wall mask; c*, k*, omega are left
+ * NULL (= 1, the placeholders).  axes = {xc, xm, yc, ym, zc, zm}: the
+ * coordinate and centre vectors (0:n?) the pre-processor holds in full
+ * precision, n? + 1 values each.  lesgpu_ibmpre_tables fills a lesgpu_ibm
+ * for lesgpu_load_ibm with pointers owned by the handle. */
+typedef struct lesgpu_ibmpre lesgpu_ibmpre;
+int lesgpu_ibmpre_run(const lesgpu_config *cfg, const lesgpu_grid *grid, const double *const axes[6],
+                      lesgpu_ibmpre **out);
+int lesgpu_ibmpre_tables(lesgpu_ibmpre *h, lesgpu_ibm *tables);
+int lesgpu_ibmpre_free(lesgpu_ibmpre *h);
+
 /* Phase-level access for parity tests (not needed by a driver). */
 int lesgpu_get_array(lesgpu_case *c, int64_t field, double *out);
 int lesgpu_set_array(lesgpu_case *c, int64_t field, const double *in);

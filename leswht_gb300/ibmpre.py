@@ -1,4 +1,6 @@
-"""Immersed-boundary pre-processing tables (host side, numpy).
+"""Immersed-boundary pre-processing tables: the host restatement (numpy)
+and, in build_tables_gpu, the same tables from the GPU kernels of
+k_ibmpre.cu (lesgpu_ibmpre_run).
 
 Restates the geometry routines the reference compiles with f2py for its
 pre-processor (02_solver/f90/lib/ibm_body.f90, driven by
@@ -235,3 +237,50 @@ def build_tables(grid, settings, gdat_axes) -> Dict:
     out["kstar"] = np.ones(6 * n)
     out["omega"] = np.ones(n, np.int64)
     return out
+
+
+def build_tables_gpu(lib, settings, grid, gdat_axes) -> Dict:
+    """The same tables as build_tables, computed on the GPU by
+    lesgpu_ibmpre_run (the compute path; build_tables is the host
+    restatement it is tested against)."""
+    import ctypes as C
+    P = C.c_void_p
+    lib.lesgpu_ibmpre_run.argtypes = [C.POINTER(abi.Config), C.POINTER(abi.Grid), C.POINTER(abi.PD), C.POINTER(P)]
+    lib.lesgpu_ibmpre_tables.argtypes = [P, C.POINTER(abi.Ibm)]
+    lib.lesgpu_ibmpre_free.argtypes = [P]
+    for f in ("lesgpu_ibmpre_run", "lesgpu_ibmpre_tables", "lesgpu_ibmpre_free"):
+        getattr(lib, f).restype = C.c_int
+    cfg = abi.pack_config(settings)
+    gr = abi.pack_grid(grid)
+    vecs = [np.ascontiguousarray(v, dtype=np.float64) for ax in ("x", "y", "z") for v in gdat_axes[ax]]
+    arr = (abi.PD * 6)(*[v.ctypes.data_as(abi.PD) for v in vecs])
+    h = P()
+    rc = lib.lesgpu_ibmpre_run(C.byref(cfg), C.byref(gr.struct), arr, C.byref(h))
+    if rc != 0:
+        raise RuntimeError(f"lesgpu_ibmpre_run: {abi.ERR_NAMES.get(rc, rc)}")
+    try:
+        t = abi.Ibm()
+        lib.lesgpu_ibmpre_tables(h, C.byref(t))
+        nl = 4 if settings.get("ihtrans", 0) == 1 else 3
+        out = dict(nintp=[0] * 4, nbody=[0] * 4, fc=[np.zeros((0, 3), np.int64)] * 4,
+                   intpindx=[np.zeros((0, 3), np.int64)] * 4, geomfac=[np.zeros((0, 27))] * 4)
+        for l in range(nl):
+            ni, nb = int(t.nintp[l]), int(t.nbody[l])
+            out["nintp"][l], out["nbody"][l] = ni, nb
+            if nb:
+                out["fc"][l] = np.ctypeslib.as_array(t.fc[l], shape=(nb * 3,)).reshape(nb, 3).copy()
+            if ni:
+                out["intpindx"][l] = np.ctypeslib.as_array(t.intpindx[l], shape=(ni * 3,)).reshape(ni, 3).copy()
+                out["geomfac"][l] = np.ctypeslib.as_array(t.geomfac[l], shape=(ni * 27,)).reshape(ni, 27).copy()
+        nz = int(t.nzero)
+        out["nzero"] = nz
+        for name in ("inz", "jnz", "knz"):
+            out[name] = np.ctypeslib.as_array(getattr(t, name), shape=(nz,)).copy() if nz else np.zeros(0, np.int64)
+        ncell = grid.n1m * grid.n2m * grid.n3m
+        out["nwall_dvm"] = np.ctypeslib.as_array(t.nwall_dvm, shape=(ncell,)).copy()
+        out["cstar"] = np.ones(ncell)
+        out["kstar"] = np.ones(6 * ncell)
+        out["omega"] = np.ones(ncell, np.int64)
+        return out
+    finally:
+        lib.lesgpu_ibmpre_free(h)
