@@ -51,6 +51,7 @@ extern "C" {
 #define LESGPU_POISSON_FTFT  0   /* poiss_ftft.f90  FFT x & z + y Thomas          */
 #define LESGPU_POISSON_Z_FT  1   /* poiss_z_ft.f90  FFT z + 2-D x-semicoarsened MG */
 #define LESGPU_POISSON_MGRD  2   /* poiss_mgrd.f90  BiCGSTAB + MG3D V-cycle        */
+#define LESGPU_POISSON_X_FT  3   /* poiss_x_ft.f90  FFT x + 2-D z-semicoarsened MG */
 
 /* Arithmetic of the step. */
 #define LESGPU_PREC_FP64   0     /* every kernel in FP64 (the plain form)          */

@@ -27,7 +27,7 @@ ERR_NAMES = {0: "OK", -1: "ERR_ARG", -2: "ERR_CONFIG", -3: "ERR_CUDA", -4: "ERR_
              -5: "ERR_NOT_CONVERGED", -6: "ERR_NAN", -7: "ERR_STATE", -8: "ERR_UNSUPPORTED",
              -9: "ERR_TOO_LARGE"}
 
-POISSON_FTFT, POISSON_Z_FT, POISSON_MGRD = 0, 1, 2
+POISSON_FTFT, POISSON_Z_FT, POISSON_MGRD, POISSON_X_FT = 0, 1, 2, 3
 PREC_FP64, PREC_MIXED = 0, 1
 BODY_NONE, BODY_CHANNEL, BODY_CYLINDER, BODY_SPHERE, BODY_SQUARE = 0, 1, 2, 3, 4
 

@@ -132,27 +132,32 @@ def channel(n1m: int = 64, n2m: int = 64, n3m: int = 64,
             lx: float = 4.0 * math.pi, ly: float = 2.0, lz: float = 4.0 * math.pi / 3.0,
             gamma: float = 2.75, re: float = 2800.0, pr: float = 0.71,
             amp: float = 0.1, seed: int = 20261203, precision: int = abi.PREC_FP64,
-            name: Optional[str] = None) -> Case:
+            zwalls: bool = False, name: Optional[str] = None) -> Case:
     """Channel with passive heat transfer (temperature decomposition source).
 
     Re is the bulk Reynolds number on the half height (Re_b = 2800 gives
     Re_tau ~ 180 for the 4pi x 2 x 4pi/3 box); the initial field is the
     laminar profile 1.5(1 - y^2) plus a seeded uniform perturbation of
-    relative amplitude `amp`, mean-corrected plane by plane."""
+    relative amplitude `amp`, mean-corrected plane by plane.  `zwalls`
+    closes z with no-slip adiabatic walls (a duct; ZPRDIC = 0, the z grid
+    clustered at both walls as y is)."""
     s = base_settings()
     s.update(re=re, pr=pr, ich=1, iconjg=1, idecomp=1, ihtrans=1, iles=1, idvmon=1,
-             xprdic=1, zprdic=1, yprdic=0, udrv_i=1.0, cflfac=0.5, idtopt=1, dt_size=0.002,
+             xprdic=1, zprdic=0 if zwalls else 1, yprdic=0, udrv_i=1.0, cflfac=0.5, idtopt=1, dt_size=0.002,
              bc_ybtm=0, bc_ytop=0, bc_t_ybtm=0, bc_t_ytop=0, poisson=abi.POISSON_FTFT,
              precision=precision,
              body=dict(kind=abi.BODY_CHANNEL, cx=0.0, cy=0.0, cz=0.0, r=0.0, p0=1.0e-6))
+    if zwalls:
+        s.update(bc_zbtm=0, bc_ztop=0, bc_t_zbtm=1, bc_t_ztop=1)
     readbcs_overrides(s)
     n1, n2, n3 = n1m + 1, n2m + 1, n3m + 1
+    zseg = (Segment("Z", 0.0, lz, 1, n3, "H", 0.5, gamma) if zwalls else Segment("Z", 0.0, lz, 1, n3, "U"))
     g, gdat, gbin = make_grid(
         n1, n2, n3, lx, ly, lz,
         [Segment("X", 0.0, lx, 1, n1, "U")],
         [Segment("Y", -1.0, 1.0, 1, n2, "H", 0.5, gamma)],
-        [Segment("Z", 0.0, lz, 1, n3, "U")],
-        xprdic=True, zprdic=True)
+        [zseg],
+        xprdic=True, zprdic=not zwalls)
     rng = np.random.Generator(np.random.PCG64(seed))
     sh = g.shape
     u = np.zeros(sh); v = np.zeros(sh); w = np.zeros(sh); p = np.zeros(sh); t = np.zeros(sh)
@@ -171,6 +176,8 @@ def channel(n1m: int = 64, n2m: int = 64, n3m: int = 64,
     w += _plane_mean_correct(pert(), fl, dx * dy, axis=0)
     u *= fl; v *= fv; w *= fl
     u[:, 0, :] = 0.0; u[:, n2, :] = 0.0
+    if zwalls:                                   # w(k = 1) lies on the wall
+        w[1, :, :] = 0.0
     # temperature of the decomposition form: t = u / Pr in the fluid (makefld :529-541)
     t[:] = 0.0
     t[1:n3m + 1, 1:n2m + 1, 1:n1m + 1] = (0.5 * (u[1:n3m + 1, 1:n2m + 1, 1:n1m + 1]

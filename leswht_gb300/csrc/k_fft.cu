@@ -181,6 +181,89 @@ __global__ void k_fft_x(double2 *ccap, int nlines, DevPlan P, int L, int inv) {
     }
 }
 
+// ---- poiss_x_ft transforms (poiss_x_ft.f90:121-150, 182-232) ------------
+// Forward: the real x lines of divgsum -> modes 1..n1mh, stored one z-y plane
+// per mode, (k-1) + n3m*(j-1) + n3m*n2m*(iv-1).  Block = (k-tile of L lines)
+// x j: lines are read along x (contiguous) and written along k.
+__global__ void k_fft_xr_fwd(KP p, double2 *ccap, DevPlan P, int L) {
+    extern __shared__ double2 sm[];
+    const DGrid &g = p.g;
+    const int N = P.n;
+    double2 *b0 = sm, *b1 = sm + (size_t)N * L;
+    const int k0 = 1 + blockIdx.x * L, j = 1 + blockIdx.y;
+    for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
+        const int e = w % N, l = w / N;
+        const int k = k0 + l;
+        const double val = k <= g.n3m ? p.f.divgsum[g.ix(e + 1, j, k)] : 0.0;
+        b0[e * L + l] = make_double2(val, 0.0);
+    }
+    __syncthreads();
+    const double2 *res = block_fft(b0, b1, L, P, 0);
+    const size_t plane = (size_t)g.n3m * g.n2m;
+    for (int w = threadIdx.x; w < g.n1mh * L; w += blockDim.x) {
+        const int l = w % L, iv = w / L;
+        const int k = k0 + l;
+        if (k <= g.n3m) ccap[(k - 1) + (size_t)g.n3m * (j - 1) + plane * iv] = res[iv * L + l];
+    }
+}
+
+// Inverse: conjugate-symmetric completion over the modes, inverse x
+// transform, real part -> phi.  With pin = 1 (ICH = 1) every block also
+// transforms the line (j = n2m, k = 1) as its slot L and subtracts that
+// line's f2fx-weighted mean, phiref = sum_i phi(i,n2m,1) f2fx(i) / xl, from
+// what it stores: the sum is formed in one fixed order, so every block gets
+// the same phiref and the reference's extra pass over phi is not needed.
+__global__ void k_fft_xr_inv(KP p, const double2 *ccap, DevPlan P, int L, int pin) {
+    extern __shared__ double2 sm[];
+    __shared__ double s_ref;
+    const DGrid &g = p.g;
+    const int N = P.n, Ls = L + pin;
+    double2 *b0 = sm, *b1 = sm + (size_t)N * Ls;
+    const int k0 = 1 + blockIdx.x * L, j = 1 + blockIdx.y;
+    const size_t plane = (size_t)g.n3m * g.n2m;
+    for (int w = threadIdx.x; w < N * Ls; w += blockDim.x) {
+        const int l = w % Ls, e = w / Ls;
+        const int k = l < L ? k0 + l : 1, jj = l < L ? j : g.n2m;
+        double2 val = make_double2(0.0, 0.0);
+        if (k <= g.n3m) {
+            const size_t base = (size_t)(k - 1) + (size_t)g.n3m * (jj - 1);
+            if (e < g.n1mh) {
+                val = ccap[base + plane * e];
+            } else {
+                // xxx(i) = conjg(ccap(k,j,n1m+2-i)), poiss_x_ft.f90:192-196
+                const double2 s = ccap[base + plane * (N - e)];
+                val = make_double2(s.x, -s.y);
+            }
+        }
+        b0[e * Ls + l] = val;
+    }
+    __syncthreads();
+    const double2 *res = block_fft(b0, b1, Ls, P, 1);
+    const double dn = 1.0 / (double)N;
+    double phiref = 0.0;
+    if (pin) {
+        if (threadIdx.x < 32) {
+            double acc = 0.0;
+            for (int e = threadIdx.x; e < N; e += 32) acc += __dmul_rn(res[e * Ls + L].x, dn) * g.f2fx[e + 1];
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+            if (threadIdx.x == 0) s_ref = acc / g.xl;
+        }
+        __syncthreads();
+        phiref = s_ref;
+    }
+    for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
+        const int e = w % N, l = w / N;
+        const int k = k0 + l;
+        if (k <= g.n3m) p.f.phi[g.ix(e + 1, j, k)] = __dmul_rn(res[e * Ls + l].x, dn) - phiref;
+    }
+}
+
+// lines per block of k_fft_xr_inv: L, or fewer if the extra line does not fit
+int fft_xr_inv_lines(int n, int L, int pin) {
+    while (L > 1 && (size_t)2 * n * (L + pin) * sizeof(double2) > (size_t)kFftSmemMax) L >>= 1;
+    return L;
+}
+
 // ---- complex Thomas along y, ctrdiag (poiss_ftft.f90:207-244) ------------
 __device__ __forceinline__ void ycoef(const DGrid &g, const double *ak1, const double *ak3, int i, int k, int j,
                                       double &am, double &ac, double &ap) {
@@ -455,7 +538,16 @@ int fft_autotune(lesgpu_case *c) {
     const DGrid &g = c->kp.g;
     DPois &P = c->pois;
     const int pois = (int)c->cfg.poisson;
-    if (pois == LESGPU_POISSON_MGRD || g.n3m <= 1) return 0;
+    if (pois == LESGPU_POISSON_MGRD) return 0;
+    if (pois == LESGPU_POISSON_X_FT) {     // forward x transforms of the real lines
+        const DevPlan px = devplan(P.fx);
+        P.Lx = fft_time_pick(c, {2, g.n1m, g.n2m, g.n3m}, g.n1m, lines_per_block(g.n1m), [&](int L) {
+            k_fft_xr_fwd<<<dim3((g.n3m + L - 1) / L, g.n2m), kThreads, (size_t)2 * g.n1m * L * sizeof(double2),
+                           c->stream>>>(c->kp, P.ccap, px, L);
+        });
+        return cudaStreamSynchronize(c->stream) == cudaSuccess ? 0 : LESGPU_ERR_CUDA;
+    }
+    if (g.n3m <= 1) return 0;
     const DevPlan pz = devplan(P.fz);
     const bool ftft = pois == LESGPU_POISSON_FTFT;
     const long long sk = ftft ? g.n1m : (long long)g.n1m * g.n2m;
@@ -478,7 +570,7 @@ int fft_autotune(lesgpu_case *c) {
 int poisson_init(lesgpu_case *c) {
     const DGrid &g = c->kp.g;
     DPois &P = c->pois;
-    if (c->cfg.poisson == LESGPU_POISSON_Z_FT) return zft_init(c);
+    if (c->cfg.poisson == LESGPU_POISSON_Z_FT || c->cfg.poisson == LESGPU_POISSON_X_FT) return mg2d_init(c);
     if (c->cfg.poisson == LESGPU_POISSON_MGRD) return mgrd_init(c);
     if (c->cfg.poisson != LESGPU_POISSON_FTFT) return LESGPU_ERR_UNSUPPORTED;
     if (c->cfg.xprdic != 1 || c->cfg.zprdic != 1) return LESGPU_ERR_CONFIG;
@@ -521,17 +613,16 @@ int poisson_init(lesgpu_case *c) {
     }
     // the attribute is per function and shared by every case: set it to the
     // largest size lines_per_block() can ask for
-    const int kMaxSmem = 200 * 1024;
-    if (cudaFuncSetAttribute(k_fft_z_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem) != cudaSuccess ||
-        cudaFuncSetAttribute(k_fft_z_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem) != cudaSuccess ||
-        cudaFuncSetAttribute(k_fft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_fft_z_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess ||
+        cudaFuncSetAttribute(k_fft_z_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess ||
+        cudaFuncSetAttribute(k_fft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess)
         return LESGPU_ERR_CUDA;
     return 0;
 }
 
 void poisson_free(lesgpu_case *c) {
     DPois &P = c->pois;
-    zft_free(c);
+    mg2d_free(c);
     mgrd_free(c);
     cudaFree(P.ak1); cudaFree(P.ak3); cudaFree(P.ccap);
     cudaFree(P.ybet); cudaFree(P.ygam); cudaFree(P.yam); cudaFree(P.pinref);
@@ -543,7 +634,7 @@ void poisson_free(lesgpu_case *c) {
 void launch_poisson(lesgpu_case *c, int msub) {
     const DGrid &g = c->kp.g;
     DPois &P = c->pois;
-    if (c->cfg.poisson == LESGPU_POISSON_Z_FT) { launch_zft(c, msub); return; }
+    if (c->cfg.poisson == LESGPU_POISSON_Z_FT || c->cfg.poisson == LESGPU_POISSON_X_FT) { launch_mg2d(c, msub); return; }
     if (c->cfg.poisson == LESGPU_POISSON_MGRD) { launch_mgrd(c, msub); return; }
     DevPlan px = devplan(P.fx), pz = devplan(P.fz);
     const int Lz = fft_lz(c), Lx = fft_lx(c);

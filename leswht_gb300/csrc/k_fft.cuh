@@ -11,10 +11,18 @@ struct DevPlan {
     const double2 *tw;
 };
 
+// dynamic shared memory a transform block may take (below the per-block
+// opt-in limit, with room for the kernels' static shared memory)
+constexpr int kFftSmemMax = 200 * 1024;
+
 // z transforms; the spectrum element (i, k, j) sits at (i-1) + sk*(k-1) + sj*(j-1)
 __global__ void k_fft_z_fwd(KP p, double2 *ccap, DevPlan P, int L, long long sk, long long sj);
 __global__ void k_fft_z_inv(KP p, const double2 *ccap, DevPlan P, int L, long long sk, long long sj);
 __global__ void k_fft_x(double2 *ccap, int nlines, DevPlan P, int L, int inv);
+// poiss_x_ft: real x lines <-> modes 1..n1mh, one z-y plane per mode
+__global__ void k_fft_xr_fwd(KP p, double2 *ccap, DevPlan P, int L);
+__global__ void k_fft_xr_inv(KP p, const double2 *ccap, DevPlan P, int L, int pin);
+int fft_xr_inv_lines(int n, int L, int pin);
 __global__ void k_ytri_elim(KP p, double2 *ccap, const double *ak1, const double *ak3, double *gam);
 __global__ void k_ytri_lu(KP p, const double *ak1, const double *ak3, double *ybet, double *ygam, double *yam,
                           double *pinref);
@@ -25,10 +33,10 @@ int fft_lz(const lesgpu_case *c);
 int fft_lx(const lesgpu_case *c);
 int make_plan(FftPlan &p, int n);
 DevPlan devplan(const FftPlan &p);
-// poiss_z_ft (k_mg.cu)
-int zft_init(lesgpu_case *c);
-void zft_free(lesgpu_case *c);
-void launch_zft(lesgpu_case *c, int msub);
+// poiss_z_ft and poiss_x_ft (k_mg.cu)
+int mg2d_init(lesgpu_case *c);
+void mg2d_free(lesgpu_case *c);
+void launch_mg2d(lesgpu_case *c, int msub);
 // poiss_mgrd (k_mgrd.cu)
 int mgrd_init(lesgpu_case *c);
 void mgrd_free(lesgpu_case *c);

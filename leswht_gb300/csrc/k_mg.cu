@@ -1,9 +1,16 @@
-// Pressure Poisson solve of poiss_z_ft.f90: FFT in z, then for each of the
-// n3mh z modes a complex 2-D problem in x-y solved by the reference's
-// multigrid -- semi-coarsened in x (levels of n1m, n1m/2, ... x-lines),
-// zebra x-line relaxation with y-Thomas solves, linear restriction and the
-// prolongation onto the even lines only -- or, for modes above IMGSOR, by
-// zebra line SOR.
+// Pressure Poisson solves of poiss_z_ft.f90 and poiss_x_ft.f90.  z_ft: FFT
+// in z, then for each of the n3mh z modes a complex 2-D problem in x-y
+// solved by the reference's multigrid -- semi-coarsened in x (levels of n1m,
+// n1m/2, ... x-lines), zebra x-line relaxation with y-Thomas solves, linear
+// restriction and the prolongation onto the even lines only -- or, for modes
+// above IMGSOR, by zebra line SOR.  x_ft is the same with x and z exchanged
+// (FFT in x, n1mh modes, each a z-y problem semi-coarsened in z), except
+// where poiss_x_ft.f90 differs: the zero wavenumber's odd lines are shifted
+// by ggii(1,n2m) before the even lines are formed (toplevel and gsor2d), the
+// prolongation runs over every coarse point with coi2 (the last one's is the
+// periodic weight or zero), the convergence criterion carries 0.9, and phi
+// gets the upper-wall mean removed when ICH = 1.  Below, "line" / i is the
+// semi-coarsened direction (x for z_ft, z for x_ft) and kv the mode.
 //
 // GPU design: one thread block per z mode runs that mode's whole solve
 // (every V-cycle and its convergence test) as one launch; the phases of a
@@ -38,20 +45,22 @@ constexpr int kMaxLev = 20;
 int mg_cluster_cap();
 
 struct MgTables {
-    int n1md, nlev;
+    int nl, nld, nlev;          // cells along the semi-coarsened direction, 2 nl, levels
+    int nmodes, xft;            // modes solved (n3mh / n1mh); 1 for poiss_x_ft
     int cs;                     // blocks per cluster (one cluster per z mode)
     int cap;                    // cap on cs set by the creator (0 = none)
     int iimg[kMaxLev + 1][3];
     double *aw, *ae, *as, *an, *coi1, *coi2, *cor1, *cor2;   // 1-based
     int *ipm, *imm;
-    double *ac, *bet, *gam;     // (i-1) + n1md*((j-1) + n2m*(kv-1))
+    double *ac, *bet, *gam;     // (i-1) + nld*((j-1) + n2m*(kv-1))
     double2 *pc, *gg, *rs;      // per-mode work arrays
     long long *iters;           // per mode, last solve
     long long pc_plane, gg_plane;
 };
 
 struct MgArgs {
-    int n1m, n2m, n1md, nlev, nbli, mgitr, imgsor;
+    int nl, n2m, nld, nlev, nbli, mgitr, imgsor;
+    int xft;                    // poiss_x_ft's pinning and prolongation
     double wwsor;
     int ldp, ldg;
     int iimg[kMaxLev + 1][3];
@@ -76,21 +85,21 @@ struct Mode {
     int kv;
     int tid, nt;                        // thread index / count over the cluster
     double2 *pc, *gg, *rs;
-    const double2 *rhs;                 // ccap plane of the mode, (i-1) + n1m*(j-1)
+    const double2 *rhs;                 // ccap plane of the mode, (i-1) + nl*(j-1)
     size_t cb;                          // coefficient base of the mode
     __device__ void sync() const { cooperative_groups::this_cluster().sync(); }
     __device__ Mode(const MgArgs &a_, int kv_, int tid_, int nt_) : a(a_), kv(kv_), tid(tid_), nt(nt_) {
         pc = a.pc + a.pc_plane * (kv - 1);
         gg = a.gg + a.gg_plane * (kv - 1);
         rs = a.rs + a.gg_plane * (kv - 1);
-        rhs = a.ccap + (size_t)a.n1m * a.n2m * (kv - 1);
-        cb = (size_t)a.n1md * a.n2m * (kv - 1);
+        rhs = a.ccap + (size_t)a.nl * a.n2m * (kv - 1);
+        cb = (size_t)a.nld * a.n2m * (kv - 1);
     }
     __device__ double2 &P(int i, int j) const { return pc[i + (size_t)a.ldp * j]; }
     __device__ double2 &G(int i, int j) const { return gg[i + (size_t)a.ldg * j]; }
     __device__ double2 &R(int i, int j) const { return rs[i + (size_t)a.ldg * j]; }
-    __device__ double2 B(int i, int j) const { return rhs[(i - 1) + (size_t)a.n1m * (j - 1)]; }
-    __device__ double AC(int i, int j) const { return a.ac[cb + (i - 1) + (size_t)a.n1md * (j - 1)]; }
+    __device__ double2 B(int i, int j) const { return rhs[(i - 1) + (size_t)a.nl * (j - 1)]; }
+    __device__ double AC(int i, int j) const { return a.ac[cb + (i - 1) + (size_t)a.nld * (j - 1)]; }
 };
 
 __device__ __forceinline__ double2 axmy(double2 y, double s, double2 x) {   // y - s*x
@@ -175,7 +184,7 @@ __device__ __noinline__ void mg_half(const Mode &m, int l1, int l2, int kind, bo
     const int ch = (n2m + 31) / 32;
     const int j0 = 1 + lane * ch;
     const int cnt = max(0, min(ch, n2m - j0 + 1));
-    const size_t sj = (size_t)a.n1md;
+    const size_t sj = (size_t)a.nld;
     for (int li = warp; li < nl; li += nw) {
         const int i = l1 + 2 * li;
         const int im = a.imm[i], ip = a.ipm[i];
@@ -254,10 +263,22 @@ __device__ double cluster_max(const Mode &m, double v) {
     return r;
 }
 
-// toplevel, poiss_z_ft.f90:302-380; returns the max-norm residual
+// Subtract tt from the odd lines of u (ld: leading dimension) -- the zero
+// wavenumber's pin of poiss_x_ft.f90:328-335, 533-540 and 582-589.  tt was read by
+// every thread before the barrier in front of this.
+__device__ void mg_shift_odd(const Mode &m, double2 *u, int ld, double2 tt) {
+    const int nh = m.a.nl / 2, n2m = m.a.n2m;
+    for (int t = m.tid; t < nh * n2m; t += m.nt) {
+        const int i = 1 + 2 * (t % nh), j = 1 + t / nh;
+        double2 &g = u[i + (size_t)ld * j];
+        g = make_double2(g.x - tt.x, g.y - tt.y);
+    }
+}
+
+// toplevel, poiss_z_ft.f90:302-380 / poiss_x_ft.f90:296-371; returns the max-norm residual
 __device__ double mg_toplevel(const Mode &m, int id, double oldv, double test) {
     const MgArgs &a = m.a;
-    const int n1m = a.n1m, n2m = a.n2m, nt = m.nt;
+    const int n1m = a.nl, n2m = a.n2m, nt = m.nt;
     const int cl = a.iimg[a.nlev - 1][0], ce = a.iimg[a.nlev - 1][1];
     if (id == 1) {   // prolong the coarse correction onto the even lines
         const int nc = ce - cl + 1;
@@ -265,7 +286,7 @@ __device__ double mg_toplevel(const Mode &m, int id, double oldv, double test) {
             const int i = cl + t % nc, j = 1 + t / nc, ic = 2 * (i - cl + 1);
             double2 p = m.P(ic, j);
             const double2 g1 = m.G(i, j);
-            if (i < ce) {
+            if (i < ce || a.xft) {
                 const double2 g2 = m.G(a.ipm[i], j);
                 p = make_double2(p.x + a.coi1[i] * g1.x + a.coi2[i] * g2.x, p.y + a.coi1[i] * g1.y + a.coi2[i] * g2.y);
             } else {
@@ -275,19 +296,28 @@ __device__ double mg_toplevel(const Mode &m, int id, double oldv, double test) {
         }
         m.sync();
     }
-    const int nh = n1m / 2;
     mg_half<kMC>(m, 1, n1m, H_ODD, true, m.pc, a.ldp, oldv, make_double2(0.0, 0.0), false, 0.0, 0.0);
     m.sync();
-    const double2 tt = m.kv == 1 ? m.G(1, n2m - 1) : make_double2(0.0, 0.0);
-    mg_half<kMC>(m, 2, n1m, H_EVEN_TT, true, m.gg, a.ldg, 1.0, tt, false, 0.0, 0.0);
-    m.sync();
-    if (m.kv == 1)
-        for (int t = m.tid; t < nh * n2m; t += nt) {      // then shift the odd lines
-            const int i = 1 + 2 * (t % nh), j = 1 + t / nh;
-            const double2 g = m.G(i, j);
-            m.G(i, j) = make_double2(g.x - tt.x, g.y - tt.y);
+    if (a.xft) {
+        // poiss_x_ft: shift the odd lines by ggii(1,n2m), then form the even
+        // lines from the shifted values as rhs - (ab*g + af*g)
+        if (m.kv == 1) {
+            const double2 tt = m.G(1, n2m);
+            m.sync();
+            mg_shift_odd(m, m.gg, a.ldg, tt);
+            m.sync();
         }
-    m.sync();
+        mg_half<kMC>(m, 2, n1m, H_ODD, true, m.gg, a.ldg, 1.0, make_double2(0.0, 0.0), false, 0.0, 0.0);
+        m.sync();
+    } else {
+        // poiss_z_ft: the even lines see the odd ones shifted by ggii(1,n2m-1)
+        // inside their right-hand side; the odd lines are shifted afterwards
+        const double2 tt = m.kv == 1 ? m.G(1, n2m - 1) : make_double2(0.0, 0.0);
+        mg_half<kMC>(m, 2, n1m, H_EVEN_TT, true, m.gg, a.ldg, 1.0, tt, false, 0.0, 0.0);
+        m.sync();
+        if (m.kv == 1) mg_shift_odd(m, m.gg, a.ldg, tt);
+        m.sync();
+    }
     double mx = 0.0;
     for (int t = m.tid; t < n1m * n2m; t += nt) {
         const int i = 1 + t % n1m, j = 1 + t / n1m;
@@ -340,7 +370,7 @@ __device__ void mg_godown(const Mode &m, int ilev) {
     m.sync();
 }
 
-// goup, poiss_z_ft.f90:411-435
+// goup, poiss_z_ft.f90:411-435 / poiss_x_ft.f90:401-419
 __device__ void mg_goup(const Mode &m, int ilev) {
     const MgArgs &a = m.a;
     const int cl = a.iimg[ilev][0], ce = a.iimg[ilev][1], n2m = a.n2m, nt = m.nt;
@@ -349,7 +379,7 @@ __device__ void mg_goup(const Mode &m, int ilev) {
         const int i = cl + t % nc, j = 1 + t / nc, f = fb + 1 + 2 * (i - cl);
         double2 g = m.G(f, j);
         const double2 g1 = m.G(i, j);
-        if (i < ce) {
+        if (i < ce || a.xft) {
             const double2 g2 = m.G(a.ipm[i], j);
             g = make_double2(g.x + a.coi1[i] * g1.x + a.coi2[i] * g2.x, g.y + a.coi1[i] * g1.y + a.coi2[i] * g2.y);
         } else {
@@ -381,10 +411,10 @@ __device__ int mg_mg2d(const Mode &m, double test) {
     return a.mgitr;       // iteration limit: the reference warns and goes on
 }
 
-// gsor2d + resid3, poiss_z_ft.f90:513-641 (pc is the iterate u)
+// gsor2d + resid3, poiss_z_ft.f90:513-641 / poiss_x_ft.f90:497-642 (pc is the iterate u)
 __device__ int mg_gsor2d(const Mode &m, double test) {
     const MgArgs &a = m.a;
-    const int n1m = a.n1m, n2m = a.n2m, nt = m.nt;
+    const int n1m = a.nl, n2m = a.n2m, nt = m.nt;
     const double ww = a.wwsor, ww2 = 1.0 - ww;
     for (int kk = 0; kk <= a.mgitr; kk++) {
         const double ov = kk == 0 ? 0.0 : 1.0, o2 = ov * ww2;
@@ -392,6 +422,12 @@ __device__ int mg_gsor2d(const Mode &m, double test) {
             const double f = half == 0 ? ov : 1.0;
             mg_half<kMC>(m, 1 + half, n1m, H_ODD, true, m.pc, a.ldp, f, make_double2(0.0, 0.0), true, ww, o2);
             m.sync();
+            if (half == 0 && a.xft && m.kv == 1) {     // poiss_x_ft pins the zero wavenumber by u(1,n2m)
+                const double2 tt = m.P(1, n2m);
+                m.sync();
+                mg_shift_odd(m, m.pc, a.ldp, tt);
+                m.sync();
+            }
         }
         double mx = 0.0;
         for (int t = m.tid; t < n1m * n2m; t += nt) {
@@ -418,9 +454,9 @@ __global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes(MgArgs a) {
     const double test = a.fixed_cycles > 0 ? -1.0 : a.S->mg_test;
     const int it = kv <= a.imgsor ? mg_mg2d(m, test) : mg_gsor2d(m, test);
     // the mode's solution replaces its right-hand side (ccap(i,j,kkk) = cp(i,j))
-    double2 *out = a.ccap + (size_t)a.n1m * a.n2m * (kv - 1);
-    for (int t = m.tid; t < a.n1m * a.n2m; t += m.nt) {
-        const int i = 1 + t % a.n1m, j = 1 + t / a.n1m;
+    double2 *out = a.ccap + (size_t)a.nl * a.n2m * (kv - 1);
+    for (int t = m.tid; t < a.nl * a.n2m; t += m.nt) {
+        const int i = 1 + t % a.nl, j = 1 + t / a.nl;
         out[t] = m.P(i, j);
     }
     if (m.tid == 0) {
@@ -429,41 +465,63 @@ __global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes(MgArgs a) {
     }
 }
 
-// convergence criterion of the substep: test1 / n3mh * n3m * 0.8 (poiss_z_ft.f90:166), test1 in 2-D
-__global__ void k_zft_begin(DScal *S, int slot, int n3m, int n3mh) {
+// convergence criterion of the substep: test1 / nmodes * nfft * fac -- 0.8 in
+// poiss_z_ft.f90:179 (test1 itself in 2-D), 0.9 in poiss_x_ft.f90:158
+__global__ void k_mg_begin(DScal *S, int slot, int nfft, int nmodes, double fac) {
     S->poisson_iters[slot] = 0;
-    S->mg_test = n3m == 1 ? S->test1 : S->test1 / (double)n3mh * (double)n3m * 0.8;
+    S->mg_test = nfft == 1 ? S->test1 : S->test1 / (double)nmodes * (double)nfft * fac;
 }
 
 // ---------------------------------------------------------------- host side
-static int set_up_tables(lesgpu_case *c, MgTables &T, std::vector<double> &h_ak3) {
+// The semi-coarsened axis of a solve, in the reference's Fortran indexing:
+// x for poiss_z_ft, z for poiss_x_ft.
+struct MgAxis {
+    int nm, n;                                      // cells, nodes (nm + 1)
+    bool prdic;
+    std::vector<double> x, xmp, c2ci, f2fi;         // x(1..n); xmp, c2c?i, f2f?i (0..n)
+    std::vector<long long> pv, fixl, fixu;          // ipv / kpv, fixil / fixkl, fixiu / fixku (1..nm)
+};
+
+// pmat, mwavenumber, coefmg and the LU factors of poisinit, in the
+// reference's arithmetic order: poiss_z_ft.f90:18-113, 643-798 and
+// poiss_x_ft.f90:18-112, 644-794.  ab/af of x_ft land in aw/ae, kpm/kmm in
+// ipm/imm, kkmg in iimg.
+static int set_up_tables(lesgpu_case *c, MgTables &T) {
     const DGrid &g = c->kp.g;
     const lesgpu_config &cf = c->cfg;
-    const int n1m = g.n1m, n2m = g.n2m, n3m = g.n3m, n3mh = g.n3mh, n1md = 2 * n1m, nlev = (int)cf.nlev;
-    const int n1 = g.n1;
+    const bool xft = T.xft != 0;
+    const int n2m = g.n2m, nmodes = T.nmodes, n1md = T.nld, nlev = T.nlev;
     const lesgpu_grid *hg = c->h_grid;
-    // host copies in Fortran index
     auto v0 = [&](const double *p, int n) { std::vector<double> v(n + 2, 0.0); for (int q = 0; q <= n; q++) v[q] = p[q]; return v; };
     auto v1 = [&](const double *p, int n) { std::vector<double> v(n + 2, 0.0); for (int q = 1; q <= n; q++) v[q] = p[q - 1]; return v; };
     auto i1 = [&](const int64_t *p, int n) { std::vector<long long> v(n + 2, 0); for (int q = 1; q <= n; q++) v[q] = p[q - 1]; return v; };
-    std::vector<double> x = v1(hg->x, n1), xmp = v0(hg->xmp, n1);
-    std::vector<double> c2cxi = v0(hg->c2cxi, n1), f2fxi = v0(hg->f2fxi, n1), c2cyi = v0(hg->c2cyi, g.n2), f2fyi = v0(hg->f2fyi, g.n2);
-    std::vector<double> f2fzi = v0(hg->f2fzi, g.n3);
-    std::vector<long long> ipv = i1(hg->ipv, n1m), jpv = i1(hg->jpv, n2m);
-    std::vector<long long> fixil = i1(hg->fixil, n1m), fixiu = i1(hg->fixiu, n1m), fixjl = i1(hg->fixjl, n2m), fixju = i1(hg->fixju, n2m);
+    MgAxis A;
+    if (xft) {
+        A.nm = g.n3m; A.n = g.n3; A.prdic = cf.zprdic == 1;
+        A.x = v1(hg->z, g.n3); A.xmp = v0(hg->zmp, g.n3); A.c2ci = v0(hg->c2czi, g.n3); A.f2fi = v0(hg->f2fzi, g.n3);
+        A.pv = i1(hg->kpv, g.n3m); A.fixl = i1(hg->fixkl, g.n3m); A.fixu = i1(hg->fixku, g.n3m);
+    } else {
+        A.nm = g.n1m; A.n = g.n1; A.prdic = cf.xprdic == 1;
+        A.x = v1(hg->x, g.n1); A.xmp = v0(hg->xmp, g.n1); A.c2ci = v0(hg->c2cxi, g.n1); A.f2fi = v0(hg->f2fxi, g.n1);
+        A.pv = i1(hg->ipv, g.n1m); A.fixl = i1(hg->fixil, g.n1m); A.fixu = i1(hg->fixiu, g.n1m);
+    }
+    const int n1m = A.nm, n1 = A.n;
+    const std::vector<double> &x = A.x;
+    std::vector<double> c2cyi = v0(hg->c2cyi, g.n2), f2fyi = v0(hg->f2fyi, g.n2);
+    std::vector<long long> jpv = i1(hg->jpv, n2m), fixjl = i1(hg->fixjl, n2m), fixju = i1(hg->fixju, n2m);
 
-    const size_t nv = (size_t)n1md + 2, na = (size_t)n1md * n2m * n3mh;
+    const size_t nv = (size_t)n1md + 2, na = (size_t)n1md * n2m * nmodes;
     std::vector<double> aw(nv, 0.0), ae(nv, 0.0), as(n2m + 2, 0.0), an(n2m + 2, 0.0);
     std::vector<double> coi1(nv, 0.0), coi2(nv, 0.0), cor1(nv, 0.0), cor2(nv, 0.0);
     std::vector<int> ipm(nv, 0), imm(nv, 0);
     std::vector<double> ac(na, 0.0), bet(na, 0.0), gam(na, 0.0);
-    h_ak3.assign(n3mh + 2, 0.0);
+    std::vector<double> ak(nmodes + 2, 0.0);          // modified wavenumbers: ak3 (z_ft) / ai3 (x_ft)
     auto AC = [&](int i, int j, int k) -> double & { return ac[(size_t)(i - 1) + (size_t)n1md * ((size_t)(j - 1) + (size_t)n2m * (size_t)(k - 1))]; };
     // pmat
     for (int i = 1; i <= n1m; i++) {
-        long long ip = ipv[i];
-        aw[i] = (1.0 - (double)fixil[i]) * c2cxi[i] * f2fxi[i];
-        ae[i] = (1.0 - (double)fixiu[i]) * c2cxi[ip] * f2fxi[i];
+        long long ip = A.pv[i];
+        aw[i] = (1.0 - (double)A.fixl[i]) * A.c2ci[i] * A.f2fi[i];
+        ae[i] = (1.0 - (double)A.fixu[i]) * A.c2ci[ip] * A.f2fi[i];
     }
     for (int j = 1; j <= n2m; j++) {
         long long jp = jpv[j];
@@ -472,20 +530,25 @@ static int set_up_tables(lesgpu_case *c, MgTables &T, std::vector<double> &h_ak3
     }
     for (int j = 1; j <= n2m; j++)
         for (int i = 1; i <= n1m; i++) AC(i, j, 1) = -1.0 * (aw[i] + ae[i] + as[j] + an[j]);
-    if (n3m > 1) {
-        const double pi = acos(-1.0);
-        for (int k = 1; k <= n3mh; k++)
-            h_ak3[k] = 2.0 * (1.0 - cos(2.0 * (double)(k - 1) * pi / (double)n3m)) * f2fzi[1] * f2fzi[1];
+    const double pi = acos(-1.0);
+    if (xft) {
+        const double sdx = hg->f2fxi[1];
+        for (int i = 1; i <= nmodes; i++)
+            ak[i] = 2.0 * (1.0 - cos(2.0 * pi * (double)(i - 1) / (double)g.n1m)) * sdx * sdx;
+    } else if (g.n3m > 1) {
+        const double sdz = hg->f2fzi[1];
+        for (int k = 1; k <= nmodes; k++)
+            ak[k] = 2.0 * (1.0 - cos(2.0 * (double)(k - 1) * pi / (double)g.n3m)) * sdz * sdz;
     }
-    for (int k = 2; k <= n3mh; k++)
+    for (int k = 2; k <= nmodes; k++)
         for (int j = 1; j <= n2m; j++)
-            for (int i = 1; i <= n1m; i++) AC(i, j, k) = AC(i, j, 1) - h_ak3[k];
+            for (int i = 1; i <= n1m; i++) AC(i, j, k) = AC(i, j, 1) - ak[k];
     // coefmg
     const int minrow = n1m / (1 << nlev);
     std::vector<double> xmpm(nv, 0.0), iwz(nv, 0.0), iez(nv, 0.0);
     int (&iimg)[kMaxLev + 1][3] = T.iimg;
     iimg[nlev][0] = 1; iimg[nlev][1] = n1m; iimg[nlev][2] = n1m;
-    for (int i = 1; i <= n1m; i++) xmpm[i] = xmp[i];
+    for (int i = 1; i <= n1m; i++) xmpm[i] = A.xmp[i];
     for (int ilev = nlev - 1; ilev >= 0; ilev--) {
         iimg[ilev][0] = iimg[ilev + 1][0] + iimg[ilev + 1][2];
         iimg[ilev][2] = minrow * (1 << ilev);
@@ -507,9 +570,9 @@ static int set_up_tables(lesgpu_case *c, MgTables &T, std::vector<double> &h_ak3
         }
         for (int j = 1; j <= n2m; j++)
             for (int i = ibg; i <= iend; i++) AC(i, j, 1) = -1.0 * (aw[i] + ae[i] + as[j] + an[j]);
-        for (int k = 2; k <= n3mh; k++)
+        for (int k = 2; k <= nmodes; k++)
             for (int j = 1; j <= n2m; j++)
-                for (int i = ibg; i <= iend; i++) AC(i, j, k) = AC(i, j, 1) - h_ak3[k];
+                for (int i = ibg; i <= iend; i++) AC(i, j, k) = AC(i, j, 1) - ak[k];
     }
     for (int ilev = nlev; ilev >= 1; ilev--) {
         int ibgh = iimg[ilev][0];
@@ -528,9 +591,12 @@ static int set_up_tables(lesgpu_case *c, MgTables &T, std::vector<double> &h_ak3
         }
         coi1[iimg[ilev][1]] = 1.0;
     }
+    // neighbours; without periodicity x_ft leaves kpm/kmm unset, and the
+    // coefficients that multiply them at the level ends are zero, so i+1 / i-1
+    // (finite work-array entries) serve both
     for (int ilev = nlev; ilev >= 0; ilev--)
         for (int i = iimg[ilev][0]; i <= iimg[ilev][1]; i++) { ipm[i] = i + 1; imm[i] = i - 1; }
-    if (cf.xprdic == 1) {
+    if (A.prdic) {
         for (int ilev = nlev; ilev >= 0; ilev--) { ipm[iimg[ilev][1]] = iimg[ilev][0]; imm[iimg[ilev][0]] = iimg[ilev][1]; }
         for (int ilev = nlev - 1; ilev >= 0; ilev--) {
             const int ibg = iimg[ilev][0], iend = iimg[ilev][1], isp = 1 << (nlev - ilev);
@@ -541,9 +607,9 @@ static int set_up_tables(lesgpu_case *c, MgTables &T, std::vector<double> &h_ak3
         for (int ilev = nlev - 1; ilev >= 0; ilev--) {
             for (int j = 1; j <= n2m; j++)
                 for (int i = iimg[ilev][0]; i <= iimg[ilev][1]; i++) AC(i, j, 1) = -1.0 * (aw[i] + ae[i] + as[j] + an[j]);
-            for (int k = 2; k <= n3mh; k++)
+            for (int k = 2; k <= nmodes; k++)
                 for (int j = 1; j <= n2m; j++)
-                    for (int i = iimg[ilev][0]; i <= iimg[ilev][1]; i++) AC(i, j, k) = AC(i, j, 1) - h_ak3[k];
+                    for (int i = iimg[ilev][0]; i <= iimg[ilev][1]; i++) AC(i, j, k) = AC(i, j, 1) - ak[k];
         }
         for (int ilev = 0; ilev <= nlev - 1; ilev++) {
             const int ibg = iimg[ilev][0], iend = iimg[ilev][1];
@@ -555,7 +621,7 @@ static int set_up_tables(lesgpu_case *c, MgTables &T, std::vector<double> &h_ak3
     // poisinit: LU factors of every level's y-operator
     auto IX3 = [&](int i, int j, int k) { return (size_t)(i - 1) + (size_t)n1md * ((size_t)(j - 1) + (size_t)n2m * (size_t)(k - 1)); };
     for (int ilev = 0; ilev <= nlev; ilev++)
-        for (int k = 1; k <= n3mh; k++) {
+        for (int k = 1; k <= nmodes; k++) {
             for (int i = iimg[ilev][0]; i <= iimg[ilev][1]; i++) bet[IX3(i, 1, k)] = 1.0 / ac[IX3(i, 1, k)];
             for (int j = 2; j <= n2m; j++)
                 for (int i = iimg[ilev][0]; i <= iimg[ilev][1]; i++) {
@@ -576,44 +642,63 @@ static int set_up_tables(lesgpu_case *c, MgTables &T, std::vector<double> &h_ak3
     return ok ? 0 : LESGPU_ERR_OOM;
 }
 
-int zft_init(lesgpu_case *c) {
+static void cluster_cfg(cudaLaunchConfig_t &lc, cudaLaunchAttribute (&at)[1], int nmodes, int cs) {
+    lc = {};
+    lc.gridDim = dim3(nmodes * cs);
+    lc.blockDim = dim3(kMgThreads);
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+}
+
+int mg2d_init(lesgpu_case *c) {
     const DGrid &g = c->kp.g;
     const lesgpu_config &cf = c->cfg;
     DPois &P = c->pois;
-    const int nlev = (int)cf.nlev;
-    if (nlev < 1 || nlev > kMaxLev || g.n1m % (1 << nlev) != 0) return LESGPU_ERR_CONFIG;
-    if (g.n3m > 1 && cf.zprdic != 1) return LESGPU_ERR_CONFIG;
+    const bool xft = cf.poisson == LESGPU_POISSON_X_FT;
+    const int nlev = (int)cf.nlev, nl = xft ? g.n3m : g.n1m, nmodes = xft ? g.n1mh : g.n3mh;
+    if (nlev < 1 || nlev > kMaxLev || nl % (1 << nlev) != 0) return LESGPU_ERR_CONFIG;
+    if (!xft && g.n3m > 1 && cf.zprdic != 1) return LESGPU_ERR_CONFIG;   // the z transform needs periodic z
+    if (xft && cf.xprdic != 1) return LESGPU_ERR_CONFIG;                 // the x transform needs periodic x
     if (cf.mgitr < 0 || cf.nbli < 1) return LESGPU_ERR_CONFIG;
     if (g.n2m > 32 * kMC) return LESGPU_ERR_UNSUPPORTED;    // one warp per y line, kMC rows per lane
-    int rc = make_plan(P.fz, g.n3m);
+    int rc = xft ? make_plan(P.fx, g.n1m) : make_plan(P.fz, g.n3m);
     if (rc) return rc;
     MgTables *T = new MgTables();
     memset(T, 0, sizeof(*T));
     P.mg = T;
-    T->n1md = 2 * g.n1m;
+    T->nl = nl;
+    T->nld = 2 * nl;
     T->nlev = nlev;
-    std::vector<double> ak3;
-    rc = set_up_tables(c, *T, ak3);
+    T->nmodes = nmodes;
+    T->xft = xft ? 1 : 0;
+    rc = set_up_tables(c, *T);
     if (rc) return rc;
-    const int ldp = g.n1m + 2, ldg = T->n1md + 1;
+    const int ldp = nl + 2, ldg = T->nld + 1;
     T->pc_plane = (long long)ldp * (g.n2m + 2);
     T->gg_plane = (long long)ldg * (g.n2m + 2);
-    const size_t nm = (size_t)g.n3mh;
+    const size_t nm = (size_t)nmodes;
     if (cudaMalloc(&T->pc, sizeof(double2) * T->pc_plane * nm) != cudaSuccess ||
         cudaMalloc(&T->gg, sizeof(double2) * T->gg_plane * nm) != cudaSuccess ||
         cudaMalloc(&T->rs, sizeof(double2) * T->gg_plane * nm) != cudaSuccess ||
         cudaMalloc(&T->iters, sizeof(long long) * nm) != cudaSuccess ||
-        cudaMalloc(&P.ccap, sizeof(double2) * (size_t)g.n1m * g.n2m * nm) != cudaSuccess)
+        cudaMalloc(&P.ccap, sizeof(double2) * (size_t)nl * g.n2m * nm) != cudaSuccess)
         return LESGPU_ERR_OOM;
     // the boundary rows and columns of pc / gg are read as zeros and never written
     cudaMemset(T->pc, 0, sizeof(double2) * T->pc_plane * nm);
     cudaMemset(T->gg, 0, sizeof(double2) * T->gg_plane * nm);
     cudaMemset(T->rs, 0, sizeof(double2) * T->gg_plane * nm);
     cudaMemset(T->iters, 0, sizeof(long long) * nm);
-    const int kMaxSmem = 200 * 1024;
-    if (cudaFuncSetAttribute(k_fft_z_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem) != cudaSuccess ||
-        cudaFuncSetAttribute(k_fft_z_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem) != cudaSuccess)
-        return LESGPU_ERR_CUDA;
+    if (xft) {
+        if (cudaFuncSetAttribute(k_fft_xr_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess ||
+            cudaFuncSetAttribute(k_fft_xr_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess)
+            return LESGPU_ERR_CUDA;
+    } else {
+        if (cudaFuncSetAttribute(k_fft_z_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess ||
+            cudaFuncSetAttribute(k_fft_z_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess)
+            return LESGPU_ERR_CUDA;
+    }
     // Cluster size: the mode solves are FP64-throughput bound (a GB300 SM
     // retires few FP64 FMAs per clock), so each mode gets as many SMs as the
     // GPU can co-schedule for all modes: minimise waves / blocks-per-mode.
@@ -623,20 +708,15 @@ int zft_init(lesgpu_case *c) {
     const int cands[5] = {16, 8, 4, 2, 1};
     for (int q = 0; q < 5; q++) {
         const int cs = cands[q];
-        cudaLaunchConfig_t lc = {};
-        lc.gridDim = dim3(g.n3mh * cs);
-        lc.blockDim = dim3(kMgThreads);
+        cudaLaunchConfig_t lc;
         cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = cs; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
-        lc.attrs = at;
-        lc.numAttrs = 1;
+        cluster_cfg(lc, at, nmodes, cs);
         int nact = 0;
         if (cudaOccupancyMaxActiveClusters(&nact, k_zft_modes, &lc) != cudaSuccess || nact < 1) {
             cudaGetLastError();
             continue;
         }
-        const double waves = (double)((g.n3mh + nact - 1) / nact);
+        const double waves = (double)((nmodes + nact - 1) / nact);
         const double cost = waves / cs;
         if (cost < best - 1e-12) { best = cost; T->cs = cs; }
     }
@@ -657,7 +737,7 @@ static thread_local int t_mg_cluster_cap = 0;
 int mg_cluster_cap() { return t_mg_cluster_cap; }
 void set_mg_cluster_cap(int cap) { t_mg_cluster_cap = cap; }
 
-void zft_free(lesgpu_case *c) {
+void mg2d_free(lesgpu_case *c) {
     MgTables *T = c->pois.mg;
     if (!T) return;
     void *ptrs[] = {T->aw, T->ae, T->as, T->an, T->coi1, T->coi2, T->cor1, T->cor2, T->ipm, T->imm,
@@ -667,17 +747,18 @@ void zft_free(lesgpu_case *c) {
     c->pois.mg = nullptr;
 }
 
-static MgArgs zft_args(lesgpu_case *c, int slot, int fixed_cycles) {
+static MgArgs mg_args(lesgpu_case *c, int slot, int fixed_cycles) {
     const DGrid &g = c->kp.g;
     const lesgpu_config &cf = c->cfg;
     DPois &P = c->pois;
     MgTables *T = P.mg;
     MgArgs a;
     memset(&a, 0, sizeof(a));
-    a.n1m = g.n1m; a.n2m = g.n2m; a.n1md = T->n1md; a.nlev = T->nlev;
+    a.nl = T->nl; a.n2m = g.n2m; a.nld = T->nld; a.nlev = T->nlev;
+    a.xft = T->xft;
     a.nbli = (int)cf.nbli; a.mgitr = fixed_cycles > 0 ? fixed_cycles : (int)cf.mgitr;
     a.imgsor = (int)cf.imgsor; a.wwsor = cf.wwsor;
-    a.ldp = g.n1m + 2; a.ldg = T->n1md + 1;
+    a.ldp = T->nl + 2; a.ldg = T->nld + 1;
     memcpy(a.iimg, T->iimg, sizeof(a.iimg));
     a.aw = T->aw; a.ae = T->ae; a.as = T->as; a.an = T->an;
     a.coi1 = T->coi1; a.coi2 = T->coi2; a.cor1 = T->cor1; a.cor2 = T->cor2;
@@ -690,50 +771,50 @@ static MgArgs zft_args(lesgpu_case *c, int slot, int fixed_cycles) {
 }
 
 static void launch_modes(lesgpu_case *c, const MgArgs &a, int cs, int nmodes = 0) {
-    cudaLaunchConfig_t lc = {};
-    lc.gridDim = dim3((nmodes > 0 ? nmodes : c->kp.g.n3mh) * cs);
-    lc.blockDim = dim3(kMgThreads);
-    lc.dynamicSmemBytes = 0;
-    lc.stream = c->stream;
+    cudaLaunchConfig_t lc;
     cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = cs; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
-    lc.attrs = at;
-    lc.numAttrs = 1;
+    cluster_cfg(lc, at, nmodes > 0 ? nmodes : c->pois.mg->nmodes, cs);
+    lc.stream = c->stream;
     cudaLaunchKernelEx(&lc, k_zft_modes, a);
 }
 
 // can a cluster of cs blocks be scheduled at all
 static bool cluster_fits(lesgpu_case *c, int cs) {
-    cudaLaunchConfig_t lc = {};
-    lc.gridDim = dim3(c->kp.g.n3mh * cs);
-    lc.blockDim = dim3(kMgThreads);
+    cudaLaunchConfig_t lc;
     cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = cs; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
-    lc.attrs = at;
-    lc.numAttrs = 1;
+    cluster_cfg(lc, at, c->pois.mg->nmodes, cs);
     int nact = 0;
     if (cudaOccupancyMaxActiveClusters(&nact, k_zft_modes, &lc) != cudaSuccess) { cudaGetLastError(); return false; }
     return nact >= 1;
 }
 
-void launch_zft(lesgpu_case *c, int msub) {
+void launch_mg2d(lesgpu_case *c, int msub) {
     const DGrid &g = c->kp.g;
-    const lesgpu_config &cf = c->cfg;
     DPois &P = c->pois;
     MgTables *T = P.mg;
-    DevPlan pz = devplan(P.fz);
     const int slot = (msub >= 1 && msub <= 3) ? msub - 1 : 0;
     inst_begin(c, LESGPU_K_POISSON);
-    k_zft_begin<<<1, 1, 0, c->stream>>>(c->S, slot, g.n3m, g.n3mh);
-    const int Lz = fft_lz(c);
-    const size_t smz = (size_t)2 * (g.n3m > 1 ? g.n3m : 1) * Lz * sizeof(double2);
-    const dim3 gz((g.n1m + Lz - 1) / Lz, g.n2m);
-    const long long sk = (long long)g.n1m * g.n2m, sj = g.n1m;
-    k_fft_z_fwd<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
-    launch_modes(c, zft_args(c, slot, 0), T->cs);
-    k_fft_z_inv<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
+    if (T->xft) {
+        k_mg_begin<<<1, 1, 0, c->stream>>>(c->S, slot, g.n1m, g.n1mh, 0.9);
+        const DevPlan px = devplan(P.fx);
+        const int Lx = fft_lx(c), pin = c->cfg.ich == 1 ? 1 : 0;
+        const int Li = fft_xr_inv_lines(g.n1m, Lx, pin);
+        k_fft_xr_fwd<<<dim3((g.n3m + Lx - 1) / Lx, g.n2m), kThreads, (size_t)2 * g.n1m * Lx * sizeof(double2),
+                       c->stream>>>(c->kp, P.ccap, px, Lx);
+        launch_modes(c, mg_args(c, slot, 0), T->cs);
+        k_fft_xr_inv<<<dim3((g.n3m + Li - 1) / Li, g.n2m), kThreads, (size_t)2 * g.n1m * (Li + pin) * sizeof(double2),
+                       c->stream>>>(c->kp, P.ccap, px, Li, pin);
+    } else {
+        k_mg_begin<<<1, 1, 0, c->stream>>>(c->S, slot, g.n3m, g.n3mh, 0.8);
+        const DevPlan pz = devplan(P.fz);
+        const int Lz = fft_lz(c);
+        const size_t smz = (size_t)2 * (g.n3m > 1 ? g.n3m : 1) * Lz * sizeof(double2);
+        const dim3 gz((g.n1m + Lz - 1) / Lz, g.n2m);
+        const long long sk = (long long)g.n1m * g.n2m, sj = g.n1m;
+        k_fft_z_fwd<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
+        launch_modes(c, mg_args(c, slot, 0), T->cs);
+        k_fft_z_inv<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
+    }
     inst_end(c, LESGPU_K_POISSON);
 }
 
@@ -742,20 +823,20 @@ void launch_zft(lesgpu_case *c, int msub) {
 // the others finish early -- and its cycle count depends on the data, so the
 // candidates are timed on that mode alone, three V-cycles with the
 // convergence test off (results go to scratch).
-static std::map<std::array<int, 6>, int> g_zft_cs;
+static std::map<std::array<int, 7>, int> g_zft_cs;
 static std::mutex g_zft_mu;
 
-int zft_autotune(lesgpu_case *c) {
+int mg2d_autotune(lesgpu_case *c) {
     const DGrid &g = c->kp.g;
     MgTables *T = c->pois.mg;
-    if (!T || c->cfg.poisson != LESGPU_POISSON_Z_FT) return 0;
-    const std::array<int, 6> key{g.n1m, g.n2m, g.n3m, T->nlev, (int)c->cfg.imgsor, T->cap};
+    if (!T || (c->cfg.poisson != LESGPU_POISSON_Z_FT && c->cfg.poisson != LESGPU_POISSON_X_FT)) return 0;
+    const std::array<int, 7> key{T->xft, g.n1m, g.n2m, g.n3m, T->nlev, (int)c->cfg.imgsor, T->cap};
     {
         std::lock_guard<std::mutex> lk(g_zft_mu);
         auto it = g_zft_cs.find(key);
         if (it != g_zft_cs.end()) { T->cs = it->second; return 0; }
     }
-    const MgArgs a = zft_args(c, 0, 3);
+    const MgArgs a = mg_args(c, 0, 3);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -779,6 +860,6 @@ int zft_autotune(lesgpu_case *c) {
     g_zft_cs[key] = best;
     return cudaStreamSynchronize(c->stream) == cudaSuccess ? 0 : LESGPU_ERR_CUDA;
 }
-int zft_cluster(const lesgpu_case *c) { return c->pois.mg ? c->pois.mg->cs : 0; }
+int mg2d_cluster(const lesgpu_case *c) { return c->pois.mg ? c->pois.mg->cs : 0; }
 
 }  // namespace lg

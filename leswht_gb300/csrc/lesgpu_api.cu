@@ -89,7 +89,8 @@ int check_config(const lesgpu_config *c, const lesgpu_grid *g) {
     if (g->n1m < 2 || g->n2m < 2 || g->n3m < 1) return LESGPU_ERR_ARG;
     if ((long long)(g->n1 + 1) * (g->n2 + 1) * (g->n3 + 1) > (1LL << 40)) return LESGPU_ERR_ARG;
     if (c->precision != LESGPU_PREC_FP64 && c->precision != LESGPU_PREC_MIXED) return LESGPU_ERR_ARG;
-    if (c->poisson != LESGPU_POISSON_FTFT && c->poisson != LESGPU_POISSON_Z_FT && c->poisson != LESGPU_POISSON_MGRD)
+    if (c->poisson != LESGPU_POISSON_FTFT && c->poisson != LESGPU_POISSON_Z_FT && c->poisson != LESGPU_POISSON_MGRD &&
+        c->poisson != LESGPU_POISSON_X_FT)
         return LESGPU_ERR_UNSUPPORTED;
     if (c->imovingon != 0) return LESGPU_ERR_UNSUPPORTED;     // moving bodies: not built
     // poiss_ftft transforms x and z: both must be periodic
@@ -554,7 +555,7 @@ extern "C" int lesgpu_start(lesgpu_case *c) {
     if (c->autotune) {
         int rc = adi_autotune(c);
         if (!rc) rc = fft_autotune(c);
-        if (!rc) rc = zft_autotune(c);
+        if (!rc) rc = mg2d_autotune(c);
         if (rc) return rc;
     }
     return cuda_rc(cudaStreamSynchronize(c->stream));
@@ -736,7 +737,7 @@ extern "C" int lesgpu_tuning(lesgpu_case *c, int64_t *out, int64_t maxn, int64_t
     int n = c->autotune ? adi_tuned(c, buf, 4 * 64) : 0;
     if (c->autotune && c->pois.Lz > 0) { buf[4 * n] = 3; buf[4 * n + 1] = 2; buf[4 * n + 2] = 0; buf[4 * n + 3] = c->pois.Lz; n++; }
     if (c->autotune && c->pois.Lx > 0) { buf[4 * n] = 3; buf[4 * n + 1] = 0; buf[4 * n + 2] = 0; buf[4 * n + 3] = c->pois.Lx; n++; }
-    if (c->autotune && zft_cluster(c) > 0) { buf[4 * n] = 4; buf[4 * n + 1] = 0; buf[4 * n + 2] = 0; buf[4 * n + 3] = zft_cluster(c); n++; }
+    if (c->autotune && mg2d_cluster(c) > 0) { buf[4 * n] = 4; buf[4 * n + 1] = 0; buf[4 * n + 2] = 0; buf[4 * n + 3] = mg2d_cluster(c); n++; }
     *nclasses = n;
     for (int q = 0; q < n && q < maxn; q++)
         for (int e = 0; e < 4; e++) out[4 * q + e] = buf[4 * q + e];

@@ -72,7 +72,7 @@ struct DScal {
     double phiref;            // pcalc's outlet-plane mean of phi
     double cvol;              // tvolcorr's volume integral of 1/c*
     double cb[4];             // convective outlet: qin, ucoef, vwcoef, qratio
-    double mg_test;           // z_ft multigrid convergence criterion of the substep
+    double mg_test;           // z_ft / x_ft multigrid convergence criterion of the substep
     long long avg_count;      // field_avg samples since the last reset
     long long ntime, m, ihist;
     long long poisson_iters[3];
@@ -122,7 +122,8 @@ struct MgrdTables;
 struct DPois {
     double *ak1, *ak3;
     double2 *ccap;            // spectrum; ftft: (n1m, n3mh, n2m) i fastest, then k, then j;
-                              // z_ft: (n1m, n2m, n3mh), one x-y plane per z mode
+                              // z_ft: (n1m, n2m, n3mh), one x-y plane per z mode;
+                              // x_ft: (n3m, n2m, n1mh), one z-y plane per x mode
     FftPlan fx, fz;
     MgTables *mg;
     MgrdTables *mgrd;         // poiss_mgrd (BiCGSTAB + MG3D)
@@ -367,8 +368,8 @@ int adi_autotune(lesgpu_case *c);
 // autotuner (k_fft.cu): FFT lines per block of the case's Poisson transforms
 int fft_autotune(lesgpu_case *c);
 // autotuner (k_mg.cu): cluster size of the z_ft multigrid; the chosen size
-int zft_autotune(lesgpu_case *c);
-int zft_cluster(const lesgpu_case *c);
+int mg2d_autotune(lesgpu_case *c);
+int mg2d_cluster(const lesgpu_case *c);
 int adi_tuned(const lesgpu_case *c, int *out, int maxn);
 // cap on the z_ft multigrid's cluster size for cases created by this thread (0 = none)
 void set_mg_cluster_cap(int cap);

@@ -704,6 +704,443 @@ static void zft_poisson(ref_case *c)
     c->poisson_iters[c->msub >= 1 && c->msub <= 3 ? c->msub - 1 : 0] = itmax;
 }
 
+/* -------------------------------------------------------- poiss_x_ft -- */
+/* FFT in x, then for every x mode a 2-D problem in z-y solved by multigrid
+   semi-coarsened in z with zebra z-line relaxation (y-Thomas per line).
+   Level ilev occupies z slots kkmg[ilev][0]..kkmg[ilev][1] of ab, af,
+   coi?, cor?, kpm, kmm; the finest level nlev is 1..n3m.  ak1 holds ai3,
+   the x modified wavenumbers.  The work arrays of one mode reuse zmode:
+   pc(0:n3,0:n2), rhs(n3,n2), resd(n3md,n2m), ggii(0:n3md,0:n2). */
+
+#define XAC(c, k, j, i) ((size_t)((k) - 1) + (size_t)(c)->n3md * ((size_t)((j) - 1) + (size_t)(c)->n2m * (size_t)((i) - 1)))
+
+/* pmat + mwavenumber, poiss_x_ft.f90:54-112 */
+static void xft_pmat(ref_case *c)
+{
+    ll n1m = c->n1m, n2m = c->n2m, n3m = c->n3m;
+    for (ll k = 1; k <= n3m; k++) {
+        ll kp = c->kpv[k];
+        c->ab[k] = (1.0 - (double)c->fixkl[k]) * c->c2czi[k] * c->f2fzi[k];
+        c->af[k] = (1.0 - (double)c->fixku[k]) * c->c2czi[kp] * c->f2fzi[k];
+    }
+    for (ll j = 1; j <= n2m; j++) {
+        ll jp = c->jpv[j];
+        c->as[j] = (1.0 - (double)c->fixjl[j]) * c->c2cyi[j] * c->f2fyi[j];
+        c->an[j] = (1.0 - (double)c->fixju[j]) * c->c2cyi[jp] * c->f2fyi[j];
+    }
+    for (ll j = 1; j <= n2m; j++)
+        for (ll k = 1; k <= n3m; k++)
+            c->ac[XAC(c, k, j, 1)] = -1.0 * (c->ab[k] + c->af[k] + c->as[j] + c->an[j]);
+    double pi = acos(-1.0);
+    for (ll i = 1; i <= c->n1mh; i++)
+        c->ak1[i] = 2.0 * (1.0 - cos(2.0 * pi * (double)(i - 1) / (double)n1m)) * c->f2fxi[1] * c->f2fxi[1];
+    for (ll i = 2; i <= c->n1mh; i++)
+        for (ll j = 1; j <= n2m; j++)
+            for (ll k = 1; k <= n3m; k++) c->ac[XAC(c, k, j, i)] = c->ac[XAC(c, k, j, 1)] - c->ak1[i];
+}
+
+/* coefmg, poiss_x_ft.f90:644-794.  Without z periodicity the reference
+   leaves kpm/kmm unset; every coefficient that multiplies them there (ab at
+   a level's first point, af and coi2 at its last) is zero, so k+1 / k-1 are
+   used, which read finite work-array entries. */
+static void xft_coefmg(ref_case *c)
+{
+    ll n2m = c->n2m, n3m = c->n3m, n3md = c->n3md, nlev = c->c.nlev, n3 = c->n3;
+    ll minrow = n3m / (1LL << nlev);
+    double *zmpm = ref_zalloc((size_t)n3md + 2), *kbz = ref_zalloc((size_t)n3md + 2), *kfz = ref_zalloc((size_t)n3md + 2);
+    const double *z = c->z;
+    c->kkmg[nlev][0] = 1; c->kkmg[nlev][1] = n3m; c->kkmg[nlev][2] = n3m;
+    for (ll k = 1; k <= n3m; k++) {
+        zmpm[k] = c->zmp[k];
+        kbz[k] = (double)(1 - 1 / k);
+        kfz[k] = (double)(1 - k / n3m);
+    }
+    for (ll ilev = nlev - 1; ilev >= 0; ilev--) {
+        c->kkmg[ilev][0] = c->kkmg[ilev + 1][0] + c->kkmg[ilev + 1][2];
+        c->kkmg[ilev][2] = minrow * (1LL << ilev);
+        c->kkmg[ilev][1] = c->kkmg[ilev][0] + c->kkmg[ilev][2] - 1;
+        ll kbg = c->kkmg[ilev][0], kend = c->kkmg[ilev][1], ksp = 1LL << (nlev - ilev);
+        ll kc = 0;
+        for (ll k = kbg; k <= kend; k++) {
+            kc++;
+            zmpm[k] = 0.5 * (z[kc * ksp + 1] + z[(kc - 1) * ksp + 1]);
+            kbz[k] = (double)(1 - kbg / k);
+            kfz[k] = (double)(1 - k / kend);
+        }
+        kc = 0;
+        for (ll k = kbg; k <= kend; k++) {
+            kc++;
+            double w = z[kc * ksp + 1] - z[(kc - 1) * ksp + 1];
+            c->ab[k] = kbz[k] / ((zmpm[k] - zmpm[k - 1]) * w);
+            c->af[k] = kfz[k] / ((zmpm[k + 1] - zmpm[k]) * w);
+        }
+        for (ll j = 1; j <= n2m; j++)
+            for (ll k = kbg; k <= kend; k++)
+                c->ac[XAC(c, k, j, 1)] = -1.0 * (c->ab[k] + c->af[k] + c->as[j] + c->an[j]);
+        for (ll i = 2; i <= c->n1mh; i++)
+            for (ll j = 1; j <= n2m; j++)
+                for (ll k = kbg; k <= kend; k++) c->ac[XAC(c, k, j, i)] = c->ac[XAC(c, k, j, 1)] - c->ak1[i];
+    }
+    for (ll ilev = nlev; ilev >= 1; ilev--) {
+        ll kbgh = c->kkmg[ilev][0];
+        for (ll k = c->kkmg[ilev - 1][0]; k <= c->kkmg[ilev - 1][1]; k++) {
+            c->cor1[k] = (zmpm[kbgh + 1] - zmpm[k]) / (zmpm[kbgh + 1] - zmpm[kbgh]);
+            c->cor2[k] = 1.0 - c->cor1[k];
+            kbgh += 2;
+        }
+    }
+    for (ll ilev = 0; ilev <= nlev - 1; ilev++) {
+        ll kbgh = c->kkmg[ilev + 1][0] + 1;
+        for (ll k = c->kkmg[ilev][0]; k <= c->kkmg[ilev][1] - 1; k++) {
+            c->coi1[k] = (zmpm[k + 1] - zmpm[kbgh]) / (zmpm[k + 1] - zmpm[k]);
+            c->coi2[k] = 1.0 - c->coi1[k];
+            kbgh += 2;
+        }
+        c->coi1[c->kkmg[ilev][1]] = 1.0;
+    }
+    for (ll ilev = nlev; ilev >= 0; ilev--)
+        for (ll k = c->kkmg[ilev][0]; k <= c->kkmg[ilev][1]; k++) { c->kpm[k] = k + 1; c->kmm[k] = k - 1; }
+    if (c->c.zprdic == 1) {
+        for (ll ilev = nlev; ilev >= 0; ilev--) {
+            ll kbg = c->kkmg[ilev][0], kend = c->kkmg[ilev][1];
+            c->kpm[kend] = kbg;
+            c->kmm[kbg] = kend;
+        }
+        for (ll ilev = nlev - 1; ilev >= 0; ilev--) {
+            ll kbg = c->kkmg[ilev][0], kend = c->kkmg[ilev][1], ksp = 1LL << (nlev - ilev);
+            double vdz_kbg = zmpm[kbg] - z[1] + z[n3] - zmpm[kend];
+            double vdz_kend = zmpm[kbg] - z[1] + z[n3] - zmpm[kend];
+            double sdz_kbg = z[1 + ksp] - z[1], sdz_kend = z[n3] - z[n3 - ksp];
+            c->ab[kbg] = 1.0 / (vdz_kbg * sdz_kbg);
+            c->af[kend] = 1.0 / (vdz_kend * sdz_kend);
+        }
+        for (ll ilev = nlev - 1; ilev >= 0; ilev--) {
+            for (ll j = 1; j <= n2m; j++)
+                for (ll k = c->kkmg[ilev][0]; k <= c->kkmg[ilev][1]; k++)
+                    c->ac[XAC(c, k, j, 1)] = -1.0 * (c->ab[k] + c->af[k] + c->as[j] + c->an[j]);
+            for (ll i = 2; i <= c->n1mh; i++)
+                for (ll j = 1; j <= n2m; j++)
+                    for (ll k = c->kkmg[ilev][0]; k <= c->kkmg[ilev][1]; k++)
+                        c->ac[XAC(c, k, j, i)] = c->ac[XAC(c, k, j, 1)] - c->ak1[i];
+        }
+        for (ll ilev = 0; ilev <= nlev - 1; ilev++) {
+            ll kbg = c->kkmg[ilev][0], kend = c->kkmg[ilev][1];
+            double vdz_kend = zmpm[kbg] - z[1] + z[n3] - zmpm[kend];
+            c->coi2[kend] = (zmpm[c->kkmg[ilev + 1][1]] - zmpm[kend]) / vdz_kend;
+            c->coi1[kend] = 1.0 - c->coi2[kend];
+        }
+    }
+    free(zmpm); free(kbz); free(kfz);
+}
+
+/* poisinit, poiss_x_ft.f90:18-52 */
+static int xft_init(ref_case *c)
+{
+    ll n3md = c->n3md, n2m = c->n2m, n1mh = c->n1mh, nlev = c->c.nlev;
+    if (c->c.xprdic != 1) return LESGPU_ERR_CONFIG;                 /* the x transform needs periodic x */
+    if (nlev < 1 || nlev > 20 || c->n3m % (1LL << nlev) != 0) return LESGPU_ERR_CONFIG;
+    if (ref_fft_plan_init(&c->fftx, (int)c->n1m)) return LESGPU_ERR_ARG;
+    size_t nv = (size_t)n3md + 2, na = (size_t)n3md * (size_t)n2m * (size_t)n1mh;
+    c->ab = ref_zalloc(nv); c->af = ref_zalloc(nv);
+    c->as = ref_zalloc((size_t)n2m + 2); c->an = ref_zalloc((size_t)n2m + 2);
+    c->coi1 = ref_zalloc(nv); c->coi2 = ref_zalloc(nv); c->cor1 = ref_zalloc(nv); c->cor2 = ref_zalloc(nv);
+    c->kpm = ref_izalloc(nv); c->kmm = ref_izalloc(nv);
+    c->ak1 = ref_zalloc((size_t)n1mh + 2);
+    c->ac = ref_zalloc(na); c->gam = ref_zalloc(na); c->bet = ref_zalloc(na);
+    xft_pmat(c);
+    xft_coefmg(c);
+    for (ll ilev = 0; ilev <= nlev; ilev++)
+        for (ll i = 1; i <= n1mh; i++) {
+            for (ll k = c->kkmg[ilev][0]; k <= c->kkmg[ilev][1]; k++) c->bet[XAC(c, k, 1, i)] = 1.0 / c->ac[XAC(c, k, 1, i)];
+            for (ll j = 2; j <= n2m; j++)
+                for (ll k = c->kkmg[ilev][0]; k <= c->kkmg[ilev][1]; k++) {
+                    c->gam[XAC(c, k, j, i)] = c->an[j - 1] * c->bet[XAC(c, k, j - 1, i)];
+                    c->bet[XAC(c, k, j, i)] = 1.0 / (c->ac[XAC(c, k, j, i)] - c->as[j] * c->gam[XAC(c, k, j, i)]);
+                }
+        }
+    return 0;
+}
+
+/* trdiag1m, poiss_x_ft.f90:373-398: y-Thomas on z-lines l1, l1+2, ..., l2 (in place) */
+static void xft_trdiag(const ref_case *c, zmode *z, ll l1, ll l2, ll iv)
+{
+    ll n2m = c->n2m;
+    for (ll k = l1; k <= l2; k += 2) {
+        double b = c->bet[XAC(c, k, 1, iv)];
+        GG(z, k, 1).re *= b; GG(z, k, 1).im *= b;
+    }
+    for (ll j = 2; j <= n2m; j++)
+        for (ll k = l1; k <= l2; k += 2) {
+            double b = c->bet[XAC(c, k, j, iv)];
+            cplx t = cx_axpy(GG(z, k, j), c->as[j], GG(z, k, j - 1));
+            GG(z, k, j).re = t.re * b; GG(z, k, j).im = t.im * b;
+        }
+    for (ll j = n2m - 1; j >= 1; j--)
+        for (ll k = l1; k <= l2; k += 2)
+            GG(z, k, j) = cx_axpy(GG(z, k, j), c->gam[XAC(c, k, j + 1, iv)], GG(z, k, j + 1));
+}
+
+/* rhs - ab*g(kmm) - af*g(kpm) - as*g(j-1) - an*g(j+1) - ac*g */
+static inline cplx xft_defect(const ref_case *c, cplx r, const cplx *g, ll ld, ll k, ll j, ll iv)
+{
+    const cplx *gm = &g[(size_t)c->kmm[k] + (size_t)ld * (size_t)j], *gp = &g[(size_t)c->kpm[k] + (size_t)ld * (size_t)j];
+    const cplx *gs = &g[(size_t)k + (size_t)ld * (size_t)(j - 1)], *gn = &g[(size_t)k + (size_t)ld * (size_t)(j + 1)];
+    const cplx *gc = &g[(size_t)k + (size_t)ld * (size_t)j];
+    double ac = c->ac[XAC(c, k, j, iv)];
+    r = cx_axpy(r, c->ab[k], *gm);
+    r = cx_axpy(r, c->af[k], *gp);
+    r = cx_axpy(r, c->as[j], *gs);
+    r = cx_axpy(r, c->an[j], *gn);
+    r = cx_axpy(r, ac, *gc);
+    return r;
+}
+
+/* rhs - f*(ab*u(kmm) + af*u(kpm)) on the lines k0, k0+2, ..., k1 of the level */
+static void xft_line_rhs(const ref_case *c, zmode *z, const cplx *u, ll ldu, int from_rhs, ll k0, ll k1, double f)
+{
+    for (ll j = 1; j <= c->n2m; j++)
+        for (ll k = k0; k <= k1; k += 2) {
+            cplx um = u[(size_t)c->kmm[k] + (size_t)ldu * (size_t)j], up = u[(size_t)c->kpm[k] + (size_t)ldu * (size_t)j];
+            cplx r = from_rhs ? RH(z, k, j) : RS(z, k, j);
+            double sre = c->ab[k] * um.re + c->af[k] * up.re, sim = c->ab[k] * um.im + c->af[k] * up.im;
+            GG(z, k, j).re = r.re - f * sre;
+            GG(z, k, j).im = r.im - f * sim;
+        }
+}
+
+/* toplevel, poiss_x_ft.f90:296-371 (zebra version) */
+static void xft_toplevel(const ref_case *c, zmode *z, int id, double *sumres, double oldv, double test, ll iv)
+{
+    ll n3m = c->n3m, n2m = c->n2m, nlev = c->c.nlev;
+    if (id == 1) {
+        ll kc = 0;
+        for (ll k = c->kkmg[nlev - 1][0]; k <= c->kkmg[nlev - 1][1]; k++) {
+            kc += 2;
+            for (ll j = 1; j <= n2m; j++) {
+                cplx p = PC(z, kc, j), a = GG(z, k, j), b = GG(z, c->kpm[k], j);
+                p.re = p.re + c->coi1[k] * a.re + c->coi2[k] * b.re;
+                p.im = p.im + c->coi1[k] * a.im + c->coi2[k] * b.im;
+                PC(z, kc, j) = p;
+            }
+        }
+    }
+    xft_line_rhs(c, z, z->pc, z->ld_p, 1, 1, n3m, oldv);
+    xft_trdiag(c, z, 1, n3m, iv);
+    if (iv == 1) {
+        cplx tt = GG(z, 1, n2m);
+        for (ll j = 1; j <= n2m; j++)
+            for (ll k = 1; k <= n3m; k += 2) { GG(z, k, j).re -= tt.re; GG(z, k, j).im -= tt.im; }
+    }
+    xft_line_rhs(c, z, z->gg, z->ld_g, 1, 2, n3m, 1.0);
+    xft_trdiag(c, z, 2, n3m, iv);
+    double sr = 0.0;
+    for (ll j = 1; j <= n2m; j++)
+        for (ll k = 1; k <= n3m; k++) {
+            cplx d = xft_defect(c, RH(z, k, j), z->gg, z->ld_g, k, j, iv);
+            RS(z, k, j) = d;
+            double a = hypot(d.re, d.im);
+            if (a > sr) sr = a;
+            PC(z, k, j) = GG(z, k, j);
+        }
+    *sumres = sr;
+    if (sr < test || id == 2) return;
+    ll kc = -1;
+    for (ll k = c->kkmg[nlev - 1][0]; k <= c->kkmg[nlev - 1][1]; k++) {
+        kc += 2;
+        for (ll j = 1; j <= n2m; j++) {
+            cplx a = RS(z, kc, j), b = RS(z, kc + 1, j);
+            RS(z, k, j).re = a.re * c->cor1[k] + b.re * c->cor2[k];
+            RS(z, k, j).im = a.im * c->cor1[k] + b.im * c->cor2[k];
+        }
+    }
+}
+
+/* relax, poiss_x_ft.f90:450-495 (zebra version): the first pass scales the
+   odd lines' neighbours by oldv; the even lines and later passes do not */
+static void xft_relax(const ref_case *c, zmode *z, ll ilev, double oldv, ll iiter, ll iv)
+{
+    ll n2m = c->n2m, kbg = c->kkmg[ilev][0], kend = c->kkmg[ilev][1];
+    for (ll it = 0; it < iiter; it++) {
+        xft_line_rhs(c, z, z->gg, z->ld_g, 0, kbg, kend, it == 0 ? oldv : 1.0);
+        xft_trdiag(c, z, kbg, kend, iv);
+        for (ll j = 1; j <= n2m; j++)
+            for (ll k = kbg + 1; k <= kend; k += 2) {
+                cplx gm = GG(z, c->kmm[k], j), gp = GG(z, c->kpm[k], j), r = RS(z, k, j);
+                GG(z, k, j).re = r.re - c->ab[k] * gm.re - c->af[k] * gp.re;
+                GG(z, k, j).im = r.im - c->ab[k] * gm.im - c->af[k] * gp.im;
+            }
+        xft_trdiag(c, z, kbg + 1, kend, iv);
+    }
+}
+
+/* godown, poiss_x_ft.f90:422-447: residual of level ilev, restricted to ilev-1 */
+static void xft_godown(const ref_case *c, zmode *z, ll ilev, ll iv)
+{
+    ll n2m = c->n2m;
+    for (ll j = 1; j <= n2m; j++)
+        for (ll k = c->kkmg[ilev][0]; k <= c->kkmg[ilev][1]; k++)
+            RS(z, k, j) = xft_defect(c, RS(z, k, j), z->gg, z->ld_g, k, j, iv);
+    ll kbg = c->kkmg[ilev][0] - 2;
+    for (ll k = c->kkmg[ilev - 1][0]; k <= c->kkmg[ilev - 1][1]; k++) {
+        kbg += 2;
+        for (ll j = 1; j <= n2m; j++) {
+            cplx a = RS(z, kbg, j), b = RS(z, kbg + 1, j);
+            RS(z, k, j).re = a.re * c->cor1[k] + b.re * c->cor2[k];
+            RS(z, k, j).im = a.im * c->cor1[k] + b.im * c->cor2[k];
+        }
+    }
+}
+
+/* goup, poiss_x_ft.f90:401-419: coarse correction onto the even lines of
+   ilev+1, every coarse point through coi1 and coi2 (the last one's coi2 is
+   the periodic weight, or zero) */
+static void xft_goup(const ref_case *c, zmode *z, ll ilev)
+{
+    ll n2m = c->n2m, kbgh = c->kkmg[ilev + 1][0] - 1;
+    for (ll k = c->kkmg[ilev][0]; k <= c->kkmg[ilev][1]; k++) {
+        kbgh += 2;
+        for (ll j = 1; j <= n2m; j++) {
+            cplx g = GG(z, kbgh, j), a = GG(z, k, j), b = GG(z, c->kpm[k], j);
+            GG(z, kbgh, j).re = g.re + c->coi1[k] * a.re + c->coi2[k] * b.re;
+            GG(z, kbgh, j).im = g.im + c->coi1[k] * a.im + c->coi2[k] * b.im;
+        }
+    }
+}
+
+/* mg2d, poiss_x_ft.f90:238-294; returns the number of V-cycles */
+static ll xft_mg2d(const ref_case *c, zmode *z, ll iv, double test, double oldv)
+{
+    ll nlev = c->c.nlev;
+    double sumres;
+    xft_toplevel(c, z, 0, &sumres, oldv, test, iv);
+    if (sumres < test) return 0;
+    for (ll ii = 1; ii <= c->c.mgitr; ii++) {
+        for (ll ilev = nlev - 1; ilev >= 1; ilev--) {
+            xft_relax(c, z, ilev, 0.0, 1, iv);
+            xft_godown(c, z, ilev, iv);
+        }
+        xft_relax(c, z, 0, 0.0, c->c.nbli, iv);
+        for (ll ilev = 0; ilev <= nlev - 2; ilev++) {
+            xft_goup(c, z, ilev);
+            xft_relax(c, z, ilev + 1, 1.0, 1, iv);
+        }
+        xft_toplevel(c, z, 1, &sumres, 1.0, test, iv);
+        if (sumres < test) return ii;
+    }
+    return c->c.mgitr;   /* iteration limit (the reference prints a warning and goes on) */
+}
+
+/* resid3, poiss_x_ft.f90:620-642 */
+static double xft_resid3(const ref_case *c, zmode *z, ll iv)
+{
+    double e = 0.0;
+    for (ll j = 1; j <= c->n2m; j++)
+        for (ll k = 1; k <= c->n3m; k++) {
+            cplx d = xft_defect(c, RH(z, k, j), z->pc, z->ld_p, k, j, iv);
+            double a = hypot(d.re, d.im);
+            if (a > e) e = a;
+        }
+    return e;
+}
+
+/* gsor2d, poiss_x_ft.f90:497-617: zebra line SOR on pc (= u); the zero
+   wavenumber's odd lines are shifted by u(1,n2m) after their update */
+static ll xft_gsor2d(const ref_case *c, zmode *z, ll iv, double test, double oldv)
+{
+    ll n3m = c->n3m, n2m = c->n2m;
+    double ww = c->c.wwsor, ww2 = 1.0 - ww;
+    for (ll ii = 0; ii <= c->c.mgitr; ii++) {
+        double ov = ii == 0 ? oldv : 1.0, o2 = ii == 0 ? oldv * ww2 : ww2;
+        for (int half = 0; half < 2; half++) {
+            ll k0 = half == 0 ? 1 : 2;
+            xft_line_rhs(c, z, z->pc, z->ld_p, 1, k0, n3m, half == 0 ? ov : 1.0);
+            xft_trdiag(c, z, k0, n3m, iv);
+            for (ll j = 1; j <= n2m; j++)
+                for (ll k = k0; k <= n3m; k += 2) {
+                    PC(z, k, j).re = ww * GG(z, k, j).re + o2 * PC(z, k, j).re;
+                    PC(z, k, j).im = ww * GG(z, k, j).im + o2 * PC(z, k, j).im;
+                }
+            if (half == 0 && iv == 1) {
+                cplx tt = PC(z, 1, n2m);
+                for (ll j = 1; j <= n2m; j++)
+                    for (ll k = 1; k <= n3m; k += 2) { PC(z, k, j).re -= tt.re; PC(z, k, j).im -= tt.im; }
+            }
+        }
+        if (xft_resid3(c, z, iv) < test) return ii;
+    }
+    return c->c.mgitr;
+}
+
+/* poisson, poiss_x_ft.f90:115-235 */
+static void xft_poisson(ref_case *c)
+{
+    ll n1m = c->n1m, n2m = c->n2m, n3m = c->n3m, n3 = c->n3, n2 = c->n2, n1mh = c->n1mh, n3md = c->n3md;
+    ll ld_p = n3 + 1, ld_g = n3md + 1;
+    size_t np = (size_t)ld_p * (size_t)(n2 + 1), ng = (size_t)ld_g * (size_t)(n2 + 1);
+    cplx *ccap = (cplx *)calloc(np * (size_t)n1mh, sizeof(cplx));
+    ll itmax = 0;
+    #pragma omp parallel
+    {
+        cplx *line = (cplx *)malloc(sizeof(cplx) * (size_t)n1m), *wk = (cplx *)malloc(sizeof(cplx) * 2 * (size_t)n1m);
+        #pragma omp for
+        for (ll j = 1; j <= n2m; j++)
+            for (ll k = 1; k <= n3m; k++) {
+                for (ll i = 1; i <= n1m; i++) { line[i - 1].re = c->divgsum[IX(c, i, j, k)]; line[i - 1].im = 0.0; }
+                ref_fft(&c->fftx, line, wk, -1);
+                for (ll i = 1; i <= n1mh; i++) ccap[(size_t)k + (size_t)ld_p * (size_t)j + np * (size_t)(i - 1)] = line[i - 1];
+            }
+        free(line); free(wk);
+    }
+    double test = c->test1 / (double)n1mh * (double)n1m * 0.9;
+    #pragma omp parallel reduction(max:itmax)
+    {
+        zmode z;
+        z.ld_p = ld_p; z.ld_g = ld_g;
+        z.pc = (cplx *)malloc(sizeof(cplx) * np);
+        z.resd = (cplx *)malloc(sizeof(cplx) * ng);
+        z.gg = (cplx *)malloc(sizeof(cplx) * ng);
+        #pragma omp for schedule(dynamic, 1)
+        for (ll iii = 1; iii <= n1mh; iii++) {
+            z.rhs = ccap + np * (size_t)(iii - 1);
+            memset(z.pc, 0, sizeof(cplx) * np);
+            memset(z.resd, 0, sizeof(cplx) * ng);
+            memset(z.gg, 0, sizeof(cplx) * ng);
+            ll it = iii <= c->c.imgsor ? xft_mg2d(c, &z, iii, test, 0.0) : xft_gsor2d(c, &z, iii, test, 0.0);
+            if (it > itmax) itmax = it;
+            for (ll j = 1; j <= n2m; j++)
+                for (ll k = 1; k <= n3m; k++) z.rhs[(size_t)k + (size_t)ld_p * (size_t)j] = PC(&z, k, j);
+        }
+        free(z.pc); free(z.resd); free(z.gg);
+    }
+    #pragma omp parallel
+    {
+        cplx *line = (cplx *)malloc(sizeof(cplx) * (size_t)n1m), *wk = (cplx *)malloc(sizeof(cplx) * 2 * (size_t)n1m);
+        #pragma omp for
+        for (ll j = 1; j <= n2m; j++)
+            for (ll k = 1; k <= n3m; k++) {
+                for (ll i = 1; i <= n1mh; i++) line[i - 1] = ccap[(size_t)k + (size_t)ld_p * (size_t)j + np * (size_t)(i - 1)];
+                for (ll i = n1mh + 1; i <= n1m; i++) {
+                    cplx s = ccap[(size_t)k + (size_t)ld_p * (size_t)j + np * (size_t)(n1m + 2 - i - 1)];
+                    s.im = -s.im;
+                    line[i - 1] = s;
+                }
+                ref_fft(&c->fftx, line, wk, 1);
+                for (ll i = 1; i <= n1m; i++) c->phi[IX(c, i, j, k)] = line[i - 1].re;
+            }
+        free(line); free(wk);
+    }
+    free(ccap);
+    if (c->c.ich == 1) {   /* the f2fx-weighted mean of phi(:,n2m,1) becomes zero */
+        double phiref = 0.0;
+        for (ll i = 1; i <= n1m; i++) phiref = phiref + c->phi[IX(c, i, n2m, 1)] * c->f2fx[i];
+        phiref = phiref / c->xl;
+        for (ll k = 1; k <= n3m; k++)
+            for (ll j = 1; j <= n2m; j++)
+                for (ll i = 1; i <= n1m; i++) c->phi[IX(c, i, j, k)] = c->phi[IX(c, i, j, k)] - phiref;
+    }
+    c->poisson_iters[c->msub >= 1 && c->msub <= 3 ? c->msub - 1 : 0] = itmax;
+}
+
 /* ------------------------------------------------------------ mgrd ---- */
 /* BiCGSTAB with a one-V-cycle MG3D preconditioner (poiss_mgrd.f90).  The
    levels are laid side by side along x and along z as in the reference
@@ -1106,6 +1543,8 @@ int ref_poisinit(ref_case *c)
         return zft_init(c);
     case LESGPU_POISSON_MGRD:
         return mgrd_init(c);
+    case LESGPU_POISSON_X_FT:
+        return xft_init(c);
     default:
         return LESGPU_ERR_UNSUPPORTED;
     }
@@ -1117,6 +1556,7 @@ void ref_poisson(ref_case *c)
     case LESGPU_POISSON_FTFT: ftft_poisson(c); break;
     case LESGPU_POISSON_Z_FT: zft_poisson(c); break;
     case LESGPU_POISSON_MGRD: mgrd_poisson(c); break;
+    case LESGPU_POISSON_X_FT: xft_poisson(c); break;
     default: break;
     }
 }
