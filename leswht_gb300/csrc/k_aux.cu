@@ -98,7 +98,7 @@ void launch_substepinit(lesgpu_case *c, int msub) { k_substepinit<<<1, 1, 0, c->
 struct QvolTerm {   // qvolcalc, slv_auxi.f90:126-149
     __device__ void operator()(const KP &p, int i, int j, int k, double *w) const {
         long long q = p.g.ix(i, j, k);
-        w[0] = (p.f.fb_u[q] >= 1.0e-10) ? p.f.u[q] * p.g.c2cx[i] * p.g.f2fy[j] * p.g.f2fz[k] : 0.0;
+        w[0] = p.f.u[q] * p.f.wq[q];     // u c2cx f2fy f2fz over the fluid u points
     }
 };
 struct QvolFinal {
@@ -110,7 +110,7 @@ void launch_qvolcalc(lesgpu_case *c, int slot) { reduce<1, false>(c, interior(c-
 struct TvolTerm {   // tvolcalc, slv_auxi.f90:152-173
     __device__ void operator()(const KP &p, int i, int j, int k, double *w) const {
         long long q = p.g.ix(i, j, k);
-        w[0] = p.f.t[q] / p.f.cstar[q] * p.g.f2fx[i] * p.g.f2fy[j] * p.g.f2fz[k];
+        w[0] = p.f.t[q] * p.f.wt[q];     // t / c* f2fx f2fy f2fz
     }
 };
 struct TvolFinal {
@@ -119,12 +119,33 @@ struct TvolFinal {
 };
 void launch_tvolcalc(lesgpu_case *c, int slot) { reduce<1, false>(c, interior(c->kp.g), TvolTerm{}, TvolFinal{slot}); }
 
+// Weights of the volume reductions: the cell-volume products and fluid masks
+// of qvolcalc / meanpg (fb_u), the bulk velocity (fb_c) and tvolcalc (1/c*),
+// formed once so each reduction does one multiply per cell.
+__global__ void k_red_weights(KP p, Box b) {
+    const DGrid &g = p.g;
+    const long long n = b.count();
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        b.at(t, i, j, k);
+        const long long q = g.ix(i, j, k);
+        const double cv = g.c2cx[i] * g.f2fy[j] * g.f2fz[k];
+        p.f.wq[q] = p.f.fb_u[q] >= 1.0e-10 ? cv : 0.0;
+        p.f.wb[q] = p.f.fb_c[q] >= 1.0e-10 ? cv : 0.0;
+        p.f.wt[q] = g.f2fx[i] * g.f2fy[j] * g.f2fz[k] / p.f.cstar[q];
+    }
+}
+void launch_red_weights(lesgpu_case *c) {
+    Box b = interior(c->kp.g);
+    k_red_weights<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b);
+}
+
 // tvolcorr, slv_auxi.f90:206-230.  The volume integral of 1/c* does not
 // change in time; it is reduced once (lesgpu_start) into S->cvol.
 struct CvolTerm {
     __device__ void operator()(const KP &p, int i, int j, int k, double *w) const {
         long long q = p.g.ix(i, j, k);
-        w[0] = 1.0 / p.f.cstar[q] * p.g.f2fx[i] * p.g.f2fy[j] * p.g.f2fz[k];
+        w[0] = p.f.wt[q];                // 1 / c* f2fx f2fy f2fz
     }
 };
 struct CvolFinal {
@@ -158,12 +179,13 @@ struct MeanpgTerm {
         const DCfg &c = p.c;
         const double *u = p.f.u;
         long long q = g.ix(i, j, k);
-        bool fl = p.f.fb_u[q] >= 1.0e-10;
-        double vol = g.c2cx[i] * g.f2fy[j] * g.f2fz[k];
-        w[0] = fl ? vol : 0.0;
-        w[1] = fl ? u[q] * g.c2cx[i] * g.f2fy[j] * g.f2fz[k] : 0.0;
+        const double vol = p.f.wq[q];    // c2cx f2fy f2fz over the fluid u points, else 0
+        w[0] = vol;
+        w[1] = u[q] * vol;
         w[2] = w[3] = w[4] = w[5] = 0.0;
-        if (fl) {
+        const bool wall = (j == 1 && c.bc_ybtm == 0) || (j == g.n2m && c.bc_ytop == 0) ||
+                          (k == 1 && c.bc_zbtm == 0) || (k == g.n3m && c.bc_ztop == 0);
+        if (wall && p.f.fb_u[q] >= 1.0e-10) {
             if (c.bc_ybtm == 0 && j == 1) {
                 double dy1 = 1.0 / g.c2cyi[1], dy2 = dy1 + 1.0 / g.c2cyi[2];
                 double gu = (u[q] * (dy2 * dy2) - u[q + g.sx] * (dy1 * dy1)) / (dy1 * dy2 * (dy2 - dy1));
@@ -345,12 +367,14 @@ struct PhirefFinal {
 __global__ void __launch_bounds__(kThreads) k_pcalc(KP p, Box b) {
     long long n = b.count();
     const DGrid &g = p.g;
-    double dtc = p.S->dtconst, phiref = p.S->phiref, re = p.c.re;
+    // 1/re (formed once) in place of a per-cell division: an FP64 division
+    // is some ten operations on the narrow FP64 pipe
+    double dtc = p.S->dtconst, phiref = p.S->phiref, rei = p.c.rei_d;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         b.at(t, i, j, k);
         long long q = g.ix(i, j, k);
-        double pn = p.f.p[q] + p.f.phi[q] - 0.5 * dtc * p.f.divgsum[q] * 1.0 / re;
+        double pn = p.f.p[q] + p.f.phi[q] - 0.5 * dtc * p.f.divgsum[q] * rei;
         p.f.p[q] = pn - phiref;
     }
 }

@@ -8,17 +8,10 @@ namespace lg {
 
 struct UbulkTerm {
     __device__ void operator()(const KP &p, int i, int j, int k, double *w) const {
-        const DGrid &g = p.g;
-        long long q = g.ix(i, j, k);
-        if (p.f.fb_c[q] >= 1.0e-10) {
-            double cv = g.c2cx[i] * g.f2fy[j] * g.f2fz[k];
-            double ucc = 0.5 * (p.f.u[q] + p.f.u[q + 1]);
-            w[0] = cv;
-            w[1] = ucc * cv;
-        } else {
-            w[0] = 0.0;
-            w[1] = 0.0;
-        }
+        const long long q = p.g.ix(i, j, k);
+        const double cv = p.f.wb[q];     // c2cx f2fy f2fz over the fluid cells, else 0
+        w[0] = cv;
+        w[1] = 0.5 * (p.f.u[q] + p.f.u[q + 1]) * cv;
     }
 };
 struct UbulkFinal {

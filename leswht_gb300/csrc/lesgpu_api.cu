@@ -255,6 +255,7 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
                 }
         f.fb_u = upload(A, fbu.data(), nt);
         f.fb_c = upload(A, fbc.data(), nt);
+        f.wq = A.get<double>(nt); f.wb = A.get<double>(nt); f.wt = A.get<double>(nt);
         // face points of heatflux (slv_auxi.f90:573-663)
         size_t nxz = (size_t)(d.n1 + 1) * (d.n3 + 1), nxy = (size_t)(d.n1 + 1) * (d.n2 + 1);
         std::vector<double> vb(nxz, 0.0), vt(nxz, 0.0), wb(nxy, 0.0), wt(nxy, 0.0);
@@ -398,6 +399,7 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
     for (long long i = 0; i <= d.n1; i++) c->h_f2fx[i] = g->f2fxi[i];
     for (long long kk = 0; kk <= d.n3; kk++) c->h_f2fz[kk] = g->f2fzi[kk];
     if (!A.ok) { lesgpu_destroy(c); return LESGPU_ERR_OOM; }
+    launch_red_weights(c);
     c->h_grid = g;
     rc = poisson_init(c);
     c->h_grid = nullptr;
@@ -497,6 +499,7 @@ extern "C" int lesgpu_load_ibm(lesgpu_case *c, const lesgpu_ibm *b) {
     if (b->kstar)
         for (int l = 0; l < 6; l++) scatter_d(b->kstar + (size_t)l * ncell, f.kstar[l]);
     if (!A.ok) return LESGPU_ERR_OOM;
+    launch_red_weights(c);
     launch_mirror(c, kMirConj);
     return cuda_rc(cudaDeviceSynchronize());
 }

@@ -87,6 +87,10 @@ struct DFields {
     double *cstar, *kstar[6];
     int *omega, *nwall;
     double *fb_u, *fb_c;
+    // per-cell weights of the volume reductions, formed once (k_red_weights):
+    // wq = c2cx f2fy f2fz where fb_u >= 1e-10 (flow rate), wb the same where
+    // fb_c >= 1e-10 (bulk velocity), wt = f2fx f2fy f2fz / c* (temperature)
+    double *wq, *wb, *wt;
     // body function on the y faces (xmp_i, y_1 | y_n2, zmp_k) and the z faces
     // (xmp_i, ymp_j, z_1 | z_n3), planes indexed i + (n1+1) * (k | j)
     double *fb_vb, *fb_vt, *fb_wb, *fb_wt;
@@ -171,11 +175,39 @@ constexpr unsigned kMirVel = kMirU | kMirV | kMirW;
 // ------------------------------------------------------------------ helpers
 __device__ __forceinline__ double fixd(int v) { return (double)v; }
 
+// Division of 0 <= n < 2^31 by an invariant d >= 1 as a multiply and a shift
+// (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994, theorem 4.2 with N = 31): l = ceil(log2 d),
+// m = ceil(2^(31+l) / d) <= 2^32, n / d = (n m) >> (31 + l), n m < 2^63.
+// A 64-bit integer division costs a GPU thread some sixty instructions.
+struct IDiv {
+    unsigned long long m;
+    int s;
+    LG_HD static IDiv make(int d) {
+        int l = 0;
+        while (l < 31 && (1LL << l) < (long long)d) l++;
+        const int s = 31 + l;
+        const unsigned long long dd = d > 0 ? (unsigned long long)d : 1ULL;
+        return IDiv{((1ULL << s) + dd - 1ULL) / dd, s};
+    }
+    LG_HD unsigned div(unsigned n) const { return (unsigned)(((unsigned long long)n * m) >> s); }
+};
+
 // Decode a linear thread index over the interior box [i0..i1]x[j0..j1]x[k0..k1].
+// Boxes of fewer than 2^31 points (every grid that fits in memory) decode
+// with two multiply-shift divisions; larger ones fall back to 64-bit division.
 struct Box {
     int i0, j0, k0, ni, nj, nk;
+    IDiv di = IDiv::make(ni), dj = IDiv::make(nj);
     LG_HD long long count() const { return (long long)ni * nj * nk; }
     LG_HD void at(long long t, int &i, int &j, int &k) const {
+        if (t < (1LL << 31)) {
+            const unsigned t32 = (unsigned)t, r = di.div(t32), kk = dj.div(r);
+            i = i0 + (int)(t32 - r * (unsigned)ni);
+            j = j0 + (int)(r - kk * (unsigned)nj);
+            k = k0 + (int)kk;
+            return;
+        }
         i = i0 + (int)(t % ni);
         long long r = t / ni;
         j = j0 + (int)(r % nj);
@@ -318,8 +350,14 @@ __global__ void __launch_bounds__(kThreads) k_reduce_fin(KP p, Box b, F f, G g) 
         b.at(t, i, j, k);
         double w[NV];
         f(p, i, j, k, w);
+        // a sum skips exact +0 terms (integer test): FP64 adds issue on the
+        // narrow FP64 pipe, and several reductions carry terms that are zero
+        // almost everywhere (the wall-shear sums of meanpg)
 #pragma unroll
-        for (int q = 0; q < NV; q++) v[q] = MAX ? fmax(v[q], w[q]) : v[q] + w[q];
+        for (int q = 0; q < NV; q++) {
+            if (MAX) v[q] = fmax(v[q], w[q]);
+            else if (__double_as_longlong(w[q]) != 0LL) v[q] = v[q] + w[q];
+        }
     }
     block_reduce<NV, MAX>(v);
     if (threadIdx.x == 0) {
@@ -374,5 +412,7 @@ int adi_tuned(const lesgpu_case *c, int *out, int maxn);
 // cap on the z_ft multigrid's cluster size for cases created by this thread (0 = none)
 void set_mg_cluster_cap(int cap);
 void launch_cvol(lesgpu_case *c);
+// the reduction weights (DFields wq, wb, wt); after fb_u/fb_c or c* change
+void launch_red_weights(lesgpu_case *c);
 void launch_rhs_t_kernel(lesgpu_case *c, int msub);
 }  // namespace lg
