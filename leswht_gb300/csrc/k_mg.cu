@@ -44,16 +44,34 @@ constexpr int kMaxLev = 20;
 
 int mg_cluster_cap();
 
+template <class T> struct V2;
+template <> struct V2<double> {
+    using t = double2;
+    __host__ __device__ static double2 mk(double x, double y) { return make_double2(x, y); }
+};
+template <> struct V2<float> {
+    using t = float2;
+    __host__ __device__ static float2 mk(float x, float y) { return make_float2(x, y); }
+};
+
+// Coefficient tables and per-mode work arrays of one arithmetic type.
+template <class T>
+struct MgSet {
+    T *aw, *ae, *as, *an, *coi1, *coi2, *cor1, *cor2;   // 1-based
+    T *ac, *bet, *gam;          // (i-1) + nld*((j-1) + n2m*(kv-1))
+    typename V2<T>::t *pc, *gg, *rs;
+};
+
 struct MgTables {
     int nl, nld, nlev;          // cells along the semi-coarsened direction, 2 nl, levels
     int nmodes, xft;            // modes solved (n3mh / n1mh); 1 for poiss_x_ft
+    int mixed;                  // FP32 cycles under an FP64 defect correction
     int cs;                     // blocks per cluster (one cluster per z mode)
     int cap;                    // cap on cs set by the creator (0 = none)
     int iimg[kMaxLev + 1][3];
-    double *aw, *ae, *as, *an, *coi1, *coi2, *cor1, *cor2;   // 1-based
     int *ipm, *imm;
-    double *ac, *bet, *gam;     // (i-1) + nld*((j-1) + n2m*(kv-1))
-    double2 *pc, *gg, *rs;      // per-mode work arrays
+    MgSet<double> d;            // FP64 tables and work arrays
+    MgSet<float> f;             // their FP32 copies (mixed form)
     long long *iters;           // per mode, last solve
     long long pc_plane, gg_plane;
 };
@@ -61,13 +79,14 @@ struct MgTables {
 struct MgArgs {
     int nl, n2m, nld, nlev, nbli, mgitr, imgsor;
     int xft;                    // poiss_x_ft's pinning and prolongation
+    int mixed;
     double wwsor;
     int ldp, ldg;
     int iimg[kMaxLev + 1][3];
-    const double *aw, *ae, *as, *an, *coi1, *coi2, *cor1, *cor2;
     const int *ipm, *imm;
-    const double *ac, *bet, *gam;
-    double2 *ccap, *pc, *gg, *rs;
+    MgSet<double> d;
+    MgSet<float> f;
+    double2 *ccap;
     long long pc_plane, gg_plane;
     long long *iters;
     DScal *S;
@@ -79,31 +98,38 @@ struct MgArgs {
 // One z mode is solved by one thread-block cluster; `tid`/`nt` number the
 // threads of the whole cluster and sync() is the cluster barrier (release /
 // acquire at cluster scope, so global writes of a phase are visible to every
-// block of the cluster in the next phase).
-struct Mode {
+// block of the cluster in the next phase).  ModeT<T> views the mode's tables
+// and work arrays of arithmetic type T.
+template <class T>
+struct ModeT {
+    using V = typename V2<T>::t;
     const MgArgs &a;
+    const MgSet<T> &s;
     int kv;
     int tid, nt;                        // thread index / count over the cluster
-    double2 *pc, *gg, *rs;
+    V *pc, *gg, *rs;
     const double2 *rhs;                 // ccap plane of the mode, (i-1) + nl*(j-1)
     size_t cb;                          // coefficient base of the mode
     __device__ void sync() const { cooperative_groups::this_cluster().sync(); }
-    __device__ Mode(const MgArgs &a_, int kv_, int tid_, int nt_) : a(a_), kv(kv_), tid(tid_), nt(nt_) {
-        pc = a.pc + a.pc_plane * (kv - 1);
-        gg = a.gg + a.gg_plane * (kv - 1);
-        rs = a.rs + a.gg_plane * (kv - 1);
+    __device__ ModeT(const MgArgs &a_, const MgSet<T> &s_, int kv_, int tid_, int nt_)
+        : a(a_), s(s_), kv(kv_), tid(tid_), nt(nt_) {
+        pc = s.pc + a.pc_plane * (kv - 1);
+        gg = s.gg + a.gg_plane * (kv - 1);
+        rs = s.rs + a.gg_plane * (kv - 1);
         rhs = a.ccap + (size_t)a.nl * a.n2m * (kv - 1);
         cb = (size_t)a.nld * a.n2m * (kv - 1);
     }
-    __device__ double2 &P(int i, int j) const { return pc[i + (size_t)a.ldp * j]; }
-    __device__ double2 &G(int i, int j) const { return gg[i + (size_t)a.ldg * j]; }
-    __device__ double2 &R(int i, int j) const { return rs[i + (size_t)a.ldg * j]; }
+    __device__ V &P(int i, int j) const { return pc[i + (size_t)a.ldp * j]; }
+    __device__ V &G(int i, int j) const { return gg[i + (size_t)a.ldg * j]; }
+    __device__ V &R(int i, int j) const { return rs[i + (size_t)a.ldg * j]; }
     __device__ double2 B(int i, int j) const { return rhs[(i - 1) + (size_t)a.nl * (j - 1)]; }
-    __device__ double AC(int i, int j) const { return a.ac[cb + (i - 1) + (size_t)a.nld * (j - 1)]; }
+    __device__ T AC(int i, int j) const { return s.ac[cb + (i - 1) + (size_t)a.nld * (j - 1)]; }
 };
+using Mode = ModeT<double>;
 
-__device__ __forceinline__ double2 axmy(double2 y, double s, double2 x) {   // y - s*x
-    return make_double2(y.x - s * x.x, y.y - s * x.y);
+template <class V, class T>
+__device__ __forceinline__ V axmy(V y, T s, V x) {   // y - s*x
+    return V{y.x - s * x.x, y.y - s * x.y};
 }
 
 // trdiag1m (poiss_z_ft.f90:383-408) of one x-line held in registers: lane
@@ -111,56 +137,56 @@ __device__ __forceinline__ double2 axmy(double2 y, double s, double2 x) {   // y
 // them; gam_{n2m+1} = 0).  Affine maps of the chunks are composed, joined by
 // a shuffle scan, then each chunk is re-run with the reference recurrence
 // from its scanned incoming value (see the file comment).
-template <int MC>
-__device__ __forceinline__ void line_solve(double2 (&v)[MC], const double (&as_)[MC], const double (&bt)[MC],
-                                           const double (&gm)[MC], int cnt, int lane) {
-    double A = 1.0;
-    double2 Bv = make_double2(0.0, 0.0);
+template <int MC, class T, class V>
+__device__ __forceinline__ void line_solve(V (&v)[MC], const T (&as_)[MC], const T (&bt)[MC],
+                                           const T (&gm)[MC], int cnt, int lane) {
+    T A = T(1.0);
+    V Bv = V{T(0.0), T(0.0)};
 #pragma unroll
     for (int q = 0; q < MC; q++)
         if (q < cnt) {
-            const double aj = -as_[q] * bt[q];
-            Bv = make_double2(aj * Bv.x + v[q].x * bt[q], aj * Bv.y + v[q].y * bt[q]);
+            const T aj = -as_[q] * bt[q];
+            Bv = V{aj * Bv.x + v[q].x * bt[q], aj * Bv.y + v[q].y * bt[q]};
             A = aj * A;
         }
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-        const double Ap = __shfl_up_sync(0xffffffffu, A, d);
-        const double bx = __shfl_up_sync(0xffffffffu, Bv.x, d), by = __shfl_up_sync(0xffffffffu, Bv.y, d);
-        if (lane >= d) { Bv = make_double2(A * bx + Bv.x, A * by + Bv.y); A = A * Ap; }
+        const T Ap = __shfl_up_sync(0xffffffffu, A, d);
+        const T bx = __shfl_up_sync(0xffffffffu, Bv.x, d), by = __shfl_up_sync(0xffffffffu, Bv.y, d);
+        if (lane >= d) { Bv = V{A * bx + Bv.x, A * by + Bv.y}; A = A * Ap; }
     }
-    double yx = __shfl_up_sync(0xffffffffu, Bv.x, 1), yy = __shfl_up_sync(0xffffffffu, Bv.y, 1);
-    if (lane == 0) { yx = 0.0; yy = 0.0; }
+    T yx = __shfl_up_sync(0xffffffffu, Bv.x, 1), yy = __shfl_up_sync(0xffffffffu, Bv.y, 1);
+    if (lane == 0) { yx = T(0.0); yy = T(0.0); }
 #pragma unroll
     for (int q = 0; q < MC; q++)
         if (q < cnt) {
             yx = (v[q].x - as_[q] * yx) * bt[q];
             yy = (v[q].y - as_[q] * yy) * bt[q];
-            v[q] = make_double2(yx, yy);
+            v[q] = V{yx, yy};
         }
-    double C = 1.0;
-    double2 D = make_double2(0.0, 0.0);
+    T C = T(1.0);
+    V D = V{T(0.0), T(0.0)};
 #pragma unroll
     for (int q = MC - 1; q >= 0; q--)
         if (q < cnt) {
-            const double cj = -gm[q];
-            D = make_double2(cj * D.x + v[q].x, cj * D.y + v[q].y);
+            const T cj = -gm[q];
+            D = V{cj * D.x + v[q].x, cj * D.y + v[q].y};
             C = cj * C;
         }
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-        const double Cn = __shfl_down_sync(0xffffffffu, C, d);
-        const double dx = __shfl_down_sync(0xffffffffu, D.x, d), dy = __shfl_down_sync(0xffffffffu, D.y, d);
-        if (lane + d < 32) { D = make_double2(C * dx + D.x, C * dy + D.y); C = C * Cn; }
+        const T Cn = __shfl_down_sync(0xffffffffu, C, d);
+        const T dx = __shfl_down_sync(0xffffffffu, D.x, d), dy = __shfl_down_sync(0xffffffffu, D.y, d);
+        if (lane + d < 32) { D = V{C * dx + D.x, C * dy + D.y}; C = C * Cn; }
     }
-    double xx = __shfl_down_sync(0xffffffffu, D.x, 1), xy = __shfl_down_sync(0xffffffffu, D.y, 1);
-    if (lane == 31) { xx = 0.0; xy = 0.0; }
+    T xx = __shfl_down_sync(0xffffffffu, D.x, 1), xy = __shfl_down_sync(0xffffffffu, D.y, 1);
+    if (lane == 31) { xx = T(0.0); xy = T(0.0); }
 #pragma unroll
     for (int q = MC - 1; q >= 0; q--)
         if (q < cnt) {
             xx = v[q].x - gm[q] * xx;
             xy = v[q].y - gm[q] * xy;
-            v[q] = make_double2(xx, xy);
+            v[q] = V{xx, xy};
         }
 }
 
@@ -174,10 +200,13 @@ enum HalfKind {
 // One zebra half sweep: lines l1, l1+2, ..., l2; one warp per line.
 //   src: the rhs plane (top level) or resd; nb: the array the neighbours come from
 //   out: G(i,j) = solution, or for gsor P(i,j) = ww*solution + o2*P(i,j)
-template <int MC>
-__device__ __noinline__ void mg_half(const Mode &m, int l1, int l2, int kind, bool src_rhs, const double2 *nb, int ldn,
-                        double ov, double2 tt, bool gsor, double ww, double o2) {
+template <int MC, class T>
+__device__ __noinline__ void mg_half(const ModeT<T> &m, int l1, int l2, int kind, bool src_rhs,
+                                     const typename V2<T>::t *nb, int ldn, T ov, typename V2<T>::t tt, bool gsor,
+                                     T ww, T o2) {
+    using V = typename V2<T>::t;
     const MgArgs &a = m.a;
+    const MgSet<T> &s = m.s;
     if (l2 < l1) return;
     const int lane = m.tid & 31, warp = m.tid >> 5, nw = m.nt >> 5;
     const int n2m = a.n2m, nl = (l2 - l1) / 2 + 1;
@@ -188,30 +217,36 @@ __device__ __noinline__ void mg_half(const Mode &m, int l1, int l2, int kind, bo
     for (int li = warp; li < nl; li += nw) {
         const int i = l1 + 2 * li;
         const int im = a.imm[i], ip = a.ipm[i];
-        const double aw = a.aw[i], ae = a.ae[i];
-        const double *bet = a.bet + m.cb + (i - 1);
-        const double *gam = a.gam + m.cb + (i - 1);
-        double2 v[MC];
-        double as_[MC], bt[MC], gm[MC];
+        const T aw = s.aw[i], ae = s.ae[i];
+        const T *bet = s.bet + m.cb + (i - 1);
+        const T *gam = s.gam + m.cb + (i - 1);
+        V v[MC];
+        T as_[MC], bt[MC], gm[MC];
 #pragma unroll
         for (int q = 0; q < MC; q++)
             if (q < cnt) {
                 const int j = j0 + q;
-                const double2 sr = src_rhs ? m.B(i, j) : m.R(i, j);
-                double2 nm = nb[im + (size_t)ldn * j], np = nb[ip + (size_t)ldn * j];
-                if (kind == H_ODD) {
-                    const double sx = aw * nm.x + ae * np.x, sy = aw * nm.y + ae * np.y;
-                    v[q] = make_double2(sr.x - ov * sx, sr.y - ov * sy);
-                } else if (kind == H_EVEN) {
-                    v[q] = make_double2(sr.x - aw * nm.x - ae * np.x, sr.y - aw * nm.y - ae * np.y);
+                V sr;
+                if (src_rhs) {
+                    const double2 b = m.B(i, j);
+                    sr = V{T(b.x), T(b.y)};
                 } else {
-                    nm = make_double2(nm.x - tt.x, nm.y - tt.y);
-                    if (ip < i) np = make_double2(np.x - tt.x, np.y - tt.y);   // x-periodic wrap: shifted already
-                    v[q] = make_double2(sr.x - aw * nm.x - ae * (np.x - tt.x), sr.y - aw * nm.y - ae * (np.y - tt.y));
+                    sr = m.R(i, j);
                 }
-                as_[q] = a.as[j];
+                V nm = nb[im + (size_t)ldn * j], np = nb[ip + (size_t)ldn * j];
+                if (kind == H_ODD) {
+                    const T sx = aw * nm.x + ae * np.x, sy = aw * nm.y + ae * np.y;
+                    v[q] = V{sr.x - ov * sx, sr.y - ov * sy};
+                } else if (kind == H_EVEN) {
+                    v[q] = V{sr.x - aw * nm.x - ae * np.x, sr.y - aw * nm.y - ae * np.y};
+                } else {
+                    nm = V{nm.x - tt.x, nm.y - tt.y};
+                    if (ip < i) np = V{np.x - tt.x, np.y - tt.y};   // x-periodic wrap: shifted already
+                    v[q] = V{sr.x - aw * nm.x - ae * (np.x - tt.x), sr.y - aw * nm.y - ae * (np.y - tt.y)};
+                }
+                as_[q] = s.as[j];
                 bt[q] = bet[sj * (j - 1)];
-                gm[q] = j < n2m ? gam[sj * j] : 0.0;
+                gm[q] = j < n2m ? gam[sj * j] : T(0.0);
             }
         line_solve<MC>(v, as_, bt, gm, cnt, lane);
 #pragma unroll
@@ -219,8 +254,8 @@ __device__ __noinline__ void mg_half(const Mode &m, int l1, int l2, int kind, bo
             if (q < cnt) {
                 const int j = j0 + q;
                 if (gsor) {
-                    const double2 u = m.P(i, j);
-                    m.P(i, j) = make_double2(ww * v[q].x + o2 * u.x, ww * v[q].y + o2 * u.y);
+                    const V u = m.P(i, j);
+                    m.P(i, j) = V{ww * v[q].x + o2 * u.x, ww * v[q].y + o2 * u.y};
                 } else {
                     m.G(i, j) = v[q];
                 }
@@ -228,13 +263,16 @@ __device__ __noinline__ void mg_half(const Mode &m, int l1, int l2, int kind, bo
     }
 }
 
-// src - aw*g(imm) - ae*g(ipm) - as*g(j-1) - an*g(j+1) - ac*g  on the gg array
-__device__ __forceinline__ double2 mg_defect(const Mode &m, double2 src, const double2 *g, int ld, int i, int j) {
+// src - aw*g(imm) - ae*g(ipm) - as*g(j-1) - an*g(j+1) - ac*g  on the array g
+template <class T>
+__device__ __forceinline__ typename V2<T>::t mg_defect(const ModeT<T> &m, typename V2<T>::t src,
+                                                      const typename V2<T>::t *g, int ld, int i, int j) {
     const MgArgs &a = m.a;
-    src = axmy(src, a.aw[i], g[a.imm[i] + (size_t)ld * j]);
-    src = axmy(src, a.ae[i], g[a.ipm[i] + (size_t)ld * j]);
-    src = axmy(src, a.as[j], g[i + (size_t)ld * (j - 1)]);
-    src = axmy(src, a.an[j], g[i + (size_t)ld * (j + 1)]);
+    const MgSet<T> &s = m.s;
+    src = axmy(src, s.aw[i], g[a.imm[i] + (size_t)ld * j]);
+    src = axmy(src, s.ae[i], g[a.ipm[i] + (size_t)ld * j]);
+    src = axmy(src, s.as[j], g[i + (size_t)ld * (j - 1)]);
+    src = axmy(src, s.an[j], g[i + (size_t)ld * (j + 1)]);
     src = axmy(src, m.AC(i, j), g[i + (size_t)ld * j]);
     return src;
 }
@@ -242,7 +280,7 @@ __device__ __forceinline__ double2 mg_defect(const Mode &m, double2 src, const d
 // Max over the cluster: warp shuffles, one value per block in shared memory,
 // then every thread reads every block's value through distributed shared
 // memory, in the same order, so all threads get the same result.
-__device__ double cluster_max(const Mode &m, double v) {
+__device__ double cluster_max(double v) {
     __shared__ double sh[kMgThreads / 32];
     __shared__ double blk;
     namespace cg = cooperative_groups;
@@ -250,7 +288,7 @@ __device__ double cluster_max(const Mode &m, double v) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
     if (lane == 0) sh[w] = v;
-    m.sync();
+    cl.sync();
     if (threadIdx.x == 0) {
         double r = 0.0;
         for (int q = 0; q < (int)(blockDim.x >> 5); q++) r = fmax(r, sh[q]);
@@ -266,58 +304,91 @@ __device__ double cluster_max(const Mode &m, double v) {
 // Subtract tt from the odd lines of u (ld: leading dimension) -- the zero
 // wavenumber's pin of poiss_x_ft.f90:328-335, 533-540 and 582-589.  tt was read by
 // every thread before the barrier in front of this.
-__device__ void mg_shift_odd(const Mode &m, double2 *u, int ld, double2 tt) {
+template <class T>
+__device__ void mg_shift_odd(const ModeT<T> &m, typename V2<T>::t *u, int ld, typename V2<T>::t tt) {
     const int nh = m.a.nl / 2, n2m = m.a.n2m;
     for (int t = m.tid; t < nh * n2m; t += m.nt) {
         const int i = 1 + 2 * (t % nh), j = 1 + t / nh;
-        double2 &g = u[i + (size_t)ld * j];
-        g = make_double2(g.x - tt.x, g.y - tt.y);
+        typename V2<T>::t &g = u[i + (size_t)ld * j];
+        g = typename V2<T>::t{g.x - tt.x, g.y - tt.y};
     }
+}
+
+// The top level's zebra relaxation (both halves, with the zero wavenumber's
+// pin) into G: poiss_z_ft.f90:331-357 / poiss_x_ft.f90:320-344.  The odd
+// lines take their neighbours from P scaled by oldv; src_rhs: the source is
+// the right-hand side plane (else R's top level).
+template <class T>
+__device__ void mg_top_relax(const ModeT<T> &m, T oldv, bool src_rhs) {
+    using V = typename V2<T>::t;
+    const MgArgs &a = m.a;
+    const int n1m = a.nl, n2m = a.n2m;
+    const V zero = V{T(0.0), T(0.0)};
+    mg_half<kMC, T>(m, 1, n1m, H_ODD, src_rhs, m.pc, a.ldp, oldv, zero, false, T(0.0), T(0.0));
+    m.sync();
+    if (a.xft) {
+        // poiss_x_ft: shift the odd lines by ggii(1,n2m), then form the even
+        // lines from the shifted values as rhs - (ab*g + af*g)
+        if (m.kv == 1) {
+            const V tt = m.G(1, n2m);
+            m.sync();
+            mg_shift_odd(m, m.gg, a.ldg, tt);
+            m.sync();
+        }
+        mg_half<kMC, T>(m, 2, n1m, H_ODD, src_rhs, m.gg, a.ldg, T(1.0), zero, false, T(0.0), T(0.0));
+        m.sync();
+    } else {
+        // poiss_z_ft: the even lines see the odd ones shifted by ggii(1,n2m-1)
+        // inside their right-hand side; the odd lines are shifted afterwards
+        const V tt = m.kv == 1 ? m.G(1, n2m - 1) : zero;
+        mg_half<kMC, T>(m, 2, n1m, H_EVEN_TT, src_rhs, m.gg, a.ldg, T(1.0), tt, false, T(0.0), T(0.0));
+        m.sync();
+        if (m.kv == 1) mg_shift_odd(m, m.gg, a.ldg, tt);
+        m.sync();
+    }
+}
+
+// Restrict the top level's residual (R) onto level nlev-1
+template <class T>
+__device__ void mg_top_restrict(const ModeT<T> &m) {
+    const MgArgs &a = m.a;
+    const int cl = a.iimg[a.nlev - 1][0], nc = a.iimg[a.nlev - 1][1] - cl + 1;
+    for (int t = m.tid; t < nc * a.n2m; t += m.nt) {
+        const int i = cl + t % nc, j = 1 + t / nc, ic = 2 * (i - cl) + 1;
+        const typename V2<T>::t r1 = m.R(ic, j), r2 = m.R(ic + 1, j);
+        m.R(i, j) = typename V2<T>::t{r1.x * m.s.cor1[i] + r2.x * m.s.cor2[i], r1.y * m.s.cor1[i] + r2.y * m.s.cor2[i]};
+    }
+    m.sync();
+}
+
+// The coarse correction of level nlev-1 interpolated onto the top level's
+// even lines: P += (FP64 form) or P = (the mixed form's correction).
+template <class T>
+__device__ void mg_top_prolong(const ModeT<T> &m, bool assign) {
+    const MgArgs &a = m.a;
+    const MgSet<T> &s = m.s;
+    const int cl = a.iimg[a.nlev - 1][0], ce = a.iimg[a.nlev - 1][1], nc = ce - cl + 1;
+    for (int t = m.tid; t < nc * a.n2m; t += m.nt) {
+        const int i = cl + t % nc, j = 1 + t / nc, ic = 2 * (i - cl + 1);
+        typename V2<T>::t p = assign ? typename V2<T>::t{T(0.0), T(0.0)} : m.P(ic, j);
+        const typename V2<T>::t g1 = m.G(i, j);
+        if (i < ce || a.xft) {
+            const typename V2<T>::t g2 = m.G(a.ipm[i], j);
+            p = typename V2<T>::t{p.x + s.coi1[i] * g1.x + s.coi2[i] * g2.x, p.y + s.coi1[i] * g1.y + s.coi2[i] * g2.y};
+        } else {
+            p = typename V2<T>::t{p.x + s.coi1[i] * g1.x, p.y + s.coi1[i] * g1.y};
+        }
+        m.P(ic, j) = p;
+    }
+    m.sync();
 }
 
 // toplevel, poiss_z_ft.f90:302-380 / poiss_x_ft.f90:296-371; returns the max-norm residual
 __device__ double mg_toplevel(const Mode &m, int id, double oldv, double test) {
     const MgArgs &a = m.a;
     const int n1m = a.nl, n2m = a.n2m, nt = m.nt;
-    const int cl = a.iimg[a.nlev - 1][0], ce = a.iimg[a.nlev - 1][1];
-    if (id == 1) {   // prolong the coarse correction onto the even lines
-        const int nc = ce - cl + 1;
-        for (int t = m.tid; t < nc * n2m; t += nt) {
-            const int i = cl + t % nc, j = 1 + t / nc, ic = 2 * (i - cl + 1);
-            double2 p = m.P(ic, j);
-            const double2 g1 = m.G(i, j);
-            if (i < ce || a.xft) {
-                const double2 g2 = m.G(a.ipm[i], j);
-                p = make_double2(p.x + a.coi1[i] * g1.x + a.coi2[i] * g2.x, p.y + a.coi1[i] * g1.y + a.coi2[i] * g2.y);
-            } else {
-                p = make_double2(p.x + a.coi1[i] * g1.x, p.y + a.coi1[i] * g1.y);
-            }
-            m.P(ic, j) = p;
-        }
-        m.sync();
-    }
-    mg_half<kMC>(m, 1, n1m, H_ODD, true, m.pc, a.ldp, oldv, make_double2(0.0, 0.0), false, 0.0, 0.0);
-    m.sync();
-    if (a.xft) {
-        // poiss_x_ft: shift the odd lines by ggii(1,n2m), then form the even
-        // lines from the shifted values as rhs - (ab*g + af*g)
-        if (m.kv == 1) {
-            const double2 tt = m.G(1, n2m);
-            m.sync();
-            mg_shift_odd(m, m.gg, a.ldg, tt);
-            m.sync();
-        }
-        mg_half<kMC>(m, 2, n1m, H_ODD, true, m.gg, a.ldg, 1.0, make_double2(0.0, 0.0), false, 0.0, 0.0);
-        m.sync();
-    } else {
-        // poiss_z_ft: the even lines see the odd ones shifted by ggii(1,n2m-1)
-        // inside their right-hand side; the odd lines are shifted afterwards
-        const double2 tt = m.kv == 1 ? m.G(1, n2m - 1) : make_double2(0.0, 0.0);
-        mg_half<kMC>(m, 2, n1m, H_EVEN_TT, true, m.gg, a.ldg, 1.0, tt, false, 0.0, 0.0);
-        m.sync();
-        if (m.kv == 1) mg_shift_odd(m, m.gg, a.ldg, tt);
-        m.sync();
-    }
+    if (id == 1) mg_top_prolong(m, false);   // prolong the coarse correction onto the even lines
+    mg_top_relax(m, oldv, true);
     double mx = 0.0;
     for (int t = m.tid; t < n1m * n2m; t += nt) {
         const int i = 1 + t % n1m, j = 1 + t / n1m;
@@ -326,33 +397,30 @@ __device__ double mg_toplevel(const Mode &m, int id, double oldv, double test) {
         mx = fmax(mx, d.x * d.x + d.y * d.y);
         m.P(i, j) = m.G(i, j);
     }
-    const double sumres = sqrt(cluster_max(m, mx));
+    const double sumres = sqrt(cluster_max(mx));
     if (sumres < test) return sumres;
-    const int nc = ce - cl + 1;                                  // restrict
-    for (int t = m.tid; t < nc * n2m; t += nt) {
-        const int i = cl + t % nc, j = 1 + t / nc, ic = 2 * (i - cl) + 1;
-        const double2 r1 = m.R(ic, j), r2 = m.R(ic + 1, j);
-        m.R(i, j) = make_double2(r1.x * a.cor1[i] + r2.x * a.cor2[i], r1.y * a.cor1[i] + r2.y * a.cor2[i]);
-    }
-    m.sync();
+    mg_top_restrict(m);
     return sumres;
 }
 
 // relax, poiss_z_ft.f90:466-511 (zebra version)
-__device__ void mg_relax(const Mode &m, int ilev, double oldv, int iiter) {
+template <class T>
+__device__ void mg_relax(const ModeT<T> &m, int ilev, T oldv, int iiter) {
     const MgArgs &a = m.a;
     const int ibg = a.iimg[ilev][0], iend = a.iimg[ilev][1];
+    const typename V2<T>::t zero{T(0.0), T(0.0)};
     for (int it = 0; it < iiter; it++) {
-        const double ov = it == 0 ? oldv : 1.0;
-        mg_half<kMC>(m, ibg, iend, H_ODD, false, m.gg, a.ldg, ov, make_double2(0.0, 0.0), false, 0.0, 0.0);
+        const T ov = it == 0 ? oldv : T(1.0);
+        mg_half<kMC, T>(m, ibg, iend, H_ODD, false, m.gg, a.ldg, ov, zero, false, T(0.0), T(0.0));
         m.sync();
-        mg_half<kMC>(m, ibg + 1, iend, H_EVEN, false, m.gg, a.ldg, 1.0, make_double2(0.0, 0.0), false, 0.0, 0.0);
+        mg_half<kMC, T>(m, ibg + 1, iend, H_EVEN, false, m.gg, a.ldg, T(1.0), zero, false, T(0.0), T(0.0));
         m.sync();
     }
 }
 
 // godown, poiss_z_ft.f90:438-463
-__device__ void mg_godown(const Mode &m, int ilev) {
+template <class T>
+__device__ void mg_godown(const ModeT<T> &m, int ilev) {
     const MgArgs &a = m.a;
     const int ibg = a.iimg[ilev][0], iend = a.iimg[ilev][1], n2m = a.n2m, nt = m.nt;
     const int nf = iend - ibg + 1;
@@ -364,26 +432,28 @@ __device__ void mg_godown(const Mode &m, int ilev) {
     const int cl = a.iimg[ilev - 1][0], nc = a.iimg[ilev - 1][1] - cl + 1;
     for (int t = m.tid; t < nc * n2m; t += nt) {
         const int i = cl + t % nc, j = 1 + t / nc, f = ibg + 2 * (i - cl);
-        const double2 r1 = m.R(f, j), r2 = m.R(f + 1, j);
-        m.R(i, j) = make_double2(r1.x * a.cor1[i] + r2.x * a.cor2[i], r1.y * a.cor1[i] + r2.y * a.cor2[i]);
+        const typename V2<T>::t r1 = m.R(f, j), r2 = m.R(f + 1, j);
+        m.R(i, j) = typename V2<T>::t{r1.x * m.s.cor1[i] + r2.x * m.s.cor2[i], r1.y * m.s.cor1[i] + r2.y * m.s.cor2[i]};
     }
     m.sync();
 }
 
 // goup, poiss_z_ft.f90:411-435 / poiss_x_ft.f90:401-419
-__device__ void mg_goup(const Mode &m, int ilev) {
+template <class T>
+__device__ void mg_goup(const ModeT<T> &m, int ilev) {
     const MgArgs &a = m.a;
+    const MgSet<T> &s = m.s;
     const int cl = a.iimg[ilev][0], ce = a.iimg[ilev][1], n2m = a.n2m, nt = m.nt;
     const int fb = a.iimg[ilev + 1][0], nc = ce - cl + 1;
     for (int t = m.tid; t < nc * n2m; t += nt) {
         const int i = cl + t % nc, j = 1 + t / nc, f = fb + 1 + 2 * (i - cl);
-        double2 g = m.G(f, j);
-        const double2 g1 = m.G(i, j);
+        typename V2<T>::t g = m.G(f, j);
+        const typename V2<T>::t g1 = m.G(i, j);
         if (i < ce || a.xft) {
-            const double2 g2 = m.G(a.ipm[i], j);
-            g = make_double2(g.x + a.coi1[i] * g1.x + a.coi2[i] * g2.x, g.y + a.coi1[i] * g1.y + a.coi2[i] * g2.y);
+            const typename V2<T>::t g2 = m.G(a.ipm[i], j);
+            g = typename V2<T>::t{g.x + s.coi1[i] * g1.x + s.coi2[i] * g2.x, g.y + s.coi1[i] * g1.y + s.coi2[i] * g2.y};
         } else {
-            g = make_double2(g.x + a.coi1[i] * g1.x, g.y + a.coi1[i] * g1.y);
+            g = typename V2<T>::t{g.x + s.coi1[i] * g1.x, g.y + s.coi1[i] * g1.y};
         }
         m.G(f, j) = g;
     }
@@ -411,6 +481,80 @@ __device__ int mg_mg2d(const Mode &m, double test) {
     return a.mgitr;       // iteration limit: the reference warns and goes on
 }
 
+// The mixed form's toplevel: the top-level relaxation runs in FP32 on the
+// correction e (source r, the FP64 residual rounded to FP32; P holds the
+// prolonged coarse correction), then in FP64 x += e and r = b - A x, whose
+// max norm is the reference's convergence test.  By the linearity of the
+// zebra relaxation, x + relax(P g; r) is the reference's relax(x + P g; b):
+// the cycle is the reference's, with the correction carried in FP32.
+__device__ double mg_top_mixed(const Mode &m, const ModeT<float> &f, int id, double test) {
+    const MgArgs &a = m.a;
+    const int n1m = a.nl, n2m = a.n2m, nt = m.nt;
+    if (id == 1) mg_top_prolong(f, true);
+    mg_top_relax(f, id == 1 ? 1.0f : 0.0f, false);
+    for (int t = m.tid; t < n1m * n2m; t += nt) {           // x += e (x = e on the first pass)
+        const int i = 1 + t % n1m, j = 1 + t / n1m;
+        const float2 e = f.G(i, j);
+        const double2 x = id == 0 ? make_double2(0.0, 0.0) : m.P(i, j);
+        m.P(i, j) = make_double2(x.x + (double)e.x, x.y + (double)e.y);
+    }
+    m.sync();
+    double mx = 0.0;
+    for (int t = m.tid; t < n1m * n2m; t += nt) {           // r = b - A x in FP64
+        const int i = 1 + t % n1m, j = 1 + t / n1m;
+        const double2 d = mg_defect(m, m.B(i, j), m.pc, a.ldp, i, j);
+        f.R(i, j) = make_float2((float)d.x, (float)d.y);
+        mx = fmax(mx, d.x * d.x + d.y * d.y);
+    }
+    const double sumres = sqrt(cluster_max(mx));
+    if (sumres < test) return sumres;
+    mg_top_restrict(f);
+    return sumres;
+}
+
+// mg2d in the mixed form: the V-cycle of mg_mg2d with every level but the
+// coarsest relaxed in FP32, the coarsest in FP64, and the residual, the
+// solution and the convergence test in FP64 (mg_top_mixed).
+__device__ int mg_mg2d_mixed(const Mode &m, const ModeT<float> &f, double test) {
+    const MgArgs &a = m.a;
+    const int n2m = a.n2m, nt = m.nt;
+    for (int t = m.tid; t < a.nl * n2m; t += nt) {          // the first source is b itself
+        const int i = 1 + t % a.nl, j = 1 + t / a.nl;
+        const double2 b = m.B(i, j);
+        f.R(i, j) = make_float2((float)b.x, (float)b.y);
+    }
+    m.sync();
+    double sumres = mg_top_mixed(m, f, 0, test);
+    if (sumres < test) return 0;
+    const int c0 = a.iimg[0][0], nc0 = a.iimg[0][1] - c0 + 1;
+    for (int kk = 1; kk <= a.mgitr; kk++) {
+        for (int ilev = a.nlev - 1; ilev >= 1; ilev--) {
+            mg_relax(f, ilev, 0.0f, 1);
+            mg_godown(f, ilev);
+        }
+        for (int t = m.tid; t < nc0 * n2m; t += nt) {       // coarsest level in FP64
+            const int i = c0 + t % nc0, j = 1 + t / nc0;
+            const float2 r = f.R(i, j);
+            m.R(i, j) = make_double2((double)r.x, (double)r.y);
+        }
+        m.sync();
+        mg_relax(m, 0, 0.0, a.nbli);
+        for (int t = m.tid; t < nc0 * n2m; t += nt) {
+            const int i = c0 + t % nc0, j = 1 + t / nc0;
+            const double2 g = m.G(i, j);
+            f.G(i, j) = make_float2((float)g.x, (float)g.y);
+        }
+        m.sync();
+        for (int ilev = 0; ilev <= a.nlev - 2; ilev++) {
+            mg_goup(f, ilev);
+            mg_relax(f, ilev + 1, 1.0f, 1);
+        }
+        sumres = mg_top_mixed(m, f, 1, test);
+        if (sumres < test) return kk;
+    }
+    return a.mgitr;
+}
+
 // gsor2d + resid3, poiss_z_ft.f90:513-641 / poiss_x_ft.f90:497-642 (pc is the iterate u)
 __device__ int mg_gsor2d(const Mode &m, double test) {
     const MgArgs &a = m.a;
@@ -420,7 +564,7 @@ __device__ int mg_gsor2d(const Mode &m, double test) {
         const double ov = kk == 0 ? 0.0 : 1.0, o2 = ov * ww2;
         for (int half = 0; half < 2; half++) {
             const double f = half == 0 ? ov : 1.0;
-            mg_half<kMC>(m, 1 + half, n1m, H_ODD, true, m.pc, a.ldp, f, make_double2(0.0, 0.0), true, ww, o2);
+            mg_half<kMC, double>(m, 1 + half, n1m, H_ODD, true, m.pc, a.ldp, f, make_double2(0.0, 0.0), true, ww, o2);
             m.sync();
             if (half == 0 && a.xft && m.kv == 1) {     // poiss_x_ft pins the zero wavenumber by u(1,n2m)
                 const double2 tt = m.P(1, n2m);
@@ -435,7 +579,7 @@ __device__ int mg_gsor2d(const Mode &m, double test) {
             const double2 d = mg_defect(m, m.B(i, j), m.pc, a.ldp, i, j);
             mx = fmax(mx, d.x * d.x + d.y * d.y);
         }
-        const double e = sqrt(cluster_max(m, mx));
+        const double e = sqrt(cluster_max(mx));
         if (e < test) return kk;
     }
     return a.mgitr;
@@ -450,9 +594,18 @@ __global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes(MgArgs a) {
     // 32-point chunks go to different SMs (the work of a phase is spread over
     // every block, each warp still touches 32 consecutive points)
     const int gw = (int)(threadIdx.x >> 5) * cs + (int)cl.block_rank();
-    Mode m(a, kv, gw * 32 + (int)(threadIdx.x & 31), cs * blockDim.x);
+    const int tid = gw * 32 + (int)(threadIdx.x & 31), nt = cs * blockDim.x;
+    Mode m(a, a.d, kv, tid, nt);
     const double test = a.fixed_cycles > 0 ? -1.0 : a.S->mg_test;
-    const int it = kv <= a.imgsor ? mg_mg2d(m, test) : mg_gsor2d(m, test);
+    int it;
+    if (kv > a.imgsor) {
+        it = mg_gsor2d(m, test);
+    } else if (a.mixed) {
+        ModeT<float> f(a, a.f, kv, tid, nt);
+        it = mg_mg2d_mixed(m, f, test);
+    } else {
+        it = mg_mg2d(m, test);
+    }
     // the mode's solution replaces its right-hand side (ccap(i,j,kkk) = cp(i,j))
     double2 *out = a.ccap + (size_t)a.nl * a.n2m * (kv - 1);
     for (int t = m.tid; t < a.nl * a.n2m; t += m.nt) {
@@ -636,9 +789,18 @@ static int set_up_tables(lesgpu_case *c, MgTables &T) {
         if (cudaMalloc((void **)&dst, sizeof(T0) * v.size()) != cudaSuccess) { ok = false; return; }
         cudaMemcpy(dst, v.data(), sizeof(T0) * v.size(), cudaMemcpyHostToDevice);
     };
-    up(T.aw, aw); up(T.ae, ae); up(T.as, as); up(T.an, an);
-    up(T.coi1, coi1); up(T.coi2, coi2); up(T.cor1, cor1); up(T.cor2, cor2);
-    up(T.ipm, ipm); up(T.imm, imm); up(T.ac, ac); up(T.bet, bet); up(T.gam, gam);
+    up(T.d.aw, aw); up(T.d.ae, ae); up(T.d.as, as); up(T.d.an, an);
+    up(T.d.coi1, coi1); up(T.d.coi2, coi2); up(T.d.cor1, cor1); up(T.d.cor2, cor2);
+    up(T.ipm, ipm); up(T.imm, imm); up(T.d.ac, ac); up(T.d.bet, bet); up(T.d.gam, gam);
+    if (T.mixed) {   // FP32 copies (the LU factors rounded from their FP64 values)
+        auto upf = [&](float *&dst, const std::vector<double> &v) {
+            std::vector<float> h(v.begin(), v.end());
+            up(dst, h);
+        };
+        upf(T.f.aw, aw); upf(T.f.ae, ae); upf(T.f.as, as); upf(T.f.an, an);
+        upf(T.f.coi1, coi1); upf(T.f.coi2, coi2); upf(T.f.cor1, cor1); upf(T.f.cor2, cor2);
+        upf(T.f.ac, ac); upf(T.f.bet, bet); upf(T.f.gam, gam);
+    }
     return ok ? 0 : LESGPU_ERR_OOM;
 }
 
@@ -673,22 +835,35 @@ int mg2d_init(lesgpu_case *c) {
     T->nlev = nlev;
     T->nmodes = nmodes;
     T->xft = xft ? 1 : 0;
+    // the mixed form runs the multigrid cycles in FP32 under an FP64 defect
+    // correction (LESGPU_MG_FP64=1 keeps them in FP64)
+    const char *mg64 = getenv("LESGPU_MG_FP64");
+    T->mixed = cf.precision == LESGPU_PREC_MIXED && !(mg64 && mg64[0] == '1');
     rc = set_up_tables(c, *T);
     if (rc) return rc;
     const int ldp = nl + 2, ldg = T->nld + 1;
     T->pc_plane = (long long)ldp * (g.n2m + 2);
     T->gg_plane = (long long)ldg * (g.n2m + 2);
     const size_t nm = (size_t)nmodes;
-    if (cudaMalloc(&T->pc, sizeof(double2) * T->pc_plane * nm) != cudaSuccess ||
-        cudaMalloc(&T->gg, sizeof(double2) * T->gg_plane * nm) != cudaSuccess ||
-        cudaMalloc(&T->rs, sizeof(double2) * T->gg_plane * nm) != cudaSuccess ||
+    if (cudaMalloc(&T->d.pc, sizeof(double2) * T->pc_plane * nm) != cudaSuccess ||
+        cudaMalloc(&T->d.gg, sizeof(double2) * T->gg_plane * nm) != cudaSuccess ||
+        cudaMalloc(&T->d.rs, sizeof(double2) * T->gg_plane * nm) != cudaSuccess ||
         cudaMalloc(&T->iters, sizeof(long long) * nm) != cudaSuccess ||
         cudaMalloc(&P.ccap, sizeof(double2) * (size_t)nl * g.n2m * nm) != cudaSuccess)
         return LESGPU_ERR_OOM;
     // the boundary rows and columns of pc / gg are read as zeros and never written
-    cudaMemset(T->pc, 0, sizeof(double2) * T->pc_plane * nm);
-    cudaMemset(T->gg, 0, sizeof(double2) * T->gg_plane * nm);
-    cudaMemset(T->rs, 0, sizeof(double2) * T->gg_plane * nm);
+    cudaMemset(T->d.pc, 0, sizeof(double2) * T->pc_plane * nm);
+    cudaMemset(T->d.gg, 0, sizeof(double2) * T->gg_plane * nm);
+    cudaMemset(T->d.rs, 0, sizeof(double2) * T->gg_plane * nm);
+    if (T->mixed) {
+        if (cudaMalloc(&T->f.pc, sizeof(float2) * T->pc_plane * nm) != cudaSuccess ||
+            cudaMalloc(&T->f.gg, sizeof(float2) * T->gg_plane * nm) != cudaSuccess ||
+            cudaMalloc(&T->f.rs, sizeof(float2) * T->gg_plane * nm) != cudaSuccess)
+            return LESGPU_ERR_OOM;
+        cudaMemset(T->f.pc, 0, sizeof(float2) * T->pc_plane * nm);
+        cudaMemset(T->f.gg, 0, sizeof(float2) * T->gg_plane * nm);
+        cudaMemset(T->f.rs, 0, sizeof(float2) * T->gg_plane * nm);
+    }
     cudaMemset(T->iters, 0, sizeof(long long) * nm);
     if (xft) {
         if (cudaFuncSetAttribute(k_fft_xr_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess ||
@@ -740,8 +915,10 @@ void set_mg_cluster_cap(int cap) { t_mg_cluster_cap = cap; }
 void mg2d_free(lesgpu_case *c) {
     MgTables *T = c->pois.mg;
     if (!T) return;
-    void *ptrs[] = {T->aw, T->ae, T->as, T->an, T->coi1, T->coi2, T->cor1, T->cor2, T->ipm, T->imm,
-                    T->ac, T->bet, T->gam, T->pc, T->gg, T->rs, T->iters};
+    void *ptrs[] = {T->d.aw, T->d.ae, T->d.as, T->d.an, T->d.coi1, T->d.coi2, T->d.cor1, T->d.cor2, T->ipm, T->imm,
+                    T->d.ac, T->d.bet, T->d.gam, T->d.pc, T->d.gg, T->d.rs, T->iters,
+                    T->f.aw, T->f.ae, T->f.as, T->f.an, T->f.coi1, T->f.coi2, T->f.cor1, T->f.cor2,
+                    T->f.ac, T->f.bet, T->f.gam, T->f.pc, T->f.gg, T->f.rs};
     for (void *q : ptrs) cudaFree(q);
     delete T;
     c->pois.mg = nullptr;
@@ -760,10 +937,10 @@ static MgArgs mg_args(lesgpu_case *c, int slot, int fixed_cycles) {
     a.imgsor = (int)cf.imgsor; a.wwsor = cf.wwsor;
     a.ldp = T->nl + 2; a.ldg = T->nld + 1;
     memcpy(a.iimg, T->iimg, sizeof(a.iimg));
-    a.aw = T->aw; a.ae = T->ae; a.as = T->as; a.an = T->an;
-    a.coi1 = T->coi1; a.coi2 = T->coi2; a.cor1 = T->cor1; a.cor2 = T->cor2;
-    a.ipm = T->ipm; a.imm = T->imm; a.ac = T->ac; a.bet = T->bet; a.gam = T->gam;
-    a.ccap = P.ccap; a.pc = T->pc; a.gg = T->gg; a.rs = T->rs;
+    a.ipm = T->ipm; a.imm = T->imm;
+    a.d = T->d; a.f = T->f;
+    a.mixed = T->mixed;
+    a.ccap = P.ccap;
     a.pc_plane = T->pc_plane; a.gg_plane = T->gg_plane;
     a.iters = T->iters; a.S = c->S; a.slot = slot;
     a.fixed_cycles = fixed_cycles;

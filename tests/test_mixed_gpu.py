@@ -1,6 +1,7 @@
-"""The mixed-precision form (FP32 stencils, SGS and x/z ADI sweeps; FP64 y
-sweeps, Poisson, projection, flow-rate and divergence) against the FP64 form
-on the same case.
+"""The mixed-precision form (FP32 stencils, SGS and x/z ADI sweeps, FP32
+multigrid cycles; FP64 y sweeps, FFT Poisson, multigrid residual / defect
+correction / coarsest level, projection, flow-rate and divergence) against the
+FP64 form on the same case.
 
 Stated error bounds (relative L2 of each field against the FP64 form): u, v,
 w, t within 1e-5 after one step and 1e-4 after ten on the channel; the
@@ -61,3 +62,31 @@ def test_mixed_is_deterministic():
     fx, fy = x.fields(), y.fields()
     for k in ("u", "v", "w", "p", "t"):
         assert np.array_equal(fx[k], fy[k]), k
+
+
+@pytest.mark.parametrize("build", [
+    lambda prec: cases.cylinder(64, 48, 8, precision=prec),                                   # poiss_z_ft
+    lambda prec: cases.with_poisson(cases.channel(32, 32, 16, zwalls=True, precision=prec),   # poiss_x_ft
+                                    abi.POISSON_X_FT, nlev=3),
+])
+def test_fp32_multigrid_meets_the_fp64_test(build):
+    """The mixed form's multigrid cycles run in FP32 under an FP64 defect
+    correction: on the same divergence and a tight RESID1 it stops on the same
+    FP64 residual test, and phi matches the FP64 form's to 1e-8 relative."""
+    ca, cb = build(abi.PREC_FP64), build(abi.PREC_MIXED)
+    for c in (ca, cb):
+        c.settings.update(resid1=1e-10, mgitr=2000)
+    a, b = leswht_gb300.gpu_solver(ca), leswht_gb300.gpu_solver(cb)
+    for s in (a, b):
+        s.phase(abi.PH_STEPINIT)
+        s.phase(abi.PH_SUBSTEPINIT, 1)
+    a.phase(abi.PH_SGS, 1)
+    a.phase(abi.PH_RHSNLHS, 1)
+    a.phase(abi.PH_DIVGS, 1)
+    b.set(abi.F_DIVGSUM, a.get(abi.F_DIVGSUM))
+    for s in (a, b):
+        s.phase(abi.PH_POISSON, 1)
+    ia, ib = a.report()["poisson_iters"][0], b.report()["poisson_iters"][0]
+    assert 1 <= ia < 2000 and 1 <= ib < 2000 and abs(ia - ib) <= max(2, ia // 5)
+    assert rel(b.get(abi.F_PHI), a.get(abi.F_PHI)) <= 1e-8
+
