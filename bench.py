@@ -96,6 +96,8 @@ def make_case(name, form):
         return cases.PRESETS["channel590"](precision=prec)
     if name == "channel_small":
         return cases.channel(32, 32, 16, precision=prec)
+    if name == "channel590_slab":
+        return cases.channel(384, 64, 384, lx=2 * math.pi, lz=math.pi, re=10950.0, precision=prec)
     if name == "cylinder100":
         return cases.PRESETS["cylinder100"](precision=prec)
     if name == "cylinder3900":
@@ -112,6 +114,8 @@ WORKLOAD = {
                  "tanh wall-normal stretching (gamma 2.75), CFR forcing, dynamic Vreman + dynamic EDM, poiss_ftft",
     "channel590": "turbulent channel Re_tau~590 with passive heat transfer, 2pi x 2 x pi, 384x256x384 cells, poiss_ftft",
     "channel_small": "turbulent channel 32x32x16 (test size)",
+    "channel590_slab": "the Re_tau~590 channel's 384x384 x-z plane with 64 wall-normal cells (9.4M cells): "
+                       "per-kernel ncu captures at the x/z line lengths of channel590 with ~3 GB resident",
     "cylinder100": "heated circular cylinder Re=100 Pr=0.71, 30D x 20D x pi D, 128x96x16 cells clustered at the "
                    "body (first spacing 0.02D), uniform inflow, convective outlet, slip lateral walls, periodic z, "
                    "dynamic SGS, direct-forcing IB, poiss_z_ft (z FFT + x-y multigrid)",
@@ -279,7 +283,8 @@ def time_form(args, form, lib, dev, world, rank, flush, full):
         tot_s = float(t.item())
     rep = s.report()
     import leswht_gb300
-    tuned = [{"dir": "xyz"[d], "components": nc, "fp32": bool(f32), "lanes_per_line": w} if d < 3 else
+    tuned = [{"dir": "xyz"[d], "components": nc, "fp32": bool(f32), "lanes_per_line": w & 63,
+              "register_capped": bool(w & 64)} if d < 3 else
              {"fft": "xyz"[nc], "lines_per_block": w} if d == 3 else {"mg_cluster_blocks": w}
              for d, nc, f32, w in leswht_gb300.tuning(lib, h)]
     out = {"case": case, "value": world * case.cells * args.steps / tot_s / 1e6, "autotune": tuned,

@@ -314,10 +314,11 @@ int lesgpu_launch_count(lesgpu_case *c, int64_t *kernels_per_step);
  * names a text file the table is read from before tuning and written back to
  * after, so several processes share one set of choices.  Writes up to maxn
  * tuples (dir 0..2 = x,y,z; components; fp32 0/1; lanes, 1 = one thread per
- * line) to out as 4 int64 each and their number to *nclasses; the Poisson
- * FFTs' lines per block, also timed at start, follow as (3, 2 = z | 0 = x,
- * 0, lines), and for poiss_z_ft the multigrid's blocks per cluster as
- * (4, 0, 0, blocks). */
+ * line, + 64 when the register-capped variant of the warp-scan kernel won)
+ * to out as 4 int64 each and their number to *nclasses; the Poisson FFTs'
+ * lines per block, also timed at start, follow as (3, 2 = z | 0 = x, 0,
+ * lines), and for poiss_z_ft / poiss_x_ft the multigrid's blocks per cluster
+ * as (4, 0, 0, blocks). */
 int lesgpu_tuning(lesgpu_case *c, int64_t *out, int64_t maxn, int64_t *nclasses);
 
 /* Event instrumentation of one kernel class for roofline measurements:

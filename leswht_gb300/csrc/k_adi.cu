@@ -90,29 +90,32 @@ __device__ __forceinline__ void adi_coef(const KP &p, int comp, int dir, int i, 
 // Elements per chunk: a thread issues the loads of CH consecutive line
 // elements before it runs the (serial) recurrence over them, so CH loads are
 // in flight instead of one.  Stores of a chunk follow all its loads, which
-// keeps in-place sweeps (src == dst) correct.
-constexpr int CH = 8;
+// keeps in-place sweeps (src == dst) correct.  The kernel is instantiated per
+// direction and periodicity, and its registers are capped so that 32 warps
+// fit on an SM: at large grids (lines >> threads) the serial sweep is
+// bound by memory latency and FP64 issue, both of which want occupancy.
+constexpr int CH = 4;
 
 struct AdiBatch {
     AdiArgs a[3];
 };
 
-template <class R>
-__global__ void __launch_bounds__(64) k_adi(KP p, AdiBatch B) {
+template <class R, int DIR, bool PER>
+__global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
     const AdiArgs &A = B.a[blockIdx.y];
     const DGrid &g = p.g;
     const R diag = (A.comp == CT) ? p.S->acoefi * p.c.pr : p.S->acoefi;
     int na = A.a1 - A.a0 + 1, nb = A.b1 - A.b0 + 1;
     long long nl = (long long)na * nb;
-    const long long stride = A.dir == 2 ? g.sxy : A.dir == 1 ? g.sx : 1;
+    const long long stride = DIR == 2 ? g.sxy : DIR == 1 ? g.sx : 1;
     const int nline = A.l2 - A.l1 + 1;
     if (nl <= 0 || A.l2 < A.l1) return;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nl; t += (long long)gridDim.x * blockDim.x) {
         const int x0 = A.a0 + (int)(t % na), x1 = A.b0 + (int)(t / na);
         int i0, j0, k0;
-        line_coords(A.dir, A.l1, x0, x1, i0, j0, k0);
+        line_coords(DIR, A.l1, x0, x1, i0, j0, k0);
         const long long q0 = g.ix(i0, j0, k0);
-        if (!A.periodic) {
+        if (!PER) {
             // ---- trdiag: forward elimination, chunk by chunk
             double *out = A.add ? A.sarr : A.dst;    // provisional solution
             R bet = R(0.0), x = R(0.0), cprev = R(0.0);
@@ -122,8 +125,8 @@ __global__ void __launch_bounds__(64) k_adi(KP p, AdiBatch B) {
                 for (int u = 0; u < CH; u++) {
                     if (c0 + u < nline) {
                         int i, j, k;
-                        line_coords(A.dir, A.l1 + c0 + u, x0, x1, i, j, k);
-                        adi_coef(p, A.comp, A.dir, i, j, k, av[u], cv[u]);
+                        line_coords(DIR, A.l1 + c0 + u, x0, x1, i, j, k);
+                        adi_coef(p, A.comp, DIR, i, j, k, av[u], cv[u]);
                         rv[u] = R(A.src[q0 + (long long)(c0 + u) * stride]);
                     }
                 }
@@ -188,8 +191,8 @@ __global__ void __launch_bounds__(64) k_adi(KP p, AdiBatch B) {
                 for (int u = 0; u < CH; u++) {
                     if (c0 + u < nline) {
                         int i, j, k;
-                        line_coords(A.dir, A.l1 + c0 + u, x0, x1, i, j, k);
-                        adi_coef(p, A.comp, A.dir, i, j, k, av[u], cv[u]);
+                        line_coords(DIR, A.l1 + c0 + u, x0, x1, i, j, k);
+                        adi_coef(p, A.comp, DIR, i, j, k, av[u], cv[u]);
                         rv[u] = R(A.src[q0 + (long long)(c0 + u) * stride]);
                     }
                 }
@@ -364,8 +367,11 @@ __device__ __forceinline__ R scan_affine_down(R C, R D, int lane) {
     return lane == W - 1 ? R(0.0) : Di;
 }
 
-template <class R, int MC, int W>
-__global__ void __launch_bounds__(128) k_adis(KP p, AdiBatch B) {
+// MINB > 1 caps the registers (65536 / (128 MINB) per thread) so that MINB
+// blocks fit on an SM: more warps in flight for some spilling -- which of the
+// two is faster depends on the shape, and the autotuner times both.
+template <class R, int MC, int W, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_adis(KP p, AdiBatch B) {
     const AdiArgs &A = B.a[blockIdx.y];
     const DGrid &g = p.g;
     const R diag = (A.comp == CT) ? p.S->acoefi * p.c.pr : p.S->acoefi;
@@ -600,15 +606,22 @@ __global__ void __launch_bounds__(128) k_adis(KP p, AdiBatch B) {
 }
 
 template <class R, int W>
-static bool adis_launch(lesgpu_case *c, const AdiBatch &B, int ncomp, long long mx, int nmax) {
+static bool adis_launch(lesgpu_case *c, const AdiBatch &B, int ncomp, long long mx, int nmax, bool capped) {
     const int m = (nmax + W - 1) / W;
     const long long lpb = 128 / W;
     dim3 grid((unsigned)((mx + lpb - 1) / lpb), (unsigned)ncomp);
-    if (m <= 2) k_adis<R, 2, W><<<grid, 128, 0, c->stream>>>(c->kp, B);
-    else if (m <= 4) k_adis<R, 4, W><<<grid, 128, 0, c->stream>>>(c->kp, B);
-    else if (m <= 8) k_adis<R, 8, W><<<grid, 128, 0, c->stream>>>(c->kp, B);
-    else if (m <= 12) k_adis<R, 12, W><<<grid, 128, 0, c->stream>>>(c->kp, B);
-    else return false;
+    // up to 4 rows per lane the kernel fits the cap anyway
+    if (m <= 2) k_adis<R, 2, W, 1><<<grid, 128, 0, c->stream>>>(c->kp, B);
+    else if (m <= 4) k_adis<R, 4, W, 1><<<grid, 128, 0, c->stream>>>(c->kp, B);
+    else if (m <= 8) {
+        if (capped) k_adis<R, 8, W, 4><<<grid, 128, 0, c->stream>>>(c->kp, B);
+        else k_adis<R, 8, W, 1><<<grid, 128, 0, c->stream>>>(c->kp, B);
+    } else if (m <= 12) {
+        if (capped) k_adis<R, 12, W, 4><<<grid, 128, 0, c->stream>>>(c->kp, B);
+        else k_adis<R, 12, W, 1><<<grid, 128, 0, c->stream>>>(c->kp, B);
+    } else {
+        return false;
+    }
     return true;
 }
 
@@ -640,26 +653,41 @@ static AdiShape adi_shape(const lesgpu_case *c, const AdiBatch &B, int ncomp) {
     return h;
 }
 
-// launch with W lanes per line; false if W cannot hold the line (MC <= 12)
-static bool adi_run(lesgpu_case *c, const AdiBatch &B, const AdiShape &h, int w) {
+// launch with W = w & 63 lanes per line (w & 64: the register-capped warp-scan
+// kernel); false if W cannot hold the line (MC <= 12)
+static bool adi_run(lesgpu_case *c, const AdiBatch &B, const AdiShape &h, int wcode) {
     if (h.mx <= 0) return true;
+    const int w = wcode & 63;
+    const bool capped = (wcode & 64) != 0;
     if (w <= 1) {
-        dim3 grid((unsigned)((h.mx + 31) / 32), (unsigned)h.ncomp);
-        if (h.f32) k_adi<float><<<grid, 32, 0, c->stream>>>(c->kp, B);
-        else k_adi<double><<<grid, 32, 0, c->stream>>>(c->kp, B);
+        // 128-thread blocks once the lines fill the GPU several times over,
+        // single-warp blocks (more SMs busy) below that
+        const int tpb = h.mx * h.ncomp >= 152LL * 512 ? 128 : 32;
+        const dim3 grid((unsigned)((h.mx + tpb - 1) / tpb), (unsigned)h.ncomp);
+        const int dir = B.a[0].dir;
+        const bool per = B.a[0].periodic != 0;
+        if (h.f32) {
+            if (dir == 0) { if (per) k_adi<float, 0, true><<<grid, tpb, 0, c->stream>>>(c->kp, B); else k_adi<float, 0, false><<<grid, tpb, 0, c->stream>>>(c->kp, B); }
+            else if (dir == 1) { if (per) k_adi<float, 1, true><<<grid, tpb, 0, c->stream>>>(c->kp, B); else k_adi<float, 1, false><<<grid, tpb, 0, c->stream>>>(c->kp, B); }
+            else { if (per) k_adi<float, 2, true><<<grid, tpb, 0, c->stream>>>(c->kp, B); else k_adi<float, 2, false><<<grid, tpb, 0, c->stream>>>(c->kp, B); }
+        } else {
+            if (dir == 0) { if (per) k_adi<double, 0, true><<<grid, tpb, 0, c->stream>>>(c->kp, B); else k_adi<double, 0, false><<<grid, tpb, 0, c->stream>>>(c->kp, B); }
+            else if (dir == 1) { if (per) k_adi<double, 1, true><<<grid, tpb, 0, c->stream>>>(c->kp, B); else k_adi<double, 1, false><<<grid, tpb, 0, c->stream>>>(c->kp, B); }
+            else { if (per) k_adi<double, 2, true><<<grid, tpb, 0, c->stream>>>(c->kp, B); else k_adi<double, 2, false><<<grid, tpb, 0, c->stream>>>(c->kp, B); }
+        }
         return true;
     }
     if (h.f32) {
         switch (w) {
-        case 8: return adis_launch<float, 8>(c, B, h.ncomp, h.mx, h.nmax);
-        case 16: return adis_launch<float, 16>(c, B, h.ncomp, h.mx, h.nmax);
-        case 32: return adis_launch<float, 32>(c, B, h.ncomp, h.mx, h.nmax);
+        case 8: return adis_launch<float, 8>(c, B, h.ncomp, h.mx, h.nmax, capped);
+        case 16: return adis_launch<float, 16>(c, B, h.ncomp, h.mx, h.nmax, capped);
+        case 32: return adis_launch<float, 32>(c, B, h.ncomp, h.mx, h.nmax, capped);
         }
     } else {
         switch (w) {
-        case 8: return adis_launch<double, 8>(c, B, h.ncomp, h.mx, h.nmax);
-        case 16: return adis_launch<double, 16>(c, B, h.ncomp, h.mx, h.nmax);
-        case 32: return adis_launch<double, 32>(c, B, h.ncomp, h.mx, h.nmax);
+        case 8: return adis_launch<double, 8>(c, B, h.ncomp, h.mx, h.nmax, capped);
+        case 16: return adis_launch<double, 16>(c, B, h.ncomp, h.mx, h.nmax, capped);
+        case 32: return adis_launch<double, 32>(c, B, h.ncomp, h.mx, h.nmax, capped);
         }
     }
     return false;
@@ -724,10 +752,13 @@ static void adi_tune_batch(lesgpu_case *c, AdiBatch B, int ncomp) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    const int cand[4] = {1, 8, 16, 32};
+    // the register-capped warp-scan variant only differs where a lane holds
+    // more than 4 rows
+    const int cand[7] = {1, 8, 16, 32, 8 | 64, 16 | 64, 32 | 64};
     int best = adi_default_w(h);
     float best_ms = 3.0e38f;
-    for (int q = 0; q < 4; q++) {
+    for (int q = 0; q < 7; q++) {
+        if ((cand[q] & 64) && (h.nmax + (cand[q] & 63) - 1) / (cand[q] & 63) <= 4) continue;
         if (!adi_run(c, B, h, cand[q])) continue;          // warm-up launch (also the feasibility check)
         cudaEventRecord(e0, c->stream);
         for (int r = 0; r < 3; r++) adi_run(c, B, h, cand[q]);

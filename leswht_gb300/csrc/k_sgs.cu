@@ -162,53 +162,55 @@ struct FiltBatch {
     int na;
 };
 
-template <class R>
-__device__ __forceinline__ R filt_x(const KP &p, const R *s, int i, long long qrow, int xf) {
-    const DGrid &g = p.g;
-    // qrow = index of (0, j, k)
-    if (!xf) return s[qrow + i];
-    const R *cf = mir<R>(p).cfx1 + 3 * i;
-    const R c0 = R(cf[0]), c1 = R(cf[1]), c2 = R(cf[2]);
-    if (i >= 2 && i <= g.n1m - 1)
-        return c0 * s[qrow + i - 1] + c1 * s[qrow + i] + c2 * s[qrow + i + 1];
-    if (p.c.xprdic == 1) {
-        if (g.n1m == 1) return s[qrow + i];
-        if (i == 1) return c0 * s[qrow + g.n1m] + c1 * s[qrow + 1] + c2 * s[qrow + 2];
-        return c0 * s[qrow + g.n1m - 1] + c1 * s[qrow + g.n1m] + c2 * s[qrow + 1];
-    }
-    return s[qrow + i];
-}
+// One cell's x filter (sgs.f90:650-733) of the rows qm, q0, qp of every array
+// of the batch is formed from the same offsets and weights: the cell's index
+// decoding, periodic wrap and weights are computed once for all arrays.
+struct FiltX {
+    int im, ip;              // x neighbours (wrapped); == i when x is not filtered here
+    bool filt;
+};
 
 template <class R>
 __global__ void __launch_bounds__(kThreads) k_filter(KP p, Box b, FiltBatch F) {
     const DGrid &g = p.g;
-    int xf = (p.c.filter == 1 || p.c.filter == 3) ? 1 : 0;
-    int zf = (p.c.filter == 2 || p.c.filter == 3) ? 1 : 0;
-    long long n = b.count();
-    long long tot = n * F.na;
-    for (long long tt = (long long)blockIdx.x * blockDim.x + threadIdx.x; tt < tot; tt += (long long)gridDim.x * blockDim.x) {
-        int a = (int)(tt / n);
+    const int xf = (p.c.filter == 1 || p.c.filter == 3) ? 1 : 0;
+    const int zf = (p.c.filter == 2 || p.c.filter == 3) ? 1 : 0;
+    const long long n = b.count();
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
-        b.at(tt - (long long)a * n, i, j, k);
-        const R *s = static_cast<const R *>(F.src[a]);
-        R out;
+        b.at(t, i, j, k);
+        // x: interior points use i-1, i, i+1; x-periodic ends wrap (with n1m = 1
+        // the value is unfiltered); other ends are unfiltered
+        FiltX X{i, i, false};
+        if (xf) {
+            if (i >= 2 && i <= g.n1m - 1) X = FiltX{i - 1, i + 1, true};
+            else if (p.c.xprdic == 1 && g.n1m > 1) X = FiltX{i == 1 ? g.n1m : g.n1m - 1, i == 1 ? 2 : 1, true};
+        }
+        const R *cfx = mir<R>(p).cfx1 + 3 * i;
+        const R c0 = X.filt ? R(cfx[0]) : R(0.0), c1 = X.filt ? R(cfx[1]) : R(0.0), c2 = X.filt ? R(cfx[2]) : R(0.0);
         // z-periodic ends use the wrapped neighbours; with n3m = 1 the weights
         // are zero (sgsfilterinit skips them), so the filtered value is 0 as
         // in test_filter (sgs.f90:735-764)
-        bool zin = zf && ((k >= 2 && k <= g.n3m - 1) || p.c.zprdic == 1);
-        if (!zin) {
-            out = filt_x<R>(p, s, i, g.ix(0, j, k), xf);
-        } else {
-            int km = k - 1, kp = k + 1;
-            if (k == 1) km = g.n3m;
-            if (k == g.n3m) kp = 1;
-            const R *cf = mir<R>(p).cfz1 + 3 * k;
-            R xm = filt_x<R>(p, s, i, g.ix(0, j, km), xf);
-            R x0 = filt_x<R>(p, s, i, g.ix(0, j, k), xf);
-            R xp = filt_x<R>(p, s, i, g.ix(0, j, kp), xf);
-            out = R(cf[0]) * xm + R(cf[1]) * x0 + R(cf[2]) * xp;
+        const bool zin = zf && ((k >= 2 && k <= g.n3m - 1) || p.c.zprdic == 1);
+        const int km = k == 1 ? g.n3m : k - 1, kp = k == g.n3m ? 1 : k + 1;
+        const R *cfz = mir<R>(p).cfz1 + 3 * k;
+        const R z0 = zin ? R(cfz[0]) : R(0.0), z1 = zin ? R(cfz[1]) : R(0.0), z2 = zin ? R(cfz[2]) : R(0.0);
+        const long long r0 = g.ix(0, j, k), rm = g.ix(0, j, km), rp = g.ix(0, j, kp);
+        for (int a = 0; a < F.na; a++) {
+            const R *s = static_cast<const R *>(F.src[a]);
+            R out;
+            if (!zin) {
+                out = X.filt ? c0 * s[r0 + X.im] + c1 * s[r0 + i] + c2 * s[r0 + X.ip] : s[r0 + i];
+            } else if (X.filt) {
+                const R xm = c0 * s[rm + X.im] + c1 * s[rm + i] + c2 * s[rm + X.ip];
+                const R x0 = c0 * s[r0 + X.im] + c1 * s[r0 + i] + c2 * s[r0 + X.ip];
+                const R xp = c0 * s[rp + X.im] + c1 * s[rp + i] + c2 * s[rp + X.ip];
+                out = z0 * xm + z1 * x0 + z2 * xp;
+            } else {
+                out = z0 * s[rm + i] + z1 * s[r0 + i] + z2 * s[rp + i];
+            }
+            static_cast<R *>(F.dst[a])[r0 + i] = out;
         }
-        static_cast<R *>(F.dst[a])[g.ix(i, j, k)] = out;
     }
 }
 
@@ -218,8 +220,8 @@ static void filter_batch(lesgpu_case *c, FiltBatch &F) {
     const DGrid &g = c->kp.g;
     Box b{1, 1, 1, g.n1m, g.n2m, g.n3m};
     inst_begin(c, LESGPU_K_SGS);
-    if (mixed(c)) k_filter<float><<<blocks_for(b.count() * F.na), kThreads, 0, c->stream>>>(c->kp, b, F);
-    else k_filter<double><<<blocks_for(b.count() * F.na), kThreads, 0, c->stream>>>(c->kp, b, F);
+    if (mixed(c)) k_filter<float><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, F);
+    else k_filter<double><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, F);
     inst_end(c, LESGPU_K_SGS);
 }
 

@@ -25,7 +25,7 @@ def test_tuned_classes_reported_and_reused(monkeypatch):
     dirs = {(d, nc, f32) for d, nc, f32, w in ta}
     # momentum (3 components) and temperature (1) in x, y, z; x/z in FP32, y in FP64
     assert {(0, 3, 1), (1, 3, 0), (2, 3, 1), (0, 1, 1), (1, 1, 0), (2, 1, 1)} <= dirs
-    assert all(w in (1, 8, 16, 32) for *_, w in ta)
+    assert all(w & 63 in (1, 8, 16, 32) and (w & 63 > 1 or w < 64) for *_, w in ta)   # + 64: register-capped
     b = leswht_gb300.gpu_solver(case)
     assert sorted(t for t in leswht_gb300.tuning(b.lib, b.h) if t[0] < 3) == sorted(ta)   # the process-wide table
     for _ in range(2):
