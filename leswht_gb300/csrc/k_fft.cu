@@ -100,26 +100,38 @@ DevPlan devplan(const FftPlan &p) {
     return d;
 }
 
-// ---- z transforms: block = (i-tile of L lines) x j ----------------------
+// ---- z transforms: block = (i-tile of 2L real lines) x j ------------------
+// Two real lines share one complex transform (the two-for-one real FFT):
+// c = a + i b, C = FFT(c), A_k = (C_k + conj C_{N-k}) / 2 and
+// B_k = (C_k - conj C_{N-k}) / (2i); the inverse transforms X + i Y of two
+// conjugate-symmetric spectra and takes x = Re, y = Im.  Half the transforms
+// of the real z lines, each exact up to rounding (on GB300 the FP64 pipe, not
+// memory, bounds these passes).  Line pair l holds i = i0 + 2l and i0 + 2l + 1.
 __global__ void k_fft_z_fwd(KP p, double2 *ccap, DevPlan P, int L, long long sk, long long sj) {
     extern __shared__ double2 sm[];
     const DGrid &g = p.g;
     const int N = P.n;
     double2 *b0 = sm, *b1 = sm + (size_t)N * L;
-    int i0 = 1 + blockIdx.x * L, j = 1 + blockIdx.y;
-    for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
-        int l = w % L, e = w / L;
-        int i = i0 + l;
-        double val = (i <= g.n1m) ? p.f.divgsum[g.ix(i, j, e + 1)] : 0.0;
-        b0[e * L + l] = make_double2(val, 0.0);
+    const int i0 = 1 + blockIdx.x * 2 * L, j = 1 + blockIdx.y;
+    for (int w = threadIdx.x; w < N * 2 * L; w += blockDim.x) {
+        const int l2 = w % (2 * L), e = w / (2 * L);       // consecutive threads: consecutive i
+        const int i = i0 + l2;
+        const double val = (i <= g.n1m) ? p.f.divgsum[g.ix(i, j, e + 1)] : 0.0;
+        double *slot = reinterpret_cast<double *>(&b0[e * L + (l2 >> 1)]);
+        slot[l2 & 1] = val;
     }
     __syncthreads();
-    double2 *res = block_fft(b0, b1, L, P, 0);
+    const double2 *res = block_fft(b0, b1, L, P, 0);
     const int n3mh = g.n3mh;
-    for (int w = threadIdx.x; w < n3mh * L; w += blockDim.x) {
-        int l = w % L, kk = w / L;
-        int i = i0 + l;
-        if (i <= g.n1m) ccap[(i - 1) + sk * kk + sj * (j - 1)] = res[kk * L + l];
+    for (int w = threadIdx.x; w < n3mh * 2 * L; w += blockDim.x) {
+        const int l2 = w % (2 * L), kk = w / (2 * L);
+        const int i = i0 + l2, l = l2 >> 1;
+        if (i > g.n1m) continue;
+        const double2 c = res[kk * L + l], cn = res[((N - kk) % N) * L + l];
+        // A_k = (C_k + conj C_{N-k}) / 2 ; B_k = -i (C_k - conj C_{N-k}) / 2
+        const double2 v = (l2 & 1) ? make_double2(0.5 * (c.y + cn.y), -0.5 * (c.x - cn.x))
+                                   : make_double2(0.5 * (c.x + cn.x), 0.5 * (c.y - cn.y));
+        ccap[(i - 1) + sk * kk + sj * (j - 1)] = v;
     }
 }
 
@@ -128,31 +140,36 @@ __global__ void k_fft_z_inv(KP p, const double2 *ccap, DevPlan P, int L, long lo
     const DGrid &g = p.g;
     const int N = P.n;
     double2 *b0 = sm, *b1 = sm + (size_t)N * L;
-    int i0 = 1 + blockIdx.x * L, j = 1 + blockIdx.y;
+    const int i0 = 1 + blockIdx.x * 2 * L, j = 1 + blockIdx.y;
     const int n3mh = g.n3mh;
-    for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
-        int l = w % L, e = w / L;
-        int i = i0 + l;
-        double2 val = make_double2(0.0, 0.0);
-        if (i <= g.n1m) {
-            if (e < n3mh) {
-                val = ccap[(i - 1) + sk * e + sj * (j - 1)];
-            } else {
-                // zzz(k) = conjg(zzz(n3m+2-k)), poiss_ftft.f90:143-147
-                int src = N - e;
-                double2 s = ccap[(i - 1) + sk * src + sj * (j - 1)];
-                val = make_double2(s.x, -s.y);
-            }
+    // coefficient e of line i (conjugate completion above n3mh, poiss_ftft.f90:143-147);
+    // the k = 0 and Nyquist coefficients enter through their real part only
+    // (the reference takes Re of the inverse)
+    auto coef = [&](int i, int e) -> double2 {
+        if (i > g.n1m) return make_double2(0.0, 0.0);
+        if (e < n3mh) {
+            double2 v = ccap[(i - 1) + sk * e + sj * (j - 1)];
+            if (e == 0 || 2 * e == N) v.y = 0.0;
+            return v;
         }
-        b0[e * L + l] = val;
+        const double2 s = ccap[(i - 1) + sk * (N - e) + sj * (j - 1)];
+        return make_double2(s.x, -s.y);
+    };
+    for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
+        const int l = w % L, e = w / L;
+        const double2 x = coef(i0 + 2 * l, e), y = coef(i0 + 2 * l + 1, e);
+        b0[e * L + l] = make_double2(x.x - y.y, x.y + y.x);     // Z = X + i Y
     }
     __syncthreads();
-    double2 *res = block_fft(b0, b1, L, P, 1);
+    const double2 *res = block_fft(b0, b1, L, P, 1);
     const double dn = 1.0 / (double)N;
-    for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
-        int l = w % L, e = w / L;
-        int i = i0 + l;
-        if (i <= g.n1m) p.f.phi[g.ix(i, j, e + 1)] = res[e * L + l].x * dn;
+    for (int w = threadIdx.x; w < N * 2 * L; w += blockDim.x) {
+        const int l2 = w % (2 * L), e = w / (2 * L);
+        const int i = i0 + l2;
+        if (i <= g.n1m) {
+            const double2 r = res[e * L + (l2 >> 1)];
+            p.f.phi[g.ix(i, j, e + 1)] = ((l2 & 1) ? r.y : r.x) * dn;
+        }
     }
 }
 
@@ -553,7 +570,7 @@ int fft_autotune(lesgpu_case *c) {
     const long long sk = ftft ? g.n1m : (long long)g.n1m * g.n2m;
     const long long sj = ftft ? (long long)g.n1m * g.n3mh : g.n1m;
     P.Lz = fft_time_pick(c, {0, g.n1m, g.n2m, g.n3m}, g.n3m, lines_per_block(g.n3m), [&](int L) {
-        const dim3 gz((g.n1m + L - 1) / L, g.n2m);
+        const dim3 gz((g.n1m + 2 * L - 1) / (2 * L), g.n2m);   // 2L real lines per block
         k_fft_z_fwd<<<gz, kThreads, (size_t)2 * g.n3m * L * sizeof(double2), c->stream>>>(c->kp, P.ccap, pz, L, sk, sj);
     });
     if (ftft) {
@@ -639,7 +656,7 @@ void launch_poisson(lesgpu_case *c, int msub) {
     DevPlan px = devplan(P.fx), pz = devplan(P.fz);
     const int Lz = fft_lz(c), Lx = fft_lx(c);
     size_t smz = (size_t)2 * g.n3m * Lz * sizeof(double2), smx = (size_t)2 * g.n1m * Lx * sizeof(double2);
-    dim3 gz((g.n1m + Lz - 1) / Lz, g.n2m);
+    dim3 gz((g.n1m + 2 * Lz - 1) / (2 * Lz), g.n2m);   // 2 Lz real lines per block
     int nxl = g.n3mh * g.n2m;
     inst_begin(c, LESGPU_K_POISSON);
     const long long sk = g.n1m, sj = (long long)g.n1m * g.n3mh;

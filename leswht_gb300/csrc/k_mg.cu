@@ -986,7 +986,7 @@ void launch_mg2d(lesgpu_case *c, int msub) {
         const DevPlan pz = devplan(P.fz);
         const int Lz = fft_lz(c);
         const size_t smz = (size_t)2 * (g.n3m > 1 ? g.n3m : 1) * Lz * sizeof(double2);
-        const dim3 gz((g.n1m + Lz - 1) / Lz, g.n2m);
+        const dim3 gz((g.n1m + 2 * Lz - 1) / (2 * Lz), g.n2m);   // 2 Lz real lines per block
         const long long sk = (long long)g.n1m * g.n2m, sj = g.n1m;
         k_fft_z_fwd<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
         launch_modes(c, mg_args(c, slot, 0), T->cs);

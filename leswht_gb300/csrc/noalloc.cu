@@ -182,7 +182,7 @@ extern "C" int lesgpu_poisson_ftft_noalloc(const lesgpu_grid *g, const double *d
     // the same launch sequence as the case-based solve (k_fft.cu launch_poisson)
     int Lz = lg::fft_lines_per_block(n3m), Lx = lg::fft_lines_per_block(n1m);
     size_t smz = (size_t)2 * n3m * Lz * sizeof(double2), smx = (size_t)2 * n1m * Lx * sizeof(double2);
-    dim3 gz((n1m + Lz - 1) / Lz, n2m);
+    dim3 gz((n1m + 2 * Lz - 1) / (2 * Lz), n2m);   // 2 Lz real lines per block
     int nxl = n3mh * n2m;
     const long long sk = n1m, sj = (long long)n1m * n3mh;
     lg::k_fft_z_fwd<<<gz, lg::kThreads, smz, st>>>(p, ccap, pz, Lz, sk, sj);
