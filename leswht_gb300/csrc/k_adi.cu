@@ -87,6 +87,27 @@ __device__ __forceinline__ void adi_coef(const KP &p, int comp, int dir, int i, 
     }
 }
 
+// Reciprocal of a pivot.  FP32: the division.  FP64: Newton-Raphson
+// iteration for 1/d, r <- r + r (1 - d r), from an FP32 reciprocal seed; each
+// step squares the relative error (2^-24 -> 2^-48 -> below the final
+// rounding), so the result is within 2 ulp of the quotient.  It takes six
+// operations on GB300's narrow FP64 pipe (two conversions, four FMAs) where a
+// correctly rounded division takes more.  Pivots outside the FP32 range, where
+// the seed would not exist, take the division.
+template <class R>
+__device__ __forceinline__ R rcp_pivot(R d) {
+    if (sizeof(R) == 4) return R(1.0) / d;
+    const float df = (float)d;
+    const float af = fabsf(df);
+    if (!(af > 1.0e-30f && af < 1.0e30f)) return R(1.0) / d;
+    double r = (double)__frcp_rn(df);
+    double e = fma(-(double)d, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-(double)d, r, 1.0);
+    r = fma(r, e, r);
+    return R(r);
+}
+
 // Elements per chunk: a thread issues the loads of CH consecutive line
 // elements before it runs the (serial) recurrence over them, so CH loads are
 // in flight instead of one.  Stores of a chunk follow all its loads, which
@@ -110,14 +131,24 @@ __global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
     const long long stride = DIR == 2 ? g.sxy : DIR == 1 ? g.sx : 1;
     const int nline = A.l2 - A.l1 + 1;
     if (nl <= 0 || A.l2 < A.l1) return;
+    // Forward-pass scratch in the arithmetic type: in FP32 the factors and
+    // provisional values never pass through FP64 (on GB300 a conversion issues
+    // on the narrow FP64 pipe) and move half the bytes.  An FP32 sweep keeps
+    // its three periodic vectors in the two scratch arrays (the gam array of
+    // nt doubles holds two float vectors).
+    constexpr bool F32 = sizeof(R) == 4;
+    R *const sg = reinterpret_cast<R *>(A.gam);
+    R *const ss = reinterpret_cast<R *>(A.sarr);
+    R *const sf = F32 ? reinterpret_cast<R *>(A.gam) + g.nt : nullptr;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nl; t += (long long)gridDim.x * blockDim.x) {
         const int x0 = A.a0 + (int)(t % na), x1 = A.b0 + (int)(t / na);
         int i0, j0, k0;
         line_coords(DIR, A.l1, x0, x1, i0, j0, k0);
         const long long q0 = g.ix(i0, j0, k0);
         if (!PER) {
-            // ---- trdiag: forward elimination, chunk by chunk
-            double *out = A.add ? A.sarr : A.dst;    // provisional solution
+            // ---- trdiag: forward elimination, chunk by chunk; the provisional
+            // solution goes to the scratch (FP32, or when adding) or to dst
+            R *xs = (F32 || A.add) ? ss : reinterpret_cast<R *>(A.dst);
             R bet = R(0.0), x = R(0.0), cprev = R(0.0);
             for (int c0 = 0; c0 < nline; c0 += CH) {
                 R av[CH], cv[CH], rv[CH];
@@ -137,15 +168,15 @@ __global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
                         const R a = av[u], c = cv[u];
                         const R b = diag - a - c;
                         if (c0 + u == 0) {
-                            bet = R(1.0) / b;
+                            bet = rcp_pivot(b);
                             x = diag * rv[u] * bet;
                         } else {
                             const R gm = cprev * bet;
-                            bet = R(1.0) / (b - a * gm);
+                            bet = rcp_pivot(b - a * gm);
                             x = (diag * rv[u] - a * x) * bet;
-                            A.gam[q] = gm;
+                            sg[q] = gm;
                         }
-                        out[q] = x;
+                        xs[q] = x;
                         cprev = c;
                     }
                 }
@@ -154,6 +185,7 @@ __global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
             R xn = x;
             const long long qlast = q0 + (long long)(nline - 1) * stride;
             if (A.add) A.dst[qlast] += xn;
+            else if (F32) A.dst[qlast] = xn;
             for (int c1 = nline - 2; c1 >= 0; c1 -= CH) {
                 R ov[CH], gv[CH], fv[CH];
 #pragma unroll
@@ -161,8 +193,8 @@ __global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
                     const int l = c1 - u;
                     if (l >= 0) {
                         const long long q = q0 + (long long)l * stride;
-                        ov[u] = R(out[q]);
-                        gv[u] = R(A.gam[q + stride]);
+                        ov[u] = xs[q];
+                        gv[u] = sg[q + stride];
                         if (A.add) fv[u] = R(A.dst[q]);
                     }
                 }
@@ -173,17 +205,20 @@ __global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
                         const long long q = q0 + (long long)l * stride;
                         const R xl = ov[u] - gv[u] * xn;
                         if (A.add) A.dst[q] = fv[u] + xl;
-                        else out[q] = xl;
+                        else if (F32) A.dst[q] = xl;
+                        else xs[q] = xl;
                         xn = xl;
                     }
                 }
             }
         } else {
-            // ---- trdiagp: forward sweep; q factors in gam, s in sarr, f in fw
-            double *fw = A.add ? (double *)A.src : A.dst;
+            // ---- trdiagp: forward sweep; q factors, s and f vectors in the
+            // scratch (FP64: q in gam, s in sarr, f in the source when adding,
+            // else in dst; FP32: q, f in gam's two halves, s in sarr)
+            R *fw = F32 ? sf : reinterpret_cast<R *>(A.add ? (double *)A.src : A.dst);
             const long long qn_last = q0 + (long long)(nline - 1) * stride;
             const R fn = diag * R(A.src[qn_last]);   // original right-hand side at the last element
-            R qq = R(0.0), ss = R(0.0), ff = R(0.0);
+            R qq = R(0.0), sv0 = R(0.0), ff = R(0.0);
             R a_last = R(0.0), b_last = R(0.0), c_last = R(0.0);
             for (int c0 = 0; c0 < nline; c0 += CH) {
                 R av[CH], cv[CH], rv[CH];
@@ -203,20 +238,20 @@ __global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
                         const R a = av[u], c = cv[u];
                         const R b = diag - a - c;
                         if (c0 + u == 0) {
-                            const R binv = R(1.0) / b;
+                            const R binv = rcp_pivot(b);
                             qq = -c * binv;
-                            ss = -a * binv;
+                            sv0 = -a * binv;
                             ff = diag * rv[u] * binv;
                         } else {
-                            const R pn = R(1.0) / (b + a * qq);
+                            const R pn = rcp_pivot(b + a * qq);
                             const R qn = -c * pn;
-                            const R sn = -a * ss * pn;
+                            const R sn = -a * sv0 * pn;
                             ff = (diag * rv[u] - a * ff) * pn;
                             qq = qn;
-                            ss = sn;
+                            sv0 = sn;
                         }
-                        A.gam[q] = qq;
-                        A.sarr[q] = ss;
+                        sg[q] = qq;
+                        ss[q] = sv0;
                         fw[q] = ff;
                         a_last = a; b_last = b; c_last = c;
                     }
@@ -231,9 +266,9 @@ __global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
                     const int l = c1 - u;
                     if (l >= 0) {
                         const long long q = q0 + (long long)l * stride;
-                        qv[u] = R(A.gam[q]);
-                        sv[u] = R(A.sarr[q]);
-                        fv[u] = R(fw[q]);
+                        qv[u] = sg[q];
+                        sv[u] = ss[q];
+                        fv[u] = fw[q];
                     }
                 }
 #pragma unroll
@@ -243,7 +278,7 @@ __global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
                         const long long q = q0 + (long long)l * stride;
                         const R sj = sv[u] + qv[u] * s_next;
                         const R qej = fv[u] + qv[u] * qe_next;
-                        A.sarr[q] = sj;
+                        ss[q] = sj;
                         fw[q] = qej;
                         if (l == nline - 2) { s_j2m1 = sj; qe_j2m1 = qej; }
                         s_next = sj;
@@ -253,7 +288,9 @@ __global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
             }
             const R s_j1 = s_next, qe_j1 = qe_next;
             const R fj2 = (fn - c_last * qe_j1 - a_last * qe_j2m1) / (c_last * s_j1 + a_last * s_j2m1 + b_last);
-            if (A.add) A.dst[qn_last] += fj2; else fw[qn_last] = fj2;
+            if (A.add) A.dst[qn_last] += fj2;
+            else if (F32) A.dst[qn_last] = fj2;
+            else fw[qn_last] = fj2;
             for (int c1 = nline - 2; c1 >= 0; c1 -= CH) {
                 R sv[CH], ev[CH], dv[CH];
 #pragma unroll
@@ -261,8 +298,8 @@ __global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
                     const int l = c1 - u;
                     if (l >= 0) {
                         const long long q = q0 + (long long)l * stride;
-                        sv[u] = R(A.sarr[q]);
-                        ev[u] = R(fw[q]);
+                        sv[u] = ss[q];
+                        ev[u] = fw[q];
                         if (A.add) dv[u] = R(A.dst[q]);
                     }
                 }
@@ -272,7 +309,9 @@ __global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
                     if (l >= 0) {
                         const long long q = q0 + (long long)l * stride;
                         const R val = fj2 * sv[u] + ev[u];
-                        if (A.add) A.dst[q] = dv[u] + val; else fw[q] = val;
+                        if (A.add) A.dst[q] = dv[u] + val;
+                        else if (F32) A.dst[q] = val;
+                        else fw[q] = val;
                     }
                 }
             }
@@ -435,11 +474,11 @@ __global__ void __launch_bounds__(128, MINB) k_adis(KP p, AdiBatch B) {
                 for (int u = 0; u < MC; u++)
                     if (u < cnt) {
                         if (lane == 0 && u == 0) {
-                            bet = R(1.0) / bv[u];
+                            bet = rcp_pivot(bv[u]);
                             gmv[u] = R(0.0);
                         } else {
                             const R gm = cp * bet;
-                            bet = R(1.0) / (bv[u] - av[u] * gm);
+                            bet = rcp_pivot(bv[u] - av[u] * gm);
                             gmv[u] = gm;
                         }
                         bv[u] = bet;          // bv now holds bet_j
@@ -498,7 +537,7 @@ __global__ void __launch_bounds__(128, MINB) k_adis(KP p, AdiBatch B) {
 #pragma unroll
             for (int u = 0; u < MC; u++)
                 if (u < cnt) {
-                    const R pn = (lane == 0 && u == 0) ? R(1.0) / bv[u] : R(1.0) / (bv[u] + av[u] * qq);
+                    const R pn = rcp_pivot((lane == 0 && u == 0) ? bv[u] : bv[u] + av[u] * qq);
                     qq = -cv[u] * pn;
                     qv[u] = qq;
                     pv[u] = pn;
@@ -903,3 +942,27 @@ int adi_tuned(const lesgpu_case *c, int *out, int maxn) {
 }
 
 }  // namespace lg
+
+// Self-check of the FP64 pivot reciprocal (no reference counterpart): r[q] =
+// rcp_pivot(x[q]) for n host values, so a test can bound its error.
+namespace lg {
+__global__ void k_rcp_check(const double *x, double *r, long long n) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) r[q] = rcp_pivot<double>(x[q]);
+}
+}  // namespace lg
+
+extern "C" int lesgpu_check_rcp(const double *x, double *r, int64_t n) {
+    if (n < 0 || (n > 0 && (!x || !r))) return LESGPU_ERR_ARG;
+    if (n == 0) return 0;
+    double *d = nullptr;
+    if (cudaMalloc(&d, sizeof(double) * 2 * (size_t)n) != cudaSuccess) return LESGPU_ERR_OOM;
+    int rc = 0;
+    if (cudaMemcpy(d, x, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess) rc = LESGPU_ERR_CUDA;
+    if (!rc) {
+        lg::k_rcp_check<<<(unsigned)((n + 255) / 256), 256>>>(d, d + n, (long long)n);
+        if (cudaMemcpy(r, d + n, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess) rc = LESGPU_ERR_CUDA;
+    }
+    cudaFree(d);
+    return rc;
+}
