@@ -287,6 +287,20 @@ int lesgpu_ibmpre_run(const lesgpu_config *cfg, const lesgpu_grid *grid, const d
 int lesgpu_ibmpre_tables(lesgpu_ibmpre *h, lesgpu_ibm *tables);
 int lesgpu_ibmpre_free(lesgpu_ibmpre *h);
 
+/* conjg_intp (ibm_body.f90:402-550, called by preprocessing.py:286 for
+ * CONJG-HTRANS): on the GPU, the conjugate heat-transfer tables of the cells
+ * 1..n?m -- c* = (1 - fp) cratio + fp from the cell's fluid fraction fp
+ * (fluid_portion, a flood fill on 6x6x6 sub-cells), the fluid mask omega
+ * (fp >= 1 - 1e-12), and k* of the east, west, north, south, top and bottom
+ * faces from the fluid fraction between the two cell centres (harmonic mean
+ * across the interface) -- for the body and periodicity of cfg, the
+ * pre-processor's coordinate vectors axes (as lesgpu_ibmpre_run) and the
+ * solid/fluid ratios cratio (heat capacity) and kratio (conductivity).
+ * Host outputs in lesgpu_ibm's layout: cstar[ncell], kstar[6 * ncell],
+ * omega[ncell], cells i fastest. */
+int lesgpu_conjg_run(const lesgpu_config *cfg, const lesgpu_grid *grid, const double *const axes[6],
+                     double cratio, double kratio, double *cstar, double *kstar, int64_t *omega);
+
 /* Phase-level access for parity tests (not needed by a driver). */
 int lesgpu_get_array(lesgpu_case *c, int64_t field, double *out);
 int lesgpu_set_array(lesgpu_case *c, int64_t field, const double *in);

@@ -302,6 +302,24 @@ def cylinder(n1m: int = 128, n2m: int = 96, n3m: int = 16, re: float = 100.0, pr
                 ihist=0, m=0, ibm=tables)
 
 
+def with_conjugate(case: Case, cratio: float, kratio: float) -> Case:
+    """The same case with conjugate heat transfer (ICONJG = 1): the body
+    conducts heat, with solid/fluid heat-capacity ratio cratio and
+    conductivity ratio kratio; c*, k* and the fluid mask omega come from
+    conjg_intp (the pre-processor's CONJG-HTRANS tables) instead of the
+    placeholders, and the body gets no thermal direct forcing."""
+    from .gridgen import axis_vectors
+    s = dict(case.settings)
+    s["iconjg"] = 1
+    axes = axis_vectors(case.grid_dat, s.get("xprdic", 0) == 1, s.get("yprdic", 0) == 1, s.get("zprdic", 0) == 1)
+    cs, ks, om = ibmpre.conjg_intp(s["body"], cratio, kratio, axes,
+                                   (s.get("xprdic", 0), s.get("yprdic", 0), s.get("zprdic", 0)))
+    ibm = dict(case.ibm)
+    ibm["cstar"], ibm["kstar"], ibm["omega"] = cs.reshape(-1), ks.reshape(-1), om.reshape(-1)
+    return Case(case.name + "_conjg", s, case.grid, case.grid_dat, case.grid_bin, case.fields, time=case.time,
+                dt=case.dt, ihist=case.ihist, m=case.m, ibm=ibm)
+
+
 def with_poisson(case: Case, poisson: int, nlev: Optional[int] = None) -> Case:
     """The same case solved with another of the reference's Poisson solvers.
     For poiss_mgrd (x and z coarsened together) the default NLEV is the

@@ -295,6 +295,99 @@ __global__ void k_zero_nu(Body b, const double *xm, const double *ym, const doub
     }
 }
 
+// ---- conjg_intp (ibm_body.f90:402-550) and fluid_portion (:553-667) ------
+// fluid_portion flood-fills a 6x6x6 sub-cell grid from sub-cell (1,1,1)
+// through 6-connected sub-cells of its phase; the sub-cells it never reaches
+// take the opposite phase.  The result is therefore the start sub-cell's
+// same-phase component, whatever the order of the fill: here the phases are
+// one 36-bit word per z layer (bit i + 6 j) and the component grows by bit
+// dilation (x: shift by 1 within a row, y: by 6, z: the neighbouring words)
+// until it stops changing.
+__device__ double fluid_portion(const Body &b, double x1, double x2, double y1, double y2, double z1, double z2) {
+    const double tx = __ddiv_rn(__dsub_rn(x2, x1), 6.0), ty = __ddiv_rn(__dsub_rn(y2, y1), 6.0),
+                 tz = __ddiv_rn(__dsub_rn(z2, z1), 6.0);
+    const unsigned long long full = (1ULL << 36) - 1ULL;
+    const unsigned long long notI0 = full & ~0x041041041ULL, notI5 = full & ~0x820820820ULL;
+    unsigned long long sol[6];
+    for (int k = 0; k < 6; k++) {
+        const double zc = __dadd_rn(z1, __dmul_rn(tz, (double)k + 0.5));   // dble(2 kk - 1) / 2
+        unsigned long long w = 0ULL;
+        for (int j = 0; j < 6; j++) {
+            const double yc = __dadd_rn(y1, __dmul_rn(ty, (double)j + 0.5));
+            for (int i = 0; i < 6; i++) {
+                const double xc = __dadd_rn(x1, __dmul_rn(tx, (double)i + 0.5));
+                if (fbody(b, xc, yc, zc) <= 1.0e-10) w |= 1ULL << (i + 6 * j);
+            }
+        }
+        sol[k] = w;
+    }
+    const bool s0 = (sol[0] & 1ULL) != 0ULL;
+    unsigned long long same[6], r[6];
+    for (int k = 0; k < 6; k++) { same[k] = s0 ? sol[k] : (~sol[k] & full); r[k] = 0ULL; }
+    r[0] = 1ULL;
+    for (int it = 0; it < 216; it++) {          // the component gains a sub-cell per pass or stops
+        unsigned long long nr[6];
+        bool changed = false;
+        for (int k = 0; k < 6; k++) {
+            unsigned long long gw = r[k] | ((r[k] << 1) & notI0) | ((r[k] >> 1) & notI5) | ((r[k] << 6) & full) | (r[k] >> 6);
+            if (k > 0) gw |= r[k - 1];
+            if (k < 5) gw |= r[k + 1];
+            nr[k] = gw & same[k];
+            changed |= nr[k] != r[k];
+        }
+        for (int k = 0; k < 6; k++) r[k] = nr[k];
+        if (!changed) break;
+    }
+    int comp = 0;
+    for (int k = 0; k < 6; k++) comp += __popcll(r[k]);
+    const int nsolid = s0 ? comp : 216 - comp;
+    return __dsub_rn(1.0, __ddiv_rn((double)nsolid, 216.0));
+}
+
+struct ConjgArgs {
+    Body b;
+    const double *x, *xm, *y, *ym, *z, *zm;   // 0..n? (the pre-processor's vectors)
+    int nx, ny, nz, xpr, ypr, zpr;
+    double cratio, kratio;
+    double *cstar, *kstar;                     // cells i fastest; kstar: 6 faces of ncell
+    long long *omega;
+};
+
+// one thread per (cell, box): box 0 is the cell (c*, omega), boxes 1..6 the
+// east, west, north, south, top and bottom faces (k*)
+__global__ void k_conjg(ConjgArgs A) {
+    const int mx = A.nx - 1, my = A.ny - 1, mz = A.nz - 1;
+    const long long ncell = (long long)mx * my * mz;
+    GLOOP(t, 7 * ncell) {
+        const int f = (int)(t % 7);
+        const long long c = t / 7;
+        const int i = 1 + (int)(c % mx), j = 1 + (int)((c / mx) % my), k = 1 + (int)(c / ((long long)mx * my));
+        double x1 = A.x[i], x2 = A.x[i + 1], y1 = A.y[j], y2 = A.y[j + 1], z1 = A.z[k], z2 = A.z[k + 1];
+        double nxc = A.xm[i], nyc = A.ym[j], nzc = A.zm[k];       // neighbour centre of the face
+        const double lx = __dsub_rn(A.x[A.nx], A.x[1]), ly = __dsub_rn(A.y[A.ny], A.y[1]), lz = __dsub_rn(A.z[A.nz], A.z[1]);
+        switch (f) {
+        case 1: nxc = (A.xpr == 1 && i == A.nx - 1) ? __dadd_rn(A.xm[1], lx) : A.xm[i + 1]; x1 = A.xm[i]; x2 = nxc; break;
+        case 2: nxc = (A.xpr == 1 && i == 1) ? __dsub_rn(A.xm[A.nx - 1], lx) : A.xm[i - 1]; x1 = nxc; x2 = A.xm[i]; break;
+        case 3: nyc = (A.ypr == 1 && j == A.ny - 1) ? __dadd_rn(A.ym[1], ly) : A.ym[j + 1]; y1 = A.ym[j]; y2 = nyc; break;
+        case 4: nyc = (A.ypr == 1 && j == 1) ? __dsub_rn(A.ym[A.ny - 1], ly) : A.ym[j - 1]; y1 = nyc; y2 = A.ym[j]; break;
+        case 5: nzc = (A.zpr == 1 && k == A.nz - 1) ? __dadd_rn(A.zm[1], lz) : A.zm[k + 1]; z1 = A.zm[k]; z2 = nzc; break;
+        case 6: nzc = (A.zpr == 1 && k == 1) ? __dsub_rn(A.zm[A.nz - 1], lz) : A.zm[k - 1]; z1 = nzc; z2 = A.zm[k]; break;
+        default: break;
+        }
+        const double fp = fluid_portion(A.b, x1, x2, y1, y2, z1, z2);
+        const double mix = __dadd_rn(__dmul_rn(__dsub_rn(1.0, fp), f == 0 ? A.cratio : A.kratio), __dmul_rn(fp, 1.0));
+        if (f == 0) {
+            A.cstar[c] = mix;
+            A.omega[c] = fp >= (1.0 - 1.0e-12) ? 1 : 0;
+        } else {
+            const double aa = fbody(A.b, A.xm[i], A.ym[j], A.zm[k]);
+            const bool same = __dmul_rn(aa, fbody(A.b, nxc, nyc, nzc)) >= 0.0;
+            A.kstar[(long long)(f - 1) * ncell + c] =
+                same ? mix : __ddiv_rn(A.kratio, __dadd_rn(__dmul_rn(A.kratio, fp), __dmul_rn(1.0, __dsub_rn(1.0, fp))));
+        }
+    }
+}
+
 struct DevBuf {
     std::vector<void *> p;
     bool ok = true;
@@ -455,3 +548,34 @@ extern "C" int lesgpu_ibmpre_free(lesgpu_ibmpre *h) {
     delete h;
     return 0;
 }
+
+extern "C" int lesgpu_conjg_run(const lesgpu_config *cfg, const lesgpu_grid *g, const double *const axes[6],
+                                double cratio, double kratio, double *cstar, double *kstar, int64_t *omega) {
+    if (!cfg || !g || !axes || !cstar || !kstar || !omega) return LESGPU_ERR_ARG;
+    for (int a = 0; a < 6; a++)
+        if (!axes[a]) return LESGPU_ERR_ARG;
+    if (g->n1 != g->n1m + 1 || g->n2 != g->n2m + 1 || g->n3 != g->n3m + 1 || g->n1m < 1 || g->n2m < 1 || g->n3m < 1)
+        return LESGPU_ERR_ARG;
+    const int n[3] = {(int)g->n1, (int)g->n2, (int)g->n3};
+    const long long ncell = (long long)g->n1m * g->n2m * g->n3m;
+    DevBuf B;
+    ConjgArgs A;
+    const double *d[6];
+    for (int a = 0; a < 6; a++) d[a] = B.up(axes[a], (size_t)n[a / 2] + 1);
+    A.x = d[0]; A.xm = d[1]; A.y = d[2]; A.ym = d[3]; A.z = d[4]; A.zm = d[5];
+    A.b = Body{(int)cfg->body.kind, cfg->body.cx, cfg->body.cy, cfg->body.cz, cfg->body.r, cfg->body.p0};
+    A.nx = n[0]; A.ny = n[1]; A.nz = n[2];
+    A.xpr = (int)cfg->xprdic; A.ypr = (int)cfg->yprdic; A.zpr = (int)cfg->zprdic;
+    A.cratio = cratio; A.kratio = kratio;
+    A.cstar = B.get<double>((size_t)ncell);
+    A.kstar = B.get<double>((size_t)6 * ncell);
+    A.omega = B.get<long long>((size_t)ncell);
+    if (!B.ok) return LESGPU_ERR_OOM;
+    k_conjg<<<blocks_for(7 * ncell, 128), 128>>>(A);
+    if (cudaMemcpy(cstar, A.cstar, sizeof(double) * (size_t)ncell, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(kstar, A.kstar, sizeof(double) * 6 * (size_t)ncell, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(omega, A.omega, sizeof(int64_t) * (size_t)ncell, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return LESGPU_ERR_CUDA;
+    return 0;
+}
+

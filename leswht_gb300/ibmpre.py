@@ -11,6 +11,10 @@ compiler:
   geomfac_preset   ibm_body.f90:126-157  coordinate tables with one ghost on each side
   geomfac_intp     ibm_body.f90:160-322  3x3x3 interpolation weights from the surface point
   find_zero_nu_sgs ibm_body.f90:357-399  zero-eddy-viscosity cells (7-point test)
+  conjg_intp       ibm_body.f90:402-550  conjugate heat transfer: c*, k* on the six
+                                         faces and the fluid mask omega, from
+  fluid_portion    ibm_body.f90:553-667  the fluid fraction of a box by a flood fill
+                                         on 6x6x6 sub-cells
 and the way preprocessing.py writes them (lib_preprocessing.py:223-328):
 geomfac rounded to '%15.8f', the zero-viscosity list written 0-based and read
 back by the solver as if 1-based (kept, the solver's behaviour depends on it).
@@ -195,6 +199,127 @@ def find_zero_nu_sgs(body, xm, ym, zm):
     return np.where(c, 0, 1).astype(np.int64)
 
 
+_SUBC = 6   # sub-cells per direction of fluid_portion (ibm_body.f90:425)
+
+
+def fluid_portion(body, x1, x2, y1, y2, z1, z2):
+    """fluid_portion (ibm_body.f90:553-667) of the boxes [x1,x2]x[y1,y2]x[z1,z2]
+    (arrays of one shape).  The reference flood-fills from sub-cell (1,1,1)
+    through 6-connected sub-cells of its phase, stops at sub-cells of the other
+    phase, and gives every sub-cell it never reached the opposite phase; so the
+    start sub-cell's 6-connected same-phase component keeps the start phase and
+    every other sub-cell takes the opposite one, whatever the order of the
+    fill.  Returns 1 - (solid sub-cells) / 216."""
+    d = _SUBC
+    x1, x2, y1, y2, z1, z2 = (np.asarray(v, dtype=np.float64).reshape(-1) for v in (x1, x2, y1, y2, z1, z2))
+    f = (2.0 * np.arange(1, d + 1) - 1.0) / 2.0                  # dble(2 ii - 1) / 2
+    xs = x1[:, None] + ((x2 - x1) / float(d))[:, None] * f[None, :]
+    ys = y1[:, None] + ((y2 - y1) / float(d))[:, None] * f[None, :]
+    zs = z1[:, None] + ((z2 - z1) / float(d))[:, None] * f[None, :]
+    solid = funcbody(body, xs[:, None, None, :], ys[:, None, :, None], zs[:, :, None, None]) <= 1.0e-10   # [p, k, j, i]
+    start_solid = solid[:, 0, 0, 0]
+    same = solid == start_solid[:, None, None, None]
+    reach = np.zeros_like(same)
+    reach[:, 0, 0, 0] = True
+    while True:
+        grow = reach.copy()
+        grow[:, 1:] |= reach[:, :-1]
+        grow[:, :-1] |= reach[:, 1:]
+        grow[:, :, 1:] |= reach[:, :, :-1]
+        grow[:, :, :-1] |= reach[:, :, 1:]
+        grow[:, :, :, 1:] |= reach[:, :, :, :-1]
+        grow[:, :, :, :-1] |= reach[:, :, :, 1:]
+        grow &= same
+        if np.array_equal(grow, reach):
+            break
+        reach = grow
+    comp = reach.reshape(reach.shape[0], -1).sum(axis=1)
+    nsolid = np.where(start_solid, comp, d ** 3 - comp)
+    return 1.0 - nsolid.astype(np.float64) / float(d ** 3)
+
+
+def fluid_portion_fill(body, x1, x2, y1, y2, z1, z2):
+    """fluid_portion of one box by the reference's own stack flood fill (a
+    literal restatement for small checks of fluid_portion)."""
+    d = _SUBC
+    def solid_at(ii, jj, kk):
+        xc = x1 + (x2 - x1) / float(d) * (float(2 * ii - 1) / 2.0)
+        yc = y1 + (y2 - y1) / float(d) * (float(2 * jj - 1) / 2.0)
+        zc = z1 + (z2 - z1) / float(d) * (float(2 * kk - 1) / 2.0)
+        return bool(funcbody(body, np.float64(xc), np.float64(yc), np.float64(zc)) <= 1.0e-10)
+    phase = {}
+    start = 0 if solid_at(1, 1, 1) else 1
+    phase[(1, 1, 1)] = start
+    stack = [(1, 1, 1)]
+    while stack:
+        i, j, k = stack.pop()
+        for kk in (k - 1, k, k + 1):
+            for jj in (j - 1, j, j + 1):
+                for ii in (i - 1, i, i + 1):
+                    if abs(ii - i) + abs(jj - j) + abs(kk - k) != 1:
+                        continue
+                    if not (1 <= ii <= d and 1 <= jj <= d and 1 <= kk <= d) or (ii, jj, kk) in phase:
+                        continue
+                    phase[(ii, jj, kk)] = 0 if solid_at(ii, jj, kk) else 1
+                    if phase[(ii, jj, kk)] == start:
+                        stack.append((ii, jj, kk))
+    nsolid = sum(1 for k in range(1, d + 1) for j in range(1, d + 1) for i in range(1, d + 1)
+                 if phase.get((i, j, k), 1 - start) == 0)
+    return 1.0 - float(nsolid) / float(d ** 3)
+
+
+def conjg_intp(body, cratio: float, kratio: float, gdat_axes, prdic, chunk: int = 4096):
+    """conjg_intp (ibm_body.f90:402-550) on the cells 1..n-1 of each
+    direction: c* = (1 - fp) cratio + fp for the cell's fluid fraction fp;
+    omega = 1 where fp >= 1 - 1e-12; k* of the six faces (east, west, north,
+    south, top, bottom) from the fluid fraction of the box between the two
+    cell centres -- (1 - fp) kratio + fp when the centres share a phase, else
+    the harmonic mean kratio / (kratio fp + (1 - fp)) -- with periodic wraps
+    shifted by the domain length.  Returns (cstar[k, j, i], kstar[6, k, j, i],
+    omega[k, j, i])."""
+    X, XM = (np.asarray(v, dtype=np.float64) for v in gdat_axes["x"])
+    Y, YM = (np.asarray(v, dtype=np.float64) for v in gdat_axes["y"])
+    Z, ZM = (np.asarray(v, dtype=np.float64) for v in gdat_axes["z"])
+    nx, ny, nz = len(X) - 1, len(Y) - 1, len(Z) - 1
+    xpr, ypr, zpr = (int(v) for v in prdic)
+    lx, ly, lz = X[nx] - X[1], Y[ny] - Y[1], Z[nz] - Z[1]
+    kk, jj, ii = np.meshgrid(np.arange(1, nz), np.arange(1, ny), np.arange(1, nx), indexing="ij")
+    i, j, k = ii.reshape(-1), jj.reshape(-1), kk.reshape(-1)
+    xm, ym, zm = XM[i], YM[j], ZM[k]
+    aa = funcbody(body, xm, ym, zm)
+    xmp = np.where((xpr == 1) & (i == nx - 1), XM[1] + lx, XM[np.minimum(i + 1, nx)])
+    xmm = np.where((xpr == 1) & (i == 1), XM[nx - 1] - lx, XM[i - 1])
+    ymp = np.where((ypr == 1) & (j == ny - 1), YM[1] + ly, YM[np.minimum(j + 1, ny)])
+    ymm = np.where((ypr == 1) & (j == 1), YM[ny - 1] - ly, YM[j - 1])
+    zmp = np.where((zpr == 1) & (k == nz - 1), ZM[1] + lz, ZM[np.minimum(k + 1, nz)])
+    zmm = np.where((zpr == 1) & (k == 1), ZM[nz - 1] - lz, ZM[k - 1])
+    boxes = [  # (x1, x2, y1, y2, z1, z2), neighbour centre for the phase test
+        ((X[i], X[i + 1], Y[j], Y[j + 1], Z[k], Z[k + 1]), None),
+        ((xm, xmp, Y[j], Y[j + 1], Z[k], Z[k + 1]), (xmp, ym, zm)),
+        ((xmm, xm, Y[j], Y[j + 1], Z[k], Z[k + 1]), (xmm, ym, zm)),
+        ((X[i], X[i + 1], ym, ymp, Z[k], Z[k + 1]), (xm, ymp, zm)),
+        ((X[i], X[i + 1], ymm, ym, Z[k], Z[k + 1]), (xm, ymm, zm)),
+        ((X[i], X[i + 1], Y[j], Y[j + 1], zm, zmp), (xm, ym, zmp)),
+        ((X[i], X[i + 1], Y[j], Y[j + 1], zmm, zm), (xm, ym, zmm)),
+    ]
+    n = i.size
+    shape = (nz - 1, ny - 1, nx - 1)
+    kstar = np.empty((6, n))
+    cstar = None
+    omega = None
+    for f, (box, nbr) in enumerate(boxes):
+        fp = np.concatenate([fluid_portion(body, *(b[s:s + chunk] for b in box)) for s in range(0, n, chunk)]) \
+            if n else np.zeros(0)
+        if nbr is None:
+            cstar = (1.0 - fp) * cratio + fp * 1.0
+            omega = np.where(fp >= (1.0 - 1.0e-12), 1, 0).astype(np.int64)
+        else:
+            same = aa * funcbody(body, *nbr) >= 0.0
+            kstar[f - 1] = np.where(same, (1.0 - fp) * kratio + fp * 1.0,
+                                    kratio / (kratio * fp + 1.0 * (1.0 - fp)))
+    return cstar.reshape(shape), kstar.reshape((6,) + shape), omega.reshape(shape)
+
+
 def _round8(gf):
     """geomfac as the solver reads it back from '%15.8f' text."""
     return np.array([float("%15.8f" % v) for v in gf.reshape(-1)]).reshape(gf.shape)
@@ -284,3 +409,26 @@ def build_tables_gpu(lib, settings, grid, gdat_axes) -> Dict:
         return out
     finally:
         lib.lesgpu_ibmpre_free(h)
+
+
+def conjg_tables_gpu(lib, settings, grid, gdat_axes, cratio: float, kratio: float):
+    """conjg_intp computed on the GPU (lesgpu_conjg_run): (cstar, kstar,
+    omega) flattened as lesgpu_ibm holds them (cells i fastest; kstar face by
+    face), the layout conjg_intp's arrays take under reshape(-1)."""
+    import ctypes as C
+    fn = lib.lesgpu_conjg_run
+    fn.argtypes = [C.POINTER(abi.Config), C.POINTER(abi.Grid), C.POINTER(abi.PD), C.c_double, C.c_double,
+                   C.c_void_p, C.c_void_p, C.c_void_p]
+    fn.restype = C.c_int
+    cfg = abi.pack_config(settings)
+    gr = abi.pack_grid(grid)
+    vecs = [np.ascontiguousarray(v, dtype=np.float64) for ax in ("x", "y", "z") for v in gdat_axes[ax]]
+    arr = (abi.PD * 6)(*[v.ctypes.data_as(abi.PD) for v in vecs])
+    n = grid.n1m * grid.n2m * grid.n3m
+    cs, ks, om = np.empty(n), np.empty(6 * n), np.empty(n, np.int64)
+    rc = fn(C.byref(cfg), C.byref(gr.struct), arr, float(cratio), float(kratio),
+            cs.ctypes.data, ks.ctypes.data, om.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"lesgpu_conjg_run: {abi.ERR_NAMES.get(rc, rc)}")
+    return cs, ks, om
+

@@ -97,3 +97,38 @@ def test_geomfac_preset_keeps_the_unset_periodic_ghosts():
     a = ibmpre.geomfac_preset(coord, center)
     assert a.shape == (len(coord) + 2, 3)
     assert np.all(a[0] == 0.0) and np.all(a[-1] == 0.0)
+
+
+@pytest.mark.parametrize("kind, z", [(abi.BODY_CYLINDER, (0.0, 0.3)), (abi.BODY_SPHERE, None), (abi.BODY_SQUARE, (0.0, 0.2))])
+def test_fluid_portion_is_the_reference_flood_fill(kind, z):
+    """fluid_portion (the start sub-cell's same-phase component) equals the
+    reference's stack flood fill with its fill-then-assign rule, on boxes
+    cut by the surface."""
+    rng = np.random.default_rng(11)
+    body = dict(kind=kind, cx=0.05, cy=-0.1, cz=0.02, r=0.45, p0=0.0)
+    n = 120
+    cx, cy = rng.uniform(-0.7, 0.7, n), rng.uniform(-0.7, 0.7, n)
+    w, h = rng.uniform(0.05, 0.7, n), rng.uniform(0.05, 0.7, n)
+    if z is None:
+        z1 = rng.uniform(-0.6, 0.4, n)
+        z2 = z1 + rng.uniform(0.05, 0.6, n)
+    else:
+        z1, z2 = np.full(n, z[0]), np.full(n, z[1])
+    box = (cx - w / 2, cx + w / 2, cy - h / 2, cy + h / 2, z1, z2)
+    fast = ibmpre.fluid_portion(body, *box)
+    fill = np.array([ibmpre.fluid_portion_fill(body, *(v[q] for v in box)) for q in range(n)])
+    assert np.array_equal(fast, fill)
+    assert np.unique(fast[(fast > 0.0) & (fast < 1.0)]).size > 10     # many boxes cut by the surface
+
+
+def test_conjugate_tables_on_a_cylinder():
+    """c* and k* are the fluid values (1) away from the body, the solid ratios
+    inside, and the harmonic mean across the interface; omega marks the cells
+    entirely in the fluid."""
+    c = cases.cylinder(32, 24, 4, nlev=2)
+    axes = axis_vectors(c.grid_dat, False, False, True)
+    cs, ks, om = ibmpre.conjg_intp(c.settings["body"], 0.5, 4.0, axes, (0, 0, 1))
+    assert set(np.unique(om)) == {0, 1}
+    assert np.all(cs[om == 1] == 1.0) and cs.min() == 0.5
+    assert np.all((ks >= 1.0) & (ks <= 4.0)) and ks.max() == 4.0
+    assert np.all(ks[:, om == 1][0] >= 1.0)

@@ -56,3 +56,20 @@ def test_step_with_gpu_tables_equals_host_tables():
     fa, fb = a.fields(), b.fields()
     for k in ("u", "v", "w", "p", "t"):
         assert np.array_equal(fa[k], fb[k]), k
+
+
+@pytest.mark.parametrize("name", ["cylinder_64x48x8", "cylinder_row", "sphere", "square"])
+def test_conjugate_tables_match_host(name):
+    """conjg_intp on the GPU (lesgpu_conjg_run) equals the host restatement
+    bit for bit: c*, the six face k* and the fluid mask."""
+    build, prd = CASES[name]
+    c = build()
+    axes = gridgen.axis_vectors(c.grid_dat, *prd)
+    flags = tuple(int(v) for v in prd)
+    s = dict(c.settings, xprdic=flags[0], yprdic=flags[1], zprdic=flags[2])
+    cs, ks, om = ibmpre.conjg_intp(s["body"], 0.4, 25.0, axes, flags)
+    gc, gk, go = ibmpre.conjg_tables_gpu(leswht_gb300.load_library(), s, c.grid, axes, 0.4, 25.0)
+    assert np.array_equal(gc.view(np.int64), cs.reshape(-1).view(np.int64))
+    assert np.array_equal(gk.view(np.int64), ks.reshape(-1).view(np.int64))
+    assert np.array_equal(go, om.reshape(-1))
+    assert 0 < int(om.sum()) < om.size and np.unique(ks).size > 3      # a real interface
