@@ -285,7 +285,8 @@ def time_form(args, form, lib, dev, world, rank, flush, full):
     import leswht_gb300
     tuned = [{"dir": "xyz"[d], "components": nc, "fp32": bool(f32), "lanes_per_line": w & 63,
               "register_capped": bool(w & 64)} if d < 3 else
-             {"fft": "xyz"[nc], "lines_per_block": w} if d == 3 else {"mg_cluster_blocks": w}
+             {"fft": "xyz"[nc], "lines_per_block": w} if d == 3 else {"mg_cluster_blocks": w} if d == 4 else
+             {"ftft_fp32_with_fp64_correction": bool(w)}
              for d, nc, f32, w in leswht_gb300.tuning(lib, h)]
     out = {"case": case, "value": world * case.cells * args.steps / tot_s / 1e6, "autotune": tuned,
            "ms_per_step": tot_s / args.steps * 1e3, "kernels_per_step": int(kps.value),

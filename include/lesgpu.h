@@ -331,8 +331,10 @@ int lesgpu_launch_count(lesgpu_case *c, int64_t *kernels_per_step);
  * line, + 64 when the register-capped variant of the warp-scan kernel won)
  * to out as 4 int64 each and their number to *nclasses; the Poisson FFTs'
  * lines per block, also timed at start, follow as (3, 2 = z | 0 = x, 0,
- * lines), and for poiss_z_ft / poiss_x_ft the multigrid's blocks per cluster
- * as (4, 0, 0, blocks). */
+ * lines), for poiss_z_ft / poiss_x_ft the multigrid's blocks per cluster
+ * as (4, 0, 0, blocks), and for poiss_ftft in the mixed form the solve chosen
+ * as (5, 0, 0, 1 = FP32 transforms under an FP64 defect correction | 0 =
+ * FP64 transforms); LESGPU_FFT_MIXED=1 / 0 forces either. */
 int lesgpu_tuning(lesgpu_case *c, int64_t *out, int64_t maxn, int64_t *nclasses);
 
 /* Event instrumentation of one kernel class for roofline measurements:

@@ -24,20 +24,25 @@
 #include <functional>
 #include <map>
 #include <mutex>
+#include <vector>
 
 namespace lg {
 
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+// complex arithmetic on double2 / float2 and the twiddle table of the type
+template <class V> __device__ __forceinline__ V cmul(V a, V b) { return V{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+template <class V> __device__ __forceinline__ V cadd(V a, V b) { return V{a.x + b.x, a.y + b.y}; }
+template <class V> __device__ __forceinline__ V csub(V a, V b) { return V{a.x - b.x, a.y - b.y}; }
+template <class V> __device__ __forceinline__ const V *twid(const DevPlan &P);
+template <> __device__ __forceinline__ const double2 *twid<double2>(const DevPlan &P) { return P.tw; }
+template <> __device__ __forceinline__ const float2 *twid<float2>(const DevPlan &P) { return P.twf; }
 
 // Run all stages on L interleaved lines; returns the buffer holding the result.
-__device__ double2 *block_fft(double2 *b0, double2 *b1, int L, const DevPlan &P, int inv) {
+template <class V>
+__device__ V *block_fft(V *b0, V *b1, int L, const DevPlan &P, int inv) {
     const int N = P.n;
+    const V *tw = twid<V>(P);
     int Ns = 1;
-    double2 *in = b0, *out = b1;
+    V *in = b0, *out = b1;
     for (int st = 0; st < P.nst; st++) {
         const int R = P.rad[st];
         const int NR = N / R;
@@ -45,36 +50,36 @@ __device__ double2 *block_fft(double2 *b0, double2 *b1, int L, const DevPlan &P,
         const int work = NR * L;
         for (int w = threadIdx.x; w < work; w += blockDim.x) {
             const int l = w % L, jb = w / L;
-            double2 v[8];
+            V v[8];
             const int jm = jb % Ns;
 #pragma unroll 4
             for (int r = 0; r < R; r++) {
-                double2 x = in[(jb + r * NR) * L + l];
+                V x = in[(jb + r * NR) * L + l];
                 if (r > 0 && jm > 0) {
-                    double2 t = P.tw[(jm * r * twstep) % N];
+                    V t = tw[(jm * r * twstep) % N];
                     if (inv) t.y = -t.y;
                     x = cmul(x, t);
                 }
                 v[r] = x;
             }
-            double2 y[8];
+            V y[8];
             if (R == 2) {
                 y[0] = cadd(v[0], v[1]);
                 y[1] = csub(v[0], v[1]);
             } else if (R == 4) {
-                double2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
-                double2 s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
+                V s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+                V s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
                 // forward: W4 = -i; inverse: +i
-                double2 jd13 = inv ? make_double2(-d13.y, d13.x) : make_double2(d13.y, -d13.x);
+                V jd13 = inv ? V{-d13.y, d13.x} : V{d13.y, -d13.x};
                 y[0] = cadd(s02, s13);
                 y[2] = csub(s02, s13);
                 y[1] = cadd(d02, jd13);
                 y[3] = csub(d02, jd13);
             } else {
                 for (int m = 0; m < R; m++) {
-                    double2 acc = v[0];
+                    V acc = v[0];
                     for (int r = 1; r < R; r++) {
-                        double2 t = P.tw[((m * r) % R) * NR];
+                        V t = tw[((m * r) % R) * NR];
                         if (inv) t.y = -t.y;
                         acc = cadd(acc, cmul(v[r], t));
                     }
@@ -85,7 +90,7 @@ __device__ double2 *block_fft(double2 *b0, double2 *b1, int L, const DevPlan &P,
             for (int r = 0; r < R; r++) out[(idxD + r * Ns) * L + l] = y[r];
         }
         __syncthreads();
-        double2 *tmp = in; in = out; out = tmp;
+        V *tmp = in; in = out; out = tmp;
         Ns *= R;
     }
     return in;
@@ -97,6 +102,7 @@ DevPlan devplan(const FftPlan &p) {
     d.nst = p.nst;
     for (int s = 0; s < 24; s++) d.rad[s] = p.rad[s];
     d.tw = p.tw;
+    d.twf = p.twf;
     return d;
 }
 
@@ -107,91 +113,103 @@ DevPlan devplan(const FftPlan &p) {
 // conjugate-symmetric spectra and takes x = Re, y = Im.  Half the transforms
 // of the real z lines, each exact up to rounding (on GB300 the FP64 pipe, not
 // memory, bounds these passes).  Line pair l holds i = i0 + 2l and i0 + 2l + 1.
-__global__ void k_fft_z_fwd(KP p, double2 *ccap, DevPlan P, int L, long long sk, long long sj) {
-    extern __shared__ double2 sm[];
+template <class V>
+__global__ void k_fft_z_fwd(KP p, const double *src, V *ccap, DevPlan P, int L, long long sk, long long sj) {
+    using T = decltype(V{}.x);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    V *sm = reinterpret_cast<V *>(smraw);
     const DGrid &g = p.g;
     const int N = P.n;
-    double2 *b0 = sm, *b1 = sm + (size_t)N * L;
+    V *b0 = sm, *b1 = sm + (size_t)N * L;
     const int i0 = 1 + blockIdx.x * 2 * L, j = 1 + blockIdx.y;
     for (int w = threadIdx.x; w < N * 2 * L; w += blockDim.x) {
         const int l2 = w % (2 * L), e = w / (2 * L);       // consecutive threads: consecutive i
         const int i = i0 + l2;
-        const double val = (i <= g.n1m) ? p.f.divgsum[g.ix(i, j, e + 1)] : 0.0;
-        double *slot = reinterpret_cast<double *>(&b0[e * L + (l2 >> 1)]);
+        const T val = (i <= g.n1m) ? T(src[g.ix(i, j, e + 1)]) : T(0.0);
+        T *slot = reinterpret_cast<T *>(&b0[e * L + (l2 >> 1)]);
         slot[l2 & 1] = val;
     }
     __syncthreads();
-    const double2 *res = block_fft(b0, b1, L, P, 0);
+    const V *res = block_fft(b0, b1, L, P, 0);
     const int n3mh = g.n3mh;
     for (int w = threadIdx.x; w < n3mh * 2 * L; w += blockDim.x) {
         const int l2 = w % (2 * L), kk = w / (2 * L);
         const int i = i0 + l2, l = l2 >> 1;
         if (i > g.n1m) continue;
-        const double2 c = res[kk * L + l], cn = res[((N - kk) % N) * L + l];
+        const V c = res[kk * L + l], cn = res[((N - kk) % N) * L + l];
         // A_k = (C_k + conj C_{N-k}) / 2 ; B_k = -i (C_k - conj C_{N-k}) / 2
-        const double2 v = (l2 & 1) ? make_double2(0.5 * (c.y + cn.y), -0.5 * (c.x - cn.x))
-                                   : make_double2(0.5 * (c.x + cn.x), 0.5 * (c.y - cn.y));
+        const V v = (l2 & 1) ? V{T(0.5) * (c.y + cn.y), T(-0.5) * (c.x - cn.x)}
+                             : V{T(0.5) * (c.x + cn.x), T(0.5) * (c.y - cn.y)};
         ccap[(i - 1) + sk * kk + sj * (j - 1)] = v;
     }
 }
 
-__global__ void k_fft_z_inv(KP p, const double2 *ccap, DevPlan P, int L, long long sk, long long sj) {
-    extern __shared__ double2 sm[];
+// ADD: phi += the result (the correction pass of the mixed form), else phi =
+template <class V, bool ADD>
+__global__ void k_fft_z_inv(KP p, const V *ccap, DevPlan P, int L, long long sk, long long sj) {
+    using T = decltype(V{}.x);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    V *sm = reinterpret_cast<V *>(smraw);
     const DGrid &g = p.g;
     const int N = P.n;
-    double2 *b0 = sm, *b1 = sm + (size_t)N * L;
+    V *b0 = sm, *b1 = sm + (size_t)N * L;
     const int i0 = 1 + blockIdx.x * 2 * L, j = 1 + blockIdx.y;
     const int n3mh = g.n3mh;
     // coefficient e of line i (conjugate completion above n3mh, poiss_ftft.f90:143-147);
     // the k = 0 and Nyquist coefficients enter through their real part only
     // (the reference takes Re of the inverse)
-    auto coef = [&](int i, int e) -> double2 {
-        if (i > g.n1m) return make_double2(0.0, 0.0);
+    auto coef = [&](int i, int e) -> V {
+        if (i > g.n1m) return V{T(0.0), T(0.0)};
         if (e < n3mh) {
-            double2 v = ccap[(i - 1) + sk * e + sj * (j - 1)];
-            if (e == 0 || 2 * e == N) v.y = 0.0;
+            V v = ccap[(i - 1) + sk * e + sj * (j - 1)];
+            if (e == 0 || 2 * e == N) v.y = T(0.0);
             return v;
         }
-        const double2 s = ccap[(i - 1) + sk * (N - e) + sj * (j - 1)];
-        return make_double2(s.x, -s.y);
+        const V s = ccap[(i - 1) + sk * (N - e) + sj * (j - 1)];
+        return V{s.x, -s.y};
     };
     for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
         const int l = w % L, e = w / L;
-        const double2 x = coef(i0 + 2 * l, e), y = coef(i0 + 2 * l + 1, e);
-        b0[e * L + l] = make_double2(x.x - y.y, x.y + y.x);     // Z = X + i Y
+        const V x = coef(i0 + 2 * l, e), y = coef(i0 + 2 * l + 1, e);
+        b0[e * L + l] = V{x.x - y.y, x.y + y.x};     // Z = X + i Y
     }
     __syncthreads();
-    const double2 *res = block_fft(b0, b1, L, P, 1);
+    const V *res = block_fft(b0, b1, L, P, 1);
     const double dn = 1.0 / (double)N;
     for (int w = threadIdx.x; w < N * 2 * L; w += blockDim.x) {
         const int l2 = w % (2 * L), e = w / (2 * L);
         const int i = i0 + l2;
         if (i <= g.n1m) {
-            const double2 r = res[e * L + (l2 >> 1)];
-            p.f.phi[g.ix(i, j, e + 1)] = ((l2 & 1) ? r.y : r.x) * dn;
+            const V r = res[e * L + (l2 >> 1)];
+            const double v = (double)((l2 & 1) ? r.y : r.x) * dn;
+            double &ph = p.f.phi[g.ix(i, j, e + 1)];
+            ph = ADD ? ph + v : v;
         }
     }
 }
 
 // ---- x transforms of the (k,j) lines of ccap, in place -------------------
-__global__ void k_fft_x(double2 *ccap, int nlines, DevPlan P, int L, int inv) {
-    extern __shared__ double2 sm[];
+template <class V>
+__global__ void k_fft_x(V *ccap, int nlines, DevPlan P, int L, int inv) {
+    using T = decltype(V{}.x);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    V *sm = reinterpret_cast<V *>(smraw);
     const int N = P.n;
-    double2 *b0 = sm, *b1 = sm + (size_t)N * L;
+    V *b0 = sm, *b1 = sm + (size_t)N * L;
     int line0 = blockIdx.x * L;
     for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
         int e = w % N, l = w / N;           // coalesced global read along the line
         int line = line0 + l;
-        b0[e * L + l] = (line < nlines) ? ccap[(size_t)line * N + e] : make_double2(0.0, 0.0);
+        b0[e * L + l] = (line < nlines) ? ccap[(size_t)line * N + e] : V{T(0.0), T(0.0)};
     }
     __syncthreads();
-    double2 *res = block_fft(b0, b1, L, P, inv);
-    const double dn = 1.0 / (double)N;
+    V *res = block_fft(b0, b1, L, P, inv);
+    const T dn = T(1.0 / (double)N);
     for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
         int e = w % N, l = w / N;
         int line = line0 + l;
         if (line < nlines) {
-            double2 v = res[e * L + l];
+            V v = res[e * L + l];
             if (inv) { v.x *= dn; v.y *= dn; }
             ccap[(size_t)line * N + e] = v;
         }
@@ -215,7 +233,7 @@ __global__ void k_fft_xr_fwd(KP p, double2 *ccap, DevPlan P, int L) {
         b0[e * L + l] = make_double2(val, 0.0);
     }
     __syncthreads();
-    const double2 *res = block_fft(b0, b1, L, P, 0);
+    const double2 *res = block_fft<double2>(b0, b1, L, P, 0);
     const size_t plane = (size_t)g.n3m * g.n2m;
     for (int w = threadIdx.x; w < g.n1mh * L; w += blockDim.x) {
         const int l = w % L, iv = w / L;
@@ -255,7 +273,7 @@ __global__ void k_fft_xr_inv(KP p, const double2 *ccap, DevPlan P, int L, int pi
         b0[e * Ls + l] = val;
     }
     __syncthreads();
-    const double2 *res = block_fft(b0, b1, Ls, P, 1);
+    const double2 *res = block_fft<double2>(b0, b1, Ls, P, 1);
     const double dn = 1.0 / (double)N;
     double phiref = 0.0;
     if (pin) {
@@ -393,7 +411,10 @@ __global__ void k_ytri_lu(KP p, const double *ak1, const double *ak3, double *yb
 // pinned as poiss_ftft.f90:93-112.  The coefficients are real, so the real
 // and imaginary parts are independent recurrences: one thread each (twice
 // the lines in flight); operands are loaded 8 rows ahead.
-__global__ void __launch_bounds__(64) k_ytri(KP p, double2 *ccap, const double *ybet, const double *ygam,
+// S: the spectrum's storage (double, or float in the mixed form's correction
+// solve, whose arithmetic here stays FP64)
+template <class S>
+__global__ void __launch_bounds__(64) k_ytri(KP p, S *ccap, const double *ybet, const double *ygam,
                                              const double *yam, const double *pinref) {
     const DGrid &g = p.g;
     const int n1m = g.n1m, n2m = g.n2m, n3mh = g.n3mh;
@@ -403,10 +424,10 @@ __global__ void __launch_bounds__(64) k_ytri(KP p, double2 *ccap, const double *
     for (long long tt = (long long)blockIdx.x * blockDim.x + threadIdx.x; tt < 2 * nl; tt += (long long)gridDim.x * blockDim.x) {
         const long long t = tt >> 1;
         const int part = (int)(tt & 1);
-        double *r = reinterpret_cast<double *>(ccap + t) + part;     // element j at r[2 * (j-1) * sj]
+        S *r = ccap + 2 * t + part;                                   // element j at r[2 * (j-1) * sj]
         const long long s2 = 2 * sj;
         const bool pin = (t == 0);
-        const double crhsref = pin ? r[(n2m - 1) * s2] : 0.0;
+        const double crhsref = pin ? (double)r[(n2m - 1) * s2] : 0.0;
         // forward: the next chunk's operands are loaded while one is computed
         // (two register buffers, alternated by unrolling the chunk loop by two)
         double x = 0.0;
@@ -415,7 +436,7 @@ __global__ void __launch_bounds__(64) k_ytri(KP p, double2 *ccap, const double *
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int j = j0 + u;
-                if (j <= n2m) { rv[u] = r[(j - 1) * s2]; bv[u] = ybet[t + (j - 1) * sj]; av[u] = yam[j]; }
+                if (j <= n2m) { rv[u] = (double)r[(j - 1) * s2]; bv[u] = ybet[t + (j - 1) * sj]; av[u] = yam[j]; }
             }
         };
         auto solve_f = [&](const double (&rv)[U], const double (&bv)[U], const double (&av)[U], int j0) {
@@ -426,7 +447,7 @@ __global__ void __launch_bounds__(64) k_ytri(KP p, double2 *ccap, const double *
                 double rj = rv[u], am = av[u];
                 if (pin && j == n2m) { am = 0.0; rj = 0.0; }
                 x = (j == 1) ? rj * bv[u] : (rj - am * x) * bv[u];
-                r[(j - 1) * s2] = x;
+                r[(j - 1) * s2] = (S)x;
             }
         };
         load_f(rA, bA, aA, 1);
@@ -445,7 +466,7 @@ __global__ void __launch_bounds__(64) k_ytri(KP p, double2 *ccap, const double *
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int j = j0 - u;
-                if (j >= 1) { xv[u] = r[(j - 1) * s2]; gv[u] = ygam[t + j * sj]; }
+                if (j >= 1) { xv[u] = (double)r[(j - 1) * s2]; gv[u] = ygam[t + j * sj]; }
             }
         };
         auto solve_b = [&](const double (&xv)[U], const double (&gv)[U], int j0) {
@@ -454,7 +475,7 @@ __global__ void __launch_bounds__(64) k_ytri(KP p, double2 *ccap, const double *
                 const int j = j0 - u;
                 if (j < 1) break;
                 const double xj = xv[u] - gv[u] * xn;
-                r[(j - 1) * s2] = xj;
+                r[(j - 1) * s2] = (S)xj;
                 xn = xj;
             }
         };
@@ -469,11 +490,38 @@ __global__ void __launch_bounds__(64) k_ytri(KP p, double2 *ccap, const double *
         if (pin) {
             // phref = (-ajmref*crhs(n2m-1,1) + crhsref)/ajcref; shift; crhs(n2m,1) = 0
             const double ajcref = pinref[0], ajmref = pinref[1];
-            const double cm = n2m >= 2 ? r[(n2m - 2) * s2] : 0.0;
+            const double cm = n2m >= 2 ? (double)r[(n2m - 2) * s2] : 0.0;
             const double ph = (-ajmref * cm + crhsref) / ajcref;
-            for (int j = 1; j <= n2m; j++) r[(j - 1) * s2] = r[(j - 1) * s2] - ph;
-            r[(n2m - 1) * s2] = 0.0;
+            for (int j = 1; j <= n2m; j++) r[(j - 1) * s2] = (S)((double)r[(j - 1) * s2] - ph);
+            r[(n2m - 1) * s2] = (S)0.0;
         }
+    }
+}
+
+// The mixed form's FP64 defect of the poiss_ftft system, r = divgsum - L phi,
+// for the operator the transforms diagonalise (poiss_ftft.f90:79-88,
+// :164-204): periodic second differences in x and z on the uniform spacings
+// (-ak1, -ak3 in wavenumber space) and the y rows ajm, ajp with the walls'
+// Neumann closure.  One FP32 solve of L e = r then corrects phi.
+// yc[3 j .. 3 j + 2] = (ajm, ajp, 2 sdx^2 + 2 sdz^2 + ajm + ajp) of row j, so a
+// cell costs a handful of FP64 operations (the FP64 pipe bounds this pass)
+__global__ void __launch_bounds__(kThreads) k_pois_resid(KP p, Box b, const double *yc, double *res) {
+    const DGrid &g = p.g;
+    const double sdx = g.f2fxi[1], sdz = g.f2fzi[1];
+    const double sx2 = sdx * sdx, sz2 = sdz * sdz;
+    const long long n = b.count();
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        b.at(t, i, j, k);
+        const long long q = g.ix(i, j, k);
+        const double *phi = p.f.phi;
+        const int ip = i < g.n1m ? i + 1 : 1, im = i > 1 ? i - 1 : g.n1m;
+        const int kp = k < g.n3m ? k + 1 : 1, km = k > 1 ? k - 1 : g.n3m;
+        const double am = yc[3 * j], ap = yc[3 * j + 1], dg = yc[3 * j + 2];
+        const double ys = (j > 1 ? am * phi[q - g.sx] : 0.0) + (j < g.n2m ? ap * phi[q + g.sx] : 0.0);
+        const double lap = sx2 * (phi[g.ix(ip, j, k)] + phi[g.ix(im, j, k)]) + sz2 * (phi[g.ix(i, j, kp)] + phi[g.ix(i, j, km)])
+                         + ys - dg * phi[q];
+        res[q] = p.f.divgsum[q] - lap;
     }
 }
 
@@ -494,19 +542,24 @@ int make_plan(FftPlan &p, int n) {
         m /= r;
     }
     double2 *h = (double2 *)malloc(sizeof(double2) * (size_t)(n > 0 ? n : 1));
+    float2 *hf = (float2 *)malloc(sizeof(float2) * (size_t)(n > 0 ? n : 1));
     for (int e = 0; e < n; e++) {
         long double ang = -2.0L * 3.14159265358979323846264338327950288L * (long double)e / (long double)n;
         h[e] = make_double2((double)cosl(ang), (double)sinl(ang));
+        hf[e] = make_float2((float)cosl(ang), (float)sinl(ang));
     }
-    if (cudaMalloc(&p.tw, sizeof(double2) * (size_t)n) != cudaSuccess) { free(h); return LESGPU_ERR_OOM; }
+    if (cudaMalloc(&p.tw, sizeof(double2) * (size_t)n) != cudaSuccess ||
+        cudaMalloc(&p.twf, sizeof(float2) * (size_t)n) != cudaSuccess) { free(h); free(hf); return LESGPU_ERR_OOM; }
     cudaMemcpy(p.tw, h, sizeof(double2) * (size_t)n, cudaMemcpyHostToDevice);
+    cudaMemcpy(p.twf, hf, sizeof(float2) * (size_t)n, cudaMemcpyHostToDevice);
     free(h);
+    free(hf);
     return 0;
 }
 
-static int lines_per_block(int n) {
+static int lines_per_block(int n, size_t elem = sizeof(double2)) {
     int L = 32;
-    while (L > 1 && (size_t)2 * n * L * sizeof(double2) > 200 * 1024) L >>= 1;
+    while (L > 1 && (size_t)2 * n * L * elem > 200 * 1024) L >>= 1;
     return L;
 }
 
@@ -520,6 +573,14 @@ int fft_lx(const lesgpu_case *c) { return c->pois.Lx > 0 ? c->pois.Lx : lines_pe
 // on the number of lines, so it is timed per shape (forward transforms on the
 // case's own arrays, whose contents are scratch outside a solve) and cached.
 static std::map<std::array<int, 4>, int> g_fft_l;
+
+// LESGPU_FFT_MIXED: 1 = the mixed form always solves poiss_ftft with FP32
+// transforms under the FP64 defect correction, 0 = always FP64; unset = timed
+static int fft_mixed_forced() {
+    const char *e = getenv("LESGPU_FFT_MIXED");
+    if (!e || (e[0] != '0' && e[0] != '1')) return -1;
+    return e[0] - '0';
+}
 static std::mutex g_fft_mu;
 
 static int fft_time_pick(lesgpu_case *c, std::array<int, 4> key, int n, int dflt,
@@ -571,14 +632,34 @@ int fft_autotune(lesgpu_case *c) {
     const long long sj = ftft ? (long long)g.n1m * g.n3mh : g.n1m;
     P.Lz = fft_time_pick(c, {0, g.n1m, g.n2m, g.n3m}, g.n3m, lines_per_block(g.n3m), [&](int L) {
         const dim3 gz((g.n1m + 2 * L - 1) / (2 * L), g.n2m);   // 2L real lines per block
-        k_fft_z_fwd<<<gz, kThreads, (size_t)2 * g.n3m * L * sizeof(double2), c->stream>>>(c->kp, P.ccap, pz, L, sk, sj);
+        k_fft_z_fwd<double2><<<gz, kThreads, (size_t)2 * g.n3m * L * sizeof(double2), c->stream>>>(c->kp, c->kp.f.divgsum, P.ccap, pz, L, sk, sj);
     });
     if (ftft) {
         const DevPlan px = devplan(P.fx);
         const int nxl = g.n3mh * g.n2m;
         P.Lx = fft_time_pick(c, {1, g.n1m, g.n2m, g.n3m}, g.n1m, lines_per_block(g.n1m), [&](int L) {
-            k_fft_x<<<(nxl + L - 1) / L, kThreads, (size_t)2 * g.n1m * L * sizeof(double2), c->stream>>>(P.ccap, nxl, px, L, 0);
+            k_fft_x<double2><<<(nxl + L - 1) / L, kThreads, (size_t)2 * g.n1m * L * sizeof(double2), c->stream>>>(P.ccap, nxl, px, L, 0);
         });
+        // the mixed form: one FP64 solve, or two FP32 solves under an FP64
+        // defect correction -- whichever is faster for the shape
+        if (c->cfg.precision == LESGPU_PREC_MIXED && fft_mixed_forced() < 0) {
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            float ms[2] = {0.0f, 0.0f};
+            for (int v = 0; v < 2; v++) {
+                P.mixed_fft = v;
+                launch_poisson(c, 1);                 // warm-up
+                cudaEventRecord(e0, c->stream);
+                for (int r = 0; r < 3; r++) launch_poisson(c, 1);
+                cudaEventRecord(e1, c->stream);
+                if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms[v], e0, e1) != cudaSuccess)
+                    ms[v] = 3.0e38f;
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            P.mixed_fft = ms[1] < ms[0] ? 1 : 0;
+        }
     }
     return cudaStreamSynchronize(c->stream) == cudaSuccess ? 0 : LESGPU_ERR_CUDA;
 }
@@ -591,6 +672,14 @@ int poisson_init(lesgpu_case *c) {
     if (c->cfg.poisson == LESGPU_POISSON_MGRD) return mgrd_init(c);
     if (c->cfg.poisson != LESGPU_POISSON_FTFT) return LESGPU_ERR_UNSUPPORTED;
     if (c->cfg.xprdic != 1 || c->cfg.zprdic != 1) return LESGPU_ERR_CONFIG;
+    // mixed form: FP32 transforms under the FP64 defect correction when forced
+    // (LESGPU_FFT_MIXED) or, until the autotuner times both, on grids of 4M
+    // cells and more (the FP64 transforms are FP64-pipe bound there)
+    {
+        const int forced = fft_mixed_forced();
+        const bool mixed = c->cfg.precision == LESGPU_PREC_MIXED;
+        P.mixed_fft = mixed && (forced == 1 || (forced < 0 && (long long)g.n1m * g.n2m * g.n3m >= (4LL << 20)));
+    }
     int rc = make_plan(P.fx, g.n1m);
     if (rc) return rc;
     rc = make_plan(P.fz, g.n3m);
@@ -621,6 +710,19 @@ int poisson_init(lesgpu_case *c) {
         cudaMalloc(&P.yam, sizeof(double) * (g.n2m + 2)) != cudaSuccess ||
         cudaMalloc(&P.pinref, sizeof(double) * 2) != cudaSuccess)
         return LESGPU_ERR_OOM;
+    {   // the residual's y rows (poiss_ftft.f90:81-84) and diagonal
+        const lesgpu_grid *hg = c->h_grid;
+        const double sx2 = hg->f2fxi[1] * hg->f2fxi[1], sz2 = hg->f2fzi[1] * hg->f2fzi[1];
+        std::vector<double> yc(3 * (size_t)(g.n2m + 2), 0.0);
+        for (int j = 1; j <= g.n2m; j++) {
+            const int jp = (int)hg->jpv[j - 1];
+            const double am = hg->f2fyi[j] * hg->c2cyi[j] * (1.0 - (double)hg->fixjl[j - 1]);
+            const double ap = hg->f2fyi[j] * hg->c2cyi[jp] * (1.0 - (double)hg->fixju[j - 1]);
+            yc[3 * j] = am; yc[3 * j + 1] = ap; yc[3 * j + 2] = 2.0 * sx2 + 2.0 * sz2 + am + ap;
+        }
+        if (cudaMalloc(&P.yres, sizeof(double) * yc.size()) != cudaSuccess) return LESGPU_ERR_OOM;
+        cudaMemcpy(P.yres, yc.data(), sizeof(double) * yc.size(), cudaMemcpyHostToDevice);
+    }
     cudaMemset(P.ygam, 0, sizeof(double) * nspec);
     cudaMemset(P.pinref, 0, sizeof(double) * 2);
     {
@@ -630,9 +732,13 @@ int poisson_init(lesgpu_case *c) {
     }
     // the attribute is per function and shared by every case: set it to the
     // largest size lines_per_block() can ask for
-    if (cudaFuncSetAttribute(k_fft_z_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess ||
-        cudaFuncSetAttribute(k_fft_z_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess ||
-        cudaFuncSetAttribute(k_fft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_fft_z_fwd<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess ||
+        cudaFuncSetAttribute(k_fft_z_inv<double2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess ||
+        cudaFuncSetAttribute(k_fft_x<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess ||
+        cudaFuncSetAttribute(k_fft_z_fwd<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess ||
+        cudaFuncSetAttribute(k_fft_z_inv<float2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess ||
+        cudaFuncSetAttribute(k_fft_z_inv<float2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess ||
+        cudaFuncSetAttribute(k_fft_x<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess)
         return LESGPU_ERR_CUDA;
     return 0;
 }
@@ -642,31 +748,81 @@ void poisson_free(lesgpu_case *c) {
     mg2d_free(c);
     mgrd_free(c);
     cudaFree(P.ak1); cudaFree(P.ak3); cudaFree(P.ccap);
-    cudaFree(P.ybet); cudaFree(P.ygam); cudaFree(P.yam); cudaFree(P.pinref);
+    cudaFree(P.ybet); cudaFree(P.ygam); cudaFree(P.yam); cudaFree(P.pinref); cudaFree(P.yres);
+    P.yres = nullptr;
     P.ybet = P.ygam = P.yam = P.pinref = nullptr;
-    cudaFree(P.fx.tw); cudaFree(P.fz.tw);
-    P.ak1 = P.ak3 = nullptr; P.ccap = nullptr; P.fx.tw = P.fz.tw = nullptr;
+    cudaFree(P.fx.tw); cudaFree(P.fz.tw); cudaFree(P.fx.twf); cudaFree(P.fz.twf);
+    P.ak1 = P.ak3 = nullptr; P.ccap = nullptr; P.fx.tw = P.fz.tw = nullptr; P.fx.twf = P.fz.twf = nullptr;
+}
+
+// One poiss_ftft solve of L x = src on the transforms of type V (FP64, or FP32
+// with FP64 y-Thomas arithmetic); ADD: phi += x, else phi = x.
+template <class V, bool ADD>
+static void ftft_solve(lesgpu_case *c, const double *src) {
+    const DGrid &g = c->kp.g;
+    DPois &P = c->pois;
+    const DevPlan px = devplan(P.fx), pz = devplan(P.fz);
+    // the FP64 transforms' lines per block (the FP32 blocks then take half the
+    // shared memory, so more of them are resident)
+    const int Lz = fft_lz(c), Lx = fft_lx(c);
+    const size_t smz = (size_t)2 * g.n3m * Lz * sizeof(V), smx = (size_t)2 * g.n1m * Lx * sizeof(V);
+    const dim3 gz((g.n1m + 2 * Lz - 1) / (2 * Lz), g.n2m);   // 2 Lz real lines per block
+    const int nxl = g.n3mh * g.n2m;
+    const long long sk = g.n1m, sj = (long long)g.n1m * g.n3mh;
+    V *spec = reinterpret_cast<V *>(P.ccap);
+    using T = decltype(V{}.x);
+    k_fft_z_fwd<V><<<gz, kThreads, smz, c->stream>>>(c->kp, src, spec, pz, Lz, sk, sj);
+    k_fft_x<V><<<(nxl + Lx - 1) / Lx, kThreads, smx, c->stream>>>(spec, nxl, px, Lx, 0);
+    const long long nl = (long long)g.n1m * g.n3mh;
+    k_ytri<T><<<blocks_for(2 * nl, 64), 64, 0, c->stream>>>(c->kp, reinterpret_cast<T *>(spec), P.ybet, P.ygam, P.yam, P.pinref);
+    k_fft_x<V><<<(nxl + Lx - 1) / Lx, kThreads, smx, c->stream>>>(spec, nxl, px, Lx, 1);
+    k_fft_z_inv<V, ADD><<<gz, kThreads, smz, c->stream>>>(c->kp, spec, pz, Lz, sk, sj);
 }
 
 void launch_poisson(lesgpu_case *c, int msub) {
-    const DGrid &g = c->kp.g;
     DPois &P = c->pois;
     if (c->cfg.poisson == LESGPU_POISSON_Z_FT || c->cfg.poisson == LESGPU_POISSON_X_FT) { launch_mg2d(c, msub); return; }
     if (c->cfg.poisson == LESGPU_POISSON_MGRD) { launch_mgrd(c, msub); return; }
-    DevPlan px = devplan(P.fx), pz = devplan(P.fz);
-    const int Lz = fft_lz(c), Lx = fft_lx(c);
-    size_t smz = (size_t)2 * g.n3m * Lz * sizeof(double2), smx = (size_t)2 * g.n1m * Lx * sizeof(double2);
-    dim3 gz((g.n1m + 2 * Lz - 1) / (2 * Lz), g.n2m);   // 2 Lz real lines per block
-    int nxl = g.n3mh * g.n2m;
     inst_begin(c, LESGPU_K_POISSON);
-    const long long sk = g.n1m, sj = (long long)g.n1m * g.n3mh;
-    k_fft_z_fwd<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
-    k_fft_x<<<(nxl + Lx - 1) / Lx, kThreads, smx, c->stream>>>(P.ccap, nxl, px, Lx, 0);
-    long long nl = (long long)g.n1m * g.n3mh;
-    k_ytri<<<blocks_for(2 * nl, 64), 64, 0, c->stream>>>(c->kp, P.ccap, P.ybet, P.ygam, P.yam, P.pinref);
-    k_fft_x<<<(nxl + Lx - 1) / Lx, kThreads, smx, c->stream>>>(P.ccap, nxl, px, Lx, 1);
-    k_fft_z_inv<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
+    if (P.mixed_fft) {
+        // FP32 transforms under an FP64 defect correction: phi = S32 divgsum,
+        // r = divgsum - L phi in FP64, phi += S32 r.  Each FP32 solve is within
+        // ~1e-6 of the FP64 one in relative terms, so the correction leaves a
+        // relative error of order 1e-12 (the constant of phi, which L does not
+        // see, keeps the first solve's FP32 rounding).
+        double *res = c->kp.f.scr[0];
+        ftft_solve<float2, false>(c, c->kp.f.divgsum);
+        const DGrid &g = c->kp.g;
+        Box b{1, 1, 1, g.n1m, g.n2m, g.n3m};
+        k_pois_resid<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, P.yres, res);
+        ftft_solve<float2, true>(c, res);
+    } else {
+        ftft_solve<double2, false>(c, c->kp.f.divgsum);
+    }
     inst_end(c, LESGPU_K_POISSON);
+}
+
+// FP64 launches for the other translation units
+void fft_z_fwd64(dim3 grid, size_t smem, cudaStream_t st, KP p, const double *src, double2 *ccap, DevPlan P, int L,
+                 long long sk, long long sj) {
+    k_fft_z_fwd<double2><<<grid, kThreads, smem, st>>>(p, src, ccap, P, L, sk, sj);
+}
+void fft_z_inv64(dim3 grid, size_t smem, cudaStream_t st, KP p, const double2 *ccap, DevPlan P, int L, long long sk,
+                 long long sj) {
+    k_fft_z_inv<double2, false><<<grid, kThreads, smem, st>>>(p, ccap, P, L, sk, sj);
+}
+void fft_x64(int nblocks, size_t smem, cudaStream_t st, double2 *ccap, int nlines, DevPlan P, int L, int inv) {
+    k_fft_x<double2><<<nblocks, kThreads, smem, st>>>(ccap, nlines, P, L, inv);
+}
+void ytri64(int nblocks, cudaStream_t st, KP p, double2 *ccap, const double *ybet, const double *ygam,
+            const double *yam, const double *pinref) {
+    k_ytri<double><<<nblocks, 64, 0, st>>>(p, reinterpret_cast<double *>(ccap), ybet, ygam, yam, pinref);
+}
+int fft_smem64(int bytes) {
+    return (cudaFuncSetAttribute(k_fft_z_fwd<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess &&
+            cudaFuncSetAttribute(k_fft_z_inv<double2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess &&
+            cudaFuncSetAttribute(k_fft_x<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess)
+               ? 0 : LESGPU_ERR_CUDA;
 }
 
 }  // namespace lg

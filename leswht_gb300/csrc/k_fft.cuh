@@ -9,6 +9,7 @@ struct DevPlan {
     int n, nst;
     int rad[24];
     const double2 *tw;
+    const float2 *twf;
 };
 
 // dynamic shared memory a transform block may take (below the per-block
@@ -16,9 +17,15 @@ struct DevPlan {
 constexpr int kFftSmemMax = 200 * 1024;
 
 // z transforms; the spectrum element (i, k, j) sits at (i-1) + sk*(k-1) + sj*(j-1)
-__global__ void k_fft_z_fwd(KP p, double2 *ccap, DevPlan P, int L, long long sk, long long sj);
-__global__ void k_fft_z_inv(KP p, const double2 *ccap, DevPlan P, int L, long long sk, long long sj);
-__global__ void k_fft_x(double2 *ccap, int nlines, DevPlan P, int L, int inv);
+// FP64 launches of the transforms (kernel templates of k_fft.cu, which other
+// translation units cannot launch directly): src is the real field transformed
+void fft_z_fwd64(dim3 grid, size_t smem, cudaStream_t st, KP p, const double *src, double2 *ccap, DevPlan P, int L,
+                 long long sk, long long sj);
+void fft_z_inv64(dim3 grid, size_t smem, cudaStream_t st, KP p, const double2 *ccap, DevPlan P, int L, long long sk,
+                 long long sj);
+void fft_x64(int nblocks, size_t smem, cudaStream_t st, double2 *ccap, int nlines, DevPlan P, int L, int inv);
+// opt the FP64 transform kernels into `bytes` of dynamic shared memory
+int fft_smem64(int bytes);
 // poiss_x_ft: real x lines <-> modes 1..n1mh, one z-y plane per mode
 __global__ void k_fft_xr_fwd(KP p, double2 *ccap, DevPlan P, int L);
 __global__ void k_fft_xr_inv(KP p, const double2 *ccap, DevPlan P, int L, int pin);
@@ -26,8 +33,8 @@ int fft_xr_inv_lines(int n, int L, int pin);
 __global__ void k_ytri_elim(KP p, double2 *ccap, const double *ak1, const double *ak3, double *gam);
 __global__ void k_ytri_lu(KP p, const double *ak1, const double *ak3, double *ybet, double *ygam, double *yam,
                           double *pinref);
-__global__ void k_ytri(KP p, double2 *ccap, const double *ybet, const double *ygam, const double *yam,
-                       const double *pinref);
+void ytri64(int nblocks, cudaStream_t st, KP p, double2 *ccap, const double *ybet, const double *ygam,
+            const double *yam, const double *pinref);
 int fft_lines_per_block(int n);
 int fft_lz(const lesgpu_case *c);
 int fft_lx(const lesgpu_case *c);

@@ -870,9 +870,7 @@ int mg2d_init(lesgpu_case *c) {
             cudaFuncSetAttribute(k_fft_xr_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess)
             return LESGPU_ERR_CUDA;
     } else {
-        if (cudaFuncSetAttribute(k_fft_z_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess ||
-            cudaFuncSetAttribute(k_fft_z_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess)
-            return LESGPU_ERR_CUDA;
+        if (fft_smem64(kFftSmemMax)) return LESGPU_ERR_CUDA;
     }
     // Cluster size: the mode solves are FP64-throughput bound (a GB300 SM
     // retires few FP64 FMAs per clock), so each mode gets as many SMs as the
@@ -988,9 +986,9 @@ void launch_mg2d(lesgpu_case *c, int msub) {
         const size_t smz = (size_t)2 * (g.n3m > 1 ? g.n3m : 1) * Lz * sizeof(double2);
         const dim3 gz((g.n1m + 2 * Lz - 1) / (2 * Lz), g.n2m);   // 2 Lz real lines per block
         const long long sk = (long long)g.n1m * g.n2m, sj = g.n1m;
-        k_fft_z_fwd<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
+        fft_z_fwd64(gz, smz, c->stream, c->kp, c->kp.f.divgsum, P.ccap, pz, Lz, sk, sj);
         launch_modes(c, mg_args(c, slot, 0), T->cs);
-        k_fft_z_inv<<<gz, kThreads, smz, c->stream>>>(c->kp, P.ccap, pz, Lz, sk, sj);
+        fft_z_inv64(gz, smz, c->stream, c->kp, P.ccap, pz, Lz, sk, sj);
     }
     inst_end(c, LESGPU_K_POISSON);
 }

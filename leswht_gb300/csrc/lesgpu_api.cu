@@ -736,11 +736,14 @@ extern "C" int lesgpu_use_graph(lesgpu_case *c, int on) {
 
 extern "C" int lesgpu_tuning(lesgpu_case *c, int64_t *out, int64_t maxn, int64_t *nclasses) {
     if (!c || !nclasses || maxn < 0 || (maxn > 0 && !out)) return LESGPU_ERR_ARG;
-    int buf[4 * 67];
+    int buf[4 * 72];
     int n = c->autotune ? adi_tuned(c, buf, 4 * 64) : 0;
     if (c->autotune && c->pois.Lz > 0) { buf[4 * n] = 3; buf[4 * n + 1] = 2; buf[4 * n + 2] = 0; buf[4 * n + 3] = c->pois.Lz; n++; }
     if (c->autotune && c->pois.Lx > 0) { buf[4 * n] = 3; buf[4 * n + 1] = 0; buf[4 * n + 2] = 0; buf[4 * n + 3] = c->pois.Lx; n++; }
     if (c->autotune && mg2d_cluster(c) > 0) { buf[4 * n] = 4; buf[4 * n + 1] = 0; buf[4 * n + 2] = 0; buf[4 * n + 3] = mg2d_cluster(c); n++; }
+    if (c->cfg.poisson == LESGPU_POISSON_FTFT && c->cfg.precision == LESGPU_PREC_MIXED) {
+        buf[4 * n] = 5; buf[4 * n + 1] = 0; buf[4 * n + 2] = 0; buf[4 * n + 3] = c->pois.mixed_fft; n++;
+    }
     *nclasses = n;
     for (int q = 0; q < n && q < maxn; q++)
         for (int e = 0; e < 4; e++) out[4 * q + e] = buf[4 * q + e];

@@ -118,6 +118,7 @@ struct FftPlan {
     int nst;
     int rad[24];
     double2 *tw;              // exp(-2 pi i e / n), e = 0..n-1 (device)
+    float2 *twf;              // the same rounded to FP32
 };
 
 struct MgTables;              // poiss_z_ft multigrid tables (k_mg.cu)
@@ -133,6 +134,8 @@ struct DPois {
     MgrdTables *mgrd;         // poiss_mgrd (BiCGSTAB + MG3D)
     double *ybet, *ygam, *yam, *pinref;   // poiss_ftft: LU of the y systems (k_ytri_lu)
     int Lz, Lx;               // FFT lines per block (0 = the shared-memory rule; set by the autotuner)
+    int mixed_fft;            // poiss_ftft in the mixed form: FP32 transforms, FP64 defect correction
+    double *yres;             // its FP64 residual's y rows and diagonal, 3 per j
 };
 
 // The arrays a kernel of arithmetic type T reads in its stencils.  Mir<double>

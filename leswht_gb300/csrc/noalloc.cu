@@ -54,10 +54,7 @@ int setup_device(int dev, unsigned char **base) {
         void *p = nullptr;
         if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return LESGPU_ERR_CUDA;
         const int kMaxSmem = 200 * 1024;
-        if (cudaFuncSetAttribute(lg::k_fft_z_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem) != cudaSuccess ||
-            cudaFuncSetAttribute(lg::k_fft_z_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem) != cudaSuccess ||
-            cudaFuncSetAttribute(lg::k_fft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem) != cudaSuccess)
-            return LESGPU_ERR_CUDA;
+        if (lg::fft_smem64(kMaxSmem)) return LESGPU_ERR_CUDA;
         g_base[dev] = p;
     }
     *base = (unsigned char *)g_base[dev];
@@ -175,6 +172,8 @@ extern "C" int lesgpu_poisson_ftft_noalloc(const lesgpu_grid *g, const double *d
     p.f.phi = d_phi;
     px.tw = (const double2 *)(base + o_twx);
     pz.tw = (const double2 *)(base + o_twz);
+    px.twf = nullptr;   // FP64 transforms only
+    pz.twf = nullptr;
     double2 *ccap = (double2 *)(base + o_ccap);
     double *gam = (double *)(base + o_gam);
     const double *dak1 = (const double *)(base + o_ak1), *dak3 = (const double *)(base + o_ak3);
@@ -185,11 +184,11 @@ extern "C" int lesgpu_poisson_ftft_noalloc(const lesgpu_grid *g, const double *d
     dim3 gz((n1m + 2 * Lz - 1) / (2 * Lz), n2m);   // 2 Lz real lines per block
     int nxl = n3mh * n2m;
     const long long sk = n1m, sj = (long long)n1m * n3mh;
-    lg::k_fft_z_fwd<<<gz, lg::kThreads, smz, st>>>(p, ccap, pz, Lz, sk, sj);
-    lg::k_fft_x<<<(nxl + Lx - 1) / Lx, lg::kThreads, smx, st>>>(ccap, nxl, px, Lx, 0);
+    lg::fft_z_fwd64(gz, smz, st, p, p.f.divgsum, ccap, pz, Lz, sk, sj);
+    lg::fft_x64((nxl + Lx - 1) / Lx, smx, st, ccap, nxl, px, Lx, 0);
     long long nl = (long long)n1m * n3mh;
     lg::k_ytri_elim<<<lg::blocks_for(nl, 128), 128, 0, st>>>(p, ccap, dak1, dak3, gam);
-    lg::k_fft_x<<<(nxl + Lx - 1) / Lx, lg::kThreads, smx, st>>>(ccap, nxl, px, Lx, 1);
-    lg::k_fft_z_inv<<<gz, lg::kThreads, smz, st>>>(p, ccap, pz, Lz, sk, sj);
+    lg::fft_x64((nxl + Lx - 1) / Lx, smx, st, ccap, nxl, px, Lx, 1);
+    lg::fft_z_inv64(gz, smz, st, p, ccap, pz, Lz, sk, sj);
     return cudaGetLastError() == cudaSuccess ? 0 : LESGPU_ERR_CUDA;
 }

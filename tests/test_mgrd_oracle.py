@@ -17,7 +17,7 @@ def phi_after_divergence(lib, case):
 
 
 @pytest.mark.parametrize("build, other, tol", [(lambda: cases.channel(16, 16, 8), abi.POISSON_FTFT, 1e-13),
-                                               (lambda: cases.cylinder(32, 24, 4, nlev=2), abi.POISSON_Z_FT, 1e-11)])
+                                               (lambda: cases.cylinder(32, 24, 4, nlev=2), abi.POISSON_Z_FT, 1e-10)])
 def test_same_solution_as_the_other_solvers(oracle_lib, build, other, tol):
     ref = cases.with_poisson(build(), other)
     ref.settings.update(resid1=tol, mgitr=2000)

@@ -90,3 +90,31 @@ def test_fp32_multigrid_meets_the_fp64_test(build):
     assert 1 <= ia < 2000 and 1 <= ib < 2000 and abs(ia - ib) <= max(2, ia // 5)
     assert rel(b.get(abi.F_PHI), a.get(abi.F_PHI)) <= 1e-8
 
+
+
+def test_fp32_fft_with_fp64_correction_matches_fp64_transforms(monkeypatch):
+    """poiss_ftft in the mixed form: FP32 transforms under the FP64 defect
+    correction give the FP64 transforms' phi to 1e-10 relative, up to the
+    constant (which the 7-point operator does not see)."""
+    c = cases.channel(64, 32, 32, precision=abi.PREC_MIXED)
+    solvers = []
+    for forced in ("0", "1"):
+        monkeypatch.setenv("LESGPU_FFT_MIXED", forced)
+        s = leswht_gb300.gpu_solver(c)
+        assert [w for d, nc, f32, w in leswht_gb300.tuning(s.lib, s.h) if d == 5] == [int(forced)]
+        solvers.append(s)
+    a, b = solvers
+    for s in (a, b):
+        s.phase(abi.PH_STEPINIT)
+        s.phase(abi.PH_SUBSTEPINIT, 1)
+    a.phase(abi.PH_SGS, 1)
+    a.phase(abi.PH_RHSNLHS, 1)
+    a.phase(abi.PH_DIVGS, 1)
+    b.set(abi.F_DIVGSUM, a.get(abi.F_DIVGSUM))
+    for s in (a, b):
+        s.phase(abi.PH_POISSON, 1)
+    g = c.grid
+    sl = np.s_[1:g.n3m + 1, 1:g.n2m + 1, 1:g.n1m + 1]
+    pa, pb = a.get(abi.F_PHI)[sl], b.get(abi.F_PHI)[sl]
+    pa, pb = pa - pa.mean(), pb - pb.mean()
+    assert rel(pb, pa) <= 1e-10
