@@ -14,7 +14,7 @@ namespace lg {
 // load is converted to R, so the whole stencil runs in R; the reference's
 // operation order is kept either way.
 template <class R>
-__global__ void __launch_bounds__(kThreads) k_rhs(KP p, Box b, R gam, R ro) {
+__global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 1) k_rhs(KP p, Box b, R gam, R ro) {
     const Mir<R> &M = mir<R>(p);
     const DGrid &g = p.g;
     const DCfg &c = p.c;
@@ -24,13 +24,17 @@ __global__ void __launch_bounds__(kThreads) k_rhs(KP p, Box b, R gam, R ro) {
     const R ichfac = c.ich != 0 ? R(1.0) : R(0.0);
     const R rei = pickr<R>(c.rei_d, c.rei_f);
     const long long sx = g.sx, sxy = g.sxy;
+    // buoyancy in the grdir equation only (decided once, not per cell)
+    const bool gbx = c.ihtrans == 1 && c.grdir == 1 && c.gterm != 0.0;
+    const bool gby = c.ihtrans == 1 && c.grdir == 2 && c.gterm != 0.0;
+    const bool gbz = c.ihtrans == 1 && c.grdir == 3 && c.gterm != 0.0;
     long long n = b.count();
     for (long long tt = (long long)blockIdx.x * blockDim.x + threadIdx.x; tt < n; tt += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         b.at(tt, i, j, k);
         long long q = g.ix(i, j, k);
-        const R fju = R(g.fixju[j]), fjl = R(g.fixjl[j]), fku = R(g.fixku[k]), fkl = R(g.fixkl[k]);
-        const R fiu = R(g.fixiu[i]), fil = R(g.fixil[i]);
+        const R fju = M.fixju[j], fjl = M.fixjl[j], fku = M.fixku[k], fkl = M.fixkl[k];
+        const R fiu = M.fixiu[i], fil = M.fixil[i];
         const R f2fxm = R(M.f2fx[i - 1]), f2fx0 = R(M.f2fx[i]), f2fxp = R(M.f2fx[i + 1]);
         const R f2fym = R(M.f2fy[j - 1]), f2fy0 = R(M.f2fy[j]), f2fyp = R(M.f2fy[j + 1]);
         const R f2fzm = R(M.f2fz[k - 1]), f2fz0 = R(M.f2fz[k]), f2fzp = R(M.f2fz[k + 1]);
@@ -69,7 +73,7 @@ __global__ void __launch_bounds__(kThreads) k_rhs(KP p, Box b, R gam, R ro) {
                 alx = alx + (R(2.0) * tx + ty + tz);
                 rk3x = rk3x + (a + bb);
             }
-            if (c.ihtrans == 1 && c.grdir == 1 && c.gterm != 0.0) rk3x = rk3x + c.gterm * R(t[q]);
+            if (gbx) rk3x = rk3x + c.gterm * R(t[q]);
             p.f.rhs1[0][q] = dt * (gam * rk3x + ro * R(p.f.rk3o[0][q]) + R(2.0) * alpha * alx
                                    - R(2.0) * alpha * (R(pp[q]) - R(pp[q - 1])) * R(M.c2cxi[i])
                                    - R(2.0) * alpha * pmi0 * ichfac);
@@ -109,7 +113,7 @@ __global__ void __launch_bounds__(kThreads) k_rhs(KP p, Box b, R gam, R ro) {
                 aly = aly + (tx + R(2.0) * ty + tz);
                 rk3y = rk3y + (a + bb);
             }
-            if (c.ihtrans == 1 && c.grdir == 2 && c.gterm != 0.0) rk3y = rk3y + c.gterm * R(t[q]);
+            if (gby) rk3y = rk3y + c.gterm * R(t[q]);
             p.f.rhs1[1][q] = dt * (gam * rk3y + ro * R(p.f.rk3o[1][q]) + R(2.0) * alpha * aly
                                    - R(2.0) * alpha * (R(pp[q]) - R(pp[q - sx])) * R(M.c2cyi[j]));
             p.f.rk3oo[1][q] = p.f.rk3o[1][q];
@@ -148,7 +152,7 @@ __global__ void __launch_bounds__(kThreads) k_rhs(KP p, Box b, R gam, R ro) {
                 alz = alz + (tx + ty + R(2.0) * tz);
                 rk3z = rk3z + (a + bb);
             }
-            if (c.ihtrans == 1 && c.grdir == 3 && c.gterm != 0.0) rk3z = rk3z + c.gterm * R(t[q]);
+            if (gbz) rk3z = rk3z + c.gterm * R(t[q]);
             p.f.rhs1[2][q] = dt * (gam * rk3z + ro * R(p.f.rk3o[2][q]) + R(2.0) * alpha * alz
                                    - R(2.0) * alpha * (R(pp[q]) - R(pp[q - sxy])) * R(M.c2czi[k]));
             p.f.rk3oo[2][q] = p.f.rk3o[2][q];
@@ -231,8 +235,8 @@ __global__ void __launch_bounds__(kThreads) k_rhs_t(KP p, Box b, R gam, R ro) {
             if (i == g.n1m) ip = g.n1;
             if (i == 1) im = 0;
         }
-        const R fiu = R(g.fixiu[i]), fil = R(g.fixil[i]), fju = R(g.fixju[j]), fjl = R(g.fixjl[j]);
-        const R fku = R(g.fixku[k]), fkl = R(g.fixkl[k]);
+        const R fiu = M.fixiu[i], fil = M.fixil[i], fju = M.fixju[j], fjl = M.fixjl[j];
+        const R fku = M.fixku[k], fkl = M.fixkl[k];
         R tq = R(t[q]);
         long long qip = g.ix(ip, j, k), qim = g.ix(im, j, k), qjp = g.ix(i, jp, k), qjm = g.ix(i, jm, k);
         long long qkp = g.ix(i, j, kp), qkm = g.ix(i, j, km);

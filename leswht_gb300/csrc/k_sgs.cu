@@ -22,8 +22,8 @@ __device__ void velgrad(const KP &p, int i, int j, int k, R a[9], R sr[6]) {
     const R *u = M.u, *v = M.v, *w = M.w;
     int kp = g.kpv[k], km = g.kmv[k], jp = g.jpv[j], jm = g.jmv[j], ip = g.ipv[i], im = g.imv[i];
     int n1 = g.n1, n2 = g.n2, n3 = g.n3;
-    R fju = R(g.fixju[j]), fjl = R(g.fixjl[j]), fku = R(g.fixku[k]), fkl = R(g.fixkl[k]);
-    R fiu = R(g.fixiu[i]), fil = R(g.fixil[i]);
+    R fju = M.fixju[j], fjl = M.fixjl[j], fku = M.fixku[k], fkl = M.fixkl[k];
+    R fiu = M.fixiu[i], fil = M.fixil[i];
     const R *f2fx = M.f2fx, *f2fy = M.f2fy, *f2fz = M.f2fz;
 #define U(a_, b_, c_) R(u[g.ix(a_, b_, c_)])
 #define V(a_, b_, c_) R(v[g.ix(a_, b_, c_)])
@@ -78,8 +78,8 @@ __device__ void temgrad(const KP &p, int i, int j, int k, R a[3]) {
     const DGrid &g = p.g;
     const R *t = M.t;
     int kp = g.kpv[k], km = g.kmv[k], jp = g.jpv[j], jm = g.jmv[j], ip = g.ipv[i], im = g.imv[i];
-    R fiu = R(g.fixiu[i]), fil = R(g.fixil[i]), fju = R(g.fixju[j]), fjl = R(g.fixjl[j]);
-    R fku = R(g.fixku[k]), fkl = R(g.fixkl[k]);
+    R fiu = M.fixiu[i], fil = M.fixil[i], fju = M.fixju[j], fjl = M.fixjl[j];
+    R fku = M.fixku[k], fkl = M.fixkl[k];
     R tc = R(t[g.ix(i, j, k)]);
     R tip = R(t[g.ix(ip, j, k)]), tim = R(t[g.ix(im, j, k)]);
     R tp = R(0.5) * (R(M.f2fx[i]) * tip + R(M.f2fx[ip]) * tc) * R(M.c2cxi[ip]) * (R(1.0) - fiu) + tip * fiu;

@@ -360,6 +360,14 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
         m.aiu = f.aiu; m.ciu = f.ciu; m.aivw = f.aivw; m.civw = f.civw; m.ajv = f.ajv; m.cjv = f.cjv;
         m.ajuw = f.ajuw; m.cjuw = f.cjuw; m.akw = f.akw; m.ckw = f.ckw; m.akuv = f.akuv; m.ckuv = f.ckuv;
         m.cfx1 = f.cfx1; m.cfy1 = f.cfy1; m.cfz1 = f.cfz1;
+        auto flags = [&](const int64_t *src, long long n) {     // (1:n) int64 -> (0:n+1) double
+            std::vector<double> h(n + 2, 0.0);
+            for (long long q = 1; q <= n; q++) h[q] = (double)src[q - 1];
+            return (const double *)upload(A, h.data(), h.size());
+        };
+        m.fixil = flags(g->fixil, d.n1m); m.fixiu = flags(g->fixiu, d.n1m);
+        m.fixjl = flags(g->fixjl, d.n2m); m.fixju = flags(g->fixju, d.n2m);
+        m.fixkl = flags(g->fixkl, d.n3m); m.fixku = flags(g->fixku, d.n3m);
         if (cfg->precision == LESGPU_PREC_MIXED) {
             Mir<float> &r = c->kp.mf;
             MirState &ms = X->mir;
@@ -390,6 +398,9 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
             r.ajv = v32(f.ajv, ny); r.cjv = v32(f.cjv, ny); r.ajuw = v32(f.ajuw, ny); r.cjuw = v32(f.cjuw, ny);
             r.akw = v32(f.akw, nz); r.ckw = v32(f.ckw, nz); r.akuv = v32(f.akuv, nz); r.ckuv = v32(f.ckuv, nz);
             r.cfx1 = v32(f.cfx1, 3 * (d.n1m + 2)); r.cfy1 = v32(f.cfy1, 3 * (d.n2m + 2)); r.cfz1 = v32(f.cfz1, 3 * (d.n3m + 2));
+            r.fixil = v32(m.fixil, d.n1m + 2); r.fixiu = v32(m.fixiu, d.n1m + 2);
+            r.fixjl = v32(m.fixjl, d.n2m + 2); r.fixju = v32(m.fixju, d.n2m + 2);
+            r.fixkl = v32(m.fixkl, d.n3m + 2); r.fixku = v32(m.fixku, d.n3m + 2);
         }
     }
     c->S = A.get<DScal>(1);

@@ -152,6 +152,9 @@ struct Mir {
     const T *f2fx, *f2fy, *f2fz, *f2fxi, *f2fyi, *f2fzi, *c2cxi, *c2cyi, *c2czi;
     const T *aiu, *ciu, *aivw, *civw, *ajv, *cjv, *ajuw, *cjuw, *akw, *ckw, *akuv, *ckuv;
     const T *cfx1, *cfy1, *cfz1;     // test-filter weights
+    // the wall flags fix?? (1-based) as T: a stencil loads them instead of
+    // converting an int per cell (conversions issue on GB300's FP64 pipe)
+    const T *fixil, *fixiu, *fixjl, *fixju, *fixkl, *fixku;
 };
 
 struct KP {                   // everything a kernel may read, passed by value
