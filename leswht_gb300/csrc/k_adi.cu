@@ -886,7 +886,10 @@ static void adi_table_load(const char *path) {
     std::lock_guard<std::mutex> lk(g_adi_mu);
     while (fscanf(f, "%15s %d %d %d %d %d %d %d %d %d", tag, &k.n1m, &k.n2m, &k.n3m, &k.dir, &k.ncomp, &k.f32,
                   &k.periodic, &k.nmax, &w) == 10)
-        if (!strcmp(tag, "adi") && (w == 1 || w == 8 || w == 16 || w == 32) && !g_adi_w.count(k)) g_adi_w[k] = w;
+        if (!strcmp(tag, "adi") && !g_adi_w.count(k)) {
+            const int wl = w & 63;    // lanes; + 64: the register-capped warp-scan kernel
+            if ((wl == 1 && w == 1) || ((wl == 8 || wl == 16 || wl == 32) && (w == wl || w == (wl | 64)))) g_adi_w[k] = w;
+        }
     fclose(f);
 }
 

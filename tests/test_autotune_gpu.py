@@ -60,6 +60,19 @@ def test_table_persists_in_a_file(tmp_path, monkeypatch):
     s = leswht_gb300.gpu_solver(cases.channel(16, 16, 8))
     lines = [ln.split() for ln in path.read_text().splitlines()]
     mine = [ln for ln in lines if ln[0] == "adi" and ln[1:4] == ["16", "16", "8"]]
-    assert mine and all(ln[-1] in ("1", "8", "16", "32") for ln in mine)
+    assert mine and all(int(ln[-1]) & 63 in (1, 8, 16, 32) for ln in mine)
     tuned = {(int(ln[4]), int(ln[5]), int(ln[6]), int(ln[-1])) for ln in mine}
     assert {t for t in leswht_gb300.tuning(s.lib, s.h) if t[0] < 3} <= tuned
+
+
+def test_table_file_choices_are_reused(tmp_path, monkeypatch):
+    """A choice read from the file -- here the register-capped 8-lane y sweep
+    (code 8 + 64) -- is used as is, not timed again."""
+    path = tmp_path / "tune.txt"
+    path.write_text("adi 24 20 12 1 3 0 0 20 72\n")
+    monkeypatch.setenv("LESGPU_AUTOTUNE", "1")
+    monkeypatch.setenv("LESGPU_TUNE_FILE", str(path))
+    s = leswht_gb300.gpu_solver(cases.channel(24, 20, 12))
+    assert (1, 3, 0, 72) in leswht_gb300.tuning(s.lib, s.h)
+    assert "adi 24 20 12 1 3 0 0 20 72" in path.read_text()
+
