@@ -149,7 +149,9 @@ struct LagTerm {
                          : l == 1 ? g.f2fx[ii] * g.c2cy[jj] * g.f2fz[kk]
                                   : g.f2fx[ii] * g.f2fy[jj] * g.c2cz[kk];
         const long long q = g.ix(ii, jj, kk);
-        w[l] = vol * (p.f.dudtr[l][n] - (gam * p.f.rk3o[l][q] + ro * p.f.rk3oo[l][q]));
+        const double ho = p.f.rk3of[l] ? (double)p.f.rk3of[l][q] : p.f.rk3o[l][q];
+        const double hoo = p.f.rk3oof[l] ? (double)p.f.rk3oof[l][q] : p.f.rk3oo[l][q];
+        w[l] = vol * (p.f.dudtr[l][n] - (gam * ho + ro * hoo));
     }
 };
 struct LagFinal {

@@ -74,11 +74,11 @@ __global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 1) k_rhs(KP p, 
                 rk3x = rk3x + (a + bb);
             }
             if (gbx) rk3x = rk3x + c.gterm * R(t[q]);
-            p.f.rhs1[0][q] = dt * (gam * rk3x + ro * R(p.f.rk3o[0][q]) + R(2.0) * alpha * alx
+            p.f.rhs1[0][q] = dt * (gam * rk3x + ro * hist_o<R>(p, 0)[q] + R(2.0) * alpha * alx
                                    - R(2.0) * alpha * (R(pp[q]) - R(pp[q - 1])) * R(M.c2cxi[i])
                                    - R(2.0) * alpha * pmi0 * ichfac);
-            p.f.rk3oo[0][q] = p.f.rk3o[0][q];
-            p.f.rk3o[0][q] = rk3x;
+            hist_oo<R>(p, 0)[q] = hist_o<R>(p, 0)[q];
+            hist_o<R>(p, 0)[q] = rk3x;
         }
         // ---------------- v momentum
         if (j >= g.j_bgpy) {
@@ -114,10 +114,10 @@ __global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 1) k_rhs(KP p, 
                 rk3y = rk3y + (a + bb);
             }
             if (gby) rk3y = rk3y + c.gterm * R(t[q]);
-            p.f.rhs1[1][q] = dt * (gam * rk3y + ro * R(p.f.rk3o[1][q]) + R(2.0) * alpha * aly
+            p.f.rhs1[1][q] = dt * (gam * rk3y + ro * hist_o<R>(p, 1)[q] + R(2.0) * alpha * aly
                                    - R(2.0) * alpha * (R(pp[q]) - R(pp[q - sx])) * R(M.c2cyi[j]));
-            p.f.rk3oo[1][q] = p.f.rk3o[1][q];
-            p.f.rk3o[1][q] = rk3y;
+            hist_oo<R>(p, 1)[q] = hist_o<R>(p, 1)[q];
+            hist_o<R>(p, 1)[q] = rk3y;
         }
         // ---------------- w momentum
         if (k >= g.k_bgpz && g.n3m != 1) {
@@ -153,10 +153,10 @@ __global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 3 : 1) k_rhs(KP p, 
                 rk3z = rk3z + (a + bb);
             }
             if (gbz) rk3z = rk3z + c.gterm * R(t[q]);
-            p.f.rhs1[2][q] = dt * (gam * rk3z + ro * R(p.f.rk3o[2][q]) + R(2.0) * alpha * alz
+            p.f.rhs1[2][q] = dt * (gam * rk3z + ro * hist_o<R>(p, 2)[q] + R(2.0) * alpha * alz
                                    - R(2.0) * alpha * (R(pp[q]) - R(pp[q - sxy])) * R(M.c2czi[k]));
-            p.f.rk3oo[2][q] = p.f.rk3o[2][q];
-            p.f.rk3o[2][q] = rk3z;
+            hist_oo<R>(p, 2)[q] = hist_o<R>(p, 2)[q];
+            hist_o<R>(p, 2)[q] = rk3z;
         }
     }
 }
@@ -282,9 +282,9 @@ __global__ void __launch_bounds__(kThreads) k_rhs_t(KP p, Box b, R gam, R ro) {
             R tz = R(M.f2fzi[k]) * (R(al3[qkp]) * R(M.c2czi[kp]) * (tkp - tq) - R(al3[q]) * R(M.c2czi[k]) * (tq - tkm));
             alt = alt + omega * (tx + ty + tz);
         }
-        p.f.rhs1[3][q] = dt * (gam * rk3t + ro * R(p.f.rk3o[3][q]) + R(2.0) * alpha * alt);
-        p.f.rk3oo[3][q] = p.f.rk3o[3][q];
-        p.f.rk3o[3][q] = rk3t;
+        p.f.rhs1[3][q] = dt * (gam * rk3t + ro * hist_o<R>(p, 3)[q] + R(2.0) * alpha * alt);
+        hist_oo<R>(p, 3)[q] = hist_o<R>(p, 3)[q];
+        hist_o<R>(p, 3)[q] = rk3t;
     }
 }
 

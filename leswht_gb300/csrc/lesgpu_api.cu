@@ -221,6 +221,8 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
     f.u = A.get<double>(nt); f.v = A.get<double>(nt); f.w = A.get<double>(nt);
     f.p = A.get<double>(nt); f.t = A.get<double>(nt);
     for (int l = 0; l < 4; l++) { f.rhs1[l] = A.get<double>(nt); f.rk3o[l] = A.get<double>(nt); f.rk3oo[l] = A.get<double>(nt); }
+    if (cfg->precision == LESGPU_PREC_MIXED)
+        for (int l = 0; l < 4; l++) { f.rk3of[l] = A.get<float>(nt); f.rk3oof[l] = A.get<float>(nt); }
     f.nusgs = A.get<double>(nt); f.alsgs = A.get<double>(nt);
     for (int l = 0; l < 3; l++) { f.nusgs1[l] = A.get<double>(nt); f.alsgs1[l] = A.get<double>(nt); }
     f.qmass = A.get<double>(nt); f.divgsum = A.get<double>(nt); f.phi = A.get<double>(nt);
@@ -841,11 +843,30 @@ static int field_ptrs(lesgpu_case *c, int64_t fld, double **ptr, int *nc) {
     }
 }
 
+// the mixed form's FP32 RK3 histories, for the array copies below (null otherwise)
+static float *const *hist32(lesgpu_case *c, int64_t fld) {
+    DFields &f = c->kp.f;
+    if (!f.rk3of[0]) return nullptr;
+    if (fld == LESGPU_F_RK3O) return f.rk3of;
+    if (fld == LESGPU_F_RK3OO) return f.rk3oof;
+    return nullptr;
+}
+
 extern "C" int lesgpu_get_array(lesgpu_case *c, int64_t fld, double *out) {
     double *ptr[4];
     int nc;
     if (!c || !out || field_ptrs(c, fld, ptr, &nc)) return LESGPU_ERR_ARG;
     size_t nt = (size_t)c->kp.g.nt;
+    if (float *const *h = hist32(c, fld)) {
+        std::vector<float> tmp(nt);
+        for (int l = 0; l < nc; l++) {
+            if (cudaMemcpyAsync(tmp.data(), h[l], nt * sizeof(float), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+                cudaStreamSynchronize(c->stream) != cudaSuccess)
+                return LESGPU_ERR_CUDA;
+            for (size_t q = 0; q < nt; q++) out[l * nt + q] = (double)tmp[q];
+        }
+        return 0;
+    }
     for (int l = 0; l < nc; l++) cudaMemcpyAsync(out + l * nt, ptr[l], nt * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     return cuda_rc(cudaStreamSynchronize(c->stream));
 }
@@ -855,6 +876,16 @@ extern "C" int lesgpu_set_array(lesgpu_case *c, int64_t fld, const double *in) {
     int nc;
     if (!c || !in || field_ptrs(c, fld, ptr, &nc)) return LESGPU_ERR_ARG;
     size_t nt = (size_t)c->kp.g.nt;
+    if (float *const *h = hist32(c, fld)) {      // rounded to the FP32 the mixed form keeps
+        std::vector<float> tmp(nt);
+        for (int l = 0; l < nc; l++) {
+            for (size_t q = 0; q < nt; q++) tmp[q] = (float)in[l * nt + q];
+            if (cudaMemcpyAsync(h[l], tmp.data(), nt * sizeof(float), cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
+                cudaStreamSynchronize(c->stream) != cudaSuccess)
+                return LESGPU_ERR_CUDA;
+        }
+        return 0;
+    }
     for (int l = 0; l < nc; l++) cudaMemcpyAsync(ptr[l], in + l * nt, nt * sizeof(double), cudaMemcpyHostToDevice, c->stream);
     launch_mirror(c, ~0u);
     return cuda_rc(cudaStreamSynchronize(c->stream));

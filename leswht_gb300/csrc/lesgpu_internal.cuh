@@ -82,6 +82,9 @@ struct DScal {
 struct DFields {
     double *u, *v, *w, *p, *t;
     double *rhs1[4], *rk3o[4], *rk3oo[4];
+    // the mixed form keeps the RK3 histories in FP32 (its FP32 stencils
+    // produce them, so the storage is exact); null in the FP64 form
+    float *rk3of[4], *rk3oof[4];
     double *nusgs, *nusgs1[3], *alsgs, *alsgs1[3];
     double *qmass, *divgsum, *phi;
     double *cstar, *kstar[6];
@@ -169,6 +172,14 @@ struct KP {                   // everything a kernel may read, passed by value
 template <class R> __device__ __forceinline__ R pickr(double d, float f);
 template <> __device__ __forceinline__ double pickr<double>(double d, float) { return d; }
 template <> __device__ __forceinline__ float pickr<float>(double, float f) { return f; }
+
+// RK3 histories N^{k-1} and N^{k-2} of component l in the arithmetic type
+template <class R> __device__ __forceinline__ R *hist_o(const KP &p, int l);
+template <> __device__ __forceinline__ double *hist_o<double>(const KP &p, int l) { return p.f.rk3o[l]; }
+template <> __device__ __forceinline__ float *hist_o<float>(const KP &p, int l) { return p.f.rk3of[l]; }
+template <class R> __device__ __forceinline__ R *hist_oo(const KP &p, int l);
+template <> __device__ __forceinline__ double *hist_oo<double>(const KP &p, int l) { return p.f.rk3oo[l]; }
+template <> __device__ __forceinline__ float *hist_oo<float>(const KP &p, int l) { return p.f.rk3oof[l]; }
 
 template <class R> __device__ __forceinline__ const Mir<R> &mir(const KP &p);
 template <> __device__ __forceinline__ const Mir<double> &mir<double>(const KP &p) { return p.md; }
