@@ -339,24 +339,31 @@ struct ZeroMaxFinal {
 };
 
 // nutinterpol / alpinterpol main loops (sgs.f90:981-1004 / 1627-1650)
+// Each edge value is c2c?i c2c?i / 4 times a bilinear combination of the four
+// surrounding cell values (sgs.f90:1002-1040); the four products of the 1-D
+// weights are formed once per edge line (ew1..3), so a value costs four FP64
+// operations instead of nine -- the pass is FP64-pipe bound on GB300.
 __global__ void __launch_bounds__(kThreads) k_edge_interp(KP p, Box b, const double *f, double *f1, double *f2,
                                                            double *f3, int ib, int jb, int kb) {
     const DGrid &g = p.g;
-    const double *f2fx = g.f2fx, *f2fy = g.f2fy, *f2fz = g.f2fz;
+    const long long n2 = g.n2 + 1, n3 = g.n3 + 1;
     GRID_LOOP(b) {
         int i, j, k;
         b.at(tt, i, j, k);
         long long q = g.ix(i, j, k);
         double c = f[q], cim = f[q - 1], cjm = f[q - g.sx], ckm = f[q - g.sxy];
-        if (k >= kb && j >= jb)
-            f1[q] = g.c2cyi[j] * g.c2czi[k] * 0.25
-                  * (f2fy[j - 1] * (f2fz[k - 1] * c + f2fz[k] * ckm) + f2fy[j] * (f2fz[k - 1] * cjm + f2fz[k] * f[q - g.sx - g.sxy]));
-        if (k >= kb && i >= ib)
-            f2[q] = g.c2czi[k] * g.c2cxi[i] * 0.25
-                  * (f2fz[k - 1] * (f2fx[i - 1] * c + f2fx[i] * cim) + f2fz[k] * (f2fx[i - 1] * ckm + f2fx[i] * f[q - 1 - g.sxy]));
-        if (j >= jb && i >= ib)
-            f3[q] = g.c2cxi[i] * g.c2cyi[j] * 0.25
-                  * (f2fx[i - 1] * (f2fy[j - 1] * c + f2fy[j] * cjm) + f2fx[i] * (f2fy[j - 1] * cim + f2fy[j] * f[q - 1 - g.sx]));
+        if (k >= kb && j >= jb) {
+            const double *w = p.f.ew1 + 4 * (j + n2 * k);
+            f1[q] = w[0] * c + w[1] * ckm + w[2] * cjm + w[3] * f[q - g.sx - g.sxy];
+        }
+        if (k >= kb && i >= ib) {
+            const double *w = p.f.ew2 + 4 * (k + n3 * i);
+            f2[q] = w[0] * c + w[1] * cim + w[2] * ckm + w[3] * f[q - 1 - g.sxy];
+        }
+        if (j >= jb && i >= ib) {
+            const double *w = p.f.ew3 + 4 * (i + (long long)(g.n1 + 1) * j);
+            f3[q] = w[0] * c + w[1] * cjm + w[2] * cim + w[3] * f[q - 1 - g.sx];
+        }
     }
 }
 

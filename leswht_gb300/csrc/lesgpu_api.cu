@@ -258,6 +258,36 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
         f.fb_u = upload(A, fbu.data(), nt);
         f.fb_c = upload(A, fbc.data(), nt);
         f.wq = A.get<double>(nt); f.wb = A.get<double>(nt); f.wt = A.get<double>(nt);
+        // nutinterpol's edge weights (sgs.f90:1002-1040), 4 per edge line
+        {
+            const long long N1 = d.n1 + 1, N2 = d.n2 + 1, N3 = d.n3 + 1;
+            std::vector<double> e1(4 * N2 * N3, 0.0), e2(4 * N3 * N1, 0.0), e3(4 * N1 * N2, 0.0);
+            const double *cxi = g->c2cxi, *cyi = g->c2cyi, *czi = g->c2czi, *fx = g->f2fx, *fy = g->f2fy, *fz = g->f2fz;
+            for (long long kk = 1; kk < N3; kk++)
+                for (long long jj = 1; jj < N2; jj++) {
+                    const double W = cyi[jj] * czi[kk] * 0.25;
+                    double *w = &e1[4 * (jj + N2 * kk)];
+                    w[0] = W * fy[jj - 1] * fz[kk - 1]; w[1] = W * fy[jj - 1] * fz[kk];
+                    w[2] = W * fy[jj] * fz[kk - 1];     w[3] = W * fy[jj] * fz[kk];
+                }
+            for (long long ii = 1; ii < N1; ii++)
+                for (long long kk = 1; kk < N3; kk++) {
+                    const double W = czi[kk] * cxi[ii] * 0.25;
+                    double *w = &e2[4 * (kk + N3 * ii)];
+                    w[0] = W * fz[kk - 1] * fx[ii - 1]; w[1] = W * fz[kk - 1] * fx[ii];
+                    w[2] = W * fz[kk] * fx[ii - 1];     w[3] = W * fz[kk] * fx[ii];
+                }
+            for (long long jj = 1; jj < N2; jj++)
+                for (long long ii = 1; ii < N1; ii++) {
+                    const double W = cxi[ii] * cyi[jj] * 0.25;
+                    double *w = &e3[4 * (ii + N1 * jj)];
+                    w[0] = W * fx[ii - 1] * fy[jj - 1]; w[1] = W * fx[ii - 1] * fy[jj];
+                    w[2] = W * fx[ii] * fy[jj - 1];     w[3] = W * fx[ii] * fy[jj];
+                }
+            f.ew1 = upload(A, e1.data(), e1.size());
+            f.ew2 = upload(A, e2.data(), e2.size());
+            f.ew3 = upload(A, e3.data(), e3.size());
+        }
         // face points of heatflux (slv_auxi.f90:573-663)
         size_t nxz = (size_t)(d.n1 + 1) * (d.n3 + 1), nxy = (size_t)(d.n1 + 1) * (d.n2 + 1);
         std::vector<double> vb(nxz, 0.0), vt(nxz, 0.0), wb(nxy, 0.0), wt(nxy, 0.0);

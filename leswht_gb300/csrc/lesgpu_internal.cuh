@@ -94,6 +94,9 @@ struct DFields {
     // wq = c2cx f2fy f2fz where fb_u >= 1e-10 (flow rate), wb the same where
     // fb_c >= 1e-10 (bulk velocity), wt = f2fx f2fy f2fz / c* (temperature)
     double *wq, *wb, *wt;
+    // weights of the edge interpolation of nutinterpol / alpinterpol, 4 per
+    // edge: ew1 over (j, k), ew2 over (k, i), ew3 over (i, j) (k_edge_interp)
+    double *ew1, *ew2, *ew3;
     // body function on the y faces (xmp_i, y_1 | y_n2, zmp_k) and the z faces
     // (xmp_i, ymp_j, z_1 | z_n3), planes indexed i + (n1+1) * (k | j)
     double *fb_vb, *fb_vt, *fb_wb, *fb_wt;
