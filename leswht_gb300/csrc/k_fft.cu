@@ -814,10 +814,6 @@ void fft_z_inv64(dim3 grid, size_t smem, cudaStream_t st, KP p, const double2 *c
 void fft_x64(int nblocks, size_t smem, cudaStream_t st, double2 *ccap, int nlines, DevPlan P, int L, int inv) {
     k_fft_x<double2><<<nblocks, kThreads, smem, st>>>(ccap, nlines, P, L, inv);
 }
-void ytri64(int nblocks, cudaStream_t st, KP p, double2 *ccap, const double *ybet, const double *ygam,
-            const double *yam, const double *pinref) {
-    k_ytri<double><<<nblocks, 64, 0, st>>>(p, reinterpret_cast<double *>(ccap), ybet, ygam, yam, pinref);
-}
 int fft_smem64(int bytes) {
     return (cudaFuncSetAttribute(k_fft_z_fwd<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess &&
             cudaFuncSetAttribute(k_fft_z_inv<double2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess &&

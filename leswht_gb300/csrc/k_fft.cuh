@@ -33,8 +33,6 @@ int fft_xr_inv_lines(int n, int L, int pin);
 __global__ void k_ytri_elim(KP p, double2 *ccap, const double *ak1, const double *ak3, double *gam);
 __global__ void k_ytri_lu(KP p, const double *ak1, const double *ak3, double *ybet, double *ygam, double *yam,
                           double *pinref);
-void ytri64(int nblocks, cudaStream_t st, KP p, double2 *ccap, const double *ybet, const double *ygam,
-            const double *yam, const double *pinref);
 int fft_lines_per_block(int n);
 int fft_lz(const lesgpu_case *c);
 int fft_lx(const lesgpu_case *c);
