@@ -29,8 +29,13 @@ struct CflTerm {
 };
 
 // stepinit, slv_auxi.f90:2-50
+__device__ void stepinit_pre(KP p);
+// The last block of the CFL reduction first does stepinit's scalar updates
+// (k_stepinit_pre's work; the per-cell terms read none of them), saving a
+// launch per step.
 struct StepinitFinal {
     __device__ void operator()(const KP &p, const double *out) const {
+        stepinit_pre(p);
         DScal *S = p.S;
         const DCfg &c = p.c;
         double cflm = out[0] * S->dt;
@@ -53,7 +58,7 @@ struct StepinitFinal {
     }
 };
 
-__global__ void k_stepinit_pre(KP p) {
+__device__ void stepinit_pre(KP p) {
     DScal *S = p.S;
     S->ntime += 1;
     S->m = S->ntime;
@@ -71,7 +76,6 @@ __global__ void k_zero_fcvavg(KP p) {
 }
 
 void launch_stepinit(lesgpu_case *c) {
-    k_stepinit_pre<<<1, 1, 0, c->stream>>>(c->kp);
     if (c->kp.c.ibmon == 1) k_zero_fcvavg<<<64, kThreads, 0, c->stream>>>(c->kp);
     reduce<1, true>(c, interior(c->kp.g), CflTerm{}, StepinitFinal{});
 }
@@ -151,8 +155,15 @@ struct CvolTerm {
 struct CvolFinal {
     __device__ void operator()(const KP &p, const double *out) const { p.S->cvol = out[0]; }
 };
-__global__ void k_tvolcorr(KP p) { p.S->thcap = (p.S->tvol[2] - p.S->tvol[1]) / p.S->cvol; }
-void launch_tvolcorr(lesgpu_case *c) { k_tvolcorr<<<1, 1, 0, c->stream>>>(c->kp); }
+// tvolcalc(tvol(2)) followed by tvolcorr in one launch: the reduction's last
+// block stores tvol(2) and forms thcap from it
+struct TvolCorrFinal {
+    __device__ void operator()(const KP &p, const double *out) const {
+        p.S->tvol[2] = out[0];
+        p.S->thcap = (p.S->tvol[2] - p.S->tvol[1]) / p.S->cvol;
+    }
+};
+void launch_tvolcalc_corr(lesgpu_case *c) { reduce<1, false>(c, interior(c->kp.g), TvolTerm{}, TvolCorrFinal{}); }
 void launch_cvol(lesgpu_case *c) { reduce<1, false>(c, interior(c->kp.g), CvolTerm{}, CvolFinal{}); }
 
 // tcalc, slv_auxi.f90:496-516
@@ -404,14 +415,17 @@ struct DivTerm {   // convergence_check, misc_init.f90:1047-1077
         w[2] = isfinite(fin) ? 0.0 : 1.0;
     }
 };
+// the last block also advances time (k_time_advance's work; the divergence
+// terms do not read it), one launch fewer per step
 struct DivFinal {
     __device__ void operator()(const KP &p, const double *o) const {
+        p.S->time = p.S->time + p.S->dt;
         p.S->dvmax = o[0];
         if (p.c.ibmon == 1 && p.c.masson == 1) p.S->qmmax = o[1];
         if (o[2] > 0.0 || !isfinite(o[0])) p.S->err |= 2;
     }
 };
-void launch_convergence(lesgpu_case *c) { reduce<3, true>(c, interior(c->kp.g), DivTerm{}, DivFinal{}); }
+void launch_advance_and_convergence(lesgpu_case *c) { reduce<3, true>(c, interior(c->kp.g), DivTerm{}, DivFinal{}); }
 
 struct BulkTerm {   // writehistory's bulk quantities, misc_hist.f90:73-181
     __device__ void operator()(const KP &p, int i, int j, int k, double *w) const {
@@ -439,7 +453,5 @@ struct BulkFinal {
 };
 void launch_bulk_diag(lesgpu_case *c) { reduce<6, false>(c, interior(c->kp.g), BulkTerm{}, BulkFinal{}); }
 
-__global__ void k_time_advance(KP p) { p.S->time = p.S->time + p.S->dt; }
-void launch_time_advance(lesgpu_case *c) { k_time_advance<<<1, 1, 0, c->stream>>>(c->kp); }
 
 }  // namespace lg

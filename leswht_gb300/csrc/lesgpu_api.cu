@@ -654,7 +654,7 @@ static void enqueue_energy(lesgpu_case *c, int msub) {
     launch_convbc_t(c);
     launch_adi_t(c);
     launch_energy_bc(c);
-    if (g.ich == 1) { launch_tvolcalc(c, 2); launch_tvolcorr(c); }
+    if (g.ich == 1) launch_tvolcalc_corr(c);        // tvolcalc(tvol(2)) + tvolcorr
     launch_tcalc(c);
     if (g.ich == 1) launch_tvolcalc(c, 0);
 }
@@ -677,8 +677,7 @@ static void enqueue_step(lesgpu_case *c, bool first) {
         if (g.ibmon == 1) launch_lagforce(c, msub);
         if (g.ihtrans == 1) enqueue_energy(c, msub);
     }
-    launch_time_advance(c);
-    launch_convergence(c);
+    launch_advance_and_convergence(c);              // time += dt, convergence_check
     launch_bulk_diag(c);
     if (g.ibmon == 1) launch_draglift(c);
     if (g.ihtrans == 1) launch_heatflux(c);

@@ -319,14 +319,13 @@ void launch_stepinit(lesgpu_case *c);
 void launch_substepinit(lesgpu_case *c, int msub);
 void launch_qvolcalc(lesgpu_case *c, int slot);
 void launch_tvolcalc(lesgpu_case *c, int slot);
-void launch_tvolcorr(lesgpu_case *c);
+void launch_tvolcalc_corr(lesgpu_case *c);
 void launch_meanpg(lesgpu_case *c);
 void launch_ucalc(lesgpu_case *c);
 void launch_pcalc(lesgpu_case *c);
 void launch_tcalc(lesgpu_case *c);
-void launch_convergence(lesgpu_case *c);
+void launch_advance_and_convergence(lesgpu_case *c);
 void launch_bulk_diag(lesgpu_case *c);
-void launch_time_advance(lesgpu_case *c);
 void launch_rhs(lesgpu_case *c, int msub);
 void launch_divgs(lesgpu_case *c);
 void launch_ghost_uvw(lesgpu_case *c);
