@@ -331,10 +331,34 @@ void ghost(lesgpu_case *c, int dir, GhostSpec *s, int na) {
     k_ghost<<<blocks_for(mx), kThreads, 0, c->stream>>>(c->kp, dir, a0, a1, a2, a3, na);
 }
 
-void launch_ucalc(lesgpu_case *c) {
+// qvolcalc(qvol(2)), ucalc and qvolcalc(qvol(0)) in one pass: per cell the
+// flow-rate term of the predicted u, the projection of u, v, w (which reads
+// only phi's neighbours), then the flow-rate term of the projected u.  The
+// sums run in the reduction kernel's own order, so qvol(2) and qvol(0) are
+// bitwise those of two separate qvolcalc launches.
+struct UcalcQvolTerm {
+    __device__ void operator()(const KP &p, int i, int j, int k, double *w) const {
+        const DGrid &g = p.g;
+        const long long q = g.ix(i, j, k);
+        const double dtc = p.S->dtconst;
+        const double *phi = p.f.phi;
+        w[0] = p.f.u[q] * p.f.wq[q];
+        const double ph = phi[q];
+        if (i >= g.i_bgpx) p.f.u[q] = p.f.u[q] - dtc * (ph - phi[g.ix(g.imv[i], j, k)]) * g.c2cxi[i];
+        if (j >= 2) p.f.v[q] = p.f.v[q] - dtc * (ph - phi[q - g.sx]) * g.c2cyi[j];
+        if (k >= g.k_bgpz) p.f.w[q] = p.f.w[q] - dtc * (ph - phi[g.ix(i, j, g.kmv[k])]) * g.c2czi[k];
+        w[1] = p.f.u[q] * p.f.wq[q];
+    }
+};
+struct UcalcQvolFinal {
+    __device__ void operator()(const KP &p, const double *o) const { p.S->qvol[2] = o[0]; p.S->qvol[0] = o[1]; }
+};
+
+void launch_ucalc(lesgpu_case *c, bool with_qvol) {
     const DGrid &g = c->kp.g;
     Box b = interior(g);
-    k_ucalc<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b);
+    if (with_qvol) reduce<2, false>(c, b, UcalcQvolTerm{}, UcalcQvolFinal{});
+    else k_ucalc<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b);
     DFields &f = c->kp.f;
     if (c->kp.c.zprdic == 1) {   // z first, then x (slv_auxi.f90:360-412)
         GhostSpec s[3] = {{f.u, 1, g.n1, 0, g.n2}, {f.v, 0, g.n1, 1, g.n2}, {f.w, 0, g.n1, 0, g.n2}};

@@ -669,9 +669,7 @@ static void enqueue_step(lesgpu_case *c, bool first) {
         enqueue_rhsnlhs(c, msub);
         launch_divgs(c);
         launch_poisson(c, msub);
-        if (g.ich == 1) launch_qvolcalc(c, 2);
-        launch_ucalc(c);
-        if (g.ich == 1) launch_qvolcalc(c, 0);
+        launch_ucalc(c, g.ich == 1);              // qvolcalc(qvol(2)), ucalc, qvolcalc(qvol(0))
         launch_pcalc(c);
         if (g.ich != 0) launch_meanpg(c);
         if (g.ibmon == 1) launch_lagforce(c, msub);
@@ -939,9 +937,7 @@ extern "C" int lesgpu_run_phase(lesgpu_case *c, int64_t phase, int64_t msub) {
         launch_poisson(c, (int)msub);
         break;
     case LESGPU_PH_UCALC:
-        if (g.ich == 1) launch_qvolcalc(c, 2);
-        launch_ucalc(c);
-        if (g.ich == 1) launch_qvolcalc(c, 0);
+        launch_ucalc(c, g.ich == 1);              // qvolcalc(qvol(2)), ucalc, qvolcalc(qvol(0))
         launch_pcalc(c);
         break;
     case LESGPU_PH_MEANPG: if (g.ich != 0) launch_meanpg(c); break;
