@@ -157,13 +157,19 @@ struct CvolFinal {
 };
 // tvolcalc(tvol(2)) followed by tvolcorr in one launch: the reduction's last
 // block stores tvol(2) and forms thcap from it
+// (slot0: tcalc leaves t unchanged, so the following tvolcalc(tvol(0)) is the
+// same sum and is stored here too)
 struct TvolCorrFinal {
+    int slot0;
     __device__ void operator()(const KP &p, const double *out) const {
         p.S->tvol[2] = out[0];
         p.S->thcap = (p.S->tvol[2] - p.S->tvol[1]) / p.S->cvol;
+        if (slot0) p.S->tvol[0] = out[0];
     }
 };
-void launch_tvolcalc_corr(lesgpu_case *c) { reduce<1, false>(c, interior(c->kp.g), TvolTerm{}, TvolCorrFinal{}); }
+void launch_tvolcalc_corr(lesgpu_case *c, bool slot0) {
+    reduce<1, false>(c, interior(c->kp.g), TvolTerm{}, TvolCorrFinal{slot0 ? 1 : 0});
+}
 void launch_cvol(lesgpu_case *c) { reduce<1, false>(c, interior(c->kp.g), CvolTerm{}, CvolFinal{}); }
 
 // tcalc, slv_auxi.f90:496-516

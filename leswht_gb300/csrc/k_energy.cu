@@ -25,12 +25,32 @@ struct UbulkFinal {
 };
 __global__ void k_set_ubulk_one(KP p) { p.S->u_bulk_t = 1.0; }
 
-void launch_rhs_t(lesgpu_case *c, int msub) {
+// tvolcalc(tvol(1)) and the bulk velocity in one reduction (both read every
+// interior cell; each sum keeps the order of its own launch, bitwise)
+struct TvolUbulkTerm {
+    __device__ void operator()(const KP &p, int i, int j, int k, double *w) const {
+        const long long q = p.g.ix(i, j, k);
+        w[0] = p.f.t[q] * p.f.wt[q];
+        UbulkTerm{}(p, i, j, k, w + 1);
+    }
+};
+struct TvolUbulkFinal {
+    __device__ void operator()(const KP &p, const double *o) const {
+        p.S->tvol[1] = o[0];
+        UbulkFinal{}(p, o + 1);
+    }
+};
+
+void launch_rhs_t(lesgpu_case *c, int msub, bool with_tvol) {
     const DGrid &g = c->kp.g;
-    if (c->kp.c.idecomp == 1)
-        reduce<2, false>(c, Box{1, 1, 1, g.n1m, g.n2m, g.n3m}, UbulkTerm{}, UbulkFinal{});
-    else
+    const Box b{1, 1, 1, g.n1m, g.n2m, g.n3m};
+    if (c->kp.c.idecomp == 1) {
+        if (with_tvol) reduce<3, false>(c, b, TvolUbulkTerm{}, TvolUbulkFinal{});
+        else reduce<2, false>(c, b, UbulkTerm{}, UbulkFinal{});
+    } else {
+        if (with_tvol) launch_tvolcalc(c, 1);
         k_set_ubulk_one<<<1, 1, 0, c->stream>>>(c->kp);
+    }
     launch_rhs_t_kernel(c, msub);
 }
 

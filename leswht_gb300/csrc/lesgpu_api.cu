@@ -648,15 +648,17 @@ static void enqueue_rhsnlhs(lesgpu_case *c, int msub) {
 static void enqueue_energy(lesgpu_case *c, int msub) {
     const lesgpu_config &g = c->cfg;
     launch_mirror(c, kMirVel | kMirT);     // the projected velocity
-    if (g.ich == 1) launch_tvolcalc(c, 1);
-    launch_rhs_t(c, msub);
+    launch_rhs_t(c, msub, g.ich == 1);              // with tvolcalc(tvol(1)) when ICH = 1
     if (g.ibmon != 0 && g.iconjg == 0) launch_rhs_ibm_t(c);
     launch_convbc_t(c);
     launch_adi_t(c);
     launch_energy_bc(c);
-    if (g.ich == 1) launch_tvolcalc_corr(c);        // tvolcalc(tvol(2)) + tvolcorr
+    // tvolcalc(tvol(2)) + tvolcorr; tcalc changes t only when x is not
+    // periodic, otherwise tvolcalc(tvol(0)) is the same sum
+    const bool tcalc_runs = g.ich == 1 && g.xprdic == 0;
+    if (g.ich == 1) launch_tvolcalc_corr(c, !tcalc_runs);
     launch_tcalc(c);
-    if (g.ich == 1) launch_tvolcalc(c, 0);
+    if (tcalc_runs) launch_tvolcalc(c, 0);
 }
 
 static void enqueue_step(lesgpu_case *c, bool first) {

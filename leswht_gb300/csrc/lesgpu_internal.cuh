@@ -319,7 +319,8 @@ void launch_stepinit(lesgpu_case *c);
 void launch_substepinit(lesgpu_case *c, int msub);
 void launch_qvolcalc(lesgpu_case *c, int slot);
 void launch_tvolcalc(lesgpu_case *c, int slot);
-void launch_tvolcalc_corr(lesgpu_case *c);
+// tvolcalc(tvol(2)) + tvolcorr; slot0: also tvol(0) (tcalc will not change t)
+void launch_tvolcalc_corr(lesgpu_case *c, bool slot0);
 void launch_meanpg(lesgpu_case *c);
 // ucalc; with_qvol: fused with the qvolcalc before (qvol(2)) and after (qvol(0))
 void launch_ucalc(lesgpu_case *c, bool with_qvol);
@@ -330,7 +331,8 @@ void launch_bulk_diag(lesgpu_case *c);
 void launch_rhs(lesgpu_case *c, int msub);
 void launch_divgs(lesgpu_case *c);
 void launch_ghost_uvw(lesgpu_case *c);
-void launch_rhs_t(lesgpu_case *c, int msub);
+// rhs_t with its bulk velocity; with_tvol: tvolcalc(tvol(1)) in the same reduction
+void launch_rhs_t(lesgpu_case *c, int msub, bool with_tvol);
 void launch_energy_bc(lesgpu_case *c);
 void launch_adi_uvw(lesgpu_case *c);
 void launch_adi_t(lesgpu_case *c);
