@@ -87,20 +87,92 @@ __device__ __forceinline__ void adi_coef(const KP &p, int comp, int dir, int i, 
     }
 }
 
+// The same coefficients in factored form, a = ma[l] (1 + cre nv[q + oa]) and
+// c = mc[l] (1 + cre nv[q + oa + s]) at line index l and line stride s.  The
+// c factor of element l is the a factor of element l + 1 (the same viscosity
+// value), so a serial sweep carries it over and reads and forms each factor
+// once.  This holds for every velocity coefficient and for the temperature
+// one without conjugate tables; with them, c* and k* differ between the two
+// sides of a face and adi_coef is used.
+template <class R>
+struct AdiFacs {
+    const R *ma, *mc, *nv;
+    R cre;
+    long long oa;
+};
+
+template <class R>
+__device__ __forceinline__ AdiFacs<R> adi_facs(const KP &p, int comp, int dir) {
+    const Mir<R> &M = mir<R>(p);
+    const R cre = pickr<R>(p.c.adi_cd[0], p.c.adi_cf[0]), cre2 = pickr<R>(p.c.adi_cd[1], p.c.adi_cf[1]);
+    const long long s = dir == 2 ? p.g.sxy : dir == 1 ? p.g.sx : 1;
+    switch (comp * 3 + dir) {
+    case CU * 3 + 2: return {M.akuv, M.ckuv, M.nusgs1[1], cre, 0};
+    case CU * 3 + 1: return {M.ajuw, M.cjuw, M.nusgs1[2], cre, 0};
+    case CU * 3 + 0: return {M.aiu, M.ciu, M.nusgs, cre2, -1};
+    case CV * 3 + 2: return {M.akuv, M.ckuv, M.nusgs1[0], cre, 0};
+    case CV * 3 + 1: return {M.ajv, M.cjv, M.nusgs, cre2, -s};
+    case CV * 3 + 0: return {M.aivw, M.civw, M.nusgs1[2], cre, 0};
+    case CW * 3 + 2: return {M.akw, M.ckw, M.nusgs, cre2, -s};
+    case CW * 3 + 1: return {M.ajuw, M.cjuw, M.nusgs1[0], cre, 0};
+    case CW * 3 + 0: return {M.aivw, M.civw, M.nusgs1[1], cre, 0};
+    default: {
+        const R c3 = pickr<R>(p.c.adi_cd[2], p.c.adi_cf[2]);
+        if (dir == 2) return {M.akuv, M.ckuv, M.alsgs1[1], c3, 0};
+        if (dir == 1) return {M.ajuw, M.cjuw, M.alsgs1[2], c3, 0};
+        return {M.aivw, M.civw, M.alsgs1[0], c3, 0};
+    }
+    }
+}
+
+// a and c of the elements c0 .. c0 + CHN - 1 (below nline) of the line that
+// starts at q0 with line index l1; factored when shared, fprev carrying the c
+// factor from element to element.
+template <class R, int CHN>
+__device__ __forceinline__ void adi_chunk_coefs(const KP &p, int comp, int dir, const AdiFacs<R> &F, bool shared,
+                                                int l1, int c0, int nline, int x0, int x1, long long q0,
+                                                long long stride, R &fprev, R (&av)[CHN], R (&cv)[CHN]) {
+#pragma unroll
+    for (int u = 0; u < CHN; u++) {
+        if (c0 + u < nline) {
+            const int l = l1 + c0 + u;
+            if (shared) {
+                const R fc = R(1.0) + F.cre * R(F.nv[q0 + (long long)(c0 + u) * stride + F.oa + stride]);
+                av[u] = R(F.ma[l]) * fprev;
+                cv[u] = R(F.mc[l]) * fc;
+                fprev = fc;
+            } else {
+                int i, j, k;
+                line_coords(dir, l, x0, x1, i, j, k);
+                adi_coef(p, comp, dir, i, j, k, av[u], cv[u]);
+            }
+        }
+    }
+}
+
 // Reciprocal of a pivot.  FP32: the division.  FP64: Newton-Raphson
 // iteration for 1/d, r <- r + r (1 - d r), from an FP32 reciprocal seed; each
-// step squares the relative error (2^-24 -> 2^-48 -> below the final
-// rounding), so the result is within 2 ulp of the quotient.  It takes six
-// operations on GB300's narrow FP64 pipe (two conversions, four FMAs) where a
-// correctly rounded division takes more.  Pivots outside the FP32 range, where
-// the seed would not exist, take the division.
+// step squares the relative error (2^-22 -> 2^-44 -> below the final
+// rounding), so the result is within 2 ulp of the quotient.  The seed's
+// FP64 <-> FP32 moves are done on the bit patterns with integer operations
+// (exponent rebias, mantissa truncated to 23 bits), not by conversions, which
+// on GB300 issue on the narrow FP64 pipe: the reciprocal then costs that pipe
+// four FMAs where a correctly rounded division takes more.  Pivots whose
+// binary exponent lies outside [-99, 99], where the FP32 seed or its
+// reciprocal would leave the normal FP32 range, take the division.
 template <class R>
 __device__ __forceinline__ R rcp_pivot(R d) {
     if (sizeof(R) == 4) return R(1.0) / d;
-    const float df = (float)d;
-    const float af = fabsf(df);
-    if (!(af > 1.0e-30f && af < 1.0e30f)) return R(1.0) / d;
-    double r = (double)__frcp_rn(df);
+    const unsigned long long bits = (unsigned long long)__double_as_longlong((double)d);
+    const unsigned hi = (unsigned)(bits >> 32);
+    const int ed = (int)((hi >> 20) & 0x7ffu);                // biased FP64 exponent
+    if ((unsigned)(ed - (1023 - 99)) > 198u) return R(1.0) / d;
+    const unsigned fs = (hi & 0x80000000u) | ((unsigned)(ed - 1023 + 127) << 23) | ((unsigned)(bits >> 29) & 0x7fffffu);
+    const unsigned rs = __float_as_uint(__frcp_rn(__uint_as_float(fs)));
+    const unsigned long long rb = ((unsigned long long)(rs & 0x80000000u) << 32)
+                                | ((unsigned long long)(((rs >> 23) & 0xffu) - 127u + 1023u) << 52)
+                                | ((unsigned long long)(rs & 0x7fffffu) << 29);
+    double r = __longlong_as_double((long long)rb);
     double e = fma(-(double)d, r, 1.0);
     r = fma(r, e, r);
     e = fma(-(double)d, r, 1.0);
@@ -121,7 +193,7 @@ struct AdiBatch {
     AdiArgs a[3];
 };
 
-template <class R, int DIR, bool PER>
+template <class R, int DIR, bool PER, bool FAC>
 __global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
     const AdiArgs &A = B.a[blockIdx.y];
     const DGrid &g = p.g;
@@ -140,6 +212,8 @@ __global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
     R *const sg = reinterpret_cast<R *>(A.gam);
     R *const ss = reinterpret_cast<R *>(A.sarr);
     R *const sf = F32 ? reinterpret_cast<R *>(A.gam) + g.nt : nullptr;
+    constexpr bool shared = FAC;
+    const AdiFacs<R> F = FAC ? adi_facs<R>(p, A.comp, DIR) : AdiFacs<R>{};
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nl; t += (long long)gridDim.x * blockDim.x) {
         const int x0 = A.a0 + (int)(t % na), x1 = A.b0 + (int)(t / na);
         int i0, j0, k0;
@@ -150,17 +224,13 @@ __global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
             // solution goes to the scratch (FP32, or when adding) or to dst
             R *xs = (F32 || A.add) ? ss : reinterpret_cast<R *>(A.dst);
             R bet = R(0.0), x = R(0.0), cprev = R(0.0);
+            R fprev = shared ? R(1.0) + F.cre * R(F.nv[q0 + F.oa]) : R(0.0);
             for (int c0 = 0; c0 < nline; c0 += CH) {
                 R av[CH], cv[CH], rv[CH];
+                adi_chunk_coefs<R, CH>(p, A.comp, DIR, F, shared, A.l1, c0, nline, x0, x1, q0, stride, fprev, av, cv);
 #pragma unroll
-                for (int u = 0; u < CH; u++) {
-                    if (c0 + u < nline) {
-                        int i, j, k;
-                        line_coords(DIR, A.l1 + c0 + u, x0, x1, i, j, k);
-                        adi_coef(p, A.comp, DIR, i, j, k, av[u], cv[u]);
-                        rv[u] = R(A.src[q0 + (long long)(c0 + u) * stride]);
-                    }
-                }
+                for (int u = 0; u < CH; u++)
+                    if (c0 + u < nline) rv[u] = R(A.src[q0 + (long long)(c0 + u) * stride]);
 #pragma unroll
                 for (int u = 0; u < CH; u++) {
                     if (c0 + u < nline) {
@@ -220,17 +290,13 @@ __global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
             const R fn = diag * R(A.src[qn_last]);   // original right-hand side at the last element
             R qq = R(0.0), sv0 = R(0.0), ff = R(0.0);
             R a_last = R(0.0), b_last = R(0.0), c_last = R(0.0);
+            R fprev = shared ? R(1.0) + F.cre * R(F.nv[q0 + F.oa]) : R(0.0);
             for (int c0 = 0; c0 < nline; c0 += CH) {
                 R av[CH], cv[CH], rv[CH];
+                adi_chunk_coefs<R, CH>(p, A.comp, DIR, F, shared, A.l1, c0, nline, x0, x1, q0, stride, fprev, av, cv);
 #pragma unroll
-                for (int u = 0; u < CH; u++) {
-                    if (c0 + u < nline) {
-                        int i, j, k;
-                        line_coords(DIR, A.l1 + c0 + u, x0, x1, i, j, k);
-                        adi_coef(p, A.comp, DIR, i, j, k, av[u], cv[u]);
-                        rv[u] = R(A.src[q0 + (long long)(c0 + u) * stride]);
-                    }
-                }
+                for (int u = 0; u < CH; u++)
+                    if (c0 + u < nline) rv[u] = R(A.src[q0 + (long long)(c0 + u) * stride]);
 #pragma unroll
                 for (int u = 0; u < CH; u++) {
                     if (c0 + u < nline) {
@@ -317,6 +383,19 @@ __global__ void __launch_bounds__(128, 6) k_adi(KP p, AdiBatch B) {
             }
         }
     }
+}
+
+template <class R, int DIR>
+static void k_adi_launch_dir(bool per, bool fac, dim3 grid, int tpb, cudaStream_t st, const KP &kp, const AdiBatch &B) {
+    if (per) { if (fac) k_adi<R, DIR, true, true><<<grid, tpb, 0, st>>>(kp, B); else k_adi<R, DIR, true, false><<<grid, tpb, 0, st>>>(kp, B); }
+    else { if (fac) k_adi<R, DIR, false, true><<<grid, tpb, 0, st>>>(kp, B); else k_adi<R, DIR, false, false><<<grid, tpb, 0, st>>>(kp, B); }
+}
+
+template <class R>
+static void k_adi_launch(int dir, bool per, bool fac, dim3 grid, int tpb, cudaStream_t st, const KP &kp, const AdiBatch &B) {
+    if (dir == 0) k_adi_launch_dir<R, 0>(per, fac, grid, tpb, st, kp, B);
+    else if (dir == 1) k_adi_launch_dir<R, 1>(per, fac, grid, tpb, st, kp, B);
+    else k_adi_launch_dir<R, 2>(per, fac, grid, tpb, st, kp, B);
 }
 
 // ------------------------------------------------------------------------
@@ -705,15 +784,10 @@ static bool adi_run(lesgpu_case *c, const AdiBatch &B, const AdiShape &h, int wc
         const dim3 grid((unsigned)((h.mx + tpb - 1) / tpb), (unsigned)h.ncomp);
         const int dir = B.a[0].dir;
         const bool per = B.a[0].periodic != 0;
-        if (h.f32) {
-            if (dir == 0) { if (per) k_adi<float, 0, true><<<grid, tpb, 0, c->stream>>>(c->kp, B); else k_adi<float, 0, false><<<grid, tpb, 0, c->stream>>>(c->kp, B); }
-            else if (dir == 1) { if (per) k_adi<float, 1, true><<<grid, tpb, 0, c->stream>>>(c->kp, B); else k_adi<float, 1, false><<<grid, tpb, 0, c->stream>>>(c->kp, B); }
-            else { if (per) k_adi<float, 2, true><<<grid, tpb, 0, c->stream>>>(c->kp, B); else k_adi<float, 2, false><<<grid, tpb, 0, c->stream>>>(c->kp, B); }
-        } else {
-            if (dir == 0) { if (per) k_adi<double, 0, true><<<grid, tpb, 0, c->stream>>>(c->kp, B); else k_adi<double, 0, false><<<grid, tpb, 0, c->stream>>>(c->kp, B); }
-            else if (dir == 1) { if (per) k_adi<double, 1, true><<<grid, tpb, 0, c->stream>>>(c->kp, B); else k_adi<double, 1, false><<<grid, tpb, 0, c->stream>>>(c->kp, B); }
-            else { if (per) k_adi<double, 2, true><<<grid, tpb, 0, c->stream>>>(c->kp, B); else k_adi<double, 2, false><<<grid, tpb, 0, c->stream>>>(c->kp, B); }
-        }
+        // factored coefficients unless a temperature sweep reads conjugate tables
+        const bool fac = !(B.a[0].comp == CT && c->kp.c.iconjg == 1);
+        if (h.f32) k_adi_launch<float>(dir, per, fac, grid, tpb, c->stream, c->kp, B);
+        else k_adi_launch<double>(dir, per, fac, grid, tpb, c->stream, c->kp, B);
         return true;
     }
     if (h.f32) {
