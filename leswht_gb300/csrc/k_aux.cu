@@ -360,20 +360,10 @@ struct UcalcQvolFinal {
     __device__ void operator()(const KP &p, const double *o) const { p.S->qvol[2] = o[0]; p.S->qvol[0] = o[1]; }
 };
 
-void launch_ucalc(lesgpu_case *c, bool with_qvol) {
-    const DGrid &g = c->kp.g;
-    Box b = interior(g);
+static void ucalc_interior(lesgpu_case *c, bool with_qvol) {
+    Box b = interior(c->kp.g);
     if (with_qvol) reduce<2, false>(c, b, UcalcQvolTerm{}, UcalcQvolFinal{});
     else k_ucalc<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b);
-    DFields &f = c->kp.f;
-    if (c->kp.c.zprdic == 1) {   // z first, then x (slv_auxi.f90:360-412)
-        GhostSpec s[3] = {{f.u, 1, g.n1, 0, g.n2}, {f.v, 0, g.n1, 1, g.n2}, {f.w, 0, g.n1, 0, g.n2}};
-        ghost(c, 2, s, 3);
-    }
-    if (c->kp.c.xprdic == 1) {
-        GhostSpec s[3] = {{f.u, 0, g.n2, 0, g.n3}, {f.v, 1, g.n2, 0, g.n3}, {f.w, 0, g.n2, 1, g.n3}};
-        ghost(c, 0, s, 3);
-    }
 }
 
 // prdic_adj_uvw(0), slv_mmtm.f90:1746-1857: x, then y, then z
@@ -420,14 +410,25 @@ __global__ void __launch_bounds__(kThreads) k_pcalc(KP p, Box b) {
     }
 }
 
-void launch_pcalc(lesgpu_case *c) {
+// ucalc then pcalc.  pcalc reads p, phi and divgsum but no velocity ghost,
+// so the periodic ghost copies of u, v, w (ucalc, slv_auxi.f90:360-412) and of
+// p (pcalc, :470-490) run after both interiors, the four arrays sharing one
+// launch per direction; each array still gets z first, then x.
+void launch_ucalc_pcalc(lesgpu_case *c, bool with_qvol) {
     const DGrid &g = c->kp.g;
+    ucalc_interior(c, with_qvol);
     reduce<1, false>(c, Box{1, 1, 1, 1, g.n2m, g.n3m}, PhirefTerm{}, PhirefFinal{});
     Box b = interior(g);
     k_pcalc<<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b);
     DFields &f = c->kp.f;
-    if (c->kp.c.zprdic == 1) { GhostSpec s[1] = {{f.p, 1, g.n1m, 1, g.n2m}}; ghost(c, 2, s, 1); }
-    if (c->kp.c.xprdic == 1) { GhostSpec s[1] = {{f.p, 1, g.n2m, 1, g.n3m}}; ghost(c, 0, s, 1); }
+    if (c->kp.c.zprdic == 1) {
+        GhostSpec s[4] = {{f.u, 1, g.n1, 0, g.n2}, {f.v, 0, g.n1, 1, g.n2}, {f.w, 0, g.n1, 0, g.n2}, {f.p, 1, g.n1m, 1, g.n2m}};
+        ghost(c, 2, s, 4);
+    }
+    if (c->kp.c.xprdic == 1) {
+        GhostSpec s[4] = {{f.u, 0, g.n2, 0, g.n3}, {f.v, 1, g.n2, 0, g.n3}, {f.w, 0, g.n2, 1, g.n3}, {f.p, 1, g.n2m, 1, g.n3m}};
+        ghost(c, 0, s, 4);
+    }
 }
 
 // ------------------------------------------------------- end-of-step checks

@@ -671,8 +671,7 @@ static void enqueue_step(lesgpu_case *c, bool first) {
         enqueue_rhsnlhs(c, msub);
         launch_divgs(c);
         launch_poisson(c, msub);
-        launch_ucalc(c, g.ich == 1);              // qvolcalc(qvol(2)), ucalc, qvolcalc(qvol(0))
-        launch_pcalc(c);
+        launch_ucalc_pcalc(c, g.ich == 1);        // qvolcalc(qvol(2)), ucalc, qvolcalc(qvol(0)), pcalc
         if (g.ich != 0) launch_meanpg(c);
         if (g.ibmon == 1) launch_lagforce(c, msub);
         if (g.ihtrans == 1) enqueue_energy(c, msub);
@@ -939,8 +938,7 @@ extern "C" int lesgpu_run_phase(lesgpu_case *c, int64_t phase, int64_t msub) {
         launch_poisson(c, (int)msub);
         break;
     case LESGPU_PH_UCALC:
-        launch_ucalc(c, g.ich == 1);              // qvolcalc(qvol(2)), ucalc, qvolcalc(qvol(0))
-        launch_pcalc(c);
+        launch_ucalc_pcalc(c, g.ich == 1);        // qvolcalc(qvol(2)), ucalc, qvolcalc(qvol(0)), pcalc
         break;
     case LESGPU_PH_MEANPG: if (g.ich != 0) launch_meanpg(c); break;
     case LESGPU_PH_ENERGY: if (g.ihtrans == 1) enqueue_energy(c, (int)msub); break;

@@ -323,8 +323,7 @@ void launch_tvolcalc(lesgpu_case *c, int slot);
 void launch_tvolcalc_corr(lesgpu_case *c, bool slot0);
 void launch_meanpg(lesgpu_case *c);
 // ucalc; with_qvol: fused with the qvolcalc before (qvol(2)) and after (qvol(0))
-void launch_ucalc(lesgpu_case *c, bool with_qvol);
-void launch_pcalc(lesgpu_case *c);
+void launch_ucalc_pcalc(lesgpu_case *c, bool with_qvol);
 void launch_tcalc(lesgpu_case *c);
 void launch_advance_and_convergence(lesgpu_case *c);
 void launch_bulk_diag(lesgpu_case *c);
