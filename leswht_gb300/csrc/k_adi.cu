@@ -784,8 +784,9 @@ static bool adi_run(lesgpu_case *c, const AdiBatch &B, const AdiShape &h, int wc
         const dim3 grid((unsigned)((h.mx + tpb - 1) / tpb), (unsigned)h.ncomp);
         const int dir = B.a[0].dir;
         const bool per = B.a[0].periodic != 0;
-        // factored coefficients unless a temperature sweep reads conjugate tables
-        const bool fac = !(B.a[0].comp == CT && c->kp.c.iconjg == 1);
+        // factored coefficients unless a temperature sweep reads conjugate
+        // tables that are not all 1
+        const bool fac = !(B.a[0].comp == CT && c->kp.c.iconjg == 1 && c->conj_general);
         if (h.f32) k_adi_launch<float>(dir, per, fac, grid, tpb, c->stream, c->kp, B);
         else k_adi_launch<double>(dir, per, fac, grid, tpb, c->stream, c->kp, B);
         return true;

@@ -541,6 +541,15 @@ extern "C" int lesgpu_load_ibm(lesgpu_case *c, const lesgpu_ibm *b) {
     if (b->cstar) scatter_d(b->cstar, f.cstar);
     if (b->kstar)
         for (int l = 0; l < 6; l++) scatter_d(b->kstar + (size_t)l * ncell, f.kstar[l]);
+    // unit tables (a channel whose ICONJG = 1 only provides the arrays tvolcalc
+    // reads) make the temperature coefficients c* k* + cre omega alpha equal
+    // to 1 + cre alpha, so the sweeps may use their factored form
+    for (size_t q = 0; b->omega && q < (size_t)ncell; q++)
+        if (b->omega[q] != 1) c->conj_general = 1;
+    for (size_t q = 0; b->cstar && q < (size_t)ncell; q++)
+        if (b->cstar[q] != 1.0) c->conj_general = 1;
+    for (size_t q = 0; b->kstar && q < 6 * (size_t)ncell; q++)
+        if (b->kstar[q] != 1.0) c->conj_general = 1;
     if (!A.ok) return LESGPU_ERR_OOM;
     launch_red_weights(c);
     launch_mirror(c, kMirConj);

@@ -290,6 +290,9 @@ struct lesgpu_case {
     int graph_ok;
     int use_graph;
     int autotune;              // use the autotuner's choices (LESGPU_AUTOTUNE != 0 at start)
+    // 1 once a loaded conjugate table (c*, k*, omega) holds a value other
+    // than 1; while 0 the temperature sweeps use the factored coefficients
+    int conj_general;
     // host mirrors of metrics used for init-time tables
     double *h_f2fx, *h_f2fy, *h_f2fz;
     const lesgpu_grid *h_grid;  // the caller's grid, valid only inside lesgpu_create
