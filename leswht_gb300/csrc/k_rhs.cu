@@ -217,8 +217,11 @@ void launch_divgs(lesgpu_case *c) {
 // ------------------------------------------------------------------- rhs_t
 struct UbulkTTerm;   // defined in k_energy via reduce; see launch_rhs_t there
 
+// conj: the conjugate tables (c*, k*, omega) are read; 0 when ICONJG = 0 or
+// when every loaded table value is 1, where each product with them is exact
+// and the terms reduce to the plain ones
 template <class R>
-__global__ void __launch_bounds__(kThreads) k_rhs_t(KP p, Box b, R gam, R ro) {
+__global__ void __launch_bounds__(kThreads) k_rhs_t(KP p, Box b, R gam, R ro, int conj) {
     const Mir<R> &M = mir<R>(p);
     const DGrid &g = p.g;
     const DCfg &c = p.c;
@@ -250,7 +253,7 @@ __global__ void __launch_bounds__(kThreads) k_rhs_t(KP p, Box b, R gam, R ro) {
         R ant1 = (te * R(u[qip]) - tw * R(u[q])) * R(M.f2fxi[i]);
         R ant2 = (tn * R(v[qjp]) - ts * R(v[q])) * R(M.f2fyi[j]);
         R ant3 = (tc * R(w[qkp]) - tf * R(w[q])) * R(M.f2fzi[k]);
-        R omega = (c.iconjg == 1 && c.imovingon == 0) ? R(p.f.omega[q]) : R(1.0);
+        R omega = (conj && c.imovingon == 0) ? R(p.f.omega[q]) : R(1.0);
         R src = R(0.0);
         if (c.idecomp == 1) {
             R ucc = R(0.5) * (R(u[q]) + R(u[q + 1]));
@@ -264,7 +267,7 @@ __global__ void __launch_bounds__(kThreads) k_rhs_t(KP p, Box b, R gam, R ro) {
         R a5 = (tkp - tq) * R(M.c2czi[kp]);
         R a6 = (tq - tkm) * R(M.c2czi[k]);
         R altx, alty, altz;
-        if (c.iconjg == 1) {
+        if (conj) {
             R cs = R(M.cstar[q]);
             altx = cs * (R(M.kstar[0][q]) * a1 - R(M.kstar[1][q]) * a2) * R(M.f2fxi[i]);
             alty = cs * (R(M.kstar[2][q]) * a3 - R(M.kstar[3][q]) * a4) * R(M.f2fyi[j]);
@@ -294,10 +297,11 @@ void launch_rhs_t_kernel(lesgpu_case *c, int msub) {
     const DGrid &g = c->kp.g;
     Box b{1, 1, 1, g.n1m, g.n2m, g.n3m};
     inst_begin(c, LESGPU_K_RHS_T);
+    const int conj = c->kp.c.iconjg == 1 && c->conj_general;
     if (c->cfg.precision == LESGPU_PREC_MIXED)
-        k_rhs_t<float><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, (float)gam[msub], (float)ro[msub]);
+        k_rhs_t<float><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, (float)gam[msub], (float)ro[msub], conj);
     else
-        k_rhs_t<double><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, gam[msub], ro[msub]);
+        k_rhs_t<double><<<blocks_for(b.count()), kThreads, 0, c->stream>>>(c->kp, b, gam[msub], ro[msub], conj);
     inst_end(c, LESGPU_K_RHS_T);
 }
 
