@@ -54,7 +54,7 @@ __device__ __forceinline__ void adi_coef(const KP &p, int comp, int dir, int i, 
         const R cre = pickr<R>(p.c.adi_cd[2], p.c.adi_cf[2]);   // iles re pr
         R cs = R(1.0), ks1 = R(1.0), ks2 = R(1.0), omc = R(1.0);
         int ka = dir == 2 ? 5 : dir == 1 ? 3 : 1;
-        if (p.c.iconjg == 1) {
+        if (p.c.conj_tables) {        // unit tables: the same expression with the values 1
             cs = R(M.cstar[q]);
             ks1 = R(M.kstar[ka][q]);
             ks2 = R(M.kstar[ka - 1][q]);

@@ -550,6 +550,7 @@ extern "C" int lesgpu_load_ibm(lesgpu_case *c, const lesgpu_ibm *b) {
         if (b->cstar[q] != 1.0) c->conj_general = 1;
     for (size_t q = 0; b->kstar && q < 6 * (size_t)ncell; q++)
         if (b->kstar[q] != 1.0) c->conj_general = 1;
+    c->kp.c.conj_tables = c->kp.c.iconjg == 1 && c->conj_general;
     if (!A.ok) return LESGPU_ERR_OOM;
     launch_red_weights(c);
     launch_mirror(c, kMirConj);

@@ -46,6 +46,7 @@ struct DCfg {
     int idtopt;
     int nintp[4], nbody[4];
     int nzero;
+    int conj_tables;          // 1: ICONJG = 1 with a loaded c*, k* or omega value other than 1
     // constants of the R-templated stencils, formed once on the host exactly
     // as the kernels formed them per cell: [0] in FP64, [1] the FP32 form's
     // value (FP64 arithmetic on the FP32-rounded re, then rounded)
