@@ -362,15 +362,21 @@ int lesgpu_instrument_read(lesgpu_case *c, double *ms, int64_t *launches);
  * Thomas in y, the (1,1) mode pinned -- on caller-owned DEVICE buffers
  * divgsum (input) and phi (output, interior written), both in the
  * (0:n1,0:n2,0:n3) layout, on `stream` (a cudaStream_t, or NULL), and keeps
- * all its temporaries in one fixed 32 MiB device array per GPU.  The grid
- * (x and z periodic, uniform) is read from host memory.
+ * all its temporaries in one fixed 32 MiB device array per GPU.  The grid is
+ * read from host memory; it must be periodic and uniform in x and z (ipv and
+ * kpv wrap to 1, every 1/dx and 1/dz within 1e-6 relative of the first),
+ * else LESGPU_ERR_UNSUPPORTED; a NULL grid vector is LESGPU_ERR_ARG.
  *   - It calls no cudaMalloc/cudaFree; grids needing more than the fixed
  *     array (24*n1m*(n3m/2+1)*n2m bytes plus tables, about 128^3 at most,
  *     and at most 1024 cells per direction) return LESGPU_ERR_TOO_LARGE.
+ *   - It copies nothing from host memory: its tables are built on the device
+ *     and the wall-normal vectors travel as kernel parameters.
  *   - The first call on a device sets it up (resolves the array's device
- *     address); make that first call before any stream capture.
+ *     address); that first call must not be made during a stream capture.
  *   - All calls on a device share the array and leave their contents in it;
  *     calls that overlap on the GPU race with each other -- serialise them.
+ *   - An error already pending in the calling thread's CUDA state is left
+ *     untouched and the call returns LESGPU_ERR_CUDA without launching.
  *   - Returns after enqueueing; synchronise `stream` before reading phi. */
 int lesgpu_poisson_ftft_noalloc(const lesgpu_grid *grid, const double *d_divgsum,
                                 double *d_phi, void *stream);

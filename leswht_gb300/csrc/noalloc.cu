@@ -26,8 +26,16 @@
 //     array and corrupt each other; serialise them.
 //   * The first call on a device sets that device up: it resolves the
 //     device address of the array (cudaGetSymbolAddress, with that device
-//     current) and raises the FFT kernels' shared-memory limit.  Make that
-//     first call before any stream capture on the device.
+//     current) and raises the FFT kernels' shared-memory limit.  That first
+//     call must not be made while a stream of the device is being captured.
+//   * A call copies nothing from host memory: the wavenumber and twiddle
+//     tables are computed on the device by a first small kernel, and the
+//     wall-normal metric and index tables reach it as kernel parameters, so
+//     a call neither stages pageable host memory nor waits for the stream.
+//   * The grid must be periodic and uniform in x and z (the transforms'
+//     assumptions): a grid whose ipv(n1m) or kpv(n3m) does not wrap to 1, or
+//     whose 1/dx or 1/dz varies by more than 1e-6 relative, is rejected with
+//     LESGPU_ERR_UNSUPPORTED.
 #include "k_fft.cuh"
 #include <math.h>
 #include <mutex>
@@ -45,6 +53,7 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 std::mutex g_mu;
+std::mutex g_ymu;
 void *g_base[kMaxDevices];
 
 int setup_device(int dev, unsigned char **base) {
@@ -80,17 +89,72 @@ int plan_radices(int n, int *rad, int *nst) {
     return 0;
 }
 
+
+// The wall-normal tables of the solve, passed by value as kernel parameters:
+// f2fyi(0:n2+1), c2cyi(0:n2+1) and jpv, fixjl, fixju over 0..n2m+1 (the
+// unused ends zero), at most kMaxDir cells.  About 20.6 KB, below the 32 KB
+// kernel-parameter limit of CUDA 12.1 and later.
+struct YTables {
+    double f2fyi[kMaxDir + 3], c2cyi[kMaxDir + 3];
+    short jpv[kMaxDir + 2];
+    unsigned char fixjl[kMaxDir + 2], fixju[kMaxDir + 2];
+};
+
+struct TableDst {
+    double *ak1, *ak3, *f2fyi, *c2cyi;
+    int *jpv, *fixjl, *fixju;
+    double2 *twx, *twz;
+};
+
+// poisinit of poiss_ftft.f90:164-204 on the device: the modified wavenumbers
+// ak1 = 2 (1 - cos(2 pi (i-1) / n1m)) / dx^2 (mirrored above n1mh) and
+// ak3 likewise over z, the twiddles exp(-2 pi i e / n) of both transforms,
+// and the y tables copied out of the parameter block.
+__global__ void k_noalloc_tables(YTables y, TableDst d, int n1m, int n2m, int n3m, double sdxis, double sdzis) {
+    const int n1mh = n1m / 2 + 1, n3mh = n3m / 2 + 1, n2 = n2m + 1;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < kMaxDir + 3; t += gridDim.x * blockDim.x) {
+        if (t <= n1m + 2) {
+            double v = 0.0;
+            const int i = (t >= n1mh + 1 && t <= n1m) ? n1m + 2 - t : t;
+            if (t >= 1 && t <= n1m) v = 2.0 * (1.0 - cospi(2.0 * (double)(i - 1) / (double)n1m)) * sdxis * sdxis;
+            d.ak1[t] = v;
+        }
+        if (t <= n3mh + 1)
+            d.ak3[t] = (t >= 1 && t <= n3mh) ? 2.0 * (1.0 - cospi(2.0 * (double)(t - 1) / (double)n3m)) * sdzis * sdzis : 0.0;
+        if (t <= n2 + 1) { d.f2fyi[t] = y.f2fyi[t]; d.c2cyi[t] = y.c2cyi[t]; }
+        if (t <= n2m + 1) { d.jpv[t] = y.jpv[t]; d.fixjl[t] = y.fixjl[t]; d.fixju[t] = y.fixju[t]; }
+        double s, c;
+        if (t < n1m) { sincospi(-2.0 * (double)t / (double)n1m, &s, &c); d.twx[t] = make_double2(c, s); }
+        if (t < n3m) { sincospi(-2.0 * (double)t / (double)n3m, &s, &c); d.twz[t] = make_double2(c, s); }
+    }
+}
+
+// x and z must wrap (ipv(n1m) = 1, kpv(n3m) = 1) and be uniform: every 1/dx
+// within 1e-6 relative of the first, which the transforms use throughout.
+bool periodic_uniform(const int64_t *pv, const double *fi, int nm) {
+    if (pv[nm - 1] != 1) return false;
+    const double f1 = fi[1];
+    if (!(f1 > 0.0)) return false;
+    for (int i = 1; i <= nm; i++)
+        if (!(fabs(fi[i] - f1) <= 1e-6 * f1)) return false;
+    return true;
+}
+
 }  // namespace
 
 // See include/lesgpu.h.  Enqueues the solve on `stream` and returns; the
 // caller synchronises before reading phi.
 extern "C" int lesgpu_poisson_ftft_noalloc(const lesgpu_grid *g, const double *d_divgsum, double *d_phi, void *stream) {
     if (!g || !d_divgsum || !d_phi) return LESGPU_ERR_ARG;
+    if (!g->ipv || !g->kpv || !g->jpv || !g->fixjl || !g->fixju || !g->f2fxi || !g->f2fzi || !g->f2fyi || !g->c2cyi)
+        return LESGPU_ERR_ARG;
     if (g->n1 != g->n1m + 1 || g->n2 != g->n2m + 1 || g->n3 != g->n3m + 1) return LESGPU_ERR_ARG;
     if (g->n1m < 1 || g->n2m < 2 || g->n3m < 1) return LESGPU_ERR_ARG;
     if (g->n1m > kMaxDir || g->n2m > kMaxDir || g->n3m > kMaxDir) return LESGPU_ERR_TOO_LARGE;
     const int n1m = (int)g->n1m, n2m = (int)g->n2m, n3m = (int)g->n3m;
     const int n1 = n1m + 1, n2 = n2m + 1, n3mh = n3m / 2 + 1, n1mh = n1m / 2 + 1;
+    if (!periodic_uniform(g->ipv, g->f2fxi, n1m) || !periodic_uniform(g->kpv, g->f2fzi, n3m))
+        return LESGPU_ERR_UNSUPPORTED;
     lg::DevPlan px{}, pz{};
     if (plan_radices(n1m, px.rad, &px.nst) || plan_radices(n3m, pz.rad, &pz.nst)) return LESGPU_ERR_UNSUPPORTED;
     px.n = n1m;
@@ -112,6 +176,9 @@ extern "C" int lesgpu_poisson_ftft_noalloc(const lesgpu_grid *g, const double *d
     const size_t o_gam = off; off = align256(off + sizeof(double) * nspec);
     if (off > kNoAllocScratchBytes) return LESGPU_ERR_TOO_LARGE;
 
+    // an error left pending by the caller's earlier work is theirs: return
+    // without touching it rather than blame (and clear) it here
+    if (cudaPeekAtLastError() != cudaSuccess) return LESGPU_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return LESGPU_ERR_CUDA;
     unsigned char *base = nullptr;
@@ -119,64 +186,49 @@ extern "C" int lesgpu_poisson_ftft_noalloc(const lesgpu_grid *g, const double *d
     if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
 
-    // host tables (stack, bounded by kMaxDir): poisinit of poiss_ftft.f90:164-204
-    double ak1[kMaxDir + 2], ak3[kMaxDir / 2 + 3], f2fyi[kMaxDir + 3], c2cyi[kMaxDir + 3];
-    int jpv[kMaxDir + 2], fixjl[kMaxDir + 2], fixju[kMaxDir + 2];
-    double2 twx[kMaxDir], twz[kMaxDir];
-    memset(ak1, 0, sizeof(ak1));
-    memset(ak3, 0, sizeof(ak3));
-    const double pi = 2.0 * asin(1.0);
-    const double sdzis = g->f2fzi[1], sdxis = g->f2fxi[1];
-    for (int k = 1; k <= n3mh; k++) {
-        double ai = (k == 1) ? 0.0 : (double)(k - 1) * 2.0 * pi;
-        ak3[k] = 2.0 * (1.0 - cos(ai / (double)n3m)) * sdzis * sdzis;
+    // the wall-normal tables go to the device as kernel parameters (static:
+    // the block is too large for a small thread stack; guarded by g_ymu until
+    // the launch has copied it)
+    static YTables y;
+    std::lock_guard<std::mutex> lk(g_ymu);
+    memset(&y, 0, sizeof(y));
+    for (int j = 0; j <= n2; j++) { y.f2fyi[j] = g->f2fyi[j]; y.c2cyi[j] = g->c2cyi[j]; }
+    for (int j = 1; j <= n2m; j++) {
+        y.jpv[j] = (short)g->jpv[j - 1];
+        y.fixjl[j] = (unsigned char)(g->fixjl[j - 1] != 0);
+        y.fixju[j] = (unsigned char)(g->fixju[j - 1] != 0);
     }
-    for (int i = 1; i <= n1mh; i++) {
-        double ai = (i == 1) ? 0.0 : (double)(i - 1) * 2.0 * pi;
-        ak1[i] = 2.0 * (1.0 - cos(ai / (double)n1m)) * sdxis * sdxis;
-    }
-    for (int i = n1m; i >= n1mh + 1; i--) ak1[i] = ak1[n1m + 2 - i];
-    for (int j = 0; j <= n2; j++) { f2fyi[j] = g->f2fyi[j]; c2cyi[j] = g->c2cyi[j]; }
-    f2fyi[n2 + 1] = c2cyi[n2 + 1] = 0.0;
-    jpv[0] = fixjl[0] = fixju[0] = 0;
-    for (int j = 1; j <= n2m; j++) { jpv[j] = (int)g->jpv[j - 1]; fixjl[j] = (int)g->fixjl[j - 1]; fixju[j] = (int)g->fixju[j - 1]; }
-    jpv[n2m + 1] = fixjl[n2m + 1] = fixju[n2m + 1] = 0;
-    for (int e = 0; e < n1m; e++) {
-        long double a = -2.0L * 3.14159265358979323846264338327950288L * (long double)e / (long double)n1m;
-        twx[e] = make_double2((double)cosl(a), (double)sinl(a));
-    }
-    for (int e = 0; e < n3m; e++) {
-        long double a = -2.0L * 3.14159265358979323846264338327950288L * (long double)e / (long double)n3m;
-        twz[e] = make_double2((double)cosl(a), (double)sinl(a));
-    }
-    struct { size_t o; const void *h; size_t b; } cp[] = {
-        {o_ak1, ak1, sizeof(double) * (n1 + 2)}, {o_ak3, ak3, sizeof(double) * (n3mh + 2)},
-        {o_f2fyi, f2fyi, sizeof(double) * (n2 + 2)}, {o_c2cyi, c2cyi, sizeof(double) * (n2 + 2)},
-        {o_jpv, jpv, sizeof(int) * (n2m + 2)}, {o_fixjl, fixjl, sizeof(int) * (n2m + 2)},
-        {o_fixju, fixju, sizeof(int) * (n2m + 2)}, {o_twx, twx, sizeof(double2) * n1m}, {o_twz, twz, sizeof(double2) * n3m}};
-    // pageable sources: each copy returns once its source has been staged
-    for (auto &c : cp)
-        if (cudaMemcpyAsync(base + c.o, c.h, c.b, cudaMemcpyHostToDevice, st) != cudaSuccess) return LESGPU_ERR_CUDA;
+
+    TableDst d;
+    d.ak1 = (double *)(base + o_ak1);
+    d.ak3 = (double *)(base + o_ak3);
+    d.f2fyi = (double *)(base + o_f2fyi);
+    d.c2cyi = (double *)(base + o_c2cyi);
+    d.jpv = (int *)(base + o_jpv);
+    d.fixjl = (int *)(base + o_fixjl);
+    d.fixju = (int *)(base + o_fixju);
+    d.twx = (double2 *)(base + o_twx);
+    d.twz = (double2 *)(base + o_twz);
+    k_noalloc_tables<<<(kMaxDir + 3 + 255) / 256, 256, 0, st>>>(y, d, n1m, n2m, n3m, g->f2fxi[1], g->f2fzi[1]);
 
     lg::KP p;
     memset(&p, 0, sizeof(p));
     p.g.n1 = n1; p.g.n2 = n2; p.g.n3 = n3m + 1;
     p.g.n1m = n1m; p.g.n2m = n2m; p.g.n3m = n3m; p.g.n1mh = n1mh; p.g.n3mh = n3mh;
     p.g.sx = n1 + 1; p.g.sxy = p.g.sx * (n2 + 1); p.g.nt = p.g.sxy * (n3m + 2);
-    p.g.f2fyi = (const double *)(base + o_f2fyi);
-    p.g.c2cyi = (const double *)(base + o_c2cyi);
-    p.g.jpv = (const int *)(base + o_jpv);
-    p.g.fixjl = (const int *)(base + o_fixjl);
-    p.g.fixju = (const int *)(base + o_fixju);
+    p.g.f2fyi = d.f2fyi;
+    p.g.c2cyi = d.c2cyi;
+    p.g.jpv = d.jpv;
+    p.g.fixjl = d.fixjl;
+    p.g.fixju = d.fixju;
     p.f.divgsum = (double *)d_divgsum;
     p.f.phi = d_phi;
-    px.tw = (const double2 *)(base + o_twx);
-    pz.tw = (const double2 *)(base + o_twz);
+    px.tw = d.twx;
+    pz.tw = d.twz;
     px.twf = nullptr;   // FP64 transforms only
     pz.twf = nullptr;
     double2 *ccap = (double2 *)(base + o_ccap);
     double *gam = (double *)(base + o_gam);
-    const double *dak1 = (const double *)(base + o_ak1), *dak3 = (const double *)(base + o_ak3);
 
     // the same launch sequence as the case-based solve (k_fft.cu launch_poisson)
     int Lz = lg::fft_lines_per_block(n3m), Lx = lg::fft_lines_per_block(n1m);
@@ -187,8 +239,9 @@ extern "C" int lesgpu_poisson_ftft_noalloc(const lesgpu_grid *g, const double *d
     lg::fft_z_fwd64(gz, smz, st, p, p.f.divgsum, ccap, pz, Lz, sk, sj);
     lg::fft_x64((nxl + Lx - 1) / Lx, smx, st, ccap, nxl, px, Lx, 0);
     long long nl = (long long)n1m * n3mh;
-    lg::k_ytri_elim<<<lg::blocks_for(nl, 128), 128, 0, st>>>(p, ccap, dak1, dak3, gam);
+    lg::k_ytri_elim<<<lg::blocks_for(nl, 128), 128, 0, st>>>(p, ccap, d.ak1, d.ak3, gam);
     lg::fft_x64((nxl + Lx - 1) / Lx, smx, st, ccap, nxl, px, Lx, 1);
     lg::fft_z_inv64(gz, smz, st, p, ccap, pz, Lz, sk, sj);
-    return cudaGetLastError() == cudaSuccess ? 0 : LESGPU_ERR_CUDA;
+    // a launch that failed leaves its error pending; report it, leave it for the caller to see
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : LESGPU_ERR_CUDA;
 }

@@ -501,10 +501,17 @@ void combine_favs(const lesgpu_config &c, const Grid &g) {
     write_fav(c, g, sum, t0, t1, h0, h1, true);
 }
 
+// settings.input's tracking points (readsettings, misc_init.f90:53-59)
+struct Trace {
+    int64_t ntrace = 0, ntr = 0;
+    std::vector<int64_t> pts;   // i, j, k of each point
+};
+
 // --dry-run: every value the readers produced, one "name value" per line
 // (integers as integers, reals with 17 significant digits, arrays as their
 // length and plain sum).
-void dump_inputs(const lesgpu_config &c, const Grid &g, const Tables &t, const State &s) {
+void dump_inputs(const lesgpu_config &c, const Grid &g, const Tables &t, const State &s, const Trace &tr,
+                 const std::string &gridfile, const std::string &prev_fld) {
 #define I_(f) printf(#f " %lld\n", (long long)c.f)
 #define D_(f) printf(#f " %.17g\n", c.f)
     D_(re); D_(pr); D_(gr); I_(grdir); D_(tflu_i); D_(tsol_i);
@@ -532,6 +539,10 @@ void dump_inputs(const lesgpu_config &c, const Grid &g, const Tables &t, const S
     printf("nwall %zu %lld\ncstar %zu %.17g\nkstar %zu %.17g\n", t.nwall.size(), isum(t.nwall), t.cstar.size(),
            dsum(t.cstar), t.kstar.size(), dsum(t.kstar));
     printf("state %lld %lld %.17g %.17g\n", (long long)s.ihist, (long long)s.m, s.time, s.dt);
+    printf("gridfile %s\nprev_fld %s\n", gridfile.c_str(), prev_fld.c_str());
+    printf("trace %lld %lld", (long long)tr.ntrace, (long long)tr.ntr);
+    for (int64_t v : tr.pts) printf(" %lld", (long long)v);
+    printf("\n");
     printf("fields %.17g %.17g %.17g %.17g %.17g\n", dsum(s.u), dsum(s.v), dsum(s.w), dsum(s.p), dsum(s.t));
 }
 
@@ -548,10 +559,11 @@ int main(int argc, char **argv) {
     if (!dry_run)
         for (const char *d : {"../output", "../output/field", "../output/ftr", "../output/field_avg"}) mkdir(d, 0755);
 
-    // ---- readsettings, misc_init.f90:271-301
+    // ---- readsettings, misc_init.f90:19-92
     lesgpu_config c;
     memset(&c, 0, sizeof(c));
     std::string gridfile, prev_fld;
+    Trace trace;
     {
         ListReader r("settings.input");
         r.skip();
@@ -583,8 +595,18 @@ int main(int argc, char **argv) {
         r.skip();
         gridfile = r.items(1)[0];
         prev_fld = r.items(1)[0];
+        // TRACE NTR and the tracking points (the tracer histories themselves
+        // are not written); rows after the last point are not read
+        r.skip();
+        v = r.items(2);
+        trace.ntrace = to_i(v[0]);
+        trace.ntr = to_i(v[1]);
+        for (int64_t n = 0; n < trace.ntrace; n++) {
+            v = r.items(3);
+            for (int q = 0; q < 3; q++) trace.pts.push_back(to_i(v[q]));
+        }
     }
-    // ---- readbcs, misc_init.f90:95-160
+    // ---- readbcs, misc_init.f90:95-158
     {
         ListReader r("boundary.input");
         r.skip();
@@ -630,7 +652,7 @@ int main(int argc, char **argv) {
     }
     if (c.ireset == 1) { s.ihist = 0; s.time = 0.0; }
     if (dry_run) {            // what was read, for checking the readers without a GPU
-        dump_inputs(c, g, t, s);
+        dump_inputs(c, g, t, s, trace, gridfile, prev_fld);
         return 0;
     }
     check(lesgpu_set_device(device), "set_device");

@@ -1,7 +1,7 @@
 """The reference's on-disk formats, for cases built here.
 
 * settings.input / boundary.input (read by readsettings / readbcs,
-  misc_init.f90:271-160): a header line, then a line of values, per group;
+  misc_init.f90:19-92 and :95-158): a header line, then a line of values, per group;
 * output/grid/grid.bin: the text file of gridgen.grid_bin_text;
 * output/ibmpre/*.bin: the text tables of the pre-processor
   (lib_preprocessing.py:172-345): ibmpre_prdic, ibmpre_fcpts(_t),
@@ -126,6 +126,33 @@ def read_fav(path: str, ihtrans: int) -> Dict:
     return out
 
 
+FAV_NAMES = ["uavg", "vavg", "wavg", "uiujavg", "pavg", "p2avg", "voravg", "vor2avg", "ssavg", "tavg", "t2avg"]
+FAV_COUNTS = [1, 1, 1, 6, 1, 1, 3, 6, 1, 1, 1]
+
+
+def write_fav(path: str, re: float, n: Sequence[int], sums: np.ndarray, timeinit: float, timeend: float,
+              ihistinit: int, ihistend: int, ihtrans: int) -> None:
+    """A fav file as field_avg writes it (misc_hist.f90:468-490) and the
+    compiled driver's write_fav writes it: (n1m, n2m, n3m, re), the window
+    (timeinit, timeend, ihistinit, ihistend as reals), then the dt-weighted
+    sums, one record per group (u, v, w, uiuj(6), p, p2, vor(3), vorvor(6),
+    ss, and t, t2 with heat transfer).  `sums` holds the LESGPU_NAVG (or
+    LESGPU_NAVG - 2) arrays of n1m*n2m*n3m values in that order, i fastest."""
+    n1m, n2m, n3m = (int(x) for x in n)
+    ncell = n1m * n2m * n3m
+    a = np.ascontiguousarray(sums, dtype="<f8").reshape(-1)
+    ng = 11 if ihtrans == 1 else 9
+    recs = [_i8(n1m, n2m, n3m) + _f8(re), _f8(timeinit, timeend, float(ihistinit), float(ihistend))]
+    a0 = 0
+    for q in range(ng):
+        c = FAV_COUNTS[q]
+        recs.append(a[a0 * ncell:(a0 + c) * ncell].tobytes())
+        a0 += c
+    if a0 * ncell != a.size:
+        raise ValueError("fav sums do not match the grid and ihtrans")
+    write_records(path, recs)
+
+
 # ---------------------------------------------------------- text inputs
 def _fmt(v) -> str:
     if isinstance(v, (int, np.integer)):
@@ -134,7 +161,7 @@ def _fmt(v) -> str:
 
 
 def settings_text(s: Dict, gridfile: str, prev_fld: str) -> str:
-    """settings.input in the layout readsettings reads (misc_init.f90:276-301)."""
+    """settings.input in the layout readsettings reads (misc_init.f90:19-92)."""
     rows = [
         ("RE#     PR#     GR#     GRDIR   TFLU_I  TSOL_I", ["re", "pr", "gr", "grdir", "tflu_i", "tsol_i"]),
         ("IRESET  IREAD   IAVG    IPZERO  EPS_PTR UDRV_I", ["ireset", "iread", "iavg", "ipzero", "eps_ptr", "udrv_i"]),
@@ -157,7 +184,7 @@ def settings_text(s: Dict, gridfile: str, prev_fld: str) -> str:
 
 
 def boundary_text(s: Dict) -> str:
-    """boundary.input in the layout readbcs reads (misc_init.f90:101-115).
+    """boundary.input in the layout readbcs reads (misc_init.f90:95-158).
     A periodic direction is written as a wall; readbcs overrides it."""
     def bc(k, prd):
         return 0 if s.get(prd, 0) == 1 else int(s[k])

@@ -45,6 +45,13 @@ def check_field(path, c, fields, rep, ihtrans):
     for k, q in sl.items():
         assert np.array_equal(r[k][q], fields[k][q]), (path, k)
     assert (r["m"], r["time"], r["dt"]) == (rep["m"], rep["time"], rep["dt"])
+    # byte for byte the file fileio.write_field makes, whose layout the
+    # reference's post-processor reads (tests/test_reference_io.py)
+    want = path + ".want"
+    fileio.write_field(want, c.settings, g, fields, r["ihist"], rep["m"], rep["time"], rep["dt"])
+    with open(path, "rb") as a, open(want, "rb") as b:
+        assert a.read() == b.read(), path
+    os.unlink(want)
 
 
 def lines(path):
@@ -92,6 +99,14 @@ def test_exec_channel_fields_history_and_averages(tmp_path):
         f = fileio.read_fav(os.path.join(root, "output", "field_avg", name), 1)
         assert np.array_equal(f["uavg"], want["uavg"]) and np.array_equal(f["t2avg"], want["t2avg"])
         assert np.array_equal(f["vor2avg"][5], want["wzwz"]) and np.array_equal(f["uiujavg"][1], want["uv"])
+        # byte for byte the file fileio.write_fav makes from the same sums
+        fpath = os.path.join(root, "output", "field_avg", name)
+        sums = np.concatenate([want[nm].ravel() for nm in abi.AVG_NAMES])
+        wpath = os.path.join(root, name + ".want")
+        fileio.write_fav(wpath, c.settings["re"], f["n"], sums, f["timeinit"], f["timeend"],
+                         int(f["ihistinit"]), int(f["ihistend"]), 1)
+        with open(fpath, "rb") as a, open(wpath, "rb") as b:
+            assert a.read() == b.read(), name
     comb = fileio.read_fav(os.path.join(root, "output", "field_avg", "combined", "fav0000001-0000006"), 1)
     assert np.array_equal(comb["ssavg"], avgs[0]["ssavg"] + avgs[1]["ssavg"])
     assert comb["timeinit"] == 0.0 and comb["timeend"] == reps[-1]["time"]
