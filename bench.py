@@ -3,9 +3,11 @@
 
 Metric: Mcell-steps/s = n1m*n2m*n3m*steps / seconds / 1e6, one step being the
 three RK3 substeps with SGS, momentum RHS + ADI, Poisson, projection,
-temperature and the per-step checks.  Workload (default): the turbulent
-channel at Re_tau ~ 180 with passive heat transfer, 64x64x64 cells, seeded
-synthetic initial field (laminar profile + 10% uniform perturbation).
+temperature and the per-step checks.  Workload (default, `--config
+channel590`): the turbulent channel at Re_tau ~ 590 with passive heat
+transfer, 2pi x 2 x pi, 384x256x384 cells (37.7M), seeded synthetic initial
+field (laminar profile + 10% uniform perturbation) -- the largest of the
+benchmark's configurations that runs on one GPU.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -28,16 +30,27 @@ Our arm (one JSON line on rank 0):
   roofline : the dominant kernel class (largest device time in the
              instrumented steps), its algorithmic bytes per launch divided by
              its average launch time (events on the launching stream), against
-             the measured HBM copy bandwidth.
+             the measured HBM copy bandwidth.  Algorithmic bytes: each distinct
+             operand read once and each result written once, at the width it
+             is stored in (FP32 mirrors, histories and SGS temporaries of the
+             mixed form at 4 B, FP64 state at 8 B); `step_roofline` is the
+             whole step against the per-phase model of the hot path (289 FP64
+             words per cell-step for the channel, with the same precision map
+             for the mixed form); `traffic` is the dominant class's measured
+             DRAM bytes per launch from the committed ncu summary
+             (profiles/roofline_traffic.md) when it holds the workload.
   serving  : a bounded sample of the serving stream through lesgpu_server
              (mixed form, cases admitted and advanced concurrently): p50/p99
              time-to-solution and aggregate Mcell-steps/s, beside the same
              cases run one at a time in the FP64 form.
   cpu_baseline : the CPU oracle (C/OpenMP restatement of the solver, the
              reference's Fortran cannot be built on this host) on a bounded
-             sample of the same workload, all host threads.
+             sample of the same workload with OMP threads set to every host
+             core (stated in `cores`), and `single_thread`: the same oracle
+             with one thread on a bounded sample (one step of the 64^3
+             channel).
 Reference arm (--impl reference): the same CPU restatement timed on the same
-config with all host threads; rank 0 alone runs under torchrun.
+config with every host core; rank 0 alone runs under torchrun.
 
 Multi-GPU: replicas only (one independent case per GPU, no collective on the
 data path); value = all ranks' cell-steps / max over ranks of the time.
@@ -61,22 +74,123 @@ sys.path.insert(0, ROOT)
 METRIC = "Mcell-steps/s (mixed vs FP64 GPU) at stated error; p50/p99 served-case latency"
 UNIT = "Mcell-steps/s"
 
-# Algorithmic FP64 words per cell of one launch of each kernel class
-# (each distinct input read once, each output written once).
-#   RHS   : read u,v,w,p,nu,nu1(3),rk3o(3); write rhs1(3),rk3o(3),rk3oo(3)   -> 20 w
-#   ADI   : one sweep of one component: z and y read rhs + a coefficient
-#           field and write the result (3 w); x also reads and writes the
-#           field (4 w); mean over the three directions                     -> 10/3 w
-#   POISSON : whole FFT/Thomas solve (div in, phi out, spectrum round trips) -> 6 w
-#             poiss_z_ft: 4 w + 14 w per V-cycle; poiss_mgrd: 2 w + 44 w per
-#             BiCGSTAB iteration (two V-cycles, two operator applications,
-#             the vector updates)
-#   SGS   : one batched test-filter launch of m arrays: read m, write m      -> 2m w
-#   RHS_T : read t,u,v,w,al1(3),rk3to; write rhs,rk3to,rk3too               -> 11 w
-#           (the conjugate tables c*, k*(6), omega, 8 w more, are read only
-#           when ICONJG = 1 with a table value other than 1: no bench case)
 KCLASS = {1: "rhs", 2: "adi", 3: "sgs_filter", 4: "poisson", 5: "rhs_t"}
-KWORDS = {1: 20.0, 2: 10.0 / 3.0, 4: 6.0, 5: 11.0}
+
+
+def poisson_words(case, rep):
+    """FP64 words per cell of one Poisson solve: poiss_ftft 6 (divgsum in,
+    phi out, the half spectrum's round trips between the z and x passes);
+    poiss_z_ft / poiss_x_ft 4 + 14 per V-cycle (mean over the step's
+    substeps); poiss_mgrd 2 + 44 per BiCGSTAB iteration (two V-cycles, two
+    operator applications, the vector updates)."""
+    from leswht_gb300 import abi
+    its = [x for x in rep["poisson_iters"] if x > 0] or [0]
+    nbar = sum(its) / len(its)
+    pk = case.settings.get("poisson", abi.POISSON_FTFT)
+    if pk in (abi.POISSON_Z_FT, abi.POISSON_X_FT):
+        return 4.0 + 14.0 * nbar, nbar
+    if pk == abi.POISSON_MGRD:
+        return 2.0 + 44.0 * nbar, nbar
+    return 6.0, 0.0
+
+
+def poisson_bytes(case, form, rep):
+    """Bytes per cell of one Poisson solve: poisson_words at 8 B, except that
+    the mixed form's multigrid cycles (poiss_z_ft / poiss_x_ft), which relax
+    and transfer the correction in FP32, count 4 B per cycle word."""
+    from leswht_gb300 import abi
+    w, nbar = poisson_words(case, rep)
+    if form == "mixed" and case.settings.get("poisson") in (abi.POISSON_Z_FT, abi.POISSON_X_FT):
+        return 4.0 * 8 + 14.0 * nbar * 4
+    return w * 8
+
+
+def class_bytes(case, form, rep):
+    """Algorithmic bytes per cell and per step of each instrumented kernel
+    class: every distinct operand read once and every result written once,
+    at the width it is stored in.  The FP64 form stores everything in 8 B;
+    the mixed form reads FP32 mirrors of the fields and eddy viscosities,
+    keeps its RK3 histories and SGS temporaries in FP32 (4 B), and keeps the
+    right-hand sides, the fields and the wall-normal sweep's operands in FP64.
+      rhs    : read u,v,w,p [nu, nu1(3)], rk3o(3); write rhs(3) (FP64),
+               rk3o(3), rk3oo(3)                         3 launches a step
+      adi    : per component: z reads and writes rhs (FP64) and reads its
+               viscosity; y reads rhs, its viscosity (FP64) and writes the
+               intermediate (FP64); x reads the intermediate and its
+               viscosity and adds to the field (FP64 read + write); the
+               x and z sweeps run in FP32 in the mixed form
+      sgs_filter : 24 (Vreman) + 19 (EDM) test-filtered temporaries, each
+               read and written once                      once a step
+      poisson : poisson_bytes                            3 solves a step
+      rhs_t  : read t,u,v,w [al1(3)], rk3to; write rhs (FP64), rk3to, rk3too"""
+    s = case.settings
+    f = 4 if form == "mixed" else 8
+    les = s.get("iles", 0) == 1
+    ht = s.get("ihtrans", 0) == 1
+    dyn = s.get("idvmon", 0) == 1
+    nc = 3 if case.grid.n3m != 1 else 2
+    nvx = f if les else 0          # viscosity of an x or z sweep
+    nvy = 8 if les else 0          # of the FP64 wall-normal sweep
+    out = {}
+    out["rhs"] = 3 * ((4 + (4 if les else 0) + 3) * f + 3 * 8 + 6 * f)
+    per_comp = (16 + nvx) + (16 + nvy) + (24 + nvx)
+    out["adi"] = 3 * (nc + (1 if ht else 0)) * per_comp
+    nf = (24 if les and dyn else 0) + (19 if les and dyn and ht else 0)
+    out["sgs_filter"] = nf * 2 * f
+    out["poisson"] = 3 * poisson_bytes(case, form, rep)
+    out["rhs_t"] = 3 * ((4 + (3 if les else 0) + 1) * f + 8 + 2 * f) if ht else 0
+    return out
+
+
+def step_bytes(case, form, rep):
+    """Bytes per cell-step of the whole step by the per-phase minimum-traffic
+    model of the hot path: in FP64 words, per substep RHS + SGS cross terms
+    17 (+3 rk3oo with IB), ADI 8 per momentum component, divergence 4,
+    Poisson (poisson_words), projection 11, flow-rate scalars 5 (ICH = 1;
+    else the CFL pass, 1), rhs_t 12, temperature ADI 8, tvolcalc 3 (ICH = 1);
+    per step the SGS model 19 (9 momentum + 10 thermal); plus per IB forcing
+    point and component 87 words a substep.  For the channel this is 289
+    words (2312 B) per cell-step.  The mixed form's FP32-stored operands
+    (field mirrors read by the FP32 stencils and x/z sweeps, RK3 histories,
+    SGS velocities) count 4 B; everything else 8 B."""
+    from leswht_gb300 import abi
+    s = case.settings
+    f = 4 if form == "mixed" else 8
+    ib = s.get("ibmon", 0) == 1
+    ht = s.get("ihtrans", 0) == 1
+    ich = s.get("ich", 0) == 1
+    nc = 3 if case.grid.n3m != 1 else 2
+    rhs = 11 * f + 3 * 8 + 3 * f + (3 * f if ib else 0)
+    adi = nc * (48 + 2 * f)
+    sub = rhs + adi + 4 * 8 + poisson_bytes(case, form, rep) + 11 * 8 + (5 if ich else 1) * 8
+    if ht:
+        sub += 9 * f + 8 + 2 * f + (48 + 2 * f) + (3 * 8 if ich else 0)
+    step = 3 * sub + (3 * f + 48) + ((4 * f + 48) if ht else 0)
+    if ib and case.ibm is not None:
+        nint = sum(int(case.ibm["nintp"][l]) for l in range(4 if ht else 3))
+        nin = sum(int(case.ibm["nbody"][l]) - int(case.ibm["nintp"][l]) for l in range(4 if ht else 3))
+        step += 3 * (87 * nint + 3 * nin) * 8 / case.cells
+    return step
+
+
+def load_traffic(config, form):
+    """Measured DRAM bytes (read + write) per cell and per step of each kernel
+    class, from the ncu summary profiles/roofline_traffic.md (rows
+    `| config | form | class | bytes per cell-step | ...`), or {}."""
+    out = {}
+    path = os.path.join(ROOT, "profiles", "roofline_traffic.md")
+    try:
+        with open(path) as fh:
+            for line in fh:
+                cols = [x.strip() for x in line.strip().strip("|").split("|")]
+                if len(cols) >= 4 and cols[0] == config and cols[1] == form:
+                    try:
+                        out[cols[2]] = float(cols[3])
+                    except ValueError:
+                        pass
+    except OSError:
+        pass
+    return out
 
 
 def peaks():
@@ -184,53 +298,75 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
-def cpu_baseline(name, form, seconds=12.0):
-    """The oracle on the host cores: a bounded sample of the same workload."""
+def host_threads():
+    """Host cores this process may use (the OpenMP thread count of the CPU legs)."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def oracle_steps(name, threads, seconds=None, warmup=1, steps=None):
+    """The oracle on `threads` OpenMP threads: `warmup` untimed steps, then
+    `steps` timed steps (or as many as fit in `seconds`, at least one)."""
     import oracle
     from leswht_gb300 import solver
-    case = make_case(name, form)
+    case = make_case(name, "fp64")
     lib = oracle.load()
+    lib.ref_set_threads(int(threads))
+    if lib.ref_get_threads() != int(threads):
+        raise RuntimeError("could not set the oracle's thread count")
     s = solver.Solver(lib, "ref_", case)
-    s.step()                                   # warm-up (page-in, first touch)
+    for _ in range(warmup):
+        s.step()                               # page-in, first touch
     n, t0 = 0, time.perf_counter()
     while True:
         s.step()
         n += 1
         el = time.perf_counter() - t0
-        if el >= seconds or n >= 200:
+        if steps is not None:
+            if n >= steps:
+                break
+        elif el >= seconds or n >= 200:
             break
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"value": case.cells * n / el / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{n} steps of {case.name} after 1 warm-up step ({el:.1f} s), C/OpenMP oracle",
-            "steps": n, "seconds": el}
+    s.close()
+    return case, n, el
+
+
+def cpu_baseline(name, seconds=12.0):
+    """The oracle on the host cores: a bounded sample of the same workload on
+    every core, and one step of the 64^3 channel on one core."""
+    threads = host_threads()
+    case, n, el = oracle_steps(name, threads, seconds=seconds)
+    out = {"value": case.cells * n / el / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{n} steps of {case.name} after 1 warm-up step ({el:.1f} s), C/OpenMP oracle, "
+                     f"OMP threads = {threads}",
+           "steps": n, "seconds": el}
+    c1, n1, e1 = oracle_steps("channel64", 1, steps=1)
+    out["single_thread"] = {"value": c1.cells * n1 / e1 / 1e6, "unit": UNIT, "cores": 1,
+                            "sample": f"{n1} step of {c1.name} after 1 warm-up step ({e1:.1f} s), OMP threads = 1"}
+    c2, n2, e2 = oracle_steps("channel64", threads, steps=2)
+    out["single_thread"]["same_sample_all_cores"] = c2.cells * n2 / e2 / 1e6
+    return out
 
 
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    import oracle
-    from leswht_gb300 import solver
-    case = make_case(args.config, "fp64")
-    lib = oracle.load()
-    s = solver.Solver(lib, "ref_", case)
-    for _ in range(args.warmup):
-        s.step()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        s.step()
-    el = time.perf_counter() - t0
+    threads = host_threads()
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    case, n, el = oracle_steps(args.config, threads, warmup=args.warmup, steps=args.steps)
     v = case.cells * args.steps / el / 1e6
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    sample = (f"{args.steps} timed steps of {case.name} after {args.warmup} warm-up, C/OpenMP restatement of "
+              f"the reference solver on {threads} OMP threads (the Fortran reference cannot be compiled: no "
+              "Fortran compiler on the host)")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded PCG64 perturbation of the laminar profile)",
             "config": {"workload": WORKLOAD[args.config], "cells": case.cells, "form": "fp64 CPU"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} timed steps of {case.name} after {args.warmup} warm-up, "
-                                       "C/OpenMP restatement of the reference solver (the Fortran reference "
-                                       "cannot be compiled: no Fortran compiler on the host)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -300,38 +436,41 @@ def time_form(args, form, lib, dev, world, rank, flush, full):
 
     # ---- live per-kernel-class timing (instrumented eager steps)
     kstats = {}
-    for cls in (1, 2, 4, 5):
+    nins = max(2, min(args.steps, 5))
+    for cls in (1, 2, 3, 4, 5):
         check(lib.lesgpu_instrument(h, cls), "instrument")
         with torch.cuda.stream(stream):
-            for q in range(max(2, min(args.steps, 5))):
+            for q in range(nins):
                 flush.zero_()
                 check(lib.lesgpu_step_async(h, 1), "step")
         ms, n = C.c_double(), C.c_int64()
         check(lib.lesgpu_instrument_read(h, C.byref(ms), C.byref(n)), "instrument_read")
-        kstats[KCLASS[cls]] = {"ms_total": ms.value, "launches": n.value,
-                               "avg_us": ms.value / max(n.value, 1) * 1e3, "cls": cls}
+        if n.value > 0:
+            kstats[KCLASS[cls]] = {"ms_total": ms.value, "launches": n.value,
+                                   "avg_us": ms.value / n.value * 1e3, "cls": cls,
+                                   "launches_per_step": n.value / nins}
     check(lib.lesgpu_instrument(h, 0), "instrument")
-    kwords = dict(KWORDS)
-    if case.settings.get("poisson") == abi.POISSON_Z_FT:
-        # z FFT in/out 4 w + 14 w per multigrid V-cycle (mean over the substeps)
-        its = [x for x in rep["poisson_iters"] if x > 0] or [0]
-        kwords[4] = 4.0 + 14.0 * sum(its) / len(its)
-    elif case.settings.get("poisson") == abi.POISSON_MGRD:
-        its = [x for x in rep["poisson_iters"] if x > 0] or [0]
-        kwords[4] = 2.0 + 44.0 * sum(its) / len(its)
     peak, src = peaks()
-    dom = max(kstats.values(), key=lambda d: d["ms_total"])
-    bytes_per_launch = kwords[dom["cls"]] * 8.0 * case.cells
-    achieved = bytes_per_launch / (dom["avg_us"] * 1e-6) / 1e9
+    cb = class_bytes(case, form, rep)
+    traffic = load_traffic(args.config, form)
     for k, d in kstats.items():
-        w = kwords.get(d["cls"])
-        if w:
-            d["achieved_gbs"] = w * 8.0 * case.cells / (d["avg_us"] * 1e-6) / 1e9
-    name = [k for k, d in kstats.items() if d is dom][0]
-    out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                       "frac": achieved / peak, "traffic": None, "kernel": name, "peak_source": src,
-                       "algorithmic_bytes_per_launch": bytes_per_launch,
-                       "avg_launch_us": dom["avg_us"], "kernels": kstats}
+        per_step = cb.get(k, 0) * case.cells            # algorithmic bytes of the class in one step
+        d["algorithmic_bytes_per_launch"] = per_step / d["launches_per_step"]
+        d["achieved_gbs"] = d["algorithmic_bytes_per_launch"] / (d["avg_us"] * 1e-6) / 1e9
+        d["frac"] = d["achieved_gbs"] / peak
+        if k in traffic:
+            d["dram_bytes_per_launch"] = traffic[k] * case.cells / d["launches_per_step"]
+    dom_name, dom = max(kstats.items(), key=lambda kv: kv[1]["ms_total"])
+    out["roofline"] = {"bound": "hbm", "achieved": dom["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                       "frac": dom["frac"], "traffic": dom.get("dram_bytes_per_launch"), "kernel": dom_name,
+                       "peak_source": src, "algorithmic_bytes_per_launch": dom["algorithmic_bytes_per_launch"],
+                       "avg_launch_us": dom["avg_us"], "kernels": kstats,
+                       "traffic_source": "profiles/roofline_traffic.md" if dom_name in traffic else None}
+    sb = step_bytes(case, form, rep)
+    step_gbs = sb * case.cells / (out["ms_per_step"] * 1e-3) / 1e9
+    out["step_roofline"] = {"bytes_per_cell_step": sb, "fp64_words_per_cell_step": sb / 8.0,
+                            "achieved": step_gbs, "peak": peak, "unit": "GB/s", "frac": step_gbs / peak,
+                            "model": "per-phase minimum traffic of the hot path, stored widths of the form"}
 
     # ---- end to end through the C ABI with host buffers
     shape = case.grid.shape
@@ -447,7 +586,7 @@ def run_ours(args):
         case, rep = main["case"], main["report"]
         cpu = None
         if world == 1 and not args.no_cpu:
-            cpu = cpu_baseline(args.config, "fp64", seconds=args.cpu_seconds)
+            cpu = cpu_baseline(args.config, seconds=args.cpu_seconds)
         line = {"metric": METRIC, "value": main["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": main["ms_per_step"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.form == "fp64" else "f32/f64",
@@ -455,7 +594,8 @@ def run_ours(args):
                 "config": {"workload": WORKLOAD[args.config], "cells": case.cells, "form": args.form,
                            "l2": "flushed between timed steps (256 MiB write, outside the timed region)",
                            "parallelism": "replicas" if world > 1 else "single GPU"},
-                "roofline": main.get("roofline"), "cpu_baseline": cpu, "e2e": main.get("e2e"),
+                "roofline": main.get("roofline"), "step_roofline": main.get("step_roofline"),
+                "cpu_baseline": cpu, "e2e": main.get("e2e"),
                 "gpu_launches": main["kernels_per_step"] * args.steps, "kernels_per_step": main["kernels_per_step"],
                 "clocks": main["clocks"],
                 "check": {"dvmax": rep["dvmax"], "ubulk": rep["ubulk"], "csgsts": rep["csgsts"],
@@ -484,7 +624,7 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", default="channel64", choices=sorted(WORKLOAD))
+    ap.add_argument("--config", default="channel590", choices=sorted(WORKLOAD))
     ap.add_argument("--form", default="mixed", choices=["fp64", "mixed"],
                     help="mixed (default): the mixed form is timed, then the FP64 form on the same "
                          "config, and the mixed form's error against FP64 is stated")

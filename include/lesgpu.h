@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define LESGPU_ABI_VERSION 1
+#define LESGPU_ABI_VERSION 2
 
 /* ---- error codes ------------------------------------------------------ */
 #define LESGPU_OK                 0
@@ -173,6 +173,19 @@ typedef struct lesgpu_step_report {
     int64_t poisson_iters[3];   /* iterations of each substep's Poisson solve */
     double phase_ms[4];     /* SGS, RHS+LHS, Poisson, whole step (device ms)  */
     double qflux;           /* flow rate qvol_u / xl (writehistory)           */
+    /* Iterative Poisson solves of this step (substeps x z or x modes, or
+     * BiCGSTAB solves) that stopped at MGITR above the tolerance: the
+     * reference prints 'ITERATION LIMIT EXCEEDED.' and goes on
+     * (poiss_z_ft.f90:289, poiss_mgrd.f90:204), as lesgpu_step does unless
+     * lesgpu_set_strict is on. */
+    int64_t poisson_unconverged;
+    /* Heat the thermal IB forcing adds to the fluid per unit time over the
+     * step, sum of fcvavg(n,4) * f2fx f2fy f2fz over the thermal forcing
+     * points (the thermal counterpart of draglift's force integral,
+     * slv_auxi.f90:705-716; fcvavg(:,4) is accumulated in slv_engy.f90:
+     * 299-303).  For a body at T = 0 in fluid at T = -1 the mean Nusselt
+     * number is heat_body * Re * Pr / (surface area * (0 - (-1))). */
+    double heat_body;
 } lesgpu_step_report;
 
 /* Fields of lesgpu_get_array / lesgpu_set_array (phase-level parity tests). */
@@ -315,6 +328,12 @@ int lesgpu_get_report(lesgpu_case *c, lesgpu_step_report *rep);
 int lesgpu_step_async(lesgpu_case *c, int64_t n);
 int lesgpu_stream(lesgpu_case *c, void **stream);
 int lesgpu_use_graph(lesgpu_case *c, int on);
+
+/* Strict convergence (no reference counterpart; the reference only prints
+ * a warning): with on != 0, lesgpu_step returns LESGPU_ERR_NOT_CONVERGED
+ * after completing a step in which report.poisson_unconverged > 0 (the
+ * state has advanced and the report is filled, as without it). */
+int lesgpu_set_strict(lesgpu_case *c, int on);
 
 /* Kernel launches one step makes (counted from the captured step graph). */
 int lesgpu_launch_count(lesgpu_case *c, int64_t *kernels_per_step);

@@ -108,7 +108,7 @@ class StepReport(C.Structure):
                 ("nutavg", f64), ("nutmax", f64), ("alpavg", f64), ("alpmax", f64),
                 ("cd", f64 * 3), ("heat_flux", f64 * 3), ("ubulk", f64),
                 ("tbulk_fluid", f64), ("tbulk_solid", f64), ("poisson_iters", i64 * 3),
-                ("phase_ms", f64 * 4), ("qflux", f64)]
+                ("phase_ms", f64 * 4), ("qflux", f64), ("poisson_unconverged", i64), ("heat_body", f64)]
 
     def as_dict(self) -> Dict[str, Any]:
         out = {}

@@ -62,6 +62,8 @@ __device__ void stepinit_pre(KP p) {
     DScal *S = p.S;
     S->ntime += 1;
     S->m = S->ntime;
+    S->poisson_unconv = 0;
+    S->heat_body = 0.0;
     if (p.c.ich != 0) S->pmiavg = 0.0;
     if (p.c.idtopt == 0) S->dt = p.c.dt_size;
     S->subdt = 0.0;

@@ -243,9 +243,27 @@ struct DragFinal {
     }
 };
 
+// The thermal counterpart of the force integral: the heat the thermal
+// forcing adds over the step, sum of fcvavg(n,4) times the cell-centre
+// volume of the T forcing points (fcvavg(:,4) accumulates in rhs_ibm_t,
+// slv_engy.f90:299-303; the reference computes no such sum).
+struct HeatIbTerm {
+    __device__ void operator()(const KP &p, int t, int, int, double *w) const {
+        const DGrid &g = p.g;
+        const int n = t + 1;
+        const int ii = p.f.ifc[3][n], jj = p.f.jfc[3][n], kk = p.f.kfc[3][n];
+        w[0] = p.f.fcvavg[3][n] * (g.f2fx[ii] * g.f2fy[jj] * g.f2fz[kk]);
+    }
+};
+struct HeatIbFinal {
+    __device__ void operator()(const KP &p, const double *o) const { p.S->heat_body = o[0]; }
+};
+
 void launch_draglift(lesgpu_case *c) {
     const DGrid &g = c->kp.g;
     reduce<3, false>(c, ibm_box(c), DragIbTerm{}, DragIbFinal{});
+    if (c->kp.c.ihtrans == 1 && c->kp.c.nbody[3] > 0)
+        reduce<1, false>(c, Box{0, 0, 0, c->kp.c.nbody[3], 1, 1}, HeatIbTerm{}, HeatIbFinal{});
     Box faces{0, 0, 0, 2 * g.n1m * g.n3m + 2 * g.n1m * g.n2m, 1, 1};
     reduce<3, false>(c, faces, WallShearTerm{}, DragFinal{});
 }

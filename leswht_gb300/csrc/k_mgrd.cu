@@ -335,6 +335,7 @@ __global__ void __launch_bounds__(kMgrdThreads) k_mgrd_solve(MgrdArgs a) {
     double rho = r1[0], rho_ol = 1.0, alp = 1.0, w = 1.0;
     const double test1 = a.S->test1;
     int done = a.mgitr;
+    bool conv = false;
     for (int it = 1; it <= a.mgitr; it++) {
         const double bet = rho / rho_ol * alp / w;
         for (long long q = tid; q < nin; q += nthr) {
@@ -390,7 +391,7 @@ __global__ void __launch_bounds__(kMgrdThreads) k_mgrd_solve(MgrdArgs a) {
         grid_reduce<2>(a, grid, mr, mx, sl3, sh);
         rho_ol = rho;
         rho = mr[1];
-        if (mr[0] < test1) { done = it; break; }
+        if (mr[0] < test1) { done = it; conv = true; break; }
     }
     const double phiref = a.phi[1 + a.sx * n2m + a.sxy * 1];
     grid.sync();
@@ -399,7 +400,10 @@ __global__ void __launch_bounds__(kMgrdThreads) k_mgrd_solve(MgrdArgs a) {
         const long long c = at(q, i, j, k);
         a.phi[c] = a.phi[c] - phiref;
     }
-    if (tid == 0) a.S->poisson_iters[a.slot] = done;
+    if (tid == 0) {
+        a.S->poisson_iters[a.slot] = done;
+        if (!conv) a.S->poisson_unconv += 1;   // poiss_mgrd.f90:204 prints NOT CONVERGED and goes on
+    }
 }
 
 // ------------------------------------------------------------ host side

@@ -728,6 +728,8 @@ static void fill_report(const lesgpu_case *c, const DScal &s, lesgpu_step_report
     r->nutavg = s.nutavg; r->nutmax = s.nutmax; r->alpavg = s.alpavg; r->alpmax = s.alpmax;
     r->ubulk = s.ubulk; r->qflux = s.qflux; r->tbulk_fluid = s.tbulk_fluid; r->tbulk_solid = s.tbulk_solid;
     for (int q = 0; q < 3; q++) r->poisson_iters[q] = s.poisson_iters[q];
+    r->poisson_unconverged = s.poisson_unconv;
+    r->heat_body = s.heat_body;
 }
 
 extern "C" int lesgpu_step(lesgpu_case *c, lesgpu_step_report *rep) {
@@ -748,6 +750,7 @@ extern "C" int lesgpu_step(lesgpu_case *c, lesgpu_step_report *rep) {
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
     if (rep) fill_report(c, c->hS, rep);
     if (c->hS.err) return LESGPU_ERR_NAN;
+    if (c->strict && c->hS.poisson_unconv > 0) return LESGPU_ERR_NOT_CONVERGED;
     return 0;
 }
 
@@ -776,6 +779,12 @@ extern "C" int lesgpu_step_async(lesgpu_case *c, int64_t n) {
 extern "C" int lesgpu_stream(lesgpu_case *c, void **stream) {
     if (!c || !stream) return LESGPU_ERR_ARG;
     *stream = (void *)c->stream;
+    return 0;
+}
+
+extern "C" int lesgpu_set_strict(lesgpu_case *c, int on) {
+    if (!c) return LESGPU_ERR_ARG;
+    c->strict = on ? 1 : 0;
     return 0;
 }
 

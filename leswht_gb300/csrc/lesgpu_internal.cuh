@@ -77,6 +77,8 @@ struct DScal {
     long long avg_count;      // field_avg samples since the last reset
     long long ntime, m, ihist;
     long long poisson_iters[3];
+    long long poisson_unconv; // solves of the step that stopped at MGITR above the tolerance
+    double heat_body;         // thermal IB forcing's heat rate over the step (draglift's thermal term)
     int err;                  // device-side error flag (non-finite values etc.)
 };
 
@@ -291,6 +293,7 @@ struct lesgpu_case {
     int graph_ok;
     int use_graph;
     int autotune;              // use the autotuner's choices (LESGPU_AUTOTUNE != 0 at start)
+    int strict;                // lesgpu_set_strict: unconverged Poisson solves are an error
     // 1 once a loaded conjugate table (c*, k*, omega) holds a value other
     // than 1; while 0 the temperature sweeps use the factored coefficients
     int conj_general;

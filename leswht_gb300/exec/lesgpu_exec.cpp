@@ -728,6 +728,9 @@ int main(int argc, char **argv) {
     // ---- the time loop, solver.f90:85-183
     while (ntime < c.nend && time < c.tend) {
         check(lesgpu_step(cs, &rep), "step");
+        // the reference's multigrid prints this once per mode that reached
+        // MGITR (poiss_z_ft.f90:289) and carries on
+        for (int64_t q = 0; q < rep.poisson_unconverged; q++) printf(" ITERATION LIMIT EXCEEDED.\n");
         ntime = rep.ntime;
         time = rep.time;
         const double dt = rep.dt;

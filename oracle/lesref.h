@@ -30,6 +30,9 @@ int ref_run_phase(ref_case *c, int64_t phase, int64_t msub);
 int ref_get_report(ref_case *c, lesgpu_step_report *rep);
 int ref_get_averages(ref_case *c, double *out, int64_t *nsamples, int reset);
 int ref_destroy(ref_case *c);
+/* OpenMP threads of the loops (omp_set_num_threads); the current count */
+int ref_set_threads(int n);
+int ref_get_threads(void);
 
 /* building blocks exposed for invariant tests */
 int ref_fft_1d(int n, const double *in_reim, double *out_reim, int iopt);

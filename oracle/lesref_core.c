@@ -9,6 +9,9 @@
 #include <math.h>
 #include "lesref_internal.h"
 #include "lesref.h"
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 double *ref_zalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(double)); }
 ll *ref_izalloc(size_t n) { return (ll *)calloc(n ? n : 1, sizeof(ll)); }
@@ -254,6 +257,8 @@ int ref_get_report(ref_case *c, lesgpu_step_report *r)
     r->nutavg = c->nutavg; r->nutmax = c->nutmax; r->alpavg = c->alpavg; r->alpmax = c->alpmax;
     r->ubulk = c->ubulk; r->qflux = c->qflux; r->tbulk_fluid = c->tbulk_fluid; r->tbulk_solid = c->tbulk_solid;
     for (int i = 0; i < 3; i++) r->poisson_iters[i] = c->poisson_iters[i];
+    r->poisson_unconverged = c->poisson_unconv;
+    r->heat_body = c->heat_body;
     return 0;
 }
 
@@ -344,6 +349,27 @@ int ref_run_phase(ref_case *c, int64_t phase, int64_t msub)
     }
 }
 
+/* Thread count of the OpenMP loops (the stated core count of a CPU timing). */
+int ref_set_threads(int n)
+{
+#ifdef _OPENMP
+    if (n < 1) return -1;
+    omp_set_num_threads(n);
+    return 0;
+#else
+    return n == 1 ? 0 : -1;
+#endif
+}
+
+int ref_get_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
 int ref_destroy(ref_case *c)
 {
     if (!c) return 0;
@@ -376,6 +402,8 @@ void ref_stepinit(ref_case *c)
     const lesgpu_config *g = &c->c;
     c->ntime += 1;
     c->m = c->ntime;
+    c->poisson_unconv = 0;
+    c->heat_body = 0.0;
     for (int l = 0; l < 4; l++)
         for (ll n = 1; n <= c->nbody[l]; n++) c->fcvavg[l][n] = 0.0;
     if (g->ich != 0) c->pmiavg = 0.0;
@@ -614,6 +642,14 @@ void ref_draglift(ref_case *c)
             cd[l] = cd[l] - c->fcvavg[l][n] * (c->c2cx[ii] * c->f2fy[jj] * c->f2fz[kk]);
         }
     cd[0] += c->dudta; cd[1] += c->dvdta; cd[2] += c->dwdta;
+    /* the thermal forcing's heat rate, with the cell-centre volume of the T points */
+    double hb = 0.0;
+    if (g->ihtrans == 1)
+        for (ll n = 1; n <= c->nbody[3]; n++) {
+            ll ii = c->ifc[3][n], jj = c->jfc[3][n], kk = c->kfc[3][n];
+            hb = hb + c->fcvavg[3][n] * (c->f2fx[ii] * c->f2fy[jj] * c->f2fz[kk]);
+        }
+    c->heat_body = hb;
     double *u = c->u, *v = c->v, *w = c->w, re = g->re;
     if (g->bc_ybtm == 0) {
         double dy1 = 1.0 / c->c2cyi[1], dy2 = dy1 + 1.0 / c->c2cyi[2];

@@ -94,6 +94,8 @@ typedef struct ref_case {
     ll *ipm, *imm, *kpm, *kmm;
     double *ac, *gam, *bet;            /* z_ft: (n1md,n2m,n3mh); mgrd: (n1md,n2m,n3md) */
     ll poisson_iters[3];               /* per substep: most cycles any mode took */
+    ll poisson_unconv;                 /* solves of the step that stopped at MGITR above the test */
+    double heat_body;                  /* draglift's thermal term: sum fcvavg(n,4) f2fx f2fy f2fz */
 
     /* scalars (mod_common) */
     ll ntime, ihist, m, msub;

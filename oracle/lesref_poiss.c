@@ -567,7 +567,7 @@ static void zft_goup(const ref_case *c, zmode *z, ll ilev)
 }
 
 /* mg2d, poiss_z_ft.f90:239-299; returns the number of V-cycles */
-static ll zft_mg2d(const ref_case *c, zmode *z, ll kv, double test, double oldv)
+static ll zft_mg2d(const ref_case *c, zmode *z, ll kv, double test, double oldv, int *unconv)
 {
     ll nlev = c->c.nlev, kk = 0;
     double sumres;
@@ -586,6 +586,7 @@ static ll zft_mg2d(const ref_case *c, zmode *z, ll kv, double test, double oldv)
         zft_toplevel(c, z, 1, &sumres, 1.0, test, kv);
         if (sumres < test) return kk;
     }
+    *unconv = 1;
     return kk;   /* iteration limit (the reference prints a warning and goes on) */
 }
 
@@ -603,7 +604,7 @@ static double zft_resid3(const ref_case *c, zmode *z, ll kv)
 }
 
 /* gsor2d, poiss_z_ft.f90:513-616: zebra line SOR on pc (= u) */
-static ll zft_gsor2d(const ref_case *c, zmode *z, ll kv, double test, double oldv)
+static ll zft_gsor2d(const ref_case *c, zmode *z, ll kv, double test, double oldv, int *unconv)
 {
     ll n1m = c->n1m, n2m = c->n2m;
     double ww = c->c.wwsor, ww2 = 1.0 - ww;
@@ -629,6 +630,7 @@ static ll zft_gsor2d(const ref_case *c, zmode *z, ll kv, double test, double old
         }
         if (zft_resid3(c, z, kv) < test) return kk;
     }
+    *unconv = 1;
     return c->c.mgitr;
 }
 
@@ -639,7 +641,7 @@ static void zft_poisson(ref_case *c)
     ll ld_p = n1 + 1, ld_g = n1md + 1;
     size_t np = (size_t)ld_p * (size_t)(n2 + 1), ng = (size_t)ld_g * (size_t)(n2 + 1);
     cplx *ccap = (cplx *)calloc(np * (size_t)n3mh, sizeof(cplx));
-    ll itmax = 0;
+    ll itmax = 0, nunc = 0;
     if (n3m == 1) {
         for (ll j = 1; j <= n2m; j++)
             for (ll i = 1; i <= n1m; i++) { ccap[(size_t)i + (size_t)ld_p * (size_t)j].re = c->divgsum[IX(c, i, j, 1)]; }
@@ -658,7 +660,7 @@ static void zft_poisson(ref_case *c)
         }
     }
     double test = n3m == 1 ? c->test1 : c->test1 / (double)n3mh * (double)n3m * 0.8;
-    #pragma omp parallel reduction(max:itmax)
+    #pragma omp parallel reduction(max:itmax) reduction(+:nunc)
     {
         zmode z;
         z.ld_p = ld_p; z.ld_g = ld_g;
@@ -671,8 +673,10 @@ static void zft_poisson(ref_case *c)
             memset(z.pc, 0, sizeof(cplx) * np);
             memset(z.resd, 0, sizeof(cplx) * ng);
             memset(z.gg, 0, sizeof(cplx) * ng);
-            ll it = kkk <= c->c.imgsor ? zft_mg2d(c, &z, kkk, test, 0.0) : zft_gsor2d(c, &z, kkk, test, 0.0);
+            int unc = 0;
+            ll it = kkk <= c->c.imgsor ? zft_mg2d(c, &z, kkk, test, 0.0, &unc) : zft_gsor2d(c, &z, kkk, test, 0.0, &unc);
             if (it > itmax) itmax = it;
+            nunc += unc;
             for (ll j = 1; j <= n2m; j++)
                 for (ll i = 1; i <= n1m; i++) z.rhs[(size_t)i + (size_t)ld_p * (size_t)j] = PC(&z, i, j);
         }
@@ -702,6 +706,7 @@ static void zft_poisson(ref_case *c)
     }
     free(ccap);
     c->poisson_iters[c->msub >= 1 && c->msub <= 3 ? c->msub - 1 : 0] = itmax;
+    c->poisson_unconv += nunc;
 }
 
 /* -------------------------------------------------------- poiss_x_ft -- */
@@ -1008,7 +1013,7 @@ static void xft_goup(const ref_case *c, zmode *z, ll ilev)
 }
 
 /* mg2d, poiss_x_ft.f90:238-294; returns the number of V-cycles */
-static ll xft_mg2d(const ref_case *c, zmode *z, ll iv, double test, double oldv)
+static ll xft_mg2d(const ref_case *c, zmode *z, ll iv, double test, double oldv, int *unconv)
 {
     ll nlev = c->c.nlev;
     double sumres;
@@ -1027,6 +1032,7 @@ static ll xft_mg2d(const ref_case *c, zmode *z, ll iv, double test, double oldv)
         xft_toplevel(c, z, 1, &sumres, 1.0, test, iv);
         if (sumres < test) return ii;
     }
+    *unconv = 1;
     return c->c.mgitr;   /* iteration limit (the reference prints a warning and goes on) */
 }
 
@@ -1045,7 +1051,7 @@ static double xft_resid3(const ref_case *c, zmode *z, ll iv)
 
 /* gsor2d, poiss_x_ft.f90:497-617: zebra line SOR on pc (= u); the zero
    wavenumber's odd lines are shifted by u(1,n2m) after their update */
-static ll xft_gsor2d(const ref_case *c, zmode *z, ll iv, double test, double oldv)
+static ll xft_gsor2d(const ref_case *c, zmode *z, ll iv, double test, double oldv, int *unconv)
 {
     ll n3m = c->n3m, n2m = c->n2m;
     double ww = c->c.wwsor, ww2 = 1.0 - ww;
@@ -1068,6 +1074,7 @@ static ll xft_gsor2d(const ref_case *c, zmode *z, ll iv, double test, double old
         }
         if (xft_resid3(c, z, iv) < test) return ii;
     }
+    *unconv = 1;
     return c->c.mgitr;
 }
 
@@ -1078,7 +1085,7 @@ static void xft_poisson(ref_case *c)
     ll ld_p = n3 + 1, ld_g = n3md + 1;
     size_t np = (size_t)ld_p * (size_t)(n2 + 1), ng = (size_t)ld_g * (size_t)(n2 + 1);
     cplx *ccap = (cplx *)calloc(np * (size_t)n1mh, sizeof(cplx));
-    ll itmax = 0;
+    ll itmax = 0, nunc = 0;
     #pragma omp parallel
     {
         cplx *line = (cplx *)malloc(sizeof(cplx) * (size_t)n1m), *wk = (cplx *)malloc(sizeof(cplx) * 2 * (size_t)n1m);
@@ -1092,7 +1099,7 @@ static void xft_poisson(ref_case *c)
         free(line); free(wk);
     }
     double test = c->test1 / (double)n1mh * (double)n1m * 0.9;
-    #pragma omp parallel reduction(max:itmax)
+    #pragma omp parallel reduction(max:itmax) reduction(+:nunc)
     {
         zmode z;
         z.ld_p = ld_p; z.ld_g = ld_g;
@@ -1105,8 +1112,10 @@ static void xft_poisson(ref_case *c)
             memset(z.pc, 0, sizeof(cplx) * np);
             memset(z.resd, 0, sizeof(cplx) * ng);
             memset(z.gg, 0, sizeof(cplx) * ng);
-            ll it = iii <= c->c.imgsor ? xft_mg2d(c, &z, iii, test, 0.0) : xft_gsor2d(c, &z, iii, test, 0.0);
+            int unc = 0;
+            ll it = iii <= c->c.imgsor ? xft_mg2d(c, &z, iii, test, 0.0, &unc) : xft_gsor2d(c, &z, iii, test, 0.0, &unc);
             if (it > itmax) itmax = it;
+            nunc += unc;
             for (ll j = 1; j <= n2m; j++)
                 for (ll k = 1; k <= n3m; k++) z.rhs[(size_t)k + (size_t)ld_p * (size_t)j] = PC(&z, k, j);
         }
@@ -1139,6 +1148,7 @@ static void xft_poisson(ref_case *c)
                 for (ll i = 1; i <= n1m; i++) c->phi[IX(c, i, j, k)] = c->phi[IX(c, i, j, k)] - phiref;
     }
     c->poisson_iters[c->msub >= 1 && c->msub <= 3 ? c->msub - 1 : 0] = itmax;
+    c->poisson_unconv += nunc;
 }
 
 /* ------------------------------------------------------------ mgrd ---- */
@@ -1521,6 +1531,7 @@ static void mgrd_poisson(ref_case *c)
         rho_ol = rho;
         if (resm < c->test1) { done = it; break; }
     }
+    if (it > c->c.mgitr) c->poisson_unconv += 1;   /* poiss_mgrd.f90:204: NOT CONVERGED, goes on */
     double phiref = phi[IX(c, 1, n2m, 1)];
     for (ll k = 1; k <= n3m; k++)
         for (ll j = 1; j <= n2m; j++)

@@ -27,7 +27,7 @@ def test_library_exports_all_declared_symbols(gpu_lib):
 
 
 def test_strerror_and_version(gpu_lib):
-    assert gpu_lib.lesgpu_abi_version() == 1
+    assert gpu_lib.lesgpu_abi_version() == 2
     assert gpu_lib.lesgpu_strerror(-8) == b"option not built in this library"
 
 

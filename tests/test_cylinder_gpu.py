@@ -66,6 +66,10 @@ def test_one_step(oracle_lib, dims):
     for q in range(2):
         assert rg["cd"][q] == pytest.approx(rr["cd"][q], rel=1e-9, abs=1e-12), q
     assert rg["heat_flux"][0] == pytest.approx(rr["heat_flux"][0], rel=1e-9)
+    # the thermal forcing's heat rate (the Nusselt number's numerator)
+    assert rg["heat_body"] != 0.0
+    assert rg["heat_body"] == pytest.approx(rr["heat_body"], rel=1e-9)
+    assert rg["poisson_unconverged"] == rr["poisson_unconverged"] == 0
     assert rg["dvmax"] < 1e-5
 
 

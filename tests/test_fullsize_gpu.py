@@ -1,0 +1,64 @@
+"""GPU parity at the benchmark's full sizes: one step of the FP64 form
+against the CPU oracle on the same initial field.
+
+* the Re_tau ~ 590 channel, 384 x 256 x 384 cells (37.7M; poiss_ftft), the
+  workload of the headline measurement;
+* the Re = 3900 heated cylinder, 256 x 192 x 64 cells (3.1M; IB direct
+  forcing on u, v, w and T, convective outlet, poiss_z_ft multigrid), with
+  equal V-cycle counts in every substep.
+
+Tolerance: relative L2 <= 1e-10 per field, as at the small sizes.  The
+oracle needs some seconds per step on all host cores at these sizes.
+"""
+import numpy as np
+import pytest
+
+import leswht_gb300
+from leswht_gb300 import cases, solver
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def rel(a, b):
+    den = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (den if den > 0 else 1.0)
+
+
+def one_step(oracle_lib, case):
+    g = leswht_gb300.gpu_solver(case)
+    rg = g.step()
+    fg = g.fields()
+    g.close()
+    r = solver.Solver(oracle_lib, "ref_", case)
+    rr = r.step()
+    fr = r.fields()
+    r.close()
+    return rg, rr, fg, fr
+
+
+def test_channel590_one_step(oracle_lib):
+    case = cases.PRESETS["channel590"]()
+    assert case.cells == 384 * 256 * 384
+    rg, rr, fg, fr = one_step(oracle_lib, case)
+    for k in ("u", "v", "w", "p", "t"):
+        assert rel(fg[k], fr[k]) <= TOL, (k, rel(fg[k], fr[k]))
+    assert rg["dt"] == pytest.approx(rr["dt"], rel=1e-13)
+    assert rg["csgsts"] == pytest.approx(rr["csgsts"], rel=1e-9)
+    assert rg["pmi"][0] == pytest.approx(rr["pmi"][0], rel=1e-9)
+    assert rg["ubulk"] == pytest.approx(rr["ubulk"], rel=1e-12)
+    assert rg["dvmax"] < 1e-10 and rr["dvmax"] < 1e-10
+
+
+def test_cylinder3900_one_step(oracle_lib):
+    case = cases.PRESETS["cylinder3900"]()
+    assert (case.grid.n1m, case.grid.n2m, case.grid.n3m) == (256, 192, 64)
+    rg, rr, fg, fr = one_step(oracle_lib, case)
+    assert rg["poisson_iters"] == rr["poisson_iters"] and min(rg["poisson_iters"]) > 0
+    for k in ("u", "v", "w", "p", "t"):
+        assert rel(fg[k], fr[k]) <= TOL, (k, rel(fg[k], fr[k]))
+    assert rg["dt"] == pytest.approx(rr["dt"], rel=1e-13)
+    for q in range(2):
+        assert rg["cd"][q] == pytest.approx(rr["cd"][q], rel=1e-9, abs=1e-12), q
+    assert rg["heat_flux"][0] == pytest.approx(rr["heat_flux"][0], rel=1e-9)
