@@ -559,6 +559,33 @@ def serving_sample(args, lib):
     return out
 
 
+def profile_one_step(args):
+    """For an ncu capture with --profile-from-start off: build the case,
+    start it (autotuning included) and run `warmup` steps, then one step
+    between cudaProfilerStart and cudaProfilerStop; prints one line."""
+    import torch
+    import leswht_gb300
+    torch.cuda.set_device(0)
+    lib = leswht_gb300.load_library()
+    case = make_case(args.config, args.form)
+    s = leswht_gb300.gpu_solver(case)
+    for _ in range(args.warmup):
+        if lib.lesgpu_step_async(s.h, 1) != 0:
+            raise RuntimeError("step failed")
+    torch.cuda.synchronize()
+    kps = C.c_int64()
+    lib.lesgpu_launch_count(s.h, C.byref(kps))
+    torch.cuda.profiler.start()
+    if lib.lesgpu_step_async(s.h, 1) != 0:
+        raise RuntimeError("step failed")
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    print(json.dumps({"profiled": case.name, "form": args.form, "cells": case.cells,
+                      "kernels_per_step": int(kps.value)}))
+    s.close()
+    return 0
+
+
 def run_ours(args):
     import torch
     import leswht_gb300
@@ -633,11 +660,16 @@ def main():
                     help="cases in the serving sample (0: skip it)")
     ap.add_argument("--serving-steps", type=int, default=40)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--profile-one-step", action="store_true",
+                    help="run warm-up steps, then one step inside cudaProfilerStart/Stop (for ncu "
+                         "--profile-from-start off); no timing, no JSON result line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_one_step:
+        return profile_one_step(args)
     return run_ours(args)
 
 
