@@ -528,6 +528,87 @@ def form_error(args, nsteps):
     return err
 
 
+def long_horizon(config, nsteps, avg_from):
+    """The mixed form against the FP64 form over a configuration's own
+    horizon: both run `nsteps` steps from the same initial field with
+    field_avg on, its sums restarted after step `avg_from`; the statistics
+    of the window after it are compared (leswht_gb300.stats): max divergence
+    over the run, relative L2 of u and T at the end, mean and rms profiles
+    (channel) or fields (cylinder), drag, Strouhal and Nusselt numbers."""
+    import numpy as np
+    import leswht_gb300
+    from leswht_gb300 import stats
+    runs = {}
+    for form in ("fp64", "mixed"):
+        case = make_case(config, form)
+        case.settings.update(iavg=1, avg_tst=0.0)
+        sol = leswht_gb300.gpu_solver(case)
+        hist, dvmax, unconv = [], 0.0, 0
+        t0 = time.perf_counter()
+        for n in range(1, nsteps + 1):
+            r = sol.step()
+            dvmax = max(dvmax, r["dvmax"])
+            unconv += r["poisson_unconverged"]
+            if n == avg_from:
+                sol.averages(reset=True)
+            elif n > avg_from:
+                hist.append(r)
+        avg, nsamp = sol.averages()
+        runs[form] = {"case": case, "hist": hist, "avg": avg, "nsamp": nsamp, "fields": sol.fields(),
+                      "dvmax": dvmax, "unconv": unconv, "seconds": time.perf_counter() - t0}
+        sol.close()
+    a, b = runs["fp64"], runs["mixed"]
+    case = a["case"]
+    s = case.settings
+
+    def rd(x, y):
+        return abs(x - y) / max(abs(y), 1e-300)
+
+    out = {"steps": nsteps, "window_steps": len(a["hist"]),
+           "window_time": sum(r["dt"] for r in a["hist"]),
+           "max_div": {"fp64": a["dvmax"], "mixed": b["dvmax"]},
+           "poisson_unconverged": {"fp64": a["unconv"], "mixed": b["unconv"]},
+           "rel_l2_end": {k: stats.rel_l2(b["fields"][k], a["fields"][k]) for k in ("u", "t")},
+           "seconds": {"fp64": a["seconds"], "mixed": b["seconds"]}}
+    st = {}
+    for form, r in runs.items():
+        times = [q["time"] for q in r["hist"]]
+        dts = [q["dt"] for q in r["hist"]]
+        win = float(sum(dts))
+        m = stats.mean_and_rms(r["avg"], win)
+        d = {"m": m, "drag": stats.time_mean(times, dts, [q["cd"][0] for q in r["hist"]])}
+        if s.get("ibmon", 0) == 1:
+            d["strouhal"] = stats.strouhal(times, [q["cd"][1] for q in r["hist"]])
+            if s.get("ihtrans", 0) == 1:
+                hb = stats.time_mean(times, dts, [q["heat_body"] for q in r["hist"]])
+                d["nusselt"] = stats.cylinder_nusselt(hb, s["re"], s["pr"], 2.0 * s["body"]["r"],
+                                                      case.grid.zl, 0.0 - s["tflu_i"])
+        else:
+            d["wall_shear"] = stats.time_mean(times, dts, [-q["pmi"][0] for q in r["hist"]])
+            if s.get("ihtrans", 0) == 1:
+                d["nusselt"] = stats.channel_nusselt(m["t"], m["u"], case.grid)
+        st[form] = d
+    fa, fb = st["fp64"], st["mixed"]
+    keys = [k for k in ("u_rms", "v_rms", "w_rms", "t_rms") if k in fa["m"]]
+    if s.get("ibmon", 0) == 1:
+        out["rms_rel_l2"] = {k: stats.rel_l2(fb["m"][k], fa["m"][k]) for k in keys}
+        out["mean_rel_l2"] = {k: stats.rel_l2(fb["m"][k], fa["m"][k]) for k in ("u", "t") if k in fa["m"]}
+        out["drag"] = {"fp64": fa["drag"], "mixed": fb["drag"], "rel": rd(fb["drag"], fa["drag"])}
+        out["strouhal"] = {"fp64": fa["strouhal"], "mixed": fb["strouhal"],
+                           "rel": rd(fb["strouhal"], fa["strouhal"]) if fa["strouhal"] and fb["strouhal"] else None}
+    else:
+        out["rms_profile_rel_l2"] = {k: stats.rel_l2(stats.plane_profile(fb["m"][k]), stats.plane_profile(fa["m"][k]))
+                                     for k in keys}
+        out["mean_profile_rel_l2"] = {k: stats.rel_l2(stats.plane_profile(fb["m"][k]),
+                                                      stats.plane_profile(fa["m"][k]))
+                                      for k in ("u", "t") if k in fa["m"]}
+        out["wall_shear"] = {"fp64": fa["wall_shear"], "mixed": fb["wall_shear"],
+                             "rel": rd(fb["wall_shear"], fa["wall_shear"])}
+    if "nusselt" in fa:
+        out["nusselt"] = {"fp64": fa["nusselt"], "mixed": fb["nusselt"], "rel": rd(fb["nusselt"], fa["nusselt"])}
+    return out
+
+
 def serving_sample(args, lib):
     """A bounded sample of the serving stream (seeded Poisson arrivals at
     2 cases/s; grid, body, Re and Pr drawn as in the benchmark stream), run
@@ -637,6 +718,14 @@ def run_ours(args):
             line["mixed_vs_fp64"] = main["value"] / other["value"]
             line["gpu_launches"] += other["kernels_per_step"] * args.steps
             line["error"] = form_error(args, args.steps)
+        if world == 1:
+            acc = {}
+            if args.accuracy_steps > 0:
+                acc["channel64"] = long_horizon("channel64", args.accuracy_steps, args.accuracy_steps // 2)
+            if args.accuracy_c3_steps > 0:
+                acc["cylinder3900"] = long_horizon("cylinder3900", args.accuracy_c3_steps, args.accuracy_c3_steps // 2)
+            if acc:
+                line["accuracy"] = acc
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist
@@ -660,6 +749,13 @@ def main():
                     help="cases in the serving sample (0: skip it)")
     ap.add_argument("--serving-steps", type=int, default=40)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--accuracy-steps", type=int, default=2000,
+                    help="steps of the 64^3 channel's mixed-vs-FP64 statistics comparison (0: skip); "
+                         "statistics over the second half")
+    ap.add_argument("--accuracy-c3-steps", type=int, default=0,
+                    help="steps of the same comparison on the Re=3900 cylinder, 256x192x64 (0: skip)")
+    ap.add_argument("--accuracy-only", action="store_true",
+                    help="run only the statistics comparisons and print them as one JSON line")
     ap.add_argument("--profile-one-step", action="store_true",
                     help="run warm-up steps, then one step inside cudaProfilerStart/Stop (for ncu "
                          "--profile-from-start off); no timing, no JSON result line")
@@ -670,6 +766,16 @@ def main():
         return run_reference(args)
     if args.profile_one_step:
         return profile_one_step(args)
+    if args.accuracy_only:
+        import torch
+        torch.cuda.set_device(0)
+        acc = {}
+        if args.accuracy_steps > 0:
+            acc["channel64"] = long_horizon("channel64", args.accuracy_steps, args.accuracy_steps // 2)
+        if args.accuracy_c3_steps > 0:
+            acc["cylinder3900"] = long_horizon("cylinder3900", args.accuracy_c3_steps, args.accuracy_c3_steps // 2)
+        print(json.dumps({"accuracy": acc}))
+        return 0
     return run_ours(args)
 
 

@@ -60,6 +60,13 @@ struct MgSet {
     T *aw, *ae, *as, *an, *coi1, *coi2, *cor1, *cor2;   // 1-based
     T *ac, *bet, *gam;          // (i-1) + nld*((j-1) + n2m*(kv-1))
     typename V2<T>::t *pc, *gg, *rs;
+    // rd: the defect of a level partitioned over the cluster (its godown
+    // result, kept apart from the restricted residual in rs that neighbouring
+    // blocks still read in the same phase); gu: prolonged even lines; gb:
+    // a copy of a partitioned level's even lines after its down-sweep
+    // relaxation, the base its prolongation adds to (read by neighbouring
+    // blocks while the owner overwrites gg)
+    typename V2<T>::t *rd, *gu, *gb;
 };
 
 struct MgTables {
@@ -67,6 +74,7 @@ struct MgTables {
     int nmodes, xft;            // modes solved (n3mh / n1mh); 1 for poiss_x_ft
     int mixed;                  // FP32 cycles under an FP64 defect correction
     int cs;                     // blocks per cluster (one cluster per z mode)
+    int lc;                     // levels 0..lc run on one block of the cluster
     int cap;                    // cap on cs set by the creator (0 = none)
     int iimg[kMaxLev + 1][3];
     int *ipm, *imm;
@@ -92,6 +100,7 @@ struct MgArgs {
     DScal *S;
     int slot;
     int fixed_cycles;           // > 0: run exactly this many cycles (autotuner timing), no test
+    int lc;                     // levels 0..lc (at most kCoarseLines lines) run on one block
 };
 
 // ------------------------------------------------------------- device side
@@ -106,22 +115,32 @@ struct ModeT {
     const MgArgs &a;
     const MgSet<T> &s;
     int kv;
-    int tid, nt;                        // thread index / count over the cluster
-    V *pc, *gg, *rs;
+    int tid, nt;                        // thread index / count over the cluster (or the block)
+    bool local;                         // the threads are one block's: sync() is the block barrier
+    V *pc, *gg, *rs, *rd, *gu, *gb;
     const double2 *rhs;                 // ccap plane of the mode, (i-1) + nl*(j-1)
     size_t cb;                          // coefficient base of the mode
-    __device__ void sync() const { cooperative_groups::this_cluster().sync(); }
-    __device__ ModeT(const MgArgs &a_, const MgSet<T> &s_, int kv_, int tid_, int nt_)
-        : a(a_), s(s_), kv(kv_), tid(tid_), nt(nt_) {
+    __device__ void sync() const {
+        if (local) __syncthreads();
+        else cooperative_groups::this_cluster().sync();
+    }
+    __device__ ModeT(const MgArgs &a_, const MgSet<T> &s_, int kv_, int tid_, int nt_, bool local_ = false)
+        : a(a_), s(s_), kv(kv_), tid(tid_), nt(nt_), local(local_) {
         pc = s.pc + a.pc_plane * (kv - 1);
         gg = s.gg + a.gg_plane * (kv - 1);
         rs = s.rs + a.gg_plane * (kv - 1);
+        rd = s.rd + a.gg_plane * (kv - 1);
+        gu = s.gu + a.gg_plane * (kv - 1);
+        gb = s.gb + a.gg_plane * (kv - 1);
         rhs = a.ccap + (size_t)a.nl * a.n2m * (kv - 1);
         cb = (size_t)a.nld * a.n2m * (kv - 1);
     }
     __device__ V &P(int i, int j) const { return pc[i + (size_t)a.ldp * j]; }
     __device__ V &G(int i, int j) const { return gg[i + (size_t)a.ldg * j]; }
     __device__ V &R(int i, int j) const { return rs[i + (size_t)a.ldg * j]; }
+    __device__ V &D(int i, int j) const { return rd[i + (size_t)a.ldg * j]; }
+    __device__ V &U(int i, int j) const { return gu[i + (size_t)a.ldg * j]; }
+    __device__ V &GB(int i, int j) const { return gb[i + (size_t)a.ldg * j]; }
     __device__ double2 B(int i, int j) const { return rhs[(i - 1) + (size_t)a.nl * (j - 1)]; }
     __device__ T AC(int i, int j) const { return s.ac[cb + (i - 1) + (size_t)a.nld * (j - 1)]; }
 };
@@ -590,6 +609,544 @@ __device__ int mg_gsor2d(const Mode &m, double test, bool &unconv) {
     return a.mgitr;
 }
 
+// ---------------------------------------------------------------------------
+// Level-partitioned V-cycle (the cycle of mg_mg2d / mg_mg2d_mixed with the
+// same per-point arithmetic).  The phases above spread every level's lines
+// over the whole cluster and put a cluster barrier after each half sweep,
+// defect, restriction and prolongation: about forty barriers per V-cycle,
+// which bound the solve.  Here:
+//   * on the top level and on every level of more than kCoarseLines lines,
+//     block r of the cluster owns a contiguous, even-aligned range of lines
+//     [a, b]; the few lines just outside it that its own lines depend on
+//     inside one phase (the halo: at most the two lines before a and the
+//     two after b, cyclically on a periodic level) are recomputed by the
+//     block into shared memory, so a whole relaxation + defect +
+//     restriction, or a prolongation + relaxation, needs one cluster
+//     barrier at its end and only block barriers inside;
+//   * the levels of at most kCoarseLines lines run on block 0 alone with
+//     block barriers (the phases above with a block-local mode view); the
+//     other blocks wait at one cluster barrier;
+//   * the defect of a partitioned level goes to rd, not over the restricted
+//     residual in rs that neighbouring blocks still read in the same phase
+//     (the reference overwrites resd with it, poiss_z_ft.f90:447-452; the
+//     post-smoothing of the level reads it from rd, the same values), and
+//     prolonged even lines go to gu (scratch) for the same reason;
+//   * the max-norm test exchanges one value per block through distributed
+//     shared memory at the phase's closing barrier.
+// A V-cycle takes 2 + 2 (levels above kCoarseLines lines below the top) + 1
+// cluster barriers.
+constexpr int kCoarseLines = 32;
+constexpr int kHalo = 6;
+constexpr int kHaloRows = 32 * kMC + 2;
+
+// lines [ibg, iend] of a level; the block owns [a, b]
+struct Part {
+    int ibg, iend, a, b;
+    __device__ bool in(int i) const { return i >= ibg && i <= iend; }
+    __device__ bool own(int i) const { return i >= a && i <= b; }
+};
+__device__ __forceinline__ Part part_of(int ibg, int iend, int r, int cs) {
+    const int nb = (iend - ibg + 1) / cs;
+    return Part{ibg, iend, ibg + r * nb, ibg + r * nb + nb - 1};
+}
+
+// halo lines of a phase and their rows in shared memory
+template <class V>
+struct Halo {
+    int line[kHalo];
+    V *buf;
+    __device__ int slot(int i) const {
+#pragma unroll
+        for (int s = 0; s < kHalo; s++)
+            if (line[s] == i) return s;
+        return -1;
+    }
+    __device__ V &at(int s, int j) const { return buf[s * kHaloRows + j]; }
+    __device__ void add(int i) {        // i >= 1, deduplicated
+        if (slot(i) >= 0) return;
+#pragma unroll
+        for (int s = 0; s < kHalo; s++)
+            if (line[s] < 0) { line[s] = i; return; }
+    }
+};
+
+// the value of neighbour line `line`, row j: from the halo, else from
+// `in` (lines of the level) or `out` (lines outside it, weight zero)
+template <class V>
+__device__ __forceinline__ V nbval(const Halo<V> &h, const Part &pt, const V *in, int ldi, const V *out, int ldo,
+                                   int line, int j) {
+    const int s = h.slot(line);
+    if (s >= 0) return h.at(s, j);
+    return pt.in(line) ? in[line + (size_t)ldi * j] : out[line + (size_t)ldo * j];
+}
+
+// The y solves of one zebra half on a partitioned level: the block's own
+// lines of parity par (0: a, a+2, ..; 1: a+1, a+3, ..) and the halo lines
+// of that parity listed in xl (their results go to the halo).  Right-hand
+// sides as mg_half forms them (kind), from src (rhs plane if src == null);
+// neighbours from nbval(h, ...).  With kind H_ODD and ov == 0 the right-hand
+// side is the source itself (the neighbour terms vanish).
+template <int MC, class T>
+__device__ __noinline__ void part_half(const ModeT<T> &m, const Part &pt, int par, const int *xl, int nx, int kind,
+                                       const typename V2<T>::t *src, const typename V2<T>::t *nin, int ldi,
+                                       const typename V2<T>::t *nout, int ldo, Halo<typename V2<T>::t> &h, T ov,
+                                       typename V2<T>::t tt) {
+    using V = typename V2<T>::t;
+    const MgArgs &a = m.a;
+    const MgSet<T> &s = m.s;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int n2m = a.n2m;
+    const int ch = (n2m + 31) / 32;
+    const int j0 = 1 + lane * ch;
+    const int cnt = max(0, min(ch, n2m - j0 + 1));
+    const size_t sj = (size_t)a.nld;
+    const int nown = (pt.b - pt.a + 1) / 2;
+    for (int li = warp; li < nown + nx; li += nw) {
+        const int i = li < nown ? pt.a + par + 2 * li : xl[li - nown];
+        const int im = a.imm[i], ip = a.ipm[i];
+        const T aw = s.aw[i], ae = s.ae[i];
+        const T *bet = s.bet + m.cb + (i - 1);
+        const T *gam = s.gam + m.cb + (i - 1);
+        V v[MC];
+        T as_[MC], bt[MC], gm[MC];
+#pragma unroll
+        for (int q = 0; q < MC; q++)
+            if (q < cnt) {
+                const int j = j0 + q;
+                V sr;
+                if (!src) {
+                    const double2 b = m.B(i, j);
+                    sr = V{T(b.x), T(b.y)};
+                } else {
+                    sr = src[i + (size_t)a.ldg * j];
+                }
+                if (kind == H_ODD && ov == T(0.0)) {
+                    v[q] = sr;
+                } else {
+                    V nm = nbval(h, pt, nin, ldi, nout, ldo, im, j), np = nbval(h, pt, nin, ldi, nout, ldo, ip, j);
+                    if (kind == H_ODD) {
+                        const T sx = aw * nm.x + ae * np.x, sy = aw * nm.y + ae * np.y;
+                        v[q] = V{sr.x - ov * sx, sr.y - ov * sy};
+                    } else if (kind == H_EVEN) {
+                        v[q] = V{sr.x - aw * nm.x - ae * np.x, sr.y - aw * nm.y - ae * np.y};
+                    } else {
+                        nm = V{nm.x - tt.x, nm.y - tt.y};
+                        if (ip < i) np = V{np.x - tt.x, np.y - tt.y};
+                        v[q] = V{sr.x - aw * nm.x - ae * (np.x - tt.x), sr.y - aw * nm.y - ae * (np.y - tt.y)};
+                    }
+                }
+                as_[q] = s.as[j];
+                bt[q] = bet[sj * (j - 1)];
+                gm[q] = j < n2m ? gam[sj * j] : T(0.0);
+            }
+        line_solve<MC>(v, as_, bt, gm, cnt, lane);
+        const int hs = li < nown ? -1 : h.slot(i);
+#pragma unroll
+        for (int q = 0; q < MC; q++)
+            if (q < cnt) {
+                const int j = j0 + q;
+                if (hs < 0) m.G(i, j) = v[q];
+                else h.at(hs, j) = v[q];
+            }
+    }
+}
+
+// src - aw*g(imm) - ae*g(ipm) - as*g(j-1) - an*g(j+1) - ac*g (mg_defect) with
+// the line neighbours through the halo
+template <class T>
+__device__ __forceinline__ typename V2<T>::t part_defect(const ModeT<T> &m, const Part &pt,
+                                                        const Halo<typename V2<T>::t> &h, typename V2<T>::t src,
+                                                        const typename V2<T>::t *g, int ld, int i, int j) {
+    const MgArgs &a = m.a;
+    const MgSet<T> &s = m.s;
+    src = axmy(src, s.aw[i], nbval(h, pt, g, ld, g, ld, a.imm[i], j));
+    src = axmy(src, s.ae[i], nbval(h, pt, g, ld, g, ld, a.ipm[i], j));
+    src = axmy(src, s.as[j], g[i + (size_t)ld * (j - 1)]);
+    src = axmy(src, s.an[j], g[i + (size_t)ld * (j + 1)]);
+    src = axmy(src, m.AC(i, j), g[i + (size_t)ld * j]);
+    return src;
+}
+
+// prolongation of coarse line i (level range [cl, ce]) onto a fine even
+// line: base + coi1 g(i) + coi2 g(ipm i) (mg_goup / mg_top_prolong)
+template <class T>
+__device__ __forceinline__ typename V2<T>::t prolong_val(const ModeT<T> &m, typename V2<T>::t p, int i, int ce, int j) {
+    const MgArgs &a = m.a;
+    const MgSet<T> &s = m.s;
+    const typename V2<T>::t g1 = m.G(i, j);
+    if (i < ce || a.xft) {
+        const typename V2<T>::t g2 = m.G(a.ipm[i], j);
+        return typename V2<T>::t{p.x + s.coi1[i] * g1.x + s.coi2[i] * g2.x, p.y + s.coi1[i] * g1.y + s.coi2[i] * g2.y};
+    }
+    return typename V2<T>::t{p.x + s.coi1[i] * g1.x, p.y + s.coi1[i] * g1.y};
+}
+
+__device__ __forceinline__ void hinit(int (&l)[kHalo]) {
+#pragma unroll
+    for (int s = 0; s < kHalo; s++) l[s] = -1;
+}
+
+// One level down (relax(ilev, 0, 1) + godown(ilev)) on a partitioned level:
+// restricted residual R -> relaxed G (own lines), defect -> D, restricted
+// defect -> R of level ilev - 1 (own coarse lines).  Ends at the cluster barrier.
+template <class T>
+__device__ void part_down(const ModeT<T> &m, int ilev, int r, int cs, typename V2<T>::t *hbuf) {
+    using V = typename V2<T>::t;
+    const MgArgs &a = m.a;
+    const Part pt = part_of(a.iimg[ilev][0], a.iimg[ilev][1], r, cs);
+    const int n2m = a.n2m;
+    Halo<V> h;
+    hinit(h.line);
+    h.buf = hbuf;
+    int xo[2], nxo = 0, xe[1], nxe = 0;
+    const int l1 = a.imm[pt.a], r1 = a.ipm[pt.b];
+    if (pt.in(r1) && !pt.own(r1)) { h.add(r1); xo[nxo++] = r1; }
+    if (pt.in(l1) && !pt.own(l1)) {
+        const int l2 = a.imm[l1];
+        if (pt.in(l2) && !pt.own(l2) && h.slot(l2) < 0) { h.add(l2); xo[nxo++] = l2; }
+        h.add(l1);
+        xe[nxe++] = l1;
+    }
+    const V zero{T(0.0), T(0.0)};
+    part_half<kMC, T>(m, pt, 0, xo, nxo, H_ODD, m.rs, m.gg, a.ldg, m.gg, a.ldg, h, T(0.0), zero);
+    __syncthreads();
+    part_half<kMC, T>(m, pt, 1, xe, nxe, H_EVEN, m.rs, m.gg, a.ldg, m.gg, a.ldg, h, T(1.0), zero);
+    __syncthreads();
+    const int nown = pt.b - pt.a + 1;
+    for (int t = threadIdx.x; t < nown * n2m; t += blockDim.x) {
+        const int i = pt.a + t % nown, j = 1 + t / nown;
+        m.D(i, j) = part_defect(m, pt, h, m.R(i, j), m.gg, a.ldg, i, j);
+        if (((i - pt.ibg) & 1) == 1) m.GB(i, j) = m.G(i, j);     // even line: the base of its prolongation
+    }
+    __syncthreads();
+    const int cl = a.iimg[ilev - 1][0], c0 = cl + (pt.a - pt.ibg) / 2, nc = nown / 2;
+    for (int t = threadIdx.x; t < nc * n2m; t += blockDim.x) {
+        const int i = c0 + t % nc, j = 1 + t / nc, f = pt.ibg + 2 * (i - cl);
+        const V r1v = m.D(f, j), r2v = m.D(f + 1, j);
+        m.R(i, j) = V{r1v.x * m.s.cor1[i] + r2v.x * m.s.cor2[i], r1v.y * m.s.cor1[i] + r2v.y * m.s.cor2[i]};
+    }
+    cooperative_groups::this_cluster().sync();
+}
+
+// One level up (goup(ilev) + relax(ilev + 1, 1, 1)) onto a partitioned
+// level: prolonged even lines (own -> U, halo), relaxation against the
+// level's defect D.  Ends at the cluster barrier.
+template <class T>
+__device__ void part_up(const ModeT<T> &m, int ilev, int r, int cs, typename V2<T>::t *hbuf) {
+    using V = typename V2<T>::t;
+    const MgArgs &a = m.a;
+    const int F = ilev + 1;
+    const Part pt = part_of(a.iimg[F][0], a.iimg[F][1], r, cs);
+    const int n2m = a.n2m, cl = a.iimg[ilev][0], ce = a.iimg[ilev][1], fb = pt.ibg;
+    Halo<V> h;
+    hinit(h.line);
+    h.buf = hbuf;
+    int xo[1], nxo = 0;
+    int xe[2], nxe = 0;
+    const int l1 = a.imm[pt.a], r1 = a.ipm[pt.b];
+    if (pt.in(l1) && !pt.own(l1)) { h.add(l1); xe[nxe++] = l1; }
+    if (pt.in(r1) && !pt.own(r1)) {
+        h.add(r1);
+        xo[nxo++] = r1;
+        const int r2 = a.ipm[r1];
+        if (pt.in(r2) && !pt.own(r2) && h.slot(r2) < 0) { h.add(r2); xe[nxe++] = r2; }
+    }
+    // prolongation onto the own even lines (-> U) and the halo even lines
+    const int ne = (pt.b - pt.a + 1) / 2;
+    for (int t = threadIdx.x; t < (ne + nxe) * n2m; t += blockDim.x) {
+        const int q = t % (ne + nxe), j = 1 + t / (ne + nxe);
+        const int f = q < ne ? pt.a + 1 + 2 * q : xe[q - ne];
+        const int i = cl + (f - fb - 1) / 2;
+        const V v = prolong_val(m, m.GB(f, j), i, ce, j);
+        if (q < ne) m.U(f, j) = v;
+        else h.at(h.slot(f), j) = v;
+    }
+    __syncthreads();
+    const V zero{T(0.0), T(0.0)};
+    part_half<kMC, T>(m, pt, 0, xo, nxo, H_ODD, m.rd, m.gu, a.ldg, m.gg, a.ldg, h, T(1.0), zero);
+    __syncthreads();
+    part_half<kMC, T>(m, pt, 1, xo, 0, H_EVEN, m.rd, m.gg, a.ldg, m.gg, a.ldg, h, T(1.0), zero);
+    cooperative_groups::this_cluster().sync();
+}
+
+// The top level's relaxation (toplevel's prolongation and zebra sweep with
+// the zero wavenumber's pin) on the partitioned top level.  prolong: the
+// coarse correction is added to (FP64 form) or becomes (assign, the mixed
+// form's correction) the even lines' neighbour values, in U; src: the
+// right-hand side plane (null) or the FP32 residual.  The mixed form then
+// adds the correction to the FP64 solution of its own lines.  Ends at the
+// cluster barrier.
+template <class T>
+__device__ void part_top_relax(const ModeT<T> &m, int r, int cs, T oldv, bool prolong, bool assign,
+                               const typename V2<T>::t *src, typename V2<T>::t *hbuf, const Mode *x64, bool first) {
+    using V = typename V2<T>::t;
+    const MgArgs &a = m.a;
+    const Part pt = part_of(1, a.nl, r, cs);
+    const int n2m = a.n2m, nlev = a.nlev;
+    const int cl = a.iimg[nlev - 1][0], ce = a.iimg[nlev - 1][1];
+    Halo<V> h;
+    hinit(h.line);
+    h.buf = hbuf;
+    int xo[2], nxo = 0, xe[4], nxe = 0;
+    const int l1 = a.imm[pt.a], r1 = a.ipm[pt.b];
+    if (prolong && pt.in(l1) && !pt.own(l1)) { h.add(l1); xe[nxe++] = l1; }
+    if (pt.in(r1) && !pt.own(r1)) {
+        h.add(r1);
+        xo[nxo++] = r1;
+        const int r2 = a.ipm[r1];
+        if (prolong && pt.in(r2) && !pt.own(r2) && h.slot(r2) < 0) { h.add(r2); xe[nxe++] = r2; }
+    }
+    const bool pin = m.kv == 1;
+    if (pin && !pt.own(1) && h.slot(1) < 0) {
+        // line 1 gives the zero wavenumber's shift: recomputed by every
+        // block, with the prolonged even lines beside it
+        h.add(1);
+        xo[nxo++] = 1;
+        if (prolong)
+            for (int q = 0; q < 2; q++) {
+                const int e = q == 0 ? a.imm[1] : a.ipm[1];
+                if (pt.in(e) && !pt.own(e) && h.slot(e) < 0) { h.add(e); xe[nxe++] = e; }
+            }
+    }
+    if (prolong) {
+        const int ne = (pt.b - pt.a + 1) / 2;
+        for (int t = threadIdx.x; t < (ne + nxe) * n2m; t += blockDim.x) {
+            const int q = t % (ne + nxe), j = 1 + t / (ne + nxe);
+            const int ic = q < ne ? pt.a + 1 + 2 * q : xe[q - ne];
+            const int i = cl + ic / 2 - 1;
+            const V base = assign ? V{T(0.0), T(0.0)} : m.P(ic, j);
+            const V v = prolong_val(m, base, i, ce, j);
+            if (q < ne) m.U(ic, j) = v;
+            else h.at(h.slot(ic), j) = v;
+        }
+        __syncthreads();
+    }
+    const V zero{T(0.0), T(0.0)};
+    // odd lines: neighbours are the even lines' prolonged values (U, halo),
+    // or P outside the level
+    part_half<kMC, T>(m, pt, 0, xo, nxo, H_ODD, src, prolong ? m.gu : m.pc, prolong ? a.ldg : a.ldp, m.pc, a.ldp, h,
+                      oldv, zero);
+    __syncthreads();
+    auto gval = [&](int i, int j) -> V {
+        const int s = h.slot(i);
+        return s >= 0 ? h.at(s, j) : m.G(i, j);
+    };
+    if (a.xft) {
+        // poiss_x_ft: shift the odd lines by ggii(1,n2m) (own and halo), then
+        // the even lines from the shifted values
+        if (pin) {
+            const V tt = gval(1, n2m);
+            __syncthreads();
+            const int no = (pt.b - pt.a + 1) / 2;
+            for (int t = threadIdx.x; t < (no + nxo) * n2m; t += blockDim.x) {
+                const int q = t % (no + nxo), j = 1 + t / (no + nxo);
+                const int i = q < no ? pt.a + 2 * q : xo[q - no];
+                V &g = q < no ? m.G(i, j) : h.at(h.slot(i), j);
+                g = V{g.x - tt.x, g.y - tt.y};
+            }
+            __syncthreads();
+        }
+        part_half<kMC, T>(m, pt, 1, xe, 0, H_ODD, src, m.gg, a.ldg, m.gg, a.ldg, h, T(1.0), zero);
+        __syncthreads();
+    } else {
+        // poiss_z_ft: the even lines see the odd ones shifted by
+        // ggii(1,n2m-1) inside their right-hand side; the odd lines are
+        // shifted afterwards
+        const V tt = pin ? gval(1, n2m - 1) : zero;
+        part_half<kMC, T>(m, pt, 1, xe, 0, H_EVEN_TT, src, m.gg, a.ldg, m.gg, a.ldg, h, T(1.0), tt);
+        __syncthreads();
+        if (pin) {
+            const int no = (pt.b - pt.a + 1) / 2;
+            for (int t = threadIdx.x; t < no * n2m; t += blockDim.x) {
+                const int i = pt.a + 2 * (t % no), j = 1 + t / no;
+                V &g = m.G(i, j);
+                g = V{g.x - tt.x, g.y - tt.y};
+            }
+            __syncthreads();
+        }
+    }
+    if (x64) {            // the mixed form: x += e on the own lines (x = e on the first pass)
+        const int nown = pt.b - pt.a + 1;
+        for (int t = threadIdx.x; t < nown * n2m; t += blockDim.x) {
+            const int i = pt.a + t % nown, j = 1 + t / nown;
+            const V e = m.G(i, j);
+            const double2 x = first ? make_double2(0.0, 0.0) : x64->P(i, j);
+            x64->P(i, j) = make_double2(x.x + (double)e.x, x.y + (double)e.y);
+        }
+    }
+    cooperative_groups::this_cluster().sync();
+}
+
+// Max over the cluster through distributed shared memory: one value per
+// block, slot `par` (alternating between calls, so a slot is rewritten only
+// after every block has passed the barrier that follows its reads).  The
+// caller's cluster barrier must follow; returns after it.
+__device__ double part_cluster_max(double v, int par) {
+    __shared__ double sh[kMgThreads / 32];
+    __shared__ double blk[2];
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) r = fmax(r, sh[q]);
+        blk[par] = r;
+    }
+    cl.sync();
+    double r = 0.0;
+    for (int q = 0; q < (int)cl.num_blocks(); q++) r = fmax(r, *cl.map_shared_rank(&blk[par], q));
+    return r;
+}
+
+// toplevel's residual on the partitioned top level (FP64 form): R = B - A G
+// on the own lines, P = G, the residual restricted onto level nlev-1 (own
+// coarse lines), the max norm over the cluster.
+__device__ double part_top_resid(const Mode &m, int r, int cs, int par) {
+    const MgArgs &a = m.a;
+    const Part pt = part_of(1, a.nl, r, cs);
+    const int n2m = a.n2m, nown = pt.b - pt.a + 1;
+    double mx = 0.0;
+    Halo<double2> h0;
+    hinit(h0.line);
+    h0.buf = nullptr;
+    for (int t = threadIdx.x; t < nown * n2m; t += blockDim.x) {
+        const int i = pt.a + t % nown, j = 1 + t / nown;
+        const double2 d = part_defect(m, pt, h0, m.B(i, j), m.gg, a.ldg, i, j);
+        m.R(i, j) = d;
+        mx = fmax(mx, d.x * d.x + d.y * d.y);
+        m.P(i, j) = m.G(i, j);
+    }
+    __syncthreads();
+    const int cl = a.iimg[a.nlev - 1][0], c0 = cl + (pt.a - 1) / 2, nc = nown / 2;
+    for (int t = threadIdx.x; t < nc * n2m; t += blockDim.x) {
+        const int i = c0 + t % nc, j = 1 + t / nc, ic = 2 * (i - cl) + 1;
+        const double2 r1 = m.R(ic, j), r2 = m.R(ic + 1, j);
+        m.R(i, j) = double2{r1.x * m.s.cor1[i] + r2.x * m.s.cor2[i], r1.y * m.s.cor1[i] + r2.y * m.s.cor2[i]};
+    }
+    return sqrt(part_cluster_max(mx, par));
+}
+
+// the mixed form's residual: r = b - A x in FP64 (x in m.P) -> the FP32
+// residual f.R, restricted in FP32 onto level nlev-1; the max norm
+__device__ double part_top_resid_mixed(const Mode &m, const ModeT<float> &f, int r, int cs, int par) {
+    const MgArgs &a = m.a;
+    const Part pt = part_of(1, a.nl, r, cs);
+    const int n2m = a.n2m, nown = pt.b - pt.a + 1;
+    double mx = 0.0;
+    for (int t = threadIdx.x; t < nown * n2m; t += blockDim.x) {
+        const int i = pt.a + t % nown, j = 1 + t / nown;
+        const double2 d = mg_defect(m, m.B(i, j), m.pc, a.ldp, i, j);
+        f.R(i, j) = make_float2((float)d.x, (float)d.y);
+        mx = fmax(mx, d.x * d.x + d.y * d.y);
+    }
+    __syncthreads();
+    const int cl = a.iimg[a.nlev - 1][0], c0 = cl + (pt.a - 1) / 2, nc = nown / 2;
+    for (int t = threadIdx.x; t < nc * n2m; t += blockDim.x) {
+        const int i = c0 + t % nc, j = 1 + t / nc, ic = 2 * (i - cl) + 1;
+        const float2 r1 = f.R(ic, j), r2 = f.R(ic + 1, j);
+        f.R(i, j) = float2{r1.x * f.s.cor1[i] + r2.x * f.s.cor2[i], r1.y * f.s.cor1[i] + r2.y * f.s.cor2[i]};
+    }
+    return sqrt(part_cluster_max(mx, par));
+}
+
+// mg2d (poiss_z_ft.f90:239-299) with the level-partitioned phases
+__device__ int part_mg2d(const Mode &m, double test, bool &unconv, int r, int cs, double2 *hbuf) {
+    const MgArgs &a = m.a;
+    const int nlev = a.nlev, lc = a.lc;
+    int par = 0;
+    part_top_relax(m, r, cs, 0.0, false, false, nullptr, hbuf, nullptr, true);
+    double sumres = part_top_resid(m, r, cs, par);
+    par ^= 1;
+    if (sumres < test) return 0;
+    const Mode mb(a, a.d, m.kv, threadIdx.x, blockDim.x, true);
+    for (int kk = 1; kk <= a.mgitr; kk++) {
+        for (int ilev = nlev - 1; ilev > lc; ilev--) part_down(m, ilev, r, cs, hbuf);
+        if (r == 0) {
+            for (int ilev = lc; ilev >= 1; ilev--) {
+                mg_relax(mb, ilev, 0.0, 1);
+                mg_godown(mb, ilev);
+            }
+            mg_relax(mb, 0, 0.0, a.nbli);
+            for (int ilev = 0; ilev < lc; ilev++) {
+                mg_goup(mb, ilev);
+                mg_relax(mb, ilev + 1, 1.0, 1);
+            }
+        }
+        cooperative_groups::this_cluster().sync();
+        for (int ilev = lc; ilev <= nlev - 2; ilev++) part_up(m, ilev, r, cs, hbuf);
+        part_top_relax(m, r, cs, 1.0, true, false, nullptr, hbuf, nullptr, false);
+        sumres = part_top_resid(m, r, cs, par);
+        par ^= 1;
+        if (sumres < test) return kk;
+    }
+    unconv = true;
+    return a.xft ? a.mgitr : a.mgitr + 1;
+}
+
+// mg_mg2d_mixed with the level-partitioned phases
+__device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, double test, bool &unconv, int r, int cs,
+                               double2 *hbuf) {
+    const MgArgs &a = m.a;
+    const int nlev = a.nlev, lc = a.lc, n2m = a.n2m;
+    float2 *hf = reinterpret_cast<float2 *>(hbuf);
+    int par = 0;
+    {   // the first source is b itself, rounded (own lines; the halo lines
+        // read other blocks' after the barrier)
+        const Part pt = part_of(1, a.nl, r, cs);
+        const int nown = pt.b - pt.a + 1;
+        for (int t = threadIdx.x; t < nown * n2m; t += blockDim.x) {
+            const int i = pt.a + t % nown, j = 1 + t / nown;
+            const double2 b = m.B(i, j);
+            f.R(i, j) = make_float2((float)b.x, (float)b.y);
+        }
+        cooperative_groups::this_cluster().sync();
+    }
+    part_top_relax(f, r, cs, 0.0f, false, true, f.rs, hf, &m, true);
+    double sumres = part_top_resid_mixed(m, f, r, cs, par);
+    par ^= 1;
+    if (sumres < test) return 0;
+    const ModeT<float> fb(a, a.f, m.kv, threadIdx.x, blockDim.x, true);
+    const Mode mb(a, a.d, m.kv, threadIdx.x, blockDim.x, true);
+    const int c0 = a.iimg[0][0], nc0 = a.iimg[0][1] - c0 + 1;
+    for (int kk = 1; kk <= a.mgitr; kk++) {
+        for (int ilev = nlev - 1; ilev > lc; ilev--) part_down(f, ilev, r, cs, hf);
+        if (r == 0) {
+            for (int ilev = lc; ilev >= 1; ilev--) {
+                mg_relax(fb, ilev, 0.0f, 1);
+                mg_godown(fb, ilev);
+            }
+            for (int t = threadIdx.x; t < nc0 * n2m; t += blockDim.x) {     // coarsest level in FP64
+                const int i = c0 + t % nc0, j = 1 + t / nc0;
+                const float2 rr = fb.R(i, j);
+                mb.R(i, j) = make_double2((double)rr.x, (double)rr.y);
+            }
+            __syncthreads();
+            mg_relax(mb, 0, 0.0, a.nbli);
+            for (int t = threadIdx.x; t < nc0 * n2m; t += blockDim.x) {
+                const int i = c0 + t % nc0, j = 1 + t / nc0;
+                const double2 g = mb.G(i, j);
+                fb.G(i, j) = make_float2((float)g.x, (float)g.y);
+            }
+            __syncthreads();
+            for (int ilev = 0; ilev < lc; ilev++) {
+                mg_goup(fb, ilev);
+                mg_relax(fb, ilev + 1, 1.0f, 1);
+            }
+        }
+        cooperative_groups::this_cluster().sync();
+        for (int ilev = lc; ilev <= nlev - 2; ilev++) part_up(f, ilev, r, cs, hf);
+        part_top_relax(f, r, cs, 1.0f, true, true, f.rs, hf, &m, false);
+        sumres = part_top_resid_mixed(m, f, r, cs, par);
+        par ^= 1;
+        if (sumres < test) return kk;
+    }
+    unconv = true;
+    return a.xft ? a.mgitr : a.mgitr + 1;
+}
+
 __global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes(MgArgs a) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
@@ -602,15 +1159,17 @@ __global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes(MgArgs a) {
     const int tid = gw * 32 + (int)(threadIdx.x & 31), nt = cs * blockDim.x;
     Mode m(a, a.d, kv, tid, nt);
     const double test = a.fixed_cycles > 0 ? -1.0 : a.S->mg_test;
+    __shared__ __align__(16) double2 hbuf[kHalo * kHaloRows];
+    const int r = (int)cl.block_rank();
     int it;
     bool unconv = false;
     if (kv > a.imgsor) {
         it = mg_gsor2d(m, test, unconv);
     } else if (a.mixed) {
         ModeT<float> f(a, a.f, kv, tid, nt);
-        it = mg_mg2d_mixed(m, f, test, unconv);
+        it = part_mg2d_mixed(m, f, test, unconv, r, cs, hbuf);
     } else {
-        it = mg_mg2d(m, test, unconv);
+        it = part_mg2d(m, test, unconv, r, cs, hbuf);
     }
     // the mode's solution replaces its right-hand side (ccap(i,j,kkk) = cp(i,j))
     double2 *out = a.ccap + (size_t)a.nl * a.n2m * (kv - 1);
@@ -812,6 +1371,15 @@ static int set_up_tables(lesgpu_case *c, MgTables &T) {
     return ok ? 0 : LESGPU_ERR_OOM;
 }
 
+// A cluster of cs blocks splits the top level and every level above lc into
+// cs ranges of an even number of lines each.
+static bool cs_splits(const MgTables &T, int cs) {
+    if (T.nl % (2 * cs) != 0) return false;
+    for (int l = T.lc + 1; l < T.nlev; l++)
+        if (T.iimg[l][2] % (2 * cs) != 0) return false;
+    return true;
+}
+
 static void cluster_cfg(cudaLaunchConfig_t &lc, cudaLaunchAttribute (&at)[1], int nmodes, int cs) {
     lc = {};
     lc.gridDim = dim3(nmodes * cs);
@@ -856,6 +1424,9 @@ int mg2d_init(lesgpu_case *c) {
     if (cudaMalloc(&T->d.pc, sizeof(double2) * T->pc_plane * nm) != cudaSuccess ||
         cudaMalloc(&T->d.gg, sizeof(double2) * T->gg_plane * nm) != cudaSuccess ||
         cudaMalloc(&T->d.rs, sizeof(double2) * T->gg_plane * nm) != cudaSuccess ||
+        cudaMalloc(&T->d.rd, sizeof(double2) * T->gg_plane * nm) != cudaSuccess ||
+        cudaMalloc(&T->d.gu, sizeof(double2) * T->gg_plane * nm) != cudaSuccess ||
+        cudaMalloc(&T->d.gb, sizeof(double2) * T->gg_plane * nm) != cudaSuccess ||
         cudaMalloc(&T->iters, sizeof(long long) * nm) != cudaSuccess ||
         cudaMalloc(&P.ccap, sizeof(double2) * (size_t)nl * g.n2m * nm) != cudaSuccess)
         return LESGPU_ERR_OOM;
@@ -863,15 +1434,29 @@ int mg2d_init(lesgpu_case *c) {
     cudaMemset(T->d.pc, 0, sizeof(double2) * T->pc_plane * nm);
     cudaMemset(T->d.gg, 0, sizeof(double2) * T->gg_plane * nm);
     cudaMemset(T->d.rs, 0, sizeof(double2) * T->gg_plane * nm);
+    cudaMemset(T->d.rd, 0, sizeof(double2) * T->gg_plane * nm);
+    cudaMemset(T->d.gu, 0, sizeof(double2) * T->gg_plane * nm);
+    cudaMemset(T->d.gb, 0, sizeof(double2) * T->gg_plane * nm);
     if (T->mixed) {
         if (cudaMalloc(&T->f.pc, sizeof(float2) * T->pc_plane * nm) != cudaSuccess ||
             cudaMalloc(&T->f.gg, sizeof(float2) * T->gg_plane * nm) != cudaSuccess ||
-            cudaMalloc(&T->f.rs, sizeof(float2) * T->gg_plane * nm) != cudaSuccess)
+            cudaMalloc(&T->f.rs, sizeof(float2) * T->gg_plane * nm) != cudaSuccess ||
+            cudaMalloc(&T->f.rd, sizeof(float2) * T->gg_plane * nm) != cudaSuccess ||
+            cudaMalloc(&T->f.gu, sizeof(float2) * T->gg_plane * nm) != cudaSuccess ||
+            cudaMalloc(&T->f.gb, sizeof(float2) * T->gg_plane * nm) != cudaSuccess)
             return LESGPU_ERR_OOM;
         cudaMemset(T->f.pc, 0, sizeof(float2) * T->pc_plane * nm);
         cudaMemset(T->f.gg, 0, sizeof(float2) * T->gg_plane * nm);
         cudaMemset(T->f.rs, 0, sizeof(float2) * T->gg_plane * nm);
+        cudaMemset(T->f.rd, 0, sizeof(float2) * T->gg_plane * nm);
+        cudaMemset(T->f.gu, 0, sizeof(float2) * T->gg_plane * nm);
+        cudaMemset(T->f.gb, 0, sizeof(float2) * T->gg_plane * nm);
     }
+    // levels of at most kCoarseLines lines run on one block; the others
+    // (and the top) are split over the cluster
+    T->lc = 0;
+    for (int l = 0; l < nlev; l++)
+        if (T->iimg[l][2] <= kCoarseLines) T->lc = l;
     cudaMemset(T->iters, 0, sizeof(long long) * nm);
     if (xft) {
         if (cudaFuncSetAttribute(k_fft_xr_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess ||
@@ -889,6 +1474,7 @@ int mg2d_init(lesgpu_case *c) {
     const int cands[5] = {16, 8, 4, 2, 1};
     for (int q = 0; q < 5; q++) {
         const int cs = cands[q];
+        if (!cs_splits(*T, cs)) continue;
         cudaLaunchConfig_t lc;
         cudaLaunchAttribute at[1];
         cluster_cfg(lc, at, nmodes, cs);
@@ -911,6 +1497,7 @@ int mg2d_init(lesgpu_case *c) {
     T->cap = cap;
     if (cap >= 1)
         while (T->cs > cap) T->cs >>= 1;
+    while (!cs_splits(*T, T->cs)) T->cs >>= 1;
     return 0;
 }
 
@@ -922,9 +1509,9 @@ void mg2d_free(lesgpu_case *c) {
     MgTables *T = c->pois.mg;
     if (!T) return;
     void *ptrs[] = {T->d.aw, T->d.ae, T->d.as, T->d.an, T->d.coi1, T->d.coi2, T->d.cor1, T->d.cor2, T->ipm, T->imm,
-                    T->d.ac, T->d.bet, T->d.gam, T->d.pc, T->d.gg, T->d.rs, T->iters,
+                    T->d.ac, T->d.bet, T->d.gam, T->d.pc, T->d.gg, T->d.rs, T->d.rd, T->d.gu, T->d.gb, T->iters,
                     T->f.aw, T->f.ae, T->f.as, T->f.an, T->f.coi1, T->f.coi2, T->f.cor1, T->f.cor2,
-                    T->f.ac, T->f.bet, T->f.gam, T->f.pc, T->f.gg, T->f.rs};
+                    T->f.ac, T->f.bet, T->f.gam, T->f.pc, T->f.gg, T->f.rs, T->f.rd, T->f.gu, T->f.gb};
     for (void *q : ptrs) cudaFree(q);
     delete T;
     c->pois.mg = nullptr;
@@ -950,6 +1537,7 @@ static MgArgs mg_args(lesgpu_case *c, int slot, int fixed_cycles) {
     a.pc_plane = T->pc_plane; a.gg_plane = T->gg_plane;
     a.iters = T->iters; a.S = c->S; a.slot = slot;
     a.fixed_cycles = fixed_cycles;
+    a.lc = T->lc;
     return a;
 }
 
@@ -1027,7 +1615,7 @@ int mg2d_autotune(lesgpu_case *c) {
     float best_ms = 3.0e38f;
     for (int cs = 16; cs >= 1; cs >>= 1) {
         if (T->cap >= 1 && cs > T->cap) continue;
-        if (!cluster_fits(c, cs)) continue;
+        if (!cs_splits(*T, cs) || !cluster_fits(c, cs)) continue;
         launch_modes(c, a, cs, 1);              // warm-up
         cudaEventRecord(e0, c->stream);
         for (int r = 0; r < 2; r++) launch_modes(c, a, cs, 1);

@@ -46,7 +46,10 @@ def test_channel590_one_step(oracle_lib):
         assert rel(fg[k], fr[k]) <= TOL, (k, rel(fg[k], fr[k]))
     assert rg["dt"] == pytest.approx(rr["dt"], rel=1e-13)
     assert rg["csgsts"] == pytest.approx(rr["csgsts"], rel=1e-9)
-    assert rg["pmi"][0] == pytest.approx(rr["pmi"][0], rel=1e-9)
+    # the flow-rate controller's dP/dx is driven by the bulk velocity's small
+    # departure from its target, a difference of two near-equal sums over
+    # 37.7M cells: held to 1e-8 relative here (1e-9 at 32x32x16)
+    assert rg["pmi"][0] == pytest.approx(rr["pmi"][0], rel=1e-8)
     assert rg["ubulk"] == pytest.approx(rr["ubulk"], rel=1e-12)
     assert rg["dvmax"] < 1e-10 and rr["dvmax"] < 1e-10
 
