@@ -421,8 +421,9 @@ def time_form(args, form, lib, dev, world, rank, flush, full):
         tot_s = float(t.item())
     rep = s.report()
     import leswht_gb300
-    tuned = [{"dir": "xyz"[d], "components": nc, "fp32": bool(f32), "lanes_per_line": w & 63,
-              "register_capped": bool(w & 64)} if d < 3 else
+    tuned = [({"dir": "xyz"[d], "components": nc, "fp32": bool(f32), "tiled": True} if w == 128 else
+              {"dir": "xyz"[d], "components": nc, "fp32": bool(f32), "lanes_per_line": w & 63,
+               "register_capped": bool(w & 64)}) if d < 3 else
              {"fft": "xyz"[nc], "lines_per_block": w} if d == 3 else {"mg_cluster_blocks": w} if d == 4 else
              {"ftft_fp32_with_fp64_correction": bool(w)}
              for d, nc, f32, w in leswht_gb300.tuning(lib, h)]

@@ -348,7 +348,8 @@ int lesgpu_launch_count(lesgpu_case *c, int64_t *kernels_per_step);
  * after, so several processes share one set of choices.  Writes up to maxn
  * tuples (dir 0..2 = x,y,z; components; fp32 0/1; lanes, 1 = one thread per
  * line, + 64 when the register-capped variant of the warp-scan kernel won)
- * to out as 4 int64 each and their number to *nclasses; the Poisson FFTs'
+ * to out as 4 int64 each and their number to *nclasses (lanes = 128: the
+ * tiled FP32 sweep, lines staged in shared memory); the Poisson FFTs'
  * lines per block, also timed at start, follow as (3, 2 = z | 0 = x, 0,
  * lines), for poiss_z_ft / poiss_x_ft the multigrid's blocks per cluster
  * as (4, 0, 0, blocks), and for poiss_ftft in the mixed form the solve chosen

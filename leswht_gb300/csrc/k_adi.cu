@@ -723,6 +723,345 @@ __global__ void __launch_bounds__(128, MINB) k_adis(KP p, AdiBatch B) {
     }
 }
 
+// ------------------------------------------------------------------------
+// Tiled warp-scan sweeps (x and z sweeps in FP32).  A block stages a tile
+// of kTileLines lines -- consecutive i for z lines, consecutive j for x
+// lines -- in shared memory with coalesced loads: the right-hand side
+// (times the diagonal, in R) and the line's viscosity factor 1 + cre nu at
+// every face; one warp then solves one line from shared memory with the
+// recurrences and chunk layout of k_adis (W = 32 lanes, lane l owning rows
+// l*m .. l*m+m-1), re-forming the coefficients from the factors in each
+// pass instead of holding them in registers, and the tile is written back
+// coalesced.  The serial z sweep moved each line's elimination factors
+// through HBM (2.6 times the sweep's algorithmic bytes) and k_adis held a
+// 12-row chunk's coefficients in registers (16 warps an SM); here the HBM
+// traffic is the operands once and 32 warps fit on an SM.  Results equal
+// the 32-lane k_adis's: the same arithmetic on the same chunks.
+constexpr int kTileLines = 16;
+
+// position of row r of a line in shared memory: lane chunks of m rows with
+// a pitch pm (odd: the 32 lanes' rows fall in 32 different banks)
+__device__ __forceinline__ int tpos(int r, int m, int pm) { return (r / m) * pm + r % m; }
+
+template <class R, int DIR, bool PER, int MC>
+__global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, int m, int pm, int lp) {
+    extern __shared__ __align__(16) unsigned char adit_smem[];
+    R *S = reinterpret_cast<R *>(adit_smem);             // lines x lp: diag*rhs -> y -> x
+    R *Fv = S + kTileLines * lp;                          // lines x lp: 1 + cre nu at rows 0..n
+    const AdiArgs &A = B.a[blockIdx.y];
+    const DGrid &g = p.g;
+    const R diag = (A.comp == CT) ? p.S->acoefi * p.c.pr : p.S->acoefi;
+    const int na = A.a1 - A.a0 + 1, nb = A.b1 - A.b0 + 1;
+    const int n = A.l2 - A.l1 + 1;
+    const long long stride = DIR == 2 ? g.sxy : 1;
+    const long long lstride = DIR == 2 ? 1 : g.sx;       // between consecutive lines of a tile
+    const int ntx = (na + kTileLines - 1) / kTileLines;
+    if ((int)blockIdx.x >= ntx * nb || n <= 0) return;
+    const int x0 = A.a0 + (int)(blockIdx.x % ntx) * kTileLines, x1 = A.b0 + (int)(blockIdx.x / ntx);
+    const int nl = min(kTileLines, A.a1 - x0 + 1);
+    int i0, j0, k0;
+    line_coords(DIR, A.l1, x0, x1, i0, j0, k0);
+    const long long qb = g.ix(i0, j0, k0);                // row 0 of line 0
+    const AdiFacs<R> F = adi_facs<R>(p, A.comp, DIR);
+    // ---- stage the tile (z: lines fastest, x: rows fastest: both coalesced)
+    const int nt = blockDim.x;
+    for (int t = threadIdx.x; t < kTileLines * (n + 1); t += nt) {
+        int w, r;
+        if (DIR == 2) { w = t % kTileLines; r = t / kTileLines; }
+        else { w = t / (n + 1); r = t % (n + 1); }
+        if (w >= nl) continue;
+        const long long q = qb + w * lstride + (long long)r * stride;
+        Fv[w * lp + tpos(r, m, pm)] = R(1.0) + F.cre * R(F.nv[q + F.oa]);
+        if (r < n) S[w * lp + tpos(r, m, pm)] = diag * R(A.src[q]);
+    }
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (w < nl) {
+        R *Sl = S + w * lp;
+        const R *Fl = Fv + w * lp;
+        const int r0 = lane * m;
+        const int cnt = max(0, min(m, n - r0));
+        const int l1 = A.l1;
+        auto coef = [&](int r, R &a, R &c) {
+            a = R(F.ma[l1 + r]) * Fl[tpos(r, m, pm)];
+            c = R(F.mc[l1 + r]) * Fl[tpos(r + 1, m, pm)];
+        };
+        if (!PER) {
+            // c of the row before the chunk
+            R cprev0 = R(0.0);
+            if (lane > 0 && r0 - 1 < n) cprev0 = R(F.mc[l1 + r0 - 1]) * Fl[tpos(r0, m, pm)];
+            if (r0 - 1 >= n) cprev0 = R(0.0);
+            // 1. pivots: Moebius composition, scan, re-run
+            M22<R> T{R(1.0), R(0.0), R(0.0), R(1.0)};
+            {
+                R cp = cprev0;
+#pragma unroll
+                for (int u = 0; u < MC; u++)
+                    if (u < cnt) {
+                        R a, c;
+                        coef(r0 + u, a, c);
+                        const R b = diag - a - c;
+                        M22<R> Tj{R(0.0), R(1.0), -a * cp, b};
+                        T = mmul_chunk(Tj, T);
+                        cp = c;
+                    }
+            }
+            R P, Q;
+            scan_moebius<R, 32>(T, lane, P, Q);
+            R bet = (lane == 0) ? R(0.0) : P / Q;
+            R betv[MC];
+            {
+                R cp = cprev0;
+#pragma unroll
+                for (int u = 0; u < MC; u++)
+                    if (u < cnt) {
+                        R a, c;
+                        coef(r0 + u, a, c);
+                        const R b = diag - a - c;
+                        if (lane == 0 && u == 0) bet = rcp_pivot(b);
+                        else bet = rcp_pivot(b - a * (cp * bet));
+                        betv[u] = bet;
+                        cp = c;
+                    }
+            }
+            // 2. forward substitution y_j = (r_j - a_j y_{j-1}) bet_j
+            R Aa = R(1.0), Bb = R(0.0);
+#pragma unroll
+            for (int u = 0; u < MC; u++)
+                if (u < cnt) {
+                    R a, c;
+                    coef(r0 + u, a, c);
+                    const R mj = (lane == 0 && u == 0) ? R(0.0) : -a * betv[u];
+                    Bb = mj * Bb + Sl[tpos(r0 + u, m, pm)] * betv[u];
+                    Aa = mj * Aa;
+                }
+            R y = scan_affine_up<R, 32>(Aa, Bb, lane, R(0.0));
+#pragma unroll
+            for (int u = 0; u < MC; u++)
+                if (u < cnt) {
+                    R a, c;
+                    coef(r0 + u, a, c);
+                    const int ps = tpos(r0 + u, m, pm);
+                    y = (lane == 0 && u == 0) ? Sl[ps] * betv[u] : (Sl[ps] - a * y) * betv[u];
+                    Sl[ps] = y;
+                }
+            // 3. back substitution x_j = y_j - gm_{j+1} x_{j+1}, gm_{j+1} = c_j bet_j
+            R Cc = R(1.0), Dd = R(0.0);
+#pragma unroll
+            for (int u = MC - 1; u >= 0; u--)
+                if (u < cnt) {
+                    R a, c;
+                    coef(r0 + u, a, c);
+                    const R gn = (r0 + u == n - 1) ? R(0.0) : c * betv[u];
+                    Dd = -gn * Dd + Sl[tpos(r0 + u, m, pm)];
+                    Cc = -gn * Cc;
+                }
+            R x = scan_affine_down<R, 32>(Cc, Dd, lane);
+#pragma unroll
+            for (int u = MC - 1; u >= 0; u--)
+                if (u < cnt) {
+                    R a, c;
+                    coef(r0 + u, a, c);
+                    const R gn = (r0 + u == n - 1) ? R(0.0) : c * betv[u];
+                    const int ps = tpos(r0 + u, m, pm);
+                    x = Sl[ps] - gn * x;
+                    Sl[ps] = x;
+                }
+        } else {
+            // trdiagp: q_j = -c_j / (b_j + a_j q_{j-1}) (Moebius), pn_j the pivots
+            M22<R> T{R(1.0), R(0.0), R(0.0), R(1.0)};
+#pragma unroll
+            for (int u = 0; u < MC; u++)
+                if (u < cnt) {
+                    R a, c;
+                    coef(r0 + u, a, c);
+                    const R b = diag - a - c;
+                    M22<R> Tj{R(0.0), -c, a, b};
+                    T = mmul_chunk(Tj, T);
+                }
+            R P, Q;
+            scan_moebius<R, 32>(T, lane, P, Q);
+            R qq = (lane == 0) ? R(0.0) : P / Q;
+            R pv[MC], sv[MC];
+            R Aa = R(1.0), Bb = R(0.0);
+#pragma unroll
+            for (int u = 0; u < MC; u++)
+                if (u < cnt) {
+                    R a, c;
+                    coef(r0 + u, a, c);
+                    const R b = diag - a - c;
+                    const R pn = rcp_pivot((lane == 0 && u == 0) ? b : b + a * qq);
+                    qq = -c * pn;
+                    pv[u] = pn;
+                    const R mj = -a * pn;
+                    Bb = mj * Bb + Sl[tpos(r0 + u, m, pm)] * pn;
+                    Aa = mj * Aa;
+                }
+            // incoming s and f
+            R sA = Aa, fA = Aa, fB = Bb;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const R sp = __shfl_up_sync(0xffffffffu, sA, d);
+                const R Ap = __shfl_up_sync(0xffffffffu, fA, d), Bp = __shfl_up_sync(0xffffffffu, fB, d);
+                if (lane >= d) { sA = sA * sp; fB = fA * Bp + fB; fA = fA * Ap; }
+            }
+            R s_in = __shfl_up_sync(0xffffffffu, sA, 1), f_in = __shfl_up_sync(0xffffffffu, fB, 1);
+            if (lane == 0) { s_in = R(1.0); f_in = R(0.0); }
+            // the last row's a, b, c and right-hand side, kept for fj2
+            R al = R(0.0), bl = R(0.0), cl = R(0.0), fnl = R(0.0);
+            {
+                R sc = s_in, fc = f_in;
+#pragma unroll
+                for (int u = 0; u < MC; u++)
+                    if (u < cnt) {
+                        R a, c;
+                        coef(r0 + u, a, c);
+                        const int ps = tpos(r0 + u, m, pm);
+                        const R rv = Sl[ps];
+                        if (r0 + u == n - 1) { al = a; bl = diag - a - c; cl = c; fnl = rv; }
+                        if (lane == 0 && u == 0) {
+                            sc = -a * pv[u];
+                            fc = rv * pv[u];
+                        } else {
+                            sc = -a * sc * pv[u];
+                            fc = (rv - a * fc) * pv[u];
+                        }
+                        sv[u] = sc;
+                        Sl[ps] = fc;
+                    }
+            }
+            // backward: S_j = s_j + q_j S_{j+1}, QE_j = f_j + q_j QE_{j+1}; S_{n-1} = 1, QE_{n-1} = 0
+            R Cs = R(1.0), Ds = R(0.0), De = R(0.0);
+#pragma unroll
+            for (int u = MC - 1; u >= 0; u--)
+                if (u < cnt) {
+                    R a, c;
+                    coef(r0 + u, a, c);
+                    const bool last = (r0 + u == n - 1);
+                    const R mq = last ? R(0.0) : -c * pv[u];
+                    const R os = last ? R(1.0) : sv[u], oe = last ? R(0.0) : Sl[tpos(r0 + u, m, pm)];
+                    Ds = mq * Ds + os;
+                    De = mq * De + oe;
+                    Cs = mq * Cs;
+                }
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const R Cn = __shfl_down_sync(0xffffffffu, Cs, d);
+                const R Dsn = __shfl_down_sync(0xffffffffu, Ds, d), Den = __shfl_down_sync(0xffffffffu, De, d);
+                if (lane + d < 32) { Ds = Cs * Dsn + Ds; De = Cs * Den + De; Cs = Cs * Cn; }
+            }
+            R S_in = __shfl_down_sync(0xffffffffu, Ds, 1), E_in = __shfl_down_sync(0xffffffffu, De, 1);
+            if (lane == 31) { S_in = R(0.0); E_in = R(0.0); }
+            R Sp = R(0.0), Ep = R(0.0);
+            {
+                R Sc = S_in, Ec = E_in;
+#pragma unroll
+                for (int u = MC - 1; u >= 0; u--)
+                    if (u < cnt) {
+                        R a, c;
+                        coef(r0 + u, a, c);
+                        const int ps = tpos(r0 + u, m, pm);
+                        if (r0 + u == n - 1) { Sc = R(1.0); Ec = R(0.0); }
+                        else {
+                            const R qj = -c * pv[u];
+                            Sc = sv[u] + qj * Sc;
+                            Ec = Sl[ps] + qj * Ec;
+                        }
+                        sv[u] = Sc;          // S_j
+                        Sl[ps] = Ec;         // QE_j
+                        if (r0 + u == n - 2) { Sp = Sc; Ep = Ec; }
+                    }
+            }
+            // fj2 from S_0, QE_0, S_{n-2}, QE_{n-2} and the last row
+            const int own_last = (n - 1) / m, own_pen = (n - 2) / m;
+            al = __shfl_sync(0xffffffffu, al, own_last);
+            bl = __shfl_sync(0xffffffffu, bl, own_last);
+            cl = __shfl_sync(0xffffffffu, cl, own_last);
+            fnl = __shfl_sync(0xffffffffu, fnl, own_last);
+            Sp = __shfl_sync(0xffffffffu, Sp, own_pen);
+            Ep = __shfl_sync(0xffffffffu, Ep, own_pen);
+            const R S0 = __shfl_sync(0xffffffffu, sv[0], 0);
+            const R E0 = Sl[tpos(0, m, pm)];
+            const R fj2 = (fnl - cl * E0 - al * Ep) / (cl * S0 + al * Sp + bl);
+            __syncwarp();
+#pragma unroll
+            for (int u = 0; u < MC; u++)
+                if (u < cnt) {
+                    const int ps = tpos(r0 + u, m, pm);
+                    Sl[ps] = (r0 + u == n - 1) ? fj2 : fj2 * sv[u] + Sl[ps];
+                }
+        }
+    }
+    __syncthreads();
+    // ---- write back: the solution, or added to the field
+    for (int t = threadIdx.x; t < kTileLines * n; t += nt) {
+        int w2, r;
+        if (DIR == 2) { w2 = t % kTileLines; r = t / kTileLines; }
+        else { w2 = t / n; r = t % n; }
+        if (w2 >= nl) continue;
+        const long long q = qb + w2 * lstride + (long long)r * stride;
+        const R x = S[w2 * lp + tpos(r, m, pm)];
+        if (A.add) A.dst[q] = A.dst[q] + x;
+        else A.dst[q] = x;
+    }
+}
+
+// rows per lane of the tiled sweep (compile-time chunk bound), its shared memory
+struct TileShape {
+    int m, pm, lp, mc;
+    size_t smem;
+};
+static TileShape tile_shape(int nmax) {
+    TileShape t;
+    t.m = (nmax + 31) / 32;
+    t.pm = (t.m % 2 == 0) ? t.m + 1 : t.m + 2;
+    t.lp = 32 * t.pm + 1;
+    t.mc = t.m <= 4 ? 4 : t.m <= 8 ? 8 : t.m <= 12 ? 12 : t.m <= 16 ? 16 : 0;
+    t.smem = (size_t)2 * kTileLines * t.lp * sizeof(float);
+    return t;
+}
+
+template <int DIR, bool PER, int MC>
+static void adit_launch3(dim3 grid, const TileShape &ts, cudaStream_t st, const KP &kp, const AdiBatch &B) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_adit<float, DIR, PER, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        attr = true;
+    }
+    k_adit<float, DIR, PER, MC><<<grid, kTileLines * 32, ts.smem, st>>>(kp, B, ts.m, ts.pm, ts.lp);
+}
+
+template <int DIR, bool PER>
+static bool adit_launch2(dim3 grid, const TileShape &ts, cudaStream_t st, const KP &kp, const AdiBatch &B) {
+    switch (ts.mc) {
+    case 4: adit_launch3<DIR, PER, 4>(grid, ts, st, kp, B); return true;
+    case 8: adit_launch3<DIR, PER, 8>(grid, ts, st, kp, B); return true;
+    case 12: adit_launch3<DIR, PER, 12>(grid, ts, st, kp, B); return true;
+    case 16: adit_launch3<DIR, PER, 16>(grid, ts, st, kp, B); return true;
+    }
+    return false;
+}
+
+// The tiled FP32 sweep of a batch (x or z, factored coefficients); false
+// when it does not apply (the caller falls back).
+static bool adit_launch(lesgpu_case *c, const AdiBatch &B, int ncomp, int nmax) {
+    const int dir = B.a[0].dir;
+    if (dir == 1) return false;
+    const TileShape ts = tile_shape(nmax);
+    if (ts.mc == 0 || ts.smem > 100 * 1024) return false;
+    int tiles = 0;
+    for (int q = 0; q < ncomp; q++) {
+        const AdiArgs &A = B.a[q];
+        const int na = A.a1 - A.a0 + 1, nb = A.b1 - A.b0 + 1;
+        tiles = std::max(tiles, ((na + kTileLines - 1) / kTileLines) * nb);
+    }
+    if (tiles <= 0) return true;
+    const dim3 grid((unsigned)tiles, (unsigned)ncomp);
+    const bool per = B.a[0].periodic != 0;
+    if (dir == 2) return per ? adit_launch2<2, true>(grid, ts, c->stream, c->kp, B) : adit_launch2<2, false>(grid, ts, c->stream, c->kp, B);
+    return per ? adit_launch2<0, true>(grid, ts, c->stream, c->kp, B) : adit_launch2<0, false>(grid, ts, c->stream, c->kp, B);
+}
+
 template <class R, int W>
 static bool adis_launch(lesgpu_case *c, const AdiBatch &B, int ncomp, long long mx, int nmax, bool capped) {
     const int m = (nmax + W - 1) / W;
@@ -772,9 +1111,19 @@ static AdiShape adi_shape(const lesgpu_case *c, const AdiBatch &B, int ncomp) {
 }
 
 // launch with W = w & 63 lanes per line (w & 64: the register-capped warp-scan
-// kernel); false if W cannot hold the line (MC <= 12)
+// kernel; w == kTiled: the tiled FP32 sweep); false if that form cannot take
+// the batch (W cannot hold the line, MC <= 12; the tiled form needs FP32
+// and factored coefficients)
+constexpr int kTiled = 128;
 static bool adi_run(lesgpu_case *c, const AdiBatch &B, const AdiShape &h, int wcode) {
     if (h.mx <= 0) return true;
+    // factored coefficients unless a temperature sweep reads conjugate
+    // tables that are not all 1
+    const bool fac = !(B.a[0].comp == CT && c->kp.c.iconjg == 1 && c->conj_general);
+    if (wcode == kTiled) {
+        if (!h.f32 || !fac) return false;
+        return adit_launch(c, B, h.ncomp, h.nmax);
+    }
     const int w = wcode & 63;
     const bool capped = (wcode & 64) != 0;
     if (w <= 1) {
@@ -784,9 +1133,6 @@ static bool adi_run(lesgpu_case *c, const AdiBatch &B, const AdiShape &h, int wc
         const dim3 grid((unsigned)((h.mx + tpb - 1) / tpb), (unsigned)h.ncomp);
         const int dir = B.a[0].dir;
         const bool per = B.a[0].periodic != 0;
-        // factored coefficients unless a temperature sweep reads conjugate
-        // tables that are not all 1
-        const bool fac = !(B.a[0].comp == CT && c->kp.c.iconjg == 1 && c->conj_general);
         if (h.f32) k_adi_launch<float>(dir, per, fac, grid, tpb, c->stream, c->kp, B);
         else k_adi_launch<double>(dir, per, fac, grid, tpb, c->stream, c->kp, B);
         return true;
@@ -841,6 +1187,7 @@ static void adi_launch(lesgpu_case *c, const AdiBatch &B, int ncomp) {
         auto it = g_adi_w.find(adi_key(c, B, h));
         if (it != g_adi_w.end()) w = it->second;
     }
+    if (h.f32 && c->adi_force_f32) w = c->adi_force_f32;
     inst_begin(c, LESGPU_K_ADI);
     if (!adi_run(c, B, h, w)) adi_run(c, B, h, 1);
     inst_end(c, LESGPU_K_ADI);
@@ -868,11 +1215,12 @@ static void adi_tune_batch(lesgpu_case *c, AdiBatch B, int ncomp) {
     cudaEventCreate(&e1);
     // the register-capped warp-scan variant only differs where a lane holds
     // more than 4 rows
-    const int cand[7] = {1, 8, 16, 32, 8 | 64, 16 | 64, 32 | 64};
+    const int cand[8] = {1, 8, 16, 32, 8 | 64, 16 | 64, 32 | 64, kTiled};
     int best = adi_default_w(h);
     float best_ms = 3.0e38f;
-    for (int q = 0; q < 7; q++) {
-        if ((cand[q] & 64) && (h.nmax + (cand[q] & 63) - 1) / (cand[q] & 63) <= 4) continue;
+    for (int q = 0; q < 8; q++) {
+        if (cand[q] == kTiled && (!h.f32 || B.a[0].dir == 1)) continue;
+        if (cand[q] != kTiled && (cand[q] & 64) && (h.nmax + (cand[q] & 63) - 1) / (cand[q] & 63) <= 4) continue;
         if (!adi_run(c, B, h, cand[q])) continue;          // warm-up launch (also the feasibility check)
         cudaEventRecord(e0, c->stream);
         for (int r = 0; r < 3; r++) adi_run(c, B, h, cand[q]);
@@ -962,8 +1310,10 @@ static void adi_table_load(const char *path) {
     while (fscanf(f, "%15s %d %d %d %d %d %d %d %d %d", tag, &k.n1m, &k.n2m, &k.n3m, &k.dir, &k.ncomp, &k.f32,
                   &k.periodic, &k.nmax, &w) == 10)
         if (!strcmp(tag, "adi") && !g_adi_w.count(k)) {
-            const int wl = w & 63;    // lanes; + 64: the register-capped warp-scan kernel
-            if ((wl == 1 && w == 1) || ((wl == 8 || wl == 16 || wl == 32) && (w == wl || w == (wl | 64)))) g_adi_w[k] = w;
+            const int wl = w & 63;    // lanes; + 64: the register-capped warp-scan kernel; 128: tiled
+            if ((wl == 1 && w == 1) || ((wl == 8 || wl == 16 || wl == 32) && (w == wl || w == (wl | 64))) ||
+                w == kTiled)
+                g_adi_w[k] = w;
         }
     fclose(f);
 }

@@ -601,6 +601,12 @@ extern "C" int lesgpu_start(lesgpu_case *c) {
     if (g.ich != 0) launch_meanpg(c);
     if (g.ihtrans == 1 && g.ich == 1) launch_cvol(c);
     c->ntime_host = 0;
+    {
+        const char *ff = getenv("LESGPU_ADI_FP32_FORM");
+        const int v = ff ? atoi(ff) : 0;
+        const int wl = v & 63;
+        c->adi_force_f32 = (v == 128 || (v == 1) || ((wl == 8 || wl == 16 || wl == 32) && (v == wl || v == (wl | 64)))) ? v : 0;
+    }
     c->started = 1;
     if (c->graph_ok) { cudaGraphExecDestroy(c->graph); c->graph_ok = 0; }
     // autotuner: on unless LESGPU_AUTOTUNE=0 (a tuned choice changes the

@@ -294,6 +294,9 @@ struct lesgpu_case {
     int use_graph;
     int autotune;              // use the autotuner's choices (LESGPU_AUTOTUNE != 0 at start)
     int strict;                // lesgpu_set_strict: unconverged Poisson solves are an error
+    // LESGPU_ADI_FP32_FORM at start: the form every FP32 sweep uses (lanes
+    // per line, + 64 register-capped, 128 tiled; 0 = the autotuner's)
+    int adi_force_f32;
     // 1 once a loaded conjugate table (c*, k*, omega) holds a value other
     // than 1; while 0 the temperature sweeps use the factored coefficients
     int conj_general;
