@@ -1147,11 +1147,11 @@ __device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, double test
     return a.xft ? a.mgitr : a.mgitr + 1;
 }
 
-__global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes(MgArgs a) {
+// One cluster's solve of mode kv of the case described by a.
+__device__ __forceinline__ void zft_mode(const MgArgs &a, int kv, double2 *hbuf) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     const int cs = (int)cl.num_blocks();
-    const int kv = blockIdx.x / cs + 1;
     // warp w of block r is the cluster's warp w*cs + r: consecutive lines and
     // 32-point chunks go to different SMs (the work of a phase is spread over
     // every block, each warp still touches 32 consecutive points)
@@ -1159,7 +1159,6 @@ __global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes(MgArgs a) {
     const int tid = gw * 32 + (int)(threadIdx.x & 31), nt = cs * blockDim.x;
     Mode m(a, a.d, kv, tid, nt);
     const double test = a.fixed_cycles > 0 ? -1.0 : a.S->mg_test;
-    __shared__ __align__(16) double2 hbuf[kHalo * kHaloRows];
     const int r = (int)cl.block_rank();
     int it;
     bool unconv = false;
@@ -1183,6 +1182,23 @@ __global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes(MgArgs a) {
         // the timing runs of the autotuner fix the cycle count: not a failure
         if (unconv && a.fixed_cycles <= 0) atomicAdd((unsigned long long *)&a.S->poisson_unconv, 1ULL);
     }
+}
+
+__global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes(MgArgs a) {
+    __shared__ __align__(16) double2 hbuf[kHalo * kHaloRows];
+    const int cs = (int)cooperative_groups::this_cluster().num_blocks();
+    zft_mode(a, blockIdx.x / cs + 1, hbuf);
+}
+
+// The modes of several cases of one grid shape in one launch (the serving
+// loop's batched solve): cluster b solves mode b % nmodes + 1 of case
+// b / nmodes, each case's tables, work arrays and scalars from its own
+// MgArgs; per case the arithmetic is that of k_zft_modes.
+__global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes_batch(const MgArgs *as, int nmodes) {
+    __shared__ __align__(16) double2 hbuf[kHalo * kHaloRows];
+    const int cs = (int)cooperative_groups::this_cluster().num_blocks();
+    const int b = blockIdx.x / cs;
+    zft_mode(as[b / nmodes], b % nmodes + 1, hbuf);
 }
 
 // convergence criterion of the substep: test1 / nmodes * nfft * fac -- 0.8 in

@@ -135,9 +135,12 @@ __global__ void __launch_bounds__(kThreads) k_mirror(MirBatch b, long long nt) {
     }
 }
 
+// Refresh the FP32 mirrors of the requested sets that are out of date.
 void launch_mirror(lesgpu_case *c, unsigned sets) {
     const MirState &ms = ((CaseExtra *)c->dmem_pool)->mir;
     if (ms.n == 0) return;                       // FP64 form
+    sets &= c->mir_dirty;
+    c->mir_dirty &= ~sets;
     MirBatch b;
     b.n = 0;
     auto take = [&](int first, int count) {
@@ -171,6 +174,7 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
     c->dmem_pool = X;
     c->cfg = *cfg;
     c->use_graph = 1;
+    c->mir_dirty = ~0u;
     Alloc &A = X->alloc;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { lesgpu_destroy(c); return LESGPU_ERR_CUDA; }
 
@@ -553,6 +557,7 @@ extern "C" int lesgpu_load_ibm(lesgpu_case *c, const lesgpu_ibm *b) {
     c->kp.c.conj_tables = c->kp.c.iconjg == 1 && c->conj_general;
     if (!A.ok) return LESGPU_ERR_OOM;
     launch_red_weights(c);
+    mark_mirror(c, kMirConj);
     launch_mirror(c, kMirConj);
     return cuda_rc(cudaDeviceSynchronize());
 }
@@ -563,6 +568,7 @@ extern "C" int lesgpu_set_fields(lesgpu_case *c, const double *u, const double *
     if (!c || !u || !v || !w || !p) return LESGPU_ERR_ARG;
     size_t bytes = sizeof(double) * (size_t)c->kp.g.nt;
     DFields &f = c->kp.f;
+    mark_mirror(c, kMirVel | kMirP | kMirT);
     cudaMemcpyAsync(f.u, u, bytes, cudaMemcpyHostToDevice, c->stream);
     cudaMemcpyAsync(f.v, v, bytes, cudaMemcpyHostToDevice, c->stream);
     cudaMemcpyAsync(f.w, w, bytes, cudaMemcpyHostToDevice, c->stream);
@@ -642,11 +648,13 @@ static void enqueue_sgs(lesgpu_case *c, bool first) {
     if (first) launch_sgs_zero_first(c, 0);
     else launch_sgs(c);
     launch_sgs_post(c);
+    mark_mirror(c, kMirNu);
     launch_mirror(c, kMirNu);
     if (g.ihtrans == 1) {
         if (first) launch_sgs_zero_first(c, 1);
         else launch_sgs_t(c);
         launch_sgs_t_post(c);
+        mark_mirror(c, kMirAl);
         launch_mirror(c, kMirAl);
     }
 }
@@ -659,6 +667,7 @@ static void enqueue_rhsnlhs(lesgpu_case *c, int msub) {
     launch_adi_uvw(c);
     k_retrv_uvw<<<blocks_for((long long)c->kp.g.n2m * c->kp.g.n3m), kThreads, 0, c->stream>>>(c->kp);
     launch_ghost_uvw(c);
+    mark_mirror(c, kMirVel);
 }
 
 static void enqueue_energy(lesgpu_case *c, int msub) {
@@ -675,6 +684,7 @@ static void enqueue_energy(lesgpu_case *c, int msub) {
     if (g.ich == 1) launch_tvolcalc_corr(c, !tcalc_runs);
     launch_tcalc(c);
     if (tcalc_runs) launch_tvolcalc(c, 0);
+    mark_mirror(c, kMirT);
 }
 
 static void enqueue_step(lesgpu_case *c, bool first) {
@@ -688,6 +698,7 @@ static void enqueue_step(lesgpu_case *c, bool first) {
         launch_divgs(c);
         launch_poisson(c, msub);
         launch_ucalc_pcalc(c, g.ich == 1);        // qvolcalc(qvol(2)), ucalc, qvolcalc(qvol(0)), pcalc
+        mark_mirror(c, kMirVel | kMirP);
         if (g.ich != 0) launch_meanpg(c);
         if (g.ibmon == 1) launch_lagforce(c, msub);
         if (g.ihtrans == 1) enqueue_energy(c, msub);
@@ -699,10 +710,23 @@ static void enqueue_step(lesgpu_case *c, bool first) {
     if (g.iavg == 1) launch_field_avg(c);
 }
 
+// The out-of-date mirror sets a step leaves behind (and the captured step
+// assumes at its start): p (pcalc), and t after the energy phase's sweeps or,
+// without heat transfer, the projected velocity.
+static unsigned mir_steady(const lesgpu_case *c) { return kMirP | (c->cfg.ihtrans == 1 ? kMirT : kMirVel); }
+
+// Before a replay of the captured step: refresh eagerly what is out of date
+// beyond the steady state (after set_fields, set_array, start).
+static void mirror_prologue(lesgpu_case *c) {
+    const unsigned extra = c->mir_dirty & ~mir_steady(c);
+    if (extra) launch_mirror(c, extra);
+}
+
 // Capture one steady-state step into a CUDA graph and count its kernels.
 static int capture_step(lesgpu_case *c) {
     cudaGraph_t gr;
     if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return LESGPU_ERR_CUDA;
+    c->mir_dirty = mir_steady(c);
     enqueue_step(c, false);
     if (cudaStreamEndCapture(c->stream, &gr) != cudaSuccess) return LESGPU_ERR_CUDA;
     size_t nn = 0;
@@ -744,11 +768,13 @@ extern "C" int lesgpu_step(lesgpu_case *c, lesgpu_step_report *rep) {
     c->ntime_host += 1;
     bool first = (c->cfg.iread == 0 && c->ntime_host == 1);
     if (c->use_graph && !first && c->inst_cls == 0) {
+        mirror_prologue(c);
         if (!c->graph_ok) {
             int rc = capture_step(c);
             if (rc) return rc;
         }
         if (cudaGraphLaunch(c->graph, c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
+        c->mir_dirty = mir_steady(c);
     } else {
         enqueue_step(c, first);
     }
@@ -770,11 +796,13 @@ extern "C" int lesgpu_step_async(lesgpu_case *c, int64_t n) {
         c->ntime_host += 1;
         bool first = (c->cfg.iread == 0 && c->ntime_host == 1);
         if (c->use_graph && !first && c->inst_cls == 0) {
+            mirror_prologue(c);
             if (!c->graph_ok) {
                 int rc = capture_step(c);
                 if (rc) return rc;
             }
             if (cudaGraphLaunch(c->graph, c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
+            c->mir_dirty = mir_steady(c);
         } else {
             enqueue_step(c, first);
         }
@@ -940,6 +968,7 @@ extern "C" int lesgpu_set_array(lesgpu_case *c, int64_t fld, const double *in) {
         return 0;
     }
     for (int l = 0; l < nc; l++) cudaMemcpyAsync(ptr[l], in + l * nt, nt * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    mark_mirror(c, ~0u);
     launch_mirror(c, ~0u);
     return cuda_rc(cudaStreamSynchronize(c->stream));
 }
@@ -947,6 +976,7 @@ extern "C" int lesgpu_set_array(lesgpu_case *c, int64_t fld, const double *in) {
 extern "C" int lesgpu_run_phase(lesgpu_case *c, int64_t phase, int64_t msub) {
     if (!c || msub < 1 || msub > 3) return LESGPU_ERR_ARG;
     const lesgpu_config &g = c->cfg;
+    c->mir_dirty = ~0u;        // a phase on its own refreshes every mirror it reads
     switch (phase) {
     case LESGPU_PH_STEPINIT: launch_stepinit(c); c->ntime_host += 1; break;
     case LESGPU_PH_SUBSTEPINIT: launch_substepinit(c, (int)msub); break;

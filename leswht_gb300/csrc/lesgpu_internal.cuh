@@ -297,6 +297,10 @@ struct lesgpu_case {
     // LESGPU_ADI_FP32_FORM at start: the form every FP32 sweep uses (lanes
     // per line, + 64 register-capped, 128 tiled; 0 = the autotuner's)
     int adi_force_f32;
+    // FP32 mirror sets (kMir*) whose FP64 arrays changed since their last
+    // refresh, as the enqueued work stands (host-side bookkeeping of the
+    // mixed form; launch_mirror converts only these)
+    unsigned mir_dirty;
     // 1 once a loaded conjugate table (c*, k*, omega) holds a value other
     // than 1; while 0 the temperature sweeps use the factored coefficients
     int conj_general;
@@ -432,6 +436,8 @@ struct GhostSpec {
 void ghost(lesgpu_case *c, int dir, GhostSpec *s, int na);
 // refresh FP32 mirrors (mixed form; no-op in the FP64 form)
 void launch_mirror(lesgpu_case *c, unsigned sets);
+// note that enqueued work changes the FP64 arrays of `sets`
+inline void mark_mirror(lesgpu_case *c, unsigned sets) { c->mir_dirty |= sets; }
 // autotuner (k_adi.cu): time the sweep classes of this shape once per process
 int adi_autotune(lesgpu_case *c);
 // autotuner (k_fft.cu): FFT lines per block of the case's Poisson transforms
