@@ -763,16 +763,38 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
     line_coords(DIR, A.l1, x0, x1, i0, j0, k0);
     const long long qb = g.ix(i0, j0, k0);                // row 0 of line 0
     const AdiFacs<R> F = adi_facs<R>(p, A.comp, DIR);
-    // ---- stage the tile (z: lines fastest, x: rows fastest: both coalesced)
+    // ---- stage the tile (z: lines fastest, x: rows fastest: both coalesced);
+    // each thread issues the loads of four elements before it stores them
     const int nt = blockDim.x;
-    for (int t = threadIdx.x; t < kTileLines * (n + 1); t += nt) {
-        int w, r;
-        if (DIR == 2) { w = t % kTileLines; r = t / kTileLines; }
-        else { w = t / (n + 1); r = t % (n + 1); }
-        if (w >= nl) continue;
-        const long long q = qb + w * lstride + (long long)r * stride;
-        Fv[w * lp + tpos(r, m, pm)] = R(1.0) + F.cre * R(F.nv[q + F.oa]);
-        if (r < n) S[w * lp + tpos(r, m, pm)] = diag * R(A.src[q]);
+    const int ntot = kTileLines * (n + 1);
+    for (int t0 = threadIdx.x; t0 < ntot; t0 += 4 * nt) {
+        double sv[4];
+        R fv[4];
+        int pos[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int t = t0 + u * nt;
+            pos[u] = -1;
+            if (t < ntot) {
+                int w, r;
+                if (DIR == 2) { w = t % kTileLines; r = t / kTileLines; }
+                else { w = t / (n + 1); r = t % (n + 1); }
+                if (w < nl) {
+                    const long long q = qb + w * lstride + (long long)r * stride;
+                    pos[u] = w * lp + tpos(r, m, pm);
+                    fv[u] = R(F.nv[q + F.oa]);
+                    sv[u] = r < n ? A.src[q] : 0.0;
+                    if (r >= n) pos[u] = -2 - pos[u];      // the factor row only
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (pos[u] == -1) continue;
+            const int ps = pos[u] >= 0 ? pos[u] : -2 - pos[u];
+            Fv[ps] = R(1.0) + F.cre * fv[u];
+            if (pos[u] >= 0) S[ps] = diag * R(sv[u]);
+        }
     }
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -993,16 +1015,30 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
         }
     }
     __syncthreads();
-    // ---- write back: the solution, or added to the field
-    for (int t = threadIdx.x; t < kTileLines * n; t += nt) {
-        int w2, r;
-        if (DIR == 2) { w2 = t % kTileLines; r = t / kTileLines; }
-        else { w2 = t / n; r = t % n; }
-        if (w2 >= nl) continue;
-        const long long q = qb + w2 * lstride + (long long)r * stride;
-        const R x = S[w2 * lp + tpos(r, m, pm)];
-        if (A.add) A.dst[q] = A.dst[q] + x;
-        else A.dst[q] = x;
+    // ---- write back: the solution, or added to the field (four elements a
+    // thread at a time, the field's loads first)
+    for (int t0 = threadIdx.x; t0 < kTileLines * n; t0 += 4 * nt) {
+        long long qv[4];
+        double dv[4];
+        R xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int t = t0 + u * nt;
+            qv[u] = -1;
+            if (t < kTileLines * n) {
+                int w2, r;
+                if (DIR == 2) { w2 = t % kTileLines; r = t / kTileLines; }
+                else { w2 = t / n; r = t % n; }
+                if (w2 < nl) {
+                    qv[u] = qb + w2 * lstride + (long long)r * stride;
+                    xv[u] = S[w2 * lp + tpos(r, m, pm)];
+                    if (A.add) dv[u] = A.dst[qv[u]];
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (qv[u] >= 0) A.dst[qv[u]] = A.add ? dv[u] + xv[u] : (double)xv[u];
     }
 }
 

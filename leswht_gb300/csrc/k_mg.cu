@@ -333,113 +333,24 @@ __device__ void mg_shift_odd(const ModeT<T> &m, typename V2<T>::t *u, int ld, ty
     }
 }
 
-// The top level's zebra relaxation (both halves, with the zero wavenumber's
-// pin) into G: poiss_z_ft.f90:331-357 / poiss_x_ft.f90:320-344.  The odd
-// lines take their neighbours from P scaled by oldv; src_rhs: the source is
-// the right-hand side plane (else R's top level).
-template <class T>
-__device__ void mg_top_relax(const ModeT<T> &m, T oldv, bool src_rhs) {
-    using V = typename V2<T>::t;
-    const MgArgs &a = m.a;
-    const int n1m = a.nl, n2m = a.n2m;
-    const V zero = V{T(0.0), T(0.0)};
-    mg_half<kMC, T>(m, 1, n1m, H_ODD, src_rhs, m.pc, a.ldp, oldv, zero, false, T(0.0), T(0.0));
-    m.sync();
-    if (a.xft) {
-        // poiss_x_ft: shift the odd lines by ggii(1,n2m), then form the even
-        // lines from the shifted values as rhs - (ab*g + af*g)
-        if (m.kv == 1) {
-            const V tt = m.G(1, n2m);
-            m.sync();
-            mg_shift_odd(m, m.gg, a.ldg, tt);
-            m.sync();
-        }
-        mg_half<kMC, T>(m, 2, n1m, H_ODD, src_rhs, m.gg, a.ldg, T(1.0), zero, false, T(0.0), T(0.0));
-        m.sync();
-    } else {
-        // poiss_z_ft: the even lines see the odd ones shifted by ggii(1,n2m-1)
-        // inside their right-hand side; the odd lines are shifted afterwards
-        const V tt = m.kv == 1 ? m.G(1, n2m - 1) : zero;
-        mg_half<kMC, T>(m, 2, n1m, H_EVEN_TT, src_rhs, m.gg, a.ldg, T(1.0), tt, false, T(0.0), T(0.0));
-        m.sync();
-        if (m.kv == 1) mg_shift_odd(m, m.gg, a.ldg, tt);
-        m.sync();
-    }
-}
-
-// Restrict the top level's residual (R) onto level nlev-1
-template <class T>
-__device__ void mg_top_restrict(const ModeT<T> &m) {
-    const MgArgs &a = m.a;
-    const int cl = a.iimg[a.nlev - 1][0], nc = a.iimg[a.nlev - 1][1] - cl + 1;
-    for (int t = m.tid; t < nc * a.n2m; t += m.nt) {
-        const int i = cl + t % nc, j = 1 + t / nc, ic = 2 * (i - cl) + 1;
-        const typename V2<T>::t r1 = m.R(ic, j), r2 = m.R(ic + 1, j);
-        m.R(i, j) = typename V2<T>::t{r1.x * m.s.cor1[i] + r2.x * m.s.cor2[i], r1.y * m.s.cor1[i] + r2.y * m.s.cor2[i]};
-    }
-    m.sync();
-}
-
-// The coarse correction of level nlev-1 interpolated onto the top level's
-// even lines: P += (FP64 form) or P = (the mixed form's correction).
-template <class T>
-__device__ void mg_top_prolong(const ModeT<T> &m, bool assign) {
-    const MgArgs &a = m.a;
-    const MgSet<T> &s = m.s;
-    const int cl = a.iimg[a.nlev - 1][0], ce = a.iimg[a.nlev - 1][1], nc = ce - cl + 1;
-    for (int t = m.tid; t < nc * a.n2m; t += m.nt) {
-        const int i = cl + t % nc, j = 1 + t / nc, ic = 2 * (i - cl + 1);
-        typename V2<T>::t p = assign ? typename V2<T>::t{T(0.0), T(0.0)} : m.P(ic, j);
-        const typename V2<T>::t g1 = m.G(i, j);
-        if (i < ce || a.xft) {
-            const typename V2<T>::t g2 = m.G(a.ipm[i], j);
-            p = typename V2<T>::t{p.x + s.coi1[i] * g1.x + s.coi2[i] * g2.x, p.y + s.coi1[i] * g1.y + s.coi2[i] * g2.y};
-        } else {
-            p = typename V2<T>::t{p.x + s.coi1[i] * g1.x, p.y + s.coi1[i] * g1.y};
-        }
-        m.P(ic, j) = p;
-    }
-    m.sync();
-}
-
-// toplevel, poiss_z_ft.f90:302-380 / poiss_x_ft.f90:296-371; returns the max-norm residual
-__device__ double mg_toplevel(const Mode &m, int id, double oldv, double test) {
-    const MgArgs &a = m.a;
-    const int n1m = a.nl, n2m = a.n2m, nt = m.nt;
-    if (id == 1) mg_top_prolong(m, false);   // prolong the coarse correction onto the even lines
-    mg_top_relax(m, oldv, true);
-    double mx = 0.0;
-    for (int t = m.tid; t < n1m * n2m; t += nt) {
-        const int i = 1 + t % n1m, j = 1 + t / n1m;
-        const double2 d = mg_defect(m, m.B(i, j), m.gg, a.ldg, i, j);
-        m.R(i, j) = d;
-        mx = fmax(mx, d.x * d.x + d.y * d.y);
-        m.P(i, j) = m.G(i, j);
-    }
-    const double sumres = sqrt(cluster_max(mx));
-    if (sumres < test) return sumres;
-    mg_top_restrict(m);
-    return sumres;
-}
-
 // relax, poiss_z_ft.f90:466-511 (zebra version)
-template <class T>
-__device__ void mg_relax(const ModeT<T> &m, int ilev, T oldv, int iiter) {
+template <int MC, class T>
+__device__ __noinline__ void mg_relax(const ModeT<T> &m, int ilev, T oldv, int iiter) {
     const MgArgs &a = m.a;
     const int ibg = a.iimg[ilev][0], iend = a.iimg[ilev][1];
     const typename V2<T>::t zero{T(0.0), T(0.0)};
     for (int it = 0; it < iiter; it++) {
         const T ov = it == 0 ? oldv : T(1.0);
-        mg_half<kMC, T>(m, ibg, iend, H_ODD, false, m.gg, a.ldg, ov, zero, false, T(0.0), T(0.0));
+        mg_half<MC, T>(m, ibg, iend, H_ODD, false, m.gg, a.ldg, ov, zero, false, T(0.0), T(0.0));
         m.sync();
-        mg_half<kMC, T>(m, ibg + 1, iend, H_EVEN, false, m.gg, a.ldg, T(1.0), zero, false, T(0.0), T(0.0));
+        mg_half<MC, T>(m, ibg + 1, iend, H_EVEN, false, m.gg, a.ldg, T(1.0), zero, false, T(0.0), T(0.0));
         m.sync();
     }
 }
 
 // godown, poiss_z_ft.f90:438-463
 template <class T>
-__device__ void mg_godown(const ModeT<T> &m, int ilev) {
+__device__ __noinline__ void mg_godown(const ModeT<T> &m, int ilev) {
     const MgArgs &a = m.a;
     const int ibg = a.iimg[ilev][0], iend = a.iimg[ilev][1], n2m = a.n2m, nt = m.nt;
     const int nf = iend - ibg + 1;
@@ -459,7 +370,7 @@ __device__ void mg_godown(const ModeT<T> &m, int ilev) {
 
 // goup, poiss_z_ft.f90:411-435 / poiss_x_ft.f90:401-419
 template <class T>
-__device__ void mg_goup(const ModeT<T> &m, int ilev) {
+__device__ __noinline__ void mg_goup(const ModeT<T> &m, int ilev) {
     const MgArgs &a = m.a;
     const MgSet<T> &s = m.s;
     const int cl = a.iimg[ilev][0], ce = a.iimg[ilev][1], n2m = a.n2m, nt = m.nt;
@@ -479,107 +390,9 @@ __device__ void mg_goup(const ModeT<T> &m, int ilev) {
     m.sync();
 }
 
-// mg2d, poiss_z_ft.f90:239-299
-__device__ int mg_mg2d(const Mode &m, double test, bool &unconv) {
-    const MgArgs &a = m.a;
-    double sumres = mg_toplevel(m, 0, 0.0, test);
-    if (sumres < test) return 0;
-    for (int kk = 1; kk <= a.mgitr; kk++) {
-        for (int ilev = a.nlev - 1; ilev >= 1; ilev--) {
-            mg_relax(m, ilev, 0.0, 1);
-            mg_godown(m, ilev);
-        }
-        mg_relax(m, 0, 0.0, a.nbli);
-        for (int ilev = 0; ilev <= a.nlev - 2; ilev++) {
-            mg_goup(m, ilev);
-            mg_relax(m, ilev + 1, 1.0, 1);
-        }
-        sumres = mg_toplevel(m, 1, 1.0, test);
-        if (sumres < test) return kk;
-    }
-    unconv = true;
-    // iteration limit: the reference warns and goes on; its cycle counter
-    // has then run past the loop (mgitr + 1 in poiss_z_ft.f90:271-289)
-    return a.xft ? a.mgitr : a.mgitr + 1;
-}
-
-// The mixed form's toplevel: the top-level relaxation runs in FP32 on the
-// correction e (source r, the FP64 residual rounded to FP32; P holds the
-// prolonged coarse correction), then in FP64 x += e and r = b - A x, whose
-// max norm is the reference's convergence test.  By the linearity of the
-// zebra relaxation, x + relax(P g; r) is the reference's relax(x + P g; b):
-// the cycle is the reference's, with the correction carried in FP32.
-__device__ double mg_top_mixed(const Mode &m, const ModeT<float> &f, int id, double test) {
-    const MgArgs &a = m.a;
-    const int n1m = a.nl, n2m = a.n2m, nt = m.nt;
-    if (id == 1) mg_top_prolong(f, true);
-    mg_top_relax(f, id == 1 ? 1.0f : 0.0f, false);
-    for (int t = m.tid; t < n1m * n2m; t += nt) {           // x += e (x = e on the first pass)
-        const int i = 1 + t % n1m, j = 1 + t / n1m;
-        const float2 e = f.G(i, j);
-        const double2 x = id == 0 ? make_double2(0.0, 0.0) : m.P(i, j);
-        m.P(i, j) = make_double2(x.x + (double)e.x, x.y + (double)e.y);
-    }
-    m.sync();
-    double mx = 0.0;
-    for (int t = m.tid; t < n1m * n2m; t += nt) {           // r = b - A x in FP64
-        const int i = 1 + t % n1m, j = 1 + t / n1m;
-        const double2 d = mg_defect(m, m.B(i, j), m.pc, a.ldp, i, j);
-        f.R(i, j) = make_float2((float)d.x, (float)d.y);
-        mx = fmax(mx, d.x * d.x + d.y * d.y);
-    }
-    const double sumres = sqrt(cluster_max(mx));
-    if (sumres < test) return sumres;
-    mg_top_restrict(f);
-    return sumres;
-}
-
-// mg2d in the mixed form: the V-cycle of mg_mg2d with every level but the
-// coarsest relaxed in FP32, the coarsest in FP64, and the residual, the
-// solution and the convergence test in FP64 (mg_top_mixed).
-__device__ int mg_mg2d_mixed(const Mode &m, const ModeT<float> &f, double test, bool &unconv) {
-    const MgArgs &a = m.a;
-    const int n2m = a.n2m, nt = m.nt;
-    for (int t = m.tid; t < a.nl * n2m; t += nt) {          // the first source is b itself
-        const int i = 1 + t % a.nl, j = 1 + t / a.nl;
-        const double2 b = m.B(i, j);
-        f.R(i, j) = make_float2((float)b.x, (float)b.y);
-    }
-    m.sync();
-    double sumres = mg_top_mixed(m, f, 0, test);
-    if (sumres < test) return 0;
-    const int c0 = a.iimg[0][0], nc0 = a.iimg[0][1] - c0 + 1;
-    for (int kk = 1; kk <= a.mgitr; kk++) {
-        for (int ilev = a.nlev - 1; ilev >= 1; ilev--) {
-            mg_relax(f, ilev, 0.0f, 1);
-            mg_godown(f, ilev);
-        }
-        for (int t = m.tid; t < nc0 * n2m; t += nt) {       // coarsest level in FP64
-            const int i = c0 + t % nc0, j = 1 + t / nc0;
-            const float2 r = f.R(i, j);
-            m.R(i, j) = make_double2((double)r.x, (double)r.y);
-        }
-        m.sync();
-        mg_relax(m, 0, 0.0, a.nbli);
-        for (int t = m.tid; t < nc0 * n2m; t += nt) {
-            const int i = c0 + t % nc0, j = 1 + t / nc0;
-            const double2 g = m.G(i, j);
-            f.G(i, j) = make_float2((float)g.x, (float)g.y);
-        }
-        m.sync();
-        for (int ilev = 0; ilev <= a.nlev - 2; ilev++) {
-            mg_goup(f, ilev);
-            mg_relax(f, ilev + 1, 1.0f, 1);
-        }
-        sumres = mg_top_mixed(m, f, 1, test);
-        if (sumres < test) return kk;
-    }
-    unconv = true;
-    return a.xft ? a.mgitr : a.mgitr + 1;
-}
-
 // gsor2d + resid3, poiss_z_ft.f90:513-641 / poiss_x_ft.f90:497-642 (pc is the iterate u)
-__device__ int mg_gsor2d(const Mode &m, double test, bool &unconv) {
+template <int MC>
+__device__ __noinline__ int mg_gsor2d(const Mode &m, double test, bool &unconv) {
     const MgArgs &a = m.a;
     const int n1m = a.nl, n2m = a.n2m, nt = m.nt;
     const double ww = a.wwsor, ww2 = 1.0 - ww;
@@ -587,7 +400,7 @@ __device__ int mg_gsor2d(const Mode &m, double test, bool &unconv) {
         const double ov = kk == 0 ? 0.0 : 1.0, o2 = ov * ww2;
         for (int half = 0; half < 2; half++) {
             const double f = half == 0 ? ov : 1.0;
-            mg_half<kMC, double>(m, 1 + half, n1m, H_ODD, true, m.pc, a.ldp, f, make_double2(0.0, 0.0), true, ww, o2);
+            mg_half<MC, double>(m, 1 + half, n1m, H_ODD, true, m.pc, a.ldp, f, make_double2(0.0, 0.0), true, ww, o2);
             m.sync();
             if (half == 0 && a.xft && m.kv == 1) {     // poiss_x_ft pins the zero wavenumber by u(1,n2m)
                 const double2 tt = m.P(1, n2m);
@@ -789,8 +602,8 @@ __device__ __forceinline__ void hinit(int (&l)[kHalo]) {
 // One level down (relax(ilev, 0, 1) + godown(ilev)) on a partitioned level:
 // restricted residual R -> relaxed G (own lines), defect -> D, restricted
 // defect -> R of level ilev - 1 (own coarse lines).  Ends at the cluster barrier.
-template <class T>
-__device__ void part_down(const ModeT<T> &m, int ilev, int r, int cs, typename V2<T>::t *hbuf) {
+template <int MC, class T>
+__device__ __noinline__ void part_down(const ModeT<T> &m, int ilev, int r, int cs, typename V2<T>::t *hbuf) {
     using V = typename V2<T>::t;
     const MgArgs &a = m.a;
     const Part pt = part_of(a.iimg[ilev][0], a.iimg[ilev][1], r, cs);
@@ -808,9 +621,9 @@ __device__ void part_down(const ModeT<T> &m, int ilev, int r, int cs, typename V
         xe[nxe++] = l1;
     }
     const V zero{T(0.0), T(0.0)};
-    part_half<kMC, T>(m, pt, 0, xo, nxo, H_ODD, m.rs, m.gg, a.ldg, m.gg, a.ldg, h, T(0.0), zero);
+    part_half<MC, T>(m, pt, 0, xo, nxo, H_ODD, m.rs, m.gg, a.ldg, m.gg, a.ldg, h, T(0.0), zero);
     __syncthreads();
-    part_half<kMC, T>(m, pt, 1, xe, nxe, H_EVEN, m.rs, m.gg, a.ldg, m.gg, a.ldg, h, T(1.0), zero);
+    part_half<MC, T>(m, pt, 1, xe, nxe, H_EVEN, m.rs, m.gg, a.ldg, m.gg, a.ldg, h, T(1.0), zero);
     __syncthreads();
     const int nown = pt.b - pt.a + 1;
     for (int t = threadIdx.x; t < nown * n2m; t += blockDim.x) {
@@ -831,8 +644,8 @@ __device__ void part_down(const ModeT<T> &m, int ilev, int r, int cs, typename V
 // One level up (goup(ilev) + relax(ilev + 1, 1, 1)) onto a partitioned
 // level: prolonged even lines (own -> U, halo), relaxation against the
 // level's defect D.  Ends at the cluster barrier.
-template <class T>
-__device__ void part_up(const ModeT<T> &m, int ilev, int r, int cs, typename V2<T>::t *hbuf) {
+template <int MC, class T>
+__device__ __noinline__ void part_up(const ModeT<T> &m, int ilev, int r, int cs, typename V2<T>::t *hbuf) {
     using V = typename V2<T>::t;
     const MgArgs &a = m.a;
     const int F = ilev + 1;
@@ -863,9 +676,9 @@ __device__ void part_up(const ModeT<T> &m, int ilev, int r, int cs, typename V2<
     }
     __syncthreads();
     const V zero{T(0.0), T(0.0)};
-    part_half<kMC, T>(m, pt, 0, xo, nxo, H_ODD, m.rd, m.gu, a.ldg, m.gg, a.ldg, h, T(1.0), zero);
+    part_half<MC, T>(m, pt, 0, xo, nxo, H_ODD, m.rd, m.gu, a.ldg, m.gg, a.ldg, h, T(1.0), zero);
     __syncthreads();
-    part_half<kMC, T>(m, pt, 1, xo, 0, H_EVEN, m.rd, m.gg, a.ldg, m.gg, a.ldg, h, T(1.0), zero);
+    part_half<MC, T>(m, pt, 1, xo, 0, H_EVEN, m.rd, m.gg, a.ldg, m.gg, a.ldg, h, T(1.0), zero);
     cooperative_groups::this_cluster().sync();
 }
 
@@ -876,8 +689,8 @@ __device__ void part_up(const ModeT<T> &m, int ilev, int r, int cs, typename V2<
 // right-hand side plane (null) or the FP32 residual.  The mixed form then
 // adds the correction to the FP64 solution of its own lines.  Ends at the
 // cluster barrier.
-template <class T>
-__device__ void part_top_relax(const ModeT<T> &m, int r, int cs, T oldv, bool prolong, bool assign,
+template <int MC, class T>
+__device__ __noinline__ void part_top_relax(const ModeT<T> &m, int r, int cs, T oldv, bool prolong, bool assign,
                                const typename V2<T>::t *src, typename V2<T>::t *hbuf, const Mode *x64, bool first) {
     using V = typename V2<T>::t;
     const MgArgs &a = m.a;
@@ -924,7 +737,7 @@ __device__ void part_top_relax(const ModeT<T> &m, int r, int cs, T oldv, bool pr
     const V zero{T(0.0), T(0.0)};
     // odd lines: neighbours are the even lines' prolonged values (U, halo),
     // or P outside the level
-    part_half<kMC, T>(m, pt, 0, xo, nxo, H_ODD, src, prolong ? m.gu : m.pc, prolong ? a.ldg : a.ldp, m.pc, a.ldp, h,
+    part_half<MC, T>(m, pt, 0, xo, nxo, H_ODD, src, prolong ? m.gu : m.pc, prolong ? a.ldg : a.ldp, m.pc, a.ldp, h,
                       oldv, zero);
     __syncthreads();
     auto gval = [&](int i, int j) -> V {
@@ -946,14 +759,14 @@ __device__ void part_top_relax(const ModeT<T> &m, int r, int cs, T oldv, bool pr
             }
             __syncthreads();
         }
-        part_half<kMC, T>(m, pt, 1, xe, 0, H_ODD, src, m.gg, a.ldg, m.gg, a.ldg, h, T(1.0), zero);
+        part_half<MC, T>(m, pt, 1, xe, 0, H_ODD, src, m.gg, a.ldg, m.gg, a.ldg, h, T(1.0), zero);
         __syncthreads();
     } else {
         // poiss_z_ft: the even lines see the odd ones shifted by
         // ggii(1,n2m-1) inside their right-hand side; the odd lines are
         // shifted afterwards
         const V tt = pin ? gval(1, n2m - 1) : zero;
-        part_half<kMC, T>(m, pt, 1, xe, 0, H_EVEN_TT, src, m.gg, a.ldg, m.gg, a.ldg, h, T(1.0), tt);
+        part_half<MC, T>(m, pt, 1, xe, 0, H_EVEN_TT, src, m.gg, a.ldg, m.gg, a.ldg, h, T(1.0), tt);
         __syncthreads();
         if (pin) {
             const int no = (pt.b - pt.a + 1) / 2;
@@ -1004,7 +817,7 @@ __device__ double part_cluster_max(double v, int par) {
 // toplevel's residual on the partitioned top level (FP64 form): R = B - A G
 // on the own lines, P = G, the residual restricted onto level nlev-1 (own
 // coarse lines), the max norm over the cluster.
-__device__ double part_top_resid(const Mode &m, int r, int cs, int par) {
+__device__ __noinline__ double part_top_resid(const Mode &m, int r, int cs, int par) {
     const MgArgs &a = m.a;
     const Part pt = part_of(1, a.nl, r, cs);
     const int n2m = a.n2m, nown = pt.b - pt.a + 1;
@@ -1031,7 +844,7 @@ __device__ double part_top_resid(const Mode &m, int r, int cs, int par) {
 
 // the mixed form's residual: r = b - A x in FP64 (x in m.P) -> the FP32
 // residual f.R, restricted in FP32 onto level nlev-1; the max norm
-__device__ double part_top_resid_mixed(const Mode &m, const ModeT<float> &f, int r, int cs, int par) {
+__device__ __noinline__ double part_top_resid_mixed(const Mode &m, const ModeT<float> &f, int r, int cs, int par) {
     const MgArgs &a = m.a;
     const Part pt = part_of(1, a.nl, r, cs);
     const int n2m = a.n2m, nown = pt.b - pt.a + 1;
@@ -1053,31 +866,32 @@ __device__ double part_top_resid_mixed(const Mode &m, const ModeT<float> &f, int
 }
 
 // mg2d (poiss_z_ft.f90:239-299) with the level-partitioned phases
+template <int MC>
 __device__ int part_mg2d(const Mode &m, double test, bool &unconv, int r, int cs, double2 *hbuf) {
     const MgArgs &a = m.a;
     const int nlev = a.nlev, lc = a.lc;
     int par = 0;
-    part_top_relax(m, r, cs, 0.0, false, false, nullptr, hbuf, nullptr, true);
+    part_top_relax<MC>(m, r, cs, 0.0, false, false, nullptr, hbuf, nullptr, true);
     double sumres = part_top_resid(m, r, cs, par);
     par ^= 1;
     if (sumres < test) return 0;
     const Mode mb(a, a.d, m.kv, threadIdx.x, blockDim.x, true);
     for (int kk = 1; kk <= a.mgitr; kk++) {
-        for (int ilev = nlev - 1; ilev > lc; ilev--) part_down(m, ilev, r, cs, hbuf);
+        for (int ilev = nlev - 1; ilev > lc; ilev--) part_down<MC>(m, ilev, r, cs, hbuf);
         if (r == 0) {
             for (int ilev = lc; ilev >= 1; ilev--) {
-                mg_relax(mb, ilev, 0.0, 1);
+                mg_relax<MC>(mb, ilev, 0.0, 1);
                 mg_godown(mb, ilev);
             }
-            mg_relax(mb, 0, 0.0, a.nbli);
+            mg_relax<MC>(mb, 0, 0.0, a.nbli);
             for (int ilev = 0; ilev < lc; ilev++) {
                 mg_goup(mb, ilev);
-                mg_relax(mb, ilev + 1, 1.0, 1);
+                mg_relax<MC>(mb, ilev + 1, 1.0, 1);
             }
         }
         cooperative_groups::this_cluster().sync();
-        for (int ilev = lc; ilev <= nlev - 2; ilev++) part_up(m, ilev, r, cs, hbuf);
-        part_top_relax(m, r, cs, 1.0, true, false, nullptr, hbuf, nullptr, false);
+        for (int ilev = lc; ilev <= nlev - 2; ilev++) part_up<MC>(m, ilev, r, cs, hbuf);
+        part_top_relax<MC>(m, r, cs, 1.0, true, false, nullptr, hbuf, nullptr, false);
         sumres = part_top_resid(m, r, cs, par);
         par ^= 1;
         if (sumres < test) return kk;
@@ -1087,6 +901,7 @@ __device__ int part_mg2d(const Mode &m, double test, bool &unconv, int r, int cs
 }
 
 // mg_mg2d_mixed with the level-partitioned phases
+template <int MC>
 __device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, double test, bool &unconv, int r, int cs,
                                double2 *hbuf) {
     const MgArgs &a = m.a;
@@ -1104,7 +919,7 @@ __device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, double test
         }
         cooperative_groups::this_cluster().sync();
     }
-    part_top_relax(f, r, cs, 0.0f, false, true, f.rs, hf, &m, true);
+    part_top_relax<MC>(f, r, cs, 0.0f, false, true, f.rs, hf, &m, true);
     double sumres = part_top_resid_mixed(m, f, r, cs, par);
     par ^= 1;
     if (sumres < test) return 0;
@@ -1112,10 +927,10 @@ __device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, double test
     const Mode mb(a, a.d, m.kv, threadIdx.x, blockDim.x, true);
     const int c0 = a.iimg[0][0], nc0 = a.iimg[0][1] - c0 + 1;
     for (int kk = 1; kk <= a.mgitr; kk++) {
-        for (int ilev = nlev - 1; ilev > lc; ilev--) part_down(f, ilev, r, cs, hf);
+        for (int ilev = nlev - 1; ilev > lc; ilev--) part_down<MC>(f, ilev, r, cs, hf);
         if (r == 0) {
             for (int ilev = lc; ilev >= 1; ilev--) {
-                mg_relax(fb, ilev, 0.0f, 1);
+                mg_relax<MC>(fb, ilev, 0.0f, 1);
                 mg_godown(fb, ilev);
             }
             for (int t = threadIdx.x; t < nc0 * n2m; t += blockDim.x) {     // coarsest level in FP64
@@ -1124,7 +939,7 @@ __device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, double test
                 mb.R(i, j) = make_double2((double)rr.x, (double)rr.y);
             }
             __syncthreads();
-            mg_relax(mb, 0, 0.0, a.nbli);
+            mg_relax<MC>(mb, 0, 0.0, a.nbli);
             for (int t = threadIdx.x; t < nc0 * n2m; t += blockDim.x) {
                 const int i = c0 + t % nc0, j = 1 + t / nc0;
                 const double2 g = mb.G(i, j);
@@ -1133,12 +948,12 @@ __device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, double test
             __syncthreads();
             for (int ilev = 0; ilev < lc; ilev++) {
                 mg_goup(fb, ilev);
-                mg_relax(fb, ilev + 1, 1.0f, 1);
+                mg_relax<MC>(fb, ilev + 1, 1.0f, 1);
             }
         }
         cooperative_groups::this_cluster().sync();
-        for (int ilev = lc; ilev <= nlev - 2; ilev++) part_up(f, ilev, r, cs, hf);
-        part_top_relax(f, r, cs, 1.0f, true, true, f.rs, hf, &m, false);
+        for (int ilev = lc; ilev <= nlev - 2; ilev++) part_up<MC>(f, ilev, r, cs, hf);
+        part_top_relax<MC>(f, r, cs, 1.0f, true, true, f.rs, hf, &m, false);
         sumres = part_top_resid_mixed(m, f, r, cs, par);
         par ^= 1;
         if (sumres < test) return kk;
@@ -1148,6 +963,7 @@ __device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, double test
 }
 
 // One cluster's solve of mode kv of the case described by a.
+template <int MC>
 __device__ __forceinline__ void zft_mode(const MgArgs &a, int kv, double2 *hbuf) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
@@ -1163,12 +979,12 @@ __device__ __forceinline__ void zft_mode(const MgArgs &a, int kv, double2 *hbuf)
     int it;
     bool unconv = false;
     if (kv > a.imgsor) {
-        it = mg_gsor2d(m, test, unconv);
+        it = mg_gsor2d<MC>(m, test, unconv);
     } else if (a.mixed) {
         ModeT<float> f(a, a.f, kv, tid, nt);
-        it = part_mg2d_mixed(m, f, test, unconv, r, cs, hbuf);
+        it = part_mg2d_mixed<MC>(m, f, test, unconv, r, cs, hbuf);
     } else {
-        it = part_mg2d(m, test, unconv, r, cs, hbuf);
+        it = part_mg2d<MC>(m, test, unconv, r, cs, hbuf);
     }
     // the mode's solution replaces its right-hand side (ccap(i,j,kkk) = cp(i,j))
     double2 *out = a.ccap + (size_t)a.nl * a.n2m * (kv - 1);
@@ -1184,21 +1000,45 @@ __device__ __forceinline__ void zft_mode(const MgArgs &a, int kv, double2 *hbuf)
     }
 }
 
+template <int MC>
 __global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes(MgArgs a) {
     __shared__ __align__(16) double2 hbuf[kHalo * kHaloRows];
     const int cs = (int)cooperative_groups::this_cluster().num_blocks();
-    zft_mode(a, blockIdx.x / cs + 1, hbuf);
+    zft_mode<MC>(a, blockIdx.x / cs + 1, hbuf);
 }
 
 // The modes of several cases of one grid shape in one launch (the serving
 // loop's batched solve): cluster b solves mode b % nmodes + 1 of case
 // b / nmodes, each case's tables, work arrays and scalars from its own
 // MgArgs; per case the arithmetic is that of k_zft_modes.
+template <int MC>
 __global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes_batch(const MgArgs *as, int nmodes) {
     __shared__ __align__(16) double2 hbuf[kHalo * kHaloRows];
     const int cs = (int)cooperative_groups::this_cluster().num_blocks();
     const int b = blockIdx.x / cs;
-    zft_mode(as[b / nmodes], b % nmodes + 1, hbuf);
+    zft_mode<MC>(as[b / nmodes], b % nmodes + 1, hbuf);
+}
+
+// the instance for y lines of n2m cells: MC = ceil(n2m / 32) rounded up to
+// 2, 4, 6 or 8 rows per lane (fewer registers, no spills, on shorter lines)
+inline int mg_mc(int n2m) { return n2m <= 64 ? 2 : n2m <= 128 ? 4 : n2m <= 192 ? 6 : 8; }
+typedef void (*ZftKernel)(MgArgs);
+inline ZftKernel zft_kernel(int n2m) {
+    switch (mg_mc(n2m)) {
+    case 2: return k_zft_modes<2>;
+    case 4: return k_zft_modes<4>;
+    case 6: return k_zft_modes<6>;
+    default: return k_zft_modes<8>;
+    }
+}
+typedef void (*ZftBatchKernel)(const MgArgs *, int);
+inline ZftBatchKernel zft_batch_kernel(int n2m) {
+    switch (mg_mc(n2m)) {
+    case 2: return k_zft_modes_batch<2>;
+    case 4: return k_zft_modes_batch<4>;
+    case 6: return k_zft_modes_batch<6>;
+    default: return k_zft_modes_batch<8>;
+    }
 }
 
 // convergence criterion of the substep: test1 / nmodes * nfft * fac -- 0.8 in
@@ -1484,7 +1324,9 @@ int mg2d_init(lesgpu_case *c) {
     // Cluster size: the mode solves are FP64-throughput bound (a GB300 SM
     // retires few FP64 FMAs per clock), so each mode gets as many SMs as the
     // GPU can co-schedule for all modes: minimise waves / blocks-per-mode.
-    cudaFuncSetAttribute(k_zft_modes, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    const ZftKernel kz = zft_kernel(g.n2m);
+    cudaFuncSetAttribute(kz, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute(zft_batch_kernel(g.n2m), cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     T->cs = 1;
     double best = 1e300;
     const int cands[5] = {16, 8, 4, 2, 1};
@@ -1495,7 +1337,7 @@ int mg2d_init(lesgpu_case *c) {
         cudaLaunchAttribute at[1];
         cluster_cfg(lc, at, nmodes, cs);
         int nact = 0;
-        if (cudaOccupancyMaxActiveClusters(&nact, k_zft_modes, &lc) != cudaSuccess || nact < 1) {
+        if (cudaOccupancyMaxActiveClusters(&nact, kz, &lc) != cudaSuccess || nact < 1) {
             cudaGetLastError();
             continue;
         }
@@ -1562,7 +1404,7 @@ static void launch_modes(lesgpu_case *c, const MgArgs &a, int cs, int nmodes = 0
     cudaLaunchAttribute at[1];
     cluster_cfg(lc, at, nmodes > 0 ? nmodes : c->pois.mg->nmodes, cs);
     lc.stream = c->stream;
-    cudaLaunchKernelEx(&lc, k_zft_modes, a);
+    cudaLaunchKernelEx(&lc, zft_kernel(c->kp.g.n2m), a);
 }
 
 // can a cluster of cs blocks be scheduled at all
@@ -1571,7 +1413,7 @@ static bool cluster_fits(lesgpu_case *c, int cs) {
     cudaLaunchAttribute at[1];
     cluster_cfg(lc, at, c->pois.mg->nmodes, cs);
     int nact = 0;
-    if (cudaOccupancyMaxActiveClusters(&nact, k_zft_modes, &lc) != cudaSuccess) { cudaGetLastError(); return false; }
+    if (cudaOccupancyMaxActiveClusters(&nact, zft_kernel(c->kp.g.n2m), &lc) != cudaSuccess) { cudaGetLastError(); return false; }
     return nact >= 1;
 }
 
