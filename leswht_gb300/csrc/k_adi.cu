@@ -831,6 +831,10 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
             R P, Q;
             scan_moebius<R, 32>(T, lane, P, Q);
             R bet = (lane == 0) ? R(0.0) : P / Q;
+            // gm of the chunk's first row, c_{r0-1} times the scanned pivot
+            // (k_adis keeps it, and the previous chunk's last row uses it)
+            const R gm_first = (lane == 0) ? R(0.0) : cprev0 * bet;
+            const R gnext0 = __shfl_down_sync(0xffffffffu, gm_first, 1);
             R betv[MC];
             {
                 R cp = cprev0;
@@ -874,7 +878,7 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
                 if (u < cnt) {
                     R a, c;
                     coef(r0 + u, a, c);
-                    const R gn = (r0 + u == n - 1) ? R(0.0) : c * betv[u];
+                    const R gn = (r0 + u == n - 1) ? R(0.0) : (u + 1 < cnt ? c * betv[u] : gnext0);
                     Dd = -gn * Dd + Sl[tpos(r0 + u, m, pm)];
                     Cc = -gn * Cc;
                 }
@@ -884,7 +888,7 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
                 if (u < cnt) {
                     R a, c;
                     coef(r0 + u, a, c);
-                    const R gn = (r0 + u == n - 1) ? R(0.0) : c * betv[u];
+                    const R gn = (r0 + u == n - 1) ? R(0.0) : (u + 1 < cnt ? c * betv[u] : gnext0);
                     const int ps = tpos(r0 + u, m, pm);
                     x = Sl[ps] - gn * x;
                     Sl[ps] = x;

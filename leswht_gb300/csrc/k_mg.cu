@@ -28,6 +28,7 @@
 // order and uploaded once.
 #include "k_fft.cuh"
 #include <cooperative_groups.h>
+#include <new>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -38,7 +39,11 @@
 
 namespace lg {
 
-constexpr int kMgThreads = 512;
+// threads per block: 256, so a thread may hold up to 255 registers -- the
+// 128 of a 512-thread block spill the sweeps' line arrays and the values
+// live across the phase calls to local memory, which 512 threads' stacks
+// push out of L1
+constexpr int kMgThreads = 256;
 constexpr int kMC = 8;            // rows per lane: y lines of up to 32 * kMC = 256 cells
 constexpr int kMaxLev = 20;
 
@@ -104,18 +109,22 @@ struct MgArgs {
 };
 
 // ------------------------------------------------------------- device side
-// One z mode is solved by one thread-block cluster; `tid`/`nt` number the
+// One z mode is solved by one thread-block cluster; tid() / nt() number the
 // threads of the whole cluster and sync() is the cluster barrier (release /
 // acquire at cluster scope, so global writes of a phase are visible to every
 // block of the cluster in the next phase).  ModeT<T> views the mode's tables
-// and work arrays of arithmetic type T.
+// and work arrays of arithmetic type T.  A view holds only what is the same
+// for every thread of a block, so one copy of it (and of the launch's
+// MgArgs) sits in the block's shared memory: the phases, compiled apart,
+// read their fields from there instead of each thread keeping its own copy
+// on the stack.
 template <class T>
 struct ModeT {
     using V = typename V2<T>::t;
     const MgArgs &a;
     const MgSet<T> &s;
     int kv;
-    int tid, nt;                        // thread index / count over the cluster (or the block)
+    int rank, csz;                      // the block's rank in the cluster, blocks in it
     bool local;                         // the threads are one block's: sync() is the block barrier
     V *pc, *gg, *rs, *rd, *gu, *gb;
     const double2 *rhs;                 // ccap plane of the mode, (i-1) + nl*(j-1)
@@ -124,8 +133,17 @@ struct ModeT {
         if (local) __syncthreads();
         else cooperative_groups::this_cluster().sync();
     }
-    __device__ ModeT(const MgArgs &a_, const MgSet<T> &s_, int kv_, int tid_, int nt_, bool local_ = false)
-        : a(a_), s(s_), kv(kv_), tid(tid_), nt(nt_), local(local_) {
+    // thread index / count over the cluster (or the block).  Warp w of
+    // block r is the cluster's warp w*csz + r: consecutive lines and 32-point
+    // chunks go to different SMs (the work of a phase is spread over every
+    // block, each warp still touches 32 consecutive points).
+    __device__ int tid() const {
+        if (local) return (int)threadIdx.x;
+        return (((int)threadIdx.x >> 5) * csz + rank) * 32 + ((int)threadIdx.x & 31);
+    }
+    __device__ int nt() const { return local ? (int)blockDim.x : csz * (int)blockDim.x; }
+    __device__ ModeT(const MgArgs &a_, const MgSet<T> &s_, int kv_, bool local_, int rank_, int csz_)
+        : a(a_), s(s_), kv(kv_), rank(rank_), csz(csz_), local(local_) {
         pc = s.pc + a.pc_plane * (kv - 1);
         gg = s.gg + a.gg_plane * (kv - 1);
         rs = s.rs + a.gg_plane * (kv - 1);
@@ -227,7 +245,7 @@ __device__ __noinline__ void mg_half(const ModeT<T> &m, int l1, int l2, int kind
     const MgArgs &a = m.a;
     const MgSet<T> &s = m.s;
     if (l2 < l1) return;
-    const int lane = m.tid & 31, warp = m.tid >> 5, nw = m.nt >> 5;
+    const int tid = m.tid(), lane = tid & 31, warp = tid >> 5, nw = m.nt() >> 5;
     const int n2m = a.n2m, nl = (l2 - l1) / 2 + 1;
     const int ch = (n2m + 31) / 32;
     const int j0 = 1 + lane * ch;
@@ -326,7 +344,7 @@ __device__ double cluster_max(double v) {
 template <class T>
 __device__ void mg_shift_odd(const ModeT<T> &m, typename V2<T>::t *u, int ld, typename V2<T>::t tt) {
     const int nh = m.a.nl / 2, n2m = m.a.n2m;
-    for (int t = m.tid; t < nh * n2m; t += m.nt) {
+    for (int t = m.tid(); t < nh * n2m; t += m.nt()) {
         const int i = 1 + 2 * (t % nh), j = 1 + t / nh;
         typename V2<T>::t &g = u[i + (size_t)ld * j];
         g = typename V2<T>::t{g.x - tt.x, g.y - tt.y};
@@ -352,15 +370,15 @@ __device__ __noinline__ void mg_relax(const ModeT<T> &m, int ilev, T oldv, int i
 template <class T>
 __device__ __noinline__ void mg_godown(const ModeT<T> &m, int ilev) {
     const MgArgs &a = m.a;
-    const int ibg = a.iimg[ilev][0], iend = a.iimg[ilev][1], n2m = a.n2m, nt = m.nt;
+    const int ibg = a.iimg[ilev][0], iend = a.iimg[ilev][1], n2m = a.n2m, nt = m.nt();
     const int nf = iend - ibg + 1;
-    for (int t = m.tid; t < nf * n2m; t += nt) {
+    for (int t = m.tid(); t < nf * n2m; t += nt) {
         const int i = ibg + t % nf, j = 1 + t / nf;
         m.R(i, j) = mg_defect(m, m.R(i, j), m.gg, a.ldg, i, j);
     }
     m.sync();
     const int cl = a.iimg[ilev - 1][0], nc = a.iimg[ilev - 1][1] - cl + 1;
-    for (int t = m.tid; t < nc * n2m; t += nt) {
+    for (int t = m.tid(); t < nc * n2m; t += nt) {
         const int i = cl + t % nc, j = 1 + t / nc, f = ibg + 2 * (i - cl);
         const typename V2<T>::t r1 = m.R(f, j), r2 = m.R(f + 1, j);
         m.R(i, j) = typename V2<T>::t{r1.x * m.s.cor1[i] + r2.x * m.s.cor2[i], r1.y * m.s.cor1[i] + r2.y * m.s.cor2[i]};
@@ -373,9 +391,9 @@ template <class T>
 __device__ __noinline__ void mg_goup(const ModeT<T> &m, int ilev) {
     const MgArgs &a = m.a;
     const MgSet<T> &s = m.s;
-    const int cl = a.iimg[ilev][0], ce = a.iimg[ilev][1], n2m = a.n2m, nt = m.nt;
+    const int cl = a.iimg[ilev][0], ce = a.iimg[ilev][1], n2m = a.n2m, nt = m.nt();
     const int fb = a.iimg[ilev + 1][0], nc = ce - cl + 1;
-    for (int t = m.tid; t < nc * n2m; t += nt) {
+    for (int t = m.tid(); t < nc * n2m; t += nt) {
         const int i = cl + t % nc, j = 1 + t / nc, f = fb + 1 + 2 * (i - cl);
         typename V2<T>::t g = m.G(f, j);
         const typename V2<T>::t g1 = m.G(i, j);
@@ -394,7 +412,7 @@ __device__ __noinline__ void mg_goup(const ModeT<T> &m, int ilev) {
 template <int MC>
 __device__ __noinline__ int mg_gsor2d(const Mode &m, double test, bool &unconv) {
     const MgArgs &a = m.a;
-    const int n1m = a.nl, n2m = a.n2m, nt = m.nt;
+    const int n1m = a.nl, n2m = a.n2m, nt = m.nt();
     const double ww = a.wwsor, ww2 = 1.0 - ww;
     for (int kk = 0; kk <= a.mgitr; kk++) {
         const double ov = kk == 0 ? 0.0 : 1.0, o2 = ov * ww2;
@@ -410,7 +428,7 @@ __device__ __noinline__ int mg_gsor2d(const Mode &m, double test, bool &unconv) 
             }
         }
         double mx = 0.0;
-        for (int t = m.tid; t < n1m * n2m; t += nt) {
+        for (int t = m.tid(); t < n1m * n2m; t += nt) {
             const int i = 1 + t % n1m, j = 1 + t / n1m;
             const double2 d = mg_defect(m, m.B(i, j), m.pc, a.ldp, i, j);
             mx = fmax(mx, d.x * d.x + d.y * d.y);
@@ -493,6 +511,21 @@ __device__ __forceinline__ V nbval(const Halo<V> &h, const Part &pt, const V *in
     return pt.in(line) ? in[line + (size_t)ldi * j] : out[line + (size_t)ldo * j];
 }
 
+// the rows of neighbour line `line` as a base and a stride (row j at
+// p[st * j]), resolved once per line: the same source nbval picks
+template <class V>
+struct LineRef {
+    const V *p;
+    size_t st;
+};
+template <class V>
+__device__ __forceinline__ LineRef<V> nbline(const Halo<V> &h, const Part &pt, const V *in, int ldi, const V *out,
+                                             int ldo, int line) {
+    const int s = h.slot(line);
+    if (s >= 0) return LineRef<V>{h.buf + (size_t)s * kHaloRows, 1};
+    return pt.in(line) ? LineRef<V>{in + line, (size_t)ldi} : LineRef<V>{out + line, (size_t)ldo};
+}
+
 // The y solves of one zebra half on a partitioned level: the block's own
 // lines of parity par (0: a, a+2, ..; 1: a+1, a+3, ..) and the halo lines
 // of that parity listed in xl (their results go to the halo).  Right-hand
@@ -520,6 +553,12 @@ __device__ __noinline__ void part_half(const ModeT<T> &m, const Part &pt, int pa
         const T aw = s.aw[i], ae = s.ae[i];
         const T *bet = s.bet + m.cb + (i - 1);
         const T *gam = s.gam + m.cb + (i - 1);
+        const bool nbr = !(kind == H_ODD && ov == T(0.0));
+        LineRef<V> lm{nullptr, 0}, lp{nullptr, 0};
+        if (nbr) {
+            lm = nbline(h, pt, nin, ldi, nout, ldo, im);
+            lp = nbline(h, pt, nin, ldi, nout, ldo, ip);
+        }
         V v[MC];
         T as_[MC], bt[MC], gm[MC];
 #pragma unroll
@@ -533,10 +572,10 @@ __device__ __noinline__ void part_half(const ModeT<T> &m, const Part &pt, int pa
                 } else {
                     sr = src[i + (size_t)a.ldg * j];
                 }
-                if (kind == H_ODD && ov == T(0.0)) {
+                if (!nbr) {
                     v[q] = sr;
                 } else {
-                    V nm = nbval(h, pt, nin, ldi, nout, ldo, im, j), np = nbval(h, pt, nin, ldi, nout, ldo, ip, j);
+                    V nm = lm.p[lm.st * j], np = lp.p[lp.st * j];
                     if (kind == H_ODD) {
                         const T sx = aw * nm.x + ae * np.x, sy = aw * nm.y + ae * np.y;
                         v[q] = V{sr.x - ov * sx, sr.y - ov * sy};
@@ -792,8 +831,9 @@ __device__ __noinline__ void part_top_relax(const ModeT<T> &m, int r, int cs, T 
 
 // Max over the cluster through distributed shared memory: one value per
 // block, slot `par` (alternating between calls, so a slot is rewritten only
-// after every block has passed the barrier that follows its reads).  The
-// caller's cluster barrier must follow; returns after it.
+// after every block has passed the barrier that follows its reads).  A
+// cluster barrier must follow before the slot is written again and before
+// any block of the cluster exits.
 __device__ double part_cluster_max(double v, int par) {
     __shared__ double sh[kMgThreads / 32];
     __shared__ double blk[2];
@@ -867,7 +907,7 @@ __device__ __noinline__ double part_top_resid_mixed(const Mode &m, const ModeT<f
 
 // mg2d (poiss_z_ft.f90:239-299) with the level-partitioned phases
 template <int MC>
-__device__ int part_mg2d(const Mode &m, double test, bool &unconv, int r, int cs, double2 *hbuf) {
+__device__ int part_mg2d(const Mode &m, const Mode &mb, double test, bool &unconv, int r, int cs, double2 *hbuf) {
     const MgArgs &a = m.a;
     const int nlev = a.nlev, lc = a.lc;
     int par = 0;
@@ -875,7 +915,6 @@ __device__ int part_mg2d(const Mode &m, double test, bool &unconv, int r, int cs
     double sumres = part_top_resid(m, r, cs, par);
     par ^= 1;
     if (sumres < test) return 0;
-    const Mode mb(a, a.d, m.kv, threadIdx.x, blockDim.x, true);
     for (int kk = 1; kk <= a.mgitr; kk++) {
         for (int ilev = nlev - 1; ilev > lc; ilev--) part_down<MC>(m, ilev, r, cs, hbuf);
         if (r == 0) {
@@ -902,8 +941,8 @@ __device__ int part_mg2d(const Mode &m, double test, bool &unconv, int r, int cs
 
 // mg_mg2d_mixed with the level-partitioned phases
 template <int MC>
-__device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, double test, bool &unconv, int r, int cs,
-                               double2 *hbuf) {
+__device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, const Mode &mb, const ModeT<float> &fb,
+                               double test, bool &unconv, int r, int cs, double2 *hbuf) {
     const MgArgs &a = m.a;
     const int nlev = a.nlev, lc = a.lc, n2m = a.n2m;
     float2 *hf = reinterpret_cast<float2 *>(hbuf);
@@ -923,8 +962,6 @@ __device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, double test
     double sumres = part_top_resid_mixed(m, f, r, cs, par);
     par ^= 1;
     if (sumres < test) return 0;
-    const ModeT<float> fb(a, a.f, m.kv, threadIdx.x, blockDim.x, true);
-    const Mode mb(a, a.d, m.kv, threadIdx.x, blockDim.x, true);
     const int c0 = a.iimg[0][0], nc0 = a.iimg[0][1] - c0 + 1;
     for (int kk = 1; kk <= a.mgitr; kk++) {
         for (int ilev = nlev - 1; ilev > lc; ilev--) part_down<MC>(f, ilev, r, cs, hf);
@@ -962,37 +999,56 @@ __device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, double test
     return a.xft ? a.mgitr : a.mgitr + 1;
 }
 
-// One cluster's solve of mode kv of the case described by a.
+// What a block keeps in shared memory for its mode: the launch's arguments
+// and the four views of the mode (cluster-wide and block-local, FP64 and
+// FP32), built once by thread 0.
+struct MgBlock {
+    MgArgs a;
+    alignas(16) unsigned char m[sizeof(ModeT<double>)], f[sizeof(ModeT<float>)];
+    alignas(16) unsigned char mb[sizeof(ModeT<double>)], fb[sizeof(ModeT<float>)];
+};
+
+// One cluster's solve of mode kv of the case described by ga.
 template <int MC>
-__device__ __forceinline__ void zft_mode(const MgArgs &a, int kv, double2 *hbuf) {
+__device__ __forceinline__ void zft_mode(const MgArgs &ga, int kv, double2 *hbuf, MgBlock &sb) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     const int cs = (int)cl.num_blocks();
-    // warp w of block r is the cluster's warp w*cs + r: consecutive lines and
-    // 32-point chunks go to different SMs (the work of a phase is spread over
-    // every block, each warp still touches 32 consecutive points)
-    const int gw = (int)(threadIdx.x >> 5) * cs + (int)cl.block_rank();
-    const int tid = gw * 32 + (int)(threadIdx.x & 31), nt = cs * blockDim.x;
-    Mode m(a, a.d, kv, tid, nt);
-    const double test = a.fixed_cycles > 0 ? -1.0 : a.S->mg_test;
     const int r = (int)cl.block_rank();
+    if (threadIdx.x == 0) {
+        sb.a = ga;
+        new (sb.m) Mode(sb.a, sb.a.d, kv, false, r, cs);
+        new (sb.f) ModeT<float>(sb.a, sb.a.f, kv, false, r, cs);
+        new (sb.mb) Mode(sb.a, sb.a.d, kv, true, 0, 1);
+        new (sb.fb) ModeT<float>(sb.a, sb.a.f, kv, true, 0, 1);
+    }
+    __syncthreads();
+    const MgArgs &a = sb.a;
+    const Mode &m = *reinterpret_cast<const Mode *>(sb.m);
+    const double test = a.fixed_cycles > 0 ? -1.0 : a.S->mg_test;
     int it;
     bool unconv = false;
     if (kv > a.imgsor) {
         it = mg_gsor2d<MC>(m, test, unconv);
     } else if (a.mixed) {
-        ModeT<float> f(a, a.f, kv, tid, nt);
-        it = part_mg2d_mixed<MC>(m, f, test, unconv, r, cs, hbuf);
+        it = part_mg2d_mixed<MC>(m, *reinterpret_cast<const ModeT<float> *>(sb.f),
+                                 *reinterpret_cast<const Mode *>(sb.mb),
+                                 *reinterpret_cast<const ModeT<float> *>(sb.fb), test, unconv, r, cs, hbuf);
     } else {
-        it = part_mg2d<MC>(m, test, unconv, r, cs, hbuf);
+        it = part_mg2d<MC>(m, *reinterpret_cast<const Mode *>(sb.mb), test, unconv, r, cs, hbuf);
     }
+    // the last max-norm test read every block's slot through distributed
+    // shared memory with no barrier after it: no block may exit (and take
+    // its shared memory with it) before all have read
+    cl.sync();
     // the mode's solution replaces its right-hand side (ccap(i,j,kkk) = cp(i,j))
     double2 *out = a.ccap + (size_t)a.nl * a.n2m * (kv - 1);
-    for (int t = m.tid; t < a.nl * a.n2m; t += m.nt) {
+    const int tid = m.tid(), nt = m.nt();
+    for (int t = tid; t < a.nl * a.n2m; t += nt) {
         const int i = 1 + t % a.nl, j = 1 + t / a.nl;
         out[t] = m.P(i, j);
     }
-    if (m.tid == 0) {
+    if (tid == 0) {
         a.iters[kv - 1] = it;
         atomicMax((unsigned long long *)&a.S->poisson_iters[a.slot], (unsigned long long)it);
         // the timing runs of the autotuner fix the cycle count: not a failure
@@ -1003,8 +1059,9 @@ __device__ __forceinline__ void zft_mode(const MgArgs &a, int kv, double2 *hbuf)
 template <int MC>
 __global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes(MgArgs a) {
     __shared__ __align__(16) double2 hbuf[kHalo * kHaloRows];
+    __shared__ MgBlock sb;
     const int cs = (int)cooperative_groups::this_cluster().num_blocks();
-    zft_mode<MC>(a, blockIdx.x / cs + 1, hbuf);
+    zft_mode<MC>(a, blockIdx.x / cs + 1, hbuf, sb);
 }
 
 // The modes of several cases of one grid shape in one launch (the serving
@@ -1014,9 +1071,10 @@ __global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes(MgArgs a) {
 template <int MC>
 __global__ void __launch_bounds__(kMgThreads, 1) k_zft_modes_batch(const MgArgs *as, int nmodes) {
     __shared__ __align__(16) double2 hbuf[kHalo * kHaloRows];
+    __shared__ MgBlock sb;
     const int cs = (int)cooperative_groups::this_cluster().num_blocks();
     const int b = blockIdx.x / cs;
-    zft_mode<MC>(as[b / nmodes], b % nmodes + 1, hbuf);
+    zft_mode<MC>(as[b / nmodes], b % nmodes + 1, hbuf, sb);
 }
 
 // the instance for y lines of n2m cells: MC = ceil(n2m / 32) rounded up to
@@ -1417,22 +1475,18 @@ static bool cluster_fits(lesgpu_case *c, int cs) {
     return nact >= 1;
 }
 
-void launch_mg2d(lesgpu_case *c, int msub) {
+// The transforms around the mode solves: pre = the criterion of the
+// substep and the forward transform into the modes, post = the inverse
+// transform back to phi (z_ft: z; x_ft: x).
+static void mg2d_pre(lesgpu_case *c, int slot) {
     const DGrid &g = c->kp.g;
     DPois &P = c->pois;
-    MgTables *T = P.mg;
-    const int slot = (msub >= 1 && msub <= 3) ? msub - 1 : 0;
-    inst_begin(c, LESGPU_K_POISSON);
-    if (T->xft) {
+    if (P.mg->xft) {
         k_mg_begin<<<1, 1, 0, c->stream>>>(c->S, slot, g.n1m, g.n1mh, 0.9);
         const DevPlan px = devplan(P.fx);
-        const int Lx = fft_lx(c), pin = c->cfg.ich == 1 ? 1 : 0;
-        const int Li = fft_xr_inv_lines(g.n1m, Lx, pin);
+        const int Lx = fft_lx(c);
         k_fft_xr_fwd<<<dim3((g.n3m + Lx - 1) / Lx, g.n2m), kThreads, (size_t)2 * g.n1m * Lx * sizeof(double2),
                        c->stream>>>(c->kp, P.ccap, px, Lx);
-        launch_modes(c, mg_args(c, slot, 0), T->cs);
-        k_fft_xr_inv<<<dim3((g.n3m + Li - 1) / Li, g.n2m), kThreads, (size_t)2 * g.n1m * (Li + pin) * sizeof(double2),
-                       c->stream>>>(c->kp, P.ccap, px, Li, pin);
     } else {
         k_mg_begin<<<1, 1, 0, c->stream>>>(c->S, slot, g.n3m, g.n3mh, 0.8);
         const DevPlan pz = devplan(P.fz);
@@ -1441,10 +1495,62 @@ void launch_mg2d(lesgpu_case *c, int msub) {
         const dim3 gz((g.n1m + 2 * Lz - 1) / (2 * Lz), g.n2m);   // 2 Lz real lines per block
         const long long sk = (long long)g.n1m * g.n2m, sj = g.n1m;
         fft_z_fwd64(gz, smz, c->stream, c->kp, c->kp.f.divgsum, P.ccap, pz, Lz, sk, sj);
-        launch_modes(c, mg_args(c, slot, 0), T->cs);
+    }
+}
+
+static void mg2d_post(lesgpu_case *c) {
+    const DGrid &g = c->kp.g;
+    DPois &P = c->pois;
+    if (P.mg->xft) {
+        const DevPlan px = devplan(P.fx);
+        const int Lx = fft_lx(c), pin = c->cfg.ich == 1 ? 1 : 0;
+        const int Li = fft_xr_inv_lines(g.n1m, Lx, pin);
+        k_fft_xr_inv<<<dim3((g.n3m + Li - 1) / Li, g.n2m), kThreads, (size_t)2 * g.n1m * (Li + pin) * sizeof(double2),
+                       c->stream>>>(c->kp, P.ccap, px, Li, pin);
+    } else {
+        const DevPlan pz = devplan(P.fz);
+        const int Lz = fft_lz(c);
+        const size_t smz = (size_t)2 * (g.n3m > 1 ? g.n3m : 1) * Lz * sizeof(double2);
+        const dim3 gz((g.n1m + 2 * Lz - 1) / (2 * Lz), g.n2m);
+        const long long sk = (long long)g.n1m * g.n2m, sj = g.n1m;
         fft_z_inv64(gz, smz, c->stream, c->kp, P.ccap, pz, Lz, sk, sj);
     }
+}
+
+void launch_mg2d(lesgpu_case *c, int msub) {
+    MgTables *T = c->pois.mg;
+    const int slot = (msub >= 1 && msub <= 3) ? msub - 1 : 0;
+    inst_begin(c, LESGPU_K_POISSON);
+    mg2d_pre(c, slot);
+    launch_modes(c, mg_args(c, slot, 0), T->cs);
+    mg2d_post(c);
     inst_end(c, LESGPU_K_POISSON);
+}
+
+// ---- the serving loop's batched solve: the pieces of launch_mg2d apart,
+// the mode solves of several cases of one shape in one launch
+void mg2d_launch_pre(lesgpu_case *c, int msub) { mg2d_pre(c, (msub >= 1 && msub <= 3) ? msub - 1 : 0); }
+void mg2d_launch_post(lesgpu_case *c) { mg2d_post(c); }
+int mg2d_batch_size(const lesgpu_case *) { return (int)sizeof(MgArgs); }
+void mg2d_batch_args(lesgpu_case *c, int msub, void *out) {
+    const MgArgs a = mg_args(c, (msub >= 1 && msub <= 3) ? msub - 1 : 0, 0);
+    memcpy(out, &a, sizeof(MgArgs));
+}
+// d_args: n MgArgs of cases with equal mg2d_batch_key
+void mg2d_launch_batch(const lesgpu_case *c0, const void *d_args, int n, cudaStream_t st) {
+    const MgTables *T = c0->pois.mg;
+    cudaLaunchConfig_t lc;
+    cudaLaunchAttribute at[1];
+    cluster_cfg(lc, at, T->nmodes * n, T->cs);
+    lc.stream = st;
+    cudaLaunchKernelEx(&lc, zft_batch_kernel(c0->kp.g.n2m), (const MgArgs *)d_args, T->nmodes);
+}
+// what cases of one grid shape must share to be solved by one batched
+// launch: the cluster size and the level layout it was checked against
+long long mg2d_batch_key(const lesgpu_case *c) {
+    const MgTables *T = c->pois.mg;
+    if (!T) return 0;
+    return (((long long)T->cs * 64 + T->nlev) * 64 + T->lc) * 4096 + T->nmodes;
 }
 
 // ---- autotuner: cluster size per mode.  A solve lasts as long as its

@@ -687,27 +687,41 @@ static void enqueue_energy(lesgpu_case *c, int msub) {
     mark_mirror(c, kMirT);
 }
 
-static void enqueue_step(lesgpu_case *c, bool first) {
+// A substep up to the Poisson solve (with stepinit before the first one)
+// and from the solve's result on (with the step's checks and diagnostics
+// after the last one): solver.f90:85-151, 154-173.
+static void enqueue_substep_pre(lesgpu_case *c, int msub, bool first) {
     const lesgpu_config &g = c->cfg;
-    launch_stepinit(c);
-    for (int msub = 1; msub <= 3; msub++) {
-        launch_substepinit(c, msub);
-        if (g.ich == 1) launch_qvolcalc(c, 1);
-        if (g.iles == 1 && msub == 1) enqueue_sgs(c, first);
-        enqueue_rhsnlhs(c, msub);
-        launch_divgs(c);
-        launch_poisson(c, msub);
-        launch_ucalc_pcalc(c, g.ich == 1);        // qvolcalc(qvol(2)), ucalc, qvolcalc(qvol(0)), pcalc
-        mark_mirror(c, kMirVel | kMirP);
-        if (g.ich != 0) launch_meanpg(c);
-        if (g.ibmon == 1) launch_lagforce(c, msub);
-        if (g.ihtrans == 1) enqueue_energy(c, msub);
+    if (msub == 1) launch_stepinit(c);
+    launch_substepinit(c, msub);
+    if (g.ich == 1) launch_qvolcalc(c, 1);
+    if (g.iles == 1 && msub == 1) enqueue_sgs(c, first);
+    enqueue_rhsnlhs(c, msub);
+    launch_divgs(c);
+}
+
+static void enqueue_substep_post(lesgpu_case *c, int msub) {
+    const lesgpu_config &g = c->cfg;
+    launch_ucalc_pcalc(c, g.ich == 1);        // qvolcalc(qvol(2)), ucalc, qvolcalc(qvol(0)), pcalc
+    mark_mirror(c, kMirVel | kMirP);
+    if (g.ich != 0) launch_meanpg(c);
+    if (g.ibmon == 1) launch_lagforce(c, msub);
+    if (g.ihtrans == 1) enqueue_energy(c, msub);
+    if (msub == 3) {
+        launch_advance_and_convergence(c);          // time += dt, convergence_check
+        launch_bulk_diag(c);
+        if (g.ibmon == 1) launch_draglift(c);
+        if (g.ihtrans == 1) launch_heatflux(c);
+        if (g.iavg == 1) launch_field_avg(c);
     }
-    launch_advance_and_convergence(c);              // time += dt, convergence_check
-    launch_bulk_diag(c);
-    if (g.ibmon == 1) launch_draglift(c);
-    if (g.ihtrans == 1) launch_heatflux(c);
-    if (g.iavg == 1) launch_field_avg(c);
+}
+
+static void enqueue_step(lesgpu_case *c, bool first) {
+    for (int msub = 1; msub <= 3; msub++) {
+        enqueue_substep_pre(c, msub, first);
+        launch_poisson(c, msub);
+        enqueue_substep_post(c, msub);
+    }
 }
 
 // The out-of-date mirror sets a step leaves behind (and the captured step
@@ -745,6 +759,116 @@ static int capture_step(lesgpu_case *c) {
     c->graph_ok = 1;
     return 0;
 }
+
+// ---- the serving loop's size buckets: one step of every case of a bucket
+// (cases of one grid shape and options) captured as one CUDA graph on the
+// bucket's stream.  Each case's kernels run on its own stream branch, forked
+// from and joined to the bucket stream; for poiss_z_ft / poiss_x_ft the
+// branches join before each substep's Poisson solve, whose mode solves run
+// as one batched launch over all the cases, and fork again after it.
+namespace lg {
+
+int bucket_prologue(lesgpu_case **cs, int n) {
+    for (int q = 0; q < n; q++) {
+        lesgpu_case *c = cs[q];
+        const unsigned extra = c->mir_dirty & ~mir_steady(c);
+        if (extra) {
+            launch_mirror(c, extra);
+            if (cudaStreamSynchronize(c->stream) != cudaSuccess) return LESGPU_ERR_CUDA;
+        }
+    }
+    return 0;
+}
+
+void bucket_replayed(lesgpu_case **cs, int n, int steps) {
+    for (int q = 0; q < n; q++) {
+        cs[q]->ntime_host += steps;
+        cs[q]->mir_dirty = mir_steady(cs[q]);
+    }
+}
+
+void free_bucket_graph(BucketGraph *bg) {
+    if (bg->exec) cudaGraphExecDestroy(bg->exec);
+    if (bg->d_args) cudaFree(bg->d_args);
+    bg->exec = nullptr;
+    bg->d_args = nullptr;
+    bg->kernels = 0;
+}
+
+int capture_bucket_step(lesgpu_case **cs, int n, cudaStream_t st, BucketGraph *bg) {
+    free_bucket_graph(bg);
+    if (n < 1) return LESGPU_ERR_ARG;
+    const int pk = (int)cs[0]->cfg.poisson;
+    const bool batched = pk == LESGPU_POISSON_Z_FT || pk == LESGPU_POISSON_X_FT;
+    for (int q = 1; q < n; q++)
+        if (cs[q]->cfg.poisson != pk || (batched && mg2d_batch_key(cs[q]) != mg2d_batch_key(cs[0])))
+            return LESGPU_ERR_ARG;
+    const size_t sz = batched ? (size_t)mg2d_batch_size(cs[0]) : 0;
+    if (batched) {
+        std::vector<unsigned char> h(3 * (size_t)n * sz);
+        for (int msub = 1; msub <= 3; msub++)
+            for (int q = 0; q < n; q++) mg2d_batch_args(cs[q], msub, h.data() + ((size_t)(msub - 1) * n + q) * sz);
+        if (cudaMalloc(&bg->d_args, h.size()) != cudaSuccess) return LESGPU_ERR_OOM;
+        if (cudaMemcpy(bg->d_args, h.data(), h.size(), cudaMemcpyHostToDevice) != cudaSuccess) return LESGPU_ERR_CUDA;
+    }
+    int rc = bucket_prologue(cs, n);
+    if (rc) return rc;
+    std::vector<cudaEvent_t> ev(n + 1, nullptr);
+    for (auto &e : ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = LESGPU_ERR_CUDA;
+    auto fork = [&]() {
+        cudaEventRecord(ev[n], st);
+        for (int q = 0; q < n; q++) cudaStreamWaitEvent(cs[q]->stream, ev[n], 0);
+    };
+    auto join = [&]() {
+        for (int q = 0; q < n; q++) {
+            cudaEventRecord(ev[q], cs[q]->stream);
+            cudaStreamWaitEvent(st, ev[q], 0);
+        }
+    };
+    cudaGraph_t gr = nullptr;
+    if (!rc && cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = LESGPU_ERR_CUDA;
+    if (!rc) {
+        for (int q = 0; q < n; q++) cs[q]->mir_dirty = mir_steady(cs[q]);
+        fork();
+        for (int msub = 1; msub <= 3; msub++) {
+            for (int q = 0; q < n; q++) {
+                enqueue_substep_pre(cs[q], msub, false);
+                if (batched) mg2d_launch_pre(cs[q], msub);
+                else launch_poisson(cs[q], msub);
+            }
+            if (batched) {
+                join();
+                mg2d_launch_batch(cs[0], (const unsigned char *)bg->d_args + (size_t)(msub - 1) * n * sz, n, st);
+                fork();
+                for (int q = 0; q < n; q++) mg2d_launch_post(cs[q]);
+            }
+            for (int q = 0; q < n; q++) enqueue_substep_post(cs[q], msub);
+        }
+        join();
+        if (cudaStreamEndCapture(st, &gr) != cudaSuccess) rc = LESGPU_ERR_CUDA;
+    }
+    for (auto &e : ev)
+        if (e) cudaEventDestroy(e);
+    if (rc) {
+        if (gr) cudaGraphDestroy(gr);
+        return rc;
+    }
+    size_t nn = 0;
+    cudaGraphGetNodes(gr, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (nn) cudaGraphGetNodes(gr, nodes.data(), &nn);
+    for (size_t q = 0; q < nn; q++) {
+        cudaGraphNodeType t;
+        cudaGraphNodeGetType(nodes[q], &t);
+        if (t == cudaGraphNodeTypeKernel) bg->kernels++;
+    }
+    if (cudaGraphInstantiate(&bg->exec, gr, 0) != cudaSuccess) rc = LESGPU_ERR_CUDA;
+    cudaGraphDestroy(gr);
+    return rc;
+}
+
+}  // namespace lg
 
 static void fill_report(const lesgpu_case *c, const DScal &s, lesgpu_step_report *r) {
     memset(r, 0, sizeof(*r));

@@ -452,4 +452,26 @@ void launch_cvol(lesgpu_case *c);
 // the reduction weights (DFields wq, wb, wt); after fb_u/fb_c or c* change
 void launch_red_weights(lesgpu_case *c);
 void launch_rhs_t_kernel(lesgpu_case *c, int msub);
+// poiss_z_ft / poiss_x_ft in pieces, for the serving loop's batched solve
+// (k_mg.cu): the transforms before and after the mode solves, the solve's
+// arguments of one case (mg2d_batch_size bytes), one launch over n cases of
+// one shape, and what the cases must share for it (cluster size, levels)
+void mg2d_launch_pre(lesgpu_case *c, int msub);
+void mg2d_launch_post(lesgpu_case *c);
+int mg2d_batch_size(const lesgpu_case *c);
+void mg2d_batch_args(lesgpu_case *c, int msub, void *out);
+void mg2d_launch_batch(const lesgpu_case *c0, const void *d_args, int n, cudaStream_t st);
+long long mg2d_batch_key(const lesgpu_case *c);
+// one step of n cases of one shape captured as a CUDA graph on stream st
+// (lesgpu_api.cu), the host bookkeeping after each replay of it, and the
+// out-of-date mirrors refreshed before the first replay
+struct BucketGraph {
+    cudaGraphExec_t exec = nullptr;
+    void *d_args = nullptr;      // batched solve arguments, 3 substeps x n cases
+    long long kernels = 0;       // kernel nodes of the graph
+};
+int capture_bucket_step(lesgpu_case **cs, int n, cudaStream_t st, BucketGraph *bg);
+void free_bucket_graph(BucketGraph *bg);
+int bucket_prologue(lesgpu_case **cs, int n);
+void bucket_replayed(lesgpu_case **cs, int n, int steps);
 }  // namespace lg

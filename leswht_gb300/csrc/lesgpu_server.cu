@@ -1,11 +1,15 @@
 // Serving loop: LES cases arrive at any time, are admitted while their
 // device footprint fits an HBM budget, stay resident on the GPU for their
-// whole run, and advance together -- each admitted case owns a stream and a
-// captured step graph, and the worker thread keeps a chunk of steps in
-// flight on every active case, so the kernels of different cases overlap on
-// the device.  A case that finishes is read back and freed at once, and the
-// freed memory admits the next waiting case (continuous batching, not a
-// queue in front of a single solver).
+// whole run, and advance together.  Resident cases are grouped in size
+// buckets (same grid shape and options); a bucket advances all its cases one
+// step at a time through one captured CUDA graph -- every case's kernels on
+// its own stream branch, and for the multigrid Poisson solvers the mode
+// solves of all the bucket's cases as one batched launch per substep -- and
+// the worker keeps a chunk of bucket steps in flight on every bucket, so the
+// work of different buckets overlaps on the device as well.  A case that
+// finishes is read back and freed at once (its bucket's graph is captured
+// again without it), and the freed memory admits the next waiting case
+// (continuous batching, not a queue in front of a single solver).
 //
 // The API (include/lesgpu.h, lesgpu_server_*) copies every input at
 // submission, so the caller's buffers are free on return; results are
@@ -21,6 +25,7 @@
 #include <map>
 #include <mutex>
 #include <thread>
+#include <utility>
 #include <vector>
 
 namespace {
@@ -116,8 +121,7 @@ struct Request {
     int state = S_PENDING;
     int rc = 0;
     lesgpu_case *c = nullptr;
-    cudaEvent_t ev = nullptr;
-    int64_t done = 0, inflight = 0;
+    int64_t done = 0, inflight = 0;   // steps completed; steps of its bucket's work in flight
     size_t footprint = 0;
     double t_submit = 0, t_admit = 0, t_done = 0;
     lesgpu_step_report rep;
@@ -134,7 +138,7 @@ struct lesgpu_server {
     std::map<long long, size_t> bucket_bytes;     // measured footprint per size bucket
     size_t budget = 0, used = 0;
     int max_active = 64;
-    int64_t chunk = 4;          // steps in flight per case
+    int64_t chunk = 4;          // steps in flight per bucket
     int device = 0;
     int64_t next_ticket = 1;
     bool stop = false;
@@ -170,7 +174,6 @@ void finish(lesgpu_server *S, Request *r, int state) {
         lesgpu_destroy(r->c);
         r->c = nullptr;
     }
-    if (r->ev) { cudaEventDestroy(r->ev); r->ev = nullptr; }
     std::lock_guard<std::mutex> lk(S->mu);
     S->used -= r->footprint;
     r->footprint = 0;
@@ -186,7 +189,6 @@ int admit(lesgpu_server *S, Request *r) {
     if (!rc) rc = lesgpu_set_fields(r->c, r->f[0].data(), r->f[1].data(), r->f[2].data(), r->f[3].data(),
                                     r->f[4].empty() ? nullptr : r->f[4].data(), r->time0, r->dt0, r->ihist0, r->m0);
     if (!rc) rc = lesgpu_start(r->c);
-    if (!rc && cudaEventCreateWithFlags(&r->ev, cudaEventDisableTiming) != cudaSuccess) rc = LESGPU_ERR_CUDA;
     size_t free1 = 0;
     cudaMemGetInfo(&free1, &total);
     size_t fp = free0 > free1 ? free0 - free1 : 0;
@@ -207,8 +209,32 @@ int admit(lesgpu_server *S, Request *r) {
     return rc;
 }
 
+struct Bucket {
+    std::vector<Request *> members;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    lg::BucketGraph bg;
+    bool valid = false;            // bg holds a step of exactly these members
+    int64_t inflight = 0;          // bucket steps enqueued since the last completed event
+};
+
+void destroy_bucket(Bucket &B) {
+    lg::free_bucket_graph(&B.bg);
+    if (B.ev) cudaEventDestroy(B.ev);
+    if (B.st) cudaStreamDestroy(B.st);
+    B.ev = nullptr;
+    B.st = nullptr;
+}
+
+void remove_active(lesgpu_server *S, Request *r) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    for (size_t q = 0; q < S->active.size(); q++)
+        if (S->active[q] == r) { S->active.erase(S->active.begin() + q); break; }
+}
+
 void worker_main(lesgpu_server *S) {
     cudaSetDevice(S->device);
+    std::map<std::pair<long long, long long>, Bucket> buckets;
     // resident cases share the GPU: their multigrid solves are latency-bound,
     // so each gets small clusters and the solves of different cases run side
     // by side (2 blocks per cluster doubled the served throughput of the
@@ -233,12 +259,37 @@ void worker_main(lesgpu_server *S) {
                 r = cand;
             }
             int rc = admit(S, r);
+            if (!rc && r->cfg.iread == 0 && r->nsteps > 0) {
+                // the first step of a fresh start differs from the others
+                // (the SGS model starts from zero): it runs on the case's own
+                // path, the bucket graphs hold steady-state steps only
+                rc = lesgpu_step_async(r->c, 1);
+                if (!rc && cudaStreamSynchronize(r->c->stream) != cudaSuccess) rc = LESGPU_ERR_CUDA;
+                if (!rc) {
+                    r->done = 1;
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    S->busy_cell_steps += (double)r->grid.g.n1m * r->grid.g.n2m * r->grid.g.n3m;
+                }
+            }
             if (rc) {
                 r->rc = rc;
                 finish(S, r, S_FAILED);
-            } else {
+                continue;
+            }
+            {
+                std::lock_guard<std::mutex> lk(S->mu);
                 S->active.push_back(r);
             }
+            // a bucket is the cases of one shape and options that can share
+            // a batched solve (the same multigrid cluster size and levels)
+            Bucket &B = buckets[std::make_pair(bucket_key(r), lg::mg2d_batch_key(r->c))];
+            if (!B.st) {
+                if (cudaStreamCreateWithFlags(&B.st, cudaStreamNonBlocking) != cudaSuccess ||
+                    cudaEventCreateWithFlags(&B.ev, cudaEventDisableTiming) != cudaSuccess)
+                    r->rc = LESGPU_ERR_CUDA;
+            }
+            B.members.push_back(r);
+            B.valid = false;
         }
         {
             std::unique_lock<std::mutex> lk(S->mu);
@@ -248,48 +299,86 @@ void worker_main(lesgpu_server *S) {
                 continue;
             }
         }
-        // ---- keep a chunk of steps in flight on every active case
+        // ---- keep a chunk of bucket steps in flight on every bucket
         bool progressed = false;
-        for (size_t q = 0; q < S->active.size();) {
-            Request *r = S->active[q];
-            bool cancelled;
-            {
-                std::lock_guard<std::mutex> lk(S->mu);
-                cancelled = r->state == S_CANCELLED;
-            }
-            if (r->inflight > 0) {
-                cudaError_t e = cudaEventQuery(r->ev);
-                if (e == cudaErrorNotReady) { q++; continue; }
-                if (e != cudaSuccess) { r->rc = LESGPU_ERR_CUDA; cancelled = true; }
-                r->done += r->inflight;
-                {
+        for (auto it = buckets.begin(); it != buckets.end();) {
+            Bucket &B = it->second;
+            if (B.inflight > 0) {
+                cudaError_t e = cudaEventQuery(B.ev);
+                if (e == cudaErrorNotReady) { ++it; continue; }
+                for (Request *r : B.members) {     // a case admitted meanwhile has nothing in flight
+                    if (r->inflight == 0) continue;
+                    if (e != cudaSuccess) r->rc = LESGPU_ERR_CUDA;
+                    r->done += r->inflight;
                     std::lock_guard<std::mutex> lk(S->mu);
                     S->busy_cell_steps += (double)r->inflight * r->grid.g.n1m * r->grid.g.n2m * r->grid.g.n3m;
+                    r->inflight = 0;
                 }
-                r->inflight = 0;
+                B.inflight = 0;
                 progressed = true;
             }
-            if (cancelled || r->done >= r->nsteps) {
-                finish(S, r, cancelled ? (r->rc ? S_FAILED : S_CANCELLED) : S_DONE);
-                S->active.erase(S->active.begin() + q);
-                progressed = true;
+            // finished, failed and cancelled cases leave the bucket (nothing
+            // of the bucket is in flight here)
+            for (size_t q = 0; q < B.members.size();) {
+                Request *r = B.members[q];
+                bool cancelled;
+                {
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    cancelled = r->state == S_CANCELLED;
+                }
+                if (r->rc || cancelled || r->done >= r->nsteps) {
+                    finish(S, r, r->rc ? S_FAILED : cancelled ? S_CANCELLED : S_DONE);
+                    remove_active(S, r);
+                    B.members.erase(B.members.begin() + q);
+                    B.valid = false;
+                    progressed = true;
+                } else {
+                    q++;
+                }
+            }
+            if (B.members.empty()) {
+                destroy_bucket(B);
+                it = buckets.erase(it);
                 continue;
             }
-            int64_t n = r->nsteps - r->done < S->chunk ? r->nsteps - r->done : S->chunk;
-            int rc = lesgpu_step_async(r->c, n);
-            if (!rc && cudaEventRecord(r->ev, r->c->stream) != cudaSuccess) rc = LESGPU_ERR_CUDA;
+            std::vector<lesgpu_case *> cs;
+            int64_t n = S->chunk;
+            for (Request *r : B.members) {
+                cs.push_back(r->c);
+                n = std::min<int64_t>(n, r->nsteps - r->done);
+            }
+            int rc = 0;
+            if (!B.valid) {
+                rc = lg::capture_bucket_step(cs.data(), (int)cs.size(), B.st, &B.bg);
+                B.valid = rc == 0;
+            }
+            if (!rc) rc = lg::bucket_prologue(cs.data(), (int)cs.size());
+            int64_t launched = 0;
+            for (int64_t k = 0; k < n && !rc; k++) {
+                if (cudaGraphLaunch(B.bg.exec, B.st) != cudaSuccess) rc = LESGPU_ERR_CUDA;
+                else launched++;
+            }
+            if (!rc && cudaEventRecord(B.ev, B.st) != cudaSuccess) rc = LESGPU_ERR_CUDA;
             if (rc) {
-                r->rc = rc;
-                finish(S, r, S_FAILED);
-                S->active.erase(S->active.begin() + q);
+                // nothing of theirs may be in flight when the members are freed
+                if (launched > 0) cudaStreamSynchronize(B.st);
+                for (Request *r : B.members) r->rc = rc;     // they leave at the next pass
+                ++it;
                 continue;
             }
-            r->inflight = n;
-            q++;
+            lg::bucket_replayed(cs.data(), (int)cs.size(), (int)n);
+            for (Request *r : B.members) r->inflight = n;
+            B.inflight = n;
+            ++it;
         }
         if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
-    // shutdown: drop whatever is still resident
+    // shutdown: wait for the work in flight, drop whatever is still resident
+    for (auto &kv : buckets) {
+        if (kv.second.inflight > 0) cudaEventSynchronize(kv.second.ev);
+        destroy_bucket(kv.second);
+    }
+    buckets.clear();
     for (Request *r : S->active) finish(S, r, S_CANCELLED);
     S->active.clear();
 }

@@ -1,7 +1,10 @@
 """Serving loop (lesgpu_server_*): cases submitted together are admitted by
-device footprint, advance concurrently on their own streams, and each
-result is the same as the case run alone (bitwise: every kernel of a case is
-deterministic and no work is shared between cases)."""
+device footprint and advance together, the cases of one grid shape as one
+size bucket (one graph per bucket step, the multigrid mode solves of the
+bucket's cases in one batched launch); each result is the same as the case
+run alone (bitwise: every kernel of a case is deterministic, and the batched
+launch gives every case's modes the arithmetic of its own solve).  SPECS
+holds buckets of three and two cases."""
 import time
 
 import numpy as np
@@ -14,7 +17,9 @@ pytestmark = pytest.mark.gpu
 
 SPECS = [dict(grid=(64, 48, 8), body=abi.BODY_CYLINDER, center=(0.2, -0.1, 0.5 * np.pi), re=100.0, pr=0.71, seed=1),
          dict(grid=(64, 48, 8), body=abi.BODY_SQUARE, center=(-0.3, 0.25, 0.5 * np.pi), re=300.0, pr=7.0, seed=2),
-         dict(grid=(96, 64, 16), body=abi.BODY_SPHERE, center=(0.1, 0.4, 0.5 * np.pi), re=60.0, pr=0.71, seed=3)]
+         dict(grid=(96, 64, 16), body=abi.BODY_SPHERE, center=(0.1, 0.4, 0.5 * np.pi), re=60.0, pr=0.71, seed=3),
+         dict(grid=(96, 64, 16), body=abi.BODY_CYLINDER, center=(-0.2, 0.1, 0.5 * np.pi), re=150.0, pr=7.0, seed=4),
+         dict(grid=(64, 48, 8), body=abi.BODY_SPHERE, center=(0.0, 0.0, 0.5 * np.pi), re=40.0, pr=0.71, seed=5)]
 NSTEPS = 6
 
 
