@@ -711,7 +711,10 @@ def run_ours(args):
                           "time": rep["time"], "dt": rep["dt"]},
                 "step_ms": main["step_ms"], "autotune": main["autotune"]}
         if args.serving_cases > 0 and world == 1:
-            line["serving"] = serving_sample(args, lib)
+            try:
+                line["serving"] = serving_sample(args, lib)
+            except Exception as e:          # the measured line above stands; say what failed
+                line["serving"] = {"error": f"{type(e).__name__}: {e}"}
         if other is not None:
             line["fp64"] = {"value": other["value"], "ms_per_step": other["ms_per_step"],
                             "kernels_per_step": other["kernels_per_step"], "clocks": other["clocks"],

@@ -446,6 +446,10 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
     for (long long i = 0; i <= d.n1; i++) c->h_f2fx[i] = g->f2fxi[i];
     for (long long kk = 0; kk <= d.n3; kk++) c->h_f2fz[kk] = g->f2fzi[kk];
     if (!A.ok) { lesgpu_destroy(c); return LESGPU_ERR_OOM; }
+    // the tables went up by cudaMemcpy on the legacy stream, whose DMA may
+    // still be in flight; the case stream (non-blocking) is ordered after it
+    // only by this wait
+    if (cudaStreamSynchronize(cudaStreamLegacy) != cudaSuccess) { lesgpu_destroy(c); return LESGPU_ERR_CUDA; }
     launch_red_weights(c);
     c->h_grid = g;
     rc = poisson_init(c);
@@ -556,6 +560,10 @@ extern "C" int lesgpu_load_ibm(lesgpu_case *c, const lesgpu_ibm *b) {
         if (b->kstar[q] != 1.0) c->conj_general = 1;
     c->kp.c.conj_tables = c->kp.c.iconjg == 1 && c->conj_general;
     if (!A.ok) return LESGPU_ERR_OOM;
+    // the tables above went up by cudaMemcpy on the legacy stream, whose DMA
+    // may still be in flight; the case stream (non-blocking) is ordered after
+    // it only by this wait
+    if (cudaStreamSynchronize(cudaStreamLegacy) != cudaSuccess) return LESGPU_ERR_CUDA;
     launch_red_weights(c);
     mark_mirror(c, kMirConj);
     launch_mirror(c, kMirConj);
@@ -809,7 +817,14 @@ int capture_bucket_step(lesgpu_case **cs, int n, cudaStream_t st, BucketGraph *b
         for (int msub = 1; msub <= 3; msub++)
             for (int q = 0; q < n; q++) mg2d_batch_args(cs[q], msub, h.data() + ((size_t)(msub - 1) * n + q) * sz);
         if (cudaMalloc(&bg->d_args, h.size()) != cudaSuccess) return LESGPU_ERR_OOM;
-        if (cudaMemcpy(bg->d_args, h.data(), h.size(), cudaMemcpyHostToDevice) != cudaSuccess) return LESGPU_ERR_CUDA;
+        // on the bucket stream, which the graph is launched on: a plain
+        // cudaMemcpy from pageable memory may return before its DMA lands and
+        // is ordered on the legacy stream only, which the non-blocking bucket
+        // stream does not wait for -- the batched solve would read the
+        // pointers in these arguments before they are there
+        if (cudaMemcpyAsync(bg->d_args, h.data(), h.size(), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            return LESGPU_ERR_CUDA;
     }
     int rc = bucket_prologue(cs, n);
     if (rc) return rc;

@@ -373,26 +373,46 @@ namespace lg {
 // partials in block order -- the same fixed order as a separate finalize
 // kernel, so results are deterministic -- applies g and resets the ticket.
 template <int NV, bool MAX, class F, class G>
-__global__ void __launch_bounds__(kThreads) k_reduce_fin(KP p, Box b, F f, G g) {
+__global__ void __launch_bounds__(kThreads, 4) k_reduce_fin(KP p, Box b, F f, G g) {
     __shared__ int last;
     double v[NV];
 #pragma unroll
     for (int q = 0; q < NV; q++) v[q] = MAX ? -1.0e308 : 0.0;
     const long long n = b.count();
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
-         t += (long long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        b.at(t, i, j, k);
-        double w[NV];
-        f(p, i, j, k, w);
-        // a sum skips exact +0 terms (integer test): FP64 adds issue on the
-        // narrow FP64 pipe, and several reductions carry terms that are zero
-        // almost everywhere (the wall-shear sums of meanpg)
+    const long long S = (long long)gridDim.x * blockDim.x;
+    // a sum skips exact +0 terms (integer test): FP64 adds issue on the
+    // narrow FP64 pipe, and several reductions carry terms that are zero
+    // almost everywhere (the wall-shear sums of meanpg)
+    auto add_terms = [&](const double (&w)[NV]) {
 #pragma unroll
         for (int q = 0; q < NV; q++) {
             if (MAX) v[q] = fmax(v[q], w[q]);
             else if (__double_as_longlong(w[q]) != 0LL) v[q] = v[q] + w[q];
         }
+    };
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    // U elements of the thread's sequence per pass (4, 2 for six sums: 4
+    // blocks of 256 threads an SM leave 64 registers a thread): their terms
+    // are all formed (loads in flight together) before they are added, in
+    // the sequence's order -- the sums of the one-at-a-time loop, bit for bit
+    constexpr int U = NV >= 6 ? 2 : 4;
+    for (; t + (U - 1) * S < n; t += U * S) {
+        double w[U][NV];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            int i, j, k;
+            b.at(t + u * S, i, j, k);
+            f(p, i, j, k, w[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) add_terms(w[u]);
+    }
+    for (; t < n; t += S) {
+        int i, j, k;
+        b.at(t, i, j, k);
+        double w[NV];
+        f(p, i, j, k, w);
+        add_terms(w);
     }
     block_reduce<NV, MAX>(v);
     if (threadIdx.x == 0) {

@@ -234,7 +234,11 @@ void remove_active(lesgpu_server *S, Request *r) {
 
 void worker_main(lesgpu_server *S) {
     cudaSetDevice(S->device);
-    std::map<std::pair<long long, long long>, Bucket> buckets;
+    std::map<std::pair<std::pair<long long, long long>, int>, Bucket> buckets;
+    // LESGPU_SERVER_BUCKET_MAX: cases per bucket at most (a full bucket's
+    // shape opens another one); 0 or unset: no limit
+    const char *bm = getenv("LESGPU_SERVER_BUCKET_MAX");
+    const size_t bucket_max = bm && atoi(bm) >= 1 ? (size_t)atoi(bm) : (size_t)-1;
     // resident cases share the GPU: their multigrid solves are latency-bound,
     // so each gets small clusters and the solves of different cases run side
     // by side (2 blocks per cluster doubled the served throughput of the
@@ -282,7 +286,13 @@ void worker_main(lesgpu_server *S) {
             }
             // a bucket is the cases of one shape and options that can share
             // a batched solve (the same multigrid cluster size and levels)
-            Bucket &B = buckets[std::make_pair(bucket_key(r), lg::mg2d_batch_key(r->c))];
+            const std::pair<long long, long long> shape(bucket_key(r), lg::mg2d_batch_key(r->c));
+            int slot = 0;
+            for (;; slot++) {
+                auto f = buckets.find(std::make_pair(shape, slot));
+                if (f == buckets.end() || f->second.members.size() < bucket_max) break;
+            }
+            Bucket &B = buckets[std::make_pair(shape, slot)];
             if (!B.st) {
                 if (cudaStreamCreateWithFlags(&B.st, cudaStreamNonBlocking) != cudaSuccess ||
                     cudaEventCreateWithFlags(&B.ev, cudaEventDisableTiming) != cudaSuccess)
