@@ -236,15 +236,19 @@ void worker_main(lesgpu_server *S) {
     cudaSetDevice(S->device);
     std::map<std::pair<std::pair<long long, long long>, int>, Bucket> buckets;
     // LESGPU_SERVER_BUCKET_MAX: cases per bucket at most (a full bucket's
-    // shape opens another one); 0 or unset: no limit
+    // shape opens another one); 0: no limit.  Default 1: on the benchmark
+    // stream (16 cases arriving at once) one case per graph served 128
+    // Mcell-steps/s against 117 with whole buckets in one graph -- the
+    // batched solve joins every case of its bucket before each Poisson
+    // solve, while separate graphs let the cases' phases overlap freely
     const char *bm = getenv("LESGPU_SERVER_BUCKET_MAX");
-    const size_t bucket_max = bm && atoi(bm) >= 1 ? (size_t)atoi(bm) : (size_t)-1;
+    const size_t bucket_max = bm ? (atoi(bm) >= 1 ? (size_t)atoi(bm) : (size_t)-1) : 1;
     // resident cases share the GPU: their multigrid solves are latency-bound,
     // so each gets small clusters and the solves of different cases run side
-    // by side (2 blocks per cluster doubled the served throughput of the
-    // benchmark stream against the single-case choice of up to 16)
+    // by side (4 blocks per cluster served the benchmark stream fastest, 128
+    // Mcell-steps/s against 122 with 2 and 101 with 8)
     const char *cap = getenv("LESGPU_SERVER_MG_CLUSTER");
-    lg::set_mg_cluster_cap(cap && atoi(cap) >= 1 ? atoi(cap) : 2);
+    lg::set_mg_cluster_cap(cap && atoi(cap) >= 1 ? atoi(cap) : 4);
     for (;;) {
         // ---- admission
         for (;;) {

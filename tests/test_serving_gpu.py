@@ -1,10 +1,11 @@
 """Serving loop (lesgpu_server_*): cases submitted together are admitted by
-device footprint and advance together, the cases of one grid shape as one
-size bucket (one graph per bucket step, the multigrid mode solves of the
-bucket's cases in one batched launch); each result is the same as the case
-run alone (bitwise: every kernel of a case is deterministic, and the batched
-launch gives every case's modes the arithmetic of its own solve).  SPECS
-holds buckets of three and two cases."""
+device footprint and advance together -- by default each in its own graph;
+with LESGPU_SERVER_BUCKET_MAX=0 the cases of one grid shape as one size
+bucket (one graph per bucket step, the multigrid mode solves of the bucket's
+cases in one batched launch).  Either way each result is the same as the
+case run alone (bitwise: every kernel of a case is deterministic, and the
+batched launch gives every case's modes the arithmetic of its own solve).
+SPECS holds buckets of three and two cases."""
 import time
 
 import numpy as np
@@ -40,8 +41,10 @@ def wait_all(srv, tickets, timeout=120.0):
         time.sleep(0.01)
 
 
+@pytest.mark.parametrize("bucket_max", ["1", "0"])
 @pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED])
-def test_results_same_alone_and_in_the_mix(precision):
+def test_results_same_alone_and_in_the_mix(monkeypatch, precision, bucket_max):
+    monkeypatch.setenv("LESGPU_SERVER_BUCKET_MAX", bucket_max)     # read when the server starts
     lib = leswht_gb300.load_library()
     srv = serving.Server(lib, hbm_budget_bytes=32 << 30, max_active=8, steps_in_flight=2)
     tickets = [srv.submit(serving.build_case(sp, precision), NSTEPS) for sp in SPECS]
