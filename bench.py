@@ -621,14 +621,17 @@ def serving_sample(args, lib):
     out = {"sample": f"{args.serving_cases} cases x {args.serving_steps} steps of the seeded serving stream "
                      "(Poisson arrivals 2/s; grids 64x48x8 .. 256x192x32; circle/square/sphere; Re 40-1000; "
                      "Pr 0.71/7); the benchmark stream has 256 cases x 500 steps"}
-    # real-time replay: latency (p50/p99 from arrival) at the stream's rate
-    srv = serving.Server(lib, hbm_budget_bytes=64 << 30, max_active=16, steps_in_flight=4)
-    mixed = serving.serve(srv, stream, precision=abi.PREC_MIXED)
-    srv.close()
-    seq = serving.one_at_a_time(lib, stream, precision=abi.PREC_FP64)
-    out["realtime"] = {"served_mixed": {k: mixed[k] for k in keys + ("completed",)},
-                       "one_at_a_time_fp64": {k: seq[k] for k in keys},
-                       "throughput_ratio": mixed["mcell_steps_per_s"] / seq["mcell_steps_per_s"]}
+    if args.serving_legs in ("both", "realtime"):
+        # real-time replay: latency (p50/p99 from arrival) at the stream's rate
+        srv = serving.Server(lib, hbm_budget_bytes=64 << 30, max_active=16, steps_in_flight=4)
+        mixed = serving.serve(srv, stream, precision=abi.PREC_MIXED)
+        srv.close()
+        seq = serving.one_at_a_time(lib, stream, precision=abi.PREC_FP64)
+        out["realtime"] = {"served_mixed": {k: mixed[k] for k in keys + ("completed",)},
+                           "one_at_a_time_fp64": {k: seq[k] for k in keys},
+                           "throughput_ratio": mixed["mcell_steps_per_s"] / seq["mcell_steps_per_s"]}
+    if args.serving_legs == "realtime":
+        return out
     # saturated: every case arrives at once, so aggregate throughput is the
     # GPU's, not the arrival rate's
     srv = serving.Server(lib, hbm_budget_bytes=64 << 30, max_active=16, steps_in_flight=4)
@@ -752,12 +755,17 @@ def main():
     ap.add_argument("--serving-cases", type=int, default=16,
                     help="cases in the serving sample (0: skip it)")
     ap.add_argument("--serving-steps", type=int, default=40)
+    ap.add_argument("--serving-legs", default="both", choices=["both", "realtime", "saturated"],
+                    help="which arrival patterns the serving sample replays (both by default)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--accuracy-steps", type=int, default=2000,
                     help="steps of the 64^3 channel's mixed-vs-FP64 statistics comparison (0: skip); "
                          "statistics over the second half")
     ap.add_argument("--accuracy-c3-steps", type=int, default=0,
                     help="steps of the same comparison on the Re=3900 cylinder, 256x192x64 (0: skip)")
+    ap.add_argument("--serving-only", action="store_true",
+                    help="run only the serving sample (--serving-cases x --serving-steps) and print it as one "
+                         "JSON line, e.g. --serving-cases 64 --serving-steps 500 --serving-legs saturated")
     ap.add_argument("--accuracy-only", action="store_true",
                     help="run only the statistics comparisons and print them as one JSON line")
     ap.add_argument("--profile-one-step", action="store_true",
@@ -770,6 +778,12 @@ def main():
         return run_reference(args)
     if args.profile_one_step:
         return profile_one_step(args)
+    if args.serving_only:
+        import torch
+        import leswht_gb300
+        torch.cuda.set_device(0)
+        print(json.dumps({"serving": serving_sample(args, leswht_gb300.load_library())}))
+        return 0
     if args.accuracy_only:
         import torch
         torch.cuda.set_device(0)
