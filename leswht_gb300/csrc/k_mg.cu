@@ -941,8 +941,8 @@ __device__ int part_mg2d(const Mode &m, const Mode &mb, double test, bool &uncon
 
 // mg_mg2d_mixed with the level-partitioned phases
 template <int MC>
-__device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, const Mode &mb, const ModeT<float> &fb,
-                               double test, bool &unconv, int r, int cs, double2 *hbuf) {
+__device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, const ModeT<float> &fb, double test,
+                               bool &unconv, int r, int cs, double2 *hbuf) {
     const MgArgs &a = m.a;
     const int nlev = a.nlev, lc = a.lc, n2m = a.n2m;
     float2 *hf = reinterpret_cast<float2 *>(hbuf);
@@ -962,7 +962,6 @@ __device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, const Mode 
     double sumres = part_top_resid_mixed(m, f, r, cs, par);
     par ^= 1;
     if (sumres < test) return 0;
-    const int c0 = a.iimg[0][0], nc0 = a.iimg[0][1] - c0 + 1;
     for (int kk = 1; kk <= a.mgitr; kk++) {
         for (int ilev = nlev - 1; ilev > lc; ilev--) part_down<MC>(f, ilev, r, cs, hf);
         if (r == 0) {
@@ -970,19 +969,10 @@ __device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, const Mode 
                 mg_relax<MC>(fb, ilev, 0.0f, 1);
                 mg_godown(fb, ilev);
             }
-            for (int t = threadIdx.x; t < nc0 * n2m; t += blockDim.x) {     // coarsest level in FP64
-                const int i = c0 + t % nc0, j = 1 + t / nc0;
-                const float2 rr = fb.R(i, j);
-                mb.R(i, j) = make_double2((double)rr.x, (double)rr.y);
-            }
-            __syncthreads();
-            mg_relax<MC>(mb, 0, 0.0, a.nbli);
-            for (int t = threadIdx.x; t < nc0 * n2m; t += blockDim.x) {
-                const int i = c0 + t % nc0, j = 1 + t / nc0;
-                const double2 g = mb.G(i, j);
-                fb.G(i, j) = make_float2((float)g.x, (float)g.y);
-            }
-            __syncthreads();
+            // the coarsest level's nbli relaxations in FP32 too: GB300's FP64
+            // latency made their dependent line recurrences a third of the
+            // cycle in FP64, and they only refine the FP32 correction
+            mg_relax<MC>(fb, 0, 0.0f, a.nbli);
             for (int ilev = 0; ilev < lc; ilev++) {
                 mg_goup(fb, ilev);
                 mg_relax<MC>(fb, ilev + 1, 1.0f, 1);
@@ -1032,7 +1022,6 @@ __device__ __forceinline__ void zft_mode(const MgArgs &ga, int kv, double2 *hbuf
         it = mg_gsor2d<MC>(m, test, unconv);
     } else if (a.mixed) {
         it = part_mg2d_mixed<MC>(m, *reinterpret_cast<const ModeT<float> *>(sb.f),
-                                 *reinterpret_cast<const Mode *>(sb.mb),
                                  *reinterpret_cast<const ModeT<float> *>(sb.fb), test, unconv, r, cs, hbuf);
     } else {
         it = part_mg2d<MC>(m, *reinterpret_cast<const Mode *>(sb.mb), test, unconv, r, cs, hbuf);

@@ -196,26 +196,21 @@ __global__ void __launch_bounds__(kThreads) k_filter(KP p, Box b, FiltBatch F) {
         const R *cfz = mir<R>(p).cfz1 + 3 * k;
         const R z0 = zin ? R(cfz[0]) : R(0.0), z1 = zin ? R(cfz[1]) : R(0.0), z2 = zin ? R(cfz[2]) : R(0.0);
         const long long r0 = g.ix(0, j, k), rm = g.ix(0, j, km), rp = g.ix(0, j, kp);
-        auto filt = [&](const R *s) -> R {
-            if (!zin) return X.filt ? c0 * s[r0 + X.im] + c1 * s[r0 + i] + c2 * s[r0 + X.ip] : s[r0 + i];
-            if (X.filt) {
+        for (int a = 0; a < F.na; a++) {
+            const R *s = static_cast<const R *>(F.src[a]);
+            R out;
+            if (!zin) {
+                out = X.filt ? c0 * s[r0 + X.im] + c1 * s[r0 + i] + c2 * s[r0 + X.ip] : s[r0 + i];
+            } else if (X.filt) {
                 const R xm = c0 * s[rm + X.im] + c1 * s[rm + i] + c2 * s[rm + X.ip];
                 const R x0 = c0 * s[r0 + X.im] + c1 * s[r0 + i] + c2 * s[r0 + X.ip];
                 const R xp = c0 * s[rp + X.im] + c1 * s[rp + i] + c2 * s[rp + X.ip];
-                return z0 * xm + z1 * x0 + z2 * xp;
+                out = z0 * xm + z1 * x0 + z2 * xp;
+            } else {
+                out = z0 * s[rm + i] + z1 * s[r0 + i] + z2 * s[rp + i];
             }
-            return z0 * s[rm + i] + z1 * s[r0 + i] + z2 * s[rp + i];
-        };
-        // two arrays per pass: both stencils' loads are in flight before
-        // either result is stored (the outputs are not the inputs)
-        int a = 0;
-        for (; a + 1 < F.na; a += 2) {
-            const R o0 = filt(static_cast<const R *>(F.src[a]));
-            const R o1 = filt(static_cast<const R *>(F.src[a + 1]));
-            static_cast<R *>(F.dst[a])[r0 + i] = o0;
-            static_cast<R *>(F.dst[a + 1])[r0 + i] = o1;
+            static_cast<R *>(F.dst[a])[r0 + i] = out;
         }
-        if (a < F.na) static_cast<R *>(F.dst[a])[r0 + i] = filt(static_cast<const R *>(F.src[a]));
     }
 }
 
