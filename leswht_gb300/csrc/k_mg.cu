@@ -455,8 +455,11 @@ __device__ __noinline__ int mg_gsor2d(const Mode &m, double test, bool &unconv) 
 //     restriction, or a prolongation + relaxation, needs one cluster
 //     barrier at its end and only block barriers inside;
 //   * the levels of at most kCoarseLines lines run on block 0 alone with
-//     block barriers (the phases above with a block-local mode view); the
-//     other blocks wait at one cluster barrier;
+//     block barriers (the phases above with a block-local mode view), the
+//     other blocks waiting at one cluster barrier -- or, in the mixed form
+//     with 16-block clusters, spread over the cluster with a cluster barrier
+//     per phase, all but the coarsest level's relaxations (measured faster
+//     both ways on the 256x192 modes, slower with small clusters);
 //   * the defect of a partitioned level goes to rd, not over the restricted
 //     residual in rs that neighbouring blocks still read in the same phase
 //     (the reference overwrites resd with it, poiss_z_ft.f90:447-452; the
@@ -962,23 +965,43 @@ __device__ int part_mg2d_mixed(const Mode &m, const ModeT<float> &f, const ModeT
     double sumres = part_top_resid_mixed(m, f, r, cs, par);
     par ^= 1;
     if (sumres < test) return 0;
+    // with 16-block clusters the coarse levels (up to kCoarseLines lines, two
+    // per warp of one block) run faster spread over the cluster despite a
+    // cluster barrier per phase; with smaller clusters, on block 0
+    const bool wide = cs >= 16;
     for (int kk = 1; kk <= a.mgitr; kk++) {
         for (int ilev = nlev - 1; ilev > lc; ilev--) part_down<MC>(f, ilev, r, cs, hf);
-        if (r == 0) {
+        if (wide) {
+            // the coarse levels' relaxations, defects, restrictions and
+            // prolongations spread over the cluster (a cluster barrier per
+            // phase), the coarsest level's relaxations on block 0
             for (int ilev = lc; ilev >= 1; ilev--) {
-                mg_relax<MC>(fb, ilev, 0.0f, 1);
-                mg_godown(fb, ilev);
+                mg_relax<MC>(f, ilev, 0.0f, 1);
+                mg_godown(f, ilev);
             }
-            // the coarsest level's nbli relaxations in FP32 too: GB300's FP64
-            // latency made their dependent line recurrences a third of the
-            // cycle in FP64, and they only refine the FP32 correction
-            mg_relax<MC>(fb, 0, 0.0f, a.nbli);
+            if (r == 0) mg_relax<MC>(fb, 0, 0.0f, a.nbli);
+            cooperative_groups::this_cluster().sync();
             for (int ilev = 0; ilev < lc; ilev++) {
-                mg_goup(fb, ilev);
-                mg_relax<MC>(fb, ilev + 1, 1.0f, 1);
+                mg_goup(f, ilev);
+                mg_relax<MC>(f, ilev + 1, 1.0f, 1);
             }
+        } else {
+            if (r == 0) {
+                for (int ilev = lc; ilev >= 1; ilev--) {
+                    mg_relax<MC>(fb, ilev, 0.0f, 1);
+                    mg_godown(fb, ilev);
+                }
+                // the coarsest level's nbli relaxations in FP32 too: GB300's
+                // FP64 latency made their dependent line recurrences a third of
+                // the cycle in FP64, and they only refine the FP32 correction
+                mg_relax<MC>(fb, 0, 0.0f, a.nbli);
+                for (int ilev = 0; ilev < lc; ilev++) {
+                    mg_goup(fb, ilev);
+                    mg_relax<MC>(fb, ilev + 1, 1.0f, 1);
+                }
+            }
+            cooperative_groups::this_cluster().sync();
         }
-        cooperative_groups::this_cluster().sync();
         for (int ilev = lc; ilev <= nlev - 2; ilev++) part_up<MC>(f, ilev, r, cs, hf);
         part_top_relax<MC>(f, r, cs, 1.0f, true, true, f.rs, hf, &m, false);
         sumres = part_top_resid_mixed(m, f, r, cs, par);
