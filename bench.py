@@ -729,6 +729,8 @@ def run_ours(args):
             acc = {}
             if args.accuracy_steps > 0:
                 acc["channel64"] = long_horizon("channel64", args.accuracy_steps, args.accuracy_steps // 2)
+            if args.accuracy_c1_steps > 0:
+                acc["cylinder100"] = long_horizon("cylinder100", args.accuracy_c1_steps, args.accuracy_c1_steps // 2)
             if args.accuracy_c3_steps > 0:
                 acc["cylinder3900"] = long_horizon("cylinder3900", args.accuracy_c3_steps, args.accuracy_c3_steps // 2)
             if acc:
@@ -761,6 +763,9 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=2000,
                     help="steps of the 64^3 channel's mixed-vs-FP64 statistics comparison (0: skip); "
                          "statistics over the second half")
+    ap.add_argument("--accuracy-c1-steps", type=int, default=0,
+                    help="steps of the same comparison on the Re=100 cylinder, 128x96x16, long enough for "
+                         "vortex shedding to set in (0: skip)")
     ap.add_argument("--accuracy-c3-steps", type=int, default=0,
                     help="steps of the same comparison on the Re=3900 cylinder, 256x192x64 (0: skip)")
     ap.add_argument("--serving-only", action="store_true",
@@ -790,6 +795,8 @@ def main():
         acc = {}
         if args.accuracy_steps > 0:
             acc["channel64"] = long_horizon("channel64", args.accuracy_steps, args.accuracy_steps // 2)
+        if args.accuracy_c1_steps > 0:
+            acc["cylinder100"] = long_horizon("cylinder100", args.accuracy_c1_steps, args.accuracy_c1_steps // 2)
         if args.accuracy_c3_steps > 0:
             acc["cylinder3900"] = long_horizon("cylinder3900", args.accuracy_c3_steps, args.accuracy_c3_steps // 2)
         print(json.dumps({"accuracy": acc}))
