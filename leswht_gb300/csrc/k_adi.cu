@@ -764,36 +764,63 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
     const long long qb = g.ix(i0, j0, k0);                // row 0 of line 0
     const AdiFacs<R> F = adi_facs<R>(p, A.comp, DIR);
     // ---- stage the tile (z: lines fastest, x: rows fastest: both coalesced);
-    // each thread issues the loads of four elements before it stores them
+    // each thread issues the loads of four elements before it stores them.
+    // tp[r]: row r's slot in a line (rows 0..n), formed once per block.
     const int nt = blockDim.x;
-    const int ntot = kTileLines * (n + 1);
-    for (int t0 = threadIdx.x; t0 < ntot; t0 += 4 * nt) {
-        double sv[4];
-        R fv[4];
-        int pos[4];
+    int *tp = reinterpret_cast<int *>(Fv + kTileLines * lp);
+    for (int r = threadIdx.x; r <= n; r += nt) tp[r] = tpos(r, m, pm);
+    __syncthreads();
+    if (DIR == 2) {
+        const int ntot = kTileLines * (n + 1);
+        for (int t0 = threadIdx.x; t0 < ntot; t0 += 4 * nt) {
+            double sv[4];
+            R fv[4];
+            int pos[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const int t = t0 + u * nt;
-            pos[u] = -1;
-            if (t < ntot) {
-                int w, r;
-                if (DIR == 2) { w = t % kTileLines; r = t / kTileLines; }
-                else { w = t / (n + 1); r = t % (n + 1); }
-                if (w < nl) {
-                    const long long q = qb + w * lstride + (long long)r * stride;
-                    pos[u] = w * lp + tpos(r, m, pm);
-                    fv[u] = R(F.nv[q + F.oa]);
-                    sv[u] = r < n ? A.src[q] : 0.0;
-                    if (r >= n) pos[u] = -2 - pos[u];      // the factor row only
+            for (int u = 0; u < 4; u++) {
+                const int t = t0 + u * nt;
+                pos[u] = -1;
+                if (t < ntot) {
+                    const int w = t % kTileLines, r = t / kTileLines;
+                    if (w < nl) {
+                        const long long q = qb + w * lstride + (long long)r * stride;
+                        pos[u] = w * lp + tp[r];
+                        fv[u] = R(F.nv[q + F.oa]);
+                        sv[u] = r < n ? A.src[q] : 0.0;
+                        if (r >= n) pos[u] = -2 - pos[u];      // the factor row only
+                    }
                 }
             }
-        }
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-            if (pos[u] == -1) continue;
-            const int ps = pos[u] >= 0 ? pos[u] : -2 - pos[u];
-            Fv[ps] = R(1.0) + F.cre * fv[u];
-            if (pos[u] >= 0) S[ps] = diag * R(sv[u]);
+            for (int u = 0; u < 4; u++) {
+                if (pos[u] == -1) continue;
+                const int ps = pos[u] >= 0 ? pos[u] : -2 - pos[u];
+                Fv[ps] = R(1.0) + F.cre * fv[u];
+                if (pos[u] >= 0) S[ps] = diag * R(sv[u]);
+            }
+        }
+    } else {
+        // a thread takes one row of four lines at a time
+        for (int r = threadIdx.x; r <= n; r += nt) {
+            const int pr = tp[r];
+            for (int w0 = 0; w0 < nl; w0 += 4) {
+                double sv[4];
+                R fv[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (w0 + u < nl) {
+                        const long long q = qb + (w0 + u) * lstride + (long long)r * stride;
+                        fv[u] = R(F.nv[q + F.oa]);
+                        sv[u] = r < n ? A.src[q] : 0.0;
+                    }
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (w0 + u < nl) {
+                        const int ps = (w0 + u) * lp + pr;
+                        Fv[ps] = R(1.0) + F.cre * fv[u];
+                        if (r < n) S[ps] = diag * R(sv[u]);
+                    }
+            }
         }
     }
     __syncthreads();
@@ -804,14 +831,17 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
         const int r0 = lane * m;
         const int cnt = max(0, min(m, n - r0));
         const int l1 = A.l1;
-        auto coef = [&](int r, R &a, R &c) {
-            a = R(F.ma[l1 + r]) * Fl[tpos(r, m, pm)];
-            c = R(F.mc[l1 + r]) * Fl[tpos(r + 1, m, pm)];
+        // the lane's rows sit at lb .. lb + m - 1; the row after its chunk is
+        // the next lane's first, at lb + pm (row n's factor included)
+        const int lb = lane * pm;
+        auto coef = [&](int u, R &a, R &c) {
+            a = R(F.ma[l1 + r0 + u]) * Fl[lb + u];
+            c = R(F.mc[l1 + r0 + u]) * Fl[u + 1 < m ? lb + u + 1 : lb + pm];
         };
         if (!PER) {
             // c of the row before the chunk
             R cprev0 = R(0.0);
-            if (lane > 0 && r0 - 1 < n) cprev0 = R(F.mc[l1 + r0 - 1]) * Fl[tpos(r0, m, pm)];
+            if (lane > 0 && r0 - 1 < n) cprev0 = R(F.mc[l1 + r0 - 1]) * Fl[lb];
             if (r0 - 1 >= n) cprev0 = R(0.0);
             // 1. pivots: Moebius composition, scan, re-run
             M22<R> T{R(1.0), R(0.0), R(0.0), R(1.0)};
@@ -821,7 +851,7 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
                 for (int u = 0; u < MC; u++)
                     if (u < cnt) {
                         R a, c;
-                        coef(r0 + u, a, c);
+                        coef(u, a, c);
                         const R b = diag - a - c;
                         M22<R> Tj{R(0.0), R(1.0), -a * cp, b};
                         T = mmul_chunk(Tj, T);
@@ -842,7 +872,7 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
                 for (int u = 0; u < MC; u++)
                     if (u < cnt) {
                         R a, c;
-                        coef(r0 + u, a, c);
+                        coef(u, a, c);
                         const R b = diag - a - c;
                         if (lane == 0 && u == 0) bet = rcp_pivot(b);
                         else bet = rcp_pivot(b - a * (cp * bet));
@@ -856,9 +886,9 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
             for (int u = 0; u < MC; u++)
                 if (u < cnt) {
                     R a, c;
-                    coef(r0 + u, a, c);
+                    coef(u, a, c);
                     const R mj = (lane == 0 && u == 0) ? R(0.0) : -a * betv[u];
-                    Bb = mj * Bb + Sl[tpos(r0 + u, m, pm)] * betv[u];
+                    Bb = mj * Bb + Sl[lb + u] * betv[u];
                     Aa = mj * Aa;
                 }
             R y = scan_affine_up<R, 32>(Aa, Bb, lane, R(0.0));
@@ -866,8 +896,8 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
             for (int u = 0; u < MC; u++)
                 if (u < cnt) {
                     R a, c;
-                    coef(r0 + u, a, c);
-                    const int ps = tpos(r0 + u, m, pm);
+                    coef(u, a, c);
+                    const int ps = lb + u;
                     y = (lane == 0 && u == 0) ? Sl[ps] * betv[u] : (Sl[ps] - a * y) * betv[u];
                     Sl[ps] = y;
                 }
@@ -877,9 +907,9 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
             for (int u = MC - 1; u >= 0; u--)
                 if (u < cnt) {
                     R a, c;
-                    coef(r0 + u, a, c);
+                    coef(u, a, c);
                     const R gn = (r0 + u == n - 1) ? R(0.0) : (u + 1 < cnt ? c * betv[u] : gnext0);
-                    Dd = -gn * Dd + Sl[tpos(r0 + u, m, pm)];
+                    Dd = -gn * Dd + Sl[lb + u];
                     Cc = -gn * Cc;
                 }
             R x = scan_affine_down<R, 32>(Cc, Dd, lane);
@@ -887,9 +917,9 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
             for (int u = MC - 1; u >= 0; u--)
                 if (u < cnt) {
                     R a, c;
-                    coef(r0 + u, a, c);
+                    coef(u, a, c);
                     const R gn = (r0 + u == n - 1) ? R(0.0) : (u + 1 < cnt ? c * betv[u] : gnext0);
-                    const int ps = tpos(r0 + u, m, pm);
+                    const int ps = lb + u;
                     x = Sl[ps] - gn * x;
                     Sl[ps] = x;
                 }
@@ -900,7 +930,7 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
             for (int u = 0; u < MC; u++)
                 if (u < cnt) {
                     R a, c;
-                    coef(r0 + u, a, c);
+                    coef(u, a, c);
                     const R b = diag - a - c;
                     M22<R> Tj{R(0.0), -c, a, b};
                     T = mmul_chunk(Tj, T);
@@ -914,13 +944,13 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
             for (int u = 0; u < MC; u++)
                 if (u < cnt) {
                     R a, c;
-                    coef(r0 + u, a, c);
+                    coef(u, a, c);
                     const R b = diag - a - c;
                     const R pn = rcp_pivot((lane == 0 && u == 0) ? b : b + a * qq);
                     qq = -c * pn;
                     pv[u] = pn;
                     const R mj = -a * pn;
-                    Bb = mj * Bb + Sl[tpos(r0 + u, m, pm)] * pn;
+                    Bb = mj * Bb + Sl[lb + u] * pn;
                     Aa = mj * Aa;
                 }
             // incoming s and f
@@ -941,8 +971,8 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
                 for (int u = 0; u < MC; u++)
                     if (u < cnt) {
                         R a, c;
-                        coef(r0 + u, a, c);
-                        const int ps = tpos(r0 + u, m, pm);
+                        coef(u, a, c);
+                        const int ps = lb + u;
                         const R rv = Sl[ps];
                         if (r0 + u == n - 1) { al = a; bl = diag - a - c; cl = c; fnl = rv; }
                         if (lane == 0 && u == 0) {
@@ -962,10 +992,10 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
             for (int u = MC - 1; u >= 0; u--)
                 if (u < cnt) {
                     R a, c;
-                    coef(r0 + u, a, c);
+                    coef(u, a, c);
                     const bool last = (r0 + u == n - 1);
                     const R mq = last ? R(0.0) : -c * pv[u];
-                    const R os = last ? R(1.0) : sv[u], oe = last ? R(0.0) : Sl[tpos(r0 + u, m, pm)];
+                    const R os = last ? R(1.0) : sv[u], oe = last ? R(0.0) : Sl[lb + u];
                     Ds = mq * Ds + os;
                     De = mq * De + oe;
                     Cs = mq * Cs;
@@ -985,8 +1015,8 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
                 for (int u = MC - 1; u >= 0; u--)
                     if (u < cnt) {
                         R a, c;
-                        coef(r0 + u, a, c);
-                        const int ps = tpos(r0 + u, m, pm);
+                        coef(u, a, c);
+                        const int ps = lb + u;
                         if (r0 + u == n - 1) { Sc = R(1.0); Ec = R(0.0); }
                         else {
                             const R qj = -c * pv[u];
@@ -1007,13 +1037,13 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
             Sp = __shfl_sync(0xffffffffu, Sp, own_pen);
             Ep = __shfl_sync(0xffffffffu, Ep, own_pen);
             const R S0 = __shfl_sync(0xffffffffu, sv[0], 0);
-            const R E0 = Sl[tpos(0, m, pm)];
+            const R E0 = Sl[0];
             const R fj2 = (fnl - cl * E0 - al * Ep) / (cl * S0 + al * Sp + bl);
             __syncwarp();
 #pragma unroll
             for (int u = 0; u < MC; u++)
                 if (u < cnt) {
-                    const int ps = tpos(r0 + u, m, pm);
+                    const int ps = lb + u;
                     Sl[ps] = (r0 + u == n - 1) ? fj2 : fj2 * sv[u] + Sl[ps];
                 }
         }
@@ -1021,28 +1051,45 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
     __syncthreads();
     // ---- write back: the solution, or added to the field (four elements a
     // thread at a time, the field's loads first)
-    for (int t0 = threadIdx.x; t0 < kTileLines * n; t0 += 4 * nt) {
-        long long qv[4];
-        double dv[4];
-        R xv[4];
+    if (DIR == 2) {
+        for (int t0 = threadIdx.x; t0 < kTileLines * n; t0 += 4 * nt) {
+            long long qv[4];
+            double dv[4];
+            R xv[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const int t = t0 + u * nt;
-            qv[u] = -1;
-            if (t < kTileLines * n) {
-                int w2, r;
-                if (DIR == 2) { w2 = t % kTileLines; r = t / kTileLines; }
-                else { w2 = t / n; r = t % n; }
-                if (w2 < nl) {
-                    qv[u] = qb + w2 * lstride + (long long)r * stride;
-                    xv[u] = S[w2 * lp + tpos(r, m, pm)];
-                    if (A.add) dv[u] = A.dst[qv[u]];
+            for (int u = 0; u < 4; u++) {
+                const int t = t0 + u * nt;
+                qv[u] = -1;
+                if (t < kTileLines * n) {
+                    const int w2 = t % kTileLines, r = t / kTileLines;
+                    if (w2 < nl) {
+                        qv[u] = qb + w2 * lstride + (long long)r * stride;
+                        xv[u] = S[w2 * lp + tp[r]];
+                        if (A.add) dv[u] = A.dst[qv[u]];
+                    }
                 }
             }
-        }
 #pragma unroll
-        for (int u = 0; u < 4; u++)
-            if (qv[u] >= 0) A.dst[qv[u]] = A.add ? dv[u] + xv[u] : (double)xv[u];
+            for (int u = 0; u < 4; u++)
+                if (qv[u] >= 0) A.dst[qv[u]] = A.add ? dv[u] + xv[u] : (double)xv[u];
+        }
+    } else {
+        for (int r = threadIdx.x; r < n; r += nt) {
+            const int pr = tp[r];
+            for (int w0 = 0; w0 < nl; w0 += 4) {
+                double dv[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (w0 + u < nl && A.add) dv[u] = A.dst[qb + (w0 + u) * lstride + (long long)r * stride];
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (w0 + u < nl) {
+                        const long long q = qb + (w0 + u) * lstride + (long long)r * stride;
+                        const R xv = S[(w0 + u) * lp + pr];
+                        A.dst[q] = A.add ? dv[u] + xv : (double)xv;
+                    }
+            }
+        }
     }
 }
 
@@ -1057,7 +1104,8 @@ static TileShape tile_shape(int nmax) {
     t.pm = (t.m % 2 == 0) ? t.m + 1 : t.m + 2;
     t.lp = 32 * t.pm + 1;
     t.mc = t.m <= 4 ? 4 : t.m <= 8 ? 8 : t.m <= 12 ? 12 : t.m <= 16 ? 16 : 0;
-    t.smem = (size_t)2 * kTileLines * t.lp * sizeof(float);
+    // the two tile arrays, then the row-slot table (rows 0 .. 32 m)
+    t.smem = (size_t)2 * kTileLines * t.lp * sizeof(float) + (size_t)(32 * t.m + 1) * sizeof(int);
     return t;
 }
 

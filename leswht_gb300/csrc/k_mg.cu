@@ -314,9 +314,20 @@ __device__ __forceinline__ typename V2<T>::t mg_defect(const ModeT<T> &m, typena
     return src;
 }
 
+// The max of every block's *v (a shared-memory variable at the same place in
+// each block) through distributed shared memory: lane q reads block q's
+// (clusters have at most 16 blocks), then a warp max; every thread gets the
+// same result (max is exact and order-free).
+__device__ __forceinline__ double dsm_max(cooperative_groups::cluster_group &cl, double *v) {
+    const int lane = threadIdx.x & 31;
+    double r = lane < (int)cl.num_blocks() ? *cl.map_shared_rank(v, lane) : 0.0;
+    for (int o = 16; o > 0; o >>= 1) r = fmax(r, __shfl_xor_sync(0xffffffffu, r, o));
+    return r;
+}
+
 // Max over the cluster: warp shuffles, one value per block in shared memory,
 // then every thread reads every block's value through distributed shared
-// memory, in the same order, so all threads get the same result.
+// memory, so all threads get the same result.
 __device__ double cluster_max(double v) {
     __shared__ double sh[kMgThreads / 32];
     __shared__ double blk;
@@ -332,8 +343,7 @@ __device__ double cluster_max(double v) {
         blk = r;
     }
     cl.sync();
-    double r = 0.0;
-    for (int q = 0; q < (int)cl.num_blocks(); q++) r = fmax(r, *cl.map_shared_rank(&blk, q));
+    const double r = dsm_max(cl, &blk);
     cl.sync();          // nobody overwrites blk before every block has read it
     return r;
 }
@@ -366,22 +376,56 @@ __device__ __noinline__ void mg_relax(const ModeT<T> &m, int ilev, T oldv, int i
     }
 }
 
+// Points of godown and goup go kMgBatch<T> at a time per thread: all of
+// their loads before any of their stores (no point of either phase reads
+// what another point of it writes), so the loads are in flight together
+// instead of one round trip per point behind the previous point's store.
+// FP32 phases only: batched FP64 points raise the register demand of the
+// whole call graph, and ptxas then spills in the 192- and 256-row instances.
+template <class T> constexpr int kMgBatch = sizeof(T) == 4 ? 4 : 1;
+
 // godown, poiss_z_ft.f90:438-463
 template <class T>
 __device__ __noinline__ void mg_godown(const ModeT<T> &m, int ilev) {
+    using V = typename V2<T>::t;
+    constexpr int B = kMgBatch<T>;
     const MgArgs &a = m.a;
     const int ibg = a.iimg[ilev][0], iend = a.iimg[ilev][1], n2m = a.n2m, nt = m.nt();
     const int nf = iend - ibg + 1;
-    for (int t = m.tid(); t < nf * n2m; t += nt) {
-        const int i = ibg + t % nf, j = 1 + t / nf;
-        m.R(i, j) = mg_defect(m, m.R(i, j), m.gg, a.ldg, i, j);
+    for (int t0 = m.tid(); t0 < nf * n2m; t0 += B * nt) {
+        V d[B];
+#pragma unroll
+        for (int q = 0; q < B; q++) {
+            const int t = t0 + q * nt;
+            if (t < nf * n2m) {
+                const int i = ibg + t % nf, j = 1 + t / nf;
+                d[q] = mg_defect(m, m.R(i, j), m.gg, a.ldg, i, j);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < B; q++) {
+            const int t = t0 + q * nt;
+            if (t < nf * n2m) m.R(ibg + t % nf, 1 + t / nf) = d[q];
+        }
     }
     m.sync();
     const int cl = a.iimg[ilev - 1][0], nc = a.iimg[ilev - 1][1] - cl + 1;
-    for (int t = m.tid(); t < nc * n2m; t += nt) {
-        const int i = cl + t % nc, j = 1 + t / nc, f = ibg + 2 * (i - cl);
-        const typename V2<T>::t r1 = m.R(f, j), r2 = m.R(f + 1, j);
-        m.R(i, j) = typename V2<T>::t{r1.x * m.s.cor1[i] + r2.x * m.s.cor2[i], r1.y * m.s.cor1[i] + r2.y * m.s.cor2[i]};
+    for (int t0 = m.tid(); t0 < nc * n2m; t0 += B * nt) {
+        V d[B];
+#pragma unroll
+        for (int q = 0; q < B; q++) {
+            const int t = t0 + q * nt;
+            if (t < nc * n2m) {
+                const int i = cl + t % nc, j = 1 + t / nc, f = ibg + 2 * (i - cl);
+                const V r1 = m.R(f, j), r2 = m.R(f + 1, j);
+                d[q] = V{r1.x * m.s.cor1[i] + r2.x * m.s.cor2[i], r1.y * m.s.cor1[i] + r2.y * m.s.cor2[i]};
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < B; q++) {
+            const int t = t0 + q * nt;
+            if (t < nc * n2m) m.R(cl + t % nc, 1 + t / nc) = d[q];
+        }
     }
     m.sync();
 }
@@ -389,21 +433,33 @@ __device__ __noinline__ void mg_godown(const ModeT<T> &m, int ilev) {
 // goup, poiss_z_ft.f90:411-435 / poiss_x_ft.f90:401-419
 template <class T>
 __device__ __noinline__ void mg_goup(const ModeT<T> &m, int ilev) {
+    using V = typename V2<T>::t;
+    constexpr int B = kMgBatch<T>;
     const MgArgs &a = m.a;
     const MgSet<T> &s = m.s;
     const int cl = a.iimg[ilev][0], ce = a.iimg[ilev][1], n2m = a.n2m, nt = m.nt();
     const int fb = a.iimg[ilev + 1][0], nc = ce - cl + 1;
-    for (int t = m.tid(); t < nc * n2m; t += nt) {
-        const int i = cl + t % nc, j = 1 + t / nc, f = fb + 1 + 2 * (i - cl);
-        typename V2<T>::t g = m.G(f, j);
-        const typename V2<T>::t g1 = m.G(i, j);
-        if (i < ce || a.xft) {
-            const typename V2<T>::t g2 = m.G(a.ipm[i], j);
-            g = typename V2<T>::t{g.x + s.coi1[i] * g1.x + s.coi2[i] * g2.x, g.y + s.coi1[i] * g1.y + s.coi2[i] * g2.y};
-        } else {
-            g = typename V2<T>::t{g.x + s.coi1[i] * g1.x, g.y + s.coi1[i] * g1.y};
+    for (int t0 = m.tid(); t0 < nc * n2m; t0 += B * nt) {
+        V d[B];
+#pragma unroll
+        for (int q = 0; q < B; q++) {
+            const int t = t0 + q * nt;
+            if (t < nc * n2m) {
+                const int i = cl + t % nc, j = 1 + t / nc, f = fb + 1 + 2 * (i - cl);
+                const V g = m.G(f, j), g1 = m.G(i, j);
+                if (i < ce || a.xft) {
+                    const V g2 = m.G(a.ipm[i], j);
+                    d[q] = V{g.x + s.coi1[i] * g1.x + s.coi2[i] * g2.x, g.y + s.coi1[i] * g1.y + s.coi2[i] * g2.y};
+                } else {
+                    d[q] = V{g.x + s.coi1[i] * g1.x, g.y + s.coi1[i] * g1.y};
+                }
+            }
         }
-        m.G(f, j) = g;
+#pragma unroll
+        for (int q = 0; q < B; q++) {
+            const int t = t0 + q * nt;
+            if (t < nc * n2m) m.G(fb + 1 + 2 * (t % nc), 1 + t / nc) = d[q];
+        }
     }
     m.sync();
 }
@@ -852,9 +908,7 @@ __device__ double part_cluster_max(double v, int par) {
         blk[par] = r;
     }
     cl.sync();
-    double r = 0.0;
-    for (int q = 0; q < (int)cl.num_blocks(); q++) r = fmax(r, *cl.map_shared_rank(&blk[par], q));
-    return r;
+    return dsm_max(cl, &blk[par]);
 }
 
 // toplevel's residual on the partitioned top level (FP64 form): R = B - A G
