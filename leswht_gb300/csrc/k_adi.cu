@@ -727,17 +727,19 @@ __global__ void __launch_bounds__(128, MINB) k_adis(KP p, AdiBatch B) {
 // Tiled warp-scan sweeps (x and z sweeps in FP32).  A block stages a tile
 // of kTileLines lines -- consecutive i for z lines, consecutive j for x
 // lines -- in shared memory with coalesced loads: the right-hand side
-// (times the diagonal, in R) and the line's viscosity factor 1 + cre nu at
-// every face; one warp then solves one line from shared memory with the
-// recurrences and chunk layout of k_adis (W = 32 lanes, lane l owning rows
-// l*m .. l*m+m-1), re-forming the coefficients from the factors in each
-// pass instead of holding them in registers, and the tile is written back
-// coalesced.  The serial z sweep moved each line's elimination factors
+// (times the diagonal, in R) and every row's coefficients a and c (the
+// metric terms times the viscosity factors 1 + cre nu of the row's two
+// faces), formed once there; one warp then solves one line from shared
+// memory with the recurrences and chunk layout of k_adis (W = 32 lanes,
+// lane l owning rows l*m .. l*m+m-1), reading the coefficients from shared
+// memory in each pass instead of holding them in registers, and the tile is
+// written back coalesced.  The serial z sweep moved each line's elimination factors
 // through HBM (2.6 times the sweep's algorithmic bytes) and k_adis held a
 // 12-row chunk's coefficients in registers (16 warps an SM); here the HBM
 // traffic is the operands once and 32 warps fit on an SM.  Results equal
 // the 32-lane k_adis's: the same arithmetic on the same chunks.
 constexpr int kTileLines = 16;
+constexpr size_t kTileSmemMax = 110 * 1024;   // two blocks an SM
 
 // position of row r of a line in shared memory: lane chunks of m rows with
 // a pitch pm (odd: the 32 lanes' rows fall in 32 different banks)
@@ -747,7 +749,8 @@ template <class R, int DIR, bool PER, int MC>
 __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, int m, int pm, int lp) {
     extern __shared__ __align__(16) unsigned char adit_smem[];
     R *S = reinterpret_cast<R *>(adit_smem);             // lines x lp: diag*rhs -> y -> x
-    R *Fv = S + kTileLines * lp;                          // lines x lp: 1 + cre nu at rows 0..n
+    R *Ca = S + kTileLines * lp;                          // lines x lp: a of rows 0..n-1
+    R *Cc = Ca + kTileLines * lp;                         // lines x lp: c of rows 0..n-1
     const AdiArgs &A = B.a[blockIdx.y];
     const DGrid &g = p.g;
     const R diag = (A.comp == CT) ? p.S->acoefi * p.c.pr : p.S->acoefi;
@@ -767,7 +770,7 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
     // each thread issues the loads of four elements before it stores them.
     // tp[r]: row r's slot in a line (rows 0..n), formed once per block.
     const int nt = blockDim.x;
-    int *tp = reinterpret_cast<int *>(Fv + kTileLines * lp);
+    int *tp = reinterpret_cast<int *>(Cc + kTileLines * lp);
     for (int r = threadIdx.x; r <= n; r += nt) tp[r] = tpos(r, m, pm);
     __syncthreads();
     if (DIR == 2) {
@@ -795,14 +798,20 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
             for (int u = 0; u < 4; u++) {
                 if (pos[u] == -1) continue;
                 const int ps = pos[u] >= 0 ? pos[u] : -2 - pos[u];
-                Fv[ps] = R(1.0) + F.cre * fv[u];
-                if (pos[u] >= 0) S[ps] = diag * R(sv[u]);
+                const int r = (t0 + u * nt) / kTileLines, w = (t0 + u * nt) % kTileLines;
+                const R f = R(1.0) + F.cre * fv[u];
+                if (pos[u] >= 0) {
+                    S[ps] = diag * R(sv[u]);
+                    Ca[ps] = R(F.ma[A.l1 + r]) * f;
+                }
+                if (r >= 1) Cc[w * lp + tp[r - 1]] = R(F.mc[A.l1 + r - 1]) * f;
             }
         }
     } else {
         // a thread takes one row of four lines at a time
         for (int r = threadIdx.x; r <= n; r += nt) {
-            const int pr = tp[r];
+            const int pr = tp[r], pr1 = r >= 1 ? tp[r - 1] : 0;
+            const R ma_r = r < n ? R(F.ma[A.l1 + r]) : R(0.0), mc_r1 = r >= 1 ? R(F.mc[A.l1 + r - 1]) : R(0.0);
             for (int w0 = 0; w0 < nl; w0 += 4) {
                 double sv[4];
                 R fv[4];
@@ -817,8 +826,12 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
                 for (int u = 0; u < 4; u++)
                     if (w0 + u < nl) {
                         const int ps = (w0 + u) * lp + pr;
-                        Fv[ps] = R(1.0) + F.cre * fv[u];
-                        if (r < n) S[ps] = diag * R(sv[u]);
+                        const R f = R(1.0) + F.cre * fv[u];
+                        if (r < n) {
+                            S[ps] = diag * R(sv[u]);
+                            Ca[ps] = ma_r * f;
+                        }
+                        if (r >= 1) Cc[(w0 + u) * lp + pr1] = mc_r1 * f;
                     }
             }
         }
@@ -827,21 +840,19 @@ __global__ void __launch_bounds__(kTileLines * 32, 2) k_adit(KP p, AdiBatch B, i
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (w < nl) {
         R *Sl = S + w * lp;
-        const R *Fl = Fv + w * lp;
+        const R *Al = Ca + w * lp, *Cl = Cc + w * lp;
         const int r0 = lane * m;
         const int cnt = max(0, min(m, n - r0));
-        const int l1 = A.l1;
-        // the lane's rows sit at lb .. lb + m - 1; the row after its chunk is
-        // the next lane's first, at lb + pm (row n's factor included)
+        // the lane's rows sit at lb .. lb + m - 1
         const int lb = lane * pm;
         auto coef = [&](int u, R &a, R &c) {
-            a = R(F.ma[l1 + r0 + u]) * Fl[lb + u];
-            c = R(F.mc[l1 + r0 + u]) * Fl[u + 1 < m ? lb + u + 1 : lb + pm];
+            a = Al[lb + u];
+            c = Cl[lb + u];
         };
         if (!PER) {
             // c of the row before the chunk
             R cprev0 = R(0.0);
-            if (lane > 0 && r0 - 1 < n) cprev0 = R(F.mc[l1 + r0 - 1]) * Fl[lb];
+            if (lane > 0 && r0 - 1 < n) cprev0 = Cl[lb - pm + m - 1];
             if (r0 - 1 >= n) cprev0 = R(0.0);
             // 1. pivots: Moebius composition, scan, re-run
             M22<R> T{R(1.0), R(0.0), R(0.0), R(1.0)};
@@ -1104,8 +1115,8 @@ static TileShape tile_shape(int nmax) {
     t.pm = (t.m % 2 == 0) ? t.m + 1 : t.m + 2;
     t.lp = 32 * t.pm + 1;
     t.mc = t.m <= 4 ? 4 : t.m <= 8 ? 8 : t.m <= 12 ? 12 : t.m <= 16 ? 16 : 0;
-    // the two tile arrays, then the row-slot table (rows 0 .. 32 m)
-    t.smem = (size_t)2 * kTileLines * t.lp * sizeof(float) + (size_t)(32 * t.m + 1) * sizeof(int);
+    // the three tile arrays, then the row-slot table (rows 0 .. 32 m)
+    t.smem = (size_t)3 * kTileLines * t.lp * sizeof(float) + (size_t)(32 * t.m + 1) * sizeof(int);
     return t;
 }
 
@@ -1113,7 +1124,7 @@ template <int DIR, bool PER, int MC>
 static void adit_launch3(dim3 grid, const TileShape &ts, cudaStream_t st, const KP &kp, const AdiBatch &B) {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_adit<float, DIR, PER, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        cudaFuncSetAttribute(k_adit<float, DIR, PER, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemMax);
         attr = true;
     }
     k_adit<float, DIR, PER, MC><<<grid, kTileLines * 32, ts.smem, st>>>(kp, B, ts.m, ts.pm, ts.lp);
@@ -1136,7 +1147,7 @@ static bool adit_launch(lesgpu_case *c, const AdiBatch &B, int ncomp, int nmax) 
     const int dir = B.a[0].dir;
     if (dir == 1) return false;
     const TileShape ts = tile_shape(nmax);
-    if (ts.mc == 0 || ts.smem > 100 * 1024) return false;
+    if (ts.mc == 0 || ts.smem > kTileSmemMax) return false;
     int tiles = 0;
     for (int q = 0; q < ncomp; q++) {
         const AdiArgs &A = B.a[q];
