@@ -36,11 +36,23 @@ template <class V> __device__ __forceinline__ const V *twid(const DevPlan &P);
 template <> __device__ __forceinline__ const double2 *twid<double2>(const DevPlan &P) { return P.tw; }
 template <> __device__ __forceinline__ const float2 *twid<float2>(const DevPlan &P) { return P.twf; }
 
+// x / d for 0 <= x, 1 <= d and x d < 2^32 by one high multiply with
+// m = ceil(2^32 / d): x m / 2^32 exceeds x / d by less than x / 2^32 < 1 / d,
+// which never reaches the next integer.  (d = 1: m = 0, the quotient is x.)
+// The index arithmetic of the transforms divides by run-time line counts and
+// stage strides; an integer division costs some twenty instructions.
+struct FastDiv {
+    unsigned m;
+    __device__ explicit FastDiv(int d) : m(d > 1 ? 0xFFFFFFFFu / (unsigned)d + 1u : 0u) {}
+    __device__ int div(int x) const { return m ? (int)__umulhi((unsigned)x, m) : x; }
+};
+
 // Run all stages on L interleaved lines; returns the buffer holding the result.
 template <class V>
 __device__ V *block_fft(V *b0, V *b1, int L, const DevPlan &P, int inv) {
     const int N = P.n;
     const V *tw = twid<V>(P);
+    const FastDiv dL(L);
     int Ns = 1;
     V *in = b0, *out = b1;
     for (int st = 0; st < P.nst; st++) {
@@ -48,15 +60,17 @@ __device__ V *block_fft(V *b0, V *b1, int L, const DevPlan &P, int inv) {
         const int NR = N / R;
         const int twstep = N / (Ns * R);
         const int work = NR * L;
+        const FastDiv dNs(Ns);
         for (int w = threadIdx.x; w < work; w += blockDim.x) {
-            const int l = w % L, jb = w / L;
+            const int jb = dL.div(w), l = w - jb * L;
+            const int jq = dNs.div(jb), jm = jb - jq * Ns;
             V v[8];
-            const int jm = jb % Ns;
 #pragma unroll 4
             for (int r = 0; r < R; r++) {
                 V x = in[(jb + r * NR) * L + l];
                 if (r > 0 && jm > 0) {
-                    V t = tw[(jm * r * twstep) % N];
+                    // jm r twstep < Ns R N / (Ns R) = N: inside the table
+                    V t = tw[jm * r * twstep];
                     if (inv) t.y = -t.y;
                     x = cmul(x, t);
                 }
@@ -78,15 +92,18 @@ __device__ V *block_fft(V *b0, V *b1, int L, const DevPlan &P, int inv) {
             } else {
                 for (int m = 0; m < R; m++) {
                     V acc = v[0];
+                    int mr = 0;                     // (m r) mod R
                     for (int r = 1; r < R; r++) {
-                        V t = tw[((m * r) % R) * NR];
+                        mr += m;
+                        if (mr >= R) mr -= R;
+                        V t = tw[mr * NR];
                         if (inv) t.y = -t.y;
                         acc = cadd(acc, cmul(v[r], t));
                     }
                     y[m] = acc;
                 }
             }
-            const int idxD = (jb / Ns) * Ns * R + jm;
+            const int idxD = jq * Ns * R + jm;
             for (int r = 0; r < R; r++) out[(idxD + r * Ns) * L + l] = y[r];
         }
         __syncthreads();
@@ -122,8 +139,9 @@ __global__ void k_fft_z_fwd(KP p, const double *src, V *ccap, DevPlan P, int L, 
     const int N = P.n;
     V *b0 = sm, *b1 = sm + (size_t)N * L;
     const int i0 = 1 + blockIdx.x * 2 * L, j = 1 + blockIdx.y;
+    const FastDiv d2L(2 * L);
     for (int w = threadIdx.x; w < N * 2 * L; w += blockDim.x) {
-        const int l2 = w % (2 * L), e = w / (2 * L);       // consecutive threads: consecutive i
+        const int e = d2L.div(w), l2 = w - e * 2 * L;       // consecutive threads: consecutive i
         const int i = i0 + l2;
         const T val = (i <= g.n1m) ? T(src[g.ix(i, j, e + 1)]) : T(0.0);
         T *slot = reinterpret_cast<T *>(&b0[e * L + (l2 >> 1)]);
@@ -133,10 +151,10 @@ __global__ void k_fft_z_fwd(KP p, const double *src, V *ccap, DevPlan P, int L, 
     const V *res = block_fft(b0, b1, L, P, 0);
     const int n3mh = g.n3mh;
     for (int w = threadIdx.x; w < n3mh * 2 * L; w += blockDim.x) {
-        const int l2 = w % (2 * L), kk = w / (2 * L);
+        const int kk = d2L.div(w), l2 = w - kk * 2 * L;
         const int i = i0 + l2, l = l2 >> 1;
         if (i > g.n1m) continue;
-        const V c = res[kk * L + l], cn = res[((N - kk) % N) * L + l];
+        const V c = res[kk * L + l], cn = res[(kk == 0 ? 0 : N - kk) * L + l];
         // A_k = (C_k + conj C_{N-k}) / 2 ; B_k = -i (C_k - conj C_{N-k}) / 2
         const V v = (l2 & 1) ? V{T(0.5) * (c.y + cn.y), T(-0.5) * (c.x - cn.x)}
                              : V{T(0.5) * (c.x + cn.x), T(0.5) * (c.y - cn.y)};
@@ -168,8 +186,9 @@ __global__ void k_fft_z_inv(KP p, const V *ccap, DevPlan P, int L, long long sk,
         const V s = ccap[(i - 1) + sk * (N - e) + sj * (j - 1)];
         return V{s.x, -s.y};
     };
+    const FastDiv dL(L), d2L(2 * L);
     for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
-        const int l = w % L, e = w / L;
+        const int e = dL.div(w), l = w - e * L;
         const V x = coef(i0 + 2 * l, e), y = coef(i0 + 2 * l + 1, e);
         b0[e * L + l] = V{x.x - y.y, x.y + y.x};     // Z = X + i Y
     }
@@ -177,7 +196,7 @@ __global__ void k_fft_z_inv(KP p, const V *ccap, DevPlan P, int L, long long sk,
     const V *res = block_fft(b0, b1, L, P, 1);
     const double dn = 1.0 / (double)N;
     for (int w = threadIdx.x; w < N * 2 * L; w += blockDim.x) {
-        const int l2 = w % (2 * L), e = w / (2 * L);
+        const int e = d2L.div(w), l2 = w - e * 2 * L;
         const int i = i0 + l2;
         if (i <= g.n1m) {
             const V r = res[e * L + (l2 >> 1)];
@@ -197,8 +216,9 @@ __global__ void k_fft_x(V *ccap, int nlines, DevPlan P, int L, int inv) {
     const int N = P.n;
     V *b0 = sm, *b1 = sm + (size_t)N * L;
     int line0 = blockIdx.x * L;
+    const FastDiv dN(N);
     for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
-        int e = w % N, l = w / N;           // coalesced global read along the line
+        int l = dN.div(w), e = w - l * N;   // coalesced global read along the line
         int line = line0 + l;
         b0[e * L + l] = (line < nlines) ? ccap[(size_t)line * N + e] : V{T(0.0), T(0.0)};
     }
@@ -206,7 +226,7 @@ __global__ void k_fft_x(V *ccap, int nlines, DevPlan P, int L, int inv) {
     V *res = block_fft(b0, b1, L, P, inv);
     const T dn = T(1.0 / (double)N);
     for (int w = threadIdx.x; w < N * L; w += blockDim.x) {
-        int e = w % N, l = w / N;
+        int l = dN.div(w), e = w - l * N;
         int line = line0 + l;
         if (line < nlines) {
             V v = res[e * L + l];
