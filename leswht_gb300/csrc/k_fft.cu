@@ -47,6 +47,63 @@ struct FastDiv {
     __device__ int div(int x) const { return m ? (int)__umulhi((unsigned)x, m) : x; }
 };
 
+// One radix-R stage of block_fft on L interleaved lines, R a compile-time
+// constant (the plans hold radices 4, 2, 3 and 5 only), so the butterfly and
+// its loads, twiddles and stores unroll.  Twiddle index jm r twstep < Ns R
+// N / (Ns R) = N: inside the table.
+template <class V, int R>
+__device__ __forceinline__ void fft_stage(const V *in, V *out, int L, const FastDiv &dL, int N, int Ns,
+                                          const V *tw, int inv) {
+    const int NR = N / R;
+    const int twstep = N / (Ns * R);
+    const int work = NR * L;
+    const FastDiv dNs(Ns);
+    for (int w = threadIdx.x; w < work; w += blockDim.x) {
+        const int jb = dL.div(w), l = w - jb * L;
+        const int jq = dNs.div(jb), jm = jb - jq * Ns;
+        V v[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            V x = in[(jb + r * NR) * L + l];
+            if (r > 0 && jm > 0) {
+                V t = tw[jm * r * twstep];
+                if (inv) t.y = -t.y;
+                x = cmul(x, t);
+            }
+            v[r] = x;
+        }
+        V y[R];
+        if constexpr (R == 2) {
+            y[0] = cadd(v[0], v[1]);
+            y[1] = csub(v[0], v[1]);
+        } else if constexpr (R == 4) {
+            V s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+            V s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
+            // forward: W4 = -i; inverse: +i
+            V jd13 = inv ? V{-d13.y, d13.x} : V{d13.y, -d13.x};
+            y[0] = cadd(s02, s13);
+            y[2] = csub(s02, s13);
+            y[1] = cadd(d02, jd13);
+            y[3] = csub(d02, jd13);
+        } else {
+#pragma unroll
+            for (int m = 0; m < R; m++) {
+                V acc = v[0];
+#pragma unroll
+                for (int r = 1; r < R; r++) {
+                    V t = tw[((m * r) % R) * NR];
+                    if (inv) t.y = -t.y;
+                    acc = cadd(acc, cmul(v[r], t));
+                }
+                y[m] = acc;
+            }
+        }
+        const int idxD = jq * Ns * R + jm;
+#pragma unroll
+        for (int r = 0; r < R; r++) out[(idxD + r * Ns) * L + l] = y[r];
+    }
+}
+
 // Run all stages on L interleaved lines; returns the buffer holding the result.
 template <class V>
 __device__ V *block_fft(V *b0, V *b1, int L, const DevPlan &P, int inv) {
@@ -57,54 +114,11 @@ __device__ V *block_fft(V *b0, V *b1, int L, const DevPlan &P, int inv) {
     V *in = b0, *out = b1;
     for (int st = 0; st < P.nst; st++) {
         const int R = P.rad[st];
-        const int NR = N / R;
-        const int twstep = N / (Ns * R);
-        const int work = NR * L;
-        const FastDiv dNs(Ns);
-        for (int w = threadIdx.x; w < work; w += blockDim.x) {
-            const int jb = dL.div(w), l = w - jb * L;
-            const int jq = dNs.div(jb), jm = jb - jq * Ns;
-            V v[8];
-#pragma unroll 4
-            for (int r = 0; r < R; r++) {
-                V x = in[(jb + r * NR) * L + l];
-                if (r > 0 && jm > 0) {
-                    // jm r twstep < Ns R N / (Ns R) = N: inside the table
-                    V t = tw[jm * r * twstep];
-                    if (inv) t.y = -t.y;
-                    x = cmul(x, t);
-                }
-                v[r] = x;
-            }
-            V y[8];
-            if (R == 2) {
-                y[0] = cadd(v[0], v[1]);
-                y[1] = csub(v[0], v[1]);
-            } else if (R == 4) {
-                V s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
-                V s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
-                // forward: W4 = -i; inverse: +i
-                V jd13 = inv ? V{-d13.y, d13.x} : V{d13.y, -d13.x};
-                y[0] = cadd(s02, s13);
-                y[2] = csub(s02, s13);
-                y[1] = cadd(d02, jd13);
-                y[3] = csub(d02, jd13);
-            } else {
-                for (int m = 0; m < R; m++) {
-                    V acc = v[0];
-                    int mr = 0;                     // (m r) mod R
-                    for (int r = 1; r < R; r++) {
-                        mr += m;
-                        if (mr >= R) mr -= R;
-                        V t = tw[mr * NR];
-                        if (inv) t.y = -t.y;
-                        acc = cadd(acc, cmul(v[r], t));
-                    }
-                    y[m] = acc;
-                }
-            }
-            const int idxD = jq * Ns * R + jm;
-            for (int r = 0; r < R; r++) out[(idxD + r * Ns) * L + l] = y[r];
+        switch (R) {
+        case 4: fft_stage<V, 4>(in, out, L, dL, N, Ns, tw, inv); break;
+        case 2: fft_stage<V, 2>(in, out, L, dL, N, Ns, tw, inv); break;
+        case 3: fft_stage<V, 3>(in, out, L, dL, N, Ns, tw, inv); break;
+        default: fft_stage<V, 5>(in, out, L, dL, N, Ns, tw, inv); break;
         }
         __syncthreads();
         V *tmp = in; in = out; out = tmp;
