@@ -113,7 +113,8 @@ __device__ V *block_fft(V *b0, V *b1, int L, const DevPlan &P, int inv) {
     int Ns = 1;
     V *in = b0, *out = b1;
     for (int st = 0; st < P.nst; st++) {
-        const int R = P.rad[st];
+        const int code = (int)(P.radc >> (2 * st)) & 3;
+        const int R = code == 0 ? 4 : code == 1 ? 2 : code == 2 ? 3 : 5;
         switch (R) {
         case 4: fft_stage<V, 4>(in, out, L, dL, N, Ns, tw, inv); break;
         case 2: fft_stage<V, 2>(in, out, L, dL, N, Ns, tw, inv); break;
@@ -127,11 +128,20 @@ __device__ V *block_fft(V *b0, V *b1, int L, const DevPlan &P, int inv) {
     return in;
 }
 
+void pack_radices(DevPlan &d) {
+    d.radc = 0ULL;
+    for (int s = 0; s < d.nst && s < 24; s++) {
+        const unsigned long long c = d.rad[s] == 4 ? 0ULL : d.rad[s] == 2 ? 1ULL : d.rad[s] == 3 ? 2ULL : 3ULL;
+        d.radc |= c << (2 * s);
+    }
+}
+
 DevPlan devplan(const FftPlan &p) {
     DevPlan d;
     d.n = p.n;
     d.nst = p.nst;
     for (int s = 0; s < 24; s++) d.rad[s] = p.rad[s];
+    pack_radices(d);
     d.tw = p.tw;
     d.twf = p.twf;
     return d;

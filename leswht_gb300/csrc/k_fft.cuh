@@ -8,9 +8,15 @@ namespace lg {
 struct DevPlan {
     int n, nst;
     int rad[24];
+    // the radices again, two bits a stage (0: 4, 1: 2, 2: 3, 3: 5): the
+    // device reads its stage's radix from this word, where indexing rad[]
+    // with the stage number would copy the whole plan to local memory
+    unsigned long long radc;
     const double2 *tw;
     const float2 *twf;
 };
+// fill radc from rad[0 .. nst-1]
+void pack_radices(DevPlan &d);
 
 // dynamic shared memory a transform block may take (below the per-block
 // opt-in limit, with room for the kernels' static shared memory)

@@ -196,8 +196,12 @@ __global__ void __launch_bounds__(kThreads) k_filter(KP p, Box b, FiltBatch F) {
         const R *cfz = mir<R>(p).cfz1 + 3 * k;
         const R z0 = zin ? R(cfz[0]) : R(0.0), z1 = zin ? R(cfz[1]) : R(0.0), z2 = zin ? R(cfz[2]) : R(0.0);
         const long long r0 = g.ix(0, j, k), rm = g.ix(0, j, km), rp = g.ix(0, j, kp);
+        // sources and destinations are distinct arrays: two arrays' loads
+        // can be in flight at once
+#pragma unroll 2
         for (int a = 0; a < F.na; a++) {
-            const R *s = static_cast<const R *>(F.src[a]);
+            const R *__restrict__ s = static_cast<const R *>(F.src[a]);
+            R *__restrict__ d = static_cast<R *>(F.dst[a]);
             R out;
             if (!zin) {
                 out = X.filt ? c0 * s[r0 + X.im] + c1 * s[r0 + i] + c2 * s[r0 + X.ip] : s[r0 + i];
@@ -209,7 +213,7 @@ __global__ void __launch_bounds__(kThreads) k_filter(KP p, Box b, FiltBatch F) {
             } else {
                 out = z0 * s[rm + i] + z1 * s[r0 + i] + z2 * s[rp + i];
             }
-            static_cast<R *>(F.dst[a])[r0 + i] = out;
+            d[r0 + i] = out;
         }
     }
 }

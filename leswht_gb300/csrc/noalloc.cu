@@ -159,6 +159,8 @@ extern "C" int lesgpu_poisson_ftft_noalloc(const lesgpu_grid *g, const double *d
     if (plan_radices(n1m, px.rad, &px.nst) || plan_radices(n3m, pz.rad, &pz.nst)) return LESGPU_ERR_UNSUPPORTED;
     px.n = n1m;
     pz.n = n3m;
+    lg::pack_radices(px);
+    lg::pack_radices(pz);
 
     // layout of the scratch array
     const size_t nspec = (size_t)n1m * n3mh * n2m;
