@@ -455,11 +455,12 @@ __global__ void k_ytri_lu(KP p, const double *ak1, const double *ak3, double *yb
 // pinned as poiss_ftft.f90:93-112.  The coefficients are real, so the real
 // and imaginary parts are independent recurrences: one thread each (twice
 // the lines in flight); operands are loaded 8 rows ahead.
-// S: the spectrum's storage (double, or float in the mixed form's correction
-// solve, whose arithmetic here stays FP64)
+// S: the spectrum's storage and the arithmetic type: double, or float in the
+// mixed form's FP32 solves (with FP32 copies of the LU tables), whose result
+// the FP64 defect correction refines
 template <class S>
-__global__ void __launch_bounds__(64) k_ytri(KP p, S *ccap, const double *ybet, const double *ygam,
-                                             const double *yam, const double *pinref) {
+__global__ void __launch_bounds__(64) k_ytri(KP p, S *ccap, const S *ybet, const S *ygam,
+                                             const S *yam, const S *pinref) {
     const DGrid &g = p.g;
     const int n1m = g.n1m, n2m = g.n2m, n3mh = g.n3mh;
     const long long nl = (long long)n1m * n3mh;
@@ -471,27 +472,27 @@ __global__ void __launch_bounds__(64) k_ytri(KP p, S *ccap, const double *ybet, 
         S *r = ccap + 2 * t + part;                                   // element j at r[2 * (j-1) * sj]
         const long long s2 = 2 * sj;
         const bool pin = (t == 0);
-        const double crhsref = pin ? (double)r[(n2m - 1) * s2] : 0.0;
+        const S crhsref = pin ? r[(n2m - 1) * s2] : S(0.0);
         // forward: the next chunk's operands are loaded while one is computed
         // (two register buffers, alternated by unrolling the chunk loop by two)
-        double x = 0.0;
-        double rA[U], bA[U], aA[U], rB[U], bB[U], aB[U];
-        auto load_f = [&](double (&rv)[U], double (&bv)[U], double (&av)[U], int j0) {
+        S x = S(0.0);
+        S rA[U], bA[U], aA[U], rB[U], bB[U], aB[U];
+        auto load_f = [&](S (&rv)[U], S (&bv)[U], S (&av)[U], int j0) {
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int j = j0 + u;
-                if (j <= n2m) { rv[u] = (double)r[(j - 1) * s2]; bv[u] = ybet[t + (j - 1) * sj]; av[u] = yam[j]; }
+                if (j <= n2m) { rv[u] = r[(j - 1) * s2]; bv[u] = ybet[t + (j - 1) * sj]; av[u] = yam[j]; }
             }
         };
-        auto solve_f = [&](const double (&rv)[U], const double (&bv)[U], const double (&av)[U], int j0) {
+        auto solve_f = [&](const S (&rv)[U], const S (&bv)[U], const S (&av)[U], int j0) {
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int j = j0 + u;
                 if (j > n2m) break;
-                double rj = rv[u], am = av[u];
-                if (pin && j == n2m) { am = 0.0; rj = 0.0; }
+                S rj = rv[u], am = av[u];
+                if (pin && j == n2m) { am = S(0.0); rj = S(0.0); }
                 x = (j == 1) ? rj * bv[u] : (rj - am * x) * bv[u];
-                r[(j - 1) * s2] = (S)x;
+                r[(j - 1) * s2] = x;
             }
         };
         load_f(rA, bA, aA, 1);
@@ -504,22 +505,22 @@ __global__ void __launch_bounds__(64) k_ytri(KP p, S *ccap, const double *ybet, 
         }
         // backward, pipelined the same way (the rows re-read here were written
         // above by this thread, so program order makes them visible)
-        double xn = x;
-        double xA[U], gA[U], xB[U], gB[U];
-        auto load_b = [&](double (&xv)[U], double (&gv)[U], int j0) {
+        S xn = x;
+        S xA[U], gA[U], xB[U], gB[U];
+        auto load_b = [&](S (&xv)[U], S (&gv)[U], int j0) {
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int j = j0 - u;
-                if (j >= 1) { xv[u] = (double)r[(j - 1) * s2]; gv[u] = ygam[t + j * sj]; }
+                if (j >= 1) { xv[u] = r[(j - 1) * s2]; gv[u] = ygam[t + j * sj]; }
             }
         };
-        auto solve_b = [&](const double (&xv)[U], const double (&gv)[U], int j0) {
+        auto solve_b = [&](const S (&xv)[U], const S (&gv)[U], int j0) {
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int j = j0 - u;
                 if (j < 1) break;
-                const double xj = xv[u] - gv[u] * xn;
-                r[(j - 1) * s2] = (S)xj;
+                const S xj = xv[u] - gv[u] * xn;
+                r[(j - 1) * s2] = xj;
                 xn = xj;
             }
         };
@@ -533,14 +534,26 @@ __global__ void __launch_bounds__(64) k_ytri(KP p, S *ccap, const double *ybet, 
         }
         if (pin) {
             // phref = (-ajmref*crhs(n2m-1,1) + crhsref)/ajcref; shift; crhs(n2m,1) = 0
-            const double ajcref = pinref[0], ajmref = pinref[1];
-            const double cm = n2m >= 2 ? (double)r[(n2m - 2) * s2] : 0.0;
-            const double ph = (-ajmref * cm + crhsref) / ajcref;
-            for (int j = 1; j <= n2m; j++) r[(j - 1) * s2] = (S)((double)r[(j - 1) * s2] - ph);
-            r[(n2m - 1) * s2] = (S)0.0;
+            const S ajcref = pinref[0], ajmref = pinref[1];
+            const S cm = n2m >= 2 ? r[(n2m - 2) * s2] : S(0.0);
+            const S ph = (-ajmref * cm + crhsref) / ajcref;
+            for (int j = 1; j <= n2m; j++) r[(j - 1) * s2] = r[(j - 1) * s2] - ph;
+            r[(n2m - 1) * s2] = S(0.0);
         }
     }
 }
+
+// FP64 -> FP32 copies of the y systems' LU tables
+__global__ void k_to_f32(const double *a, float *b, long long n) {
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        b[q] = (float)a[q];
+}
+
+// the LU tables of the y systems in the arithmetic type of k_ytri<T>
+template <class T> struct YtriTabs { const T *bet, *gam, *am, *pin; };
+template <class T> YtriTabs<T> ytri_tabs(const DPois &P);
+template <> YtriTabs<double> ytri_tabs<double>(const DPois &P) { return {P.ybet, P.ygam, P.yam, P.pinref}; }
+template <> YtriTabs<float> ytri_tabs<float>(const DPois &P) { return {P.ybetf, P.ygamf, P.yamf, P.pinreff}; }
 
 // The mixed form's FP64 defect of the poiss_ftft system, r = divgsum - L phi,
 // for the operator the transforms diagonalise (poiss_ftft.f90:79-88,
@@ -774,6 +787,19 @@ int poisson_init(lesgpu_case *c) {
         k_ytri_lu<<<blocks_for(nl, 128), 128>>>(c->kp, P.ak1, P.ak3, P.ybet, P.ygam, P.yam, P.pinref);
         if (cudaDeviceSynchronize() != cudaSuccess) return LESGPU_ERR_CUDA;
     }
+    // their FP32 copies, for the mixed form's FP32 solves
+    if (c->cfg.precision == LESGPU_PREC_MIXED) {
+        if (cudaMalloc(&P.ybetf, sizeof(float) * nspec) != cudaSuccess ||
+            cudaMalloc(&P.ygamf, sizeof(float) * nspec) != cudaSuccess ||
+            cudaMalloc(&P.yamf, sizeof(float) * (g.n2m + 2)) != cudaSuccess ||
+            cudaMalloc(&P.pinreff, sizeof(float) * 2) != cudaSuccess)
+            return LESGPU_ERR_OOM;
+        k_to_f32<<<blocks_for((long long)nspec), kThreads>>>(P.ybet, P.ybetf, (long long)nspec);
+        k_to_f32<<<blocks_for((long long)nspec), kThreads>>>(P.ygam, P.ygamf, (long long)nspec);
+        k_to_f32<<<1, kThreads>>>(P.yam, P.yamf, (long long)(g.n2m + 2));
+        k_to_f32<<<1, kThreads>>>(P.pinref, P.pinreff, 2LL);
+        if (cudaDeviceSynchronize() != cudaSuccess) return LESGPU_ERR_CUDA;
+    }
     // the attribute is per function and shared by every case: set it to the
     // largest size lines_per_block() can ask for
     if (cudaFuncSetAttribute(k_fft_z_fwd<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFftSmemMax) != cudaSuccess ||
@@ -793,8 +819,10 @@ void poisson_free(lesgpu_case *c) {
     mgrd_free(c);
     cudaFree(P.ak1); cudaFree(P.ak3); cudaFree(P.ccap);
     cudaFree(P.ybet); cudaFree(P.ygam); cudaFree(P.yam); cudaFree(P.pinref); cudaFree(P.yres);
+    cudaFree(P.ybetf); cudaFree(P.ygamf); cudaFree(P.yamf); cudaFree(P.pinreff);
     P.yres = nullptr;
     P.ybet = P.ygam = P.yam = P.pinref = nullptr;
+    P.ybetf = P.ygamf = P.yamf = P.pinreff = nullptr;
     cudaFree(P.fx.tw); cudaFree(P.fz.tw); cudaFree(P.fx.twf); cudaFree(P.fz.twf);
     P.ak1 = P.ak3 = nullptr; P.ccap = nullptr; P.fx.tw = P.fz.tw = nullptr; P.fx.twf = P.fz.twf = nullptr;
 }
@@ -818,7 +846,8 @@ static void ftft_solve(lesgpu_case *c, const double *src) {
     k_fft_z_fwd<V><<<gz, kThreads, smz, c->stream>>>(c->kp, src, spec, pz, Lz, sk, sj);
     k_fft_x<V><<<(nxl + Lx - 1) / Lx, kThreads, smx, c->stream>>>(spec, nxl, px, Lx, 0);
     const long long nl = (long long)g.n1m * g.n3mh;
-    k_ytri<T><<<blocks_for(2 * nl, 64), 64, 0, c->stream>>>(c->kp, reinterpret_cast<T *>(spec), P.ybet, P.ygam, P.yam, P.pinref);
+    const YtriTabs<T> yt = ytri_tabs<T>(P);
+    k_ytri<T><<<blocks_for(2 * nl, 64), 64, 0, c->stream>>>(c->kp, reinterpret_cast<T *>(spec), yt.bet, yt.gam, yt.am, yt.pin);
     k_fft_x<V><<<(nxl + Lx - 1) / Lx, kThreads, smx, c->stream>>>(spec, nxl, px, Lx, 1);
     k_fft_z_inv<V, ADD><<<gz, kThreads, smz, c->stream>>>(c->kp, spec, pz, Lz, sk, sj);
 }

@@ -142,6 +142,7 @@ struct DPois {
     MgTables *mg;
     MgrdTables *mgrd;         // poiss_mgrd (BiCGSTAB + MG3D)
     double *ybet, *ygam, *yam, *pinref;   // poiss_ftft: LU of the y systems (k_ytri_lu)
+    float *ybetf, *ygamf, *yamf, *pinreff;  // their FP32 copies (mixed form)
     int Lz, Lx;               // FFT lines per block (0 = the shared-memory rule; set by the autotuner)
     int mixed_fft;            // poiss_ftft in the mixed form: FP32 transforms, FP64 defect correction
     double *yres;             // its FP64 residual's y rows and diagonal, 3 per j
