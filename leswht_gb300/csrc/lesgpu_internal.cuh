@@ -64,6 +64,7 @@ struct DScal {
     double cflmax, dvmax, qmmax;
     double alpha, dtconst, dtconsti, test1, acoef, acoefi;
     double pmi[5], pmiavg, qvol[3], tvol[3], thcap;
+    double pmiw[4];           // meanpg's wall-shear sums (y bottom, y top, z bottom, z top)
     double csgsts, csgshf, nutavg, nutmax, alpavg, alpmax;
     double err_integral;
     double dudta, dvdta, dwdta;
