@@ -483,7 +483,12 @@ struct DivFinal {
 };
 void launch_advance_and_convergence(lesgpu_case *c) { reduce<3, true>(c, interior(c->kp.g), DivTerm{}, DivFinal{}); }
 
-struct BulkTerm {   // writehistory's bulk quantities, misc_hist.f90:73-181
+// writehistory's bulk quantities, misc_hist.f90:73-181: the flow rate and
+// the fluid cells' temperature sums in one pass; the solid cells' sums
+// (temperature inside bodies) in a second pass only when some cell centre
+// lies inside a body -- carried through one pass they cost it half its time
+// on bodiless cases, where they are zero.
+struct BulkTerm {
     __device__ void operator()(const KP &p, int i, int j, int k, double *w) const {
         const DGrid &g = p.g;
         long long q = g.ix(i, j, k);
@@ -491,23 +496,42 @@ struct BulkTerm {   // writehistory's bulk quantities, misc_hist.f90:73-181
         bool flu = p.f.fb_u[q] >= 1.0e-10;
         w[0] = flu ? p.f.u[q] * cv : 0.0;
         w[1] = flu ? cv : 0.0;
-        w[2] = w[3] = w[4] = w[5] = 0.0;
-        if (p.c.ihtrans == 1) {
-            if (p.f.fb_c[q] >= 1.0e-10) { w[2] = cv; w[3] = p.f.t[q] * cv; }
-            else { w[4] = cv; w[5] = p.f.t[q] * cv; }
+        w[2] = w[3] = 0.0;
+        if (p.c.ihtrans == 1 && p.f.fb_c[q] >= 1.0e-10) { w[2] = cv; w[3] = p.f.t[q] * cv; }
+    }
+};
+struct BulkSolidTerm {
+    __device__ void operator()(const KP &p, int i, int j, int k, double *w) const {
+        const DGrid &g = p.g;
+        long long q = g.ix(i, j, k);
+        w[0] = w[1] = 0.0;
+        if (p.f.fb_c[q] < 1.0e-10) {
+            double cv = g.c2cx[i] * g.f2fy[j] * g.f2fz[k];
+            w[0] = cv;
+            w[1] = p.f.t[q] * cv;
         }
     }
 };
 struct BulkFinal {
+    int solid;      // the solid pass follows (else the solid bulk temperature is 0)
     __device__ void operator()(const KP &p, const double *o) const {
         DScal *S = p.S;
         S->ubulk = o[1] > 0.0 ? o[0] / o[1] : 0.0;
         S->qflux = o[0] / p.g.xl;
         S->tbulk_fluid = o[2] > 0.0 ? o[3] / o[2] : 0.0;
-        S->tbulk_solid = o[4] > 0.0 ? o[5] / o[4] : 0.0;
+        if (!solid) S->tbulk_solid = 0.0;
     }
 };
-void launch_bulk_diag(lesgpu_case *c) { reduce<6, false>(c, interior(c->kp.g), BulkTerm{}, BulkFinal{}); }
+struct BulkSolidFinal {
+    __device__ void operator()(const KP &p, const double *o) const {
+        p.S->tbulk_solid = o[0] > 0.0 ? o[1] / o[0] : 0.0;
+    }
+};
+void launch_bulk_diag(lesgpu_case *c) {
+    const bool solid = c->kp.c.ihtrans == 1 && c->bulk_solid;
+    reduce<4, false>(c, interior(c->kp.g), BulkTerm{}, BulkFinal{solid ? 1 : 0});
+    if (solid) reduce<2, false>(c, interior(c->kp.g), BulkSolidTerm{}, BulkSolidFinal{});
+}
 
 
 }  // namespace lg

@@ -261,6 +261,11 @@ extern "C" int lesgpu_create(const lesgpu_config *cfg, const lesgpu_grid *g, les
                 }
         f.fb_u = upload(A, fbu.data(), nt);
         f.fb_c = upload(A, fbc.data(), nt);
+        c->bulk_solid = 0;
+        for (long long kk = 1; kk <= d.n3 - 1 && !c->bulk_solid; kk++)
+            for (long long jj = 1; jj <= d.n2 - 1 && !c->bulk_solid; jj++)
+                for (long long ii = 1; ii <= d.n1 - 1; ii++)
+                    if (fbc[(size_t)(ii + d.sx * jj + d.sxy * kk)] < 1.0e-10) { c->bulk_solid = 1; break; }
         f.wq = A.get<double>(nt); f.wb = A.get<double>(nt); f.wt = A.get<double>(nt);
         // nutinterpol's edge weights (sgs.f90:1002-1040), 4 per edge line
         {

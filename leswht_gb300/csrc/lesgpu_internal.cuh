@@ -296,6 +296,7 @@ struct lesgpu_case {
     int use_graph;
     int autotune;              // use the autotuner's choices (LESGPU_AUTOTUNE != 0 at start)
     int strict;                // lesgpu_set_strict: unconverged Poisson solves are an error
+    int bulk_solid;            // some interior cell centre lies inside a body (fb_c < 1e-10)
     // LESGPU_ADI_FP32_FORM at start: the form every FP32 sweep uses (lanes
     // per line, + 64 register-capped, 128 tiled; 0 = the autotuner's)
     int adi_force_f32;
