@@ -14,7 +14,8 @@ benchmark's configurations that runs on one GPU.
 Our arm (one JSON line on rank 0):
   value    : device-resident throughput of the mixed-precision form (FP32
              stencils, SGS and x/z ADI sweeps; FP64 wall-normal sweeps,
-             Poisson, projection, flow-rate and divergence); every step is
+             projection, flow-rate and divergence; Poisson solves in FP32
+             under an FP64 defect correction where timed faster); every step is
              bracketed by CUDA events on the case's own stream and L2 is
              flushed (256 MiB write) between timed steps, outside the timed
              region.  `--form fp64` times the plain FP64 form instead.
